@@ -1,0 +1,60 @@
+/*
+ * Extensions of the GB300 NGT search library that have no counterpart in the
+ * reference C API: batched search of many queries in one call (the
+ * reference's only batch path is the OpenMP loop of ngtpy.Index.batch_search,
+ * python/src/ngtpy.cpp:422-458) and device-resident variants for callers that
+ * keep queries and results in GPU memory.
+ *
+ * Handles, result structs and error objects are the ones of ngt_capi.h.
+ */
+#pragma once
+#include "ngt_capi.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Kernel selection for the batched calls. */
+#define NGTGPU_KERNEL_EXACT 0u  /* reference-order search, one query per CTA (results equal the reference's) */
+
+/* Per-query statistics (distance computations, expanded nodes, visited ids, status bits). */
+typedef struct {
+  uint32_t distance_computations;
+  uint32_t expansions;
+  uint32_t visited;
+  uint32_t status;
+} NGTGPUQueryStats;
+
+/* Dimension of the objects of an open index (the user dimension). */
+int32_t ngtgpu_get_dimension(NGTIndex, NGTError);
+
+/* Graph search of nq float queries (row-major nq x dim) in one call.
+ * params holds nparams entries: 1 (shared by every query) or nq.  Results of
+ * query i are written to results[i*kmax .. i*kmax+counts[i]) ascending by
+ * (distance, id); kmax must be >= every params[].size.  stats may be NULL. */
+bool ngtgpu_search_batch_float(NGTIndex, const float *queries, size_t nq, int32_t dim,
+                               const NGTQueryParameters *params, size_t nparams, NGTObjectDistance *results,
+                               size_t kmax, uint32_t *counts, NGTGPUQueryStats *stats, uint32_t kernel, NGTError);
+
+/* Size in bytes of one converted query row (padded object layout). */
+size_t ngtgpu_query_row_bytes(NGTIndex, NGTError);
+
+/* Converts nq float queries to the padded object rows the device calls take
+ * (object type, normalisation and augmentation as the index requires). */
+bool ngtgpu_convert_queries_float(NGTIndex, const float *queries, size_t nq, int32_t dim, void *rows_out,
+                                  NGTError);
+
+/* Same search as ngtgpu_search_batch_float on device memory: d_rows holds nq
+ * converted rows, d_results / d_counts / d_stats are device buffers, and the
+ * work is queued on `stream` (a cudaStream_t; NULL = the index's own stream)
+ * without synchronising. */
+bool ngtgpu_search_batch_device(NGTIndex, const void *d_rows, size_t nq, const NGTQueryParameters *params,
+                                size_t nparams, NGTObjectDistance *d_results, size_t kmax, uint32_t *d_counts,
+                                NGTGPUQueryStats *d_stats, void *stream, uint32_t kernel, NGTError);
+
+/* Number of kernel launches issued by this index since it was opened. */
+uint64_t ngtgpu_kernel_launches(NGTIndex, NGTError);
+
+#ifdef __cplusplus
+}
+#endif

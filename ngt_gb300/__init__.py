@@ -1,0 +1,9 @@
+"""GB300-native batched k-NN search for NGT indexes.
+
+The compute path is the native library libngtgpu.so (hand-written CUDA for
+sm_103a behind NGT's C ABI); this package only loads it and offers a thin
+Python mirror of NGT's ctypes wrapper (``ngt.base.Index``).
+"""
+from .base import Index, ObjectDistance, NativeError, load_library  # noqa: F401
+
+__all__ = ["Index", "ObjectDistance", "NativeError", "load_library"]

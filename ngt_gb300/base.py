@@ -1,0 +1,232 @@
+"""Python mirror of NGT's ctypes wrapper (python/ngt/base.py in the reference)
+over libngtgpu.so.
+
+``Index(path, read_only=False)`` opens an existing NGT index directory,
+``search(query, k=20, epsilon=0.1)`` returns a list of ``ObjectDistance``
+(1-based ids, ascending distance) exactly as the reference's
+``ngt.base.Index.search`` does (python/ngt/base.py:281-363).  Errors raised by
+the library surface as ``NativeError`` with the library's message.
+
+Extensions (not in the reference wrapper): ``batch_search`` runs many queries
+in one native call and returns numpy arrays; ``linear_search`` is the
+exhaustive search of the C API.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from ctypes import POINTER, c_bool, c_char_p, c_float, c_int32, c_size_t, c_uint32, c_uint64, c_void_p
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libngtgpu.so")
+
+KERNEL_EXACT = 0
+
+
+class NativeError(Exception):
+    pass
+
+
+class ObjectDistance(ctypes.Structure):
+    """NGTObjectDistance (lib/NGT/Capi.h:36-39)."""
+    _fields_ = [("id", c_uint32), ("distance", c_float)]
+
+    def __repr__(self):
+        return "ObjectDistance({},{})".format(self.id, self.distance)
+
+
+class QueryParameters(ctypes.Structure):
+    """NGTQueryParameters (lib/NGT/Capi.h:50-55)."""
+    _fields_ = [("size", c_size_t), ("epsilon", c_float), ("radius", c_float), ("edge_size", c_size_t)]
+
+
+class QueryStats(ctypes.Structure):
+    _fields_ = [("distance_computations", c_uint32), ("expansions", c_uint32), ("visited", c_uint32),
+                ("status", c_uint32)]
+
+
+QUERY_STATS_DTYPE = np.dtype([("distance_computations", np.uint32), ("expansions", np.uint32),
+                              ("visited", np.uint32), ("status", np.uint32)])
+RESULT_DTYPE = np.dtype([("id", np.uint32), ("distance", np.float32)])
+
+_lib = None
+
+
+def load_library() -> ctypes.CDLL:
+    """Loads libngtgpu.so; raises if it has not been built (there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libngtgpu.so is missing: build it with `python -c 'import __graft_entry__ as g; "
+                          "g.build()'` (needs nvcc)")
+    L = ctypes.CDLL(LIB_PATH)
+    sig = {
+        "ngt_open_index": ([c_char_p, c_void_p], c_void_p),
+        "ngt_open_index_as_read_only": ([c_char_p, c_void_p], c_void_p),
+        "ngt_close_index": ([c_void_p], None),
+        "ngt_get_number_of_objects": ([c_void_p, c_void_p], c_uint32),
+        "ngt_create_empty_results": ([c_void_p], c_void_p),
+        "ngt_search_index": ([c_void_p, POINTER(ctypes.c_double), c_int32, c_size_t, c_float, c_float, c_void_p,
+                              c_void_p], c_bool),
+        "ngt_search_index_as_float": ([c_void_p, POINTER(c_float), c_int32, c_size_t, c_float, c_float, c_void_p,
+                                       c_void_p], c_bool),
+        "ngt_search_index_as_uint8": ([c_void_p, POINTER(ctypes.c_uint8), c_int32, c_size_t, c_float, c_float,
+                                       c_void_p, c_void_p], c_bool),
+        "ngt_linear_search_index_as_float": ([c_void_p, POINTER(c_float), c_int32, c_size_t, c_void_p, c_void_p],
+                                             c_bool),
+        "ngt_get_result_size": ([c_void_p, c_void_p], c_uint32),
+        "ngt_get_result": ([c_void_p, c_uint32, c_void_p], ObjectDistance),
+        "ngt_destroy_results": ([c_void_p], None),
+        "ngt_create_error_object": ([], c_void_p),
+        "ngt_get_error_string": ([c_void_p], c_char_p),
+        "ngt_clear_error_string": ([c_void_p], None),
+        "ngt_destroy_error_object": ([c_void_p], None),
+        "ngt_initialize_query_parameters": ([POINTER(QueryParameters)], None),
+        "ngtgpu_get_dimension": ([c_void_p, c_void_p], c_int32),
+        "ngtgpu_search_batch_float": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QueryParameters), c_size_t,
+                                       c_void_p, c_size_t, c_void_p, c_void_p, c_uint32, c_void_p], c_bool),
+        "ngtgpu_query_row_bytes": ([c_void_p, c_void_p], c_size_t),
+        "ngtgpu_convert_queries_float": ([c_void_p, c_void_p, c_size_t, c_int32, c_void_p, c_void_p], c_bool),
+        "ngtgpu_search_batch_device": ([c_void_p, c_void_p, c_size_t, POINTER(QueryParameters), c_size_t, c_void_p,
+                                        c_size_t, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p], c_bool),
+        "ngtgpu_kernel_launches": ([c_void_p, c_void_p], c_uint64),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def _edge_field(edge_size):
+    """NGTQueryParameters.edge_size: INT_MIN (stored in a size_t) = index default."""
+    if edge_size is None or edge_size == -1:
+        return ctypes.c_size_t(-2147483648).value
+    return ctypes.c_size_t(int(edge_size)).value
+
+
+class Index:
+    """An NGT index opened on the GPU (mirror of ngt.base.Index)."""
+
+    def __init__(self, path: str, read_only: bool = False):
+        self._lib = load_library()
+        self._err = self._lib.ngt_create_error_object()
+        opener = self._lib.ngt_open_index_as_read_only if read_only else self._lib.ngt_open_index
+        self._index = opener(path.encode(), self._err)
+        self._check(self._index is not None)
+        self.dimension = self._lib.ngtgpu_get_dimension(self._index, self._err)
+        self._results = self._lib.ngt_create_empty_results(self._err)
+
+    def _check(self, ok):
+        if not ok:
+            msg = self._lib.ngt_get_error_string(self._err).decode()
+            self._lib.ngt_clear_error_string(self._err)
+            raise NativeError(msg)
+
+    def close(self):
+        if getattr(self, "_index", None):
+            self._lib.ngt_close_index(self._index)
+            self._index = None
+        if getattr(self, "_results", None):
+            self._lib.ngt_destroy_results(self._results)
+            self._results = None
+        if getattr(self, "_err", None):
+            self._lib.ngt_destroy_error_object(self._err)
+            self._err = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _collect(self):
+        n = self._lib.ngt_get_result_size(self._results, self._err)
+        return [self._lib.ngt_get_result(self._results, i, self._err) for i in range(n)]
+
+    def search(self, query, k: int = 20, epsilon: float = 0.1, radius: float = -1.0):
+        """Graph search of one query: list of ObjectDistance (id, distance)."""
+        q = np.ascontiguousarray(query, dtype=np.float32)
+        ok = self._lib.ngt_search_index_as_float(self._index, q.ctypes.data_as(POINTER(c_float)), q.shape[0], k,
+                                                 epsilon, radius, self._results, self._err)
+        self._check(ok)
+        return self._collect()
+
+    def linear_search(self, query, k: int = 20):
+        q = np.ascontiguousarray(query, dtype=np.float32)
+        ok = self._lib.ngt_linear_search_index_as_float(self._index, q.ctypes.data_as(POINTER(c_float)),
+                                                        q.shape[0], k, self._results, self._err)
+        self._check(ok)
+        return self._collect()
+
+    def number_of_objects(self) -> int:
+        return self._lib.ngt_get_number_of_objects(self._index, self._err)
+
+    @staticmethod
+    def make_params(k, epsilon, radius=-1.0, edge_size=None):
+        """Per-query NGTQueryParameters array from scalars or sequences."""
+        ks, es, rs, eds = (np.atleast_1d(np.asarray(x)) for x in (k, epsilon, radius,
+                                                                  -1 if edge_size is None else edge_size))
+        n = max(len(ks), len(es), len(rs), len(eds))
+        arr = (QueryParameters * n)()
+        for i in range(n):
+            arr[i].size = int(ks[i % len(ks)])
+            arr[i].epsilon = float(es[i % len(es)])
+            arr[i].radius = float(rs[i % len(rs)])
+            arr[i].edge_size = _edge_field(int(eds[i % len(eds)]))
+        return arr, n
+
+    def batch_search(self, queries, k=10, epsilon=0.1, radius=-1.0, edge_size=None, kernel: int = KERNEL_EXACT,
+                     with_stats: bool = False):
+        """Searches every row of `queries` in one native call.
+
+        k / epsilon / radius / edge_size may be scalars or per-query sequences.
+        Returns (ids[nq, kmax], distances[nq, kmax], counts[nq]) and, with
+        with_stats, the per-query counters.
+        """
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        nq = q.shape[0]
+        params, n = self.make_params(k, epsilon, radius, edge_size)
+        # room for round((1+epsilon)*k): the updatable search on an index with
+        # EpsilonType ResultSize returns that many results
+        kmax = int(np.ceil(max(np.atleast_1d(k)) * (1.0 + max(0.0, float(np.max(epsilon)))))) + 1
+        res = np.zeros((nq, kmax), RESULT_DTYPE)
+        counts = np.zeros(nq, np.uint32)
+        stats = np.zeros(nq, QUERY_STATS_DTYPE)
+        ok = self._lib.ngtgpu_search_batch_float(self._index, q.ctypes.data, nq, q.shape[1], params, n,
+                                                 res.ctypes.data, kmax, counts.ctypes.data, stats.ctypes.data,
+                                                 kernel, self._err)
+        self._check(ok)
+        m = int(counts.max()) if nq else 0
+        out = (res["id"][:, :m].copy(), res["distance"][:, :m].copy(), counts)
+        return out + (stats,) if with_stats else out
+
+    def kernel_launches(self) -> int:
+        return int(self._lib.ngtgpu_kernel_launches(self._index, self._err))
+
+    # device-resident path (used by bench.py for the HBM-resident measurement)
+    def query_row_bytes(self) -> int:
+        return int(self._lib.ngtgpu_query_row_bytes(self._index, self._err))
+
+    def convert_queries(self, queries) -> np.ndarray:
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        rows = np.zeros((q.shape[0], self.query_row_bytes()), np.uint8)
+        self._check(self._lib.ngtgpu_convert_queries_float(self._index, q.ctypes.data, q.shape[0], q.shape[1],
+                                                           rows.ctypes.data, self._err))
+        return rows
+
+    def search_device(self, d_rows: int, nq: int, params, nparams: int, d_results: int, kmax: int, d_counts: int,
+                      d_stats: int, stream: int = 0, kernel: int = KERNEL_EXACT):
+        ok = self._lib.ngtgpu_search_batch_device(self._index, d_rows, nq, params, nparams, d_results, kmax,
+                                                  d_counts, d_stats, stream or None, kernel, self._err)
+        self._check(ok)

@@ -1,0 +1,425 @@
+// C ABI: NGT's search-side C API (lib/NGT/Capi.cpp) over the GB300 engine,
+// plus the batched extensions declared in include/ngtgpu.h.
+//
+// Error convention (lib/NGT/Capi.cpp:26-39): every entry point catches
+// exceptions, writes "Capi : <function>() : ..." into the NGTError string (or
+// stderr when it is NULL) and returns false / NULL / 0.  Nothing throws across
+// the ABI.
+#include <cfloat>
+#include <climits>
+#include <cstring>
+#include <iostream>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "engine.h"
+
+extern "C" {
+#include "../../include/ngt_capi.h"
+#include "../../include/ngtgpu.h"
+}
+
+using ngtg::GraphEngine;
+using ngtg::GraphMode;
+using ngtg::QueryType;
+using ngtg::SearchArgs;
+using ngtg::SearchOutput;
+
+namespace {
+
+typedef std::vector<NGTObjectDistance> Results;
+
+void set_error(const std::stringstream& ss, NGTError error) {
+  if (error != nullptr) {
+    *static_cast<std::string*>(error) = ss.str();
+  } else {
+    std::cerr << ss.str() << std::endl;
+  }
+}
+
+#define CAPI_PARAM_ERROR(error, what)                                                   \
+  do {                                                                                  \
+    std::stringstream ss_;                                                              \
+    ss_ << "Capi : " << __FUNCTION__ << "() : parametor error: " << what;               \
+    set_error(ss_, error);                                                              \
+  } while (0)
+
+#define CAPI_CATCH(error, retval)                                                       \
+  catch (std::exception & err) {                                                        \
+    std::stringstream ss_;                                                              \
+    ss_ << "Capi : " << __FUNCTION__ << "() : Error: " << err.what();                   \
+    set_error(ss_, error);                                                              \
+    return retval;                                                                      \
+  }
+
+GraphEngine* engine(NGTIndex index) { return static_cast<GraphEngine*>(index); }
+
+void fill_results(const SearchOutput& out, size_t q, NGTObjectDistances results) {
+  Results& r = *static_cast<Results*>(results);
+  r.clear();
+  uint32_t n = out.counts[q];
+  r.reserve(n);
+  for (uint32_t i = 0; i < n; i++) {
+    const ngtg::ObjDist& o = out.results[q * out.kmax + i];
+    r.push_back(NGTObjectDistance{o.id, o.distance});
+  }
+}
+
+SearchArgs make_args(size_t size, float epsilon, float radius, int64_t edge_size) {
+  SearchArgs a;
+  a.size = size;
+  a.epsilon = epsilon;
+  a.radius = radius < 0.0f ? FLT_MAX : radius;
+  a.edge_size = edge_size;
+  return a;
+}
+
+// The reference stores INT_MIN ("use the index default") in a size_t field.
+int64_t edge_size_from_field(size_t v) {
+  int e = (int)v;
+  return e == INT_MIN ? -1 : (int64_t)e;
+}
+
+bool search_common(NGTIndex index, const void* query, QueryType qt, int32_t dim, size_t size, float epsilon,
+                   float radius, int64_t edge_size, NGTObjectDistances results) {
+  SearchArgs a = make_args(size, epsilon, radius, edge_size);
+  SearchOutput out;
+  engine(index)->search(query, qt, 1, (size_t)dim, &a, 1, out);
+  fill_results(out, 0, results);
+  return true;
+}
+
+bool linear_common(NGTIndex index, const void* query, QueryType qt, int32_t dim, size_t size,
+                   NGTObjectDistances results) {
+  SearchOutput out;
+  engine(index)->linear_search(query, qt, 1, (size_t)dim, size, out);
+  fill_results(out, 0, results);
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+NGTIndex ngt_open_index(const char* index_path, NGTError error) {
+  try {
+    if (index_path == nullptr) throw std::runtime_error("index path is NULL");
+    return static_cast<NGTIndex>(new GraphEngine(index_path, GraphMode::Updatable));
+  }
+  CAPI_CATCH(error, nullptr)
+}
+
+NGTIndex ngt_open_index_as_read_only(const char* index_path, NGTError error) {
+  try {
+    if (index_path == nullptr) throw std::runtime_error("index path is NULL");
+    return static_cast<NGTIndex>(new GraphEngine(index_path, GraphMode::ReadOnly));
+  }
+  CAPI_CATCH(error, nullptr)
+}
+
+void ngt_close_index(NGTIndex index) {
+  if (index == nullptr) return;
+  delete engine(index);
+}
+
+uint32_t ngt_get_number_of_objects(NGTIndex index, NGTError error) {
+  if (index == nullptr) {
+    CAPI_PARAM_ERROR(error, "index = " << index);
+    return 0;
+  }
+  const auto& p = engine(index)->host().present;
+  uint32_t n = 0;
+  for (size_t i = 1; i < p.size(); i++) n += p[i];
+  return n;
+}
+
+NGTObjectDistances ngt_create_empty_results(NGTError error) {
+  try {
+    return static_cast<NGTObjectDistances>(new Results());
+  }
+  CAPI_CATCH(error, nullptr)
+}
+
+#define SEARCH_ARGS_CHECK()                                                                                \
+  if (index == nullptr || query == nullptr || results == nullptr || query_dim <= 0) {                      \
+    CAPI_PARAM_ERROR(error, "index = " << index << " query = " << (const void*)query                      \
+                                       << " results = " << results << " query_dim = " << query_dim);       \
+    return false;                                                                                          \
+  }
+
+bool ngt_search_index(NGTIndex index, double* query, int32_t query_dim, size_t size, float epsilon, float radius,
+                      NGTObjectDistances results, NGTError error) {
+  SEARCH_ARGS_CHECK();
+  try {
+    return search_common(index, query, QueryType::Float64, query_dim, size, epsilon, radius, -1, results);
+  }
+  CAPI_CATCH(error, false)
+}
+
+bool ngt_search_index_as_float(NGTIndex index, float* query, int32_t query_dim, size_t size, float epsilon,
+                               float radius, NGTObjectDistances results, NGTError error) {
+  SEARCH_ARGS_CHECK();
+  try {
+    return search_common(index, query, QueryType::Float32, query_dim, size, epsilon, radius, -1, results);
+  }
+  CAPI_CATCH(error, false)
+}
+
+bool ngt_search_index_as_uint8(NGTIndex index, uint8_t* query, int32_t query_dim, size_t size, float epsilon,
+                               float radius, NGTObjectDistances results, NGTError error) {
+  SEARCH_ARGS_CHECK();
+  try {
+    return search_common(index, query, QueryType::Uint8, query_dim, size, epsilon, radius, -1, results);
+  }
+  CAPI_CATCH(error, false)
+}
+
+bool ngt_search_index_as_float16(NGTIndex index, NGTFloat16* query, int32_t query_dim, size_t size, float epsilon,
+                                 float radius, NGTObjectDistances results, NGTError error) {
+  SEARCH_ARGS_CHECK();
+  try {
+    return search_common(index, query, QueryType::Float16, query_dim, size, epsilon, radius, -1, results);
+  }
+  CAPI_CATCH(error, false)
+}
+
+bool ngt_search_index_with_query(NGTIndex index, NGTQuery query, NGTObjectDistances results, NGTError error) {
+  if (index == nullptr || query.query == nullptr || results == nullptr) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " query = " << query.query << " results = " << results);
+    return false;
+  }
+  try {
+    int32_t dim = (int32_t)engine(index)->dimension();
+    return search_common(index, query.query, QueryType::Float32, dim, query.size, query.epsilon, query.radius,
+                         edge_size_from_field(query.edge_size), results);
+  }
+  CAPI_CATCH(error, false)
+}
+
+void ngt_initialize_query_parameters(NGTQueryParameters* params) {
+  // lib/NGT/Capi.cpp:690-695
+  params->epsilon = 0.1f;
+  params->edge_size = (size_t)INT_MIN;
+  params->radius = -1;
+  params->size = 10;
+}
+
+#define WITH_QUERY_BODY(QT)                                                                                  \
+  if (index == nullptr || query.query == nullptr || results == nullptr) {                                    \
+    CAPI_PARAM_ERROR(error, "index = " << index << " query = " << (const void*)query.query                  \
+                                       << " results = " << results);                                         \
+    return false;                                                                                            \
+  }                                                                                                          \
+  try {                                                                                                      \
+    int32_t dim = (int32_t)engine(index)->dimension();                                                       \
+    return search_common(index, query.query, QT, dim, query.params.size, query.params.epsilon,               \
+                         query.params.radius, edge_size_from_field(query.params.edge_size), results);        \
+  }                                                                                                          \
+  CAPI_CATCH(error, false)
+
+bool ngt_search_index_with_query_float(NGTIndex index, NGTQueryFloat query, NGTObjectDistances results,
+                                       NGTError error) {
+  WITH_QUERY_BODY(QueryType::Float32)
+}
+
+bool ngt_search_index_with_query_uint8(NGTIndex index, NGTQueryUint8 query, NGTObjectDistances results,
+                                       NGTError error) {
+  WITH_QUERY_BODY(QueryType::Uint8)
+}
+
+bool ngt_search_index_with_query_float16(NGTIndex index, NGTQueryFloat16 query, NGTObjectDistances results,
+                                         NGTError error) {
+  WITH_QUERY_BODY(QueryType::Float16)
+}
+
+bool ngt_linear_search_index(NGTIndex index, double* query, int32_t query_dim, size_t size,
+                             NGTObjectDistances results, NGTError error) {
+  SEARCH_ARGS_CHECK();
+  try {
+    return linear_common(index, query, QueryType::Float64, query_dim, size, results);
+  }
+  CAPI_CATCH(error, false)
+}
+
+bool ngt_linear_search_index_as_float(NGTIndex index, float* query, int32_t query_dim, size_t size,
+                                      NGTObjectDistances results, NGTError error) {
+  SEARCH_ARGS_CHECK();
+  try {
+    return linear_common(index, query, QueryType::Float32, query_dim, size, results);
+  }
+  CAPI_CATCH(error, false)
+}
+
+bool ngt_linear_search_index_with_query(NGTIndex index, NGTQuery query, NGTObjectDistances results,
+                                        NGTError error) {
+  if (index == nullptr || query.query == nullptr || results == nullptr) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " query = " << query.query << " results = " << results);
+    return false;
+  }
+  try {
+    int32_t dim = (int32_t)engine(index)->dimension();
+    return linear_common(index, query.query, QueryType::Float32, dim, query.size, results);
+  }
+  CAPI_CATCH(error, false)
+}
+
+int32_t ngt_get_size(NGTObjectDistances results, NGTError error) {
+  if (results == nullptr) {
+    CAPI_PARAM_ERROR(error, "results = " << results);
+    return -1;
+  }
+  return (int32_t) static_cast<Results*>(results)->size();
+}
+
+uint32_t ngt_get_result_size(NGTObjectDistances results, NGTError error) {
+  if (results == nullptr) {
+    CAPI_PARAM_ERROR(error, "results = " << results);
+    return 0;
+  }
+  return (uint32_t) static_cast<Results*>(results)->size();
+}
+
+NGTObjectDistance ngt_get_result(const NGTObjectDistances results, const uint32_t i, NGTError error) {
+  NGTObjectDistance none = {0, 0.0f};
+  if (results == nullptr) {
+    CAPI_PARAM_ERROR(error, "results = " << results);
+    return none;
+  }
+  const Results& r = *static_cast<const Results*>(results);
+  if (i >= r.size()) {
+    std::stringstream ss;
+    ss << "Capi : " << __FUNCTION__ << "() : Error: index " << i << " out of range (size " << r.size() << ")";
+    set_error(ss, error);
+    return none;
+  }
+  return r[i];
+}
+
+void ngt_destroy_results(NGTObjectDistances results) {
+  if (results == nullptr) return;
+  delete static_cast<Results*>(results);
+}
+
+NGTError ngt_create_error_object() {
+  try {
+    return static_cast<NGTError>(new std::string());
+  } catch (std::exception& err) {
+    std::cerr << "Capi : " << __FUNCTION__ << "() : Error: " << err.what();
+    return nullptr;
+  }
+}
+
+const char* ngt_get_error_string(const NGTError error) { return static_cast<std::string*>(error)->c_str(); }
+
+void ngt_clear_error_string(NGTError error) { *static_cast<std::string*>(error) = ""; }
+
+void ngt_destroy_error_object(NGTError error) { delete static_cast<std::string*>(error); }
+
+// ---------------------------------------------------------------------------
+// Extensions (include/ngtgpu.h)
+
+int32_t ngtgpu_get_dimension(NGTIndex index, NGTError error) {
+  if (index == nullptr) {
+    CAPI_PARAM_ERROR(error, "index = " << index);
+    return -1;
+  }
+  return (int32_t)engine(index)->dimension();
+}
+
+static std::vector<SearchArgs> args_from(const NGTQueryParameters* params, size_t nparams) {
+  std::vector<SearchArgs> a(nparams);
+  for (size_t i = 0; i < nparams; i++)
+    a[i] = make_args(params[i].size, params[i].epsilon, params[i].radius, edge_size_from_field(params[i].edge_size));
+  return a;
+}
+
+static void check_kernel(uint32_t kernel) {
+  if (kernel != NGTGPU_KERNEL_EXACT) throw std::runtime_error("unknown kernel selector " + std::to_string(kernel));
+}
+
+bool ngtgpu_search_batch_float(NGTIndex index, const float* queries, size_t nq, int32_t dim,
+                               const NGTQueryParameters* params, size_t nparams, NGTObjectDistance* results,
+                               size_t kmax, uint32_t* counts, NGTGPUQueryStats* stats, uint32_t kernel,
+                               NGTError error) {
+  if (index == nullptr || (nq && (queries == nullptr || results == nullptr || counts == nullptr)) ||
+      params == nullptr || dim <= 0 || !(nparams == 1 || nparams == nq)) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " queries = " << queries << " nq = " << nq
+                                       << " nparams = " << nparams << " dim = " << dim);
+    return false;
+  }
+  try {
+    check_kernel(kernel);
+    std::vector<SearchArgs> a = args_from(params, nparams);
+    for (const auto& x : a)
+      if (engine(index)->output_size(x) > kmax) throw std::runtime_error("a query asks for more results than kmax");
+    SearchOutput out;
+    engine(index)->search(queries, QueryType::Float32, nq, (size_t)dim, a.data(), a.size(), out);
+    for (size_t q = 0; q < nq; q++) {
+      counts[q] = out.counts[q];
+      for (uint32_t i = 0; i < out.counts[q]; i++) {
+        const ngtg::ObjDist& o = out.results[q * out.kmax + i];
+        results[q * kmax + i] = NGTObjectDistance{o.id, o.distance};
+      }
+      if (stats) std::memcpy(&stats[q], &out.stats[q], sizeof(NGTGPUQueryStats));
+    }
+    return true;
+  }
+  CAPI_CATCH(error, false)
+}
+
+size_t ngtgpu_query_row_bytes(NGTIndex index, NGTError error) {
+  if (index == nullptr) {
+    CAPI_PARAM_ERROR(error, "index = " << index);
+    return 0;
+  }
+  return engine(index)->host().row_bytes();
+}
+
+bool ngtgpu_convert_queries_float(NGTIndex index, const float* queries, size_t nq, int32_t dim, void* rows_out,
+                                  NGTError error) {
+  if (index == nullptr || (nq && (queries == nullptr || rows_out == nullptr)) || dim <= 0) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " queries = " << queries << " rows = " << rows_out);
+    return false;
+  }
+  try {
+    std::vector<uint8_t> rows;
+    engine(index)->convert_queries(queries, QueryType::Float32, nq, (size_t)dim, rows);
+    if (!rows.empty()) std::memcpy(rows_out, rows.data(), rows.size());
+    return true;
+  }
+  CAPI_CATCH(error, false)
+}
+
+bool ngtgpu_search_batch_device(NGTIndex index, const void* d_rows, size_t nq, const NGTQueryParameters* params,
+                                size_t nparams, NGTObjectDistance* d_results, size_t kmax, uint32_t* d_counts,
+                                NGTGPUQueryStats* d_stats, void* stream, uint32_t kernel, NGTError error) {
+  if (index == nullptr || (nq && (d_rows == nullptr || d_results == nullptr || d_counts == nullptr ||
+                                  d_stats == nullptr)) ||
+      params == nullptr || !(nparams == 1 || nparams == nq)) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " rows = " << d_rows << " nq = " << nq << " nparams = " << nparams);
+    return false;
+  }
+  try {
+    check_kernel(kernel);
+    std::vector<SearchArgs> a = args_from(params, nparams);
+    GraphEngine* e = engine(index);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : e->stream();
+    e->search_device(static_cast<const uint4*>(d_rows), nq, a.data(), a.size(),
+                     reinterpret_cast<ngtg::ObjDist*>(d_results), d_counts,
+                     reinterpret_cast<ngtg::QueryStats*>(d_stats), kmax, s);
+    return true;
+  }
+  CAPI_CATCH(error, false)
+}
+
+uint64_t ngtgpu_kernel_launches(NGTIndex index, NGTError error) {
+  if (index == nullptr) {
+    CAPI_PARAM_ERROR(error, "index = " << index);
+    return 0;
+  }
+  return engine(index)->launches();
+}
+
+}  // extern "C"

@@ -1,0 +1,73 @@
+// Device-resident index layout and per-query parameter blocks shared by the
+// host engine and the kernels.
+//
+// HBM layout (all arrays 16-byte aligned, row 0 is NGT's dummy object so that
+// object ids index rows directly):
+//   objects  : [nrows][row_chunks] uint4  -- the object's native type, zero padded
+//              to ((dim-1)/16+1)*16 elements like the reference's padded rows
+//              (lib/NGT/ObjectSpace.h:354)
+//   offsets  : [nrows+1] uint32           -- CSR of the graph (edge order kept)
+//   edges    : [E] uint32                 -- neighbour ids
+//   internals: DVP-tree internal nodes, pivots: [npivots][row_chunks] uint4
+//   leaf_seed_off/ids : per-leaf seed lists, already thinned on the host exactly
+//              as GraphAndTreeIndex::getSeedsFromTree does (lib/NGT/Index.h:2173-2220)
+#pragma once
+#include <cstdint>
+#include "ngt_types.h"
+
+namespace ngtg {
+
+struct DevInternal {
+  uint32_t pivot;
+  uint32_t nchildren;
+  uint32_t children[5];
+  float borders[4];
+  uint32_t pad;
+};
+
+struct DevGraph {
+  const uint4* objects = nullptr;
+  uint32_t row_chunks = 0;      // 16-byte chunks per row
+  uint32_t nrows = 0;
+  const uint32_t* offsets = nullptr;
+  const uint32_t* edges = nullptr;
+  const DevInternal* internals = nullptr;
+  uint32_t ninternals = 0;
+  const uint4* pivots = nullptr;
+  uint32_t root = 0;            // raw node id (bit 31 = leaf)
+  uint32_t nleaves = 0;
+  const uint32_t* leaf_seed_off = nullptr;
+  const uint32_t* leaf_seed_ids = nullptr;
+};
+
+// Per-query search parameters (one SearchContainer of the reference,
+// lib/NGT/Common.h:2456-2534, after the C API and getEdgeSize have resolved
+// the defaults).
+struct QueryParams {
+  uint32_t size;         // sc.size as used during the search (after RESULT_DEFINED_RANGE expansion)
+  uint32_t size_out;     // number of results kept at the end (sizeBackup or size)
+  float radius;          // initial sc.radius
+  float coef;            // coefficient applied to the radius to get explorationRadius
+  uint32_t edge_size;    // neighbours read per expanded node
+  uint32_t seed_off;     // explicit seeds: offset into the seed list (tree seeds: unused)
+  uint32_t seed_cnt;     // explicit seeds: count; 0xffffffff = take seeds from the tree
+  uint32_t out_off;      // offset of this query's results in the output arrays
+};
+
+// Per-query counters written by the kernels.
+struct QueryStats {
+  uint32_t distance_computations;
+  uint32_t expansions;
+  uint32_t visited;
+  uint32_t status;       // bit flags below
+};
+
+enum StatusBits : uint32_t {
+  kStatusCandidateOverflow = 1u,   // candidate list hit its capacity (result may differ)
+  kStatusVisitedSpill = 2u,        // visited set moved to the global bitmap
+  kStatusEmptySeeds = 4u,          // no seed was available
+  kStatusTreeError = 8u,           // tree descent exceeded its depth bound
+  kStatusIterationLimit = 16u,     // search loop hit its iteration bound
+};
+
+}  // namespace ngtg

@@ -1,0 +1,462 @@
+// Host engine implementation: uploads an opened index to HBM, converts
+// queries, resolves per-query parameters like the reference's C API and
+// search containers do, and launches the search kernels.
+#include "engine.h"
+
+#include <cuda_fp16.h>
+#include <algorithm>
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+
+#include "graph_exact.cuh"
+#include "kernels.h"
+#include "linear_select.cuh"
+#include "seed_rng.h"
+
+namespace ngtg {
+
+#define NGT_CUDA(x)                                                                                 \
+  do {                                                                                              \
+    cudaError_t e_ = (x);                                                                           \
+    if (e_ != cudaSuccess)                                                                          \
+      throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e_) + " in " #x);     \
+  } while (0)
+
+namespace {
+
+template <typename T>
+T* dmalloc_copy(const void* src, size_t bytes) {
+  void* p = nullptr;
+  size_t n = bytes ? bytes : 16;
+  NGT_CUDA(cudaMalloc(&p, n));
+  if (bytes) NGT_CUDA(cudaMemcpy(p, src, bytes, cudaMemcpyHostToDevice));
+  return static_cast<T*>(p);
+}
+
+uint32_t next_pow2(uint32_t v) {
+  uint32_t p = 1;
+  while (p < v) p <<= 1;
+  return p;
+}
+
+ExactKernelFn exact_kernel(ObjType t, Metric m) {
+  m = kernel_metric(m);
+  switch (t) {
+    case ObjType::Float: return exact_kernel_float(m);
+    case ObjType::Float16: return exact_kernel_half(m);
+    case ObjType::Uint8: return exact_kernel_u8(m);
+    default: return nullptr;
+  }
+}
+
+LinearKernelFn linear_kernel(ObjType t, Metric m) {
+  m = kernel_metric(m);
+  switch (t) {
+    case ObjType::Float: return linear_kernel_float(m);
+    case ObjType::Float16: return linear_kernel_half(m);
+    case ObjType::Uint8: return linear_kernel_u8(m);
+    default: return nullptr;
+  }
+}
+
+double query_elem(const void* q, QueryType qt, size_t i) {
+  switch (qt) {
+    case QueryType::Float32: return static_cast<const float*>(q)[i];
+    case QueryType::Float64: return static_cast<const double*>(q)[i];
+    case QueryType::Uint8: return static_cast<const uint8_t*>(q)[i];
+    case QueryType::Float16: return __half2float(static_cast<const __half*>(q)[i]);
+  }
+  return 0.0;
+}
+
+bool is_normalized(Metric m) {
+  return m == Metric::NormalizedAngle || m == Metric::NormalizedCosine || m == Metric::NormalizedL2;
+}
+
+}  // namespace
+
+GraphEngine::GraphEngine(const std::string& path, GraphMode mode) : mode_(mode) {
+  load_index(path, host_);
+  if (!exact_kernel(host_.prop.otype, host_.prop.metric))
+    throw std::runtime_error("unsupported combination of object type and distance type in " + path);
+  if (is_normalized(host_.prop.metric) && host_.prop.otype == ObjType::Uint8)
+    throw std::runtime_error("normalized distances over uint8 objects are not supported");
+  NGT_CUDA(cudaGetDevice(&device_));
+  NGT_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  upload();
+}
+
+GraphEngine::~GraphEngine() {
+  cudaSetDevice(device_);
+  cudaFree(d_objects_);
+  cudaFree(d_offsets_);
+  cudaFree(d_edges_);
+  cudaFree(d_internals_);
+  cudaFree(d_pivots_);
+  cudaFree(d_present_);
+  cudaFree(d_seed_off_);
+  cudaFree(d_seed_ids_);
+  cudaFree(d_bitmaps_);
+  if (stream_) cudaStreamDestroy(stream_);
+}
+
+void GraphEngine::upload() {
+  const HostIndex& h = host_;
+  d_objects_ = dmalloc_copy<void>(h.objects.data(), h.objects.size());
+  d_present_ = dmalloc_copy<uint8_t>(h.present.data(), h.present.size());
+  d_offsets_ = dmalloc_copy<uint32_t>(h.offsets.data(), h.offsets.size() * 4);
+  d_edges_ = dmalloc_copy<uint32_t>(h.edges.data(), h.edges.size() * 4);
+  std::vector<DevInternal> ins(h.tree.internals.size());
+  for (size_t i = 0; i < ins.size(); i++) {
+    const auto& s = h.tree.internals[i];
+    DevInternal d{};
+    d.pivot = s.pivot;
+    d.nchildren = s.nchildren;
+    for (int k = 0; k < 5; k++) d.children[k] = s.children[k];
+    for (int k = 0; k < 4; k++) d.borders[k] = s.borders[k];
+    ins[i] = d;
+  }
+  d_internals_ = dmalloc_copy<DevInternal>(ins.data(), ins.size() * sizeof(DevInternal));
+  d_pivots_ = dmalloc_copy<void>(h.tree.pivots.data(), h.tree.pivots.size());
+  nleaves_ = (uint32_t)h.tree.leaves.size();
+  dev_.objects = static_cast<const uint4*>(d_objects_);
+  dev_.row_chunks = (uint32_t)(h.row_bytes() / 16);
+  dev_.nrows = h.nrows;
+  dev_.offsets = d_offsets_;
+  dev_.edges = d_edges_;
+  dev_.internals = d_internals_;
+  dev_.ninternals = (uint32_t)ins.size();
+  dev_.pivots = static_cast<const uint4*>(d_pivots_);
+  dev_.root = h.tree.root;
+  dev_.nleaves = nleaves_;
+}
+
+// Thinned seed lists of every leaf for one effective seed size, concatenated
+// after the tables built so far.  Table t's offsets start at t*(nleaves+1).
+uint32_t GraphEngine::seed_table(size_t seed_size) {
+  auto it = seed_tables_.find(seed_size);
+  if (it != seed_tables_.end()) return it->second;
+  const HostTree& t = host_.tree;
+  uint32_t table = (uint32_t)seed_tables_.size();
+  std::vector<uint32_t> ids;
+  for (uint32_t leaf = 0; leaf < nleaves_; leaf++) {
+    h_seed_off_.push_back((uint32_t)h_seed_ids_.size());
+    if (!t.leaf_present[leaf]) continue;
+    const auto& L = t.leaves[leaf];
+    ids.assign(t.leaf_ids.begin() + L.first, t.leaf_ids.begin() + L.first + L.count);
+    thin_leaf_seeds(ids, leaf, seed_size);
+    h_seed_ids_.insert(h_seed_ids_.end(), ids.begin(), ids.end());
+  }
+  h_seed_off_.push_back((uint32_t)h_seed_ids_.size());
+  cudaFree(d_seed_off_);
+  cudaFree(d_seed_ids_);
+  d_seed_off_ = dmalloc_copy<uint32_t>(h_seed_off_.data(), h_seed_off_.size() * 4);
+  d_seed_ids_ = dmalloc_copy<uint32_t>(h_seed_ids_.data(), h_seed_ids_.size() * 4);
+  dev_.leaf_seed_off = d_seed_off_;
+  dev_.leaf_seed_ids = d_seed_ids_;
+  seed_tables_[seed_size] = table;
+  return table;
+}
+
+// NeighborhoodGraph::getEdgeSize (lib/NGT/Graph.h:991-1010).
+size_t GraphEngine::edge_size_for(const SearchArgs& a) const {
+  int64_t esize = a.edge_size == -1 ? host_.prop.edge_size_for_search : a.edge_size;
+  if (esize == 0) return INT_MAX;
+  if (esize > 0) return (size_t)esize;
+  if (esize == -2) {
+    float coef = a.epsilon + 1.0f;
+    double add = std::pow(10.0, ((double)coef - 1.0) * (double)(float)host_.prop.dynamic_edge_size_rate);
+    return add >= (double)INT_MAX ? (size_t)INT_MAX : (size_t)(host_.prop.dynamic_edge_size_base + add);
+  }
+  throw std::runtime_error("invalid edge size parameter " + std::to_string(a.edge_size));
+}
+
+void GraphEngine::build_params(const SearchArgs* args, size_t nargs, size_t nq, size_t kmax,
+                               std::vector<QueryParams>& params, std::vector<uint32_t>& seed_list,
+                               uint32_t& max_size) {
+  params.resize(nq);
+  seed_list.clear();
+  max_size = 0;
+  const Property& p = host_.prop;
+  for (size_t i = 0; i < nq; i++) {
+    const SearchArgs& a = args[nargs == 1 ? 0 : i];
+    QueryParams qp{};
+    float coef = a.epsilon + 1.0f;                     // SearchContainer::setEpsilon
+    if (coef == 0.0f) coef = 1.1f;                     // NGT_EXPLORATION_COEFFICIENT
+    size_t size = a.size;
+    size_t size_out = size;
+    bool size_backup = p.epsilon_type == 2;            // EpsilonTypeResultSize
+    if (size_backup) {
+      size = (size_t)std::round(coef * (float)size);
+      coef = 1.0f;
+      // Only the read-only search cuts the results back to the requested size
+      // (lib/NGT/Graph.cpp:821-828); the updatable search returns them all.
+      if (mode_ == GraphMode::Updatable) size_out = size;
+    }
+    if (size_out > kmax) throw std::runtime_error("result size larger than the output capacity");
+    qp.size = (uint32_t)size;
+    qp.size_out = (uint32_t)size_out;
+    qp.radius = a.radius < 0.0f ? FLT_MAX : a.radius;
+    qp.coef = coef;
+    qp.edge_size = (uint32_t)std::min<size_t>(edge_size_for(a), 0xffffffffu);
+    qp.out_off = (uint32_t)(i * kmax);
+    if (p.has_tree) {
+      // GraphAndTreeIndex::getSeedsFromTree: seedSize = SeedSize or size, capped by size;
+      // AllLeafNodes keeps the whole leaf.
+      size_t seed_size = p.seed_size == 0 ? a.size : (size_t)p.seed_size;
+      if (seed_size > a.size) seed_size = a.size;
+      if (p.seed_type == 4) seed_size = SIZE_MAX;
+      uint32_t t = seed_table(seed_size == 0 ? 1 : seed_size);
+      qp.seed_off = t * (nleaves_ + 1);
+      qp.seed_cnt = 0xffffffffu;
+    } else {
+      // Graph-only index: GraphIndex::getSeedsFromGraph (lib/NGT/Index.h:1658-1679).
+      size_t n = host_.nrows ? host_.nrows - 1 : 0;
+      size_t ss = std::min<size_t>(n, (size_t)p.seed_size);
+      qp.seed_off = (uint32_t)seed_list.size();
+      if (p.seed_type == 2) {
+        for (size_t s = 1; s <= ss; s++) seed_list.push_back((uint32_t)s);
+      } else if (p.seed_type == 3) {
+        seed_list.push_back(1u);
+      } else {
+        // getRandomSeeds draws from the process-global rand() without
+        // reseeding; here every query draws from a generator seeded with 1 so
+        // that results are reproducible.
+        GlibcRand rng(1);
+        std::vector<uint32_t> chosen;
+        size_t empty = 0;
+        while (chosen.size() < ss) {
+          double r = rng.unit();
+          size_t idx = (size_t)std::floor((double)n * r) + 1;
+          if (!host_.present[idx]) {
+            if (++empty > n) break;
+            continue;
+          }
+          if (std::find(chosen.begin(), chosen.end(), (uint32_t)idx) != chosen.end()) continue;
+          chosen.push_back((uint32_t)idx);
+        }
+        seed_list.insert(seed_list.end(), chosen.begin(), chosen.end());
+      }
+      qp.seed_cnt = (uint32_t)(seed_list.size() - qp.seed_off);
+    }
+    params[i] = qp;
+    max_size = std::max<uint32_t>(max_size, qp.size);
+  }
+  if (seed_list.empty()) seed_list.push_back(0);
+}
+
+size_t GraphEngine::output_size(const SearchArgs& a) const {
+  if (host_.prop.epsilon_type == 2 && mode_ == GraphMode::Updatable) {
+    float coef = a.epsilon + 1.0f;
+    if (coef == 0.0f) coef = 1.1f;
+    return (size_t)std::round(coef * (float)a.size);
+  }
+  return a.size;
+}
+
+void GraphEngine::convert_queries(const void* queries, QueryType qt, size_t nq, size_t qdim,
+                                  std::vector<uint8_t>& rows) const {
+  const size_t user_dim = (size_t)host_.prop.dimension;
+  if (qdim != host_.dim && !(host_.prop.metric == Metric::InnerProduct && qdim == user_dim))
+    throw std::runtime_error("the query dimension " + std::to_string(qdim) + " differs from the index dimension " +
+                             std::to_string(user_dim));
+  const size_t rb = host_.row_bytes();
+  rows.assign(nq * rb, 0);
+  const bool norm = is_normalized(host_.prop.metric);
+  std::vector<float> tmp(qdim);
+  for (size_t q = 0; q < nq; q++) {
+    uint8_t* dst = rows.data() + q * rb;
+    for (size_t i = 0; i < qdim; i++) tmp[i] = (float)query_elem(queries, qt, q * qdim + i);
+    switch (host_.prop.otype) {
+      case ObjType::Float: {
+        float* o = reinterpret_cast<float*>(dst);
+        for (size_t i = 0; i < qdim; i++) o[i] = qt == QueryType::Float64
+                                                   ? (float)static_cast<const double*>(queries)[q * qdim + i]
+                                                   : tmp[i];
+        if (norm) {
+          // ObjectSpace::normalize (lib/NGT/ObjectSpace.h:356-384): float sum, sqrt, divide.
+          float sum = 0.0f;
+          for (size_t i = 0; i < qdim; i++) sum += o[i] * o[i];
+          if (sum == 0.0f) throw std::runtime_error("the query is a zero vector; it cannot be normalized");
+          sum = (float)std::sqrt(sum);
+          for (size_t i = 0; i < qdim; i++) o[i] = o[i] / sum;
+        }
+        break;
+      }
+      case ObjType::Float16: {
+        __half* o = reinterpret_cast<__half*>(dst);
+        for (size_t i = 0; i < qdim; i++) o[i] = __float2half_rn(tmp[i]);
+        if (norm) {
+          float sum = 0.0f;
+          for (size_t i = 0; i < qdim; i++) {
+            float v = __half2float(o[i]);
+            sum += v * v;
+          }
+          if (sum == 0.0f) throw std::runtime_error("the query is a zero vector; it cannot be normalized");
+          sum = (float)std::sqrt(sum);
+          for (size_t i = 0; i < qdim; i++) o[i] = __float2half_rn(__half2float(o[i]) / sum);
+        }
+        break;
+      }
+      case ObjType::Uint8: {
+        for (size_t i = 0; i < qdim; i++) {
+          double v = query_elem(queries, qt, q * qdim + i);
+          dst[i] = (uint8_t)(int)v;       // static_cast<uint8_t> truncates toward zero
+        }
+        break;
+      }
+      default: throw std::runtime_error("unsupported object type");
+    }
+  }
+}
+
+void GraphEngine::ensure_scratch(size_t grid) {
+  if (grid <= bitmap_grid_) return;
+  cudaFree(d_bitmaps_);
+  d_bitmaps_ = nullptr;
+  size_t words = (host_.nrows + 31) / 32;
+  NGT_CUDA(cudaMalloc(&d_bitmaps_, grid * words * 4));
+  NGT_CUDA(cudaMemsetAsync(d_bitmaps_, 0, grid * words * 4, stream_));
+  bitmap_grid_ = grid;
+}
+
+void GraphEngine::search_device(const uint4* d_rows, size_t nq, const SearchArgs* args, size_t nargs, ObjDist* d_out,
+                                uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream) {
+  std::lock_guard<std::mutex> lock(mu_);
+  NGT_CUDA(cudaSetDevice(device_));
+  if (nq == 0) return;
+  std::vector<QueryParams> params;
+  std::vector<uint32_t> seeds;
+  uint32_t max_size = 0;
+  build_params(args, nargs, nq, kmax, params, seeds, max_size);
+  ExactConfig cfg{};
+  cfg.kcap = max_size + 1;
+  cfg.ccap = 1024;
+  cfg.hcap = 8192;
+  cfg.mode = (uint32_t)mode_;
+  cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));
+  cfg.bitmap_words = (host_.nrows + 31) / 32;
+  int max_smem = 0;
+  NGT_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
+  size_t smem = exact_smem_bytes(dev_.row_chunks, cfg);
+  while (smem > (size_t)max_smem && cfg.hcap > 2048) {
+    cfg.hcap >>= 1;
+    smem = exact_smem_bytes(dev_.row_chunks, cfg);
+  }
+  while (smem > (size_t)max_smem && cfg.ccap > 256) {
+    cfg.ccap >>= 1;
+    smem = exact_smem_bytes(dev_.row_chunks, cfg);
+  }
+  if (smem > (size_t)max_smem) throw std::runtime_error("result size too large for the on-chip search state");
+  ExactKernelFn fn = exact_kernel(host_.prop.otype, host_.prop.metric);
+  NGT_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0, sms = 0;
+  NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kExactThreads, smem));
+  NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+  size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
+  ensure_scratch(grid);
+  // per-call parameter buffers
+  QueryParams* d_params = nullptr;
+  uint32_t* d_seeds = nullptr;
+  NGT_CUDA(cudaMallocAsync(&d_params, nq * sizeof(QueryParams), stream));
+  NGT_CUDA(cudaMallocAsync(&d_seeds, seeds.size() * 4, stream));
+  NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QueryParams), cudaMemcpyHostToDevice, stream));
+  NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, stream));
+  fn<<<(unsigned)grid, kExactThreads, smem, stream>>>(dev_, d_rows, (uint32_t)nq, d_params, d_seeds, d_out, d_counts,
+                                                       d_stats, d_bitmaps_, cfg);
+  NGT_CUDA(cudaGetLastError());
+  launches_++;
+  NGT_CUDA(cudaFreeAsync(d_params, stream));
+  NGT_CUDA(cudaFreeAsync(d_seeds, stream));
+}
+
+void GraphEngine::search(const void* queries, QueryType qt, size_t nq, size_t qdim, const SearchArgs* args,
+                         size_t nargs, SearchOutput& out) {
+  NGT_CUDA(cudaSetDevice(device_));
+  std::vector<uint8_t> rows;
+  convert_queries(queries, qt, nq, qdim, rows);
+  size_t kmax = 1;
+  for (size_t i = 0; i < nargs; i++) kmax = std::max(kmax, output_size(args[i]));
+  out.kmax = kmax;
+  out.results.assign(nq * kmax, ObjDist{0, 0.f});
+  out.counts.assign(nq, 0);
+  out.stats.assign(nq, QueryStats{});
+  if (nq == 0) return;
+  uint4* d_rows = nullptr;
+  ObjDist* d_out = nullptr;
+  uint32_t* d_counts = nullptr;
+  QueryStats* d_stats = nullptr;
+  cudaStream_t s = stream_;
+  NGT_CUDA(cudaMallocAsync(&d_rows, rows.size(), s));
+  NGT_CUDA(cudaMallocAsync(&d_out, nq * kmax * sizeof(ObjDist), s));
+  NGT_CUDA(cudaMallocAsync(&d_counts, nq * 4, s));
+  NGT_CUDA(cudaMallocAsync(&d_stats, nq * sizeof(QueryStats), s));
+  NGT_CUDA(cudaMemcpyAsync(d_rows, rows.data(), rows.size(), cudaMemcpyHostToDevice, s));
+  search_device(d_rows, nq, args, nargs, d_out, d_counts, d_stats, kmax, s);
+  NGT_CUDA(cudaMemcpyAsync(out.results.data(), d_out, nq * kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, s));
+  NGT_CUDA(cudaMemcpyAsync(out.counts.data(), d_counts, nq * 4, cudaMemcpyDeviceToHost, s));
+  NGT_CUDA(cudaMemcpyAsync(out.stats.data(), d_stats, nq * sizeof(QueryStats), cudaMemcpyDeviceToHost, s));
+  NGT_CUDA(cudaFreeAsync(d_rows, s));
+  NGT_CUDA(cudaFreeAsync(d_out, s));
+  NGT_CUDA(cudaFreeAsync(d_counts, s));
+  NGT_CUDA(cudaFreeAsync(d_stats, s));
+  NGT_CUDA(cudaStreamSynchronize(s));
+}
+
+void GraphEngine::linear_search(const void* queries, QueryType qt, size_t nq, size_t qdim, size_t size,
+                                SearchOutput& out) {
+  std::lock_guard<std::mutex> lock(mu_);
+  NGT_CUDA(cudaSetDevice(device_));
+  std::vector<uint8_t> rows;
+  convert_queries(queries, qt, nq, qdim, rows);
+  size = std::min<size_t>(size, host_.nrows ? host_.nrows - 1 : 0);   // never more results than objects
+  size_t kmax = std::max<size_t>(size, 1);
+  out.kmax = kmax;
+  out.results.assign(nq * kmax, ObjDist{0, 0.f});
+  out.counts.assign(nq, 0);
+  out.stats.assign(nq, QueryStats{});
+  if (nq == 0 || size == 0) return;
+  if (size > 12288) throw std::runtime_error("linear search supports at most 12288 results per query");
+  LinearKernelFn fn = linear_kernel(host_.prop.otype, host_.prop.metric);
+  if (!fn) throw std::runtime_error("unsupported distance for linear search");
+  cudaStream_t s = stream_;
+  const uint32_t rc = dev_.row_chunks;
+  const size_t nrows = host_.nrows;
+  size_t qb = std::max<size_t>(1, std::min<size_t>({nq, (size_t)(1u << 28) / nrows, (size_t)65535}));
+  uint4* d_rows = nullptr;
+  float* d_dist = nullptr;
+  ObjDist* d_out = nullptr;
+  uint32_t* d_counts = nullptr;
+  NGT_CUDA(cudaMallocAsync(&d_rows, rows.size(), s));
+  NGT_CUDA(cudaMallocAsync(&d_dist, qb * nrows * 4, s));
+  NGT_CUDA(cudaMallocAsync(&d_out, nq * kmax * sizeof(ObjDist), s));
+  NGT_CUDA(cudaMallocAsync(&d_counts, nq * 4, s));
+  NGT_CUDA(cudaMemcpyAsync(d_rows, rows.data(), rows.size(), cudaMemcpyHostToDevice, s));
+  const uint32_t group = std::min<uint32_t>(32, next_pow2(rc));
+  const size_t sel_smem = (256 + 16) * 4 + 2 * kmax * 8;
+  NGT_CUDA(cudaFuncSetAttribute((const void*)linear_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)sel_smem));
+  for (size_t q0 = 0; q0 < nq; q0 += qb) {
+    size_t nb = std::min(qb, nq - q0);
+    dim3 grid((unsigned)((nrows + kLinRowsPerBlock - 1) / kLinRowsPerBlock), (unsigned)nb);
+    fn<<<grid, kLinThreads, rc * 16, s>>>(dev_, d_rows, (uint32_t)q0, (uint32_t)nb, d_present_, d_dist, group);
+    NGT_CUDA(cudaGetLastError());
+    linear_select_kernel<<<(unsigned)nb, 512, sel_smem, s>>>(d_dist, (uint32_t)nrows, (uint32_t)q0, (uint32_t)nb,
+                                                               (uint32_t)size, FLT_MAX, d_out, d_counts);
+    NGT_CUDA(cudaGetLastError());
+    launches_ += 2;
+  }
+  NGT_CUDA(cudaMemcpyAsync(out.results.data(), d_out, nq * kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, s));
+  NGT_CUDA(cudaMemcpyAsync(out.counts.data(), d_counts, nq * 4, cudaMemcpyDeviceToHost, s));
+  NGT_CUDA(cudaFreeAsync(d_rows, s));
+  NGT_CUDA(cudaFreeAsync(d_dist, s));
+  NGT_CUDA(cudaFreeAsync(d_out, s));
+  NGT_CUDA(cudaFreeAsync(d_counts, s));
+  NGT_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace ngtg

@@ -1,0 +1,108 @@
+// Host engine: one opened index resident in HBM plus the launch logic of the
+// search kernels.  The C ABI (capi.cpp) and the batched extension entry points
+// are thin wrappers around this class.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+#include "device_index.h"
+#include "index_files.h"
+
+namespace ngtg {
+
+// Search parameters of one query, as the reference's C API receives them
+// (ngt_search_index_ in lib/NGT/Capi.cpp:514-532).
+struct SearchArgs {
+  size_t size = 10;
+  float epsilon = 0.1f;
+  float radius = -1.0f;            // < 0 means FLT_MAX
+  int64_t edge_size = -1;          // -1: index default (EdgeSizeForSearch)
+};
+
+// Query element type accepted at the boundary.
+enum class QueryType { Float32 = 0, Float64 = 1, Uint8 = 2, Float16 = 3 };
+
+enum class Kernel { Exact = 0 };
+
+struct SearchOutput {
+  std::vector<ObjDist> results;    // nq * kmax
+  std::vector<uint32_t> counts;    // nq
+  std::vector<QueryStats> stats;   // nq
+  size_t kmax = 0;
+};
+
+class CudaError;
+
+class GraphEngine {
+ public:
+  GraphEngine(const std::string& path, GraphMode mode);
+  ~GraphEngine();
+  GraphEngine(const GraphEngine&) = delete;
+  GraphEngine& operator=(const GraphEngine&) = delete;
+
+  const HostIndex& host() const { return host_; }
+  GraphMode mode() const { return mode_; }
+  uint32_t dimension() const { return (uint32_t)host_.prop.dimension; }
+
+  // Graph search over host queries (row-major nq x qdim).
+  void search(const void* queries, QueryType qt, size_t nq, size_t qdim, const SearchArgs* args, size_t nargs,
+              SearchOutput& out);
+  // Exhaustive search (exact ids, ties broken by id).
+  void linear_search(const void* queries, QueryType qt, size_t nq, size_t qdim, size_t size, SearchOutput& out);
+
+  // Converts user queries to padded object rows exactly as the reference's
+  // allocateObject does (cast to the object type, normalisation for the
+  // normalised metrics, zero augmentation for inner product).
+  void convert_queries(const void* queries, QueryType qt, size_t nq, size_t qdim, std::vector<uint8_t>& rows) const;
+
+  // Device-side entry used by the batched extension: queries already converted
+  // and resident on the device.
+  void search_device(const uint4* d_rows, size_t nq, const SearchArgs* args, size_t nargs, ObjDist* d_out,
+                     uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream);
+
+  // Number of results a query can return (larger than args.size only for the
+  // updatable search on an index with EpsilonType ResultSize).
+  size_t output_size(const SearchArgs& a) const;
+
+  cudaStream_t stream() const { return stream_; }
+  int device() const { return device_; }
+  size_t row_chunks() const { return host_.row_bytes() / 16; }
+  // Number of launches of our kernels since the engine was created.
+  uint64_t launches() const { return launches_; }
+
+ private:
+  void upload();
+  uint32_t seed_table(size_t seed_size);        // index of the thinned-seed table
+  void build_params(const SearchArgs* args, size_t nargs, size_t nq, size_t kmax, std::vector<QueryParams>& params,
+                    std::vector<uint32_t>& seed_list, uint32_t& max_size);
+  size_t edge_size_for(const SearchArgs& a) const;
+  void ensure_scratch(size_t grid);
+
+  HostIndex host_;
+  GraphMode mode_;
+  int device_ = 0;
+  cudaStream_t stream_ = nullptr;
+  std::mutex mu_;
+  uint64_t launches_ = 0;
+  // device data
+  void* d_objects_ = nullptr;
+  uint32_t* d_offsets_ = nullptr;
+  uint32_t* d_edges_ = nullptr;
+  DevInternal* d_internals_ = nullptr;
+  void* d_pivots_ = nullptr;
+  uint8_t* d_present_ = nullptr;
+  uint32_t* d_seed_off_ = nullptr;
+  uint32_t* d_seed_ids_ = nullptr;
+  std::map<size_t, uint32_t> seed_tables_;
+  std::vector<uint32_t> h_seed_off_, h_seed_ids_;
+  uint32_t nleaves_ = 0;
+  // scratch (grown on demand, reused across calls)
+  uint32_t* d_bitmaps_ = nullptr;
+  size_t bitmap_grid_ = 0;
+  DevGraph dev_;
+};
+
+}  // namespace ngtg

@@ -1,0 +1,261 @@
+// Readers for the NGT index directory.  See index_files.h for the format
+// citations.  Every read is bounds-checked; a truncated or corrupted file is
+// rejected with a message instead of producing a partial index.
+#include "index_files.h"
+
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <stdexcept>
+
+namespace ngtg {
+
+namespace {
+
+[[noreturn]] void fail(const std::string& msg) { throw std::runtime_error(msg); }
+
+struct Reader {
+  std::vector<char> buf;
+  size_t pos = 0;
+  std::string name;
+  explicit Reader(const std::string& path) : name(path) {
+    std::ifstream f(path, std::ios::binary | std::ios::ate);
+    if (!f.is_open()) fail("cannot open " + path);
+    std::streamsize n = f.tellg();
+    f.seekg(0);
+    buf.resize((size_t)n);
+    if (n > 0 && !f.read(buf.data(), n)) fail("cannot read " + path);
+  }
+  template <typename T>
+  T get() {
+    if (pos + sizeof(T) > buf.size()) fail("truncated file " + name);
+    T v;
+    std::memcpy(&v, buf.data() + pos, sizeof(T));
+    pos += sizeof(T);
+    return v;
+  }
+  const char* take(size_t n) {
+    if (pos + n > buf.size()) fail("truncated file " + name);
+    const char* p = buf.data() + pos;
+    pos += n;
+    return p;
+  }
+  bool at_end() const { return pos == buf.size(); }
+};
+
+Metric parse_metric(const std::string& s) {
+  if (s == "L1") return Metric::L1;
+  if (s == "L2") return Metric::L2;
+  if (s == "Hamming") return Metric::Hamming;
+  if (s == "Jaccard") return Metric::Jaccard;
+  if (s == "SparseJaccard") return Metric::SparseJaccard;
+  if (s == "Angle") return Metric::Angle;
+  if (s == "Cosine") return Metric::Cosine;
+  if (s == "NormalizedAngle") return Metric::NormalizedAngle;
+  if (s == "NormalizedCosine") return Metric::NormalizedCosine;
+  if (s == "NormalizedL2") return Metric::NormalizedL2;
+  if (s == "InnerProduct") return Metric::InnerProduct;
+  if (s == "Poincare") return Metric::Poincare;
+  if (s == "Lorentz") return Metric::Lorentz;
+  fail("unsupported DistanceType '" + s + "'");
+}
+
+ObjType parse_objtype(const std::string& s) {
+  if (s == "Float-4") return ObjType::Float;
+  if (s == "Integer-1") return ObjType::Uint8;
+  if (s == "Float-2") return ObjType::Float16;
+  fail("unsupported ObjectType '" + s + "' (quantized object types are not supported)");
+}
+
+int to_int(const std::string& s, const char* key) {
+  try {
+    size_t used = 0;
+    long v = std::stol(s, &used);
+    return (int)v;
+  } catch (...) {
+    fail(std::string("invalid integer for ") + key + ": '" + s + "'");
+  }
+}
+
+}  // namespace
+
+std::string Property::get(const std::string& k, const std::string& dflt) const {
+  auto it = kv.find(k);
+  return it == kv.end() ? dflt : it->second;
+}
+
+Property load_property(const std::string& dir) {
+  Property p;
+  std::ifstream f(dir + "/prf");
+  if (!f.is_open()) fail("cannot open " + dir + "/prf");
+  std::string line;
+  while (std::getline(f, line)) {
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    auto tab = line.find('\t');
+    if (tab == std::string::npos) continue;
+    p.kv[line.substr(0, tab)] = line.substr(tab + 1);
+  }
+  p.dimension = to_int(p.get("Dimension", "0"), "Dimension");
+  if (p.dimension <= 0) fail("invalid Dimension in " + dir + "/prf");
+  p.metric = parse_metric(p.get("DistanceType", "L2"));
+  p.otype = parse_objtype(p.get("ObjectType", "Float-4"));
+  p.has_tree = p.get("IndexType", "GraphAndTree") == "GraphAndTree";
+  p.edge_size_for_search = to_int(p.get("EdgeSizeForSearch", "40"), "EdgeSizeForSearch");
+  p.dynamic_edge_size_base = to_int(p.get("DynamicEdgeSizeBase", "30"), "DynamicEdgeSizeBase");
+  p.dynamic_edge_size_rate = to_int(p.get("DynamicEdgeSizeRate", "20"), "DynamicEdgeSizeRate");
+  p.seed_size = to_int(p.get("SeedSize", "10"), "SeedSize");
+  std::string st = p.get("SeedType", "None");
+  p.seed_type = st == "RandomNodes" ? 1 : st == "FixedNodes" ? 2 : st == "FirstNode" ? 3 : st == "AllLeafNodes" ? 4 : 0;
+  std::string et = p.get("EpsilonType", "None");
+  p.epsilon_type = et == "ByQuery" ? 1 : et == "ResultSize" ? 2 : 0;
+  p.graph_type = p.get("GraphType", "ANNG");
+  if (p.metric == Metric::SparseJaccard) fail("SparseJaccard indexes are not supported");
+  return p;
+}
+
+static void read_objects(const std::string& path, HostIndex& ix) {
+  Reader r(path);
+  uint64_t n = r.get<uint64_t>();
+  if (n == 0 || n > 0xFFFFFFF0ull) fail("invalid object count in " + path);
+  const size_t es = ix.elem_size();
+  const size_t file_row = (size_t)ix.dim * es;
+  ix.nrows = (uint32_t)n;
+  ix.objects.assign((size_t)n * ix.row_bytes(), 0);
+  ix.present.assign(n, 0);
+  for (uint64_t i = 0; i < n; i++) {
+    char t = r.get<char>();
+    if (t == '-') continue;
+    if (t != '+') fail("corrupted object file " + path);
+    const char* src = r.take(file_row);
+    std::memcpy(ix.objects.data() + i * ix.row_bytes(), src, file_row);
+    ix.present[i] = 1;
+  }
+  if (!r.at_end()) fail("trailing bytes in object file " + path);
+}
+
+static void read_graph(const std::string& path, HostIndex& ix) {
+  Reader r(path);
+  uint64_t n = r.get<uint64_t>();
+  if (n > 0xFFFFFFF0ull) fail("invalid node count in " + path);
+  ix.offsets.assign(ix.nrows + 1, 0);
+  ix.edges.clear();
+  std::vector<uint32_t> start(ix.nrows, 0), deg(ix.nrows, 0);
+  for (uint64_t i = 0; i < n; i++) {
+    char t = r.get<char>();
+    if (t == '-') continue;
+    if (t != '+') fail("corrupted graph file " + path);
+    uint32_t cnt = r.get<uint32_t>();
+    const char* p = r.take((size_t)cnt * 8);
+    if (i >= ix.nrows) fail("graph node beyond the object repository in " + path);
+    start[i] = (uint32_t)ix.edges.size();
+    deg[i] = cnt;
+    for (uint32_t e = 0; e < cnt; e++) {
+      uint32_t id;
+      std::memcpy(&id, p + (size_t)e * 8, 4);
+      if (id == 0 || id >= ix.nrows) fail("edge to an invalid object id in " + path);
+      ix.edges.push_back(id);
+    }
+  }
+  // A trailing uint32-counted vector of uint16 (GraphRepository::prevsize) may follow.
+  if (!r.at_end()) {
+    uint32_t m = r.get<uint32_t>();
+    r.take((size_t)m * 2);
+    if (!r.at_end()) fail("trailing bytes in graph file " + path);
+  }
+  // Rows are laid out in id order already; offsets is the CSR prefix.
+  uint32_t acc = 0;
+  for (uint32_t i = 0; i < ix.nrows; i++) {
+    if (deg[i] && start[i] != acc) fail("internal error: non-monotone graph layout");
+    ix.offsets[i] = acc;
+    acc += deg[i];
+  }
+  ix.offsets[ix.nrows] = acc;
+}
+
+static void read_tree(const std::string& path, HostIndex& ix) {
+  Reader r(path);
+  HostTree& t = ix.tree;
+  const size_t es = ix.elem_size();
+  const size_t file_row = (size_t)ix.dim * es;
+  const size_t row = ix.row_bytes();
+  auto add_pivot = [&](const char* src) {
+    t.pivots.resize((size_t)(t.npivots + 1) * row, 0);
+    std::memcpy(t.pivots.data() + (size_t)t.npivots * row, src, file_row);
+    return t.npivots++;
+  };
+  // leaves
+  uint64_t nl = r.get<uint64_t>();
+  if (nl > 0xFFFFFFFull) fail("invalid leaf count in " + path);
+  t.leaves.assign(nl, {});
+  t.leaf_present.assign(nl, 0);
+  for (uint64_t i = 0; i < nl; i++) {
+    char c = r.get<char>();
+    if (c == '-') continue;
+    if (c != '+') fail("corrupted tree file " + path);
+    r.get<uint32_t>();                 // node id
+    uint32_t parent = r.get<uint32_t>();
+    uint16_t cnt = r.get<uint16_t>();
+    t.leaves[i].first = (uint32_t)t.leaf_ids.size();
+    t.leaves[i].count = cnt;
+    for (uint16_t k = 0; k < cnt; k++) {
+      uint32_t id = r.get<uint32_t>();
+      r.get<float>();
+      t.leaf_ids.push_back(id);
+    }
+    if (!((parent & 0x7fffffffu) == 0 && cnt == 0)) r.take(file_row);  // leaf pivot (unused for seeds)
+    t.leaf_present[i] = 1;
+  }
+  // internal nodes
+  uint64_t ni = r.get<uint64_t>();
+  if (ni > 0xFFFFFFFull) fail("invalid internal-node count in " + path);
+  t.internals.assign(ni, {});
+  t.internal_present.assign(ni, 0);
+  for (uint64_t i = 0; i < ni; i++) {
+    char c = r.get<char>();
+    if (c == '-') continue;
+    if (c != '+') fail("corrupted tree file " + path);
+    r.get<uint32_t>();
+    r.get<uint32_t>();
+    HostTree::Internal in;
+    in.pivot = add_pivot(r.take(file_row));
+    uint64_t cs = r.get<uint64_t>();
+    if (cs < 2 || cs > 5) fail("unsupported internal fan-out in " + path);
+    in.nchildren = (uint32_t)cs;
+    for (uint64_t k = 0; k < cs; k++) in.children[k] = r.get<uint32_t>();
+    for (uint64_t k = 0; k + 1 < cs; k++) in.borders[k] = r.get<float>();
+    t.internals[i] = in;
+    t.internal_present[i] = 1;
+  }
+  if (!r.at_end()) fail("trailing bytes in tree file " + path);
+  // Root is node 1: internal if present, otherwise the leaf (lib/NGT/Tree.h:217-233).
+  if (ni > 1 && t.internal_present[1]) t.root = 1u;
+  else if (nl > 1 && t.leaf_present[1]) t.root = 0x80000000u | 1u;
+  else fail("tree has no root node in " + path);
+  // Validate child references so the device never follows a bad id.
+  for (uint64_t i = 0; i < ni; i++) {
+    if (!t.internal_present[i]) continue;
+    for (uint32_t k = 0; k < t.internals[i].nchildren; k++) {
+      uint32_t raw = t.internals[i].children[k];
+      uint32_t idx = raw & 0x7fffffffu;
+      bool leaf = (raw & 0x80000000u) != 0;
+      if (leaf ? (idx >= nl || !t.leaf_present[idx]) : (idx >= ni || !t.internal_present[idx]))
+        fail("tree child reference out of range in " + path);
+    }
+  }
+  for (uint32_t id : t.leaf_ids)
+    if (id == 0 || id >= ix.nrows) fail("tree leaf holds an invalid object id in " + path);
+}
+
+void load_index(const std::string& dir, HostIndex& ix) {
+  ix.path = dir;
+  ix.prop = load_property(dir);
+  ix.dim = (uint32_t)ix.prop.dimension + (ix.prop.metric == Metric::InnerProduct ? 1u : 0u);
+  ix.dpad = ((ix.dim - 1) / 16 + 1) * 16;
+  read_objects(dir + "/obj", ix);
+  read_graph(dir + "/grp", ix);
+  if (ix.prop.has_tree) {
+    read_tree(dir + "/tre", ix);
+  }
+}
+
+}  // namespace ngtg

@@ -1,0 +1,82 @@
+// Readers for the on-disk NGT index directory (prf / obj / grp / tre).
+//
+// The formats are fixed by the reference and must be read byte-for-byte:
+//   prf : text "key<TAB>value" lines               (lib/NGT/Common.h:915-1000 PropertySet,
+//                                                    keys written by lib/NGT/Index.h:121-200
+//                                                    and lib/NGT/Graph.h:627-739)
+//   obj : Repository<Object>: size_t n, then per slot '-' or '+' and
+//         Dimension*sizeof(type) raw bytes          (lib/NGT/Common.h:2181-2238,
+//                                                    lib/NGT/ObjectSpace.h:620-640)
+//   grp : Repository<GraphNode>: size_t n, per slot '-' or '+' then
+//         uint32 count + count*{uint32 id,float d}  (lib/NGT/Graph.h:153-160,
+//                                                    lib/NGT/ObjectSpace.h:72-80)
+//   tre : leaf repository then internal repository (lib/NGT/Tree.h:347-355,
+//                                                    lib/NGT/Node.h:88-110,218-280,441-510)
+#pragma once
+#include <map>
+#include <string>
+#include <vector>
+#include <cstdint>
+#include "ngt_types.h"
+
+namespace ngtg {
+
+struct Property {
+  std::map<std::string, std::string> kv;
+  int dimension = 0;               // user dimension (prf "Dimension")
+  Metric metric = Metric::L2;
+  ObjType otype = ObjType::Float;
+  bool has_tree = true;            // IndexType GraphAndTree
+  int edge_size_for_search = 40;
+  int dynamic_edge_size_base = 30;
+  int dynamic_edge_size_rate = 20;
+  int seed_size = 10;
+  int seed_type = 0;               // SeedType (lib/NGT/Graph.h:297-304)
+  int epsilon_type = 0;            // EpsilonType (lib/NGT/Graph.h:306)
+  std::string graph_type;
+  std::string get(const std::string& k, const std::string& dflt = "") const;
+};
+
+// DVP tree with the pivots flattened into one arena.
+struct HostTree {
+  // Node ids keep the reference's raw encoding: bit 31 = leaf, low bits = index.
+  struct Internal {
+    uint32_t pivot = 0;            // row in pivots (in units of padded rows)
+    uint32_t children[5] = {0, 0, 0, 0, 0};
+    float borders[4] = {0, 0, 0, 0};
+    uint32_t nchildren = 0;
+  };
+  struct Leaf {
+    uint32_t first = 0;            // offset into leaf_ids
+    uint32_t count = 0;
+  };
+  std::vector<Internal> internals;  // index = node index (slot 0 unused)
+  std::vector<uint8_t> internal_present;
+  std::vector<Leaf> leaves;
+  std::vector<uint8_t> leaf_present;
+  std::vector<uint32_t> leaf_ids;   // object ids stored in leaves, in stored order
+  std::vector<uint8_t> pivots;      // [npivots][dpad] elements of the object type
+  uint32_t npivots = 0;
+  uint32_t root = 0;                // raw id of the root node
+};
+
+struct HostIndex {
+  std::string path;
+  Property prop;
+  uint32_t nrows = 0;               // repository size including the dummy row 0
+  uint32_t dim = 0;                 // stored dimension (D, or D+1 for inner product)
+  uint32_t dpad = 0;                // ((dim-1)/16+1)*16
+  std::vector<uint8_t> objects;     // [nrows][dpad] elements, zero padded
+  std::vector<uint8_t> present;     // 1 if the object slot is occupied
+  std::vector<uint32_t> offsets;    // CSR of the graph, nrows+1 entries
+  std::vector<uint32_t> edges;
+  HostTree tree;
+  size_t elem_size() const { return objtype_size(prop.otype); }
+  size_t row_bytes() const { return (size_t)dpad * elem_size(); }
+};
+
+// Throws std::runtime_error with a message on any format or I/O error.
+Property load_property(const std::string& dir);
+void load_index(const std::string& dir, HostIndex& out);
+
+}  // namespace ngtg

@@ -1,0 +1,26 @@
+// Kernel lookup by (object type, metric).  Each object type's instantiations
+// live in their own translation unit so they compile in parallel.
+#pragma once
+#include <cuda_runtime.h>
+#include "device_index.h"
+
+namespace ngtg {
+
+struct ExactConfig;
+
+typedef void (*ExactKernelFn)(DevGraph, const uint4*, uint32_t, const QueryParams*, const uint32_t*, ObjDist*,
+                              uint32_t*, QueryStats*, uint32_t*, ExactConfig);
+typedef void (*LinearKernelFn)(DevGraph, const uint4*, uint32_t, uint32_t, const uint8_t*, float*, uint32_t);
+
+// Return nullptr when the (type, metric) pair is not supported.
+ExactKernelFn exact_kernel_float(Metric m);
+ExactKernelFn exact_kernel_half(Metric m);
+ExactKernelFn exact_kernel_u8(Metric m);
+LinearKernelFn linear_kernel_float(Metric m);
+LinearKernelFn linear_kernel_half(Metric m);
+LinearKernelFn linear_kernel_u8(Metric m);
+
+// Metric used by the kernels: inner product runs as L2 over the augmented rows.
+inline Metric kernel_metric(Metric m) { return m == Metric::InnerProduct ? Metric::L2 : m; }
+
+}  // namespace ngtg

@@ -1,0 +1,36 @@
+"""Seeded synthetic workloads with the shapes and value distributions of the
+benchmark configurations (no public dataset is available offline).
+
+All generators use numpy's PCG64 (``default_rng(seed)``), whose streams are
+identical on x86-64 and aarch64, so an object file regenerated on the GPU
+host is byte-identical to the one the reference indexed here.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def clipped_exponential(n: int, dim: int, seed: int, mean: float = 25.0) -> np.ndarray:
+    """Coordinates min(255, rint(Exponential(mean))) as float32 (integer valued)."""
+    rng = np.random.default_rng(seed)
+    return np.minimum(255.0, np.rint(rng.exponential(mean, size=(n, dim)))).astype(np.float32)
+
+
+def gaussian_mixture(n: int, dim: int, nclusters: int, seed_means: int, seed: int, sigma: float = 0.5,
+                     normalize: bool = False) -> np.ndarray:
+    """Points drawn around `nclusters` N(0,1) means with per-coordinate sigma."""
+    means = np.random.default_rng(seed_means).standard_normal((nclusters, dim)).astype(np.float32)
+    rng = np.random.default_rng(seed)
+    lab = rng.integers(0, nclusters, size=n)
+    x = means[lab] + sigma * rng.standard_normal((n, dim)).astype(np.float32)
+    x = x.astype(np.float32)
+    if normalize:
+        x /= np.linalg.norm(x, axis=1, keepdims=True).astype(np.float32)
+    return x
+
+
+def random_bytes(n: int, dim: int, seed: int, p_one: float = 0.5) -> np.ndarray:
+    """uint8 vectors whose bits are 1 with probability p_one (for Hamming / Jaccard)."""
+    rng = np.random.default_rng(seed)
+    bits = (rng.random((n, dim * 8)) < p_one).astype(np.uint8)
+    return np.packbits(bits, axis=1, bitorder="little").astype(np.float32)

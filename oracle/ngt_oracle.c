@@ -1,0 +1,505 @@
+/*
+ * ORACLE -- test infrastructure only.  A plain-C, single-threaded-per-query
+ * restatement of NGT's search path, used by tests/ to check the CUDA library
+ * and by bench.py as the timed CPU baseline (OpenMP over queries, the pattern
+ * of ngtpy.Index.batch_search, python/src/ngtpy.cpp:422-458).  Nothing in the
+ * product links or calls this file.
+ *
+ * Restated from the reference (file:line in the NGT source tree):
+ *   comparators       lib/NGT/PrimitiveComparatorNoArch.h:30-390 (scalar forms;
+ *                     double accumulation, exact for integer-valued data)
+ *   linear search     lib/NGT/ObjectSpaceRepository.h:860-922
+ *   graph search      lib/NGT/Graph.cpp:716-835 (read-only) and 840-1024 (updatable),
+ *                     setupDistances/setupSeeds lib/NGT/Graph.cpp:420-586,
+ *                     getEdgeSize lib/NGT/Graph.h:991-1010
+ *   result heap       ResultSet push / pop / push_pop lib/NGT/Common.h:2412-2431
+ *                     (libstdc++ pop_heap on Linux: push_pop replaces the top)
+ *   tree seeds        DVPTree::search SearchLeaf lib/NGT/Tree.cpp:403-559,
+ *                     getSeedsFromTree thinning lib/NGT/Index.h:2173-2220
+ *   glibc rand()      random_r TYPE_3 (degree 31, separation 3) as published
+ *   query conversion  ObjectRepository::setObject lib/NGT/ObjectRepository.h:238-282,
+ *                     ObjectSpace::normalize lib/NGT/ObjectSpace.h:356-384
+ */
+#include <float.h>
+#include <limits.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+enum { OT_FLOAT = 0, OT_UINT8 = 1, OT_HALF = 2 };
+enum {
+  M_L1 = 0, M_L2 = 1, M_HAMMING = 2, M_ANGLE = 3, M_COSINE = 4, M_NANGLE = 5, M_NCOSINE = 6,
+  M_JACCARD = 7, M_NL2 = 9, M_IP = 10, M_POINCARE = 100, M_LORENTZ = 101
+};
+
+typedef struct {
+  int otype, metric;
+  uint32_t nrows, dpad;
+  const void *objects;
+  const uint8_t *present;
+  const uint32_t *offsets, *edges;
+  int has_tree;
+  uint32_t root, ninternals, nleaves;
+  const uint32_t *in_pivot, *in_nchildren, *in_children; /* children: [ninternals][5] */
+  const float *in_borders;                               /* [ninternals][4] */
+  const void *pivots;
+  const uint32_t *leaf_first, *leaf_count, *leaf_ids;
+  int seed_size, seed_type, epsilon_type, edge_size_for_search, dyn_base, dyn_rate;
+} OracleIndex;
+
+/* ---------------- glibc rand() ---------------- */
+typedef struct { int32_t s[31]; int f, r; } grand_t;
+
+static int32_t grand_next(grand_t *g) {
+  uint32_t v = (uint32_t)g->s[g->f] + (uint32_t)g->s[g->r];
+  g->s[g->f] = (int32_t)v;
+  if (++g->f == 31) g->f = 0;
+  if (++g->r == 31) g->r = 0;
+  return (int32_t)(v >> 1);
+}
+
+static void grand_seed(grand_t *g, uint32_t seed) {
+  if (seed == 0) seed = 1;
+  int64_t w = (int32_t)seed;
+  g->s[0] = (int32_t)seed;
+  for (int i = 1; i < 31; i++) {
+    int64_t hi = w / 127773, lo = w % 127773;
+    w = 16807 * lo - 2836 * hi;
+    if (w < 0) w += 2147483647;
+    g->s[i] = (int32_t)w;
+  }
+  g->f = 3;
+  g->r = 0;
+  for (int i = 0; i < 310; i++) grand_next(g);
+}
+
+void oracle_rand_sequence(uint32_t seed, size_t n, int32_t *out) {
+  grand_t g;
+  grand_seed(&g, seed);
+  for (size_t i = 0; i < n; i++) out[i] = grand_next(&g);
+}
+
+/* ---------------- element access ---------------- */
+static double half_to_double(uint16_t h) {
+  uint32_t sign = (h >> 15) & 1, exp = (h >> 10) & 31, man = h & 1023;
+  double v;
+  if (exp == 0) v = ldexp((double)man, -24);
+  else if (exp == 31) v = man ? NAN : INFINITY;
+  else v = ldexp((double)(man | 1024), (int)exp - 25);
+  return sign ? -v : v;
+}
+
+static inline double elem(const void *row, int ot, size_t i) {
+  switch (ot) {
+    case OT_FLOAT: return ((const float *)row)[i];
+    case OT_UINT8: return ((const uint8_t *)row)[i];
+    default: return half_to_double(((const uint16_t *)row)[i]);
+  }
+}
+
+static size_t elem_size(int ot) { return ot == OT_FLOAT ? 4 : ot == OT_UINT8 ? 1 : 2; }
+
+/* ---------------- comparators ---------------- */
+static float compare(int ot, int metric, const void *a, const void *b, size_t n) {
+  switch (metric) {
+    case M_L2:
+    case M_IP: {
+      double d = 0.0;
+      for (size_t i = 0; i < n; i++) {
+        double x = elem(a, ot, i) - elem(b, ot, i);
+        d += x * x;
+      }
+      return (float)sqrt(d);
+    }
+    case M_L1: {
+      double d = 0.0;
+      for (size_t i = 0; i < n; i++) d += fabs(elem(a, ot, i) - elem(b, ot, i));
+      return (float)d;
+    }
+    case M_HAMMING:
+    case M_JACCARD: {
+      const uint8_t *x = (const uint8_t *)a, *y = (const uint8_t *)b;
+      size_t nb = n * elem_size(ot);
+      uint64_t c = 0, u = 0;
+      for (size_t i = 0; i < nb; i++) {
+        if (metric == M_HAMMING) c += (uint64_t)__builtin_popcount((unsigned)(x[i] ^ y[i]));
+        else {
+          c += (uint64_t)__builtin_popcount((unsigned)(x[i] & y[i]));
+          u += (uint64_t)__builtin_popcount((unsigned)(x[i] | y[i]));
+        }
+      }
+      if (metric == M_HAMMING) return (float)(double)c;
+      return (float)(1.0 - (double)c / (double)u);
+    }
+    case M_NCOSINE:
+    case M_NANGLE:
+    case M_NL2: {
+      double s = 0.0;
+      for (size_t i = 0; i < n; i++) s += (double)(float)elem(a, ot, i) * (double)(float)elem(b, ot, i);
+      if (metric == M_NCOSINE) { double v = 1.0 - s; return (float)(v < 0.0 ? -v : v); }
+      if (metric == M_NL2) { double v = 2.0 - 2.0 * s; return (float)(v < 0.0 ? 0.0 : sqrt(v)); }
+      if (s >= 1.0) return 0.0f;
+      if (s <= -1.0) return (float)acos(-1.0);
+      return (float)acos(s);
+    }
+    case M_COSINE:
+    case M_ANGLE: {
+      double na = 0, nb = 0, s = 0;
+      for (size_t i = 0; i < n; i++) {
+        double x = elem(a, ot, i), y = elem(b, ot, i);
+        na += x * x; nb += y * y; s += x * y;
+      }
+      double c = s / sqrt(na * nb);
+      if (metric == M_COSINE) { double v = 1.0 - c; return (float)(v < 0.0 ? -v : v); }
+      if (c >= 1.0) return 0.0f;
+      if (c <= -1.0) return (float)acos(-1.0);
+      return (float)acos(c);
+    }
+    case M_POINCARE: {
+      double a2 = 0, b2 = 0, l2 = 0;
+      for (size_t i = 0; i < n; i++) {
+        double x = elem(a, ot, i), y = elem(b, ot, i);
+        a2 += x * x; b2 += y * y; l2 += (x - y) * (x - y);
+      }
+      double c2 = sqrt(l2);
+      return (float)acosh(1 + 2.0 * c2 * c2 / (1.0 - a2) / (1.0 - b2));
+    }
+    case M_LORENTZ: {
+      double s = elem(a, ot, 0) * elem(b, ot, 0);
+      for (size_t i = 1; i < n; i++) s -= elem(a, ot, i) * elem(b, ot, i);
+      return (float)acosh(s);
+    }
+  }
+  return NAN;
+}
+
+float oracle_distance(int ot, int metric, const void *a, const void *b, size_t n) {
+  return compare(ot, metric, a, b, n);
+}
+
+static const void *row_ptr(const OracleIndex *ix, const void *base, size_t r) {
+  return (const uint8_t *)base + r * (size_t)ix->dpad * elem_size(ix->otype);
+}
+
+/* ---------------- (distance, id) order and heaps ---------------- */
+typedef struct { uint32_t id; float d; } od_t;
+
+static inline int od_less(od_t a, od_t b) { return a.d == b.d ? a.id < b.id : a.d < b.d; }
+
+/* max-heap (ResultSet) */
+static void maxheap_push(od_t *h, size_t *n, od_t x) {
+  size_t i = (*n)++;
+  h[i] = x;
+  while (i > 0) {
+    size_t p = (i - 1) / 2;
+    if (!od_less(h[p], h[i])) break;
+    od_t t = h[p]; h[p] = h[i]; h[i] = t;
+    i = p;
+  }
+}
+static void maxheap_siftdown(od_t *h, size_t n, size_t i) {
+  for (;;) {
+    size_t l = 2 * i + 1, r = l + 1, m = i;
+    if (l < n && od_less(h[m], h[l])) m = l;
+    if (r < n && od_less(h[m], h[r])) m = r;
+    if (m == i) break;
+    od_t t = h[m]; h[m] = h[i]; h[i] = t;
+    i = m;
+  }
+}
+static void maxheap_pop(od_t *h, size_t *n) {
+  h[0] = h[--(*n)];
+  maxheap_siftdown(h, *n, 0);
+}
+/* push_pop as the reference executes it on Linux: the new element replaces the
+ * current top, whatever their order (pop_heap without the preceding push_heap). */
+static void maxheap_replace_top(od_t *h, size_t n, od_t x) {
+  h[0] = x;
+  maxheap_siftdown(h, n, 0);
+}
+
+/* min-heap (UncheckedSet) with growth */
+typedef struct { od_t *a; size_t n, cap; } minheap_t;
+static void minheap_push(minheap_t *m, od_t x) {
+  if (m->n == m->cap) {
+    m->cap = m->cap ? m->cap * 2 : 256;
+    m->a = (od_t *)realloc(m->a, m->cap * sizeof(od_t));
+  }
+  size_t i = m->n++;
+  m->a[i] = x;
+  while (i > 0) {
+    size_t p = (i - 1) / 2;
+    if (!od_less(m->a[i], m->a[p])) break;
+    od_t t = m->a[p]; m->a[p] = m->a[i]; m->a[i] = t;
+    i = p;
+  }
+}
+static od_t minheap_pop(minheap_t *m) {
+  od_t top = m->a[0];
+  m->a[0] = m->a[--m->n];
+  size_t i = 0;
+  for (;;) {
+    size_t l = 2 * i + 1, r = l + 1, s = i;
+    if (l < m->n && od_less(m->a[l], m->a[s])) s = l;
+    if (r < m->n && od_less(m->a[r], m->a[s])) s = r;
+    if (s == i) break;
+    od_t t = m->a[s]; m->a[s] = m->a[i]; m->a[i] = t;
+    i = s;
+  }
+  return top;
+}
+
+static int od_cmp(const void *x, const void *y) {
+  od_t a = *(const od_t *)x, b = *(const od_t *)y;
+  return od_less(a, b) ? -1 : od_less(b, a) ? 1 : 0;
+}
+
+/* heap -> ascending array (ObjectDistances::moveFrom) */
+static size_t heap_to_sorted(od_t *h, size_t n, uint32_t *ids, float *ds) {
+  qsort(h, n, sizeof(od_t), od_cmp);
+  for (size_t i = 0; i < n; i++) { ids[i] = h[i].id; ds[i] = h[i].d; }
+  return n;
+}
+
+/* ---------------- linear search ---------------- */
+static size_t linear_one(const OracleIndex *ix, const void *q, size_t k, uint32_t *ids, float *ds) {
+  od_t *h = (od_t *)malloc((k + 1) * sizeof(od_t));
+  size_t n = 0;
+  for (uint32_t r = 1; r < ix->nrows; r++) {
+    if (!ix->present[r]) continue;
+    float d = compare(ix->otype, ix->metric, q, row_ptr(ix, ix->objects, r), ix->dpad);
+    od_t x = {r, d};
+    maxheap_push(h, &n, x);
+    if (n > k) maxheap_pop(h, &n);
+  }
+  size_t m = heap_to_sorted(h, n, ids, ds);
+  free(h);
+  return m;
+}
+
+void oracle_linear_search(const OracleIndex *ix, const void *qrows, size_t nq, size_t k, uint32_t *out_ids,
+                          float *out_d, uint32_t *out_n, int nthreads) {
+  size_t rb = (size_t)ix->dpad * elem_size(ix->otype);
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads)
+  for (long q = 0; q < (long)nq; q++) {
+    out_n[q] = k ? (uint32_t)linear_one(ix, (const uint8_t *)qrows + q * rb, k, out_ids + q * k, out_d + q * k) : 0;
+  }
+}
+
+/* ---------------- seeds ---------------- */
+static size_t tree_seeds(const OracleIndex *ix, const void *q, size_t size, uint32_t *seeds, uint32_t *ndc) {
+  uint32_t node = ix->root;
+  while (!(node & 0x80000000u)) {
+    float d = compare(ix->otype, ix->metric, q, row_ptr(ix, ix->pivots, ix->in_pivot[node]), ix->dpad);
+    (*ndc)++;
+    uint32_t bsize = ix->in_nchildren[node] - 1, mid;
+    for (mid = 0; mid < bsize; mid++)
+      if (d < ix->in_borders[(size_t)node * 4 + mid]) break;
+    node = ix->in_children[(size_t)node * 5 + mid];
+  }
+  uint32_t leaf = node & 0x7fffffffu;
+  size_t cnt = ix->leaf_count[leaf];
+  for (size_t i = 0; i < cnt; i++) seeds[i] = ix->leaf_ids[ix->leaf_first[leaf] + i];
+  if (ix->seed_type == 4) return cnt; /* AllLeafNodes */
+  size_t seed_size = ix->seed_size == 0 ? size : (size_t)ix->seed_size;
+  if (seed_size > size) seed_size = size;
+  if (cnt > seed_size) {
+    grand_t g;
+    grand_seed(&g, leaf);
+    for (size_t i = cnt; i > seed_size; i--) {
+      double random = ((double)grand_next(&g) + 1.0) / ((double)2147483647 + 2.0);
+      size_t idx = (size_t)floor((double)i * random);
+      seeds[idx] = seeds[i - 1];
+    }
+    cnt = seed_size;
+  }
+  return cnt;
+}
+
+/* GraphIndex::getSeedsFromGraph / getRandomSeeds (lib/NGT/Index.h:1270-1302,1658-1679),
+ * with the generator freshly seeded with 1 for every query. */
+static size_t graph_seeds(const OracleIndex *ix, uint32_t *seeds) {
+  size_t n = ix->nrows ? ix->nrows - 1 : 0;
+  size_t ss = (size_t)ix->seed_size < n ? (size_t)ix->seed_size : n;
+  size_t cnt = 0;
+  if (ix->seed_type == 2) {
+    for (size_t i = 1; i <= ss; i++) seeds[cnt++] = (uint32_t)i;
+    return cnt;
+  }
+  if (ix->seed_type == 3) { seeds[0] = 1; return 1; }
+  grand_t g;
+  grand_seed(&g, 1);
+  size_t empty = 0;
+  while (cnt < ss) {
+    double r = ((double)grand_next(&g) + 1.0) / ((double)2147483647 + 2.0);
+    size_t idx = (size_t)floor((double)n * r) + 1;
+    if (!ix->present[idx]) { if (++empty > n) break; continue; }
+    int dup = 0;
+    for (size_t i = 0; i < cnt; i++) dup |= seeds[i] == idx;
+    if (dup) continue;
+    seeds[cnt++] = (uint32_t)idx;
+  }
+  return cnt;
+}
+
+static size_t edge_size_for(const OracleIndex *ix, int64_t edge_size, float coef) {
+  int64_t e = edge_size == -1 ? ix->edge_size_for_search : edge_size;
+  if (e == 0) return INT_MAX;
+  if (e > 0) return (size_t)e;
+  double add = pow(10, ((double)coef - 1.0) * (double)(float)ix->dyn_rate);
+  return add >= (double)INT_MAX ? (size_t)INT_MAX : (size_t)(ix->dyn_base + add);
+}
+
+/* ---------------- graph search ---------------- */
+static size_t graph_one(const OracleIndex *ix, const void *q, size_t k, size_t kout, float epsilon, float radius0,
+                        int64_t edge_size, int mode, uint32_t *ids, float *ds, uint32_t *dc_out,
+                        const uint32_t *given_seeds, size_t ngiven) {
+  float coef = epsilon + 1.0f;
+  if (coef == 0.0f) coef = 1.1f;
+  size_t size = k, size_backup = 0;
+  if (ix->epsilon_type == 2) { size_backup = k; size = (size_t)roundf(coef * (float)k); }
+  float radius = radius0 < 0.0f ? FLT_MAX : radius0;
+  size_t esz = edge_size_for(ix, edge_size, coef);
+  float expcoef = size_backup ? 1.0f : coef;
+  uint32_t dc = 0;
+  uint32_t *seeds = (uint32_t *)malloc(sizeof(uint32_t) * (65536 + ngiven));
+  size_t ns;
+  if (ix->has_tree) ns = tree_seeds(ix, q, size, seeds, &dc), dc = 0;
+  else if (given_seeds) { memcpy(seeds, given_seeds, ngiven * sizeof(uint32_t)); ns = ngiven; }
+  else ns = graph_seeds(ix, seeds);
+  if (k == 0 || ns == 0) { free(seeds); *dc_out = 0; return 0; }
+  od_t *sd = (od_t *)malloc(ns * sizeof(od_t));
+  for (size_t i = 0; i < ns; i++) {
+    sd[i].id = seeds[i];
+    sd[i].d = compare(ix->otype, ix->metric, q, row_ptr(ix, ix->objects, seeds[i]), ix->dpad);
+  }
+  dc += (uint32_t)ns;
+  qsort(sd, ns, sizeof(od_t), od_cmp);
+  od_t *res = (od_t *)malloc((size + 2) * sizeof(od_t));
+  size_t nres = 0;
+  for (size_t i = 0; i < ns; i++) {
+    if (nres < size && sd[i].d <= radius) maxheap_push(res, &nres, sd[i]);
+    else break;
+  }
+  if (nres >= size) radius = res[0].d;
+  uint8_t *visited = (uint8_t *)calloc(ix->nrows, 1);
+  minheap_t cand = {0, 0, 0};
+  for (size_t i = 0; i < ns; i++) {
+    visited[sd[i].id] = 1;
+    minheap_push(&cand, sd[i]);
+  }
+  float expR = expcoef * radius;
+  while (cand.n) {
+    od_t t = minheap_pop(&cand);
+    if (t.d > expR) break;
+    uint32_t e0 = ix->offsets[t.id], deg = ix->offsets[t.id + 1] - e0;
+    size_t nsz = deg < esz ? deg : esz;
+    for (size_t j = 0; j < nsz; j++) {
+      uint32_t v = ix->edges[e0 + j];
+      if (visited[v]) continue;
+      visited[v] = 1;
+      float d = compare(ix->otype, ix->metric, q, row_ptr(ix, ix->objects, v), ix->dpad);
+      dc++;
+      if (d <= expR) {
+        od_t x = {v, d};
+        minheap_push(&cand, x);
+        if (d <= radius) {
+          if (mode == 0) {          /* read-only: push_pop when full */
+            if (nres >= size) {
+              maxheap_replace_top(res, nres, x);
+              radius = res[0].d;
+              expR = expcoef * radius;
+            } else {
+              maxheap_push(res, &nres, x);
+            }
+          } else {                  /* updatable: push, pop when over, radius = top */
+            maxheap_push(res, &nres, x);
+            if (nres >= size) {
+              if (res[0].d >= d) {
+                if (nres > size) maxheap_pop(res, &nres);
+                radius = res[0].d;
+                expR = expcoef * radius;
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  /* Only the read-only search cuts the expanded result set back to sizeBackup
+   * (lib/NGT/Graph.cpp:821-828); the updatable search returns it as is. */
+  if (size_backup && mode == 0) while (nres > size_backup) maxheap_pop(res, &nres);
+  qsort(res, nres, sizeof(od_t), od_cmp);
+  size_t n = nres;
+  for (size_t i = 0; i < n && i < kout; i++) { ids[i] = res[i].id; ds[i] = res[i].d; }
+  free(res); free(sd); free(seeds); free(visited); free(cand.a);
+  *dc_out = dc;
+  return n;
+}
+
+/* out arrays are nq x kout (kout >= the largest result count).  seed_list/seed_off/seed_cnt are used for graph-only indexes. */
+void oracle_graph_search(const OracleIndex *ix, const void *qrows, size_t nq, size_t k, size_t kout, float epsilon,
+                         float radius, int64_t edge_size, int mode, uint32_t *out_ids, float *out_d, uint32_t *out_n,
+                         uint32_t *out_dc, const uint32_t *seed_list, const uint32_t *seed_off,
+                         const uint32_t *seed_cnt, int nthreads) {
+  size_t rb = (size_t)ix->dpad * elem_size(ix->otype);
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads)
+  for (long q = 0; q < (long)nq; q++) {
+    const uint32_t *gs = seed_list ? seed_list + seed_off[q] : NULL;
+    size_t ng = seed_list ? seed_cnt[q] : 0;
+    uint32_t dc = 0;
+    out_n[q] = (uint32_t)graph_one(ix, (const uint8_t *)qrows + q * rb, k, kout, epsilon, radius, edge_size, mode,
+                                   out_ids + q * kout, out_d + q * kout, &dc, gs, ng);
+    if (out_dc) out_dc[q] = dc;
+  }
+}
+
+/* float -> IEEE half, round to nearest even (half.hpp's default rounding). */
+static uint16_t float_to_half(float f) {
+  uint32_t x;
+  memcpy(&x, &f, 4);
+  uint32_t sign = (x >> 16) & 0x8000u;
+  int32_t exp = (int32_t)((x >> 23) & 0xff) - 127 + 15;
+  uint32_t man = x & 0x7fffffu;
+  if (((x >> 23) & 0xff) == 0xff) return (uint16_t)(sign | 0x7c00u | (man ? 0x200u : 0));
+  if (exp >= 31) return (uint16_t)(sign | 0x7c00u);
+  if (exp <= 0) {
+    if (exp < -10) return (uint16_t)sign;
+    man |= 0x800000u;
+    uint32_t shift = (uint32_t)(14 - exp);
+    uint32_t h = man >> shift, rem = man & ((1u << shift) - 1), half = 1u << (shift - 1);
+    if (rem > half || (rem == half && (h & 1u))) h++;
+    return (uint16_t)(sign | h);
+  }
+  uint32_t h = ((uint32_t)exp << 10) | (man >> 13), rem = man & 0x1fffu;
+  if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) h++;
+  return (uint16_t)(sign | h);
+}
+
+/* Query conversion: cast to the object type, normalise (float sum, sqrt,
+ * divide, in the object type) for the normalised metrics. */
+void oracle_prepare_queries(int ot, int metric, uint32_t dpad, const float *q, size_t nq, size_t dim, void *rows) {
+  size_t rb = (size_t)dpad * elem_size(ot);
+  memset(rows, 0, nq * rb);
+  int norm = metric == M_NCOSINE || metric == M_NANGLE || metric == M_NL2;
+  for (size_t i = 0; i < nq; i++) {
+    uint8_t *dst = (uint8_t *)rows + i * rb;
+    const float *src = q + i * dim;
+    if (ot == OT_FLOAT) {
+      float *o = (float *)dst;
+      for (size_t j = 0; j < dim; j++) o[j] = src[j];
+      if (norm) {
+        volatile float sum = 0.0f;
+        for (size_t j = 0; j < dim; j++) { float p = o[j] * o[j]; sum = sum + p; }
+        float s = (float)sqrt((double)sum);
+        for (size_t j = 0; j < dim; j++) o[j] = o[j] / s;
+      }
+    } else if (ot == OT_UINT8) {
+      for (size_t j = 0; j < dim; j++) dst[j] = (uint8_t)(int)src[j];
+    } else {
+      uint16_t *o = (uint16_t *)dst;
+      for (size_t j = 0; j < dim; j++) o[j] = float_to_half(src[j]);
+    }
+  }
+}

@@ -1,0 +1,201 @@
+"""Generates the golden fixtures under tests/golden/ by running the reference.
+
+Each fixture is a small NGT index built by the unmodified reference CLI
+(oracle/_ref/ngt, compiled from the reference sources by `make -C oracle ref`)
+over seeded synthetic data, plus the reference's own search results for a set
+of (k, epsilon, edge_size, open mode) settings, obtained through the
+reference C API by oracle/_ref/ref_dump.  Only this script needs the
+reference; the tests read the committed files.
+
+Stored per fixture (tests/golden/<name>/):
+  prf               the index property file, verbatim
+  grp.gz, tre.gz    the graph and tree files, gzip-compressed
+  obj.gz            the object file, unless it is regenerated from the seeds
+                    (meta.json "regenerate_obj": true, sha256 recorded)
+  meta.json         generator, shapes, seeds, the ngt create options
+  golden.npz        queries seed + per-setting ids / distances / counts
+
+usage: python tests/golden/make_golden.py [fixture ...]
+"""
+from __future__ import annotations
+
+import gzip
+import hashlib
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from ngt_gb300 import synthetic  # noqa: E402
+import oracle  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref")
+
+# name -> spec.  "gen": (generator, kwargs) for base and queries; "create": ngt create options.
+FIXTURES = {
+    "c1_f32_l2": dict(
+        base=("clipped_exponential", dict(n=5000, dim=128, seed=1)),
+        query=("clipped_exponential", dict(n=1000, dim=128, seed=2)),
+        create="-d 128 -o f -D 2 -E 10 -S 40 -i t", regenerate_obj=True, otype="f",
+        settings=[("graph", 10, 0.1, None, "ro"), ("graph", 10, 0.0, None, "ro"), ("graph", 20, 0.2, None, "ro"),
+                  ("graph", 10, 0.3, None, "ro"), ("graph", 10, 0.1, 0, "ro"), ("graph", 10, 0.1, -2, "ro"),
+                  ("graph", 10, 0.1, 10, "ro"), ("graph", 10, 0.1, None, "rw"), ("graph", 100, 0.1, None, "ro:200"),
+                  ("graph", 100, 0.1, None, "rw:200"), ("linear", 10, 0.0, None, "ro"),
+                  ("linear", 100, 0.0, None, "ro:200")]),
+    "c1_f32_l2_onng": dict(
+        base=("clipped_exponential", dict(n=5000, dim=128, seed=1)),
+        query=("clipped_exponential", dict(n=500, dim=128, seed=2)),
+        create="-d 128 -o f -D 2 -E 100 -S 0 -e 0.1 -i t", reconstruct="-m S -o 10 -i 100",
+        regenerate_obj=True, otype="f",
+        settings=[("graph", 10, 0.1, None, "ro"), ("graph", 10, 0.02, None, "ro"), ("graph", 100, 0.1, None, "ro:100")]),
+    "u8_l2": dict(
+        base=("clipped_exponential", dict(n=3000, dim=64, seed=31)),
+        query=("clipped_exponential", dict(n=300, dim=64, seed=32)),
+        create="-d 64 -o c -D 2 -E 10 -S 40 -i t", regenerate_obj=True, otype="c",
+        settings=[("graph", 10, 0.1, None, "ro"), ("graph", 10, 0.1, None, "rw"), ("linear", 10, 0.0, None, "ro")]),
+    "u8_l1": dict(
+        base=("clipped_exponential", dict(n=2000, dim=48, seed=41)),
+        query=("clipped_exponential", dict(n=200, dim=48, seed=42)),
+        create="-d 48 -o c -D 1 -E 10 -S 40 -i t", regenerate_obj=True, otype="c",
+        settings=[("graph", 10, 0.1, None, "ro"), ("linear", 10, 0.0, None, "ro")]),
+    "u8_hamming": dict(
+        base=("random_bytes", dict(n=2000, dim=32, seed=51, p_one=0.3)),
+        query=("random_bytes", dict(n=200, dim=32, seed=52, p_one=0.3)),
+        create="-d 32 -o c -D h -E 10 -S 40 -i t", regenerate_obj=True, otype="c",
+        settings=[("graph", 10, 0.1, None, "ro"), ("linear", 10, 0.0, None, "ro")]),
+    "u8_jaccard": dict(
+        base=("random_bytes", dict(n=2000, dim=32, seed=61, p_one=0.3)),
+        query=("random_bytes", dict(n=200, dim=32, seed=62, p_one=0.3)),
+        create="-d 32 -o c -D j -E 10 -S 40 -i t", regenerate_obj=True, otype="c",
+        settings=[("graph", 10, 0.1, None, "ro"), ("linear", 10, 0.0, None, "ro")]),
+    "f32_l1": dict(
+        base=("gaussian_mixture", dict(n=2000, dim=32, nclusters=16, seed_means=71, seed=72)),
+        query=("gaussian_mixture", dict(n=200, dim=32, nclusters=16, seed_means=71, seed=73)),
+        create="-d 32 -o f -D 1 -E 10 -S 40 -i t", regenerate_obj=True, otype="f",
+        settings=[("graph", 10, 0.1, None, "ro"), ("linear", 10, 0.0, None, "ro")]),
+    "f32_cosine": dict(
+        base=("gaussian_mixture", dict(n=2000, dim=32, nclusters=16, seed_means=81, seed=82)),
+        query=("gaussian_mixture", dict(n=200, dim=32, nclusters=16, seed_means=81, seed=83)),
+        create="-d 32 -o f -D c -E 10 -S 40 -i t", regenerate_obj=True, otype="f",
+        settings=[("graph", 10, 0.1, None, "ro"), ("linear", 10, 0.0, None, "ro")]),
+    "f32_angle": dict(
+        base=("gaussian_mixture", dict(n=2000, dim=32, nclusters=16, seed_means=91, seed=92)),
+        query=("gaussian_mixture", dict(n=200, dim=32, nclusters=16, seed_means=91, seed=93)),
+        create="-d 32 -o f -D a -E 10 -S 40 -i t", regenerate_obj=True, otype="f",
+        settings=[("graph", 10, 0.1, None, "ro"), ("linear", 10, 0.0, None, "ro")]),
+    "f32_ncosine": dict(
+        base=("gaussian_mixture", dict(n=2000, dim=32, nclusters=16, seed_means=101, seed=102)),
+        query=("gaussian_mixture", dict(n=200, dim=32, nclusters=16, seed_means=101, seed=103)),
+        create="-d 32 -o f -D C -E 10 -S 40 -i t", regenerate_obj=False, otype="f",
+        settings=[("graph", 10, 0.1, None, "ro"), ("linear", 10, 0.0, None, "ro")]),
+    "f32_nl2": dict(
+        base=("gaussian_mixture", dict(n=2000, dim=32, nclusters=16, seed_means=111, seed=112)),
+        query=("gaussian_mixture", dict(n=200, dim=32, nclusters=16, seed_means=111, seed=113)),
+        create="-d 32 -o f -D E -E 10 -S 40 -i t", regenerate_obj=False, otype="f",
+        settings=[("graph", 10, 0.1, None, "ro"), ("linear", 10, 0.0, None, "ro")]),
+    "f16_l2": dict(
+        base=("clipped_exponential", dict(n=2000, dim=64, seed=131)),
+        query=("clipped_exponential", dict(n=200, dim=64, seed=132)),
+        create="-d 64 -o h -D 2 -E 10 -S 40 -i t", regenerate_obj=True, otype="h",
+        settings=[("graph", 10, 0.1, None, "ro"), ("linear", 10, 0.0, None, "ro")]),
+    "f32_l2_graphonly": dict(
+        base=("clipped_exponential", dict(n=2000, dim=32, seed=141)),
+        query=("clipped_exponential", dict(n=200, dim=32, seed=142)),
+        create="-d 32 -o f -D 2 -E 10 -S 40 -i g", regenerate_obj=True, otype="f",
+        settings=[("graph", 10, 0.1, None, "ro"), ("graph", 10, 0.1, None, "rw")]),
+    "f32_l2_resultsize": dict(
+        base=("clipped_exponential", dict(n=2000, dim=32, seed=151)),
+        query=("clipped_exponential", dict(n=200, dim=32, seed=152)),
+        create="-d 32 -o f -D 2 -E 10 -S 40 -i t", regenerate_obj=True, otype="f",
+        prf_set={"EpsilonType": "ResultSize"},
+        settings=[("graph", 10, 0.1, None, "ro"), ("graph", 10, 0.2, None, "rw")]),
+}
+
+
+def gen(spec):
+    name, kw = spec
+    return getattr(synthetic, name)(**kw)
+
+
+def object_rows(x: np.ndarray, otype: str) -> np.ndarray:
+    return {"f": np.float32, "c": np.uint8, "h": np.float16}[otype](x) if otype != "f" else x.astype(np.float32)
+
+
+def run(cmd, **kw):
+    r = subprocess.run(cmd, capture_output=True, text=True, **kw)
+    if r.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
+    return r.stdout
+
+
+def make(name: str, spec: dict) -> None:
+    out = os.path.join(HERE, name)
+    base = gen(spec["base"])
+    queries = gen(spec["query"])
+    with tempfile.TemporaryDirectory() as tmp:
+        tsv = os.path.join(tmp, "base.tsv")
+        np.savetxt(tsv, base, fmt="%.9g", delimiter="\t")
+        idx = os.path.join(tmp, "idx")
+        run([os.path.join(REF, "ngt"), "create"] + spec["create"].split() + [idx, tsv])
+        if "reconstruct" in spec:
+            idx2 = os.path.join(tmp, "idx2")
+            run([os.path.join(REF, "ngt"), "reconstruct-graph"] + spec["reconstruct"].split() + [idx, idx2])
+            idx = idx2
+        if "prf_set" in spec:
+            prf = oracle.read_property(idx)
+            prf.update(spec["prf_set"])
+            with open(os.path.join(idx, "prf"), "w") as f:
+                for k in sorted(prf):
+                    f.write("%s\t%s\n" % (k, prf[k]))
+        os.makedirs(out, exist_ok=True)
+        shutil.copy(os.path.join(idx, "prf"), os.path.join(out, "prf"))
+        for fn in ("grp", "tre", "obj"):
+            src = os.path.join(idx, fn)
+            if not os.path.exists(src) or (fn == "obj" and spec["regenerate_obj"]):
+                continue
+            with open(src, "rb") as fi, gzip.GzipFile(os.path.join(out, fn + ".gz"), "wb", mtime=0) as fo:
+                fo.write(fi.read())
+        obj_sha = hashlib.sha256(open(os.path.join(idx, "obj"), "rb").read()).hexdigest()
+        if spec["regenerate_obj"]:
+            regen = os.path.join(tmp, "obj_regen")
+            oracle.write_objects(regen, object_rows(base, spec["otype"]))
+            if hashlib.sha256(open(regen, "rb").read()).hexdigest() != obj_sha:
+                raise RuntimeError(name + ": regenerated object file differs from the reference's")
+        qf = os.path.join(tmp, "q.f32")
+        queries.astype(np.float32).tofile(qf)
+        arrays = {}
+        settings = []
+        for i, (op, k, eps, edge, mode) in enumerate(spec["settings"]):
+            nq = queries.shape[0]
+            if ":" in mode:
+                mode, nq = mode.split(":")[0], int(mode.split(":")[1])
+            dump = os.path.join(tmp, "out%d" % i)
+            run([os.path.join(REF, "ref_dump"), op, idx, qf, str(nq), str(queries.shape[1]), str(k), repr(eps),
+                 "x" if edge is None else str(edge), mode, dump])
+            raw = np.fromfile(dump, np.uint8)
+            ids = raw[:nq * k * 4].view(np.uint32).reshape(nq, k)
+            ds = raw[nq * k * 4:2 * nq * k * 4].view(np.float32).reshape(nq, k)
+            cnt = raw[2 * nq * k * 4:].view(np.uint32)
+            arrays["ids_%d" % i], arrays["dist_%d" % i], arrays["count_%d" % i] = ids, ds, cnt
+            settings.append(dict(op=op, k=k, epsilon=eps, edge_size=edge, mode=mode, nq=nq))
+        np.savez_compressed(os.path.join(out, "golden.npz"), **arrays)
+    meta = dict(name=name, base=spec["base"], query=spec["query"], create=spec["create"],
+                reconstruct=spec.get("reconstruct"), prf_set=spec.get("prf_set"), otype=spec["otype"],
+                regenerate_obj=spec["regenerate_obj"], obj_sha256=obj_sha, settings=settings,
+                reference="NGT " + open(os.path.join(REF, "include", "NGT", "version_defs.h")).read().split('"')[-2])
+    with open(os.path.join(out, "meta.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    print("wrote", out)
+
+
+if __name__ == "__main__":
+    names = sys.argv[1:] or list(FIXTURES)
+    for n in names:
+        make(n, FIXTURES[n])

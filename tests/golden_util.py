@@ -1,0 +1,52 @@
+"""Helpers shared by the tests: materialise a committed golden fixture as an
+NGT index directory and load its golden vectors."""
+from __future__ import annotations
+
+import gzip
+import json
+import os
+import shutil
+
+import numpy as np
+
+import oracle
+from ngt_gb300 import synthetic
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+INTEGER_FIXTURES = {"c1_f32_l2", "c1_f32_l2_onng", "u8_l2", "u8_l1", "u8_hamming", "u8_jaccard", "f16_l2",
+                    "f32_l2_graphonly", "f32_l2_resultsize"}
+
+
+def fixture_names():
+    return sorted(d for d in os.listdir(GOLDEN) if os.path.isdir(os.path.join(GOLDEN, d)))
+
+
+def generate(spec):
+    name, kw = spec
+    return getattr(synthetic, name)(**kw)
+
+
+def materialize(name: str, root: str):
+    """Writes the index of fixture `name` under root/name; returns (path, meta, queries, golden)."""
+    src = os.path.join(GOLDEN, name)
+    meta = json.load(open(os.path.join(src, "meta.json")))
+    out = os.path.join(root, name)
+    if not os.path.exists(os.path.join(out, "obj")):
+        os.makedirs(out, exist_ok=True)
+        shutil.copy(os.path.join(src, "prf"), out)
+        for fn in ("grp", "tre", "obj"):
+            p = os.path.join(src, fn + ".gz")
+            if os.path.exists(p):
+                with gzip.open(p) as fi, open(os.path.join(out, fn), "wb") as fo:
+                    fo.write(fi.read())
+        if meta["regenerate_obj"]:
+            base = generate(meta["base"])
+            rows = {"f": np.float32, "c": np.uint8, "h": np.float16}[meta["otype"]](base)
+            oracle.write_objects(os.path.join(out, "obj"), rows)
+    queries = generate(meta["query"])
+    golden = np.load(os.path.join(src, "golden.npz"))
+    return out, meta, queries, golden
+
+
+def is_integer_fixture(name: str) -> bool:
+    return name in INTEGER_FIXTURES

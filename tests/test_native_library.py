@@ -1,0 +1,112 @@
+"""CPU-side checks of the native library: it builds, loads, exports every
+function the public headers declare, and its index loader rejects damaged
+index files with an error message (the loader runs before any CUDA call, so
+this needs no GPU)."""
+import ctypes
+import gzip
+import os
+import re
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from golden_util import materialize
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB = os.path.join(ROOT, "ngt_gb300", "libngtgpu.so")
+
+
+def _have_nvcc():
+    return shutil.which("nvcc") or os.path.exists("/usr/local/cuda/bin/nvcc")
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(LIB):
+        if not _have_nvcc():
+            pytest.skip("libngtgpu.so not built and nvcc unavailable")
+        from ngt_gb300.build import build_native
+        build_native()
+    return ctypes.CDLL(LIB)
+
+
+def declared_functions():
+    names = []
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        if not h.endswith(".h"):
+            continue
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        text = re.sub(r"//[^\n]*", "", text)
+        for m in re.finditer(r"^[A-Za-z_][\w \*]*?\b((?:ngt|ngtgpu|ngtqg|qbg)_\w+)\s*\(", text, flags=re.M):
+            names.append(m.group(1))
+    return sorted(set(names))
+
+
+def test_headers_declare_the_search_api():
+    names = declared_functions()
+    for must in ("ngt_open_index_as_read_only", "ngt_search_index_as_float", "ngt_linear_search_index_as_float",
+                 "ngt_get_result", "ngtgpu_search_batch_float"):
+        assert must in names
+
+
+def test_library_exports_every_declared_function(lib):
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_library_is_built_for_sm_103a(lib):
+    # the fatbin carries an sm_103a cubin; cuobjdump-free check through the ELF note nvcc writes
+    data = open(LIB, "rb").read()
+    assert b"sm_103a" in data or b"sm_103" in data
+
+
+def _error_string(lib, fn, path):
+    lib.ngt_create_error_object.restype = ctypes.c_void_p
+    lib.ngt_get_error_string.restype = ctypes.c_char_p
+    lib.ngt_get_error_string.argtypes = [ctypes.c_void_p]
+    getattr(lib, fn).restype = ctypes.c_void_p
+    getattr(lib, fn).argtypes = [ctypes.c_char_p, ctypes.c_void_p]
+    err = lib.ngt_create_error_object()
+    h = getattr(lib, fn)(path.encode(), ctypes.c_void_p(err))
+    return h, lib.ngt_get_error_string(ctypes.c_void_p(err)).decode()
+
+
+@pytest.mark.parametrize("damage", ["truncate_obj", "truncate_grp", "bad_edge", "missing_tre", "bad_prf"])
+def test_loader_rejects_damaged_index(lib, tmp_path, damage):
+    path, meta, _, _ = materialize("u8_l2", str(tmp_path))
+    if damage == "truncate_obj":
+        data = open(os.path.join(path, "obj"), "rb").read()
+        open(os.path.join(path, "obj"), "wb").write(data[:-100])
+    elif damage == "truncate_grp":
+        data = open(os.path.join(path, "grp"), "rb").read()
+        open(os.path.join(path, "grp"), "wb").write(data[: len(data) // 2])
+    elif damage == "bad_edge":
+        data = bytearray(open(os.path.join(path, "grp"), "rb").read())
+        # first '+' record after the 8-byte count and the dummy '-': count, then (id, dist) pairs
+        pos = 8 + 1 + 1 + 4
+        data[pos:pos + 4] = np.uint32(10 ** 9).tobytes()
+        open(os.path.join(path, "grp"), "wb").write(bytes(data))
+    elif damage == "missing_tre":
+        os.remove(os.path.join(path, "tre"))
+    elif damage == "bad_prf":
+        open(os.path.join(path, "prf"), "w").write("Dimension\tzero\n")
+    h, msg = _error_string(lib, "ngt_open_index_as_read_only", path)
+    assert h is None
+    assert msg.startswith("Capi : ngt_open_index_as_read_only() : Error:")
+    assert "CUDA" not in msg, msg
+
+
+def test_null_arguments_return_false_with_message(lib):
+    lib.ngt_create_error_object.restype = ctypes.c_void_p
+    lib.ngt_get_error_string.restype = ctypes.c_char_p
+    lib.ngt_get_error_string.argtypes = [ctypes.c_void_p]
+    lib.ngt_search_index_as_float.restype = ctypes.c_bool
+    lib.ngt_search_index_as_float.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_size_t,
+                                              ctypes.c_float, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p]
+    err = ctypes.c_void_p(lib.ngt_create_error_object())
+    ok = lib.ngt_search_index_as_float(None, None, 0, 10, 0.1, -1.0, None, err)
+    assert not ok
+    assert "parametor error" in lib.ngt_get_error_string(err).decode()
