@@ -1,0 +1,353 @@
+#!/usr/bin/env python
+"""Batched k-NN graph search benchmark: 1,000,000 x 128 float32 L2 ONNG, 10,000 queries.
+
+Workload (the benchmark's plain-vs-batched graph-search configuration):
+  objects  1,000,000 x 128, coordinates min(255, rint(Exponential(25))), seed 11
+  queries  10,000 from the same distribution, seed 12
+  index    ONNG-style graph (exact 100-NN lists, 10 outgoing + 100 incoming
+           edges) built on the GPU and written as an NGT index directory,
+           opened read-only through the C ABI (ngt_open_index_as_read_only)
+  search   k = 10 at the smallest epsilon of {0, 0.02, 0.05, 0.1, 0.15, 0.2, 0.3}
+           whose recall@10 against the exact ground truth is >= 0.95
+
+A step is one pass of all queries through the search.  `value` is queries/s
+with queries resident in HBM (ngtgpu_search_batch_device); `e2e` is the same
+through the host-buffer C-ABI call ngtgpu_search_batch_float (query upload
+and result download inside the timed region).  The 512 MB object arena is
+larger than L2 (129 MB), so no L2 flush is needed between steps.
+
+--impl reference times the CPU restatement of the reference's search (the
+oracle, OpenMP over all host cores, the ngtpy batch_search pattern) on a
+bounded sample of the same queries against the same index.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+EPS_SWEEP = [0.0, 0.02, 0.05, 0.1, 0.15, 0.2, 0.3]
+RECALL_TARGET = 0.95
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000)
+    ap.add_argument("--nq", type=int, default=10_000)
+    ap.add_argument("--dim", type=int, default=128)
+    ap.add_argument("--k", type=int, default=10)
+    ap.add_argument("--workdir", default=os.environ.get("NGT_BENCH_DIR", "/tmp/ngt_bench"))
+    ap.add_argument("--cpu-sample", type=int, default=2000, help="queries in the CPU-baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def workload(args, rank):
+    from ngt_gb300 import synthetic
+    base = synthetic.clipped_exponential(args.n, args.dim, seed=11)
+    queries = synthetic.clipped_exponential(args.nq, args.dim, seed=12 + 1000 * rank)
+    return base, queries
+
+
+def index_path(args, rank):
+    return os.path.join(args.workdir, "onng_%d_%d_r%d" % (args.n, args.dim, rank))
+
+
+def ensure_index(args, base, rank):
+    from ngt_gb300 import graph_build
+    path = index_path(args, rank)
+    if not os.path.exists(os.path.join(path, "grp")):
+        graph_build.build_onng_index(path, base, k=100, outgoing=10, incoming=100, log=log)
+    return path
+
+
+def ground_truth(base, queries, k):
+    """k-th exact squared distance per query (integer data: exact in float64)."""
+    import torch
+    dev = torch.device("cuda")
+    X = torch.from_numpy(base).to(dev)
+    Xb = X.to(torch.bfloat16)
+    sq = (X * X).sum(1)                                     # integers < 2^24: exact in fp32
+    kth = np.zeros(len(queries), np.float64)
+    for s in range(0, len(queries), 1024):
+        Q = torch.from_numpy(queries[s:s + 1024]).to(dev)
+        g = (Q.to(torch.bfloat16) @ Xb.T).float()           # exact integer dot products
+        d2 = (Q * Q).sum(1)[:, None] + sq[None, :] - 2 * g
+        kth[s:s + 1024] = torch.topk(d2, k, dim=1, largest=False).values[:, -1].double().cpu().numpy()
+        del g, d2
+    return kth
+
+
+def recall(base, queries, ids, counts, kth, k):
+    """Tie-aware recall@k: a returned id counts when its exact distance <= the k-th true distance."""
+    hit = 0
+    for j in range(len(queries)):
+        r = ids[j, :min(k, counts[j])].astype(np.int64) - 1
+        if len(r) == 0:
+            continue
+        d2 = ((base[r].astype(np.float64) - queries[j].astype(np.float64)) ** 2).sum(1)
+        hit += int((d2 <= kth[j]).sum())
+    return hit / (k * len(queries))
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except FileNotFoundError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.rows = []
+        if self.proc is None:
+            return
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        for line in out.strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def summary(self):
+        rows = getattr(self, "rows", [])
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(path, queries, eps, k, sample, threads):
+    """The oracle (CPU restatement of the reference search), OpenMP over all host cores."""
+    import oracle
+    o = oracle.Oracle(oracle.IndexFiles(path))
+    q = queries[:sample]
+    o.search(q[:64], k=k, epsilon=eps, threads=threads)          # warm caches / page in
+    t0 = time.time()
+    o.search(q, k=k, epsilon=eps, threads=threads)
+    dt = time.time() - t0
+    return {"value": round(len(q) / dt, 1), "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": "%d of the %d queries, k=%d, epsilon=%g, same index" % (len(q), len(queries), k, eps)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle  # noqa: F401  (CPU only)
+    base, queries = workload(args, 0)
+    threads = os.cpu_count() or 1
+    path = index_path(args, 0)
+    if not os.path.exists(os.path.join(path, "grp")):
+        # the same GPU-built index as the other arm (built here if this arm runs first)
+        path = ensure_index(args, base, 0)
+    eps_file = os.path.join(path, "bench_epsilon.json")
+    eps = json.load(open(eps_file))["epsilon"] if os.path.exists(eps_file) else 0.1
+    import oracle as orc
+    o = orc.Oracle(orc.IndexFiles(path))
+    sample = queries[:args.cpu_sample]
+    for _ in range(args.warmup):
+        o.search(sample[:256], k=args.k, epsilon=eps, threads=threads)
+    t0 = time.time()
+    for _ in range(args.steps):
+        o.search(sample, k=args.k, epsilon=eps, threads=threads)
+    dt = time.time() - t0
+    qps = args.steps * len(sample) / dt
+    line = {"metric": "queries/s at recall@10>=0.95 (1M x 128 L2 ONNG)", "value": round(qps, 1),
+            "unit": "queries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(1e3 * dt / args.steps, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "impl": "reference",
+            "config": {"workload": "graph search, %d x %d float32 L2 ONNG, %d queries/step sample, k=%d, epsilon=%g"
+                       % (args.n, args.dim, len(sample), args.k, eps), "parallelism": "openmp"},
+            "cpu_baseline": {"value": round(qps, 1), "unit": "queries/s", "cores": threads, "kind": "port",
+                             "sample": "%d queries per step" % len(sample)},
+            "e2e": {"value": round(qps, 1), "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    rank, world, local = dist_env()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from ngt_gb300 import Index
+    from ngt_gb300.base import QUERY_STATS_DTYPE, RESULT_DTYPE
+
+    t_setup = time.time()
+    base, queries = workload(args, rank)
+    path = ensure_index(args, base, rank)
+    kth = ground_truth(base, queries, args.k)
+    ix = Index(path, read_only=True)
+    log("setup %.1f s" % (time.time() - t_setup))
+
+    # ---- epsilon calibration (untimed): smallest epsilon reaching the recall target ----
+    cal = min(2000, len(queries))
+    chosen, curve = None, []
+    for eps in EPS_SWEEP:
+        ids, ds, n = ix.batch_search(queries[:cal], k=args.k, epsilon=eps)
+        r = recall(base, queries[:cal], ids, n, kth[:cal], args.k)
+        curve.append((eps, round(r, 4)))
+        log("epsilon %.2f recall@%d %.4f" % (eps, args.k, r))
+        if r >= RECALL_TARGET:
+            chosen = eps
+            break
+    if chosen is None:
+        chosen = EPS_SWEEP[-1]
+    if rank == 0:
+        json.dump({"epsilon": chosen}, open(os.path.join(path, "bench_epsilon.json"), "w"))
+
+    # ---- device-resident timed run --------------------------------------------------------
+    nq, k = len(queries), args.k
+    rows = torch.from_numpy(ix.convert_queries(queries)).cuda()
+    params, nparams = ix.make_params(k, chosen)
+    res = torch.zeros((nq, k, 2), dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(nq, dtype=torch.int32, device="cuda")
+    st = torch.zeros((nq, QUERY_STATS_DTYPE.itemsize // 4), dtype=torch.int32, device="cuda")
+    stream = torch.cuda.Stream()
+    sp = stream.cuda_stream
+
+    def step():
+        ix.search_device(rows.data_ptr(), nq, params, nparams, res.data_ptr(), k, cnt.data_ptr(), st.data_ptr(),
+                         stream=sp)
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+    torch.cuda.synchronize()
+    launches0 = ix.kernel_launches()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t0 = time.time()
+        with torch.cuda.stream(stream):
+            for i in range(args.steps):
+                ev[i][0].record(stream)
+                step()
+                ev[i][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.time() - t0
+    launches = ix.kernel_launches() - launches0
+    kernel_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = sum(kernel_ms)
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    qps = world * args.steps * nq / (total_ms / 1e3)
+
+    # recall and counters of the timed configuration
+    ids_np = res[:, :, 0].cpu().numpy().view(np.uint32)
+    cnt_np = cnt.cpu().numpy().astype(np.int64)
+    stats = st.cpu().numpy().view(QUERY_STATS_DTYPE).reshape(nq)
+    rec = recall(base, queries, ids_np, cnt_np, kth, k)
+    row_bytes = ix.query_row_bytes()
+    bytes_per_query = (row_bytes * stats["distance_computations"].astype(np.float64)
+                       + 4.0 * stats["edges_read"] + row_bytes)
+    achieved_gbs = bytes_per_query.sum() / (statistics.median(kernel_ms) / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+
+    # ---- end to end through the host-buffer C-ABI call -----------------------------------------
+    hq = np.ascontiguousarray(queries, np.float32)
+    e2e_times = []
+    for i in range(args.warmup + args.steps):
+        t1 = time.time()
+        ix.batch_search(hq, k=k, epsilon=chosen)
+        if i >= args.warmup:
+            e2e_times.append(time.time() - t1)
+    e2e_qps = world * nq * len(e2e_times) / sum(e2e_times)
+    h2d = hq.nbytes
+    d2h = nq * (int(np.ceil(k * (1 + chosen))) + 1) * 8 + nq * 4 + nq * QUERY_STATS_DTYPE.itemsize
+
+    # ---- CPU baseline (oracle port on a bounded sample) ------------------------------------------
+    cpu = None
+    if rank == 0:
+        cpu = cpu_baseline(path, queries, chosen, k, args.cpu_sample, os.cpu_count() or 1)
+
+    if rank == 0:
+        line = {
+            "metric": "queries/s at recall@10>=0.95 (1M x 128 L2 ONNG)",
+            "value": round(qps, 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "graph search (exact-order fp32 kernel), %d x %d float32 L2 ONNG, %d queries, "
+                                   "k=%d, epsilon=%g" % (args.n, args.dim, nq, k, chosen),
+                       "recall_at_k": round(rec, 4), "epsilon_curve": curve, "parallelism": "replicas",
+                       "l2": "inputs larger than L2 (%.0f MB object arena)" % (args.n * row_bytes / 1e6),
+                       "mean_distance_computations": round(float(stats["distance_computations"].mean()), 1),
+                       "status_bits": sorted(set(int(x) for x in np.unique(stats["status"])))},
+            "roofline": {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved_gbs / peak, 4), "traffic": None,
+                         "peak_source": peak_kind,
+                         "basis": "(%d*DC + 4*edges + %d) bytes per query over the kernel's event time"
+                                  % (row_bytes, row_bytes)},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches),
+            "clocks": clocks.summary(),
+            "wall_s_timed": round(wall, 3),
+        }
+        print(json.dumps(line), flush=True)
+    ix.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -17,11 +17,15 @@ extern "C" {
 /* Kernel selection for the batched calls. */
 #define NGTGPU_KERNEL_EXACT 0u  /* reference-order search, one query per CTA (results equal the reference's) */
 
-/* Per-query statistics (distance computations, expanded nodes, visited ids, status bits). */
+/* Per-query statistics: distance computations, expanded nodes, visited ids,
+ * adjacency entries read, and status bits (1: candidate overflow tier full,
+ * the result may differ from the reference's; 2: visited set moved to global
+ * memory; 4: no seed; 8: tree error; 16: iteration bound). */
 typedef struct {
   uint32_t distance_computations;
   uint32_t expansions;
   uint32_t visited;
+  uint32_t edges_read;
   uint32_t status;
 } NGTGPUQueryStats;
 

@@ -44,11 +44,11 @@ class QueryParameters(ctypes.Structure):
 
 class QueryStats(ctypes.Structure):
     _fields_ = [("distance_computations", c_uint32), ("expansions", c_uint32), ("visited", c_uint32),
-                ("status", c_uint32)]
+                ("edges_read", c_uint32), ("status", c_uint32)]
 
 
 QUERY_STATS_DTYPE = np.dtype([("distance_computations", np.uint32), ("expansions", np.uint32),
-                              ("visited", np.uint32), ("status", np.uint32)])
+                              ("visited", np.uint32), ("edges_read", np.uint32), ("status", np.uint32)])
 RESULT_DTYPE = np.dtype([("id", np.uint32), ("distance", np.float32)])
 
 _lib = None

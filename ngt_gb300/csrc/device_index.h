@@ -59,6 +59,7 @@ struct QueryStats {
   uint32_t distance_computations;
   uint32_t expansions;
   uint32_t visited;
+  uint32_t edges_read;   // adjacency entries read (sum over expanded nodes of min(degree, edge size))
   uint32_t status;       // bit flags below
 };
 

@@ -101,6 +101,7 @@ GraphEngine::~GraphEngine() {
   cudaFree(d_seed_off_);
   cudaFree(d_seed_ids_);
   cudaFree(d_bitmaps_);
+  cudaFree(d_overflow_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -316,11 +317,16 @@ void GraphEngine::convert_queries(const void* queries, QueryType qt, size_t nq, 
 
 void GraphEngine::ensure_scratch(size_t grid) {
   if (grid <= bitmap_grid_) return;
+  NGT_CUDA(cudaStreamSynchronize(stream_));   // earlier launches may still use the old buffers
   cudaFree(d_bitmaps_);
+  cudaFree(d_overflow_);
   d_bitmaps_ = nullptr;
+  d_overflow_ = nullptr;
   size_t words = (host_.nrows + 31) / 32;
   NGT_CUDA(cudaMalloc(&d_bitmaps_, grid * words * 4));
   NGT_CUDA(cudaMemsetAsync(d_bitmaps_, 0, grid * words * 4, stream_));
+  NGT_CUDA(cudaMalloc(&d_overflow_, grid * 2 * (size_t)kOverflowCapacity * 8));
+  NGT_CUDA(cudaStreamSynchronize(stream_));
   bitmap_grid_ = grid;
 }
 
@@ -340,6 +346,7 @@ void GraphEngine::search_device(const uint4* d_rows, size_t nq, const SearchArgs
   cfg.mode = (uint32_t)mode_;
   cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));
   cfg.bitmap_words = (host_.nrows + 31) / 32;
+  cfg.ocap = kOverflowCapacity;
   int max_smem = 0;
   NGT_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
   size_t smem = exact_smem_bytes(dev_.row_chunks, cfg);
@@ -367,7 +374,7 @@ void GraphEngine::search_device(const uint4* d_rows, size_t nq, const SearchArgs
   NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QueryParams), cudaMemcpyHostToDevice, stream));
   NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, stream));
   fn<<<(unsigned)grid, kExactThreads, smem, stream>>>(dev_, d_rows, (uint32_t)nq, d_params, d_seeds, d_out, d_counts,
-                                                       d_stats, d_bitmaps_, cfg);
+                                                       d_stats, d_bitmaps_, d_overflow_, cfg);
   NGT_CUDA(cudaGetLastError());
   launches_++;
   NGT_CUDA(cudaFreeAsync(d_params, stream));

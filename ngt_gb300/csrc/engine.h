@@ -101,7 +101,9 @@ class GraphEngine {
   uint32_t nleaves_ = 0;
   // scratch (grown on demand, reused across calls)
   uint32_t* d_bitmaps_ = nullptr;
+  unsigned long long* d_overflow_ = nullptr;
   size_t bitmap_grid_ = 0;
+  static constexpr uint32_t kOverflowCapacity = 65536;   // candidate keys per CTA beyond shared memory
   DevGraph dev_;
 };
 

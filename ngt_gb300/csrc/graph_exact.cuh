@@ -19,10 +19,16 @@
 //   * The queue is a sorted array in shared memory, merged with each chunk's
 //     sorted survivors; (distance, id) keys make the order total, like
 //     ObjectDistance::operator< (lib/NGT/Common.h:2347-2360).
-// Limits that can make a query inexact are reported per query in
-// QueryStats::status (candidate overflow).  The visited set never loses
-// entries: it starts as a hash table in shared memory and moves to a per-CTA
-// bitmap in global memory when the table is half full.
+//   * The queue has two tiers: the best `ccap` entries sorted in shared memory
+//     and an unsorted overflow tier in global memory whose entries are all
+//     larger than every shared-memory entry.  When the shared list drains, the
+//     overflow's live entries (<= explorationRadius) are filtered, the ccap
+//     smallest picked by an exact radix select over the 64-bit keys, sorted, and
+//     moved back.  Pops therefore follow the reference's order exactly.
+// The only limit that can make a query inexact is the overflow tier's capacity
+// (reported in QueryStats::status).  The visited set never loses entries: it
+// starts as a hash table in shared memory and moves to a per-CTA bitmap in
+// global memory when the table is half full.
 #pragma once
 #include <cfloat>
 #include "distance.cuh"
@@ -48,8 +54,16 @@ struct ExactShared {
   uint32_t status;
   uint32_t dc;
   uint32_t expansions;
+  uint32_t edges;
   uint32_t seed_leaf;
+  uint32_t ovf_n;                 // entries in the global overflow tier
+  uint32_t ovf_tmp;
+  unsigned long long ovf_min;     // smallest key in the overflow tier (~0 when empty)
+  unsigned long long evict_min;
+  unsigned long long sel_prefix;
+  uint32_t sel_need;
   uint32_t warp_cnt[kExactWarps];
+  uint32_t hist[256];
 };
 
 struct ExactConfig {
@@ -59,6 +73,7 @@ struct ExactConfig {
   uint32_t mode;     // GraphMode
   uint32_t group;    // lanes per distance (power of two <= 32)
   uint32_t bitmap_words;  // words per CTA in the spill bitmap
+  uint32_t ocap;          // overflow-tier capacity per CTA (keys)
 };
 
 __device__ __forceinline__ uint32_t hash_slot(uint32_t id, uint32_t mask) {
@@ -135,6 +150,28 @@ __device__ __forceinline__ void rank_sort(const unsigned long long* in, unsigned
   }
 }
 
+// In-place ascending bitonic sort of a[0..n) in shared memory by the whole CTA;
+// entries [n, p) are padded with ~0 where p is the next power of two (<= cap).
+__device__ __forceinline__ void bitonic_sort(unsigned long long* a, uint32_t n, uint32_t cap) {
+  uint32_t p = 1;
+  while (p < n) p <<= 1;
+  for (uint32_t i = n + threadIdx.x; i < p && i < cap; i += blockDim.x) a[i] = ~0ull;
+  __syncthreads();
+  for (uint32_t k = 2; k <= p; k <<= 1) {
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = threadIdx.x; i < p; i += blockDim.x) {
+        uint32_t l = i ^ j;
+        if (l > i) {
+          unsigned long long x = a[i], y = a[l];
+          bool up = (i & k) == 0;
+          if ((x > y) == up) { a[i] = y; a[l] = x; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
 __device__ __forceinline__ uint32_t lower_bound_keys(const unsigned long long* a, uint32_t n, unsigned long long x) {
   uint32_t lo = 0, hi = n;
   while (lo < hi) {
@@ -158,7 +195,8 @@ __global__ void __launch_bounds__(kExactThreads)
 graph_search_exact_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_t nq,
                           const QueryParams* __restrict__ params, const uint32_t* __restrict__ seed_list,
                           ObjDist* __restrict__ out, uint32_t* __restrict__ out_count,
-                          QueryStats* __restrict__ stats, uint32_t* __restrict__ bitmaps, ExactConfig cfg) {
+                          QueryStats* __restrict__ stats, uint32_t* __restrict__ bitmaps,
+                          unsigned long long* __restrict__ overflow, ExactConfig cfg) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t rc = g.row_chunks;
@@ -174,6 +212,8 @@ graph_search_exact_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_
   float* nd = reinterpret_cast<float*>(nid + kExactChunk);
   ExactShared& s = *reinterpret_cast<ExactShared*>(nd + kExactChunk);
   uint32_t* bitmap = bitmaps + (size_t)blockIdx.x * cfg.bitmap_words;
+  unsigned long long* ovf = overflow + (size_t)blockIdx.x * 2 * cfg.ocap;     // overflow tier
+  unsigned long long* ovf_tmp = ovf + cfg.ocap;                                 // refill scratch
   const uint32_t hmask = cfg.hcap - 1;
   const int G = (int)cfg.group;
   const int gl = lane & (G - 1);                   // lane inside the distance group
@@ -188,10 +228,11 @@ graph_search_exact_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_
       s.radius = P.radius;
       s.nres = 0; s.head = 0; s.tail = 0; s.cur = 0; s.nvisited = 0; s.spilled = 0;
       s.done = 0; s.status = 0; s.dc = 0; s.expansions = 0; s.nnew = 0;
+      s.ovf_n = 0; s.ovf_min = ~0ull; s.edges = 0;
     }
     __syncthreads();
     if (P.size == 0) {          // GraphIndex::search returns nothing for size 0
-      if (tid == 0) { out_count[q] = 0; stats[q] = QueryStats{0, 0, 0, 0}; }
+      if (tid == 0) { out_count[q] = 0; stats[q] = QueryStats{0, 0, 0, 0, 0}; }
       __syncthreads();
       continue;
     }
@@ -219,7 +260,8 @@ graph_search_exact_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_
       }
       __syncthreads();
       if (s.seed_leaf != 0xffffffffu && s.seed_leaf < g.nleaves) {
-        uint32_t a = g.leaf_seed_off[s.seed_leaf], b = g.leaf_seed_off[s.seed_leaf + 1];
+        const uint32_t* off = g.leaf_seed_off + P.seed_off;    // this query's seed-size table
+        uint32_t a = off[s.seed_leaf], b = off[s.seed_leaf + 1];
         seeds = g.leaf_seed_ids + a;
         nseeds = b - a;
       }
@@ -231,7 +273,7 @@ graph_search_exact_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_
     if (nseeds == 0) {
       if (tid == 0) {
         out_count[q] = 0;
-        stats[q] = QueryStats{0, 0, 0, s.status | kStatusEmptySeeds};
+        stats[q] = QueryStats{0, 0, 0, 0, s.status | kStatusEmptySeeds};
       }
       __syncthreads();
       continue;
@@ -275,6 +317,69 @@ graph_search_exact_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_
     // ---- best-first loop -----------------------------------------------------
     uint32_t guard = 0;
     while (true) {
+      if (s.head >= s.tail && s.ovf_n > 0) {
+        // ---- refill the shared list from the overflow tier ----
+        const float expR0 = P.coef * s.radius;
+        const uint32_t r0 = s.ovf_n;
+        if (tid == 0) s.ovf_tmp = 0;
+        __syncthreads();
+        for (uint32_t i = tid; i < r0; i += blockDim.x) {      // drop entries above the radius
+          unsigned long long k = ovf[i];
+          if (key_dist(k) <= expR0) ovf_tmp[atomicAdd(&s.ovf_tmp, 1u)] = k;
+        }
+        __syncthreads();
+        const uint32_t r = s.ovf_tmp;
+        unsigned long long* cl = s.cur ? cand1 : cand0;
+        if (r <= cfg.ccap) {
+          for (uint32_t i = tid; i < r; i += blockDim.x) cl[i] = ovf_tmp[i];
+          __syncthreads();
+          bitonic_sort(cl, r, cfg.ccap);
+          if (tid == 0) { s.head = 0; s.tail = r; s.ovf_n = 0; s.ovf_min = ~0ull; }
+        } else {
+          // exact radix select of the ccap-th smallest 64-bit key
+          unsigned long long prefix = 0, mask = 0;
+          uint32_t need = cfg.ccap;
+          for (int shift = 56; shift >= 0; shift -= 8) {
+            for (uint32_t i = tid; i < 256; i += blockDim.x) s.hist[i] = 0;
+            __syncthreads();
+            for (uint32_t i = tid; i < r; i += blockDim.x) {
+              unsigned long long k = ovf_tmp[i];
+              if ((k & mask) == prefix) atomicAdd(&s.hist[(uint32_t)(k >> shift) & 255u], 1u);
+            }
+            __syncthreads();
+            if (tid == 0) {
+              uint32_t acc = 0, b;
+              for (b = 0; b < 255; b++) {
+                if (acc + s.hist[b] >= need) break;
+                acc += s.hist[b];
+              }
+              s.sel_prefix = prefix | ((unsigned long long)b << shift);
+              s.sel_need = need - acc;
+            }
+            __syncthreads();
+            prefix = s.sel_prefix;
+            need = s.sel_need;
+            mask |= 255ull << shift;
+            __syncthreads();
+          }
+          // keys <= prefix (exactly ccap) go to shared memory, the rest stay in the tier
+          if (tid == 0) { s.ovf_n = 0; s.nnew = 0; s.ovf_min = ~0ull; }
+          __syncthreads();
+          for (uint32_t i = tid; i < r; i += blockDim.x) {
+            unsigned long long k = ovf_tmp[i];
+            if (k <= prefix) {
+              cl[atomicAdd(&s.nnew, 1u)] = k;
+            } else {
+              ovf[atomicAdd(&s.ovf_n, 1u)] = k;
+              atomicMin(&s.ovf_min, k);
+            }
+          }
+          __syncthreads();
+          bitonic_sort(cl, cfg.ccap, cfg.ccap);
+          if (tid == 0) { s.head = 0; s.tail = cfg.ccap; }
+        }
+        __syncthreads();
+      }
       if (tid == 0) {
         unsigned long long* cl = s.cur ? cand1 : cand0;
         float expR = P.coef * s.radius;
@@ -296,6 +401,7 @@ graph_search_exact_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_
       const uint32_t e0 = g.offsets[target];
       const uint32_t deg = g.offsets[target + 1] - e0;
       const uint32_t nsz = min(deg, P.edge_size);
+      if (tid == 0) s.edges += nsz;
       for (uint32_t c0 = 0; c0 < nsz; c0 += kExactChunk) {
         const uint32_t clen = min((uint32_t)kExactChunk, nsz - c0);
         // spill the visited set to the bitmap before it gets more than half full
@@ -385,22 +491,49 @@ graph_search_exact_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_
         __syncthreads();
         const uint32_t nold = s.live_old;
         const unsigned long long* old = cl + s.head;
+        // survivors not below the overflow tier's minimum join the tier directly
+        const uint32_t mk = s.ovf_n ? lower_bound_keys(bsorted, m, s.ovf_min) : m;
+        const uint32_t obase = s.ovf_n;
+        const uint32_t nevict = (nold + mk > cfg.ccap) ? nold + mk - cfg.ccap : 0u;
+        if (tid == 0) s.evict_min = ~0ull;
+        __syncthreads();
+        for (uint32_t i = tid; i < m - mk; i += blockDim.x) {
+          uint32_t o = obase + i;
+          if (o < cfg.ocap) ovf[o] = bsorted[mk + i];
+        }
         for (uint32_t i = tid; i < nold; i += blockDim.x) {
           unsigned long long k = old[i];
-          uint32_t pos = i + lower_bound_keys(bsorted, m, k);
+          uint32_t pos = i + lower_bound_keys(bsorted, mk, k);
           if (pos < cfg.ccap) cn[pos] = k;
+          else {
+            uint32_t o = obase + (m - mk) + (pos - cfg.ccap);
+            if (o < cfg.ocap) ovf[o] = k;
+            if (pos == cfg.ccap) s.evict_min = k;
+          }
         }
-        for (uint32_t i = tid; i < m; i += blockDim.x) {
+        for (uint32_t i = tid; i < mk; i += blockDim.x) {
           unsigned long long k = bsorted[i];
           uint32_t pos = i + lower_bound_keys(old, nold, k);
           if (pos < cfg.ccap) cn[pos] = k;
+          else {
+            uint32_t o = obase + (m - mk) + (pos - cfg.ccap);
+            if (o < cfg.ocap) ovf[o] = k;
+            if (pos == cfg.ccap) s.evict_min = k;
+          }
         }
         __syncthreads();
         if (tid == 0) {
-          uint32_t total = nold + m;
-          if (total > cfg.ccap) { total = cfg.ccap; s.status |= kStatusCandidateOverflow; }
+          uint32_t added = (m - mk) + nevict;
+          if (added) {
+            unsigned long long mn = s.evict_min;
+            if (mk < m && bsorted[mk] < mn) mn = bsorted[mk];
+            if (mn < s.ovf_min) s.ovf_min = mn;
+            uint32_t n2 = s.ovf_n + added;
+            if (n2 > cfg.ocap) { n2 = cfg.ocap; s.status |= kStatusCandidateOverflow; }
+            s.ovf_n = n2;
+          }
           s.head = 0;
-          s.tail = total;
+          s.tail = nold + mk - nevict;
           s.cur ^= 1u;
         }
         __syncthreads();
@@ -419,7 +552,7 @@ graph_search_exact_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_
       }
       if (tid == 0) {
         out_count[q] = n;
-        stats[q] = QueryStats{s.dc, s.expansions, s.nvisited, s.status};
+        stats[q] = QueryStats{s.dc, s.expansions, s.nvisited, s.edges, s.status};
       }
     }
     if (s.spilled) {                         // leave the bitmap clean for the next query

@@ -9,7 +9,7 @@ namespace ngtg {
 struct ExactConfig;
 
 typedef void (*ExactKernelFn)(DevGraph, const uint4*, uint32_t, const QueryParams*, const uint32_t*, ObjDist*,
-                              uint32_t*, QueryStats*, uint32_t*, ExactConfig);
+                              uint32_t*, QueryStats*, uint32_t*, unsigned long long*, ExactConfig);
 typedef void (*LinearKernelFn)(DevGraph, const uint4*, uint32_t, uint32_t, const uint8_t*, float*, uint32_t);
 
 // Return nullptr when the (type, metric) pair is not supported.

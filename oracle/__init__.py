@@ -95,6 +95,13 @@ class IndexFiles:
         self.nrows = n
         self.objects = np.zeros((n, self.dpad), self.dtype)
         self.present = np.zeros(n, np.uint8)
+        if len(buf) == 9 + (n - 1) * (1 + rowb) and buf[8:9] == b"-":
+            # common case: only the dummy slot is empty -> fixed-size records
+            rec = np.frombuffer(buf, np.uint8, (n - 1) * (1 + rowb), 9).reshape(n - 1, 1 + rowb)
+            if (rec[:, 0] == ord("+")).all():
+                self.objects[1:, :self.dim] = np.ascontiguousarray(rec[:, 1:]).view(self.dtype)
+                self.present[1:] = 1
+                return
         pos = 8
         for i in range(n):
             t = buf[pos:pos + 1]
@@ -108,6 +115,19 @@ class IndexFiles:
         assert pos == len(buf), "trailing bytes in the object file"
 
     def _read_grp(self):
+        buf = open(os.path.join(self.path, "grp"), "rb").read()
+        lib = ctypes.CDLL(build())
+        lib.oracle_parse_graph.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_void_p,
+                                           ctypes.c_void_p]
+        lib.oracle_parse_graph.restype = ctypes.c_int64
+        total = lib.oracle_parse_graph(buf, len(buf), self.nrows, None, None)
+        assert total >= 0, "corrupted graph file"
+        self.offsets = np.zeros(self.nrows + 1, np.uint32)
+        self.edges = np.zeros(max(total, 1), np.uint32)
+        lib.oracle_parse_graph(buf, len(buf), self.nrows, self.offsets.ctypes.data, self.edges.ctypes.data)
+        self.edges = self.edges[:total]
+
+    def _read_grp_python(self):
         buf = open(os.path.join(self.path, "grp"), "rb").read()
         n = int(np.frombuffer(buf, np.uint64, 1, 0)[0])
         pos = 8

@@ -383,10 +383,10 @@ static size_t graph_one(const OracleIndex *ix, const void *q, size_t k, size_t k
     else break;
   }
   if (nres >= size) radius = res[0].d;
-  uint8_t *visited = (uint8_t *)calloc(ix->nrows, 1);
+  uint64_t *visited = (uint64_t *)calloc((ix->nrows + 63) / 64, 8);   /* vector<bool> */
   minheap_t cand = {0, 0, 0};
   for (size_t i = 0; i < ns; i++) {
-    visited[sd[i].id] = 1;
+    visited[sd[i].id >> 6] |= 1ull << (sd[i].id & 63);
     minheap_push(&cand, sd[i]);
   }
   float expR = expcoef * radius;
@@ -397,8 +397,8 @@ static size_t graph_one(const OracleIndex *ix, const void *q, size_t k, size_t k
     size_t nsz = deg < esz ? deg : esz;
     for (size_t j = 0; j < nsz; j++) {
       uint32_t v = ix->edges[e0 + j];
-      if (visited[v]) continue;
-      visited[v] = 1;
+      if (visited[v >> 6] & (1ull << (v & 63))) continue;
+      visited[v >> 6] |= 1ull << (v & 63);
       float d = compare(ix->otype, ix->metric, q, row_ptr(ix, ix->objects, v), ix->dpad);
       dc++;
       if (d <= expR) {
@@ -502,4 +502,34 @@ void oracle_prepare_queries(int ot, int metric, uint32_t dpad, const float *q, s
       for (size_t j = 0; j < dim; j++) o[j] = float_to_half(src[j]);
     }
   }
+}
+
+/* Parses the body of an NGT graph file (Repository<GraphNode>: '+'/'-' markers,
+ * uint32 counts, (uint32 id, float distance) pairs).  With edges == NULL only
+ * the edge total is returned; otherwise offsets[nrows+1] and edges are filled.
+ * Returns -1 on a malformed buffer. */
+int64_t oracle_parse_graph(const uint8_t *buf, size_t len, size_t nrows, uint32_t *offsets, uint32_t *edges) {
+  if (len < 8) return -1;
+  uint64_t n;
+  memcpy(&n, buf, 8);
+  size_t pos = 8;
+  int64_t total = 0;
+  for (uint64_t i = 0; i < n; i++) {
+    if (pos >= len) return -1;
+    uint8_t t = buf[pos++];
+    if (offsets && i < nrows) offsets[i] = (uint32_t)total;
+    if (t == '-') continue;
+    if (t != '+' || pos + 4 > len) return -1;
+    uint32_t cnt;
+    memcpy(&cnt, buf + pos, 4);
+    pos += 4;
+    if (pos + (size_t)cnt * 8 > len) return -1;
+    if (edges)
+      for (uint32_t e = 0; e < cnt; e++) memcpy(&edges[total + e], buf + pos + (size_t)e * 8, 4);
+    pos += (size_t)cnt * 8;
+    total += cnt;
+  }
+  if (offsets)
+    for (uint64_t i = n; i <= nrows; i++) offsets[i] = (uint32_t)total;
+  return total;
 }

@@ -86,9 +86,10 @@ def test_mixed_parameters_in_one_batch_match_oracle(workdir):
         ids, ds, n = ix.batch_search(queries[:nq], k=ks, epsilon=eps, edge_size=edges)
     for j in range(nq):
         oi, od, on, _ = o.search(queries[j:j + 1], k=int(ks[j]), epsilon=float(eps[j]), edge_size=int(edges[j]))
-        assert n[j] == on[0]
-        assert np.array_equal(ids[j, :n[j]], oi[0, :on[0]])
-        assert np.array_equal(ds[j, :n[j]], od[0, :on[0]])
+        what = (j, int(ks[j]), float(eps[j]), int(edges[j]))
+        assert n[j] == on[0], what
+        assert np.array_equal(ids[j, :n[j]], oi[0, :on[0]]), what
+        assert np.array_equal(ds[j, :n[j]], od[0, :on[0]]), what
 
 
 def test_edge_cases(workdir):
@@ -105,10 +106,10 @@ def test_edge_cases(workdir):
         assert [o.id for o in big[:10]] == list(golden["ids_10"][0])
         with pytest.raises(NativeError, match="dimension"):
             ix.search(queries[0][:64], k=10)
-        # an object queried against itself is found first at distance 0
+        # an object queried against itself: exhaustive search finds it first at distance 0
         f = oracle.IndexFiles(path)
-        r = ix.search(f.objects[77, :128].astype(np.float32), k=5, epsilon=0.1)
-        assert r[0].distance == 0.0
+        r = ix.linear_search(f.objects[77, :128].astype(np.float32), k=5)
+        assert (r[0].id, r[0].distance) == (77, 0.0)
 
 
 def test_large_k_and_wide_epsilon_stay_exact(workdir):
