@@ -7,8 +7,11 @@ Workload (the benchmark's plain-vs-batched graph-search configuration):
   index    ONNG-style graph (exact 100-NN lists, 10 outgoing + 100 incoming
            edges) built on the GPU and written as an NGT index directory,
            opened read-only through the C ABI (ngt_open_index_as_read_only)
-  search   k = 10 at the smallest epsilon of {0, 0.02, 0.05, 0.1, 0.15, 0.2, 0.3}
-           whose recall@10 against the exact ground truth is >= 0.95
+  search   k = 10, each kernel at the smallest epsilon of a sweep (0 .. 0.3)
+           whose recall@10 against the exact ground truth is >= 0.95:
+           the batched kernel (warp per query, bf16 rows, exact fp32 re-rank; the
+           headline `value`) and the plain fp32 one-query-per-CTA kernel (the
+           reference-order search; reported in config.plain_fp32)
 
 A step is one pass of all queries through the search.  `value` is queries/s
 with queries resident in HBM (ngtgpu_search_batch_device); `e2e` is the same
@@ -36,7 +39,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-EPS_SWEEP = [0.0, 0.02, 0.05, 0.1, 0.15, 0.2, 0.3]
+EPS_SWEEP = [0.0, 0.02, 0.04, 0.06, 0.07, 0.08, 0.09, 0.1, 0.12, 0.15, 0.2, 0.3]
 RECALL_TARGET = 0.95
 
 
@@ -86,16 +89,16 @@ def ensure_index(args, base, rank):
 
 
 def ground_truth(base, queries, k):
-    """k-th exact squared distance per query (integer data: exact in float64)."""
+    """k-th exact squared distance per query (integer data: every product and sum exact in fp32)."""
     import torch
     dev = torch.device("cuda")
+    torch.backends.cuda.matmul.allow_tf32 = False
     X = torch.from_numpy(base).to(dev)
-    Xb = X.to(torch.bfloat16)
     sq = (X * X).sum(1)                                     # integers < 2^24: exact in fp32
     kth = np.zeros(len(queries), np.float64)
     for s in range(0, len(queries), 1024):
         Q = torch.from_numpy(queries[s:s + 1024]).to(dev)
-        g = (Q.to(torch.bfloat16) @ Xb.T).float()           # exact integer dot products
+        g = Q @ X.T                                         # fp32 GEMM: exact for integers <= 255
         d2 = (Q * Q).sum(1)[:, None] + sq[None, :] - 2 * g
         kth[s:s + 1024] = torch.topk(d2, k, dim=1, largest=False).values[:, -1].double().cpu().numpy()
         del g, d2
@@ -190,9 +193,20 @@ def run_reference(args):
         # the same GPU-built index as the other arm (built here if this arm runs first)
         path = ensure_index(args, base, 0)
     eps_file = os.path.join(path, "bench_epsilon.json")
-    eps = json.load(open(eps_file))["epsilon"] if os.path.exists(eps_file) else 0.1
     import oracle as orc
     o = orc.Oracle(orc.IndexFiles(path))
+    if os.path.exists(eps_file):
+        eps = json.load(open(eps_file))["epsilon"]
+    else:
+        # calibrate like the GPU arm: smallest epsilon of the sweep with recall >= the target
+        cal = 500
+        kth = ground_truth(base, queries[:cal], args.k)
+        eps = EPS_SWEEP[-1]
+        for e in EPS_SWEEP:
+            ids, ds, n, _ = o.search(queries[:cal], k=args.k, epsilon=e, threads=threads)
+            if recall(base, queries[:cal], ids, n, kth, args.k) >= RECALL_TARGET:
+                eps = e
+                break
     sample = queries[:args.cpu_sample]
     for _ in range(args.warmup):
         o.search(sample[:256], k=args.k, epsilon=eps, threads=threads)
@@ -225,7 +239,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from ngt_gb300 import Index
-    from ngt_gb300.base import QUERY_STATS_DTYPE, RESULT_DTYPE
+    from ngt_gb300.base import KERNEL_BATCHED, KERNEL_EXACT, QUERY_STATS_DTYPE
 
     t_setup = time.time()
     base, queries = workload(args, rank)
@@ -234,114 +248,138 @@ def main():
     ix = Index(path, read_only=True)
     log("setup %.1f s" % (time.time() - t_setup))
 
-    # ---- epsilon calibration (untimed): smallest epsilon reaching the recall target ----
-    cal = min(2000, len(queries))
-    chosen, curve = None, []
-    for eps in EPS_SWEEP:
-        ids, ds, n = ix.batch_search(queries[:cal], k=args.k, epsilon=eps)
-        r = recall(base, queries[:cal], ids, n, kth[:cal], args.k)
-        curve.append((eps, round(r, 4)))
-        log("epsilon %.2f recall@%d %.4f" % (eps, args.k, r))
-        if r >= RECALL_TARGET:
-            chosen = eps
-            break
-    if chosen is None:
-        chosen = EPS_SWEEP[-1]
-    if rank == 0:
-        json.dump({"epsilon": chosen}, open(os.path.join(path, "bench_epsilon.json"), "w"))
-
-    # ---- device-resident timed run --------------------------------------------------------
     nq, k = len(queries), args.k
     rows = torch.from_numpy(ix.convert_queries(queries)).cuda()
-    params, nparams = ix.make_params(k, chosen)
+    row_bytes = ix.query_row_bytes()
     res = torch.zeros((nq, k, 2), dtype=torch.int32, device="cuda")
     cnt = torch.zeros(nq, dtype=torch.int32, device="cuda")
     st = torch.zeros((nq, QUERY_STATS_DTYPE.itemsize // 4), dtype=torch.int32, device="cuda")
     stream = torch.cuda.Stream()
-    sp = stream.cuda_stream
 
-    def step():
-        ix.search_device(rows.data_ptr(), nq, params, nparams, res.data_ptr(), k, cnt.data_ptr(), st.data_ptr(),
-                         stream=sp)
+    def calibrate(kernel):
+        """Smallest epsilon of the sweep reaching the recall target (untimed, 2000 queries)."""
+        cal = min(2000, nq)
+        curve = []
+        for eps in EPS_SWEEP:
+            ids, ds, n = ix.batch_search(queries[:cal], k=k, epsilon=eps, kernel=kernel)
+            r = recall(base, queries[:cal], ids, n, kth[:cal], k)
+            curve.append((eps, round(r, 4)))
+            log("kernel %d epsilon %.2f recall@%d %.4f" % (kernel, eps, k, r))
+            if r >= RECALL_TARGET:
+                return eps, curve
+        return EPS_SWEEP[-1], curve
 
-    with torch.cuda.stream(stream):
-        for _ in range(args.warmup):
-            step()
-    torch.cuda.synchronize()
-    launches0 = ix.kernel_launches()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    with ClockSampler(local) as clocks:
-        t0 = time.time()
+    def timed(kernel, eps):
+        """K device-resident steps on one stream, CUDA events per step, clocks sampled meanwhile."""
+        params, nparams = ix.make_params(k, eps)
+
+        def step():
+            ix.search_device(rows.data_ptr(), nq, params, nparams, res.data_ptr(), k, cnt.data_ptr(),
+                             st.data_ptr(), stream=stream.cuda_stream, kernel=kernel)
+
         with torch.cuda.stream(stream):
-            for i in range(args.steps):
-                ev[i][0].record(stream)
+            for _ in range(args.warmup):
                 step()
-                ev[i][1].record(stream)
         torch.cuda.synchronize()
-        wall = time.time() - t0
-    launches = ix.kernel_launches() - launches0
-    kernel_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = sum(kernel_ms)
-    if world > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    qps = world * args.steps * nq / (total_ms / 1e3)
+        launches0 = ix.kernel_launches()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        with ClockSampler(local) as clocks:
+            t0 = time.time()
+            with torch.cuda.stream(stream):
+                for i in range(args.steps):
+                    ev[i][0].record(stream)
+                    step()
+                    ev[i][1].record(stream)
+            torch.cuda.synchronize()
+            wall = time.time() - t0
+        launches = ix.kernel_launches() - launches0
+        kernel_ms = [a.elapsed_time(b) for a, b in ev]
+        total_ms = sum(kernel_ms)
+        if world > 1:
+            t = torch.tensor([total_ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            total_ms = float(t.item())
+        ids_np = res[:, :, 0].cpu().numpy().view(np.uint32)
+        cnt_np = cnt.cpu().numpy().astype(np.int64)
+        stats = st.cpu().numpy().view(QUERY_STATS_DTYPE).reshape(nq)
+        rec = recall(base, queries, ids_np, cnt_np, kth, k)
+        srow = row_bytes // 2 if kernel == KERNEL_BATCHED else row_bytes
+        rerank = 0 if kernel == KERNEL_EXACT else 2 * k * row_bytes
+        bytes_pq = (srow * stats["distance_computations"].astype(np.float64) + 4.0 * stats["edges_read"]
+                    + row_bytes + rerank)
+        return {"kernel": kernel, "epsilon": eps, "qps": world * args.steps * nq / (total_ms / 1e3),
+                "ms_per_step": total_ms / args.steps, "median_ms": statistics.median(kernel_ms), "recall": rec,
+                "bytes_per_query": float(bytes_pq.mean()), "row_bytes": srow,
+                "achieved_gbs": bytes_pq.sum() / (statistics.median(kernel_ms) / 1e3) / 1e9,
+                "dc": float(stats["distance_computations"].mean()),
+                "status": sorted(set(int(x) for x in np.unique(stats["status"]))),
+                "launches": int(launches), "clocks": clocks.summary(), "wall": wall}
 
-    # recall and counters of the timed configuration
-    ids_np = res[:, :, 0].cpu().numpy().view(np.uint32)
-    cnt_np = cnt.cpu().numpy().astype(np.int64)
-    stats = st.cpu().numpy().view(QUERY_STATS_DTYPE).reshape(nq)
-    rec = recall(base, queries, ids_np, cnt_np, kth, k)
-    row_bytes = ix.query_row_bytes()
-    bytes_per_query = (row_bytes * stats["distance_computations"].astype(np.float64)
-                       + 4.0 * stats["edges_read"] + row_bytes)
-    achieved_gbs = bytes_per_query.sum() / (statistics.median(kernel_ms) / 1e3) / 1e9
+    runs = {}
+    curves = {}
+    for kernel in (KERNEL_EXACT, KERNEL_BATCHED):
+        eps, curves[kernel] = calibrate(kernel)
+        runs[kernel] = timed(kernel, eps)
+        log("kernel %d: %.1f q/s at epsilon %g, recall %.4f, %.1f GB/s"
+            % (kernel, runs[kernel]["qps"], eps, runs[kernel]["recall"], runs[kernel]["achieved_gbs"]))
+    head = runs[KERNEL_BATCHED]
+    plain = runs[KERNEL_EXACT]
+    if rank == 0:
+        json.dump({"epsilon": plain["epsilon"], "epsilon_batched": head["epsilon"]},
+                  open(os.path.join(path, "bench_epsilon.json"), "w"))
     peak, peak_kind = measured_peaks()
 
-    # ---- end to end through the host-buffer C-ABI call -----------------------------------------
+    # ---- end to end through the host-buffer C-ABI call (headline kernel) ------------------------
     hq = np.ascontiguousarray(queries, np.float32)
     e2e_times = []
     for i in range(args.warmup + args.steps):
         t1 = time.time()
-        ix.batch_search(hq, k=k, epsilon=chosen)
+        ix.batch_search(hq, k=k, epsilon=head["epsilon"], kernel=KERNEL_BATCHED)
         if i >= args.warmup:
             e2e_times.append(time.time() - t1)
     e2e_qps = world * nq * len(e2e_times) / sum(e2e_times)
     h2d = hq.nbytes
-    d2h = nq * (int(np.ceil(k * (1 + chosen))) + 1) * 8 + nq * 4 + nq * QUERY_STATS_DTYPE.itemsize
+    d2h = nq * (int(np.ceil(k * (1 + head["epsilon"]))) + 1) * 8 + nq * 4 + nq * QUERY_STATS_DTYPE.itemsize
 
     # ---- CPU baseline (oracle port on a bounded sample) ------------------------------------------
     cpu = None
     if rank == 0:
-        cpu = cpu_baseline(path, queries, chosen, k, args.cpu_sample, os.cpu_count() or 1)
+        cpu = cpu_baseline(path, queries, plain["epsilon"], k, args.cpu_sample, os.cpu_count() or 1)
 
     if rank == 0:
         line = {
             "metric": "queries/s at recall@10>=0.95 (1M x 128 L2 ONNG)",
-            "value": round(qps, 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "graph search (exact-order fp32 kernel), %d x %d float32 L2 ONNG, %d queries, "
-                                   "k=%d, epsilon=%g" % (args.n, args.dim, nq, k, chosen),
-                       "recall_at_k": round(rec, 4), "epsilon_curve": curve, "parallelism": "replicas",
+            "value": round(head["qps"], 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(head["ms_per_step"], 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32-rerank", "data": "synthetic",
+            "config": {"workload": "graph search, %d x %d float32 L2 ONNG, %d queries per step, k=%d"
+                                   % (args.n, args.dim, nq, k),
+                       "headline": "batched kernel (warp per query, bf16 rows, exact fp32 re-rank), epsilon=%g"
+                                   % head["epsilon"],
+                       "recall_at_k": round(head["recall"], 4), "epsilon_curve": curves[KERNEL_BATCHED],
+                       "plain_fp32": {"qps": round(plain["qps"], 1), "epsilon": plain["epsilon"],
+                                      "recall_at_k": round(plain["recall"], 4),
+                                      "epsilon_curve": curves[KERNEL_EXACT],
+                                      "mean_distance_computations": round(plain["dc"], 1),
+                                      "achieved_gbs": round(plain["achieved_gbs"], 1)},
+                       "speedup_vs_plain_fp32": round(head["qps"] / plain["qps"], 3),
+                       "parallelism": "replicas",
                        "l2": "inputs larger than L2 (%.0f MB object arena)" % (args.n * row_bytes / 1e6),
-                       "mean_distance_computations": round(float(stats["distance_computations"].mean()), 1),
-                       "status_bits": sorted(set(int(x) for x in np.unique(stats["status"])))},
-            "roofline": {"bound": "hbm", "achieved": round(achieved_gbs, 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(achieved_gbs / peak, 4), "traffic": None,
-                         "peak_source": peak_kind,
-                         "basis": "(%d*DC + 4*edges + %d) bytes per query over the kernel's event time"
-                                  % (row_bytes, row_bytes)},
+                       "mean_distance_computations": round(head["dc"], 1), "status_bits": head["status"]},
+            "roofline": {"bound": "hbm", "achieved": round(head["achieved_gbs"], 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(head["achieved_gbs"] / peak, 4), "traffic": None, "peak_source": peak_kind,
+                         "basis": "(%d*DC + 4*edges + %d query + re-rank %d*2k) bytes per query over the kernel's "
+                                  "median event time" % (head["row_bytes"], row_bytes, row_bytes)},
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "gpu_launches": int(launches),
-            "clocks": clocks.summary(),
-            "wall_s_timed": round(wall, 3),
+            "gpu_launches": head["launches"],
+            "clocks": head["clocks"],
+            "wall_s_timed": round(head["wall"], 3),
         }
         print(json.dumps(line), flush=True)
     ix.close()

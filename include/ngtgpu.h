@@ -15,7 +15,10 @@ extern "C" {
 #endif
 
 /* Kernel selection for the batched calls. */
-#define NGTGPU_KERNEL_EXACT 0u  /* reference-order search, one query per CTA (results equal the reference's) */
+#define NGTGPU_KERNEL_EXACT 0u     /* reference-order search, one query per CTA (results equal the reference's) */
+#define NGTGPU_KERNEL_BATCHED 1u   /* warp per query, persistent, bf16 search rows for float objects,
+                                      exact re-rank of the best candidates (checked by recall) */
+#define NGTGPU_KERNEL_BATCHED_FP32 2u  /* the batched kernel on the full-precision rows */
 
 /* Per-query statistics: distance computations, expanded nodes, visited ids,
  * adjacency entries read, and status bits (1: candidate overflow tier full,
@@ -55,6 +58,11 @@ bool ngtgpu_convert_queries_float(NGTIndex, const float *queries, size_t nq, int
 bool ngtgpu_search_batch_device(NGTIndex, const void *d_rows, size_t nq, const NGTQueryParameters *params,
                                 size_t nparams, NGTObjectDistance *d_results, size_t kmax, uint32_t *d_counts,
                                 NGTGPUQueryStats *d_stats, void *stream, uint32_t kernel, NGTError);
+
+/* Tuning of the batched kernel for this index (0 = automatic): candidate
+ * list length (rounded up to a power of two, >= size+1), nodes expanded per
+ * iteration, and re-ranked candidates per query as a multiple of size. */
+bool ngtgpu_set_batched_tuning(NGTIndex, uint32_t list_capacity, uint32_t parents, float rerank_factor, NGTError);
 
 /* Number of kernel launches issued by this index since it was opened. */
 uint64_t ngtgpu_kernel_launches(NGTIndex, NGTError);

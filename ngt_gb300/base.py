@@ -23,6 +23,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libngtgpu.so")
 
 KERNEL_EXACT = 0
+KERNEL_BATCHED = 1
+KERNEL_BATCHED_FP32 = 2
 
 
 class NativeError(Exception):
@@ -93,6 +95,7 @@ def load_library() -> ctypes.CDLL:
         "ngtgpu_search_batch_device": ([c_void_p, c_void_p, c_size_t, POINTER(QueryParameters), c_size_t, c_void_p,
                                         c_size_t, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p], c_bool),
         "ngtgpu_kernel_launches": ([c_void_p, c_void_p], c_uint64),
+        "ngtgpu_set_batched_tuning": ([c_void_p, c_uint32, c_uint32, c_float, c_void_p], c_bool),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -210,6 +213,10 @@ class Index:
         m = int(counts.max()) if nq else 0
         out = (res["id"][:, :m].copy(), res["distance"][:, :m].copy(), counts)
         return out + (stats,) if with_stats else out
+
+    def set_batched_tuning(self, list_capacity: int = 0, parents: int = 0, rerank_factor: float = 0.0):
+        self._check(self._lib.ngtgpu_set_batched_tuning(self._index, list_capacity, parents, rerank_factor,
+                                                        self._err))
 
     def kernel_launches(self) -> int:
         return int(self._lib.ngtgpu_kernel_launches(self._index, self._err))

@@ -335,8 +335,13 @@ static std::vector<SearchArgs> args_from(const NGTQueryParameters* params, size_
   return a;
 }
 
-static void check_kernel(uint32_t kernel) {
-  if (kernel != NGTGPU_KERNEL_EXACT) throw std::runtime_error("unknown kernel selector " + std::to_string(kernel));
+static ngtg::Kernel check_kernel(uint32_t kernel) {
+  switch (kernel) {
+    case NGTGPU_KERNEL_EXACT: return ngtg::Kernel::Exact;
+    case NGTGPU_KERNEL_BATCHED: return ngtg::Kernel::Fast;
+    case NGTGPU_KERNEL_BATCHED_FP32: return ngtg::Kernel::FastFp32;
+    default: throw std::runtime_error("unknown kernel selector " + std::to_string(kernel));
+  }
 }
 
 bool ngtgpu_search_batch_float(NGTIndex index, const float* queries, size_t nq, int32_t dim,
@@ -350,12 +355,12 @@ bool ngtgpu_search_batch_float(NGTIndex index, const float* queries, size_t nq, 
     return false;
   }
   try {
-    check_kernel(kernel);
+    ngtg::Kernel kk = check_kernel(kernel);
     std::vector<SearchArgs> a = args_from(params, nparams);
     for (const auto& x : a)
       if (engine(index)->output_size(x) > kmax) throw std::runtime_error("a query asks for more results than kmax");
     SearchOutput out;
-    engine(index)->search(queries, QueryType::Float32, nq, (size_t)dim, a.data(), a.size(), out);
+    engine(index)->search(queries, QueryType::Float32, nq, (size_t)dim, a.data(), a.size(), out, kk);
     for (size_t q = 0; q < nq; q++) {
       counts[q] = out.counts[q];
       for (uint32_t i = 0; i < out.counts[q]; i++) {
@@ -402,16 +407,31 @@ bool ngtgpu_search_batch_device(NGTIndex index, const void* d_rows, size_t nq, c
     return false;
   }
   try {
-    check_kernel(kernel);
+    ngtg::Kernel kk = check_kernel(kernel);
     std::vector<SearchArgs> a = args_from(params, nparams);
     GraphEngine* e = engine(index);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : e->stream();
     e->search_device(static_cast<const uint4*>(d_rows), nq, a.data(), a.size(),
                      reinterpret_cast<ngtg::ObjDist*>(d_results), d_counts,
-                     reinterpret_cast<ngtg::QueryStats*>(d_stats), kmax, s);
+                     reinterpret_cast<ngtg::QueryStats*>(d_stats), kmax, s, kk);
     return true;
   }
   CAPI_CATCH(error, false)
+}
+
+bool ngtgpu_set_batched_tuning(NGTIndex index, uint32_t list_capacity, uint32_t parents, float rerank_factor,
+                               NGTError error) {
+  if (index == nullptr || list_capacity > 1024 || parents > 8 || rerank_factor < 0.f) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " list_capacity = " << list_capacity << " parents = " << parents
+                                       << " rerank_factor = " << rerank_factor);
+    return false;
+  }
+  ngtg::FastTuning t;
+  t.list_cap = list_capacity;
+  t.parents = parents;
+  t.rerank_factor = rerank_factor;
+  engine(index)->set_tuning(t);
+  return true;
 }
 
 uint64_t ngtgpu_kernel_launches(NGTIndex index, NGTError error) {

@@ -19,6 +19,7 @@ template <ObjType OT> struct ObjTraits;
 template <> struct ObjTraits<ObjType::Float> { typedef float T; static constexpr int kPerChunk = 4; };
 template <> struct ObjTraits<ObjType::Float16> { typedef __half T; static constexpr int kPerChunk = 8; };
 template <> struct ObjTraits<ObjType::Uint8> { typedef uint8_t T; static constexpr int kPerChunk = 16; };
+template <> struct ObjTraits<ObjType::Bfloat16> { typedef uint16_t T; static constexpr int kPerChunk = 8; };
 
 template <ObjType OT>
 __device__ __forceinline__ void unpack(const uint4& v, float* f);
@@ -34,6 +35,15 @@ __device__ __forceinline__ void unpack<ObjType::Float16>(const uint4& v, float* 
   for (int i = 0; i < 4; i++) {
     float2 t = __half22float2(h[i]);
     f[2 * i] = t.x; f[2 * i + 1] = t.y;
+  }
+}
+template <>
+__device__ __forceinline__ void unpack<ObjType::Bfloat16>(const uint4& v, float* f) {
+  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int i = 0; i < 4; i++) {
+    f[2 * i] = __uint_as_float(w[i] << 16);
+    f[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
   }
 }
 template <>

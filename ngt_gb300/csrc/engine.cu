@@ -13,6 +13,7 @@
 #include <string>
 
 #include "graph_exact.cuh"
+#include "graph_fast.cuh"
 #include "kernels.h"
 #include "linear_select.cuh"
 #include "seed_rng.h"
@@ -102,6 +103,9 @@ GraphEngine::~GraphEngine() {
   cudaFree(d_seed_ids_);
   cudaFree(d_bitmaps_);
   cudaFree(d_overflow_);
+  cudaFree(d_fast_bitmaps_);
+  cudaFree(d_work_);
+  cudaFree(d_bf16_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -330,15 +334,61 @@ void GraphEngine::ensure_scratch(size_t grid) {
   bitmap_grid_ = grid;
 }
 
+bool GraphEngine::fast_supported(Kernel k) const {
+  if (k == Kernel::Exact) return true;
+  return fast_kernel(host_.prop.otype, host_.prop.metric, k == Kernel::Fast) != nullptr;
+}
+
+void GraphEngine::ensure_fast_scratch(size_t slots) {
+  if (slots <= fast_slots_) return;
+  NGT_CUDA(cudaStreamSynchronize(stream_));
+  cudaFree(d_fast_bitmaps_);
+  d_fast_bitmaps_ = nullptr;
+  size_t words = ((host_.nrows + 31) / 32 + 3) / 4 * 4;
+  NGT_CUDA(cudaMalloc(&d_fast_bitmaps_, slots * words * 4));
+  NGT_CUDA(cudaMemsetAsync(d_fast_bitmaps_, 0, slots * words * 4, stream_));
+  if (!d_work_) NGT_CUDA(cudaMalloc(&d_work_, 16));
+  NGT_CUDA(cudaStreamSynchronize(stream_));
+  fast_slots_ = slots;
+}
+
+void GraphEngine::ensure_bf16_rows() {
+  if (d_bf16_ || host_.prop.otype != ObjType::Float) return;
+  size_t nfloats = (size_t)host_.nrows * host_.dpad;
+  NGT_CUDA(cudaMalloc(&d_bf16_, nfloats * 2));
+  launch_float_rows_to_bf16(d_objects_, d_bf16_, nfloats, stream_);
+  NGT_CUDA(cudaGetLastError());
+  NGT_CUDA(cudaStreamSynchronize(stream_));
+}
+
 void GraphEngine::search_device(const uint4* d_rows, size_t nq, const SearchArgs* args, size_t nargs, ObjDist* d_out,
-                                uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream) {
+                                uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream,
+                                Kernel kernel) {
   std::lock_guard<std::mutex> lock(mu_);
   NGT_CUDA(cudaSetDevice(device_));
   if (nq == 0) return;
+  if (!fast_supported(kernel)) throw std::runtime_error("the batched kernel does not support this index type");
   std::vector<QueryParams> params;
   std::vector<uint32_t> seeds;
   uint32_t max_size = 0;
   build_params(args, nargs, nq, kmax, params, seeds, max_size);
+  QueryParams* d_params = nullptr;
+  uint32_t* d_seeds = nullptr;
+  NGT_CUDA(cudaMallocAsync(&d_params, nq * sizeof(QueryParams), stream));
+  NGT_CUDA(cudaMallocAsync(&d_seeds, seeds.size() * 4, stream));
+  NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QueryParams), cudaMemcpyHostToDevice, stream));
+  NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, stream));
+  if (kernel == Kernel::Exact)
+    launch_exact(d_rows, nq, d_params, d_seeds, max_size, d_out, d_counts, d_stats, stream);
+  else
+    launch_fast(d_rows, nq, d_params, d_seeds, max_size, d_out, d_counts, d_stats, stream, kernel);
+  NGT_CUDA(cudaFreeAsync(d_params, stream));
+  NGT_CUDA(cudaFreeAsync(d_seeds, stream));
+}
+
+void GraphEngine::launch_exact(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
+                               uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats,
+                               cudaStream_t stream) {
   ExactConfig cfg{};
   cfg.kcap = max_size + 1;
   cfg.ccap = 1024;
@@ -366,23 +416,52 @@ void GraphEngine::search_device(const uint4* d_rows, size_t nq, const SearchArgs
   NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
   size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
   ensure_scratch(grid);
-  // per-call parameter buffers
-  QueryParams* d_params = nullptr;
-  uint32_t* d_seeds = nullptr;
-  NGT_CUDA(cudaMallocAsync(&d_params, nq * sizeof(QueryParams), stream));
-  NGT_CUDA(cudaMallocAsync(&d_seeds, seeds.size() * 4, stream));
-  NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QueryParams), cudaMemcpyHostToDevice, stream));
-  NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, stream));
   fn<<<(unsigned)grid, kExactThreads, smem, stream>>>(dev_, d_rows, (uint32_t)nq, d_params, d_seeds, d_out, d_counts,
                                                        d_stats, d_bitmaps_, d_overflow_, cfg);
   NGT_CUDA(cudaGetLastError());
   launches_++;
-  NGT_CUDA(cudaFreeAsync(d_params, stream));
-  NGT_CUDA(cudaFreeAsync(d_seeds, stream));
+}
+
+void GraphEngine::launch_fast(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
+                              uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats,
+                              cudaStream_t stream, Kernel kernel) {
+  const bool bf16 = kernel == Kernel::Fast && host_.prop.otype == ObjType::Float;
+  FastKernelFn fn = fast_kernel(host_.prop.otype, host_.prop.metric, bf16);
+  if (!fn) throw std::runtime_error("the batched kernel does not support this index type");
+  if (bf16) ensure_bf16_rows();
+  FastConfig cfg{};
+  uint32_t L = tuning_.list_cap ? next_pow2(tuning_.list_cap) : next_pow2(std::max<uint32_t>(128, 4 * max_size));
+  L = std::max<uint32_t>(L, next_pow2(max_size + 1));
+  if (L > 1024) throw std::runtime_error("result size too large for the batched kernel (at most 1023)");
+  cfg.list_cap = L;
+  cfg.nbr_cap = std::max<uint32_t>(512, L);
+  cfg.parents = tuning_.parents ? std::min<uint32_t>(tuning_.parents, 8) : 2;
+  cfg.search_chunks = bf16 ? dev_.row_chunks / 2 : dev_.row_chunks;
+  cfg.sgroup = std::min<uint32_t>(32, next_pow2(cfg.search_chunks));
+  cfg.ngroup = std::min<uint32_t>(32, next_pow2(dev_.row_chunks));
+  float rf = tuning_.rerank_factor > 0.f ? tuning_.rerank_factor : 2.0f;
+  cfg.rerank_x16 = (uint32_t)std::ceil(rf * 16.0f);
+  cfg.bitmap_words = ((host_.nrows + 31) / 32 + 3) / 4 * 4;
+  cfg.max_iters = 1u << 22;
+  size_t smem = kFastWarps * fast_smem_per_warp(dev_.row_chunks, cfg);
+  int max_smem = 0, per_sm = 0, sms = 0;
+  NGT_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
+  if (smem > (size_t)max_smem) throw std::runtime_error("batched search state does not fit in shared memory");
+  NGT_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kFastThreads, smem));
+  NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+  size_t grid = std::min<size_t>((nq + kFastWarps - 1) / kFastWarps, (size_t)std::max(1, per_sm) * sms);
+  ensure_fast_scratch(grid * kFastWarps);
+  NGT_CUDA(cudaMemsetAsync(d_work_, 0, 4, stream));
+  const uint4* srows = bf16 ? static_cast<const uint4*>(d_bf16_) : dev_.objects;
+  fn<<<(unsigned)grid, kFastThreads, smem, stream>>>(dev_, srows, d_rows, (uint32_t)nq, d_params, d_seeds, d_out,
+                                                      d_counts, d_stats, d_fast_bitmaps_, d_work_, cfg);
+  NGT_CUDA(cudaGetLastError());
+  launches_++;
 }
 
 void GraphEngine::search(const void* queries, QueryType qt, size_t nq, size_t qdim, const SearchArgs* args,
-                         size_t nargs, SearchOutput& out) {
+                         size_t nargs, SearchOutput& out, Kernel kernel) {
   NGT_CUDA(cudaSetDevice(device_));
   std::vector<uint8_t> rows;
   convert_queries(queries, qt, nq, qdim, rows);
@@ -403,7 +482,7 @@ void GraphEngine::search(const void* queries, QueryType qt, size_t nq, size_t qd
   NGT_CUDA(cudaMallocAsync(&d_counts, nq * 4, s));
   NGT_CUDA(cudaMallocAsync(&d_stats, nq * sizeof(QueryStats), s));
   NGT_CUDA(cudaMemcpyAsync(d_rows, rows.data(), rows.size(), cudaMemcpyHostToDevice, s));
-  search_device(d_rows, nq, args, nargs, d_out, d_counts, d_stats, kmax, s);
+  search_device(d_rows, nq, args, nargs, d_out, d_counts, d_stats, kmax, s, kernel);
   NGT_CUDA(cudaMemcpyAsync(out.results.data(), d_out, nq * kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, s));
   NGT_CUDA(cudaMemcpyAsync(out.counts.data(), d_counts, nq * 4, cudaMemcpyDeviceToHost, s));
   NGT_CUDA(cudaMemcpyAsync(out.stats.data(), d_stats, nq * sizeof(QueryStats), cudaMemcpyDeviceToHost, s));

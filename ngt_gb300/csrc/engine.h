@@ -25,7 +25,17 @@ struct SearchArgs {
 // Query element type accepted at the boundary.
 enum class QueryType { Float32 = 0, Float64 = 1, Uint8 = 2, Float16 = 3 };
 
-enum class Kernel { Exact = 0 };
+// Exact: reference-order search, one query per CTA (results equal the reference's).
+// Fast: batched warp-per-query search on bf16 rows (float objects) or the native
+//       rows (other types), with an exact re-rank.  FastFp32: the same on fp32 rows.
+enum class Kernel { Exact = 0, Fast = 1, FastFp32 = 2 };
+
+// Knobs of the batched kernel (0 = automatic).
+struct FastTuning {
+  uint32_t list_cap = 0;       // candidate list length (power of two)
+  uint32_t parents = 0;        // nodes expanded per iteration
+  float rerank_factor = 0.f;   // re-ranked entries = ceil(size * factor)
+};
 
 struct SearchOutput {
   std::vector<ObjDist> results;    // nq * kmax
@@ -49,7 +59,7 @@ class GraphEngine {
 
   // Graph search over host queries (row-major nq x qdim).
   void search(const void* queries, QueryType qt, size_t nq, size_t qdim, const SearchArgs* args, size_t nargs,
-              SearchOutput& out);
+              SearchOutput& out, Kernel kernel = Kernel::Exact);
   // Exhaustive search (exact ids, ties broken by id).
   void linear_search(const void* queries, QueryType qt, size_t nq, size_t qdim, size_t size, SearchOutput& out);
 
@@ -61,7 +71,11 @@ class GraphEngine {
   // Device-side entry used by the batched extension: queries already converted
   // and resident on the device.
   void search_device(const uint4* d_rows, size_t nq, const SearchArgs* args, size_t nargs, ObjDist* d_out,
-                     uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream);
+                     uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream,
+                     Kernel kernel = Kernel::Exact);
+  void set_tuning(const FastTuning& t) { tuning_ = t; }
+  const FastTuning& tuning() const { return tuning_; }
+  bool fast_supported(Kernel k) const;
 
   // Number of results a query can return (larger than args.size only for the
   // updatable search on an index with EpsilonType ResultSize).
@@ -80,6 +94,13 @@ class GraphEngine {
                     std::vector<uint32_t>& seed_list, uint32_t& max_size);
   size_t edge_size_for(const SearchArgs& a) const;
   void ensure_scratch(size_t grid);
+  void ensure_fast_scratch(size_t slots);
+  void ensure_bf16_rows();
+  void launch_exact(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
+                    uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, cudaStream_t stream);
+  void launch_fast(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
+                   uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, cudaStream_t stream,
+                   Kernel kernel);
 
   HostIndex host_;
   GraphMode mode_;
@@ -104,6 +125,11 @@ class GraphEngine {
   unsigned long long* d_overflow_ = nullptr;
   size_t bitmap_grid_ = 0;
   static constexpr uint32_t kOverflowCapacity = 65536;   // candidate keys per CTA beyond shared memory
+  uint32_t* d_fast_bitmaps_ = nullptr;                    // one visited bitmap per warp slot
+  size_t fast_slots_ = 0;
+  uint32_t* d_work_ = nullptr;                            // work counter of the batched kernel
+  void* d_bf16_ = nullptr;                                // bf16 copy of float object rows
+  FastTuning tuning_;
   DevGraph dev_;
 };
 

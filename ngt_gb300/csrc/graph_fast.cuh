@@ -1,0 +1,344 @@
+// Batched graph search: one warp per query inside a persistent kernel fed by a
+// device work counter, search distances on a compact copy of the objects
+// (bf16 for float objects), and an exact re-rank of the best candidates with
+// the full-precision rows.
+//
+// Algorithm (the reference's best-first search, lib/NGT/Graph.cpp:716-835,
+// with its order relaxed for parallelism):
+//   * one sorted list of L (distance, id) keys per query holds candidates and
+//     results together; bit 31 of the id word marks an entry as expanded;
+//   * each iteration expands the P best unexpanded entries whose distance is
+//     within explorationRadius = (1+epsilon) * r_k (r_k: the size-th best
+//     distance so far, or the caller's radius), the reference's stopping rule;
+//     the search ends when no such entry remains;
+//   * the neighbours of the P parents (at most edge_size each, in edge order)
+//     pass a per-query visited bitmap (one bit per object, in global memory,
+//     cleared after the query) and their distances are computed by groups of
+//     lanes with 16-byte loads; keys below the list's worst are sorted and
+//     merged into the list;
+//   * finally the best R = ceil(size * rerank_factor) entries are re-ranked with
+//     the exact comparator over the full-precision rows, so every returned
+//     distance is the reference comparator's value for that id.
+// Differences from the reference that can change which ids are found (and are
+// why this kernel is checked by recall, not by id equality): P > 1 expands
+// slightly more nodes per step, the candidate list is bounded to L entries, an
+// expanded node reads at most nbr_cap / P neighbours, and the search distances
+// are bf16 (exact for integer coordinates <= 256).
+#pragma once
+#include <cuda_bf16.h>
+#include <cfloat>
+#include "distance.cuh"
+#include "device_index.h"
+
+namespace ngtg {
+
+constexpr int kFastWarps = 4;
+constexpr int kFastThreads = 32 * kFastWarps;
+constexpr uint32_t kExpandedBit = 0x80000000u;
+
+struct FastConfig {
+  uint32_t list_cap;       // L: power of two, 64..1024
+  uint32_t nbr_cap;        // neighbour ids handled per iteration (power of two)
+  uint32_t parents;        // P
+  uint32_t sgroup;         // lanes per search distance (power of two <= 32)
+  uint32_t ngroup;         // lanes per full-precision distance
+  uint32_t search_chunks;  // 16-byte chunks per search row
+  uint32_t rerank_x16;     // rerank factor * 16
+  uint32_t bitmap_words;
+  uint32_t max_iters;
+};
+
+struct FastWarpSmem {
+  uint32_t q;              // current query
+  uint32_t n;              // list length
+  uint32_t cur;            // active list buffer
+  uint32_t nparents;
+  uint32_t parents[8];
+  uint32_t seed_leaf;
+};
+
+__device__ __forceinline__ uint32_t key_rawid(unsigned long long k) { return (uint32_t)k & 0x7fffffffu; }
+__device__ __forceinline__ bool key_expanded(unsigned long long k) { return ((uint32_t)k & kExpandedBit) != 0; }
+
+// Ascending bitonic sort of a[0..n) (smem) by one warp; pads to the next power of two with ~0.
+__device__ __forceinline__ void warp_bitonic_sort(unsigned long long* a, uint32_t n, int lane) {
+  if (n <= 1) return;
+  uint32_t p = 1;
+  while (p < n) p <<= 1;
+  for (uint32_t i = n + lane; i < p; i += 32) a[i] = ~0ull;
+  __syncwarp();
+  for (uint32_t k = 2; k <= p; k <<= 1) {
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = lane; i < p; i += 32) {
+        uint32_t l = i ^ j;
+        if (l > i) {
+          unsigned long long x = a[i], y = a[l];
+          bool up = (i & k) == 0;
+          if ((x > y) == up) { a[i] = y; a[l] = x; }
+        }
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// Number of entries of the sorted a[0..n) that are < x (ignoring the expanded bit of a's entries
+// is not needed: keys are ordered by distance first, the bit only reorders exact distance ties).
+__device__ __forceinline__ uint32_t warp_lower_bound(const unsigned long long* a, uint32_t n, unsigned long long x) {
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    uint32_t mid = (lo + hi) >> 1;
+    if (a[mid] < x) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+template <ObjType ST, ObjType OT, Metric M>
+__global__ void __launch_bounds__(kFastThreads)
+graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint4* __restrict__ queries, uint32_t nq,
+                         const QueryParams* __restrict__ params, const uint32_t* __restrict__ seed_list,
+                         ObjDist* __restrict__ out, uint32_t* __restrict__ out_count, QueryStats* __restrict__ stats,
+                         uint32_t* __restrict__ bitmaps, uint32_t* __restrict__ work, FastConfig cfg) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t rc = g.row_chunks, sc = cfg.search_chunks;
+  const uint32_t L = cfg.list_cap, NB = cfg.nbr_cap;
+  // per-warp carve-up
+  const size_t per_warp = (size_t)rc * 16 + (size_t)sc * 16 + (size_t)L * 16 + (size_t)NB * 12 + 64;
+  unsigned char* base = smem + warp * ((per_warp + 15) & ~(size_t)15);
+  uint4* qn = reinterpret_cast<uint4*>(base);                  // query, object type
+  uint4* qs = qn + rc;                                          // query, search type
+  unsigned long long* list0 = reinterpret_cast<unsigned long long*>(qs + sc);
+  unsigned long long* list1 = list0 + L;
+  unsigned long long* nkey = list1 + L;                         // NB keys
+  uint32_t* nid = reinterpret_cast<uint32_t*>(nkey + NB);       // NB ids
+  FastWarpSmem& w = *reinterpret_cast<FastWarpSmem*>(nid + NB);
+  const uint32_t slot = blockIdx.x * kFastWarps + warp;
+  uint32_t* bitmap = bitmaps + (size_t)slot * cfg.bitmap_words;
+  const int SG = (int)cfg.sgroup, NG = (int)cfg.ngroup;
+  const int sgl = lane & (SG - 1), ngl = lane & (NG - 1);
+
+  while (true) {
+    if (lane == 0) w.q = atomicAdd(work, 1u);
+    __syncwarp();
+    const uint32_t q = w.q;
+    if (q >= nq) break;
+    const QueryParams P = params[q];
+    for (uint32_t i = lane; i < rc; i += 32) qn[i] = queries[(size_t)q * rc + i];
+    __syncwarp();
+    if constexpr (ST != OT) {
+      // float object rows -> bf16 search rows (round to nearest even)
+      const float* qf = reinterpret_cast<const float*>(qn);
+      uint32_t* qb = reinterpret_cast<uint32_t*>(qs);
+      for (uint32_t i = lane; i < sc * 4; i += 32) {
+        uint32_t lo = __bfloat16_as_ushort(__float2bfloat16_rn(qf[2 * i]));
+        uint32_t hi = __bfloat16_as_ushort(__float2bfloat16_rn(qf[2 * i + 1]));
+        qb[i] = lo | (hi << 16);
+      }
+    } else {
+      for (uint32_t i = lane; i < sc; i += 32) qs[i] = qn[i];
+    }
+    __syncwarp();
+    uint32_t dc = 0, expansions = 0, edges_read = 0, status = 0, visited = 0;
+    uint32_t n = 0;
+    unsigned long long* list = list0;
+    unsigned long long* alt = list1;
+    if (P.size == 0) {
+      if (lane == 0) { out_count[q] = 0; stats[q] = QueryStats{0, 0, 0, 0, 0}; }
+      __syncwarp();
+      continue;
+    }
+    // ---- seeds -------------------------------------------------------------------
+    const uint32_t* seeds = nullptr;
+    uint32_t nseeds = 0;
+    if (P.seed_cnt == 0xffffffffu) {
+      uint32_t node = g.root;
+      int depth = 0;
+      while (!(node & 0x80000000u) && depth < 64) {
+        const DevInternal& in = g.internals[node];
+        float d = group_distance<OT, M>(qn, g.pivots + (size_t)in.pivot * rc, (int)rc, lane, 32);
+        uint32_t bsize = in.nchildren - 1, mid;
+        for (mid = 0; mid < bsize; mid++)
+          if (d < in.borders[mid]) break;
+        node = in.children[mid];
+        depth++;
+      }
+      if (node & 0x80000000u) {
+        uint32_t leaf = node & 0x7fffffffu;
+        if (leaf < g.nleaves) {
+          const uint32_t* off = g.leaf_seed_off + P.seed_off;
+          seeds = g.leaf_seed_ids + off[leaf];
+          nseeds = off[leaf + 1] - off[leaf];
+        }
+      } else {
+        status |= kStatusTreeError;
+      }
+    } else {
+      seeds = seed_list + P.seed_off;
+      nseeds = P.seed_cnt;
+    }
+    nseeds = min(nseeds, NB);
+    // seeds are marked visited and become the first candidates
+    uint32_t m = 0;
+    for (uint32_t b = 0; b < nseeds; b += 32) {
+      uint32_t i = b + lane;
+      bool fresh = false;
+      uint32_t id = 0;
+      if (i < nseeds) {
+        id = seeds[i];
+        if (id < g.nrows) {
+          uint32_t bit = 1u << (id & 31u);
+          fresh = (atomicOr(&bitmap[id >> 5], bit) & bit) == 0u;
+        }
+      }
+      unsigned bal = __ballot_sync(0xffffffffu, fresh);
+      if (fresh) nid[m + __popc(bal & ((1u << lane) - 1u))] = id;
+      m += __popc(bal);
+    }
+    __syncwarp();
+    for (uint32_t b = 0; b < m; b += 32 / SG) {     // warp-uniform trip count
+      uint32_t i = b + (uint32_t)(lane / SG);
+      bool valid = i < m;
+      uint32_t id = valid ? nid[i] : 0u;
+      float d = group_distance<ST, M>(qs, srows + (size_t)id * sc, (int)sc, sgl, SG);
+      if (valid && sgl == 0) nkey[i] = pack_key(d, id);
+    }
+    __syncwarp();
+    dc += m;
+    visited += m;
+    warp_bitonic_sort(nkey, m, lane);
+    n = min(m, L);
+    for (uint32_t i = lane; i < n; i += 32) list[i] = nkey[i];
+    __syncwarp();
+    if (nseeds == 0) status |= kStatusEmptySeeds;
+
+    // ---- best-first iterations ----------------------------------------------------------
+    const float user_radius = P.radius;
+    for (uint32_t it = 0; it < cfg.max_iters; it++) {
+      float rk = (n >= P.size) ? fminf(key_dist(list[P.size - 1]), user_radius) : user_radius;
+      const float limit = P.coef * rk;
+      // pick up to `parents` unexpanded entries within the limit, in list order
+      uint32_t np = 0;
+      bool stop = false;
+      for (uint32_t b = 0; b < n && !stop && np < cfg.parents; b += 32) {
+        uint32_t i = b + lane;
+        unsigned long long k = i < n ? list[i] : ~0ull;
+        unsigned ball = __ballot_sync(0xffffffffu, i < n && !key_expanded(k));
+        while (ball && np < cfg.parents) {
+          int j = __ffs(ball) - 1;
+          unsigned long long kj = __shfl_sync(0xffffffffu, k, j);
+          if (key_dist(kj) > limit) { stop = true; break; }
+          if (lane == j) list[i] = k | kExpandedBit;
+          if (lane == 0) w.parents[np] = key_rawid(kj);
+          np++;
+          ball &= ball - 1;
+        }
+      }
+      __syncwarp();
+      if (np == 0) break;
+      expansions += np;
+      // gather unvisited neighbours of the parents, in edge order
+      const uint32_t per_parent = min(P.edge_size, NB / np);
+      uint32_t cnt = 0;
+      for (uint32_t pi = 0; pi < np; pi++) {
+        const uint32_t v = w.parents[pi];
+        const uint32_t e0 = g.offsets[v];
+        const uint32_t ne = min(g.offsets[v + 1] - e0, per_parent);
+        edges_read += ne;
+        for (uint32_t b = 0; b < ne; b += 32) {
+          uint32_t t = b + lane;
+          bool fresh = false;
+          uint32_t id = 0;
+          if (t < ne) {
+            id = __ldg(g.edges + e0 + t);
+            uint32_t bit = 1u << (id & 31u);
+            fresh = (atomicOr(&bitmap[id >> 5], bit) & bit) == 0u;
+          }
+          unsigned bal = __ballot_sync(0xffffffffu, fresh);
+          if (fresh) nid[cnt + __popc(bal & ((1u << lane) - 1u))] = id;
+          cnt += __popc(bal);
+        }
+      }
+      __syncwarp();
+      visited += cnt;
+      dc += cnt;
+      // distances of the new neighbours; keep the ones that can enter the list
+      const unsigned long long worst = (n >= L) ? (list[L - 1] & ~(unsigned long long)kExpandedBit) : ~0ull;
+      const float insert_limit = P.coef * user_radius;
+      uint32_t kept = 0;
+      const uint32_t gpw = 32 / SG;
+      for (uint32_t b = 0; b < cnt; b += gpw) {
+        uint32_t i = b + (uint32_t)(lane / SG);
+        bool valid = i < cnt;
+        uint32_t id = valid ? nid[i] : 0u;
+        float d = group_distance<ST, M>(qs, srows + (size_t)id * sc, (int)sc, sgl, SG);
+        unsigned long long key = pack_key(d, id);
+        bool keep = valid && sgl == 0 && key < worst && d <= insert_limit;
+        unsigned bal = __ballot_sync(0xffffffffu, keep);
+        if (keep) nkey[kept + __popc(bal & ((1u << lane) - 1u))] = key;
+        kept += __popc(bal);
+      }
+      __syncwarp();
+      if (kept == 0) continue;
+      warp_bitonic_sort(nkey, kept, lane);
+      // merge list[0..n) with nkey[0..kept) into alt, keeping the first L
+      for (uint32_t i = lane; i < n; i += 32) {
+        unsigned long long k = list[i];
+        uint32_t pos = i + warp_lower_bound(nkey, kept, k & ~(unsigned long long)kExpandedBit);
+        if (pos < L) alt[pos] = k;
+      }
+      for (uint32_t i = lane; i < kept; i += 32) {
+        unsigned long long k = nkey[i];
+        // entries of the list compare without their expanded bit
+        uint32_t lo = 0, hi = n;
+        while (lo < hi) {
+          uint32_t mid = (lo + hi) >> 1;
+          if ((list[mid] & ~(unsigned long long)kExpandedBit) < k) lo = mid + 1; else hi = mid;
+        }
+        uint32_t pos = i + lo;
+        if (pos < L) alt[pos] = k;
+      }
+      __syncwarp();
+      n = min(n + kept, L);
+      unsigned long long* t = list; list = alt; alt = t;
+    }
+
+    // ---- exact re-rank of the best entries with the full-precision rows -------------------
+    uint32_t R = min(n, max(P.size, (uint32_t)((P.size * cfg.rerank_x16 + 15) / 16)));
+    const uint32_t gpn = 32 / NG;
+    for (uint32_t b = 0; b < R; b += gpn) {
+      uint32_t i = b + (uint32_t)(lane / NG);
+      bool valid = i < R;
+      uint32_t id = valid ? key_rawid(list[i]) : 0u;
+      float d = group_distance<OT, M>(qn, g.objects + (size_t)id * rc, (int)rc, ngl, NG);
+      if (valid && ngl == 0) nkey[i] = pack_key(d, id);
+    }
+    __syncwarp();
+    warp_bitonic_sort(nkey, R, lane);
+    uint32_t nout = 0;
+    for (uint32_t b = 0; b < R && nout < P.size_out; b += 32) {
+      uint32_t i = b + lane;
+      bool ok = i < R && key_dist(nkey[i]) <= user_radius;
+      unsigned bal = __ballot_sync(0xffffffffu, ok);
+      uint32_t pos = nout + __popc(bal & ((1u << lane) - 1u));
+      if (ok && pos < P.size_out) out[P.out_off + pos] = ObjDist{key_id(nkey[i]), key_dist(nkey[i])};
+      nout = min(P.size_out, nout + __popc(bal));
+    }
+    if (lane == 0) {
+      out_count[q] = nout;
+      stats[q] = QueryStats{dc, expansions, visited, edges_read, status};
+    }
+    // clear this slot's visited bitmap for the next query
+    uint4* bm4 = reinterpret_cast<uint4*>(bitmap);
+    for (uint32_t i = lane; i < cfg.bitmap_words / 4; i += 32) bm4[i] = make_uint4(0, 0, 0, 0);
+    __syncwarp();
+  }
+}
+
+inline size_t fast_smem_per_warp(uint32_t row_chunks, const FastConfig& c) {
+  size_t per = (size_t)row_chunks * 16 + (size_t)c.search_chunks * 16 + (size_t)c.list_cap * 16 +
+               (size_t)c.nbr_cap * 12 + 64;
+  return (per + 15) & ~(size_t)15;
+}
+
+}  // namespace ngtg

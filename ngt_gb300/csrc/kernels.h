@@ -12,6 +12,15 @@ typedef void (*ExactKernelFn)(DevGraph, const uint4*, uint32_t, const QueryParam
                               uint32_t*, QueryStats*, uint32_t*, unsigned long long*, ExactConfig);
 typedef void (*LinearKernelFn)(DevGraph, const uint4*, uint32_t, uint32_t, const uint8_t*, float*, uint32_t);
 
+struct FastConfig;
+typedef void (*FastKernelFn)(DevGraph, const uint4*, const uint4*, uint32_t, const QueryParams*, const uint32_t*,
+                             ObjDist*, uint32_t*, QueryStats*, uint32_t*, uint32_t*, FastConfig);
+
+// Batched kernel for (object type, metric); bf16_rows selects the bf16 search
+// rows for float objects.  nullptr when unsupported.
+FastKernelFn fast_kernel(ObjType ot, Metric m, bool bf16_rows);
+void launch_float_rows_to_bf16(const void* in, void* out, size_t nfloats, cudaStream_t s);
+
 // Return nullptr when the (type, metric) pair is not supported.
 ExactKernelFn exact_kernel_float(Metric m);
 ExactKernelFn exact_kernel_half(Metric m);

@@ -8,9 +8,9 @@ and searched through the C ABI exactly like a reference-built index.
 
 Construction (ONNG, lib/NGT/GraphReconstructor.h:645-760 reconstructGraph):
   1. the exact K-nearest-neighbour graph (K = 100, the ANNG creation edge
-     count), from L2 distances computed as |x|^2 + |y|^2 - 2 x.y with a bf16
-     GEMM: for integer coordinates <= 255 every product and sum is exact in the
-     fp32 accumulator, so the neighbour lists are exact;
+     count), from L2 distances computed as |x|^2 + |y|^2 - 2 x.y with an fp32
+     GEMM (TF32 off): for integer coordinates <= 255 every product and partial
+     sum is an integer below 2^24, so the neighbour lists are exact;
   2. outgoing edges: the first `outgoing` neighbours of every node;
   3. incoming edges: node u is added to the list of each of its first
      `incoming` neighbours (reverse edges), duplicates removed, every list
@@ -19,7 +19,9 @@ The reference's path adjustment (shortcut reduction) is not applied.
 
 Written files: prf, obj (NGT Repository<Object>), grp (Repository<GraphNode>
 with the trailing per-node size vector), and no tree: the index is
-IndexType Graph, so searches start from seeded random nodes.
+IndexType Graph, so searches start from seeded random nodes.  Like a
+reference ONNG it searches with the dynamic edge size (EdgeSizeForSearch -2:
+30 + 10^(20*epsilon) edges per expanded node, NGT's default base and rate).
 """
 from __future__ import annotations
 
@@ -34,15 +36,15 @@ def knn_graph(x: np.ndarray, k: int, chunk: int = 2048, log=print):
     import torch
     dev = torch.device("cuda")
     n = x.shape[0]
+    torch.backends.cuda.matmul.allow_tf32 = False
     X = torch.from_numpy(x).to(dev)
-    Xb = X.to(torch.bfloat16)
     sq = (X * X).sum(1)                                   # integers < 2^24: exact in fp32
     ids = torch.empty((n, k), dtype=torch.int32, device=dev)
     dst = torch.empty((n, k), dtype=torch.float32, device=dev)
     t0 = time.time()
     for s in range(0, n, chunk):
         e = min(n, s + chunk)
-        g = (Xb[s:e] @ Xb.T).float()                       # exact for integer data <= 255
+        g = X[s:e] @ X.T                                   # fp32 GEMM: exact for integer data <= 255
         d2 = sq[s:e, None] + sq[None, :] - 2.0 * g
         d2[torch.arange(e - s, device=dev), torch.arange(s, e, device=dev)] = float("inf")
         v, i = torch.topk(d2, k, dim=1, largest=False, sorted=True)
@@ -94,7 +96,7 @@ def write_index(path: str, x: np.ndarray, offsets: np.ndarray, edges: np.ndarray
     n, dim = x.shape
     nrows = n + 1
     prf = {"Dimension": str(dim), "DistanceType": "L2", "ObjectType": "Float-4", "IndexType": "Graph",
-           "GraphType": "ONNG", "EdgeSizeForSearch": "0", "EdgeSizeForCreation": "100", "SeedSize": "10",
+           "GraphType": "ONNG", "EdgeSizeForSearch": "-2", "EdgeSizeForCreation": "100", "SeedSize": "10",
            "SeedType": "None", "EpsilonType": "None", "DynamicEdgeSizeBase": "30", "DynamicEdgeSizeRate": "20",
            "DatabaseType": "Memory", "ObjectAlignment": "False", "RefinementObjectType": "Float-4",
            "OutgoingEdge": "10", "IncomingEdge": "100"}

@@ -1,0 +1,105 @@
+"""GPU tests of the batched (warp-per-query, bf16 + exact re-rank) graph search.
+
+Its visit order is parallel, so its ids are judged by recall: against the
+exact ground truth (the reference's own linear-search golden results, ties by
+id) its recall@k must be no lower than the reference's graph search at the
+same epsilon and edge size.  Every distance it returns must be the exact
+comparator's value for that id (the oracle's; bit-identical on integer data).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from golden_util import is_integer_fixture, materialize
+
+pytestmark = pytest.mark.gpu
+
+KERNEL_BATCHED = 1
+
+
+@pytest.fixture(scope="module")
+def workdir(tmp_path_factory):
+    return str(tmp_path_factory.mktemp("gpu_batched"))
+
+
+def _tie_aware_recall(ids, counts, gt_d, k, qrows, objects, metric_fn):
+    hit = 0
+    for j in range(ids.shape[0]):
+        kth = gt_d[j, k - 1]
+        for i in ids[j, :min(k, counts[j])]:
+            if metric_fn(qrows[j], objects[i]) <= kth:
+                hit += 1
+    return hit / (k * ids.shape[0])
+
+
+CASES = [("c1_f32_l2", 0, 10), ("c1_f32_l2", 3, 10), ("c1_f32_l2_onng", 0, 11), ("u8_l2", 0, 2),
+         ("u8_l1", 0, 1), ("f32_cosine", 0, 1), ("f32_ncosine", 0, 1), ("f16_l2", 0, 1)]
+
+
+@pytest.mark.parametrize("name,graph_setting,linear_setting", CASES)
+def test_batched_recall_not_below_reference(name, graph_setting, linear_setting, workdir):
+    from ngt_gb300 import Index
+    path, meta, queries, golden = materialize(name, workdir)
+    s = meta["settings"][graph_setting]
+    k, eps, nq = s["k"], s["epsilon"], s["nq"]
+    files = oracle.IndexFiles(path)
+    o = oracle.Oracle(files)
+    lin = meta["settings"][linear_setting] if linear_setting < len(meta["settings"]) else None
+    if lin is not None and lin["op"] == "linear" and lin["k"] >= k:
+        gt_d = golden["dist_%d" % linear_setting][:nq]
+    else:
+        _, gt_d, _ = o.linear_search(queries[:nq], k=k, threads=4)
+    qrows = o.prepare(queries[:nq])
+
+    def dist(a, b):
+        return oracle_dist(files, a, b)
+
+    ref_ids, ref_n = golden["ids_%d" % graph_setting], golden["count_%d" % graph_setting]
+    with Index(path, read_only=True) as ix:
+        ids, ds, n = ix.batch_search(queries[:nq], k=k, epsilon=eps, kernel=KERNEL_BATCHED)
+    r_ref = _tie_aware_recall(ref_ids, ref_n, gt_d, k, qrows, files.objects, dist)
+    r_ours = _tie_aware_recall(ids, n, gt_d, k, qrows, files.objects, dist)
+    assert r_ours >= r_ref - 1e-12, (name, r_ours, r_ref)
+    # returned distances are the exact comparator's values for the returned ids
+    for j in range(nq):
+        for i in range(n[j]):
+            want = dist(qrows[j], files.objects[ids[j, i]])
+            if is_integer_fixture(name):
+                assert ds[j, i] == want, (name, j, i)
+            else:
+                assert abs(ds[j, i] - want) <= 1e-5 * max(abs(want), 0.1), (name, j, i)
+        # ascending by (distance, id)
+        pairs = list(zip(ds[j, :n[j]], ids[j, :n[j]]))
+        assert pairs == sorted(pairs)
+
+
+_DIST_LIB = {}
+
+
+def oracle_dist(files, a, b):
+    import ctypes
+    lib = _DIST_LIB.get("lib")
+    if lib is None:
+        lib = ctypes.CDLL(oracle.build())
+        lib.oracle_distance.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
+        lib.oracle_distance.restype = ctypes.c_float
+        _DIST_LIB["lib"] = lib
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    return np.float32(lib.oracle_distance(files.otype, files.metric, a.ctypes.data, b.ctypes.data, files.dpad))
+
+
+def test_batched_mixed_parameters_and_edge_cases(workdir):
+    from ngt_gb300 import Index
+    path, meta, queries, golden = materialize("c1_f32_l2", workdir)
+    with Index(path, read_only=True) as ix:
+        ids, ds, n = ix.batch_search(queries[:50], k=0, epsilon=0.1, kernel=KERNEL_BATCHED)
+        assert (n == 0).all()
+        ids, ds, n = ix.batch_search(queries[:50], k=10, epsilon=0.1, radius=0.0, kernel=KERNEL_BATCHED)
+        assert (n == 0).all()
+        ks = np.array([1, 5, 10, 50, 100] * 40)
+        ids, ds, n = ix.batch_search(queries[:200], k=ks, epsilon=0.1, kernel=KERNEL_BATCHED)
+        assert (n == ks).all()
+        # a radius keeps only results within it
+        ids, ds, n = ix.batch_search(queries[:200], k=10, epsilon=0.1, radius=300.0, kernel=KERNEL_BATCHED)
+        assert all((ds[j, :n[j]] <= 300.0).all() for j in range(200))
