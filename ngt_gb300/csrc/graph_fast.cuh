@@ -104,13 +104,12 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
   const uint32_t rc = g.row_chunks, sc = cfg.search_chunks;
   const uint32_t L = cfg.list_cap, NB = cfg.nbr_cap;
   // per-warp carve-up
-  const size_t per_warp = (size_t)rc * 16 + (size_t)sc * 16 + (size_t)L * 16 + (size_t)NB * 12 + 64;
+  const size_t per_warp = (size_t)rc * 16 + (size_t)sc * 16 + (size_t)L * 8 + (size_t)NB * 12 + 64;
   unsigned char* base = smem + warp * ((per_warp + 15) & ~(size_t)15);
   uint4* qn = reinterpret_cast<uint4*>(base);                  // query, object type
   uint4* qs = qn + rc;                                          // query, search type
-  unsigned long long* list0 = reinterpret_cast<unsigned long long*>(qs + sc);
-  unsigned long long* list1 = list0 + L;
-  unsigned long long* nkey = list1 + L;                         // NB keys
+  unsigned long long* list = reinterpret_cast<unsigned long long*>(qs + sc);
+  unsigned long long* nkey = list + L;                          // NB keys
   uint32_t* nid = reinterpret_cast<uint32_t*>(nkey + NB);       // NB ids
   FastWarpSmem& w = *reinterpret_cast<FastWarpSmem*>(nid + NB);
   const uint32_t slot = blockIdx.x * kFastWarps + warp;
@@ -141,8 +140,7 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
     __syncwarp();
     uint32_t dc = 0, expansions = 0, edges_read = 0, status = 0, visited = 0;
     uint32_t n = 0;
-    unsigned long long* list = list0;
-    unsigned long long* alt = list1;
+    uint32_t scan0 = 0;        // no unexpanded entry before this position
     if (P.size == 0) {
       if (lane == 0) { out_count[q] = 0; stats[q] = QueryStats{0, 0, 0, 0, 0}; }
       __syncwarp();
@@ -220,7 +218,7 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       // pick up to `parents` unexpanded entries within the limit, in list order
       uint32_t np = 0;
       bool stop = false;
-      for (uint32_t b = 0; b < n && !stop && np < cfg.parents; b += 32) {
+      for (uint32_t b = scan0 & ~31u; b < n && !stop && np < cfg.parents; b += 32) {
         uint32_t i = b + lane;
         unsigned long long k = i < n ? list[i] : ~0ull;
         unsigned ball = __ballot_sync(0xffffffffu, i < n && !key_expanded(k));
@@ -231,6 +229,7 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
           if (lane == j) list[i] = k | kExpandedBit;
           if (lane == 0) w.parents[np] = key_rawid(kj);
           np++;
+          scan0 = b + (uint32_t)j + 1;
           ball &= ball - 1;
         }
       }
@@ -281,26 +280,40 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       __syncwarp();
       if (kept == 0) continue;
       warp_bitonic_sort(nkey, kept, lane);
-      // merge list[0..n) with nkey[0..kept) into alt, keeping the first L
-      for (uint32_t i = lane; i < n; i += 32) {
-        unsigned long long k = list[i];
-        uint32_t pos = i + warp_lower_bound(nkey, kept, k & ~(unsigned long long)kExpandedBit);
-        if (pos < L) alt[pos] = k;
-      }
+      // In-place merge of nkey[0..kept) into list[0..n), keeping the first L.
+      // 1. merged positions of the new keys (list entries compare without their
+      //    expanded bit), parked in nid (no longer needed)
       for (uint32_t i = lane; i < kept; i += 32) {
         unsigned long long k = nkey[i];
-        // entries of the list compare without their expanded bit
         uint32_t lo = 0, hi = n;
         while (lo < hi) {
           uint32_t mid = (lo + hi) >> 1;
           if ((list[mid] & ~(unsigned long long)kExpandedBit) < k) lo = mid + 1; else hi = mid;
         }
-        uint32_t pos = i + lo;
-        if (pos < L) alt[pos] = k;
+        nid[i] = i + lo;
       }
       __syncwarp();
+      const uint32_t first_new = nid[0];
+      // 2. list entries move right (never left): chunks from the top down, each
+      //    read completely before any of it is written
+      for (int hi = (int)n; hi > 0; hi -= 32) {
+        int idx = hi - 32 + lane;
+        unsigned long long k = 0;
+        uint32_t pos = 0xffffffffu;
+        if (idx >= 0) {
+          k = list[idx];
+          pos = (uint32_t)idx + warp_lower_bound(nkey, kept, k & ~(unsigned long long)kExpandedBit);
+        }
+        __syncwarp();
+        if (idx >= 0 && pos < L) list[pos] = k;
+        __syncwarp();
+      }
+      // 3. the new keys
+      for (uint32_t i = lane; i < kept; i += 32)
+        if (nid[i] < L) list[nid[i]] = nkey[i];
+      __syncwarp();
       n = min(n + kept, L);
-      unsigned long long* t = list; list = alt; alt = t;
+      if (first_new < scan0) scan0 = first_new;
     }
 
     // ---- exact re-rank of the best entries with the full-precision rows -------------------
@@ -336,7 +349,7 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
 }
 
 inline size_t fast_smem_per_warp(uint32_t row_chunks, const FastConfig& c) {
-  size_t per = (size_t)row_chunks * 16 + (size_t)c.search_chunks * 16 + (size_t)c.list_cap * 16 +
+  size_t per = (size_t)row_chunks * 16 + (size_t)c.search_chunks * 16 + (size_t)c.list_cap * 8 +
                (size_t)c.nbr_cap * 12 + 64;
   return (per + 15) & ~(size_t)15;
 }
