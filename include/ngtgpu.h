@@ -64,6 +64,24 @@ bool ngtgpu_search_batch_device(NGTIndex, const void *d_rows, size_t nq, const N
  * iteration, and re-ranked candidates per query as a multiple of size. */
 bool ngtgpu_set_batched_tuning(NGTIndex, uint32_t list_capacity, uint32_t parents, float rerank_factor, NGTError);
 
+/* Exact graph search (results equal ngtgpu_search_batch_device with
+ * NGTGPU_KERNEL_EXACT) that allocates no device memory, for callers that cannot
+ * call cudaMalloc while they search: hosts that own and budget all device
+ * memory themselves, and serving paths that must never enter the allocator.
+ * No counterpart in the reference.  Its scratch (query parameters, seed lists,
+ * per-CTA visited bitmaps and candidate overflow tiers) lives in one fixed
+ * 32 MiB device array that the library reserves on every GPU that loads it,
+ * until the process exits.  The first call on a device looks up that array's
+ * address (no allocation), so make it before any stream capture.  Calls share
+ * the array: calls that overlap on the GPU race.  A call is rejected with an
+ * error when its parameters plus one CTA's scratch exceed 32 MiB, and when a
+ * query's result size has no seed table yet (run one regular search with that
+ * size on the index first).  Buffers are device memory, as in
+ * ngtgpu_search_batch_device; the call returns after the search completed. */
+bool ngtgpu_search_exact_noalloc(NGTIndex, const void *d_rows, size_t nq, const NGTQueryParameters *params,
+                                 size_t nparams, NGTObjectDistance *d_results, size_t kmax, uint32_t *d_counts,
+                                 NGTGPUQueryStats *d_stats, void *stream, NGTError);
+
 /* Number of kernel launches issued by this index since it was opened. */
 uint64_t ngtgpu_kernel_launches(NGTIndex, NGTError);
 

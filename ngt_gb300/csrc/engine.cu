@@ -10,6 +10,7 @@
 #include <cmath>
 #include <cstring>
 #include <stdexcept>
+#include <sstream>
 #include <string>
 
 #include "graph_exact.cuh"
@@ -104,6 +105,7 @@ GraphEngine::~GraphEngine() {
   cudaFree(d_bitmaps_);
   cudaFree(d_overflow_);
   cudaFree(d_fast_bitmaps_);
+  cudaFree(d_fast_spill_);
   cudaFree(d_work_);
   cudaFree(d_bf16_);
   if (stream_) cudaStreamDestroy(stream_);
@@ -343,9 +345,12 @@ void GraphEngine::ensure_fast_scratch(size_t slots) {
   if (slots <= fast_slots_) return;
   NGT_CUDA(cudaStreamSynchronize(stream_));
   cudaFree(d_fast_bitmaps_);
+  cudaFree(d_fast_spill_);
   d_fast_bitmaps_ = nullptr;
+  d_fast_spill_ = nullptr;
   size_t words = ((host_.nrows + 31) / 32 + 3) / 4 * 4;
   NGT_CUDA(cudaMalloc(&d_fast_bitmaps_, slots * words * 4));
+  NGT_CUDA(cudaMalloc(&d_fast_spill_, slots * 2 * (size_t)kSpillCapacity * 8));
   NGT_CUDA(cudaMemsetAsync(d_fast_bitmaps_, 0, slots * words * 4, stream_));
   if (!d_work_) NGT_CUDA(cudaMalloc(&d_work_, 16));
   NGT_CUDA(cudaStreamSynchronize(stream_));
@@ -438,7 +443,7 @@ void GraphEngine::launch_fast(const uint4* d_rows, size_t nq, const QueryParams*
   cfg.parents = tuning_.parents ? std::min<uint32_t>(tuning_.parents, 8) : 2;
   float rf0 = tuning_.rerank_factor > 0.f ? tuning_.rerank_factor : 2.0f;
   uint32_t rerank_max = std::min<uint32_t>(L, (uint32_t)std::ceil(rf0 * (float)max_size) + 1);
-  cfg.nbr_cap = std::max<uint32_t>(512, next_pow2(rerank_max));
+  cfg.nbr_cap = std::max<uint32_t>({512u, next_pow2(rerank_max), L});
   cfg.search_chunks = bf16 ? dev_.row_chunks / 2 : dev_.row_chunks;
   cfg.sgroup = std::min<uint32_t>(32, next_pow2(cfg.search_chunks));
   cfg.ngroup = std::min<uint32_t>(32, next_pow2(dev_.row_chunks));
@@ -446,6 +451,7 @@ void GraphEngine::launch_fast(const uint4* d_rows, size_t nq, const QueryParams*
   cfg.rerank_x16 = (uint32_t)std::ceil(rf * 16.0f);
   cfg.bitmap_words = ((host_.nrows + 31) / 32 + 3) / 4 * 4;
   cfg.max_iters = 1u << 22;
+  cfg.spill_cap = kSpillCapacity;
   size_t smem = kFastWarps * fast_smem_per_warp(dev_.row_chunks, cfg);
   int max_smem = 0, per_sm = 0, sms = 0;
   NGT_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
@@ -458,7 +464,7 @@ void GraphEngine::launch_fast(const uint4* d_rows, size_t nq, const QueryParams*
   NGT_CUDA(cudaMemsetAsync(d_work_, 0, 4, stream));
   const uint4* srows = bf16 ? static_cast<const uint4*>(d_bf16_) : dev_.objects;
   fn<<<(unsigned)grid, kFastThreads, smem, stream>>>(dev_, srows, d_rows, (uint32_t)nq, d_params, d_seeds, d_out,
-                                                      d_counts, d_stats, d_fast_bitmaps_, d_work_, cfg);
+                                                      d_counts, d_stats, d_fast_bitmaps_, d_work_, d_fast_spill_, cfg);
   NGT_CUDA(cudaGetLastError());
   launches_++;
 }
@@ -546,6 +552,93 @@ void GraphEngine::linear_search(const void* queries, QueryType qt, size_t nq, si
   NGT_CUDA(cudaFreeAsync(d_out, s));
   NGT_CUDA(cudaFreeAsync(d_counts, s));
   NGT_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace ngtg
+
+namespace ngtg {
+
+void GraphEngine::search_device_noalloc(void* scratch, size_t scratch_bytes, const uint4* d_rows, size_t nq,
+                                        const SearchArgs* args, size_t nargs, ObjDist* d_out, uint32_t* d_counts,
+                                        QueryStats* d_stats, size_t kmax, cudaStream_t stream) {
+  std::lock_guard<std::mutex> lock(mu_);
+  NGT_CUDA(cudaSetDevice(device_));
+  if (nq == 0) return;
+  const Property& p = host_.prop;
+  // every seed table the queries need must exist already (building one allocates)
+  if (p.has_tree) {
+    for (size_t i = 0; i < nargs; i++) {
+      const SearchArgs& a = args[i];
+      float coef = a.epsilon + 1.0f;
+      if (coef == 0.0f) coef = 1.1f;
+      size_t ss = p.seed_size == 0 ? a.size : (size_t)p.seed_size;
+      if (ss > a.size) ss = a.size;
+      if (p.seed_type == 4) ss = SIZE_MAX;
+      if (ss == 0) ss = 1;
+      if (!seed_tables_.count(ss))
+        throw std::runtime_error("no seed table for result size " + std::to_string(a.size) +
+                                 " yet: run one regular search with this result size on the index first");
+    }
+  }
+  std::vector<QueryParams> params;
+  std::vector<uint32_t> seeds;
+  uint32_t max_size = 0;
+  build_params(args, nargs, nq, kmax, params, seeds, max_size);
+  ExactConfig cfg{};
+  cfg.kcap = max_size + 1;
+  cfg.ccap = 1024;
+  cfg.hcap = 8192;
+  cfg.mode = (uint32_t)mode_;
+  cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));
+  cfg.bitmap_words = (host_.nrows + 31) / 32;
+  cfg.ocap = kOverflowCapacity;
+  int max_smem = 0;
+  NGT_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
+  size_t smem = exact_smem_bytes(dev_.row_chunks, cfg);
+  while (smem > (size_t)max_smem && cfg.hcap > 2048) {
+    cfg.hcap >>= 1;
+    smem = exact_smem_bytes(dev_.row_chunks, cfg);
+  }
+  while (smem > (size_t)max_smem && cfg.ccap > 256) {
+    cfg.ccap >>= 1;
+    smem = exact_smem_bytes(dev_.row_chunks, cfg);
+  }
+  if (smem > (size_t)max_smem) throw std::runtime_error("result size too large for the on-chip search state");
+  // scratch layout: params | seeds | bitmaps[grid] | overflow[grid], each 256-byte aligned
+  auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  const size_t params_bytes = up(nq * sizeof(QueryParams));
+  const size_t seeds_bytes = up(seeds.size() * 4);
+  const size_t bitmap_bytes = up((size_t)cfg.bitmap_words * 4);
+  const size_t overflow_bytes = (size_t)2 * cfg.ocap * 8;
+  const size_t per_cta = bitmap_bytes + overflow_bytes;
+  const size_t fixed = params_bytes + seeds_bytes;
+  if (fixed + per_cta > scratch_bytes) {
+    std::ostringstream m;
+    m << "the no-allocation search needs " << fixed + per_cta << " bytes of scratch for " << nq
+      << " queries on this index, more than its fixed " << scratch_bytes << "-byte scratch; use fewer queries per call";
+    throw std::runtime_error(m.str());
+  }
+  ExactKernelFn fn = exact_kernel(host_.prop.otype, host_.prop.metric);
+  NGT_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0, sms = 0;
+  NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kExactThreads, smem));
+  NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+  size_t grid = std::min<size_t>({nq, (size_t)std::max(1, per_sm) * sms, (scratch_bytes - fixed) / per_cta});
+  unsigned char* base = static_cast<unsigned char*>(scratch);
+  QueryParams* d_params = reinterpret_cast<QueryParams*>(base);
+  uint32_t* d_seeds = reinterpret_cast<uint32_t*>(base + params_bytes);
+  uint32_t* d_bitmaps = reinterpret_cast<uint32_t*>(base + fixed);
+  unsigned long long* d_overflow = reinterpret_cast<unsigned long long*>(base + fixed + grid * bitmap_bytes);
+  NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QueryParams), cudaMemcpyHostToDevice, stream));
+  NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, stream));
+  NGT_CUDA(cudaMemsetAsync(d_bitmaps, 0, grid * bitmap_bytes, stream));   // the kernel expects clear bitmaps
+  cfg.bitmap_words = (uint32_t)(bitmap_bytes / 4);
+  fn<<<(unsigned)grid, kExactThreads, smem, stream>>>(dev_, d_rows, (uint32_t)nq, d_params, d_seeds, d_out, d_counts,
+                                                       d_stats, d_bitmaps, d_overflow, cfg);
+  NGT_CUDA(cudaGetLastError());
+  // the host parameter vectors must outlive the copies above
+  NGT_CUDA(cudaStreamSynchronize(stream));
+  launches_++;
 }
 
 }  // namespace ngtg

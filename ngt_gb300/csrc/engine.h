@@ -73,6 +73,14 @@ class GraphEngine {
   void search_device(const uint4* d_rows, size_t nq, const SearchArgs* args, size_t nargs, ObjDist* d_out,
                      uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream,
                      Kernel kernel = Kernel::Exact);
+  // The exact search with every scratch buffer carved from the caller-provided
+  // device memory `scratch` (scratch_bytes long) instead of allocated: query
+  // parameters, seed lists, per-CTA visited bitmaps and overflow tiers.  Throws
+  // when the scratch cannot hold one CTA's share, or when a seed table the
+  // queries need has not been built by an earlier regular search.
+  void search_device_noalloc(void* scratch, size_t scratch_bytes, const uint4* d_rows, size_t nq,
+                             const SearchArgs* args, size_t nargs, ObjDist* d_out, uint32_t* d_counts,
+                             QueryStats* d_stats, size_t kmax, cudaStream_t stream);
   void set_tuning(const FastTuning& t) { tuning_ = t; }
   const FastTuning& tuning() const { return tuning_; }
   bool fast_supported(Kernel k) const;
@@ -126,6 +134,8 @@ class GraphEngine {
   size_t bitmap_grid_ = 0;
   static constexpr uint32_t kOverflowCapacity = 65536;   // candidate keys per CTA beyond shared memory
   uint32_t* d_fast_bitmaps_ = nullptr;                    // one visited bitmap per warp slot
+  unsigned long long* d_fast_spill_ = nullptr;            // spill tier per warp slot (2 x kSpillCapacity)
+  static constexpr uint32_t kSpillCapacity = 32768;
   size_t fast_slots_ = 0;
   uint32_t* d_work_ = nullptr;                            // work counter of the batched kernel
   void* d_bf16_ = nullptr;                                // bf16 copy of float object rows

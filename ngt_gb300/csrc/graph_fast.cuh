@@ -19,11 +19,16 @@
 //   * finally the best R = ceil(size * rerank_factor) entries are re-ranked with
 //     the exact comparator over the full-precision rows, so every returned
 //     distance is the reference comparator's value for that id.
+//   * candidates that do not fit in the list (or are pushed out of it) go to a
+//     per-warp spill tier in global memory, all larger than every list key;
+//     when every list entry is expanded, the spill entries still within the
+//     exploration limit come back (the smallest first, by an exact radix
+//     select), so the candidate set is as unbounded as the reference's queue.
 // Differences from the reference that can change which ids are found (and are
 // why this kernel is checked by recall, not by id equality): P > 1 expands
-// slightly more nodes per step, the candidate list is bounded to L entries, an
-// expanded node reads at most nbr_cap / P neighbours, and the search distances
-// are bf16 (exact for integer coordinates <= 256).
+// slightly more nodes per step, an expanded node reads at most nbr_cap / P
+// neighbours, and the search distances are bf16 (exact for integer coordinates
+// <= 256).
 #pragma once
 #include <cuda_bf16.h>
 #include <cfloat>
@@ -46,6 +51,7 @@ struct FastConfig {
   uint32_t rerank_x16;     // rerank factor * 16
   uint32_t bitmap_words;
   uint32_t max_iters;
+  uint32_t spill_cap;      // keys per warp slot in the global spill tier
 };
 
 struct FastWarpSmem {
@@ -55,6 +61,7 @@ struct FastWarpSmem {
   uint32_t nparents;
   uint32_t parents[8];
   uint32_t seed_leaf;
+  uint32_t hist[256];
 };
 
 __device__ __forceinline__ uint32_t key_rawid(unsigned long long k) { return (uint32_t)k & 0x7fffffffu; }
@@ -98,13 +105,14 @@ __global__ void __launch_bounds__(kFastThreads)
 graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint4* __restrict__ queries, uint32_t nq,
                          const QueryParams* __restrict__ params, const uint32_t* __restrict__ seed_list,
                          ObjDist* __restrict__ out, uint32_t* __restrict__ out_count, QueryStats* __restrict__ stats,
-                         uint32_t* __restrict__ bitmaps, uint32_t* __restrict__ work, FastConfig cfg) {
+                         uint32_t* __restrict__ bitmaps, uint32_t* __restrict__ work,
+                         unsigned long long* __restrict__ spills, FastConfig cfg) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t rc = g.row_chunks, sc = cfg.search_chunks;
   const uint32_t L = cfg.list_cap, NB = cfg.nbr_cap;
   // per-warp carve-up
-  const size_t per_warp = (size_t)rc * 16 + (size_t)sc * 16 + (size_t)L * 8 + (size_t)NB * 12 + 64;
+  const size_t per_warp = (size_t)rc * 16 + (size_t)sc * 16 + (size_t)L * 8 + (size_t)NB * 12 + sizeof(FastWarpSmem);
   unsigned char* base = smem + warp * ((per_warp + 15) & ~(size_t)15);
   uint4* qn = reinterpret_cast<uint4*>(base);                  // query, object type
   uint4* qs = qn + rc;                                          // query, search type
@@ -114,6 +122,9 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
   FastWarpSmem& w = *reinterpret_cast<FastWarpSmem*>(nid + NB);
   const uint32_t slot = blockIdx.x * kFastWarps + warp;
   uint32_t* bitmap = bitmaps + (size_t)slot * cfg.bitmap_words;
+  // spill tier: candidates that do not fit in the list, all larger than every list key
+  unsigned long long* spill = spills + (size_t)slot * 2 * cfg.spill_cap;
+  unsigned long long* spill_tmp = spill + cfg.spill_cap;
   const int SG = (int)cfg.sgroup, NG = (int)cfg.ngroup;
   const int sgl = lane & (SG - 1), ngl = lane & (NG - 1);
 
@@ -141,6 +152,9 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
     uint32_t dc = 0, expansions = 0, edges_read = 0, status = 0, visited = 0;
     uint32_t n = 0;
     uint32_t scan0 = 0;        // no unexpanded entry before this position
+    uint32_t spill_n = 0;
+    unsigned long long spill_min = ~0ull;
+    bool refill = false;
     if (P.size == 0) {
       if (lane == 0) { out_count[q] = 0; stats[q] = QueryStats{0, 0, 0, 0, 0}; }
       __syncwarp();
@@ -218,6 +232,75 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       // pick up to `parents` unexpanded entries within the limit, in list order
       uint32_t np = 0;
       bool stop = false;
+      if (refill) {
+        // ---- every list entry is expanded: refill from the spill tier ----
+        // keep the first `size` entries (the results so far), drop the other expanded ones
+        n = min(n, P.size);
+        const uint32_t room = L - n;
+        uint32_t r = 0;
+        for (uint32_t b = 0; b < spill_n; b += 32) {           // live spill entries -> spill_tmp
+          uint32_t i = b + lane;
+          unsigned long long k = i < spill_n ? spill[i] : ~0ull;
+          bool live = i < spill_n && key_dist(k) <= limit;
+          unsigned bal = __ballot_sync(0xffffffffu, live);
+          if (live) spill_tmp[r + __popc(bal & ((1u << lane) - 1u))] = k;
+          r += __popc(bal);
+        }
+        __syncwarp();
+        unsigned long long thr = ~0ull;                           // take keys <= thr
+        if (r > room) {
+          // exact radix select of the room-th smallest key
+          unsigned long long prefix = 0, mask = 0;
+          uint32_t need = room;
+          for (int shift = 56; shift >= 0; shift -= 8) {
+            for (uint32_t i = lane; i < 256; i += 32) w.hist[i] = 0;
+            __syncwarp();
+            for (uint32_t i = lane; i < r; i += 32) {
+              unsigned long long k = spill_tmp[i];
+              if ((k & mask) == prefix) atomicAdd(&w.hist[(uint32_t)(k >> shift) & 255u], 1u);
+            }
+            __syncwarp();
+            uint32_t acc = 0, bsel = 255;
+            for (uint32_t b = 0; b < 256; b++) {
+              uint32_t h = w.hist[b];
+              if (acc + h >= need) { bsel = b; break; }
+              acc += h;
+            }
+            prefix |= (unsigned long long)bsel << shift;
+            need -= acc;
+            mask |= 255ull << shift;
+            __syncwarp();
+          }
+          thr = prefix;
+        }
+        // entries <= thr go behind the kept results (all larger than them); the rest stay
+        uint32_t moved = 0, stay = 0;
+        unsigned long long smin = ~0ull;
+        for (uint32_t b = 0; b < r; b += 32) {
+          uint32_t i = b + lane;
+          unsigned long long k = i < r ? spill_tmp[i] : ~0ull;
+          bool take = i < r && k <= thr;
+          bool keep = i < r && k > thr;
+          unsigned bt = __ballot_sync(0xffffffffu, take), bk = __ballot_sync(0xffffffffu, keep);
+          if (take) nkey[moved + __popc(bt & ((1u << lane) - 1u))] = k;
+          if (keep) { spill[stay + __popc(bk & ((1u << lane) - 1u))] = k; smin = k < smin ? k : smin; }
+          moved += __popc(bt);
+          stay += __popc(bk);
+        }
+        for (int off = 16; off > 0; off >>= 1) {
+          unsigned long long o = __shfl_xor_sync(0xffffffffu, smin, off);
+          smin = o < smin ? o : smin;
+        }
+        __syncwarp();
+        warp_bitonic_sort(nkey, moved, lane);
+        for (uint32_t i = lane; i < moved; i += 32) list[n + i] = nkey[i];
+        __syncwarp();
+        scan0 = n;
+        n += moved;
+        spill_n = stay;
+        spill_min = smin;
+        refill = false;
+      }
       for (uint32_t b = scan0 & ~31u; b < n && !stop && np < cfg.parents; b += 32) {
         uint32_t i = b + lane;
         unsigned long long k = i < n ? list[i] : ~0ull;
@@ -234,7 +317,15 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
         }
       }
       __syncwarp();
-      if (np == 0) break;
+      if (np == 0) {
+        // the list is exhausted (not stopped by the radius): continue from the spill tier
+        if (!stop && spill_n > 0 && key_dist(spill_min) <= limit) {
+          scan0 = n;
+          refill = true;
+          continue;
+        }
+        break;
+      }
       expansions += np;
       // gather unvisited neighbours of the parents, in edge order
       const uint32_t per_parent = min(P.edge_size, NB / np);
@@ -261,22 +352,39 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       __syncwarp();
       visited += cnt;
       dc += cnt;
-      // distances of the new neighbours; keep the ones that can enter the list
+      // distances of the new neighbours: keys below the list's worst are merged,
+      // the others (still within the exploration limit) join the spill tier
       const unsigned long long worst = (n >= L) ? (list[L - 1] & ~(unsigned long long)kExpandedBit) : ~0ull;
-      const float insert_limit = P.coef * user_radius;
+      float rk2 = (n >= P.size) ? fminf(key_dist(list[P.size - 1]), user_radius) : user_radius;
+      const float insert_limit = P.coef * rk2;
       uint32_t kept = 0;
       const uint32_t gpw = 32 / SG;
+      unsigned long long smin = spill_min;
       for (uint32_t b = 0; b < cnt; b += gpw) {
         uint32_t i = b + (uint32_t)(lane / SG);
         bool valid = i < cnt;
         uint32_t id = valid ? nid[i] : 0u;
         float d = group_distance<ST, M>(qs, srows + (size_t)id * sc, (int)sc, sgl, SG);
         unsigned long long key = pack_key(d, id);
-        bool keep = valid && sgl == 0 && key < worst && d <= insert_limit;
-        unsigned bal = __ballot_sync(0xffffffffu, keep);
+        bool live = valid && sgl == 0 && d <= insert_limit;
+        bool keep = live && key < worst;
+        bool spl = live && key >= worst;
+        unsigned bal = __ballot_sync(0xffffffffu, keep), bs = __ballot_sync(0xffffffffu, spl);
         if (keep) nkey[kept + __popc(bal & ((1u << lane) - 1u))] = key;
+        if (spl) {
+          uint32_t o = spill_n + __popc(bs & ((1u << lane) - 1u));
+          if (o < cfg.spill_cap) spill[o] = key;
+          smin = key < smin ? key : smin;
+        }
         kept += __popc(bal);
+        spill_n += __popc(bs);
       }
+      for (int off = 16; off > 0; off >>= 1) {
+        unsigned long long o = __shfl_xor_sync(0xffffffffu, smin, off);
+        smin = o < smin ? o : smin;
+      }
+      spill_min = smin;
+      if (spill_n > cfg.spill_cap) { spill_n = cfg.spill_cap; status |= kStatusCandidateOverflow; }
       __syncwarp();
       if (kept == 0) continue;
       warp_bitonic_sort(nkey, kept, lane);
@@ -295,7 +403,9 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       __syncwarp();
       const uint32_t first_new = nid[0];
       // 2. list entries move right (never left): chunks from the top down, each
-      //    read completely before any of it is written
+      //    read completely before any of it is written; unexpanded entries pushed
+      //    past the end join the spill tier
+      unsigned long long emin = ~0ull;
       for (int hi = (int)n; hi > 0; hi -= 32) {
         int idx = hi - 32 + lane;
         unsigned long long k = 0;
@@ -306,11 +416,36 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
         }
         __syncwarp();
         if (idx >= 0 && pos < L) list[pos] = k;
+        bool ev = idx >= 0 && pos >= L && !key_expanded(k);
+        unsigned be = __ballot_sync(0xffffffffu, ev);
+        if (ev) {
+          uint32_t o = spill_n + __popc(be & ((1u << lane) - 1u));
+          if (o < cfg.spill_cap) spill[o] = k;
+          emin = k < emin ? k : emin;
+        }
+        spill_n += __popc(be);
         __syncwarp();
       }
-      // 3. the new keys
-      for (uint32_t i = lane; i < kept; i += 32)
-        if (nid[i] < L) list[nid[i]] = nkey[i];
+      // 3. the new keys (those pushed past the end join the spill tier)
+      for (uint32_t b = 0; b < kept; b += 32) {
+        uint32_t i = b + lane;
+        bool in = i < kept && nid[i] < L;
+        bool ev = i < kept && nid[i] >= L;
+        if (in) list[nid[i]] = nkey[i];
+        unsigned be = __ballot_sync(0xffffffffu, ev);
+        if (ev) {
+          uint32_t o = spill_n + __popc(be & ((1u << lane) - 1u));
+          if (o < cfg.spill_cap) spill[o] = nkey[i];
+          emin = nkey[i] < emin ? nkey[i] : emin;
+        }
+        spill_n += __popc(be);
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        unsigned long long o = __shfl_xor_sync(0xffffffffu, emin, off);
+        emin = o < emin ? o : emin;
+      }
+      if (emin < spill_min) spill_min = emin;
+      if (spill_n > cfg.spill_cap) { spill_n = cfg.spill_cap; status |= kStatusCandidateOverflow; }
       __syncwarp();
       n = min(n + kept, L);
       if (first_new < scan0) scan0 = first_new;
@@ -350,7 +485,7 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
 
 inline size_t fast_smem_per_warp(uint32_t row_chunks, const FastConfig& c) {
   size_t per = (size_t)row_chunks * 16 + (size_t)c.search_chunks * 16 + (size_t)c.list_cap * 8 +
-               (size_t)c.nbr_cap * 12 + 64;
+               (size_t)c.nbr_cap * 12 + sizeof(FastWarpSmem);
   return (per + 15) & ~(size_t)15;
 }
 

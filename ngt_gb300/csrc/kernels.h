@@ -14,7 +14,7 @@ typedef void (*LinearKernelFn)(DevGraph, const uint4*, uint32_t, uint32_t, const
 
 struct FastConfig;
 typedef void (*FastKernelFn)(DevGraph, const uint4*, const uint4*, uint32_t, const QueryParams*, const uint32_t*,
-                             ObjDist*, uint32_t*, QueryStats*, uint32_t*, uint32_t*, FastConfig);
+                             ObjDist*, uint32_t*, QueryStats*, uint32_t*, uint32_t*, unsigned long long*, FastConfig);
 
 // Batched kernel for (object type, metric); bf16_rows selects the bf16 search
 // rows for float objects.  nullptr when unsupported.

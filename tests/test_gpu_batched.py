@@ -32,7 +32,7 @@ def _tie_aware_recall(ids, counts, gt_d, k, qrows, objects, metric_fn):
     return hit / (k * ids.shape[0])
 
 
-# (fixture, graph setting, linear setting).  Epsilon <= 0.1: with its bounded
+# (fixture, graph setting, linear setting).  Epsilon <= 0.2: with its bounded
 # candidate list the batched kernel explores at least what the reference does.
 CASES = [("c1_f32_l2", 0, 10), ("c1_f32_l2", 2, 10), ("c1_f32_l2_onng", 0, 11), ("u8_l2", 0, 2),
          ("u8_l1", 0, 1), ("f32_cosine", 0, 1), ("f32_ncosine", 0, 1), ("f16_l2", 0, 1)]
