@@ -41,7 +41,8 @@ sys.path.insert(0, ROOT)
 
 EPS_SWEEP = [0.0, 0.02, 0.04, 0.06, 0.07, 0.08, 0.09, 0.1, 0.12, 0.15, 0.2, 0.3]
 RECALL_TARGET = 0.95
-LIST_SWEEP = [128, 256, 512, 1024]
+LIST_SWEEP = [128, 256, 512]
+PARENT_SWEEP = [1, 2, 4]
 
 
 def log(*a):
@@ -328,18 +329,20 @@ def main():
     # batched kernel: pick the candidate-list length whose recall-target epsilon runs fastest
     best = None
     for L in LIST_SWEEP:
-        ix.set_batched_tuning(list_capacity=L)
-        eps_l, curve_l = calibrate(KERNEL_BATCHED)
-        probe = timed(KERNEL_BATCHED, eps_l, steps=2)
-        log("batched L=%d: epsilon %g recall %.4f %.1f q/s" % (L, eps_l, probe["recall"], probe["qps"]))
-        if probe["recall"] >= RECALL_TARGET and (best is None or probe["qps"] > best[2]):
-            best = (L, eps_l, probe["qps"], curve_l)
+        for P in PARENT_SWEEP:
+            ix.set_batched_tuning(list_capacity=L, parents=P)
+            eps_l, curve_l = calibrate(KERNEL_BATCHED)
+            probe = timed(KERNEL_BATCHED, eps_l, steps=2)
+            log("batched L=%d P=%d: epsilon %g recall %.4f %.1f q/s" % (L, P, eps_l, probe["recall"], probe["qps"]))
+            if probe["recall"] >= RECALL_TARGET and (best is None or probe["qps"] > best[3]):
+                best = (L, P, eps_l, probe["qps"], curve_l)
     if best is None:
-        best = (LIST_SWEEP[-1], EPS_SWEEP[-1], 0.0, curve_l)
-    ix.set_batched_tuning(list_capacity=best[0])
-    curves[KERNEL_BATCHED] = best[3]
-    runs[KERNEL_BATCHED] = timed(KERNEL_BATCHED, best[1])
+        best = (LIST_SWEEP[-1], PARENT_SWEEP[0], EPS_SWEEP[-1], 0.0, curve_l)
+    ix.set_batched_tuning(list_capacity=best[0], parents=best[1])
+    curves[KERNEL_BATCHED] = best[4]
+    runs[KERNEL_BATCHED] = timed(KERNEL_BATCHED, best[2])
     runs[KERNEL_BATCHED]["list_capacity"] = best[0]
+    runs[KERNEL_BATCHED]["parents"] = best[1]
     for kernel in (KERNEL_EXACT, KERNEL_BATCHED):
         log("kernel %d: %.1f q/s at epsilon %g, recall %.4f, %.1f GB/s"
             % (kernel, runs[kernel]["qps"], runs[kernel]["epsilon"], runs[kernel]["recall"],
@@ -377,7 +380,8 @@ def main():
             "config": {"workload": "graph search, %d x %d float32 L2 ONNG, %d queries per step, k=%d"
                                    % (args.n, args.dim, nq, k),
                        "headline": "batched kernel (warp per query, bf16 rows, exact fp32 re-rank), epsilon=%g, "
-                                   "candidate list %d" % (head["epsilon"], head["list_capacity"]),
+                                   "candidate list %d, %d parents per step"
+                                   % (head["epsilon"], head["list_capacity"], head["parents"]),
                        "recall_at_k": round(head["recall"], 4), "epsilon_curve": curves[KERNEL_BATCHED],
                        "plain_fp32": {"qps": round(plain["qps"], 1), "epsilon": plain["epsilon"],
                                       "recall_at_k": round(plain["recall"], 4),

@@ -433,12 +433,37 @@ graph_search_exact_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_
         uint32_t nnew = 0;
         for (int w = 0; w < kExactWarps; w++) nnew += s.warp_cnt[w];
         // distances
-        for (uint32_t b = (uint32_t)(warp * (32 / G)); b < nnew; b += ngroups) {
-          uint32_t i = b + (uint32_t)(lane / G);
-          bool valid = i < nnew;
-          uint32_t v = valid ? nid[i] : 0u;
-          float d = group_distance<OT, M>(qv, g.objects + (size_t)v * rc, (int)rc, gl, G);
-          if (valid && gl == 0) nd[i] = d;
+        if (rc <= (uint32_t)G) {
+          // one 16-byte chunk per lane per row: U rows per group in flight
+          constexpr int U = 4;
+          const uint4 q1 = (uint32_t)gl < rc ? qv[gl] : make_uint4(0, 0, 0, 0);
+          const uint32_t step = (uint32_t)ngroups;
+          for (uint32_t b = (uint32_t)(warp * (32 / G)); b < nnew; b += step * U) {
+            uint4 xv[U];
+            uint32_t iu[U];
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+              iu[u] = b + u * step + (uint32_t)(lane / G);
+              uint32_t v = iu[u] < nnew ? nid[iu[u]] : 0u;
+              xv[u] = (uint32_t)gl < rc ? __ldg(g.objects + (size_t)v * rc + gl) : make_uint4(0, 0, 0, 0);
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+              Acc<OT, M> acc;
+              if ((uint32_t)gl < rc) acc.add(q1, xv[u], gl);
+              acc.reduce(G);
+              float d = acc.finish();
+              if (iu[u] < nnew && gl == 0) nd[iu[u]] = d;
+            }
+          }
+        } else {
+          for (uint32_t b = (uint32_t)(warp * (32 / G)); b < nnew; b += ngroups) {
+            uint32_t i = b + (uint32_t)(lane / G);
+            bool valid = i < nnew;
+            uint32_t v = valid ? nid[i] : 0u;
+            float d = group_distance<OT, M>(qv, g.objects + (size_t)v * rc, (int)rc, gl, G);
+            if (valid && gl == 0) nd[i] = d;
+          }
         }
         __syncthreads();
         // sequential replay of the result-set updates (warp 0)

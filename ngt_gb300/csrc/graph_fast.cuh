@@ -101,7 +101,7 @@ __device__ __forceinline__ uint32_t warp_lower_bound(const unsigned long long* a
 }
 
 template <ObjType ST, ObjType OT, Metric M>
-__global__ void __launch_bounds__(kFastThreads)
+__global__ void __launch_bounds__(kFastThreads, 5)
 graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint4* __restrict__ queries, uint32_t nq,
                          const QueryParams* __restrict__ params, const uint32_t* __restrict__ seed_list,
                          ObjDist* __restrict__ out, uint32_t* __restrict__ out_count, QueryStats* __restrict__ stats,
@@ -327,25 +327,66 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
         break;
       }
       expansions += np;
-      // gather unvisited neighbours of the parents, in edge order
+      // gather unvisited neighbours of the parents, in edge order.  All edge
+      // loads are issued before any visited-bit atomic, and all atomics before
+      // any compaction, so the gather costs a few memory round trips, not one
+      // per 32 edges.
       const uint32_t per_parent = min(P.edge_size, NB / np);
+      uint32_t pe0 = 0, pne = 0;
+      if ((uint32_t)lane < np) {
+        const uint32_t v = w.parents[lane];
+        const uint32_t a = g.offsets[v];
+        pe0 = a;
+        pne = min(g.offsets[v + 1] - a, per_parent);
+      }
+      uint32_t incl = pne;
+#pragma unroll
+      for (int off = 1; off < 8; off <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= off) incl += t;
+      }
+      const uint32_t total = __shfl_sync(0xffffffffu, incl, np - 1);
+      uint32_t pstart[8], pbase[8];
+#pragma unroll
+      for (int p2 = 0; p2 < 8; p2++) {
+        pstart[p2] = __shfl_sync(0xffffffffu, incl - pne, p2);
+        pbase[p2] = __shfl_sync(0xffffffffu, pe0, p2);
+      }
+      edges_read += total;
       uint32_t cnt = 0;
-      for (uint32_t pi = 0; pi < np; pi++) {
-        const uint32_t v = w.parents[pi];
-        const uint32_t e0 = g.offsets[v];
-        const uint32_t ne = min(g.offsets[v + 1] - e0, per_parent);
-        edges_read += ne;
-        for (uint32_t b = 0; b < ne; b += 32) {
-          uint32_t t = b + lane;
-          bool fresh = false;
-          uint32_t id = 0;
-          if (t < ne) {
-            id = __ldg(g.edges + e0 + t);
-            uint32_t bit = 1u << (id & 31u);
-            fresh = (atomicOr(&bitmap[id >> 5], bit) & bit) == 0u;
+      constexpr int J = 8;
+      for (uint32_t base0 = 0; base0 < total; base0 += 32 * J) {
+        uint32_t ids[J];
+        bool fresh[J];
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+          uint32_t t = base0 + lane + 32 * j;
+          ids[j] = 0;
+          if (t < total) {
+            int p2 = 0;
+#pragma unroll
+            for (int c = 1; c < 8; c++)
+              if ((uint32_t)c < np && t >= pstart[c]) p2 = c;
+            uint32_t b2 = 0, s2 = 0;
+#pragma unroll
+            for (int c = 0; c < 8; c++)
+              if (c == p2) { b2 = pbase[c]; s2 = pstart[c]; }
+            ids[j] = __ldg(g.edges + b2 + (t - s2));
           }
-          unsigned bal = __ballot_sync(0xffffffffu, fresh);
-          if (fresh) nid[cnt + __popc(bal & ((1u << lane) - 1u))] = id;
+        }
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+          uint32_t t = base0 + lane + 32 * j;
+          fresh[j] = false;
+          if (t < total) {
+            uint32_t bit = 1u << (ids[j] & 31u);
+            fresh[j] = (atomicOr(&bitmap[ids[j] >> 5], bit) & bit) == 0u;
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+          unsigned bal = __ballot_sync(0xffffffffu, fresh[j]);
+          if (fresh[j]) nid[cnt + __popc(bal & ((1u << lane) - 1u))] = ids[j];
           cnt += __popc(bal);
         }
       }
@@ -360,13 +401,9 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       uint32_t kept = 0;
       const uint32_t gpw = 32 / SG;
       unsigned long long smin = spill_min;
-      for (uint32_t b = 0; b < cnt; b += gpw) {
-        uint32_t i = b + (uint32_t)(lane / SG);
-        bool valid = i < cnt;
-        uint32_t id = valid ? nid[i] : 0u;
-        float d = group_distance<ST, M>(qs, srows + (size_t)id * sc, (int)sc, sgl, SG);
+      auto place = [&](uint32_t i, float d, uint32_t id) {
         unsigned long long key = pack_key(d, id);
-        bool live = valid && sgl == 0 && d <= insert_limit;
+        bool live = i < cnt && sgl == 0 && d <= insert_limit;
         bool keep = live && key < worst;
         bool spl = live && key >= worst;
         unsigned bal = __ballot_sync(0xffffffffu, keep), bs = __ballot_sync(0xffffffffu, spl);
@@ -378,6 +415,35 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
         }
         kept += __popc(bal);
         spill_n += __popc(bs);
+      };
+      if (sc <= (uint32_t)SG) {
+        // one 16-byte chunk per lane per row: U rows per group in flight
+        constexpr int U = 8;
+        const uint4 qv = (uint32_t)sgl < sc ? qs[sgl] : make_uint4(0, 0, 0, 0);
+        for (uint32_t b = 0; b < cnt; b += gpw * U) {
+          uint4 xv[U];
+          uint32_t idu[U];
+#pragma unroll
+          for (int u = 0; u < U; u++) {
+            uint32_t i = b + u * gpw + (uint32_t)(lane / SG);
+            idu[u] = i < cnt ? nid[i] : 0u;
+            xv[u] = (uint32_t)sgl < sc ? __ldg(srows + (size_t)idu[u] * sc + sgl) : make_uint4(0, 0, 0, 0);
+          }
+#pragma unroll
+          for (int u = 0; u < U; u++) {
+            Acc<ST, M> acc;
+            if ((uint32_t)sgl < sc) acc.add(qv, xv[u], sgl);
+            acc.reduce(SG);
+            place(b + u * gpw + (uint32_t)(lane / SG), acc.finish(), idu[u]);
+          }
+        }
+      } else {
+        for (uint32_t b = 0; b < cnt; b += gpw) {
+          uint32_t i = b + (uint32_t)(lane / SG);
+          uint32_t id = i < cnt ? nid[i] : 0u;
+          float d = group_distance<ST, M>(qs, srows + (size_t)id * sc, (int)sc, sgl, SG);
+          place(i, d, id);
+        }
       }
       for (int off = 16; off > 0; off >>= 1) {
         unsigned long long o = __shfl_xor_sync(0xffffffffu, smin, off);
