@@ -61,6 +61,9 @@ def parse():
     ap.add_argument("--k", type=int, default=10)
     ap.add_argument("--workdir", default=os.environ.get("NGT_BENCH_DIR", "/tmp/ngt_bench"))
     ap.add_argument("--cpu-sample", type=int, default=2000, help="queries in the CPU-baseline sample")
+    ap.add_argument("--served-rates", type=lambda s: [int(x) for x in s.split(",")], default=[5000, 20000, 50000],
+                    help="offered query rates of the serving measurement")
+    ap.add_argument("--served-seconds", type=float, default=2.0, help="length of each served-rate run")
     return ap.parse_args()
 
 
@@ -168,6 +171,62 @@ def measured_peaks():
         d = json.load(open(p))
         return d.get("hbm_gbs", 6800.0), "measured"
     return 6800.0, "fallback"
+
+
+def served_latency(ix, queries, k, eps, rates, seconds):
+    """Poisson arrivals of requests (sizes geometric on 1..256, mean ~16 queries) at each
+    target query rate through the serving loop; p50/p99 request latency (submit to completion)."""
+    import threading
+    from ngt_gb300 import Server
+    out = []
+    rng = np.random.default_rng(43)
+    with Server(ix, max_batch=4096, inflight=3, max_k=max(16, k)) as srv:
+        for rate in rates:
+            sizes, gaps = [], []
+            t = 0.0
+            while t < seconds:
+                n = int(min(256, rng.geometric(1.0 / 16.0)))
+                sizes.append(n)
+                gap = rng.exponential(n / rate)
+                gaps.append(gap)
+                t += gap
+            tickets = []
+            done = threading.Event()
+            lat = []
+
+            def waiter():
+                i = 0
+                while True:
+                    while i >= len(tickets):
+                        if done.is_set() and i >= len(tickets):
+                            return
+                        time.sleep(0.0002)
+                    lat.append(srv.wait(tickets[i])[3])
+                    i += 1
+
+            th = threading.Thread(target=waiter)
+            th.start()
+            t0 = time.perf_counter()
+            nxt = t0
+            pos = 0
+            total = 0
+            for n, gap in zip(sizes, gaps):
+                nxt += gap
+                while time.perf_counter() < nxt:
+                    pass
+                q = queries[pos:pos + n] if pos + n <= len(queries) else queries[:n]
+                pos = (pos + n) % max(1, len(queries) - 256)
+                tickets.append(srv.submit(q, k=k, epsilon=eps))
+                total += n
+            done.set()
+            th.join()
+            wall = time.perf_counter() - t0
+            lat_np = np.array(lat)
+            out.append({"offered_qps": rate, "achieved_qps": round(total / wall, 1), "requests": len(sizes),
+                        "p50_ms": round(float(np.percentile(lat_np, 50)), 3),
+                        "p99_ms": round(float(np.percentile(lat_np, 99)), 3)})
+            log("served at %d q/s offered: %s" % (rate, out[-1]))
+    return out
 
 
 def cpu_baseline(path, queries, eps, k, sample, threads):
@@ -366,6 +425,10 @@ def main():
     h2d = hq.nbytes
     d2h = nq * (int(np.ceil(k * (1 + head["epsilon"]))) + 1) * 8 + nq * 4 + nq * QUERY_STATS_DTYPE.itemsize
 
+    # ---- served: continuous batching under a Poisson request stream ------------------------------
+    served = served_latency(ix, queries, k, head["epsilon"], args.served_rates, args.served_seconds) \
+        if args.served_seconds > 0 else None
+
     # ---- CPU baseline (oracle port on a bounded sample) ------------------------------------------
     cpu = None
     if rank == 0:
@@ -396,6 +459,7 @@ def main():
                          "frac": round(head["achieved_gbs"] / peak, 4), "traffic": None, "peak_source": peak_kind,
                          "basis": "(%d*DC + 4*edges + %d query + re-rank %d*2k) bytes per query over the kernel's "
                                   "median event time" % (head["row_bytes"], row_bytes, row_bytes)},
+            "served": served,
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

@@ -82,6 +82,26 @@ bool ngtgpu_search_exact_noalloc(NGTIndex, const void *d_rows, size_t nq, const 
                                  size_t nparams, NGTObjectDistance *d_results, size_t kmax, uint32_t *d_counts,
                                  NGTGPUQueryStats *d_stats, void *stream, NGTError);
 
+/* Serving loop (continuous batching).  A server keeps up to `inflight`
+ * batched-kernel launches on the GPU at once, each on its own stream and
+ * scratch set; requests submitted from any thread while others run join the
+ * next launch that has room (`max_batch_queries` queries per launch), so their
+ * work overlaps on the device.  A request holds 1..max_batch_queries queries
+ * with one parameter block or one per query, result sizes up to max_k.
+ * ngtgpu_server_submit copies the queries and returns a ticket (>= 0, or -1 on
+ * error); ngtgpu_server_wait blocks until that request completed, writes its
+ * results (results[q*kmax ..], counts[q]) and its latency from submission to
+ * completion in milliseconds.  A request's results do not depend on what else
+ * is in flight. */
+typedef void *NGTGPUServer;
+NGTGPUServer ngtgpu_server_create(NGTIndex, uint32_t max_batch_queries, uint32_t inflight, uint32_t max_k,
+                                  NGTError);
+int64_t ngtgpu_server_submit(NGTGPUServer, const float *queries, size_t nq, int32_t dim,
+                             const NGTQueryParameters *params, size_t nparams, NGTError);
+bool ngtgpu_server_wait(NGTGPUServer, int64_t ticket, NGTObjectDistance *results, size_t kmax, uint32_t *counts,
+                        double *latency_ms, NGTError);
+void ngtgpu_server_destroy(NGTGPUServer);
+
 /* Number of kernel launches issued by this index since it was opened. */
 uint64_t ngtgpu_kernel_launches(NGTIndex, NGTError);
 

@@ -96,6 +96,12 @@ def load_library() -> ctypes.CDLL:
                                         c_size_t, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p], c_bool),
         "ngtgpu_kernel_launches": ([c_void_p, c_void_p], c_uint64),
         "ngtgpu_set_batched_tuning": ([c_void_p, c_uint32, c_uint32, c_float, c_void_p], c_bool),
+        "ngtgpu_server_create": ([c_void_p, c_uint32, c_uint32, c_uint32, c_void_p], c_void_p),
+        "ngtgpu_server_submit": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QueryParameters), c_size_t,
+                                  c_void_p], ctypes.c_int64),
+        "ngtgpu_server_wait": ([c_void_p, ctypes.c_int64, c_void_p, c_size_t, c_void_p, POINTER(ctypes.c_double),
+                                c_void_p], c_bool),
+        "ngtgpu_server_destroy": ([c_void_p], None),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -237,3 +243,61 @@ class Index:
         ok = self._lib.ngtgpu_search_batch_device(self._index, d_rows, nq, params, nparams, d_results, kmax,
                                                   d_counts, d_stats, stream or None, kernel, self._err)
         self._check(ok)
+
+
+class Server:
+    """Continuous-batching serving loop over an open Index (ngtgpu_server_*)."""
+
+    def __init__(self, index: Index, max_batch: int = 4096, inflight: int = 3, max_k: int = 128):
+        self._ix = index
+        self._lib = index._lib
+        self._err = self._lib.ngt_create_error_object()
+        self._srv = self._lib.ngtgpu_server_create(index._index, max_batch, inflight, max_k, self._err)
+        if not self._srv:
+            raise NativeError(self._lib.ngt_get_error_string(self._err).decode())
+        self.max_k = max_k
+        self._pending = {}
+
+    def submit(self, queries, k=10, epsilon=0.1, radius=-1.0, edge_size=None) -> int:
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        if q.ndim == 1:
+            q = q[None, :]
+        params, n = Index.make_params(k, epsilon, radius, edge_size)
+        t = self._lib.ngtgpu_server_submit(self._srv, q.ctypes.data, q.shape[0], q.shape[1], params, n, self._err)
+        if t < 0:
+            raise NativeError(self._lib.ngt_get_error_string(self._err).decode())
+        self._pending[t] = q.shape[0]
+        return t
+
+    def wait(self, ticket: int, kmax: int | None = None):
+        nq = self._pending.pop(ticket)
+        kmax = kmax or self.max_k
+        res = np.zeros((nq, kmax), RESULT_DTYPE)
+        counts = np.zeros(nq, np.uint32)
+        lat = ctypes.c_double(0.0)
+        ok = self._lib.ngtgpu_server_wait(self._srv, ticket, res.ctypes.data, kmax, counts.ctypes.data,
+                                          ctypes.byref(lat), self._err)
+        if not ok:
+            raise NativeError(self._lib.ngt_get_error_string(self._err).decode())
+        m = int(counts.max()) if nq else 0
+        return res["id"][:, :m].copy(), res["distance"][:, :m].copy(), counts, lat.value
+
+    def close(self):
+        if getattr(self, "_srv", None):
+            self._lib.ngtgpu_server_destroy(self._srv)
+            self._srv = None
+        if getattr(self, "_err", None):
+            self._lib.ngt_destroy_error_object(self._err)
+            self._err = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -109,15 +109,25 @@ struct Acc {
     }
   }
 
+  // Which accumulators a metric uses (only those are reduced across lanes).
+  static constexpr bool kUint8Sq = OT == ObjType::Uint8 && (M == Metric::L2 || M == Metric::InnerProduct);
+  static constexpr bool kUseI0 = kUint8Sq || (OT == ObjType::Uint8 && M == Metric::L1) || M == Metric::Hamming ||
+                                 M == Metric::Jaccard;
+  static constexpr bool kUseI1 = kUint8Sq || M == Metric::Jaccard;
+  static constexpr bool kUseF0 = !kUseI0;
+  static constexpr bool kUseF12 = !kUseI0 && (M == Metric::Cosine || M == Metric::Angle || M == Metric::Poincare);
+
   __device__ __forceinline__ void reduce(int width) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       if (off < width) {
-        f0 += __shfl_xor_sync(0xffffffffu, f0, off);
-        f1 += __shfl_xor_sync(0xffffffffu, f1, off);
-        f2 += __shfl_xor_sync(0xffffffffu, f2, off);
-        i0 += __shfl_xor_sync(0xffffffffu, i0, off);
-        i1 += __shfl_xor_sync(0xffffffffu, i1, off);
+        if constexpr (kUseF0) f0 += __shfl_xor_sync(0xffffffffu, f0, off);
+        if constexpr (kUseF12) {
+          f1 += __shfl_xor_sync(0xffffffffu, f1, off);
+          f2 += __shfl_xor_sync(0xffffffffu, f2, off);
+        }
+        if constexpr (kUseI0) i0 += __shfl_xor_sync(0xffffffffu, i0, off);
+        if constexpr (kUseI1) i1 += __shfl_xor_sync(0xffffffffu, i1, off);
       }
     }
   }

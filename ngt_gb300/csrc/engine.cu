@@ -104,9 +104,11 @@ GraphEngine::~GraphEngine() {
   cudaFree(d_seed_ids_);
   cudaFree(d_bitmaps_);
   cudaFree(d_overflow_);
-  cudaFree(d_fast_bitmaps_);
-  cudaFree(d_fast_spill_);
-  cudaFree(d_work_);
+  for (auto& sc : fast_scratch_) {
+    cudaFree(sc.bitmaps);
+    cudaFree(sc.spill);
+    cudaFree(sc.work);
+  }
   cudaFree(d_bf16_);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -341,20 +343,30 @@ bool GraphEngine::fast_supported(Kernel k) const {
   return fast_kernel(host_.prop.otype, host_.prop.metric, k == Kernel::Fast) != nullptr;
 }
 
-void GraphEngine::ensure_fast_scratch(size_t slots) {
-  if (slots <= fast_slots_) return;
-  NGT_CUDA(cudaStreamSynchronize(stream_));
-  cudaFree(d_fast_bitmaps_);
-  cudaFree(d_fast_spill_);
-  d_fast_bitmaps_ = nullptr;
-  d_fast_spill_ = nullptr;
+void GraphEngine::ensure_fast_scratch(FastScratch& sc, size_t slots, cudaStream_t stream) {
+  if (slots <= sc.slots) return;
+  NGT_CUDA(cudaStreamSynchronize(stream));   // earlier launches on this set may still use it
+  cudaFree(sc.bitmaps);
+  cudaFree(sc.spill);
+  sc.bitmaps = nullptr;
+  sc.spill = nullptr;
   size_t words = ((host_.nrows + 31) / 32 + 3) / 4 * 4;
-  NGT_CUDA(cudaMalloc(&d_fast_bitmaps_, slots * words * 4));
-  NGT_CUDA(cudaMalloc(&d_fast_spill_, slots * 2 * (size_t)kSpillCapacity * 8));
-  NGT_CUDA(cudaMemsetAsync(d_fast_bitmaps_, 0, slots * words * 4, stream_));
-  if (!d_work_) NGT_CUDA(cudaMalloc(&d_work_, 16));
-  NGT_CUDA(cudaStreamSynchronize(stream_));
-  fast_slots_ = slots;
+  NGT_CUDA(cudaMalloc(&sc.bitmaps, slots * words * 4));
+  NGT_CUDA(cudaMalloc(&sc.spill, slots * 2 * (size_t)kSpillCapacity * 8));
+  NGT_CUDA(cudaMemsetAsync(sc.bitmaps, 0, slots * words * 4, stream));
+  if (!sc.work) NGT_CUDA(cudaMalloc(&sc.work, 16));
+  NGT_CUDA(cudaStreamSynchronize(stream));
+  sc.slots = slots;
+}
+
+void GraphEngine::reserve_scratch_sets(size_t n) {
+  std::lock_guard<std::mutex> lock(mu_);
+  if (fast_scratch_.size() < n) fast_scratch_.resize(n);
+}
+
+size_t GraphEngine::batched_scratch_bytes(size_t nq) const {
+  size_t words = ((host_.nrows + 31) / 32 + 3) / 4 * 4;
+  return nq * (words * 4 + 2 * (size_t)kSpillCapacity * 8) + nq * (sizeof(QueryParams) + 64);
 }
 
 void GraphEngine::ensure_bf16_rows() {
@@ -386,9 +398,35 @@ void GraphEngine::search_device(const uint4* d_rows, size_t nq, const SearchArgs
   if (kernel == Kernel::Exact)
     launch_exact(d_rows, nq, d_params, d_seeds, max_size, d_out, d_counts, d_stats, stream);
   else
-    launch_fast(d_rows, nq, d_params, d_seeds, max_size, d_out, d_counts, d_stats, stream, kernel);
+    launch_fast(d_rows, nq, d_params, d_seeds, max_size, d_out, d_counts, d_stats, stream, kernel,
+                fast_scratch_[0]);
   NGT_CUDA(cudaFreeAsync(d_params, stream));
   NGT_CUDA(cudaFreeAsync(d_seeds, stream));
+}
+
+void GraphEngine::search_device_slot(const uint4* d_rows, size_t nq, const SearchArgs* args, size_t nargs,
+                                     ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, size_t kmax,
+                                     cudaStream_t stream, size_t slot) {
+  std::lock_guard<std::mutex> lock(mu_);
+  NGT_CUDA(cudaSetDevice(device_));
+  if (nq == 0) return;
+  if (slot == 0 || slot >= fast_scratch_.size()) throw std::runtime_error("invalid scratch set");
+  if (!fast_supported(Kernel::Fast)) throw std::runtime_error("the batched kernel does not support this index type");
+  std::vector<QueryParams> params;
+  std::vector<uint32_t> seeds;
+  uint32_t max_size = 0;
+  build_params(args, nargs, nq, kmax, params, seeds, max_size);
+  QueryParams* d_params = nullptr;
+  uint32_t* d_seeds = nullptr;
+  NGT_CUDA(cudaMallocAsync(&d_params, nq * sizeof(QueryParams), stream));
+  NGT_CUDA(cudaMallocAsync(&d_seeds, seeds.size() * 4, stream));
+  NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QueryParams), cudaMemcpyHostToDevice, stream));
+  NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, stream));
+  launch_fast(d_rows, nq, d_params, d_seeds, max_size, d_out, d_counts, d_stats, stream, Kernel::Fast,
+              fast_scratch_[slot]);
+  NGT_CUDA(cudaFreeAsync(d_params, stream));
+  NGT_CUDA(cudaFreeAsync(d_seeds, stream));
+  // the pageable host parameter copies above are complete once they return
 }
 
 void GraphEngine::launch_exact(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
@@ -429,7 +467,7 @@ void GraphEngine::launch_exact(const uint4* d_rows, size_t nq, const QueryParams
 
 void GraphEngine::launch_fast(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
                               uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats,
-                              cudaStream_t stream, Kernel kernel) {
+                              cudaStream_t stream, Kernel kernel, FastScratch& scratch) {
   const bool bf16 = kernel == Kernel::Fast && host_.prop.otype == ObjType::Float;
   FastKernelFn fn = fast_kernel(host_.prop.otype, host_.prop.metric, bf16);
   if (!fn) throw std::runtime_error("the batched kernel does not support this index type");
@@ -460,11 +498,12 @@ void GraphEngine::launch_fast(const uint4* d_rows, size_t nq, const QueryParams*
   NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kFastThreads, smem));
   NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
   size_t grid = std::min<size_t>((nq + kFastWarps - 1) / kFastWarps, (size_t)std::max(1, per_sm) * sms);
-  ensure_fast_scratch(grid * kFastWarps);
-  NGT_CUDA(cudaMemsetAsync(d_work_, 0, 4, stream));
+  ensure_fast_scratch(scratch, grid * kFastWarps, stream);
+  NGT_CUDA(cudaMemsetAsync(scratch.work, 0, 4, stream));
   const uint4* srows = bf16 ? static_cast<const uint4*>(d_bf16_) : dev_.objects;
   fn<<<(unsigned)grid, kFastThreads, smem, stream>>>(dev_, srows, d_rows, (uint32_t)nq, d_params, d_seeds, d_out,
-                                                      d_counts, d_stats, d_fast_bitmaps_, d_work_, d_fast_spill_, cfg);
+                                                      d_counts, d_stats, scratch.bitmaps, scratch.work,
+                                                      scratch.spill, cfg);
   NGT_CUDA(cudaGetLastError());
   launches_++;
 }

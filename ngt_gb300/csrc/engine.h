@@ -73,6 +73,13 @@ class GraphEngine {
   void search_device(const uint4* d_rows, size_t nq, const SearchArgs* args, size_t nargs, ObjDist* d_out,
                      uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream,
                      Kernel kernel = Kernel::Exact);
+  // The batched kernel with scratch set `slot` (1 .. scratch_sets-1 are free for
+  // concurrent launches on different streams; slot 0 belongs to search_device).
+  void search_device_slot(const uint4* d_rows, size_t nq, const SearchArgs* args, size_t nargs, ObjDist* d_out,
+                          uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream, size_t slot);
+  void reserve_scratch_sets(size_t n);
+  // Bytes of device scratch one batched launch of nq queries uses (admission).
+  size_t batched_scratch_bytes(size_t nq) const;
   // The exact search with every scratch buffer carved from the caller-provided
   // device memory `scratch` (scratch_bytes long) instead of allocated: query
   // parameters, seed lists, per-CTA visited bitmaps and overflow tiers.  Throws
@@ -96,19 +103,28 @@ class GraphEngine {
   uint64_t launches() const { return launches_; }
 
  private:
+  // Scratch of the batched kernel: one visited bitmap and one spill tier
+  // (2 x kSpillCapacity keys) per warp slot, and the work counter.  Set 0 serves
+  // search_device; the serving loop owns one set per in-flight launch.
+  struct FastScratch {
+    uint32_t* bitmaps = nullptr;
+    unsigned long long* spill = nullptr;
+    uint32_t* work = nullptr;
+    size_t slots = 0;
+  };
   void upload();
   uint32_t seed_table(size_t seed_size);        // index of the thinned-seed table
   void build_params(const SearchArgs* args, size_t nargs, size_t nq, size_t kmax, std::vector<QueryParams>& params,
                     std::vector<uint32_t>& seed_list, uint32_t& max_size);
   size_t edge_size_for(const SearchArgs& a) const;
   void ensure_scratch(size_t grid);
-  void ensure_fast_scratch(size_t slots);
+  void ensure_fast_scratch(FastScratch& sc, size_t slots, cudaStream_t stream);
   void ensure_bf16_rows();
   void launch_exact(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
                     uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, cudaStream_t stream);
   void launch_fast(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
                    uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, cudaStream_t stream,
-                   Kernel kernel);
+                   Kernel kernel, FastScratch& scratch);
 
   HostIndex host_;
   GraphMode mode_;
@@ -133,11 +149,8 @@ class GraphEngine {
   unsigned long long* d_overflow_ = nullptr;
   size_t bitmap_grid_ = 0;
   static constexpr uint32_t kOverflowCapacity = 65536;   // candidate keys per CTA beyond shared memory
-  uint32_t* d_fast_bitmaps_ = nullptr;                    // one visited bitmap per warp slot
-  unsigned long long* d_fast_spill_ = nullptr;            // spill tier per warp slot (2 x kSpillCapacity)
   static constexpr uint32_t kSpillCapacity = 32768;
-  size_t fast_slots_ = 0;
-  uint32_t* d_work_ = nullptr;                            // work counter of the batched kernel
+  std::vector<FastScratch> fast_scratch_ = std::vector<FastScratch>(1);
   void* d_bf16_ = nullptr;                                // bf16 copy of float object rows
   FastTuning tuning_;
   DevGraph dev_;

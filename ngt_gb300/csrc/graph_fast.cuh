@@ -89,6 +89,27 @@ __device__ __forceinline__ void warp_bitonic_sort(unsigned long long* a, uint32_
   }
 }
 
+// Ascending sort of a[0..n), n <= 32, in registers (one key per lane, shuffle
+// bitonic network), written back to a.
+__device__ __forceinline__ void warp_sort32(unsigned long long* a, uint32_t n, int lane) {
+  unsigned long long x = (uint32_t)lane < n ? a[lane] : ~0ull;
+#pragma unroll
+  for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      unsigned long long y = __shfl_xor_sync(0xffffffffu, x, j);
+      bool lower = (lane & j) == 0;
+      bool up = (lane & k) == 0;
+      // keep the smaller key in the lower lane of an ascending pair
+      bool take_min = lower == up;
+      x = take_min ? (y < x ? y : x) : (y > x ? y : x);
+    }
+  }
+  __syncwarp();
+  if ((uint32_t)lane < n) a[lane] = x;
+  __syncwarp();
+}
+
 // Number of entries of the sorted a[0..n) that are < x (ignoring the expanded bit of a's entries
 // is not needed: keys are ordered by distance first, the bit only reorders exact distance ties).
 __device__ __forceinline__ uint32_t warp_lower_bound(const unsigned long long* a, uint32_t n, unsigned long long x) {
@@ -453,7 +474,8 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       if (spill_n > cfg.spill_cap) { spill_n = cfg.spill_cap; status |= kStatusCandidateOverflow; }
       __syncwarp();
       if (kept == 0) continue;
-      warp_bitonic_sort(nkey, kept, lane);
+      if (kept <= 32) warp_sort32(nkey, kept, lane);
+      else warp_bitonic_sort(nkey, kept, lane);
       // In-place merge of nkey[0..kept) into list[0..n), keeping the first L.
       // 1. merged positions of the new keys (list entries compare without their
       //    expanded bit), parked in nid (no longer needed)
@@ -472,8 +494,9 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       //    read completely before any of it is written; unexpanded entries pushed
       //    past the end join the spill tier
       unsigned long long emin = ~0ull;
-      for (int hi = (int)n; hi > 0; hi -= 32) {
+      for (int hi = (int)n; hi > (int)first_new; hi -= 32) {
         int idx = hi - 32 + lane;
+        if (idx < (int)first_new) idx = -1;          // below the first insertion: unchanged
         unsigned long long k = 0;
         uint32_t pos = 0xffffffffu;
         if (idx >= 0) {

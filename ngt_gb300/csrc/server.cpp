@@ -1,0 +1,346 @@
+// Serving loop: continuous batching of search requests over one opened index.
+//
+// The index (objects, graph, seeds) stays resident in HBM.  Callers submit
+// requests of any size (up to the batch capacity) with their own k / epsilon /
+// radius / edge size, from any thread.  A dispatcher thread keeps up to
+// `inflight` batched-kernel launches on the device at once, each on its own
+// stream with its own scratch set; whenever a launch slot is free and requests
+// are waiting, it admits the waiting requests in arrival order (as many as fit
+// the slot's query capacity), uploads them, launches, and queues the result
+// download -- so requests arriving while others run join the next launch and
+// overlap with them on the GPU.  Completed launches are harvested by polling
+// their events; each request's latency is measured from submit to completion.
+// A request's results depend only on its queries and parameters (the batched
+// kernel handles every query independently), so they are the same alone and
+// in any mix.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <sstream>
+#include <stdexcept>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "engine.h"
+
+extern "C" {
+#include "../../include/ngtgpu.h"
+}
+
+namespace ngtg {
+
+namespace {
+
+#define SRV_CUDA(x)                                                                                \
+  do {                                                                                             \
+    cudaError_t e_ = (x);                                                                          \
+    if (e_ != cudaSuccess)                                                                         \
+      throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e_) + " in " #x);    \
+  } while (0)
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+  int64_t ticket = 0;
+  std::vector<uint8_t> rows;          // converted query rows
+  size_t nq = 0;
+  std::vector<SearchArgs> args;       // 1 or nq entries
+  size_t kmax = 0;
+  Clock::time_point arrival;
+  std::vector<ObjDist> results;       // nq * kmax
+  std::vector<uint32_t> counts;
+  bool done = false;
+  std::string error;
+  double latency_ms = 0.0;
+};
+
+struct Lane {
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done_event = nullptr;
+  size_t slot = 0;                    // scratch set of the engine
+  uint4* d_rows = nullptr;
+  ObjDist* d_out = nullptr;
+  uint32_t* d_counts = nullptr;
+  QueryStats* d_stats = nullptr;
+  uint8_t* h_rows = nullptr;          // pinned staging
+  ObjDist* h_out = nullptr;
+  uint32_t* h_counts = nullptr;
+  bool busy = false;
+  size_t kmax = 0;
+  std::vector<std::shared_ptr<Request>> batch;
+};
+
+}  // namespace
+
+class Server {
+ public:
+  Server(GraphEngine* e, size_t max_batch, size_t inflight, size_t max_k)
+      : e_(e), max_batch_(max_batch), max_k_(max_k), row_bytes_(e->host().row_bytes()) {
+    if (max_batch == 0 || inflight == 0 || max_k == 0) throw std::runtime_error("invalid server sizes");
+    SRV_CUDA(cudaSetDevice(e->device()));
+    e->reserve_scratch_sets(inflight + 1);
+    lanes_.resize(inflight);
+    for (size_t i = 0; i < inflight; i++) {
+      Lane& l = lanes_[i];
+      l.slot = i + 1;
+      SRV_CUDA(cudaStreamCreateWithFlags(&l.stream, cudaStreamNonBlocking));
+      SRV_CUDA(cudaEventCreateWithFlags(&l.done_event, cudaEventDisableTiming));
+      SRV_CUDA(cudaMalloc(&l.d_rows, max_batch * row_bytes_));
+      SRV_CUDA(cudaMalloc(&l.d_out, max_batch * max_k * sizeof(ObjDist)));
+      SRV_CUDA(cudaMalloc(&l.d_counts, max_batch * 4));
+      SRV_CUDA(cudaMalloc(&l.d_stats, max_batch * sizeof(QueryStats)));
+      SRV_CUDA(cudaMallocHost(&l.h_rows, max_batch * row_bytes_));
+      SRV_CUDA(cudaMallocHost(&l.h_out, max_batch * max_k * sizeof(ObjDist)));
+      SRV_CUDA(cudaMallocHost(&l.h_counts, max_batch * 4));
+    }
+    worker_ = std::thread([this] { run(); });
+  }
+
+  ~Server() {
+    {
+      std::lock_guard<std::mutex> lock(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    if (worker_.joinable()) worker_.join();
+    cudaSetDevice(e_->device());
+    for (Lane& l : lanes_) {
+      if (l.stream) cudaStreamSynchronize(l.stream);
+      cudaFree(l.d_rows);
+      cudaFree(l.d_out);
+      cudaFree(l.d_counts);
+      cudaFree(l.d_stats);
+      cudaFreeHost(l.h_rows);
+      cudaFreeHost(l.h_out);
+      cudaFreeHost(l.h_counts);
+      if (l.done_event) cudaEventDestroy(l.done_event);
+      if (l.stream) cudaStreamDestroy(l.stream);
+    }
+  }
+
+  int64_t submit(const float* queries, size_t nq, size_t dim, const SearchArgs* args, size_t nargs) {
+    if (nq == 0 || nq > max_batch_)
+      throw std::runtime_error("request size must be 1.." + std::to_string(max_batch_) + " queries");
+    if (!(nargs == 1 || nargs == nq)) throw std::runtime_error("parameters must be 1 or one per query");
+    auto r = std::make_shared<Request>();
+    e_->convert_queries(queries, QueryType::Float32, nq, dim, r->rows);
+    r->nq = nq;
+    r->args.assign(args, args + nargs);
+    size_t kmax = 1;
+    for (const auto& a : r->args) kmax = std::max(kmax, e_->output_size(a));
+    if (kmax > max_k_) throw std::runtime_error("result size above the server's maximum " + std::to_string(max_k_));
+    r->kmax = kmax;
+    r->arrival = Clock::now();
+    std::lock_guard<std::mutex> lock(mu_);
+    r->ticket = next_ticket_++;
+    pending_.push_back(r);
+    tickets_[r->ticket] = r;
+    cv_.notify_all();
+    return r->ticket;
+  }
+
+  void wait(int64_t ticket, ObjDist* out, size_t kmax, uint32_t* counts, double* latency_ms) {
+    std::shared_ptr<Request> r;
+    std::unique_lock<std::mutex> lock(mu_);
+    auto it = tickets_.find(ticket);
+    if (it == tickets_.end()) throw std::runtime_error("unknown ticket " + std::to_string(ticket));
+    r = it->second;
+    done_cv_.wait(lock, [&] { return r->done; });
+    tickets_.erase(ticket);
+    lock.unlock();
+    if (!r->error.empty()) throw std::runtime_error(r->error);
+    for (size_t q = 0; q < r->nq; q++) {
+      uint32_t n = r->counts[q];
+      if (n > kmax) throw std::runtime_error("kmax smaller than the results of the request");
+      counts[q] = n;
+      std::memcpy(out + q * kmax, r->results.data() + q * r->kmax, n * sizeof(ObjDist));
+    }
+    if (latency_ms) *latency_ms = r->latency_ms;
+  }
+
+ private:
+  // Dispatcher: harvest finished lanes, then admit waiting requests into free lanes.
+  void run() {
+    cudaSetDevice(e_->device());
+    while (true) {
+      bool any_busy = false;
+      for (Lane& l : lanes_) {
+        if (!l.busy) continue;
+        cudaError_t q = cudaEventQuery(l.done_event);
+        if (q == cudaErrorNotReady) {
+          any_busy = true;
+          continue;
+        }
+        finish(l, q == cudaSuccess ? std::string() : std::string(cudaGetErrorString(q)));
+      }
+      std::vector<std::shared_ptr<Request>> batch;
+      Lane* free_lane = nullptr;
+      {
+        std::unique_lock<std::mutex> lock(mu_);
+        if (stop_ && pending_.empty() && !any_busy) break;
+        for (Lane& l : lanes_)
+          if (!l.busy) { free_lane = &l; break; }
+        if (free_lane && !pending_.empty()) {
+          size_t total = 0;
+          while (!pending_.empty() && total + pending_.front()->nq <= max_batch_) {
+            total += pending_.front()->nq;
+            batch.push_back(pending_.front());
+            pending_.pop_front();
+          }
+        } else if (!any_busy) {
+          cv_.wait_for(lock, std::chrono::milliseconds(2), [&] { return stop_ || !pending_.empty(); });
+          continue;
+        }
+      }
+      if (!batch.empty()) {
+        launch(*free_lane, batch);
+      } else if (any_busy) {
+        std::this_thread::sleep_for(std::chrono::microseconds(20));
+      }
+    }
+  }
+
+  void launch(Lane& l, std::vector<std::shared_ptr<Request>>& batch) {
+    l.batch = batch;
+    l.kmax = 1;
+    size_t nq = 0;
+    std::vector<SearchArgs> args;
+    for (auto& r : batch) {
+      std::memcpy(l.h_rows + nq * row_bytes_, r->rows.data(), r->nq * row_bytes_);
+      for (size_t q = 0; q < r->nq; q++) args.push_back(r->args[r->args.size() == 1 ? 0 : q]);
+      nq += r->nq;
+      l.kmax = std::max(l.kmax, r->kmax);
+    }
+    try {
+      SRV_CUDA(cudaMemcpyAsync(l.d_rows, l.h_rows, nq * row_bytes_, cudaMemcpyHostToDevice, l.stream));
+      e_->search_device_slot(l.d_rows, nq, args.data(), args.size(), l.d_out, l.d_counts, l.d_stats, l.kmax,
+                             l.stream, l.slot);
+      SRV_CUDA(cudaMemcpyAsync(l.h_out, l.d_out, nq * l.kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, l.stream));
+      SRV_CUDA(cudaMemcpyAsync(l.h_counts, l.d_counts, nq * 4, cudaMemcpyDeviceToHost, l.stream));
+      SRV_CUDA(cudaEventRecord(l.done_event, l.stream));
+      l.busy = true;
+    } catch (std::exception& ex) {
+      l.busy = true;
+      finish(l, ex.what());
+    }
+  }
+
+  void finish(Lane& l, const std::string& err) {
+    auto now = Clock::now();
+    size_t off = 0;
+    for (auto& r : l.batch) {
+      if (err.empty()) {
+        r->results.resize(r->nq * r->kmax);
+        r->counts.resize(r->nq);
+        for (size_t q = 0; q < r->nq; q++) {
+          uint32_t n = std::min<uint32_t>(l.h_counts[off + q], (uint32_t)r->kmax);
+          r->counts[q] = n;
+          std::memcpy(r->results.data() + q * r->kmax, l.h_out + (off + q) * l.kmax, n * sizeof(ObjDist));
+        }
+      } else {
+        r->error = err;
+      }
+      off += r->nq;
+      r->latency_ms = std::chrono::duration<double, std::milli>(now - r->arrival).count();
+    }
+    {
+      std::lock_guard<std::mutex> lock(mu_);
+      for (auto& r : l.batch) r->done = true;
+    }
+    done_cv_.notify_all();
+    l.batch.clear();
+    l.busy = false;
+  }
+
+  GraphEngine* e_;
+  size_t max_batch_, max_k_, row_bytes_;
+  std::vector<Lane> lanes_;
+  std::deque<std::shared_ptr<Request>> pending_;
+  std::map<int64_t, std::shared_ptr<Request>> tickets_;
+  int64_t next_ticket_ = 0;
+  std::mutex mu_;
+  std::condition_variable cv_, done_cv_;
+  bool stop_ = false;
+  std::thread worker_;
+};
+
+}  // namespace ngtg
+
+namespace {
+void server_error(const char* fn, const std::string& msg, NGTError error) {
+  std::string s = std::string("Capi : ") + fn + "() : Error: " + msg;
+  if (error) *static_cast<std::string*>(error) = s;
+  else fprintf(stderr, "%s\n", s.c_str());
+}
+
+std::vector<ngtg::SearchArgs> server_args(const NGTQueryParameters* params, size_t nparams) {
+  std::vector<ngtg::SearchArgs> a(nparams);
+  for (size_t i = 0; i < nparams; i++) {
+    int es = (int)params[i].edge_size;
+    a[i].size = params[i].size;
+    a[i].epsilon = params[i].epsilon;
+    a[i].radius = params[i].radius < 0.0f ? 3.402823466e+38f : params[i].radius;
+    a[i].edge_size = es == INT32_MIN ? -1 : es;
+  }
+  return a;
+}
+}  // namespace
+
+extern "C" {
+
+NGTGPUServer ngtgpu_server_create(NGTIndex index, uint32_t max_batch_queries, uint32_t inflight, uint32_t max_k,
+                                  NGTError error) {
+  if (index == nullptr) {
+    server_error(__FUNCTION__, "parametor error: index is NULL", error);
+    return nullptr;
+  }
+  try {
+    return new ngtg::Server(static_cast<ngtg::GraphEngine*>(index), max_batch_queries, inflight, max_k);
+  } catch (std::exception& ex) {
+    server_error(__FUNCTION__, ex.what(), error);
+    return nullptr;
+  }
+}
+
+int64_t ngtgpu_server_submit(NGTGPUServer server, const float* queries, size_t nq, int32_t dim,
+                             const NGTQueryParameters* params, size_t nparams, NGTError error) {
+  if (server == nullptr || queries == nullptr || params == nullptr || dim <= 0) {
+    server_error(__FUNCTION__, "parametor error: server, queries or params", error);
+    return -1;
+  }
+  try {
+    auto a = server_args(params, nparams);
+    return static_cast<ngtg::Server*>(server)->submit(queries, nq, (size_t)dim, a.data(), a.size());
+  } catch (std::exception& ex) {
+    server_error(__FUNCTION__, ex.what(), error);
+    return -1;
+  }
+}
+
+bool ngtgpu_server_wait(NGTGPUServer server, int64_t ticket, NGTObjectDistance* results, size_t kmax,
+                        uint32_t* counts, double* latency_ms, NGTError error) {
+  if (server == nullptr || results == nullptr || counts == nullptr) {
+    server_error(__FUNCTION__, "parametor error: server or output buffers", error);
+    return false;
+  }
+  try {
+    static_cast<ngtg::Server*>(server)->wait(ticket, reinterpret_cast<ngtg::ObjDist*>(results), kmax, counts,
+                                             latency_ms);
+    return true;
+  } catch (std::exception& ex) {
+    server_error(__FUNCTION__, ex.what(), error);
+    return false;
+  }
+}
+
+void ngtgpu_server_destroy(NGTGPUServer server) { delete static_cast<ngtg::Server*>(server); }
+
+}  // extern "C"

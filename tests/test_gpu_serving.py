@@ -1,0 +1,72 @@
+"""GPU tests of the serving loop (continuous batching, ngtgpu_server_*).
+
+Requests of different sizes and parameters are submitted from several
+threads while earlier ones are on the GPU; each request's results must be
+exactly what the same queries return alone through the batched kernel (it
+handles every query independently), and latencies must be measured.
+"""
+import threading
+
+import numpy as np
+import pytest
+
+from golden_util import materialize
+
+pytestmark = pytest.mark.gpu
+KERNEL_BATCHED = 1
+
+
+@pytest.fixture(scope="module")
+def index_path(tmp_path_factory):
+    path, meta, queries, golden = materialize("c1_f32_l2", str(tmp_path_factory.mktemp("serving")))
+    return path, queries
+
+
+def test_results_in_the_mix_equal_results_alone(index_path):
+    from ngt_gb300 import Index, Server
+    path, queries = index_path
+    rng = np.random.default_rng(7)
+    reqs = []
+    start = 0
+    for _ in range(60):
+        n = int(rng.integers(1, 48))
+        q = queries[start % 900: start % 900 + n]
+        start += n
+        reqs.append((q, int(rng.choice([5, 10, 20])), float(rng.choice([0.05, 0.1, 0.15]))))
+    with Index(path, read_only=True) as ix:
+        alone = [ix.batch_search(q, k=k, epsilon=e, kernel=KERNEL_BATCHED) for q, k, e in reqs]
+        with Server(ix, max_batch=256, inflight=3, max_k=64) as srv:
+            tickets = [None] * len(reqs)
+
+            def submitter(part):
+                for i in part:
+                    q, k, e = reqs[i]
+                    tickets[i] = srv.submit(q, k=k, epsilon=e)
+
+            threads = [threading.Thread(target=submitter, args=(range(t, len(reqs), 3),)) for t in range(3)]
+            for t in threads:
+                t.start()
+            for t in threads:
+                t.join()
+            for i, (q, k, e) in enumerate(reqs):
+                ids, ds, n, lat = srv.wait(tickets[i])
+                ai, ad, an = alone[i]
+                assert np.array_equal(n, an), i
+                for j in range(len(q)):
+                    assert np.array_equal(ids[j, :n[j]], ai[j, :an[j]]), (i, j)
+                    assert np.array_equal(ds[j, :n[j]], ad[j, :an[j]]), (i, j)
+                assert lat > 0.0
+
+
+def test_server_rejects_bad_requests(index_path):
+    from ngt_gb300 import Index, NativeError, Server
+    path, queries = index_path
+    with Index(path, read_only=True) as ix:
+        with Server(ix, max_batch=32, inflight=2, max_k=16) as srv:
+            with pytest.raises(NativeError, match="request size"):
+                srv.submit(queries[:40], k=10)
+            with pytest.raises(NativeError, match="maximum"):
+                srv.submit(queries[:4], k=40)
+            t = srv.submit(queries[:4], k=10)
+            ids, ds, n, lat = srv.wait(t)
+            assert (n == 10).all()
