@@ -41,8 +41,8 @@ sys.path.insert(0, ROOT)
 
 EPS_SWEEP = [0.0, 0.02, 0.04, 0.06, 0.07, 0.08, 0.09, 0.1, 0.12, 0.15, 0.2, 0.3]
 RECALL_TARGET = 0.95
-LIST_SWEEP = [128, 256, 512]
-PARENT_SWEEP = [1, 2, 4]
+LIST_SWEEP = [128, 256]
+PARENT_SWEEP = [4, 8, 16]
 
 
 def log(*a):
@@ -378,6 +378,7 @@ def main():
                 "bytes_per_query": float(bytes_pq.mean()), "row_bytes": srow,
                 "achieved_gbs": bytes_pq.sum() / (statistics.median(kernel_ms) / 1e3) / 1e9,
                 "dc": float(stats["distance_computations"].mean()),
+                "expansions": float(stats["expansions"].mean()), "edges": float(stats["edges_read"].mean()),
                 "status": sorted(set(int(x) for x in np.unique(stats["status"]))),
                 "launches": int(launches), "clocks": clocks.summary(), "wall": wall}
 
@@ -450,11 +451,14 @@ def main():
                                       "recall_at_k": round(plain["recall"], 4),
                                       "epsilon_curve": curves[KERNEL_EXACT],
                                       "mean_distance_computations": round(plain["dc"], 1),
+                                      "mean_expansions": round(plain["expansions"], 1),
                                       "achieved_gbs": round(plain["achieved_gbs"], 1)},
                        "speedup_vs_plain_fp32": round(head["qps"] / plain["qps"], 3),
                        "parallelism": "replicas",
                        "l2": "inputs larger than L2 (%.0f MB object arena)" % (args.n * row_bytes / 1e6),
-                       "mean_distance_computations": round(head["dc"], 1), "status_bits": head["status"]},
+                       "mean_distance_computations": round(head["dc"], 1),
+                       "mean_expansions": round(head["expansions"], 1), "mean_edges_read": round(head["edges"], 1),
+                       "status_bits": head["status"]},
             "roofline": {"bound": "hbm", "achieved": round(head["achieved_gbs"], 1), "peak": peak, "unit": "GB/s",
                          "frac": round(head["achieved_gbs"] / peak, 4), "traffic": None, "peak_source": peak_kind,
                          "basis": "(%d*DC + 4*edges + %d query + re-rank %d*2k) bytes per query over the kernel's "

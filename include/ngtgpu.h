@@ -60,8 +60,9 @@ bool ngtgpu_search_batch_device(NGTIndex, const void *d_rows, size_t nq, const N
                                 NGTGPUQueryStats *d_stats, void *stream, uint32_t kernel, NGTError);
 
 /* Tuning of the batched kernel for this index (0 = automatic): candidate
- * list length (rounded up to a power of two, >= size+1), nodes expanded per
- * iteration, and re-ranked candidates per query as a multiple of size. */
+ * list length (rounded up to a power of two, >= size+1, <= 1024), nodes
+ * expanded per iteration (<= 16), and re-ranked candidates per query as a
+ * multiple of size. */
 bool ngtgpu_set_batched_tuning(NGTIndex, uint32_t list_capacity, uint32_t parents, float rerank_factor, NGTError);
 
 /* Exact graph search (results equal ngtgpu_search_batch_device with

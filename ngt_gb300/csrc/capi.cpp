@@ -421,7 +421,7 @@ bool ngtgpu_search_batch_device(NGTIndex index, const void* d_rows, size_t nq, c
 
 bool ngtgpu_set_batched_tuning(NGTIndex index, uint32_t list_capacity, uint32_t parents, float rerank_factor,
                                NGTError error) {
-  if (index == nullptr || list_capacity > 1024 || parents > 8 || rerank_factor < 0.f) {
+  if (index == nullptr || list_capacity > 1024 || parents > 16 || rerank_factor < 0.f) {
     CAPI_PARAM_ERROR(error, "index = " << index << " list_capacity = " << list_capacity << " parents = " << parents
                                        << " rerank_factor = " << rerank_factor);
     return false;

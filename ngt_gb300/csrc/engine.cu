@@ -478,10 +478,10 @@ void GraphEngine::launch_fast(const uint4* d_rows, size_t nq, const QueryParams*
   if (L > 1024) throw std::runtime_error("result size too large for the batched kernel (at most 1023)");
   cfg.list_cap = L;
   // neighbour buffer: P parents' edges per iteration, and the re-rank set (sorted in place)
-  cfg.parents = tuning_.parents ? std::min<uint32_t>(tuning_.parents, 8) : 2;
+  cfg.parents = tuning_.parents ? std::min<uint32_t>(tuning_.parents, 16) : 4;
   float rf0 = tuning_.rerank_factor > 0.f ? tuning_.rerank_factor : 2.0f;
   uint32_t rerank_max = std::min<uint32_t>(L, (uint32_t)std::ceil(rf0 * (float)max_size) + 1);
-  cfg.nbr_cap = std::max<uint32_t>({512u, next_pow2(rerank_max), L});
+  cfg.nbr_cap = std::max<uint32_t>({512u, next_pow2(rerank_max), L, next_pow2(cfg.parents * 64)});
   cfg.search_chunks = bf16 ? dev_.row_chunks / 2 : dev_.row_chunks;
   cfg.sgroup = std::min<uint32_t>(32, next_pow2(cfg.search_chunks));
   cfg.ngroup = std::min<uint32_t>(32, next_pow2(dev_.row_chunks));

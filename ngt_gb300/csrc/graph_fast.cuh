@@ -59,7 +59,9 @@ struct FastWarpSmem {
   uint32_t n;              // list length
   uint32_t cur;            // active list buffer
   uint32_t nparents;
-  uint32_t parents[8];
+  uint32_t parents[16];
+  uint32_t pexcl[16];
+  uint32_t pbase[16];
   uint32_t seed_leaf;
   uint32_t hist[256];
 };
@@ -122,7 +124,7 @@ __device__ __forceinline__ uint32_t warp_lower_bound(const unsigned long long* a
 }
 
 template <ObjType ST, ObjType OT, Metric M>
-__global__ void __launch_bounds__(kFastThreads, 5)
+__global__ void __launch_bounds__(kFastThreads, 6)
 graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint4* __restrict__ queries, uint32_t nq,
                          const QueryParams* __restrict__ params, const uint32_t* __restrict__ seed_list,
                          ObjDist* __restrict__ out, uint32_t* __restrict__ out_count, QueryStats* __restrict__ stats,
@@ -362,17 +364,17 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       }
       uint32_t incl = pne;
 #pragma unroll
-      for (int off = 1; off < 8; off <<= 1) {
+      for (int off = 1; off < 16; off <<= 1) {
         uint32_t t = __shfl_up_sync(0xffffffffu, incl, off);
         if (lane >= off) incl += t;
       }
       const uint32_t total = __shfl_sync(0xffffffffu, incl, np - 1);
-      uint32_t pstart[8], pbase[8];
-#pragma unroll
-      for (int p2 = 0; p2 < 8; p2++) {
-        pstart[p2] = __shfl_sync(0xffffffffu, incl - pne, p2);
-        pbase[p2] = __shfl_sync(0xffffffffu, pe0, p2);
+      // parent of edge slot t: the last parent whose exclusive prefix is <= t
+      if ((uint32_t)lane < np) {
+        w.pexcl[lane] = incl - pne;
+        w.pbase[lane] = pe0;
       }
+      __syncwarp();
       edges_read += total;
       uint32_t cnt = 0;
       constexpr int J = 8;
@@ -384,15 +386,10 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
           uint32_t t = base0 + lane + 32 * j;
           ids[j] = 0;
           if (t < total) {
-            int p2 = 0;
-#pragma unroll
-            for (int c = 1; c < 8; c++)
-              if ((uint32_t)c < np && t >= pstart[c]) p2 = c;
-            uint32_t b2 = 0, s2 = 0;
-#pragma unroll
-            for (int c = 0; c < 8; c++)
-              if (c == p2) { b2 = pbase[c]; s2 = pstart[c]; }
-            ids[j] = __ldg(g.edges + b2 + (t - s2));
+            uint32_t p2 = 0;
+            for (uint32_t c = 1; c < np; c++)
+              if (t >= w.pexcl[c]) p2 = c;
+            ids[j] = __ldg(g.edges + w.pbase[p2] + (t - w.pexcl[p2]));
           }
         }
 #pragma unroll
