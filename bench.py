@@ -42,7 +42,7 @@ sys.path.insert(0, ROOT)
 EPS_SWEEP = [0.0, 0.02, 0.04, 0.06, 0.07, 0.08, 0.09, 0.1, 0.12, 0.15, 0.2, 0.3]
 RECALL_TARGET = 0.95
 LIST_SWEEP = [128, 256]
-PARENT_SWEEP = [4, 8, 16]
+PARENT_SWEEP = [2, 4, 8]
 
 
 def log(*a):

@@ -123,8 +123,29 @@ __device__ __forceinline__ uint32_t warp_lower_bound(const unsigned long long* a
   return lo;
 }
 
+// L2 over float-typed rows with the packed fp32 instructions of sm_100-class
+// GPUs (two lanes of IEEE fma per instruction, the same rounding as the scalar
+// form): sum of (x - q)^2 accumulated in a float2.
+template <ObjType ST, Metric M>
+struct PackedL2 {
+  static constexpr bool kOn = (M == Metric::L2 || M == Metric::InnerProduct) &&
+                              (ST == ObjType::Bfloat16 || ST == ObjType::Float || ST == ObjType::Float16);
+  __device__ __forceinline__ static float2 add(float2 acc, const uint4& q, const uint4& x) {
+    constexpr int P = ObjTraits<ST>::kPerChunk;
+    float a[P], b[P];
+    unpack<ST>(q, a);
+    unpack<ST>(x, b);
+#pragma unroll
+    for (int i = 0; i < P; i += 2) {
+      float2 dlt = __fadd2_rn(make_float2(b[i], b[i + 1]), make_float2(-a[i], -a[i + 1]));
+      acc = __ffma2_rn(dlt, dlt, acc);
+    }
+    return acc;
+  }
+};
+
 template <ObjType ST, ObjType OT, Metric M>
-__global__ void __launch_bounds__(kFastThreads, 6)
+__global__ void __launch_bounds__(kFastThreads, 5)
 graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint4* __restrict__ queries, uint32_t nq,
                          const QueryParams* __restrict__ params, const uint32_t* __restrict__ seed_list,
                          ObjDist* __restrict__ out, uint32_t* __restrict__ out_count, QueryStats* __restrict__ stats,
@@ -434,25 +455,43 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
         kept += __popc(bal);
         spill_n += __popc(bs);
       };
-      if (sc <= (uint32_t)SG) {
-        // one 16-byte chunk per lane per row: U rows per group in flight
-        constexpr int U = 8;
-        const uint4 qv = (uint32_t)sgl < sc ? qs[sgl] : make_uint4(0, 0, 0, 0);
+      if (sc <= (uint32_t)SG * 2) {
+        // at most two 16-byte chunks per lane per row; U rows per group in flight
+        constexpr int U = 4;
+        const uint32_t c0 = (uint32_t)sgl, c1 = (uint32_t)sgl + (uint32_t)SG;
+        const uint4 zero = make_uint4(0, 0, 0, 0);
+        const uint4 q0 = c0 < sc ? qs[c0] : zero, q1 = c1 < sc ? qs[c1] : zero;
         for (uint32_t b = 0; b < cnt; b += gpw * U) {
-          uint4 xv[U];
+          uint4 x0[U], x1[U];
           uint32_t idu[U];
 #pragma unroll
           for (int u = 0; u < U; u++) {
             uint32_t i = b + u * gpw + (uint32_t)(lane / SG);
             idu[u] = i < cnt ? nid[i] : 0u;
-            xv[u] = (uint32_t)sgl < sc ? __ldg(srows + (size_t)idu[u] * sc + sgl) : make_uint4(0, 0, 0, 0);
+            const uint4* row = srows + (size_t)idu[u] * sc;
+            x0[u] = c0 < sc ? __ldg(row + c0) : zero;
+            x1[u] = c1 < sc ? __ldg(row + c1) : zero;
           }
 #pragma unroll
           for (int u = 0; u < U; u++) {
-            Acc<ST, M> acc;
-            if ((uint32_t)sgl < sc) acc.add(qv, xv[u], sgl);
-            acc.reduce(SG);
-            place(b + u * gpw + (uint32_t)(lane / SG), acc.finish(), idu[u]);
+            float d;
+            if constexpr (PackedL2<ST, M>::kOn) {
+              float2 acc = make_float2(0.f, 0.f);
+              if (c0 < sc) acc = PackedL2<ST, M>::add(acc, q0, x0[u]);
+              if (c1 < sc) acc = PackedL2<ST, M>::add(acc, q1, x1[u]);
+              float v = acc.x + acc.y;
+#pragma unroll
+              for (int off = 16; off > 0; off >>= 1)
+                if (off < SG) v += __shfl_xor_sync(0xffffffffu, v, off);
+              d = sqrtf(v);
+            } else {
+              Acc<ST, M> acc;
+              if (c0 < sc) acc.add(q0, x0[u], (int)c0);
+              if (c1 < sc) acc.add(q1, x1[u], (int)c1);
+              acc.reduce(SG);
+              d = acc.finish();
+            }
+            place(b + u * gpw + (uint32_t)(lane / SG), d, idu[u]);
           }
         }
       } else {
