@@ -156,14 +156,15 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
   const uint32_t rc = g.row_chunks, sc = cfg.search_chunks;
   const uint32_t L = cfg.list_cap, NB = cfg.nbr_cap;
   // per-warp carve-up
-  const size_t per_warp = (size_t)rc * 16 + (size_t)sc * 16 + (size_t)L * 8 + (size_t)NB * 12 + sizeof(FastWarpSmem);
+  const size_t per_warp = (size_t)rc * 16 + (size_t)sc * 16 + (size_t)L * 8 + (size_t)NB * 16 + sizeof(FastWarpSmem);
   unsigned char* base = smem + warp * ((per_warp + 15) & ~(size_t)15);
   uint4* qn = reinterpret_cast<uint4*>(base);                  // query, object type
   uint4* qs = qn + rc;                                          // query, search type
   unsigned long long* list = reinterpret_cast<unsigned long long*>(qs + sc);
   unsigned long long* nkey = list + L;                          // NB keys
   uint32_t* nid = reinterpret_cast<uint32_t*>(nkey + NB);       // NB ids
-  FastWarpSmem& w = *reinterpret_cast<FastWarpSmem*>(nid + NB);
+  float* nd = reinterpret_cast<float*>(nid + NB);                // NB search distances
+  FastWarpSmem& w = *reinterpret_cast<FastWarpSmem*>(nd + NB);
   const uint32_t slot = blockIdx.x * kFastWarps + warp;
   uint32_t* bitmap = bitmaps + (size_t)slot * cfg.bitmap_words;
   // spill tier: candidates that do not fit in the list, all larger than every list key
@@ -440,20 +441,9 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       uint32_t kept = 0;
       const uint32_t gpw = 32 / SG;
       unsigned long long smin = spill_min;
-      auto place = [&](uint32_t i, float d, uint32_t id) {
-        unsigned long long key = pack_key(d, id);
-        bool live = i < cnt && sgl == 0 && d <= insert_limit;
-        bool keep = live && key < worst;
-        bool spl = live && key >= worst;
-        unsigned bal = __ballot_sync(0xffffffffu, keep), bs = __ballot_sync(0xffffffffu, spl);
-        if (keep) nkey[kept + __popc(bal & ((1u << lane) - 1u))] = key;
-        if (spl) {
-          uint32_t o = spill_n + __popc(bs & ((1u << lane) - 1u));
-          if (o < cfg.spill_cap) spill[o] = key;
-          smin = key < smin ? key : smin;
-        }
-        kept += __popc(bal);
-        spill_n += __popc(bs);
+      // distances are parked in nd[] by the group leaders and placed 32 at a time below
+      auto place = [&](uint32_t i, float d, uint32_t) {
+        if (i < cnt && sgl == 0) nd[i] = d;
       };
       if (sc <= (uint32_t)SG * 2) {
         // at most two 16-byte chunks per lane per row; U rows per group in flight
@@ -501,6 +491,26 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
           float d = group_distance<ST, M>(qs, srows + (size_t)id * sc, (int)sc, sgl, SG);
           place(i, d, id);
         }
+      }
+      __syncwarp();
+      // placement: keys below the list's worst are merged, the others still within
+      // the exploration limit join the spill tier (one entry per lane per step)
+      for (uint32_t b = 0; b < cnt; b += 32) {
+        uint32_t i = b + lane;
+        float d = i < cnt ? nd[i] : 0.f;
+        unsigned long long key = i < cnt ? pack_key(d, nid[i]) : ~0ull;
+        bool live = i < cnt && d <= insert_limit;
+        bool keep = live && key < worst;
+        bool spl = live && key >= worst;
+        unsigned bal = __ballot_sync(0xffffffffu, keep), bs = __ballot_sync(0xffffffffu, spl);
+        if (keep) nkey[kept + __popc(bal & ((1u << lane) - 1u))] = key;
+        if (spl) {
+          uint32_t o = spill_n + __popc(bs & ((1u << lane) - 1u));
+          if (o < cfg.spill_cap) spill[o] = key;
+          smin = key < smin ? key : smin;
+        }
+        kept += __popc(bal);
+        spill_n += __popc(bs);
       }
       for (int off = 16; off > 0; off >>= 1) {
         unsigned long long o = __shfl_xor_sync(0xffffffffu, smin, off);
@@ -610,7 +620,7 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
 
 inline size_t fast_smem_per_warp(uint32_t row_chunks, const FastConfig& c) {
   size_t per = (size_t)row_chunks * 16 + (size_t)c.search_chunks * 16 + (size_t)c.list_cap * 8 +
-               (size_t)c.nbr_cap * 12 + sizeof(FastWarpSmem);
+               (size_t)c.nbr_cap * 16 + sizeof(FastWarpSmem);
   return (per + 15) & ~(size_t)15;
 }
 
