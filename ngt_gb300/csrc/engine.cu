@@ -482,6 +482,8 @@ void GraphEngine::launch_fast(const uint4* d_rows, size_t nq, const QueryParams*
   float rf0 = tuning_.rerank_factor > 0.f ? tuning_.rerank_factor : 2.0f;
   uint32_t rerank_max = std::min<uint32_t>(L, (uint32_t)std::ceil(rf0 * (float)max_size) + 1);
   cfg.nbr_cap = std::max<uint32_t>({512u, next_pow2(rerank_max), L, next_pow2(cfg.parents * 128)});
+  // nd doubles as the 256-bin refill histogram
+  cfg.nbr_cap = std::max<uint32_t>(cfg.nbr_cap, 256u);
   cfg.search_chunks = bf16 ? dev_.row_chunks / 2 : dev_.row_chunks;
   cfg.sgroup = std::min<uint32_t>(32, next_pow2((cfg.search_chunks + 1) / 2));   // two chunks per lane
   cfg.ngroup = std::min<uint32_t>(32, next_pow2(dev_.row_chunks));

@@ -63,7 +63,6 @@ struct FastWarpSmem {
   uint32_t pexcl[16];
   uint32_t pbase[16];
   uint32_t seed_leaf;
-  uint32_t hist[256];
 };
 
 __device__ __forceinline__ uint32_t key_rawid(unsigned long long k) { return (uint32_t)k & 0x7fffffffu; }
@@ -298,16 +297,17 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
           unsigned long long prefix = 0, mask = 0;
           uint32_t need = room;
           for (int shift = 56; shift >= 0; shift -= 8) {
-            for (uint32_t i = lane; i < 256; i += 32) w.hist[i] = 0;
+            uint32_t* hist = reinterpret_cast<uint32_t*>(nd);     // nd is idle during a refill
+            for (uint32_t i = lane; i < 256; i += 32) hist[i] = 0;
             __syncwarp();
             for (uint32_t i = lane; i < r; i += 32) {
               unsigned long long k = spill_tmp[i];
-              if ((k & mask) == prefix) atomicAdd(&w.hist[(uint32_t)(k >> shift) & 255u], 1u);
+              if ((k & mask) == prefix) atomicAdd(&hist[(uint32_t)(k >> shift) & 255u], 1u);
             }
             __syncwarp();
             uint32_t acc = 0, bsel = 255;
             for (uint32_t b = 0; b < 256; b++) {
-              uint32_t h = w.hist[b];
+              uint32_t h = hist[b];
               if (acc + h >= need) { bsel = b; break; }
               acc += h;
             }
