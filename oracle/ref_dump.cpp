@@ -3,11 +3,13 @@
 // in this directory) through its own C API (lib/NGT/Capi.h) and dumps the
 // results in binary, so tests/golden/make_golden.py can record golden vectors.
 //
-// usage: ref_dump <graph|linear> <index> <queries.f32> <nq> <dim> <k> <eps> <edge_size|x> <ro|rw> <out>
+// usage: ref_dump <graph|linear|qg> <index> <queries.f32> <nq> <dim> <k> <eps> <edge_size|x> <ro|rw> <out>
 //   out: nq x k uint32 ids, then nq x k float distances, then nq uint32 counts.
+//   For qg the edge_size argument is the result expansion (ngtqg_search_index_float).
 //   For graph-only indexes srand(1) runs before every query, so that the
 //   random seeds the reference draws are reproducible.
 #include <NGT/Capi.h>
+#include <NGT/NGTQ/Capi.h>
 
 #include <climits>
 #include <cstdio>
@@ -35,13 +37,49 @@ int main(int argc, char** argv) {
   if (!f || std::fread(q.data(), 4, q.size(), f) != q.size()) return 3;
   std::fclose(f);
   NGTError err = ngt_create_error_object();
+  std::vector<uint32_t> ids(nq * k, 0), cnt(nq, 0);
+  std::vector<float> ds(nq * k, 0.f);
+  if (op == "qg") {
+    NGTQGIndex qg = ngtqg_open_index(index_path, err);
+    if (!qg) {
+      std::fprintf(stderr, "open failed: %s\n", ngt_get_error_string(err));
+      return 4;
+    }
+    NGTObjectDistances res = ngt_create_empty_results(err);
+    for (size_t i = 0; i < nq; i++) {
+      std::srand(1);
+      NGTQGQueryFloat qf;
+      qf.query = &q[i * dim];
+      ngtqg_initialize_query_parameters(&qf.params);
+      qf.params.size = k;
+      qf.params.epsilon = eps;
+      qf.params.result_expansion = std::strtof(argv[8], nullptr);
+      if (!ngtqg_search_index_float(qg, qf, res, err)) {
+        std::fprintf(stderr, "search failed: %s\n", ngt_get_error_string(err));
+        return 5;
+      }
+      uint32_t n = ngt_get_result_size(res, err);
+      cnt[i] = n;
+      for (uint32_t j = 0; j < n && j < k; j++) {
+        NGTObjectDistance od = ngt_get_result(res, j, err);
+        ids[i * k + j] = od.id;
+        ds[i * k + j] = od.distance;
+      }
+    }
+    ngt_destroy_results(res);
+    ngtqg_close_index(qg);
+    FILE* o = std::fopen(argv[10], "wb");
+    std::fwrite(ids.data(), 4, ids.size(), o);
+    std::fwrite(ds.data(), 4, ds.size(), o);
+    std::fwrite(cnt.data(), 4, cnt.size(), o);
+    std::fclose(o);
+    return 0;
+  }
   NGTIndex index = ro ? ngt_open_index_as_read_only(index_path, err) : ngt_open_index(index_path, err);
   if (!index) {
     std::fprintf(stderr, "open failed: %s\n", ngt_get_error_string(err));
     return 4;
   }
-  std::vector<uint32_t> ids(nq * k, 0), cnt(nq, 0);
-  std::vector<float> ds(nq * k, 0.f);
   NGTObjectDistances res = ngt_create_empty_results(err);
   for (size_t i = 0; i < nq; i++) {
     bool ok;
