@@ -11,6 +11,15 @@ Index file formats restated from the reference:
   obj  Repository<Object>       lib/NGT/Common.h:2181-2238, lib/NGT/ObjectSpace.h:620-640
   grp  Repository<GraphNode>    lib/NGT/Graph.h:153-160, lib/NGT/ObjectSpace.h:72-80
   tre  DVP tree                 lib/NGT/Tree.h:347-355, lib/NGT/Node.h:88-110,218-280,441-510
+
+Quantized-graph files (<index>/qg, written by `qbg create-qg` / `qbg build-qg`):
+  prf       text key/value (NGTQ::Property)      lib/NGT/NGTQ/Quantizer.h:560-700
+  qr        uint32 n, n floats (Rotation)        lib/NGT/NGTQ/Quantizer.h:164-186
+  rqcb      uint32 size, dimension, paddedDimension, floats (QuantizationCodebook)
+                                                 lib/NGT/NGTQ/Quantizer.h:355-378
+  local-i   NGT index whose obj holds subspace i's 16 centroids
+  grp       uint64 subspaces, uint64 n, per node uint32 sid, uint32 count, count ids,
+            the node's 4-bit code stream          lib/NGT/NGTQ/QuantizedGraph.h:170-226
 """
 from __future__ import annotations
 
@@ -192,6 +201,80 @@ class IndexFiles:
         self.root = 1 if (ni > 1 and self.in_nchildren[1] > 0) else (0x80000000 | 1)
 
 
+class OracleQGC(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_uint32), ("m", ctypes.c_uint32), ("ld", ctypes.c_uint32), ("ma", ctypes.c_uint32),
+                ("rotation", ctypes.c_void_p), ("gcentroid", ctypes.c_void_p), ("lcentroids", ctypes.c_void_p),
+                ("nnodes", ctypes.c_uint32), ("offsets", ctypes.c_void_p), ("ids", ctypes.c_void_p),
+                ("code_off", ctypes.c_void_p), ("codes", ctypes.c_void_p)]
+
+
+def _read_rows(path: str, dim: int) -> np.ndarray:
+    """Float rows of an NGT object file (slot 0 and deleted slots as zeros)."""
+    buf = open(path, "rb").read()
+    n = int(np.frombuffer(buf, np.uint64, 1, 0)[0])
+    rows = np.zeros((n, dim), np.float32)
+    pos = 8
+    for i in range(n):
+        t = buf[pos:pos + 1]
+        pos += 1
+        if t == b"-":
+            continue
+        rows[i] = np.frombuffer(buf, np.float32, dim, pos)
+        pos += 4 * dim
+    assert pos == len(buf), "trailing bytes in " + path
+    return rows
+
+
+class QGFiles:
+    """numpy view of the quantized graph of an index (<index>/qg)."""
+
+    def __init__(self, index_path: str):
+        qg = os.path.join(index_path, "qg")
+        self.prop = read_property(qg)
+        self.dim = int(self.prop["Dimension"])
+        self.m = int(self.prop["LocalDivisionNo"])
+        assert self.dim % self.m == 0, "dimension is not a multiple of the subspace count"
+        self.ld = self.dim // self.m
+        self.ma = (self.m + 1) // 2 * 2
+        assert int(self.prop.get("LocalCentroidLimit", "16")) == 16, "QG needs 16 local centroids"
+        raw = open(os.path.join(qg, "qr"), "rb").read()
+        n = int(np.frombuffer(raw, np.uint32, 1, 0)[0]) if raw else 0
+        self.rotation = np.frombuffer(raw, np.float32, n, 4).reshape(self.dim, self.dim).copy() if n else None
+        raw = open(os.path.join(qg, "rqcb"), "rb").read()
+        size, _cdim, pdim = np.frombuffer(raw, np.uint32, 3, 0)
+        cb = np.frombuffer(raw, np.float32, int(size), 12)
+        self.gcentroid = np.zeros(self.dim, np.float32)
+        self.gcentroid[:min(int(pdim), self.dim)] = cb[:min(int(pdim), self.dim)]
+        self.lcentroids = np.zeros((self.m, 16, self.ld), np.float32)
+        for i in range(self.m):
+            rows = _read_rows(os.path.join(qg, "local-%d" % i, "obj"), self.ld)
+            assert rows.shape[0] == 17, "local codebook %d does not hold 16 centroids" % i
+            self.lcentroids[i] = rows[1:17]
+        raw = open(os.path.join(qg, "grp"), "rb").read()
+        _nsub, nn = np.frombuffer(raw, np.uint64, 2, 0)
+        pos = 16
+        counts, ids, code_off, chunks = [], [], [], []
+        total = 0
+        for _ in range(int(nn)):
+            _sid, cnt = (int(v) for v in np.frombuffer(raw, np.uint32, 2, pos))
+            pos += 8
+            ids.append(np.frombuffer(raw, np.uint32, cnt, pos))
+            pos += 4 * cnt
+            ssz = ((cnt + 15) // 16) * 16 * self.ma // 2 if cnt else 0
+            code_off.append(total)
+            chunks.append(np.frombuffer(raw, np.uint8, ssz, pos))
+            pos += ssz
+            total += ssz
+            counts.append(cnt)
+        assert pos == len(raw), "trailing bytes in the quantized graph"
+        self.nnodes = int(nn)
+        self.offsets = np.zeros(self.nnodes + 1, np.uint32)
+        self.offsets[1:] = np.cumsum(counts)
+        self.ids = np.concatenate(ids).astype(np.uint32) if ids else np.zeros(0, np.uint32)
+        self.code_off = np.array(code_off, np.uint64)
+        self.codes = np.concatenate(chunks) if chunks else np.zeros(0, np.uint8)
+
+
 class Oracle:
     """ctypes binding of ngt_oracle.c over one IndexFiles."""
 
@@ -210,6 +293,17 @@ class Oracle:
         L.oracle_rand_sequence.argtypes = [ctypes.c_uint32, ctypes.c_size_t, ctypes.c_void_p]
         L.oracle_distance.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
         L.oracle_distance.restype = ctypes.c_float
+        L.oracle_qg_search.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                       ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_float,
+                                       ctypes.c_float, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                       ctypes.c_void_p, ctypes.c_int]
+        L.oracle_qg_rotate.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.oracle_qg_lut.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                    ctypes.c_void_p]
+        L.oracle_qg_scan.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.c_float,
+                                     ctypes.c_uint32, ctypes.c_void_p]
+        self.qg = None
         f = files
         self._keep = []
 
@@ -267,6 +361,68 @@ class Oracle:
                                      sc.ctypes.data if sc is not None else None, threads)
         w = max(k, int(n.max()) if nq else 0, 1)
         return ids[:, :w], ds[:, :w], n, dc
+
+    def _qg(self):
+        if self.qg is None:
+            g = QGFiles(self.f.path)
+            self.qgf = g
+            s = OracleQGC()
+            s.dim, s.m, s.ld, s.ma, s.nnodes = g.dim, g.m, g.ld, g.ma, g.nnodes
+            s.rotation = self._p(g.rotation) if g.rotation is not None else None
+            s.gcentroid, s.lcentroids = self._p(g.gcentroid), self._p(g.lcentroids)
+            s.offsets, s.ids, s.code_off, s.codes = (self._p(g.offsets), self._p(g.ids), self._p(g.code_off),
+                                                     self._p(g.codes))
+            self.qg = s
+        return self.qg
+
+    def _p(self, a):
+        a = np.ascontiguousarray(a)
+        self._keep.append(a)
+        return a.ctypes.data
+
+    def qg_search(self, queries, k=20, epsilon=0.03, result_expansion=3.0, radius=-1.0, threads=1, seeds=None):
+        """ngtqg_search_index_float over the quantized graph (defaults of
+        ngtqg_initialize_query_parameters, lib/NGT/NGTQ/Capi.cpp:46-51)."""
+        qg = self._qg()
+        qf = np.ascontiguousarray(queries, np.float32)
+        rows = self.prepare(qf)
+        nq = rows.shape[0]
+        kk = max(k, 1)
+        ids = np.zeros((nq, kk), np.uint32)
+        ds = np.zeros((nq, kk), np.float32)
+        n = np.zeros(nq, np.uint32)
+        dc = np.zeros(nq, np.uint32)
+        sl = so = sc = None
+        if seeds is not None:
+            sl, so, sc = (np.ascontiguousarray(a, np.uint32) for a in seeds)
+        self.lib.oracle_qg_search(ctypes.byref(self.s), ctypes.byref(qg), qf.ctypes.data, qf.shape[1],
+                                  rows.ctypes.data, nq, k, epsilon, result_expansion, radius, ids.ctypes.data,
+                                  ds.ctypes.data, n.ctypes.data, dc.ctypes.data,
+                                  sl.ctypes.data if sl is not None else None,
+                                  so.ctypes.data if so is not None else None,
+                                  sc.ctypes.data if sc is not None else None, threads)
+        return ids, ds, n, dc
+
+    def qg_lut(self, query):
+        """Rotated query, uint8 lookup table, scale and offset of one query."""
+        qg = self._qg()
+        x = np.zeros(qg.dim, np.float32)
+        q = np.asarray(query, np.float32)
+        x[:min(len(q), qg.dim)] = q[:qg.dim]
+        rq = np.zeros(qg.dim, np.float32)
+        self.lib.oracle_qg_rotate(ctypes.byref(qg), x.ctypes.data, rq.ctypes.data)
+        lut = np.zeros(qg.m * 16, np.uint8)
+        sc, of = ctypes.c_float(), ctypes.c_float()
+        self.lib.oracle_qg_lut(ctypes.byref(qg), rq.ctypes.data, lut.ctypes.data, ctypes.byref(sc), ctypes.byref(of))
+        return rq, lut, sc.value, of.value
+
+    def qg_scan(self, lut, scale, offset, node):
+        qg = self._qg()
+        n = int(self.qgf.offsets[node + 1] - self.qgf.offsets[node])
+        ds = np.zeros(max(n, 1), np.float32)
+        lut = np.ascontiguousarray(lut, np.uint8)
+        self.lib.oracle_qg_scan(ctypes.byref(qg), lut.ctypes.data, scale, offset, node, ds.ctypes.data)
+        return ds[:n]
 
     def linear_search(self, queries, k=10, threads=1):
         rows = self.prepare(queries)

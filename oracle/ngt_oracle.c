@@ -533,3 +533,215 @@ int64_t oracle_parse_graph(const uint8_t *buf, size_t len, size_t nrows, uint32_
     for (uint64_t i = n; i <= nrows; i++) offsets[i] = (uint32_t)total;
   return total;
 }
+
+/* ---------------- quantized graph (QG) ----------------
+ * NGTQG::Index::searchQuantizedGraph (lib/NGT/NGTQ/QuantizedGraph.h:283-447) over the
+ * quantized graph written by `qbg build-qg`: every node stores its first <= E graph
+ * edges and the 4-bit codes of those neighbours (QuantizedGraphRepository,
+ * lib/NGT/NGTQ/QuantizedGraph.h:67-257). */
+typedef struct {
+  uint32_t dim;              /* quantizer dimension (queries are zero-padded to it) */
+  uint32_t m;                /* subspaces (LocalDivisionNo), one codebook each */
+  uint32_t ld;               /* dimensions per subspace */
+  uint32_t ma;               /* m rounded up to even: subspaces per code block */
+  const float *rotation;     /* dim x dim, element [p * dim + c]; NULL = none */
+  const float *gcentroid;    /* dim (the single global centroid) */
+  const float *lcentroids;   /* [m][16][ld] */
+  uint32_t nnodes;
+  const uint32_t *offsets;   /* nnodes + 1 */
+  const uint32_t *ids;       /* neighbour ids */
+  const uint64_t *code_off;  /* byte offset of each node's code stream in codes */
+  const uint8_t *codes;
+} OracleQG;
+
+/* Rotation::mul (lib/NGT/NGTQ/Quantizer.h:117-160), y[c] = sum_p R[p][c] x[p].  The
+ * reference hands it to BLAS sgemv('N'); the summation order here is the one the x86-64
+ * OpenBLAS build the reference links uses, which this reproduces bit for bit for
+ * dimensions <= 48 (one FMA chain over p) and for multiples of 32 up to 512 (blocks of 8
+ * columns: first product, then FMAs, the block total added to y[c]).  For other
+ * dimensions OpenBLAS's order depends on its thread partition of the rows, and single
+ * elements can differ from it by an ulp. */
+void oracle_qg_rotate(const OracleQG *qg, const float *x, float *y) {
+  size_t d = qg->dim;
+  if (!qg->rotation) { memcpy(y, x, d * sizeof(float)); return; }
+  for (size_t c = 0; c < d; c++) {
+    float acc = 0.0f;
+    if (d <= 48) {
+      for (size_t p = 0; p < d; p++) acc = fmaf(qg->rotation[p * d + c], x[p], acc);
+    } else {
+      for (size_t p0 = 0; p0 < d; p0 += 8) {
+        size_t p1 = p0 + 8 < d ? p0 + 8 : d;
+        float t = qg->rotation[p0 * d + c] * x[p0];
+        for (size_t p = p0 + 1; p < p1; p++) t = fmaf(qg->rotation[p * d + c], x[p], t);
+        acc = acc + t;
+      }
+    }
+    y[c] = acc;
+  }
+}
+
+/* createFloatL2DistanceLookup for the uint8 table (lib/NGT/NGTQ/Quantizer.h:1731-1810,
+ * NGTQ_TOTAL_SCALE_OFFSET_COMPRESSION): squared L2 of the rotated query's subvector (minus
+ * the global centroid) to each of the 16 local centroids, summed in float (first term a
+ * product, then FMAs: the contraction of the reference's mul + add); one offset (the
+ * table's minimum) and one scale ((max - min) / 255.0) for the whole table; entries
+ * (v - offset) / scale rounded to nearest even. */
+void oracle_qg_lut(const OracleQG *qg, const float *rq, uint8_t *lut, float *scale_out, float *offset_out) {
+  size_t m = qg->m, ld = qg->ld;
+  float *fl = (float *)malloc(m * 16 * sizeof(float));
+  float mn = FLT_MAX, mx = -FLT_MAX;
+  for (size_t s = 0; s < m; s++) {
+    for (size_t c = 0; c < 16; c++) {
+      float v = 0.0f;
+      for (size_t d = 0; d < ld; d++) {
+        float rsv = rq[s * ld + d] - qg->gcentroid[s * ld + d];
+        float sub = rsv - qg->lcentroids[(s * 16 + c) * ld + d];
+        v = d == 0 ? sub * sub : fmaf(sub, sub, v);
+      }
+      fl[s * 16 + c] = v;
+      if (v < mn) mn = v;
+      if (v > mx) mx = v;
+    }
+  }
+  float scale = (float)((double)(mx - mn) / 255.0);
+  for (size_t i = 0; i < m * 16; i++) lut[i] = (uint8_t)(int32_t)nearbyintf((fl[i] - mn) / scale);
+  *scale_out = scale;
+  *offset_out = mn * (float)m;
+  free(fl);
+}
+
+/* The 4-bit scan of one node's neighbours (lib/NGT/NGTQ/Quantizer.h:2331-2440): neighbour
+ * o of block o / 16 has its code for subspace s in byte (o / 16) * 8 * ma + 8 * s + (o % 16) / 2,
+ * low nibble for even o (QuantizedObjectProcessingStream, lib/NGT/NGTQ/Quantizer.h:1040-1120).
+ * Even and odd subspaces sum in separate saturating 16-bit lanes; the distance is
+ * sqrt(sum * scale + offset) with the multiply-add fused. */
+void oracle_qg_scan(const OracleQG *qg, const uint8_t *lut, float scale, float offset, uint32_t node, float *ds) {
+  uint32_t a = qg->offsets[node], n = qg->offsets[node + 1] - a;
+  const uint8_t *st = qg->codes + qg->code_off[node];
+  for (uint32_t o = 0; o < n; o++) {
+    const uint8_t *blk = st + (size_t)(o / 16) * 8 * qg->ma;
+    uint32_t oo = o % 16, se = 0, so = 0;
+    for (uint32_t s = 0; s < qg->m; s++) {
+      uint8_t b = blk[8 * s + oo / 2];
+      uint32_t code = (oo & 1) ? (uint32_t)(b >> 4) : (uint32_t)(b & 15);
+      if (s & 1) so += lut[s * 16 + code]; else se += lut[s * 16 + code];
+    }
+    if (se > 65535) se = 65535;
+    if (so > 65535) so = 65535;
+    ds[o] = sqrtf(fmaf((float)(se + so), scale, offset));
+  }
+}
+
+static size_t qg_one(const OracleIndex *ix, const OracleQG *qg, const float *qf, size_t qdim, const void *q,
+                     size_t k, float epsilon, float expansion, float radius0, uint32_t *ids, float *ds,
+                     uint32_t *dc_out, const uint32_t *given_seeds, size_t ngiven) {
+  *dc_out = 0;
+  if (k == 0) return 0;
+  float coef = epsilon + 1.0f;
+  if (coef == 0.0f) coef = 1.1f;                     /* NGT_EXPLORATION_COEFFICIENT */
+  float radius = radius0 < 0.0f ? FLT_MAX : radius0;
+  const float specified = radius;
+  size_t size = k;
+  if (expansion > 1.0f) size = (size_t)((float)k * expansion);
+  /* seeds: the tree leaf of the query (getSeedsFromTree, thinned to k), else graph seeds */
+  uint32_t *seeds = (uint32_t *)malloc(sizeof(uint32_t) * (65536 + ngiven));
+  uint32_t tdc = 0;
+  size_t ns = 0;
+  if (ix->has_tree) ns = tree_seeds(ix, q, k, seeds, &tdc);
+  if (ns == 0) {
+    if (given_seeds) { memcpy(seeds, given_seeds, ngiven * sizeof(uint32_t)); ns = ngiven; }
+    else ns = graph_seeds(ix, seeds);
+  }
+  /* the lookup table of the rotated query */
+  float *rq = (float *)calloc(qg->dim > qdim ? qg->dim : qdim, sizeof(float));
+  memcpy(rq, qf, qdim * sizeof(float));
+  float *rot = (float *)malloc(qg->dim * sizeof(float));
+  oracle_qg_rotate(qg, rq, rot);
+  uint8_t *lut = (uint8_t *)malloc((size_t)qg->m * 16);
+  float scale, offset;
+  oracle_qg_lut(qg, rot, lut, &scale, &offset);
+  /* setupDistances with L2Float::compare, setupSeeds (lib/NGT/Graph.cpp:533-558) */
+  od_t *sd = (od_t *)malloc((ns + 1) * sizeof(od_t));
+  for (size_t i = 0; i < ns; i++) {
+    sd[i].id = seeds[i];
+    sd[i].d = compare(ix->otype, ix->metric, q, row_ptr(ix, ix->objects, seeds[i]), ix->dpad);
+  }
+  qsort(sd, ns, sizeof(od_t), od_cmp);
+  od_t *res = (od_t *)malloc((size + 2) * sizeof(od_t));
+  size_t nres = 0;
+  for (size_t i = 0; i < ns; i++) {
+    if (nres < size && sd[i].d <= radius) maxheap_push(res, &nres, sd[i]);
+    else break;
+  }
+  if (nres >= size && nres > 0) radius = res[0].d;
+  uint64_t *visited = (uint64_t *)calloc((ix->nrows + 63) / 64 + 1, 8);
+  minheap_t cand = {0, 0, 0};
+  for (size_t i = 0; i < ns; i++) {
+    visited[sd[i].id >> 6] |= 1ull << (sd[i].id & 63);
+    minheap_push(&cand, sd[i]);
+  }
+  float expR = coef * radius;
+  float *qd = (float *)malloc(sizeof(float) * 65536);
+  uint32_t dc = 0;
+  while (cand.n) {
+    od_t t = minheap_pop(&cand);
+    if (t.d > expR) break;
+    if (t.id >= qg->nnodes) continue;
+    uint32_t a = qg->offsets[t.id], n = qg->offsets[t.id + 1] - a;
+    oracle_qg_scan(qg, lut, scale, offset, t.id, qd);
+    dc += n;
+    for (uint32_t j = 0; j < n; j++) {
+      float d = qd[j];
+      uint32_t v = qg->ids[a + j];
+      if (d <= expR) {
+        if (visited[v >> 6] & (1ull << (v & 63))) continue;
+        visited[v >> 6] |= 1ull << (v & 63);
+        od_t x = {v, d};
+        minheap_push(&cand, x);
+        if (d <= radius) {
+          maxheap_push(res, &nres, x);
+          if (nres >= size) {
+            if (nres > size) maxheap_pop(res, &nres);
+            radius = res[0].d;
+            expR = coef * radius;
+          }
+        }
+      }
+    }
+  }
+  qsort(res, nres, sizeof(od_t), od_cmp);
+  if (expansion >= 1.0f) {
+    /* exact re-rank, then the radius cut (upper_bound at (0, radius): d < radius) and k */
+    for (size_t i = 0; i < nres; i++)
+      res[i].d = compare(ix->otype, ix->metric, q, row_ptr(ix, ix->objects, res[i].id), ix->dpad);
+    qsort(res, nres, sizeof(od_t), od_cmp);
+    if (specified < FLT_MAX) {
+      size_t keep = 0;
+      while (keep < nres && res[keep].d < specified) keep++;
+      nres = keep;
+    }
+    if (nres > k) nres = k;
+  }
+  for (size_t i = 0; i < nres; i++) { ids[i] = res[i].id; ds[i] = res[i].d; }
+  free(qd); free(visited); free(cand.a); free(res); free(sd); free(lut); free(rot); free(rq); free(seeds);
+  *dc_out = dc;
+  return nres;
+}
+
+/* qf: nq x qdim float queries (as given); qrows: the same prepared as index rows.
+ * Out arrays are nq x k (a QG search returns at most k results). */
+void oracle_qg_search(const OracleIndex *ix, const OracleQG *qg, const float *qf, size_t qdim, const void *qrows,
+                      size_t nq, size_t k, float epsilon, float expansion, float radius, uint32_t *out_ids,
+                      float *out_d, uint32_t *out_n, uint32_t *out_dc, const uint32_t *seed_list,
+                      const uint32_t *seed_off, const uint32_t *seed_cnt, int nthreads) {
+  size_t rb = (size_t)ix->dpad * elem_size(ix->otype);
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads)
+  for (long q = 0; q < (long)nq; q++) {
+    const uint32_t *gs = seed_list ? seed_list + seed_off[q] : NULL;
+    size_t ng = seed_list ? seed_cnt[q] : 0;
+    uint32_t dc = 0;
+    out_n[q] = (uint32_t)qg_one(ix, qg, qf + q * qdim, qdim, (const uint8_t *)qrows + q * rb, k, epsilon,
+                                expansion, radius, out_ids + q * k, out_d + q * k, &dc, gs, ng);
+    if (out_dc) out_dc[q] = dc;
+  }
+}

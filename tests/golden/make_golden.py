@@ -12,6 +12,9 @@ Stored per fixture (tests/golden/<name>/):
   grp.gz, tre.gz    the graph and tree files, gzip-compressed
   obj.gz            the object file, unless it is regenerated from the seeds
                     (meta.json "regenerate_obj": true, sha256 recorded)
+  qg.tar.gz         for quantized-graph fixtures: the files of <index>/qg that a
+                    QG search reads (prf, qr, rqcb, grp, local-*/obj), built by
+                    `qbg create-qg` + `qbg build-qg` (oracle/_ref/qbg)
   meta.json         generator, shapes, seeds, the ngt create options
   golden.npz        queries seed + per-setting ids / distances / counts
 
@@ -26,6 +29,7 @@ import os
 import shutil
 import subprocess
 import sys
+import tarfile
 import tempfile
 
 import numpy as np
@@ -116,6 +120,21 @@ FIXTURES = {
         create="-d 32 -o f -D 2 -E 10 -S 40 -i t", regenerate_obj=True, otype="f",
         prf_set={"EpsilonType": "ResultSize"},
         settings=[("graph", 10, 0.1, None, "ro"), ("graph", 10, 0.2, None, "rw")]),
+    # Quantized graphs (ngtqg_search_index_float); for "qg" settings the edge
+    # column holds the result expansion.
+    "qg_f32_l2_d32": dict(
+        base=("clipped_exponential", dict(n=2000, dim=32, seed=161)),
+        query=("clipped_exponential", dict(n=200, dim=32, seed=162)),
+        create="-d 32 -o f -D 2 -E 16 -S 40 -i t",
+        regenerate_obj=True, otype="f", qg=dict(create="", build="-E 64"),
+        settings=[("qg", 10, 0.1, 3.0, "rw"), ("qg", 10, 0.02, 3.0, "rw"), ("qg", 10, 0.1, 0.0, "rw"),
+                  ("qg", 20, 0.1, 1.5, "rw"), ("qg", 10, 0.1, 1.0, "rw")]),
+    "qg_f32_l2_d64_q2": dict(
+        base=("clipped_exponential", dict(n=2000, dim=64, seed=171)),
+        query=("clipped_exponential", dict(n=200, dim=64, seed=172)),
+        create="-d 64 -o f -D 2 -E 16 -S 40 -i t",
+        regenerate_obj=True, otype="f", qg=dict(create="-Q 2", build="-Q 2 -E 48"),
+        settings=[("qg", 10, 0.1, 3.0, "rw"), ("qg", 10, 0.1, 0.0, "rw")]),
 }
 
 
@@ -154,8 +173,21 @@ def make(name: str, spec: dict) -> None:
             with open(os.path.join(idx, "prf"), "w") as f:
                 for k in sorted(prf):
                     f.write("%s\t%s\n" % (k, prf[k]))
+        if "qg" in spec:
+            run([os.path.join(REF, "qbg"), "create-qg"] + spec["qg"]["create"].split() + [idx])
+            run([os.path.join(REF, "qbg"), "build-qg"] + spec["qg"]["build"].split() + [idx])
         os.makedirs(out, exist_ok=True)
         shutil.copy(os.path.join(idx, "prf"), os.path.join(out, "prf"))
+        if "qg" in spec:
+            qgdir = os.path.join(idx, "qg")
+            members = ["prf", "qr", "rqcb", "grp"] + sorted(
+                "%s/obj" % d for d in os.listdir(qgdir) if d.startswith("local-"))
+            with tarfile.open(os.path.join(out, "qg.tar.gz"), "w:gz") as tf:
+                for m in members:
+                    info = tf.gettarinfo(os.path.join(qgdir, m), arcname=m)
+                    info.mtime, info.uid, info.gid, info.uname, info.gname = 0, 0, 0, "", ""
+                    with open(os.path.join(qgdir, m), "rb") as fi:
+                        tf.addfile(info, fi)
         for fn in ("grp", "tre", "obj"):
             src = os.path.join(idx, fn)
             if not os.path.exists(src) or (fn == "obj" and spec["regenerate_obj"]):
@@ -178,7 +210,7 @@ def make(name: str, spec: dict) -> None:
                 mode, nq = mode.split(":")[0], int(mode.split(":")[1])
             dump = os.path.join(tmp, "out%d" % i)
             run([os.path.join(REF, "ref_dump"), op, idx, qf, str(nq), str(queries.shape[1]), str(k), repr(eps),
-                 "x" if edge is None else str(edge), mode, dump])
+                 "x" if edge is None else repr(edge) if op == "qg" else str(edge), mode, dump])
             raw = np.fromfile(dump, np.uint8)
             ids = raw[:nq * k * 4].view(np.uint32).reshape(nq, k)
             ds = raw[nq * k * 4:2 * nq * k * 4].view(np.float32).reshape(nq, k)
@@ -187,7 +219,8 @@ def make(name: str, spec: dict) -> None:
             settings.append(dict(op=op, k=k, epsilon=eps, edge_size=edge, mode=mode, nq=nq))
         np.savez_compressed(os.path.join(out, "golden.npz"), **arrays)
     meta = dict(name=name, base=spec["base"], query=spec["query"], create=spec["create"],
-                reconstruct=spec.get("reconstruct"), prf_set=spec.get("prf_set"), otype=spec["otype"],
+                reconstruct=spec.get("reconstruct"), prf_set=spec.get("prf_set"), qg=spec.get("qg"),
+                otype=spec["otype"],
                 regenerate_obj=spec["regenerate_obj"], obj_sha256=obj_sha, settings=settings,
                 reference="NGT " + open(os.path.join(REF, "include", "NGT", "version_defs.h")).read().split('"')[-2])
     with open(os.path.join(out, "meta.json"), "w") as f:

@@ -6,6 +6,7 @@ import gzip
 import json
 import os
 import shutil
+import tarfile
 
 import numpy as np
 
@@ -14,7 +15,7 @@ from ngt_gb300 import synthetic
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 INTEGER_FIXTURES = {"c1_f32_l2", "c1_f32_l2_onng", "u8_l2", "u8_l1", "u8_hamming", "u8_jaccard", "f16_l2",
-                    "f32_l2_graphonly", "f32_l2_resultsize"}
+                    "f32_l2_graphonly", "f32_l2_resultsize", "qg_f32_l2_d32", "qg_f32_l2_d64_q2"}
 
 
 def fixture_names():
@@ -39,6 +40,14 @@ def materialize(name: str, root: str):
             if os.path.exists(p):
                 with gzip.open(p) as fi, open(os.path.join(out, fn), "wb") as fo:
                     fo.write(fi.read())
+        qgtar = os.path.join(src, "qg.tar.gz")
+        if os.path.exists(qgtar):
+            with tarfile.open(qgtar) as tf:
+                for m in tf.getmembers():
+                    dst = os.path.join(out, "qg", m.name)
+                    os.makedirs(os.path.dirname(dst), exist_ok=True)
+                    with tf.extractfile(m) as fi, open(dst, "wb") as fo:
+                        fo.write(fi.read())
         if meta["regenerate_obj"]:
             base = generate(meta["base"])
             rows = {"f": np.float32, "c": np.uint8, "h": np.float16}[meta["otype"]](base)

@@ -32,6 +32,10 @@ def test_oracle_matches_reference_golden(name, workdir):
         gi, gd, gc = golden["ids_%d" % i], golden["dist_%d" % i], golden["count_%d" % i]
         if s["op"] == "linear":
             ids, ds, n = o.linear_search(queries[:nq], k=k, threads=4)
+        elif s["op"] == "qg":
+            # quantized graph: the edge column holds the result expansion
+            ids, ds, n, _ = o.qg_search(queries[:nq], k=k, epsilon=s["epsilon"], result_expansion=s["edge_size"],
+                                        threads=4)
         else:
             es = -1 if s["edge_size"] is None else s["edge_size"]
             ids, ds, n, _ = o.search(queries[:nq], k=k, epsilon=s["epsilon"], edge_size=es,
