@@ -44,6 +44,16 @@ class QueryParameters(ctypes.Structure):
     _fields_ = [("size", c_size_t), ("epsilon", c_float), ("radius", c_float), ("edge_size", c_size_t)]
 
 
+class QGQueryParameters(ctypes.Structure):
+    """NGTQGQueryParameters (lib/NGT/NGTQ/Capi.h:41-46)."""
+    _fields_ = [("size", c_size_t), ("epsilon", c_float), ("result_expansion", c_float), ("radius", c_float)]
+
+
+class QGQueryFloat(ctypes.Structure):
+    """NGTQGQueryFloat (lib/NGT/NGTQ/Capi.h:48-51)."""
+    _fields_ = [("query", POINTER(c_float)), ("params", QGQueryParameters)]
+
+
 class QueryStats(ctypes.Structure):
     _fields_ = [("distance_computations", c_uint32), ("expansions", c_uint32), ("visited", c_uint32),
                 ("edges_read", c_uint32), ("status", c_uint32)]
@@ -102,6 +112,14 @@ def load_library() -> ctypes.CDLL:
         "ngtgpu_server_wait": ([c_void_p, ctypes.c_int64, c_void_p, c_size_t, c_void_p, POINTER(ctypes.c_double),
                                 c_void_p], c_bool),
         "ngtgpu_server_destroy": ([c_void_p], None),
+        "ngtqg_open_index": ([c_char_p, c_void_p], c_void_p),
+        "ngtqg_close_index": ([c_void_p], None),
+        "ngtqg_initialize_query_parameters": ([POINTER(QGQueryParameters)], None),
+        "ngtqg_search_index_float": ([c_void_p, QGQueryFloat, c_void_p, c_void_p], c_bool),
+        "ngtqg_gpu_search_batch_float": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QGQueryParameters),
+                                          c_size_t, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p], c_bool),
+        "ngtqg_gpu_search_batch_device": ([c_void_p, c_void_p, c_size_t, POINTER(QGQueryParameters), c_size_t,
+                                           c_void_p, c_size_t, c_void_p, c_void_p, c_void_p, c_void_p], c_bool),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -243,6 +261,129 @@ class Index:
         ok = self._lib.ngtgpu_search_batch_device(self._index, d_rows, nq, params, nparams, d_results, kmax,
                                                   d_counts, d_stats, stream or None, kernel, self._err)
         self._check(ok)
+
+
+class QuantizedIndex:
+    """A quantized-graph index opened on the GPU: mirror of ngtpy.QuantizedIndex
+    (python/src/ngtpy.cpp:573-700) over the ngtqg_* C API.
+
+    ``search(query, size, epsilon, result_expansion)`` returns a list of
+    (id, distance) tuples, ids zero-based unless zero_based_numbering=False;
+    unset arguments take the defaults (size 20, epsilon 0.02, result
+    expansion 3.0, no radius).  The index needs a quantized graph built by the
+    reference (`qbg create-qg` + `qbg build-qg`).
+    """
+
+    def __init__(self, path: str, max_no_of_edges: int = 128, zero_based_numbering: bool = True,
+                 tree_disabled: bool = False, log_disabled: bool = False):
+        if tree_disabled:
+            raise NativeError("tree_disabled=True is not supported: seeds come from the tree when it exists")
+        self._lib = load_library()
+        self._err = self._lib.ngt_create_error_object()
+        self._index = self._lib.ngtqg_open_index(path.encode(), self._err)
+        if not self._index:
+            raise NativeError(self._lib.ngt_get_error_string(self._err).decode())
+        self._results = self._lib.ngt_create_empty_results(self._err)
+        self.dimension = self._lib.ngtgpu_get_dimension(self._index, self._err)
+        self.zero = 1 if zero_based_numbering else 0
+        self.defaults = dict(size=20, epsilon=0.02, result_expansion=3.0, radius=-1.0)
+
+    def _check(self, ok):
+        if not ok:
+            msg = self._lib.ngt_get_error_string(self._err).decode()
+            self._lib.ngt_clear_error_string(self._err)
+            raise NativeError(msg)
+
+    def set(self, num_of_search_objects=0, radius=-1.0, epsilon=-float("inf"), result_expansion=-1.0):
+        """QuantizedIndex.set (python/src/ngtpy.cpp:674-693)."""
+        if num_of_search_objects > 0:
+            self.defaults["size"] = num_of_search_objects
+        if epsilon > -1.0:
+            self.defaults["epsilon"] = epsilon
+        if radius >= 0.0:
+            self.defaults["radius"] = radius
+        if result_expansion >= 0.0:
+            self.defaults["result_expansion"] = result_expansion
+
+    def _params(self, size, epsilon, result_expansion):
+        p = QGQueryParameters()
+        p.size = int(size) if size and size > 0 else self.defaults["size"]
+        p.epsilon = float(epsilon) if epsilon is not None and epsilon > -1.0 else self.defaults["epsilon"]
+        p.result_expansion = (float(result_expansion) if result_expansion is not None and result_expansion >= 0.0
+                              else self.defaults["result_expansion"])
+        p.radius = self.defaults["radius"]
+        return p
+
+    def search(self, query, size=0, epsilon=None, result_expansion=None):
+        q = np.ascontiguousarray(query, dtype=np.float32)
+        qq = QGQueryFloat()
+        qq.query = q.ctypes.data_as(POINTER(c_float))
+        qq.params = self._params(size, epsilon, result_expansion)
+        self._check(self._lib.ngtqg_search_index_float(self._index, qq, self._results, self._err))
+        n = self._lib.ngt_get_result_size(self._results, self._err)
+        out = []
+        for i in range(n):
+            r = self._lib.ngt_get_result(self._results, i, self._err)
+            out.append((r.id - self.zero, r.distance))
+        return out
+
+    def batch_search(self, queries, size=0, epsilon=None, result_expansion=None, with_stats: bool = False):
+        """Every row of `queries` in one launch: (ids[nq, m], distances[nq, m], counts[nq]),
+        ids as stored (1-based)."""
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        nq = q.shape[0]
+        p = self._params(size, epsilon, result_expansion)
+        kmax = max(int(p.size), 1)
+        res = np.zeros((nq, kmax), RESULT_DTYPE)
+        counts = np.zeros(nq, np.uint32)
+        stats = np.zeros(nq, QUERY_STATS_DTYPE)
+        ok = self._lib.ngtqg_gpu_search_batch_float(self._index, q.ctypes.data, nq, q.shape[1], ctypes.byref(p), 1,
+                                                    res.ctypes.data, kmax, counts.ctypes.data, stats.ctypes.data,
+                                                    self._err)
+        self._check(ok)
+        m = int(counts.max()) if nq else 0
+        out = (res["id"][:, :m].copy(), res["distance"][:, :m].copy(), counts)
+        return out + (stats,) if with_stats else out
+
+    def search_device(self, d_rows: int, nq: int, params, d_results: int, kmax: int, d_counts: int, d_stats: int,
+                      stream: int = 0):
+        ok = self._lib.ngtqg_gpu_search_batch_device(self._index, d_rows, nq, ctypes.byref(params), 1, d_results,
+                                                     kmax, d_counts, d_stats, stream or None, self._err)
+        self._check(ok)
+
+    def convert_queries(self, queries) -> np.ndarray:
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        rb = int(self._lib.ngtgpu_query_row_bytes(self._index, self._err))
+        rows = np.zeros((q.shape[0], rb), np.uint8)
+        self._check(self._lib.ngtgpu_convert_queries_float(self._index, q.ctypes.data, q.shape[0], q.shape[1],
+                                                           rows.ctypes.data, self._err))
+        return rows
+
+    def kernel_launches(self) -> int:
+        return int(self._lib.ngtgpu_kernel_launches(self._index, self._err))
+
+    def close(self):
+        if getattr(self, "_index", None):
+            self._lib.ngtqg_close_index(self._index)
+            self._index = None
+        if getattr(self, "_results", None):
+            self._lib.ngt_destroy_results(self._results)
+            self._results = None
+        if getattr(self, "_err", None):
+            self._lib.ngt_destroy_error_object(self._err)
+            self._err = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 class Server:

@@ -19,9 +19,11 @@
 extern "C" {
 #include "../../include/ngt_capi.h"
 #include "../../include/ngtgpu.h"
+#include "../../include/ngtq_capi.h"
 }
 
 using ngtg::GraphEngine;
+using ngtg::QGArgs;
 using ngtg::GraphMode;
 using ngtg::QueryType;
 using ngtg::SearchArgs;
@@ -440,6 +442,152 @@ uint64_t ngtgpu_kernel_launches(NGTIndex index, NGTError error) {
     return 0;
   }
   return engine(index)->launches();
+}
+
+// ---- quantized graph (lib/NGT/NGTQ/Capi.cpp) ---------------------------------
+
+NGTQGIndex ngtqg_open_index(const char* index_path, NGTQGError error) {
+  try {
+    if (index_path == nullptr) throw std::runtime_error("index path is NULL");
+    // NGTQG::Index opens the index updatable (tree seeds) plus its quantized graph
+    return static_cast<NGTQGIndex>(new GraphEngine(index_path, GraphMode::Updatable, true));
+  }
+  CAPI_CATCH(error, nullptr)
+}
+
+void ngtqg_close_index(NGTQGIndex index) {
+  if (index == nullptr) return;
+  delete engine(index);
+}
+
+void ngtqg_initialize_query_parameters(NGTQGQueryParameters* parameters) {
+  if (parameters == nullptr) return;
+  parameters->size = 20;
+  parameters->epsilon = 0.03f;
+  parameters->result_expansion = 3.0f;
+  parameters->radius = FLT_MAX;
+}
+
+void ngtqg_initialize_query(NGTQGQuery* query) {
+  if (query == nullptr) return;
+  query->query = nullptr;
+  query->size = 20;
+  query->epsilon = 0.03f;
+  query->result_expansion = 3.0f;
+  query->radius = FLT_MAX;
+}
+
+}  // extern "C"
+
+namespace {
+
+QGArgs qg_args(const NGTQGQueryParameters& p) {
+  QGArgs a;
+  a.size = p.size;
+  a.epsilon = p.epsilon;
+  a.result_expansion = p.result_expansion;
+  a.radius = p.radius < 0.0f ? FLT_MAX : p.radius;      // ngtqg_search_index_ (Capi.cpp:110-112)
+  return a;
+}
+
+bool qg_search_common(NGTQGIndex index, const void* query, QueryType qt, const NGTQGQueryParameters& p,
+                      NGTObjectDistances results, NGTQGError error, const char* fn) {
+  if (index == nullptr || query == nullptr || results == nullptr) {
+    std::stringstream ss;
+    ss << "Capi : " << fn << "() : parametor error: index = " << index << " query = " << query
+       << " results = " << results;
+    set_error(ss, error);
+    return false;
+  }
+  try {
+    GraphEngine* e = engine(index);
+    QGArgs a = qg_args(p);
+    SearchOutput out;
+    e->qg_search(query, qt, 1, e->dimension(), &a, 1, out);
+    fill_results(out, 0, results);
+    return true;
+  } catch (std::exception& err) {
+    std::stringstream ss;
+    ss << "Capi : " << fn << "() : Error: " << err.what();
+    set_error(ss, error);
+    return false;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+bool ngtqg_search_index(NGTQGIndex index, NGTQGQuery query, NGTObjectDistances results, NGTQGError error) {
+  NGTQGQueryParameters p{query.size, query.epsilon, query.result_expansion, query.radius};
+  return qg_search_common(index, query.query, QueryType::Float32, p, results, error, __FUNCTION__);
+}
+
+bool ngtqg_search_index_float(NGTQGIndex index, NGTQGQueryFloat query, NGTObjectDistances results,
+                              NGTQGError error) {
+  return qg_search_common(index, query.query, QueryType::Float32, query.params, results, error, __FUNCTION__);
+}
+
+bool ngtqg_search_index_uint8(NGTQGIndex index, NGTQGQueryUint8 query, NGTObjectDistances results,
+                              NGTQGError error) {
+  return qg_search_common(index, query.query, QueryType::Uint8, query.params, results, error, __FUNCTION__);
+}
+
+bool ngtqg_search_index_float16(NGTQGIndex index, NGTQGQueryFloat16 query, NGTObjectDistances results,
+                                NGTQGError error) {
+  return qg_search_common(index, query.query, QueryType::Float16, query.params, results, error, __FUNCTION__);
+}
+
+bool ngtqg_gpu_search_batch_float(NGTQGIndex index, const float* queries, size_t nq, int32_t dim,
+                                  const NGTQGQueryParameters* params, size_t nparams, NGTObjectDistance* results,
+                                  size_t kmax, uint32_t* counts, void* stats, NGTQGError error) {
+  if (index == nullptr || (nq && (queries == nullptr || results == nullptr || counts == nullptr)) ||
+      params == nullptr || dim <= 0 || !(nparams == 1 || nparams == nq)) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " queries = " << queries << " nq = " << nq
+                                       << " nparams = " << nparams << " dim = " << dim);
+    return false;
+  }
+  try {
+    std::vector<QGArgs> a;
+    for (size_t i = 0; i < nparams; i++) {
+      a.push_back(qg_args(params[i]));
+      if (a.back().size > kmax) throw std::runtime_error("a query asks for more results than kmax");
+    }
+    SearchOutput out;
+    engine(index)->qg_search(queries, QueryType::Float32, nq, (size_t)dim, a.data(), a.size(), out);
+    for (size_t q = 0; q < nq; q++) {
+      counts[q] = out.counts[q];
+      for (uint32_t i = 0; i < out.counts[q]; i++) {
+        const ngtg::ObjDist& o = out.results[q * out.kmax + i];
+        results[q * kmax + i] = NGTObjectDistance{o.id, o.distance};
+      }
+      if (stats) std::memcpy(static_cast<NGTGPUQueryStats*>(stats) + q, &out.stats[q], sizeof(NGTGPUQueryStats));
+    }
+    return true;
+  }
+  CAPI_CATCH(error, false)
+}
+
+bool ngtqg_gpu_search_batch_device(NGTQGIndex index, const void* d_rows, size_t nq,
+                                   const NGTQGQueryParameters* params, size_t nparams, NGTObjectDistance* d_results,
+                                   size_t kmax, uint32_t* d_counts, void* d_stats, void* stream, NGTQGError error) {
+  if (index == nullptr || (nq && (d_rows == nullptr || d_results == nullptr || d_counts == nullptr ||
+                                  d_stats == nullptr)) ||
+      params == nullptr || !(nparams == 1 || nparams == nq)) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " rows = " << d_rows << " nq = " << nq << " nparams = " << nparams);
+    return false;
+  }
+  try {
+    std::vector<QGArgs> a;
+    for (size_t i = 0; i < nparams; i++) a.push_back(qg_args(params[i]));
+    GraphEngine* e = engine(index);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : e->stream();
+    e->qg_search_device(static_cast<const uint4*>(d_rows), nq, a.data(), a.size(),
+                        reinterpret_cast<ngtg::ObjDist*>(d_results), d_counts,
+                        static_cast<ngtg::QueryStats*>(d_stats), kmax, s);
+    return true;
+  }
+  CAPI_CATCH(error, false)
 }
 
 }  // extern "C"

@@ -54,6 +54,39 @@ struct QueryParams {
   uint32_t out_off;      // offset of this query's results in the output arrays
 };
 
+// Quantized graph in HBM (NGTQG, lib/NGT/NGTQ/QuantizedGraph.h):
+//   rotation   : [dim][dim] float, element [p*dim + c] (null: no rotation)
+//   gcentroid  : [dim] float (the single global centroid)
+//   lcentroids : [m][16][ld] float
+//   offsets/ids: CSR of the quantized graph (each node's first <= E edges)
+//   codes      : per node, blocks of 16 neighbours x ma subspaces x 4 bits
+//                (8*ma bytes per block; neighbour o of a block has subspace s's
+//                code in byte 8*s + o/2, low nibble for even o), starting at
+//                byte 16*code_off16[node]
+struct DevQG {
+  const float* rotation = nullptr;
+  const float* gcentroid = nullptr;
+  const float* lcentroids = nullptr;
+  const uint32_t* offsets = nullptr;
+  const uint32_t* ids = nullptr;
+  const uint32_t* code_off16 = nullptr;
+  const uint8_t* codes = nullptr;
+  uint32_t dim = 0, m = 0, ld = 0, ma = 0, nnodes = 0;
+};
+
+// Per-query parameters of a quantized-graph search (NGTQG::SearchContainer
+// after ngtqg_search_index_, lib/NGT/NGTQ/Capi.cpp:81-127).
+struct QGParams {
+  uint32_t size;         // result-set size during the search: size x result expansion when that is > 1
+  uint32_t k;            // requested size
+  float radius;          // initial radius (FLT_MAX for none)
+  float coef;            // exploration coefficient (1 + epsilon)
+  uint32_t rerank;       // 1 when result expansion >= 1: exact re-rank, radius cut, truncation to k
+  uint32_t seed_off;     // as QueryParams
+  uint32_t seed_cnt;
+  uint32_t out_off;
+};
+
 // Per-query counters written by the kernels.
 struct QueryStats {
   uint32_t distance_computations;

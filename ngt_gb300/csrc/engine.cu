@@ -15,6 +15,7 @@
 
 #include "graph_exact.cuh"
 #include "graph_fast.cuh"
+#include "qg_search.cuh"
 #include "kernels.h"
 #include "linear_select.cuh"
 #include "seed_rng.h"
@@ -81,15 +82,17 @@ bool is_normalized(Metric m) {
 
 }  // namespace
 
-GraphEngine::GraphEngine(const std::string& path, GraphMode mode) : mode_(mode) {
+GraphEngine::GraphEngine(const std::string& path, GraphMode mode, bool quantized) : mode_(mode) {
   load_index(path, host_);
   if (!exact_kernel(host_.prop.otype, host_.prop.metric))
     throw std::runtime_error("unsupported combination of object type and distance type in " + path);
   if (is_normalized(host_.prop.metric) && host_.prop.otype == ObjType::Uint8)
     throw std::runtime_error("normalized distances over uint8 objects are not supported");
+  if (quantized) read_qg();
   NGT_CUDA(cudaGetDevice(&device_));
   NGT_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
   upload();
+  if (quantized) upload_qg();
 }
 
 GraphEngine::~GraphEngine() {
@@ -110,6 +113,7 @@ GraphEngine::~GraphEngine() {
     cudaFree(sc.work);
   }
   cudaFree(d_bf16_);
+  for (void* p : qg_buffers_) cudaFree(p);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -213,49 +217,54 @@ void GraphEngine::build_params(const SearchArgs* args, size_t nargs, size_t nq, 
     qp.coef = coef;
     qp.edge_size = (uint32_t)std::min<size_t>(edge_size_for(a), 0xffffffffu);
     qp.out_off = (uint32_t)(i * kmax);
-    if (p.has_tree) {
-      // GraphAndTreeIndex::getSeedsFromTree: seedSize = SeedSize or size, capped by size;
-      // AllLeafNodes keeps the whole leaf.
-      size_t seed_size = p.seed_size == 0 ? a.size : (size_t)p.seed_size;
-      if (seed_size > a.size) seed_size = a.size;
-      if (p.seed_type == 4) seed_size = SIZE_MAX;
-      uint32_t t = seed_table(seed_size == 0 ? 1 : seed_size);
-      qp.seed_off = t * (nleaves_ + 1);
-      qp.seed_cnt = 0xffffffffu;
-    } else {
-      // Graph-only index: GraphIndex::getSeedsFromGraph (lib/NGT/Index.h:1658-1679).
-      size_t n = host_.nrows ? host_.nrows - 1 : 0;
-      size_t ss = std::min<size_t>(n, (size_t)p.seed_size);
-      qp.seed_off = (uint32_t)seed_list.size();
-      if (p.seed_type == 2) {
-        for (size_t s = 1; s <= ss; s++) seed_list.push_back((uint32_t)s);
-      } else if (p.seed_type == 3) {
-        seed_list.push_back(1u);
-      } else {
-        // getRandomSeeds draws from the process-global rand() without
-        // reseeding; here every query draws from a generator seeded with 1 so
-        // that results are reproducible.
-        GlibcRand rng(1);
-        std::vector<uint32_t> chosen;
-        size_t empty = 0;
-        while (chosen.size() < ss) {
-          double r = rng.unit();
-          size_t idx = (size_t)std::floor((double)n * r) + 1;
-          if (!host_.present[idx]) {
-            if (++empty > n) break;
-            continue;
-          }
-          if (std::find(chosen.begin(), chosen.end(), (uint32_t)idx) != chosen.end()) continue;
-          chosen.push_back((uint32_t)idx);
-        }
-        seed_list.insert(seed_list.end(), chosen.begin(), chosen.end());
-      }
-      qp.seed_cnt = (uint32_t)(seed_list.size() - qp.seed_off);
-    }
+    seed_params(a.size, qp.seed_off, qp.seed_cnt, seed_list);
     params[i] = qp;
     max_size = std::max<uint32_t>(max_size, qp.size);
   }
   if (seed_list.empty()) seed_list.push_back(0);
+}
+
+void GraphEngine::seed_params(size_t k, uint32_t& seed_off, uint32_t& seed_cnt, std::vector<uint32_t>& seed_list) {
+  const Property& p = host_.prop;
+  if (p.has_tree) {
+    // GraphAndTreeIndex::getSeedsFromTree: seedSize = SeedSize or size, capped by size;
+    // AllLeafNodes keeps the whole leaf.
+    size_t seed_size = p.seed_size == 0 ? k : (size_t)p.seed_size;
+    if (seed_size > k) seed_size = k;
+    if (p.seed_type == 4) seed_size = SIZE_MAX;
+    uint32_t t = seed_table(seed_size == 0 ? 1 : seed_size);
+    seed_off = t * (nleaves_ + 1);
+    seed_cnt = 0xffffffffu;
+    return;
+  }
+  // Graph-only index: GraphIndex::getSeedsFromGraph (lib/NGT/Index.h:1658-1679).
+  size_t n = host_.nrows ? host_.nrows - 1 : 0;
+  size_t ss = std::min<size_t>(n, (size_t)p.seed_size);
+  seed_off = (uint32_t)seed_list.size();
+  if (p.seed_type == 2) {
+    for (size_t s = 1; s <= ss; s++) seed_list.push_back((uint32_t)s);
+  } else if (p.seed_type == 3) {
+    seed_list.push_back(1u);
+  } else {
+    // getRandomSeeds draws from the process-global rand() without reseeding;
+    // here every query draws from a generator seeded with 1 so that results
+    // are reproducible.
+    GlibcRand rng(1);
+    std::vector<uint32_t> chosen;
+    size_t empty = 0;
+    while (chosen.size() < ss) {
+      double r = rng.unit();
+      size_t idx = (size_t)std::floor((double)n * r) + 1;
+      if (!host_.present[idx]) {
+        if (++empty > n) break;
+        continue;
+      }
+      if (std::find(chosen.begin(), chosen.end(), (uint32_t)idx) != chosen.end()) continue;
+      chosen.push_back((uint32_t)idx);
+    }
+    seed_list.insert(seed_list.end(), chosen.begin(), chosen.end());
+  }
+  seed_cnt = (uint32_t)(seed_list.size() - seed_off);
 }
 
 size_t GraphEngine::output_size(const SearchArgs& a) const {
@@ -680,6 +689,149 @@ void GraphEngine::search_device_noalloc(void* scratch, size_t scratch_bytes, con
   // the host parameter vectors must outlive the copies above
   NGT_CUDA(cudaStreamSynchronize(stream));
   launches_++;
+}
+
+// ---- quantized graph --------------------------------------------------------
+
+void GraphEngine::read_qg() {
+  if (host_.prop.otype != ObjType::Float || host_.prop.metric != Metric::L2)
+    throw std::runtime_error("the quantized graph search supports float objects with the L2 distance only");
+  load_qg(host_.path, host_.nrows, qg_);
+  if (!qg_kernel(qg_.m)) throw std::runtime_error("too many subspaces in the quantized graph");
+}
+
+void GraphEngine::upload_qg() {
+  NGT_CUDA(cudaSetDevice(device_));
+  auto up = [&](const void* src, size_t bytes) {
+    void* p = dmalloc_copy<void>(src, bytes);
+    qg_buffers_.push_back(p);
+    return p;
+  };
+  dqg_.rotation = qg_.rotation.empty() ? nullptr
+                                       : static_cast<const float*>(up(qg_.rotation.data(), qg_.rotation.size() * 4));
+  dqg_.gcentroid = static_cast<const float*>(up(qg_.gcentroid.data(), qg_.gcentroid.size() * 4));
+  dqg_.lcentroids = static_cast<const float*>(up(qg_.lcentroids.data(), qg_.lcentroids.size() * 4));
+  dqg_.offsets = static_cast<const uint32_t*>(up(qg_.offsets.data(), qg_.offsets.size() * 4));
+  dqg_.ids = static_cast<const uint32_t*>(up(qg_.ids.data(), qg_.ids.size() * 4));
+  dqg_.code_off16 = static_cast<const uint32_t*>(up(qg_.code_off16.data(), qg_.code_off16.size() * 4));
+  dqg_.codes = static_cast<const uint8_t*>(up(qg_.codes.data(), qg_.codes.size()));
+  dqg_.dim = qg_.dim;
+  dqg_.m = qg_.m;
+  dqg_.ld = qg_.ld;
+  dqg_.ma = qg_.ma;
+  dqg_.nnodes = qg_.nnodes;
+  qg_loaded_ = true;
+}
+
+void GraphEngine::open_qg() {
+  std::lock_guard<std::mutex> lock(mu_);
+  if (qg_loaded_) return;
+  read_qg();
+  upload_qg();
+}
+
+void GraphEngine::qg_search_device(const uint4* d_rows, size_t nq, const QGArgs* args, size_t nargs,
+                                   ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, size_t kmax,
+                                   cudaStream_t stream) {
+  if (!qg_loaded_) open_qg();
+  std::lock_guard<std::mutex> lock(mu_);
+  NGT_CUDA(cudaSetDevice(device_));
+  if (nq == 0) return;
+  // ngtqg_search_index_ / NGTQG::Index::search (lib/NGT/NGTQ/Capi.cpp:81-127,
+  // lib/NGT/NGTQ/QuantizedGraph.h:283-296,449-497)
+  std::vector<QGParams> params(nq);
+  std::vector<uint32_t> seeds;
+  uint32_t max_size = 1;
+  for (size_t i = 0; i < nq; i++) {
+    const QGArgs& a = args[nargs == 1 ? 0 : i];
+    if (a.size > kmax) throw std::runtime_error("result size larger than the output capacity");
+    QGParams qp{};
+    float coef = a.epsilon + 1.0f;
+    if (coef == 0.0f) coef = 1.1f;
+    size_t size = a.size;
+    if (a.result_expansion > 1.0f) size = (size_t)((float)a.size * a.result_expansion);
+    qp.size = (uint32_t)std::min<size_t>(size, 0xffffffffu);
+    qp.k = (uint32_t)a.size;
+    qp.radius = a.radius < 0.0f ? FLT_MAX : a.radius;
+    qp.coef = coef;
+    qp.rerank = a.result_expansion >= 1.0f ? 1u : 0u;
+    qp.out_off = (uint32_t)(i * kmax);
+    if (a.size > 0) seed_params(a.size, qp.seed_off, qp.seed_cnt, seeds);
+    params[i] = qp;
+    max_size = std::max<uint32_t>(max_size, qp.size);
+  }
+  if (seeds.empty()) seeds.push_back(0);
+  ExactConfig cfg{};
+  cfg.kcap = max_size + 1;
+  cfg.ccap = 1024;
+  cfg.hcap = 8192;
+  cfg.mode = (uint32_t)GraphMode::Updatable;
+  cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));
+  cfg.bitmap_words = (host_.nrows + 31) / 32;
+  cfg.ocap = kOverflowCapacity;
+  if (cfg.kcap > cfg.ccap) throw std::runtime_error("size x result expansion too large for the quantized graph search");
+  int max_smem = 0;
+  NGT_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
+  size_t smem = qg_kernel_smem_bytes(dev_.row_chunks, qg_.dim, qg_.m, cfg);
+  while (smem > (size_t)max_smem && cfg.hcap > 2048) {
+    cfg.hcap >>= 1;
+    smem = qg_kernel_smem_bytes(dev_.row_chunks, qg_.dim, qg_.m, cfg);
+  }
+  if (smem > (size_t)max_smem) throw std::runtime_error("quantized graph search state does not fit in shared memory");
+  QGKernelFn fn = qg_kernel(qg_.m);
+  NGT_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0, sms = 0;
+  NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kExactThreads, smem));
+  NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+  size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
+  ensure_scratch(grid);
+  QGParams* d_params = nullptr;
+  uint32_t* d_seeds = nullptr;
+  NGT_CUDA(cudaMallocAsync(&d_params, nq * sizeof(QGParams), stream));
+  NGT_CUDA(cudaMallocAsync(&d_seeds, seeds.size() * 4, stream));
+  NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QGParams), cudaMemcpyHostToDevice, stream));
+  NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, stream));
+  fn<<<(unsigned)grid, kExactThreads, smem, stream>>>(dev_, dqg_, d_rows, (uint32_t)nq, d_params, d_seeds, d_out,
+                                                       d_counts, d_stats, d_bitmaps_, d_overflow_, cfg);
+  NGT_CUDA(cudaGetLastError());
+  launches_++;
+  NGT_CUDA(cudaFreeAsync(d_params, stream));
+  NGT_CUDA(cudaFreeAsync(d_seeds, stream));
+  // the pageable host parameter copies above are complete once they return
+}
+
+void GraphEngine::qg_search(const void* queries, QueryType qt, size_t nq, size_t qdim, const QGArgs* args,
+                            size_t nargs, SearchOutput& out) {
+  if (!qg_loaded_) open_qg();
+  NGT_CUDA(cudaSetDevice(device_));
+  std::vector<uint8_t> rows;
+  convert_queries(queries, qt, nq, qdim, rows);
+  size_t kmax = 1;                                  // a quantized-graph query returns at most its size
+  for (size_t i = 0; i < nargs; i++) kmax = std::max(kmax, args[i].size);
+  out.kmax = kmax;
+  out.results.assign(nq * kmax, ObjDist{0, 0.f});
+  out.counts.assign(nq, 0);
+  out.stats.assign(nq, QueryStats{});
+  if (nq == 0) return;
+  uint4* d_rows = nullptr;
+  ObjDist* d_out = nullptr;
+  uint32_t* d_counts = nullptr;
+  QueryStats* d_stats = nullptr;
+  cudaStream_t s = stream_;
+  NGT_CUDA(cudaMallocAsync(&d_rows, rows.size(), s));
+  NGT_CUDA(cudaMallocAsync(&d_out, nq * kmax * sizeof(ObjDist), s));
+  NGT_CUDA(cudaMallocAsync(&d_counts, nq * 4, s));
+  NGT_CUDA(cudaMallocAsync(&d_stats, nq * sizeof(QueryStats), s));
+  NGT_CUDA(cudaMemcpyAsync(d_rows, rows.data(), rows.size(), cudaMemcpyHostToDevice, s));
+  qg_search_device(d_rows, nq, args, nargs, d_out, d_counts, d_stats, kmax, s);
+  NGT_CUDA(cudaMemcpyAsync(out.results.data(), d_out, nq * kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, s));
+  NGT_CUDA(cudaMemcpyAsync(out.counts.data(), d_counts, nq * 4, cudaMemcpyDeviceToHost, s));
+  NGT_CUDA(cudaMemcpyAsync(out.stats.data(), d_stats, nq * sizeof(QueryStats), cudaMemcpyDeviceToHost, s));
+  NGT_CUDA(cudaFreeAsync(d_rows, s));
+  NGT_CUDA(cudaFreeAsync(d_out, s));
+  NGT_CUDA(cudaFreeAsync(d_counts, s));
+  NGT_CUDA(cudaFreeAsync(d_stats, s));
+  NGT_CUDA(cudaStreamSynchronize(s));
 }
 
 }  // namespace ngtg

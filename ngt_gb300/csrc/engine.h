@@ -37,6 +37,15 @@ struct FastTuning {
   float rerank_factor = 0.f;   // re-ranked entries = ceil(size * factor)
 };
 
+// Parameters of one quantized-graph query (NGTQGQueryParameters,
+// lib/NGT/NGTQ/Capi.h; defaults of ngtqg_initialize_query_parameters).
+struct QGArgs {
+  size_t size = 20;
+  float epsilon = 0.03f;
+  float result_expansion = 3.0f;
+  float radius = -1.0f;            // < 0 means FLT_MAX
+};
+
 struct SearchOutput {
   std::vector<ObjDist> results;    // nq * kmax
   std::vector<uint32_t> counts;    // nq
@@ -48,7 +57,9 @@ class CudaError;
 
 class GraphEngine {
  public:
-  GraphEngine(const std::string& path, GraphMode mode);
+  // quantized = true also reads the quantized graph (<path>/qg) before any
+  // device work, so that a damaged one is reported like a damaged index.
+  GraphEngine(const std::string& path, GraphMode mode, bool quantized = false);
   ~GraphEngine();
   GraphEngine(const GraphEngine&) = delete;
   GraphEngine& operator=(const GraphEngine&) = delete;
@@ -60,6 +71,21 @@ class GraphEngine {
   // Graph search over host queries (row-major nq x qdim).
   void search(const void* queries, QueryType qt, size_t nq, size_t qdim, const SearchArgs* args, size_t nargs,
               SearchOutput& out, Kernel kernel = Kernel::Exact);
+  // Quantized graph (<index>/qg): loads it on first use; throws when the index
+  // has none or it cannot be searched here (float objects, L2 only).
+  void open_qg();
+  bool has_qg() const { return qg_loaded_; }
+ private:
+  void read_qg();
+  void upload_qg();
+ public:
+  const HostQG& qg_host() const { return qg_; }
+  // ngtqg_search_index over host queries (row-major nq x qdim).
+  void qg_search(const void* queries, QueryType qt, size_t nq, size_t qdim, const QGArgs* args, size_t nargs,
+                 SearchOutput& out);
+  // The same over converted query rows resident on the device.
+  void qg_search_device(const uint4* d_rows, size_t nq, const QGArgs* args, size_t nargs, ObjDist* d_out,
+                        uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream);
   // Exhaustive search (exact ids, ties broken by id).
   void linear_search(const void* queries, QueryType qt, size_t nq, size_t qdim, size_t size, SearchOutput& out);
 
@@ -116,6 +142,8 @@ class GraphEngine {
   uint32_t seed_table(size_t seed_size);        // index of the thinned-seed table
   void build_params(const SearchArgs* args, size_t nargs, size_t nq, size_t kmax, std::vector<QueryParams>& params,
                     std::vector<uint32_t>& seed_list, uint32_t& max_size);
+  // Seeds of one query of requested size k: tree seeds thinned to k, or graph seeds.
+  void seed_params(size_t k, uint32_t& seed_off, uint32_t& seed_cnt, std::vector<uint32_t>& seed_list);
   size_t edge_size_for(const SearchArgs& a) const;
   void ensure_scratch(size_t grid);
   void ensure_fast_scratch(FastScratch& sc, size_t slots, cudaStream_t stream);
@@ -128,6 +156,11 @@ class GraphEngine {
 
   HostIndex host_;
   GraphMode mode_;
+  // quantized graph
+  HostQG qg_;
+  bool qg_loaded_ = false;
+  DevQG dqg_;
+  std::vector<void*> qg_buffers_;
   int device_ = 0;
   cudaStream_t stream_ = nullptr;
   std::mutex mu_;

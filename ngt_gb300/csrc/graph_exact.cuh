@@ -472,16 +472,21 @@ graph_search_exact_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_
           uint32_t n = s.nres;
           for (uint32_t b = 0; b < nnew; b += 32) {
             uint32_t i = b + lane;
+            // a neighbour joins when within the exploration radius and the radius
+            // of that moment (both only shrink; with epsilon < 0 the first is
+            // the tighter one)
             float d = i < nnew ? nd[i] : FLT_MAX;
-            bool inr = i < nnew && d <= radius;
-            unsigned m = __ballot_sync(0xffffffffu, inr);
+            float lim = fminf(radius, P.coef * radius);
+            unsigned m = __ballot_sync(0xffffffffu, i < nnew && d <= lim);
             while (m) {
               int src = __ffs(m) - 1;
               float dj = __shfl_sync(0xffffffffu, d, src);
               uint32_t idj = nid[b + src];
-              if (dj <= radius) result_insert(res, n, radius, P.size, cfg.mode, pack_key(dj, idj), lane);
+              if (dj <= radius && dj <= P.coef * radius)
+                result_insert(res, n, radius, P.size, cfg.mode, pack_key(dj, idj), lane);
               m &= (src == 31) ? 0u : ~((2u << src) - 1u);
-              m &= __ballot_sync(0xffffffffu, i < nnew && d <= radius);
+              lim = fminf(radius, P.coef * radius);
+              m &= __ballot_sync(0xffffffffu, i < nnew && d <= lim);
             }
           }
           if (lane == 0) {

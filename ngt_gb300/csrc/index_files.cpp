@@ -3,6 +3,7 @@
 // rejected with a message instead of producing a partial index.
 #include "index_files.h"
 
+#include <algorithm>
 #include <cstring>
 #include <fstream>
 #include <sstream>
@@ -255,6 +256,111 @@ void load_index(const std::string& dir, HostIndex& ix) {
   read_graph(dir + "/grp", ix);
   if (ix.prop.has_tree) {
     read_tree(dir + "/tre", ix);
+  }
+}
+
+namespace {
+
+std::vector<float> read_float_rows(const std::string& path, uint32_t dim, uint32_t& n_out) {
+  Reader r(path);
+  uint64_t n = r.get<uint64_t>();
+  if (n == 0 || n > 0xFFFFFFFull) fail("invalid object count in " + path);
+  std::vector<float> rows((size_t)n * dim, 0.f);
+  for (uint64_t i = 0; i < n; i++) {
+    char t = r.get<char>();
+    if (t == '-') continue;
+    if (t != '+') fail("corrupted object file " + path);
+    std::memcpy(rows.data() + i * dim, r.take((size_t)dim * 4), (size_t)dim * 4);
+  }
+  if (!r.at_end()) fail("trailing bytes in object file " + path);
+  n_out = (uint32_t)n;
+  return rows;
+}
+
+}  // namespace
+
+void load_qg(const std::string& index_dir, uint32_t nrows, HostQG& q) {
+  const std::string dir = index_dir + "/qg";
+  Property p;
+  {
+    std::ifstream f(dir + "/prf");
+    if (!f.is_open()) fail("no quantized graph: cannot open " + dir + "/prf");
+    std::string line;
+    while (std::getline(f, line)) {
+      if (!line.empty() && line.back() == '\r') line.pop_back();
+      auto tab = line.find('\t');
+      if (tab != std::string::npos) p.kv[line.substr(0, tab)] = line.substr(tab + 1);
+    }
+  }
+  int dim = to_int(p.get("Dimension", "0"), "Dimension");
+  int m = to_int(p.get("LocalDivisionNo", "0"), "LocalDivisionNo");
+  if (dim <= 0 || m <= 0 || dim % m != 0) fail("invalid Dimension / LocalDivisionNo in " + dir + "/prf");
+  if (to_int(p.get("LocalCentroidLimit", "16"), "LocalCentroidLimit") != 16)
+    fail("a quantized graph needs 16 local centroids per subspace");
+  if (to_int(p.get("SingleLocalCodebook", "0"), "SingleLocalCodebook") != 0)
+    fail("a single shared local codebook is not supported for the quantized graph");
+  if (m > 512) fail("more than 512 subspaces are not supported");
+  q.dim = (uint32_t)dim;
+  q.m = (uint32_t)m;
+  q.ld = q.dim / q.m;
+  q.ma = (q.m + 1) / 2 * 2;
+  {
+    Reader r(dir + "/qr");
+    q.rotation.clear();
+    if (!r.at_end()) {
+      uint32_t n = r.get<uint32_t>();
+      if (n != 0) {
+        if ((uint64_t)n != (uint64_t)q.dim * q.dim) fail("rotation size does not match the dimension in " + dir);
+        q.rotation.resize(n);
+        std::memcpy(q.rotation.data(), r.take((size_t)n * 4), (size_t)n * 4);
+      }
+    }
+  }
+  {
+    Reader r(dir + "/rqcb");
+    uint32_t size = r.get<uint32_t>();
+    (void)r.get<uint32_t>();
+    uint32_t pdim = r.get<uint32_t>();
+    if (pdim == 0 || size < pdim) fail("invalid global codebook in " + dir + "/rqcb");
+    const char* src = r.take((size_t)size * 4);
+    q.gcentroid.assign(q.dim, 0.f);
+    std::memcpy(q.gcentroid.data(), src, (size_t)std::min(pdim, q.dim) * 4);
+  }
+  q.lcentroids.assign((size_t)q.m * 16 * q.ld, 0.f);
+  for (uint32_t i = 0; i < q.m; i++) {
+    uint32_t n = 0;
+    std::vector<float> rows = read_float_rows(dir + "/local-" + std::to_string(i) + "/obj", q.ld, n);
+    if (n != 17) fail("local codebook " + std::to_string(i) + " does not hold 16 centroids");
+    std::memcpy(q.lcentroids.data() + (size_t)i * 16 * q.ld, rows.data() + q.ld, (size_t)16 * q.ld * 4);
+  }
+  {
+    Reader r(dir + "/grp");
+    (void)r.get<uint64_t>();
+    uint64_t n = r.get<uint64_t>();
+    if (n > nrows) fail("quantized graph has more nodes than the object repository in " + dir);
+    q.nnodes = (uint32_t)n;
+    q.offsets.assign(n + 1, 0);
+    q.code_off16.assign(n, 0);
+    q.ids.clear();
+    q.codes.clear();
+    for (uint64_t i = 0; i < n; i++) {
+      (void)r.get<uint32_t>();
+      uint32_t cnt = r.get<uint32_t>();
+      const char* src = r.take((size_t)cnt * 4);
+      size_t base = q.ids.size();
+      q.ids.resize(base + cnt);
+      std::memcpy(q.ids.data() + base, src, (size_t)cnt * 4);
+      for (size_t j = base; j < base + cnt; j++)
+        if (q.ids[j] == 0 || q.ids[j] >= nrows) fail("quantized graph edge to an invalid object id in " + dir);
+      q.offsets[i + 1] = (uint32_t)q.ids.size();
+      size_t bytes = cnt ? (size_t)((cnt + 15) / 16) * q.block_bytes() : 0;
+      if (q.codes.size() / 16 > 0xFFFFFFFFull) fail("quantized graph codes exceed 64 GB");
+      q.code_off16[i] = (uint32_t)(q.codes.size() / 16);
+      const char* cs = r.take(bytes);
+      q.codes.insert(q.codes.end(), cs, cs + bytes);
+      q.codes.resize((q.codes.size() + 15) / 16 * 16, 0);
+    }
+    if (!r.at_end()) fail("trailing bytes in " + dir + "/grp");
   }
 }
 

@@ -75,8 +75,39 @@ struct HostIndex {
   size_t row_bytes() const { return (size_t)dpad * elem_size(); }
 };
 
+// Quantized graph of an index (<index>/qg, written by `qbg create-qg` and
+// `qbg build-qg`), as NGTQG::Index reads it:
+//   qg/prf     NGTQ::Property text file           (lib/NGT/NGTQ/Quantizer.h:560-700)
+//   qg/qr      uint32 n, n floats: the rotation   (lib/NGT/NGTQ/Quantizer.h:164-186)
+//   qg/rqcb    uint32 size, dimension, padded dimension, size floats: the
+//              (rotated) global codebook, one centroid for QG
+//                                                 (lib/NGT/NGTQ/Quantizer.h:355-378,3790-3805)
+//   qg/local-i NGT index whose objects 1..16 are subspace i's centroids
+//   qg/grp     uint64 subspaces, uint64 n, then per node: uint32 subspace id,
+//              uint32 count, count neighbour ids, and the neighbours' 4-bit codes
+//              (QuantizedGraphRepository::serialize, lib/NGT/NGTQ/QuantizedGraph.h:170-226;
+//              code layout of QuantizedObjectProcessingStream,
+//              lib/NGT/NGTQ/Quantizer.h:1040-1180)
+struct HostQG {
+  uint32_t dim = 0;                 // quantizer dimension
+  uint32_t m = 0;                   // subspaces (LocalDivisionNo)
+  uint32_t ld = 0;                  // dimensions per subspace
+  uint32_t ma = 0;                  // m rounded up to even
+  std::vector<float> rotation;      // dim*dim, [p*dim + c]; empty = none
+  std::vector<float> gcentroid;     // dim
+  std::vector<float> lcentroids;    // [m][16][ld]
+  uint32_t nnodes = 0;
+  std::vector<uint32_t> offsets;    // nnodes+1
+  std::vector<uint32_t> ids;
+  std::vector<uint32_t> code_off16; // start of each node's code stream, in 16-byte units
+  std::vector<uint8_t> codes;       // every stream padded to 16 bytes
+  size_t block_bytes() const { return (size_t)8 * ma; }   // 16 neighbours
+};
+
 // Throws std::runtime_error with a message on any format or I/O error.
 Property load_property(const std::string& dir);
 void load_index(const std::string& dir, HostIndex& out);
+// Reads <index_dir>/qg; nrows bounds the neighbour ids.
+void load_qg(const std::string& index_dir, uint32_t nrows, HostQG& out);
 
 }  // namespace ngtg

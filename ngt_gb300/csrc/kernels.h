@@ -16,6 +16,12 @@ struct FastConfig;
 typedef void (*FastKernelFn)(DevGraph, const uint4*, const uint4*, uint32_t, const QueryParams*, const uint32_t*,
                              ObjDist*, uint32_t*, QueryStats*, uint32_t*, uint32_t*, unsigned long long*, FastConfig);
 
+typedef void (*QGKernelFn)(DevGraph, DevQG, const uint4*, uint32_t, const QGParams*, const uint32_t*, ObjDist*,
+                           uint32_t*, QueryStats*, uint32_t*, unsigned long long*, ExactConfig);
+// Quantized-graph kernel for m subspaces (nullptr above 512) and its shared memory.
+QGKernelFn qg_kernel(uint32_t m);
+size_t qg_kernel_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, const ExactConfig& c);
+
 // Batched kernel for (object type, metric); bf16_rows selects the bf16 search
 // rows for float objects.  nullptr when unsupported.
 FastKernelFn fast_kernel(ObjType ot, Metric m, bool bf16_rows);

@@ -40,6 +40,8 @@ def test_batch_search_matches_reference(name, workdir):
     from ngt_gb300 import Index
     path, meta, queries, golden = materialize(name, workdir)
     for i, s in enumerate(meta["settings"]):
+        if s["op"] == "qg":
+            continue                      # quantized-graph settings: tests/test_gpu_qg.py
         nq, k = s["nq"], s["k"]
         gi, gd, gc = golden["ids_%d" % i], golden["dist_%d" % i], golden["count_%d" % i]
         with Index(path, read_only=(s["mode"] == "ro")) as ix:
@@ -125,3 +127,21 @@ def test_large_k_and_wide_epsilon_stay_exact(workdir):
     assert np.array_equal(ds, od[:, :ds.shape[1]])
     assert np.array_equal(st["distance_computations"], dc)
     assert (st["status"] & 1 == 0).all()        # no candidate overflow
+
+
+@pytest.mark.parametrize("mode", ["read_only", "updatable"])
+def test_negative_epsilon_matches_oracle(mode, workdir):
+    """With epsilon < 0 the exploration radius is tighter than the radius: a
+    neighbour joins the results only within both (lib/NGT/Graph.cpp:800-818)."""
+    from ngt_gb300 import Index
+    path, meta, queries, _ = materialize("c1_f32_l2", workdir)
+    o = oracle.Oracle(oracle.IndexFiles(path))
+    q = queries[:200]
+    for eps in (-0.02, -0.05):
+        oi, od, on, _ = o.search(q, k=10, epsilon=eps, mode=mode, threads=8)
+        with Index(path, read_only=(mode == "read_only")) as ix:
+            ids, ds, n = ix.batch_search(q, k=10, epsilon=eps)
+        assert np.array_equal(n, on), eps
+        for j in range(len(q)):
+            assert np.array_equal(ids[j, :n[j]], oi[j, :n[j]]), (eps, j)
+            assert np.array_equal(ds[j, :n[j]].view(np.uint32), od[j, :n[j]].view(np.uint32)), (eps, j)

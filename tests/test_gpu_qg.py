@@ -1,0 +1,142 @@
+"""GPU parity of the quantized-graph search (ngtqg_* C API) with the reference.
+
+The golden fixtures were produced by the reference's own ngtqg_search_index_float
+over quantized graphs built by `qbg build-qg`; the GPU results must equal them
+bit for bit (ids, distances, counts), through the single-query C API and the
+batched entry point.  Further settings (radius cut, other epsilons, sizes,
+uint8 queries) are checked against the oracle, itself pinned to the reference.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+import oracle
+from golden_util import materialize
+
+pytestmark = pytest.mark.gpu
+QG_FIXTURES = ["qg_f32_l2_d32", "qg_f32_l2_d64_q2"]
+
+
+@pytest.fixture(scope="module")
+def workdir(tmp_path_factory):
+    return str(tmp_path_factory.mktemp("qg"))
+
+
+@pytest.mark.parametrize("name", QG_FIXTURES)
+def test_qg_batch_equals_reference_golden(name, workdir):
+    from ngt_gb300 import QuantizedIndex
+    path, meta, queries, golden = materialize(name, workdir)
+    with QuantizedIndex(path, zero_based_numbering=False) as ix:
+        for i, s in enumerate(meta["settings"]):
+            nq, k = s["nq"], s["k"]
+            ids, ds, n = ix.batch_search(queries[:nq], size=k, epsilon=s["epsilon"],
+                                         result_expansion=s["edge_size"])
+            gi, gd, gc = golden["ids_%d" % i], golden["dist_%d" % i], golden["count_%d" % i]
+            assert np.array_equal(n, gc), (name, s)
+            w = ids.shape[1]
+            assert np.array_equal(ids, gi[:, :w]), (name, s)
+            assert np.array_equal(ds.view(np.uint32), gd[:, :w].view(np.uint32)), (name, s)
+
+
+@pytest.mark.parametrize("name", QG_FIXTURES)
+def test_qg_single_query_api_equals_reference_golden(name, workdir):
+    from ngt_gb300 import QuantizedIndex
+    path, meta, queries, golden = materialize(name, workdir)
+    with QuantizedIndex(path, zero_based_numbering=False) as ix:
+        s = meta["settings"][0]
+        for j in range(0, 40):
+            r = ix.search(queries[j], size=s["k"], epsilon=s["epsilon"], result_expansion=s["edge_size"])
+            assert len(r) == golden["count_0"][j]
+            assert [a for a, _ in r] == list(golden["ids_0"][j, :len(r)])
+            assert np.array_equal(np.array([b for _, b in r], np.float32), golden["dist_0"][j, :len(r)])
+
+
+@pytest.mark.parametrize("name", QG_FIXTURES)
+@pytest.mark.parametrize("k,eps,expansion", [(10, 0.0, 3.0), (10, 0.05, 2.0), (5, 0.2, 3.0), (30, 0.1, 1.2),
+                                             (10, 0.1, 0.5), (1, 0.1, 3.0), (10, -0.05, 3.0)])
+def test_qg_equals_oracle(name, k, eps, expansion, workdir):
+    from ngt_gb300 import QuantizedIndex
+    path, meta, queries, _ = materialize(name, workdir)
+    o = oracle.Oracle(oracle.IndexFiles(path))
+    q = queries[:120]
+    oi, od, on, _ = o.qg_search(q, k=k, epsilon=eps, result_expansion=expansion, threads=8)
+    with QuantizedIndex(path, zero_based_numbering=False) as ix:
+        ids, ds, n = ix.batch_search(q, size=k, epsilon=eps, result_expansion=expansion)
+    assert np.array_equal(n, on)
+    w = ids.shape[1]
+    assert np.array_equal(ids, oi[:, :w])
+    assert np.array_equal(ds.view(np.uint32), od[:, :w].view(np.uint32))
+
+
+def test_qg_radius_cut_equals_oracle(workdir):
+    from ngt_gb300 import load_library
+    from ngt_gb300.base import QGQueryParameters, RESULT_DTYPE
+    name = "qg_f32_l2_d32"
+    path, meta, queries, _ = materialize(name, workdir)
+    o = oracle.Oracle(oracle.IndexFiles(path))
+    q = np.ascontiguousarray(queries[:100], np.float32)
+    # a radius inside the typical 10-NN distances cuts some results
+    oi, od, on, _ = o.qg_search(q, k=10, epsilon=0.1, result_expansion=3.0, threads=8)
+    radius = float(np.median(od[:, 5]))
+    oi, od, on, _ = o.qg_search(q, k=10, epsilon=0.1, result_expansion=3.0, radius=radius, threads=8)
+    assert (on < 10).any() and (on > 0).any()
+    L = load_library()
+    err = L.ngt_create_error_object()
+    ix = L.ngtqg_open_index(path.encode(), err)
+    assert ix
+    p = QGQueryParameters(10, 0.1, 3.0, radius)
+    res = np.zeros((len(q), 10), RESULT_DTYPE)
+    n = np.zeros(len(q), np.uint32)
+    ok = L.ngtqg_gpu_search_batch_float(ix, q.ctypes.data, len(q), q.shape[1], ctypes.byref(p), 1, res.ctypes.data,
+                                        10, n.ctypes.data, None, err)
+    L.ngtqg_close_index(ix)
+    L.ngt_destroy_error_object(err)
+    assert ok
+    assert np.array_equal(n, on)
+    for j in range(len(q)):
+        assert np.array_equal(res["id"][j, :n[j]], oi[j, :n[j]])
+        assert np.array_equal(res["distance"][j, :n[j]].view(np.uint32), od[j, :n[j]].view(np.uint32))
+
+
+def test_qg_uint8_queries_match_float_queries(workdir):
+    """ngtqg_search_index_uint8 casts the query to the object type (float) first."""
+    from ngt_gb300 import load_library
+    from ngt_gb300.base import QGQueryParameters
+    path, meta, queries, _ = materialize("qg_f32_l2_d32", workdir)
+    L = load_library()
+
+    class QGQueryUint8(ctypes.Structure):
+        _fields_ = [("query", ctypes.POINTER(ctypes.c_uint8)), ("params", QGQueryParameters)]
+
+    L.ngtqg_search_index_uint8.argtypes = [ctypes.c_void_p, QGQueryUint8, ctypes.c_void_p, ctypes.c_void_p]
+    L.ngtqg_search_index_uint8.restype = ctypes.c_bool
+    from ngt_gb300 import QuantizedIndex
+    with QuantizedIndex(path, zero_based_numbering=False) as ix:
+        for j in range(10):
+            qu = np.ascontiguousarray(queries[j].astype(np.uint8))     # integer-valued data: exact
+            qq = QGQueryUint8(qu.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), QGQueryParameters(10, 0.1, 3.0, -1))
+            assert L.ngtqg_search_index_uint8(ix._index, qq, ix._results, ix._err)
+            n = L.ngt_get_result_size(ix._results, ix._err)
+            got = [(L.ngt_get_result(ix._results, i, ix._err).id) for i in range(n)]
+            want = [a for a, _ in ix.search(queries[j], size=10, epsilon=0.1, result_expansion=3.0)]
+            assert got == want
+
+
+def test_qg_size_zero_returns_nothing(workdir):
+    """NGTQG::Index::search returns no result for size 0 (lib/NGT/NGTQ/QuantizedGraph.h:453-457)."""
+    from ngt_gb300 import load_library
+    from ngt_gb300.base import QGQueryParameters, RESULT_DTYPE
+    path, meta, queries, _ = materialize("qg_f32_l2_d32", workdir)
+    q = np.ascontiguousarray(queries[:4], np.float32)
+    L = load_library()
+    err = L.ngt_create_error_object()
+    ix = L.ngtqg_open_index(path.encode(), err)
+    p = QGQueryParameters(0, 0.1, 3.0, -1.0)
+    res = np.zeros((4, 1), RESULT_DTYPE)
+    n = np.full(4, 7, np.uint32)
+    ok = L.ngtqg_gpu_search_batch_float(ix, q.ctypes.data, 4, q.shape[1], ctypes.byref(p), 1, res.ctypes.data, 1,
+                                        n.ctypes.data, None, err)
+    L.ngtqg_close_index(ix)
+    L.ngt_destroy_error_object(err)
+    assert ok and (n == 0).all()

@@ -110,3 +110,35 @@ def test_null_arguments_return_false_with_message(lib):
     ok = lib.ngt_search_index_as_float(None, None, 0, 10, 0.1, -1.0, None, err)
     assert not ok
     assert "parametor error" in lib.ngt_get_error_string(err).decode()
+
+
+@pytest.mark.parametrize("damage", ["truncate_qg_grp", "missing_qr", "short_codebook", "bad_qg_edge", "no_qg",
+                                    "wrong_metric"])
+def test_qg_loader_rejects_damaged_quantized_graph(lib, tmp_path, damage):
+    path, meta, _, _ = materialize("qg_f32_l2_d32", str(tmp_path))
+    qg = os.path.join(path, "qg")
+    if damage == "truncate_qg_grp":
+        data = open(os.path.join(qg, "grp"), "rb").read()
+        open(os.path.join(qg, "grp"), "wb").write(data[: len(data) - 7])
+    elif damage == "missing_qr":
+        os.remove(os.path.join(qg, "qr"))
+    elif damage == "short_codebook":
+        data = open(os.path.join(qg, "local-3", "obj"), "rb").read()
+        rec = 1 + 4                                   # '+' and one float (one dimension per subspace)
+        out = np.uint64(16).tobytes() + data[8:8 + 1 + 15 * rec]
+        open(os.path.join(qg, "local-3", "obj"), "wb").write(out)
+    elif damage == "bad_qg_edge":
+        data = bytearray(open(os.path.join(qg, "grp"), "rb").read())
+        # node 0 (no edges): sid, count 0; node 1: sid, count, then its first id
+        pos = 16 + 8 + 4 + 4
+        data[pos:pos + 4] = np.uint32(10 ** 9).tobytes()
+        open(os.path.join(qg, "grp"), "wb").write(bytes(data))
+    elif damage == "no_qg":
+        shutil.rmtree(qg)
+    elif damage == "wrong_metric":
+        prf = open(os.path.join(path, "prf")).read().replace("DistanceType\tL2", "DistanceType\tL1")
+        open(os.path.join(path, "prf"), "w").write(prf)
+    h, msg = _error_string(lib, "ngtqg_open_index", path)
+    assert h is None
+    assert msg.startswith("Capi : ngtqg_open_index() : Error:"), msg
+    assert "CUDA" not in msg, msg
