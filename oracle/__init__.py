@@ -205,7 +205,7 @@ class OracleQGC(ctypes.Structure):
     _fields_ = [("dim", ctypes.c_uint32), ("m", ctypes.c_uint32), ("ld", ctypes.c_uint32), ("ma", ctypes.c_uint32),
                 ("rotation", ctypes.c_void_p), ("gcentroid", ctypes.c_void_p), ("lcentroids", ctypes.c_void_p),
                 ("nnodes", ctypes.c_uint32), ("offsets", ctypes.c_void_p), ("ids", ctypes.c_void_p),
-                ("code_off", ctypes.c_void_p), ("codes", ctypes.c_void_p)]
+                ("code_off", ctypes.c_void_p), ("codes", ctypes.c_void_p), ("sid", ctypes.c_void_p)]
 
 
 def _read_rows(path: str, dim: int) -> np.ndarray:
@@ -226,10 +226,12 @@ def _read_rows(path: str, dim: int) -> np.ndarray:
 
 
 class QGFiles:
-    """numpy view of the quantized graph of an index (<index>/qg)."""
+    """numpy view of the quantized graph of an index (<index>/qg), or, with
+    blobs=True, of a QBG index directory (same file formats at its top level,
+    one rotated codebook centroid per blob subspace id, blob codes in grp)."""
 
-    def __init__(self, index_path: str):
-        qg = os.path.join(index_path, "qg")
+    def __init__(self, index_path: str, blobs: bool = False):
+        qg = index_path if blobs else os.path.join(index_path, "qg")
         self.prop = read_property(qg)
         self.dim = int(self.prop["Dimension"])
         self.m = int(self.prop["LocalDivisionNo"])
@@ -241,10 +243,11 @@ class QGFiles:
         n = int(np.frombuffer(raw, np.uint32, 1, 0)[0]) if raw else 0
         self.rotation = np.frombuffer(raw, np.float32, n, 4).reshape(self.dim, self.dim).copy() if n else None
         raw = open(os.path.join(qg, "rqcb"), "rb").read()
-        size, _cdim, pdim = np.frombuffer(raw, np.uint32, 3, 0)
-        cb = np.frombuffer(raw, np.float32, int(size), 12)
-        self.gcentroid = np.zeros(self.dim, np.float32)
-        self.gcentroid[:min(int(pdim), self.dim)] = cb[:min(int(pdim), self.dim)]
+        size, _cdim, pdim = (int(v) for v in np.frombuffer(raw, np.uint32, 3, 0))
+        cb = np.frombuffer(raw, np.float32, size, 12).reshape(size // pdim, pdim)
+        self.ncentroids = cb.shape[0]
+        self.gcentroid = np.zeros((self.ncentroids, self.dim), np.float32)
+        self.gcentroid[:, :min(pdim, self.dim)] = cb[:, :min(pdim, self.dim)]
         self.lcentroids = np.zeros((self.m, 16, self.ld), np.float32)
         for i in range(self.m):
             rows = _read_rows(os.path.join(qg, "local-%d" % i, "obj"), self.ld)
@@ -253,10 +256,11 @@ class QGFiles:
         raw = open(os.path.join(qg, "grp"), "rb").read()
         _nsub, nn = np.frombuffer(raw, np.uint64, 2, 0)
         pos = 16
-        counts, ids, code_off, chunks = [], [], [], []
+        counts, ids, code_off, chunks, sids = [], [], [], [], []
         total = 0
         for _ in range(int(nn)):
-            _sid, cnt = (int(v) for v in np.frombuffer(raw, np.uint32, 2, pos))
+            sid, cnt = (int(v) for v in np.frombuffer(raw, np.uint32, 2, pos))
+            sids.append(sid)
             pos += 8
             ids.append(np.frombuffer(raw, np.uint32, cnt, pos))
             pos += 4 * cnt
@@ -273,6 +277,8 @@ class QGFiles:
         self.ids = np.concatenate(ids).astype(np.uint32) if ids else np.zeros(0, np.uint32)
         self.code_off = np.array(code_off, np.uint64)
         self.codes = np.concatenate(chunks) if chunks else np.zeros(0, np.uint8)
+        self.sid = np.array(sids, np.uint32)
+        assert (self.sid < self.ncentroids).all(), "blob subspace id beyond the codebook"
 
 
 class Oracle:
@@ -298,11 +304,17 @@ class Oracle:
                                        ctypes.c_float, ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                        ctypes.c_void_p, ctypes.c_int]
+        L.oracle_qbg_search.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                        ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t,
+                                        ctypes.c_float, ctypes.c_float, ctypes.c_size_t, ctypes.c_int64,
+                                        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_int]
         L.oracle_qg_rotate.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.oracle_qg_lut.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                     ctypes.c_void_p]
         L.oracle_qg_scan.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.c_float,
                                      ctypes.c_uint32, ctypes.c_void_p]
+        L.oracle_qg_scan.restype = ctypes.c_float
         self.qg = None
         f = files
         self._keep = []
@@ -362,9 +374,9 @@ class Oracle:
         w = max(k, int(n.max()) if nq else 0, 1)
         return ids[:, :w], ds[:, :w], n, dc
 
-    def _qg(self):
+    def _qg(self, blobs_path=None):
         if self.qg is None:
-            g = QGFiles(self.f.path)
+            g = QGFiles(blobs_path, blobs=True) if blobs_path else QGFiles(self.f.path)
             self.qgf = g
             s = OracleQGC()
             s.dim, s.m, s.ld, s.ma, s.nnodes = g.dim, g.m, g.ld, g.ma, g.nnodes
@@ -372,6 +384,7 @@ class Oracle:
             s.gcentroid, s.lcentroids = self._p(g.gcentroid), self._p(g.lcentroids)
             s.offsets, s.ids, s.code_off, s.codes = (self._p(g.offsets), self._p(g.ids), self._p(g.code_off),
                                                      self._p(g.codes))
+            s.sid = self._p(g.sid) if blobs_path else None
             self.qg = s
         return self.qg
 
@@ -402,6 +415,28 @@ class Oracle:
                                   so.ctypes.data if so is not None else None,
                                   sc.ctypes.data if sc is not None else None, threads)
         return ids, ds, n, dc
+
+    def qbg_search(self, queries, qbg_path, k=20, epsilon=0.1, blob_epsilon=0.0, result_expansion=3.0,
+                   explored_blobs=256, edges=0, threads=1):
+        """qbg_search_index_float over a QBG index whose global index this Oracle
+        was built on (defaults of qbg_initialize_query_parameters,
+        lib/NGT/NGTQ/Capi.cpp:528-536).  Returns ids, distances, counts, blobs judged."""
+        qg = self._qg(qbg_path)
+        qf = np.zeros((len(queries), self.f.dpad), np.float32)
+        q = np.asarray(queries, np.float32)
+        qf[:, :q.shape[1]] = q
+        rows = self.prepare(q)
+        nq = rows.shape[0]
+        size = int(np.float32(k) * np.float32(result_expansion)) if result_expansion >= 1.0 else k
+        kout = max(size, 1)
+        ids = np.zeros((nq, kout), np.uint32)
+        ds = np.zeros((nq, kout), np.float32)
+        n = np.zeros(nq, np.uint32)
+        nb = np.zeros(nq, np.uint32)
+        self.lib.oracle_qbg_search(ctypes.byref(self.s), ctypes.byref(qg), qf.ctypes.data, self.f.dpad,
+                                   rows.ctypes.data, nq, size, kout, epsilon, blob_epsilon, explored_blobs, edges,
+                                   ids.ctypes.data, ds.ctypes.data, n.ctypes.data, nb.ctypes.data, threads)
+        return ids, ds, n, nb
 
     def qg_lut(self, query):
         """Rotated query, uint8 lookup table, scale and offset of one query."""

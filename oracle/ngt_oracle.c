@@ -552,6 +552,7 @@ typedef struct {
   const uint32_t *ids;       /* neighbour ids */
   const uint64_t *code_off;  /* byte offset of each node's code stream in codes */
   const uint8_t *codes;
+  const uint32_t *sid;       /* QBG: per blob, the codebook centroid of its LUT (NULL: centroid 0) */
 } OracleQG;
 
 /* Rotation::mul (lib/NGT/NGTQ/Quantizer.h:117-160), y[c] = sum_p R[p][c] x[p].  The
@@ -586,7 +587,15 @@ void oracle_qg_rotate(const OracleQG *qg, const float *x, float *y) {
  * product, then FMAs: the contraction of the reference's mul + add); one offset (the
  * table's minimum) and one scale ((max - min) / 255.0) for the whole table; entries
  * (v - offset) / scale rounded to nearest even. */
+static void qg_lut_centroid(const OracleQG *qg, const float *rq, const float *gc, uint8_t *lut, float *scale_out,
+                            float *offset_out);
+
 void oracle_qg_lut(const OracleQG *qg, const float *rq, uint8_t *lut, float *scale_out, float *offset_out) {
+  qg_lut_centroid(qg, rq, qg->gcentroid, lut, scale_out, offset_out);
+}
+
+static void qg_lut_centroid(const OracleQG *qg, const float *rq, const float *gc, uint8_t *lut, float *scale_out,
+                            float *offset_out) {
   size_t m = qg->m, ld = qg->ld;
   float *fl = (float *)malloc(m * 16 * sizeof(float));
   float mn = FLT_MAX, mx = -FLT_MAX;
@@ -594,7 +603,7 @@ void oracle_qg_lut(const OracleQG *qg, const float *rq, uint8_t *lut, float *sca
     for (size_t c = 0; c < 16; c++) {
       float v = 0.0f;
       for (size_t d = 0; d < ld; d++) {
-        float rsv = rq[s * ld + d] - qg->gcentroid[s * ld + d];
+        float rsv = rq[s * ld + d] - gc[s * ld + d];
         float sub = rsv - qg->lcentroids[(s * 16 + c) * ld + d];
         v = d == 0 ? sub * sub : fmaf(sub, sub, v);
       }
@@ -615,7 +624,7 @@ void oracle_qg_lut(const OracleQG *qg, const float *rq, uint8_t *lut, float *sca
  * low nibble for even o (QuantizedObjectProcessingStream, lib/NGT/NGTQ/Quantizer.h:1040-1120).
  * Even and odd subspaces sum in separate saturating 16-bit lanes; the distance is
  * sqrt(sum * scale + offset) with the multiply-add fused. */
-void oracle_qg_scan(const OracleQG *qg, const uint8_t *lut, float scale, float offset, uint32_t node, float *ds) {
+float oracle_qg_scan(const OracleQG *qg, const uint8_t *lut, float scale, float offset, uint32_t node, float *ds) {
   uint32_t a = qg->offsets[node], n = qg->offsets[node + 1] - a;
   const uint8_t *st = qg->codes + qg->code_off[node];
   for (uint32_t o = 0; o < n; o++) {
@@ -630,6 +639,9 @@ void oracle_qg_scan(const OracleQG *qg, const uint8_t *lut, float scale, float o
     if (so > 65535) so = 65535;
     ds[o] = sqrtf(fmaf((float)(se + so), scale, offset));
   }
+  float mn = FLT_MAX;                 /* the scan's minimum (NGTQBG_MIN) */
+  for (uint32_t o = 0; o < n; o++) mn = ds[o] < mn ? ds[o] : mn;
+  return mn;
 }
 
 static size_t qg_one(const OracleIndex *ix, const OracleQG *qg, const float *qf, size_t qdim, const void *q,
@@ -743,5 +755,130 @@ void oracle_qg_search(const OracleIndex *ix, const OracleQG *qg, const float *qf
     out_n[q] = (uint32_t)qg_one(ix, qg, qf + q * qdim, qdim, (const uint8_t *)qrows + q * rb, k, epsilon,
                                 expansion, radius, out_ids + q * k, out_d + q * k, &dc, gs, ng);
     if (out_dc) out_dc[q] = dc;
+  }
+}
+
+/* ---------------- quantized blob graph (QBG) ----------------
+ * QBG::Index::searchInOneStep (lib/NGT/NGTQ/QuantizedBlobGraph.h:1332-1594) as the C API
+ * (qbg_search_index_, lib/NGT/NGTQ/Capi.cpp:549-574) drives it: the result size is
+ * number_of_results x result_expansion (>= 1), no refinement (the C API leaves
+ * refinementExpansion at 0), so the distances returned are the quantized ones.
+ * ix is the global index (blob centroids, their graph and tree); qg the blobs. */
+static size_t qbg_one(const OracleIndex *ix, const OracleQG *qg, const float *qf, size_t qdim, const void *q,
+                      size_t size, float epsilon, float blob_epsilon, size_t explored, int64_t edge_size,
+                      uint32_t *ids, float *ds, uint32_t *blobs_out) {
+  *blobs_out = 0;
+  if (size == 0) return 0;
+  float coef = epsilon + 1.0f;
+  if (coef == 0.0f) coef = 1.1f;
+  float bcoef = blob_epsilon + 1.0f;
+  size_t esz = edge_size_for(ix, edge_size, coef);
+  /* seeds: getSeedsFromTree over the global graph with sc.size = size, else 20 random */
+  uint32_t *seeds = (uint32_t *)malloc(sizeof(uint32_t) * 65536);
+  uint32_t tdc = 0;
+  size_t ns = 0;
+  if (ix->has_tree) ns = tree_seeds(ix, q, size, seeds, &tdc);
+  if (ns == 0) {
+    OracleIndex tmp = *ix;
+    tmp.seed_size = 20;
+    tmp.seed_type = 1;
+    ns = graph_seeds(&tmp, seeds);
+  }
+  od_t *sd = (od_t *)malloc((ns + 1) * sizeof(od_t));
+  for (size_t i = 0; i < ns; i++) {
+    sd[i].id = seeds[i];
+    sd[i].d = compare(ix->otype, ix->metric, q, row_ptr(ix, ix->objects, seeds[i]), ix->dpad);
+  }
+  qsort(sd, ns, sizeof(od_t), od_cmp);
+  uint64_t *checked = (uint64_t *)calloc((ix->nrows + 63) / 64 + 1, 8);
+  minheap_t untraced = {0, 0, 0}, discarded = {0, 0, 0};
+  od_t current = sd[0];
+  float expR = bcoef * current.d;
+  for (size_t i = 0; i < ns; i++) {
+    minheap_push(&untraced, sd[i]);
+    checked[sd[i].id >> 6] |= 1ull << (sd[i].id & 63);
+    if (i > 0) minheap_push(&discarded, sd[i]);
+  }
+  /* rotated query (the query zero-padded to the quantizer dimension) */
+  float *rq = (float *)calloc(qg->dim > qdim ? qg->dim : qdim, sizeof(float));
+  memcpy(rq, qf, qdim * sizeof(float));
+  float *rot = (float *)malloc(qg->dim * sizeof(float));
+  oracle_qg_rotate(qg, rq, rot);
+  uint8_t *lut = (uint8_t *)malloc((size_t)qg->m * 16);
+  float *bd = (float *)malloc(sizeof(float) * 65536);
+  od_t *res = (od_t *)malloc((size + 2) * sizeof(od_t));
+  size_t nres = 0;
+  float radius = FLT_MAX;
+  size_t exploration = 1;
+  uint32_t nblobs = 0;
+  for (;;) {
+    if (untraced.n == 0 || untraced.a[0].d > expR) {
+      exploration++;
+      /* judge the current blob (lib/NGT/NGTQ/QuantizedBlobGraph.h:1033-1080) */
+      uint32_t blob = current.id;
+      float bmin = FLT_MAX;
+      if (blob < qg->nnodes) {
+        uint32_t a = qg->offsets[blob], n = qg->offsets[blob + 1] - a;
+        float scale, offset;
+        uint32_t c = qg->sid ? qg->sid[blob] : 0;
+        qg_lut_centroid(qg, rot, qg->gcentroid + (size_t)c * qg->dim, lut, &scale, &offset);
+        bmin = n ? oracle_qg_scan(qg, lut, scale, offset, blob, bd) : FLT_MAX;
+        nblobs++;
+        if (bmin < radius) {
+          for (uint32_t i = 0; i < n; i++) {
+            if (bd[i] <= radius) {
+              od_t x = {qg->ids[a + i], bd[i]};
+              maxheap_push(res, &nres, x);
+              if (nres > size) maxheap_pop(res, &nres);
+            }
+          }
+          if (nres >= size) radius = res[0].d;
+        }
+      }
+      if (bmin > radius * coef) break;
+      if (exploration > explored) break;
+      if (discarded.n == 0) break;
+      current = minheap_pop(&discarded);
+      expR = bcoef * current.d;
+      continue;
+    }
+    od_t t = minheap_pop(&untraced);
+    uint32_t e0 = ix->offsets[t.id], deg = ix->offsets[t.id + 1] - e0;
+    size_t nsz = deg < esz ? deg : esz;
+    for (size_t j = 0; j < nsz; j++) {
+      uint32_t v = ix->edges[e0 + j];
+      if (checked[v >> 6] & (1ull << (v & 63))) continue;
+      checked[v >> 6] |= 1ull << (v & 63);
+      od_t r = {v, compare(ix->otype, ix->metric, q, row_ptr(ix, ix->objects, v), ix->dpad)};
+      minheap_push(&untraced, r);
+      if (r.d < current.d) {
+        minheap_push(&discarded, current);
+        current = r;
+        expR = bcoef * current.d;
+      } else {
+        minheap_push(&discarded, r);
+      }
+    }
+  }
+  qsort(res, nres, sizeof(od_t), od_cmp);
+  for (size_t i = 0; i < nres; i++) { ids[i] = res[i].id; ds[i] = res[i].d; }
+  free(res); free(bd); free(lut); free(rot); free(rq); free(untraced.a); free(discarded.a); free(checked);
+  free(sd); free(seeds);
+  *blobs_out = nblobs;
+  return nres;
+}
+
+/* qf: nq x qdim float queries; qrows: the same prepared as global-index rows.  kout >= size. */
+void oracle_qbg_search(const OracleIndex *ix, const OracleQG *qg, const float *qf, size_t qdim, const void *qrows,
+                       size_t nq, size_t size, size_t kout, float epsilon, float blob_epsilon, size_t explored,
+                       int64_t edge_size, uint32_t *out_ids, float *out_d, uint32_t *out_n, uint32_t *out_blobs,
+                       int nthreads) {
+  size_t rb = (size_t)ix->dpad * elem_size(ix->otype);
+#pragma omp parallel for schedule(dynamic) num_threads(nthreads)
+  for (long q = 0; q < (long)nq; q++) {
+    uint32_t nb = 0;
+    out_n[q] = (uint32_t)qbg_one(ix, qg, qf + q * qdim, qdim, (const uint8_t *)qrows + q * rb, size, epsilon,
+                                 blob_epsilon, explored, edge_size, out_ids + q * kout, out_d + q * kout, &nb);
+    if (out_blobs) out_blobs[q] = nb;
   }
 }

@@ -3,9 +3,12 @@
 // in this directory) through its own C API (lib/NGT/Capi.h) and dumps the
 // results in binary, so tests/golden/make_golden.py can record golden vectors.
 //
-// usage: ref_dump <graph|linear|qg> <index> <queries.f32> <nq> <dim> <k> <eps> <edge_size|x> <ro|rw> <out>
+// usage: ref_dump <graph|linear|qg|qbg> <index> <queries.f32> <nq> <dim> <k> <eps> <edge_size|x> <ro|rw> <out>
 //   out: nq x k uint32 ids, then nq x k float distances, then nq uint32 counts.
 //   For qg the edge_size argument is the result expansion (ngtqg_search_index_float).
+//   For qbg it is "expansion:explored_blobs:blob_epsilon" (qbg_search_index_float),
+//   and the rows are floor(k * expansion) wide when expansion >= 1 (the C API
+//   returns that many results).
 //   For graph-only indexes srand(1) runs before every query, so that the
 //   random seeds the reference draws are reproducible.
 #include <NGT/Capi.h>
@@ -39,6 +42,50 @@ int main(int argc, char** argv) {
   NGTError err = ngt_create_error_object();
   std::vector<uint32_t> ids(nq * k, 0), cnt(nq, 0);
   std::vector<float> ds(nq * k, 0.f);
+  if (op == "qbg") {
+    float expansion = 0.f, blob_eps = 0.f;
+    unsigned long blobs = 0;
+    if (std::sscanf(argv[8], "%f:%lu:%f", &expansion, &blobs, &blob_eps) != 3) return 2;
+    size_t w = expansion >= 1.0f ? (size_t)((float)k * expansion) : k;
+    ids.assign(nq * w, 0);
+    ds.assign(nq * w, 0.f);
+    QBGIndex qbg = qbg_open_index(index_path, true, err);
+    if (!qbg) {
+      std::fprintf(stderr, "open failed: %s\n", ngt_get_error_string(err));
+      return 4;
+    }
+    NGTObjectDistances res = ngt_create_empty_results(err);
+    for (size_t i = 0; i < nq; i++) {
+      std::srand(1);
+      QBGQueryFloat qf;
+      qf.query = &q[i * dim];
+      qbg_initialize_query_parameters(&qf.params);
+      qf.params.number_of_results = k;
+      qf.params.epsilon = eps;
+      qf.params.blob_epsilon = blob_eps;
+      qf.params.result_expansion = expansion;
+      qf.params.number_of_explored_blobs = blobs;
+      if (!qbg_search_index_float(qbg, qf, res, err)) {
+        std::fprintf(stderr, "search failed: %s\n", ngt_get_error_string(err));
+        return 5;
+      }
+      uint32_t n = ngt_get_result_size(res, err);
+      cnt[i] = n;
+      for (uint32_t j = 0; j < n && j < w; j++) {
+        NGTObjectDistance od = ngt_get_result(res, j, err);
+        ids[i * w + j] = od.id;
+        ds[i * w + j] = od.distance;
+      }
+    }
+    ngt_destroy_results(res);
+    qbg_close_index(qbg);
+    FILE* o = std::fopen(argv[10], "wb");
+    std::fwrite(ids.data(), 4, ids.size(), o);
+    std::fwrite(ds.data(), 4, ds.size(), o);
+    std::fwrite(cnt.data(), 4, cnt.size(), o);
+    std::fclose(o);
+    return 0;
+  }
   if (op == "qg") {
     NGTQGIndex qg = ngtqg_open_index(index_path, err);
     if (!qg) {

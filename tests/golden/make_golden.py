@@ -15,6 +15,10 @@ Stored per fixture (tests/golden/<name>/):
   qg.tar.gz         for quantized-graph fixtures: the files of <index>/qg that a
                     QG search reads (prf, qr, rqcb, grp, local-*/obj), built by
                     `qbg create-qg` + `qbg build-qg` (oracle/_ref/qbg)
+  qbg.tar.gz        for quantized-blob-graph fixtures (no prf/grp/tre/obj.gz of
+                    their own): the files of the QBG index directory a search
+                    reads (prf, qr, rqcb, grp, local-*/obj, global/{prf,obj,grp,tre}),
+                    built by `qbg create` + `qbg append` + `qbg build`
   meta.json         generator, shapes, seeds, the ngt create options
   golden.npz        queries seed + per-setting ids / distances / counts
 
@@ -138,6 +142,66 @@ FIXTURES = {
 }
 
 
+# Quantized blob graphs (qbg_search_index_float).  Settings: ("qbg", k, epsilon,
+# "expansion:explored_blobs:blob_epsilon", "rw").
+QBG_FIXTURES = {
+    "qbg_u8_l2_d32": dict(
+        base=("clipped_exponential", dict(n=20000, dim=32, seed=181)),
+        query=("clipped_exponential", dict(n=100, dim=32, seed=182)),
+        create="-d 32 -D 2 -N 16 -o c", build="-B 1000:10,1000:40,0:200",
+        settings=[("qbg", 10, 0.1, "3.0:16:0.0", "rw"), ("qbg", 10, 0.1, "3.0:256:0.0", "rw"),
+                  ("qbg", 10, 0.0, "1.0:8:0.05", "rw"), ("qbg", 5, 0.2, "2.0:32:0.1", "rw"),
+                  ("qbg", 10, 0.1, "0.5:16:0.0", "rw")]),
+}
+
+
+def make_qbg(name: str, spec: dict) -> None:
+    out = os.path.join(HERE, name)
+    base = gen(spec["base"])
+    queries = gen(spec["query"])
+    with tempfile.TemporaryDirectory() as tmp:
+        tsv = os.path.join(tmp, "base.tsv")
+        np.savetxt(tsv, base.astype(np.int64), fmt="%d", delimiter="\t")
+        idx = os.path.join(tmp, "idx")
+        run([os.path.join(REF, "qbg"), "create"] + spec["create"].split() + [idx])
+        run([os.path.join(REF, "qbg"), "append", idx, tsv])
+        run([os.path.join(REF, "qbg"), "build"] + spec["build"].split() + [idx])
+        os.makedirs(out, exist_ok=True)
+        members = ["prf", "qr", "rqcb", "grp"] + sorted(
+            "%s/obj" % d for d in os.listdir(idx) if d.startswith("local-")) + [
+            "global/prf", "global/obj", "global/grp", "global/tre"]
+        with tarfile.open(os.path.join(out, "qbg.tar.gz"), "w:gz") as tf:
+            for m in members:
+                info = tf.gettarinfo(os.path.join(idx, m), arcname=m)
+                info.mtime, info.uid, info.gid, info.uname, info.gname = 0, 0, 0, "", ""
+                with open(os.path.join(idx, m), "rb") as fi:
+                    tf.addfile(info, fi)
+        qf = os.path.join(tmp, "q.f32")
+        queries.astype(np.float32).tofile(qf)
+        arrays, settings = {}, []
+        for i, (op, k, eps, edge, mode) in enumerate(spec["settings"]):
+            nq = queries.shape[0]
+            dump = os.path.join(tmp, "out%d" % i)
+            run([os.path.join(REF, "ref_dump"), op, idx, qf, str(nq), str(queries.shape[1]), str(k), repr(eps),
+                 edge, mode, dump])
+            exp = float(edge.split(":")[0])
+            w = int(np.float32(k) * np.float32(exp)) if exp >= 1.0 else k
+            raw = np.fromfile(dump, np.uint8)
+            arrays["ids_%d" % i] = raw[:nq * w * 4].view(np.uint32).reshape(nq, w)
+            arrays["dist_%d" % i] = raw[nq * w * 4:2 * nq * w * 4].view(np.float32).reshape(nq, w)
+            arrays["count_%d" % i] = raw[2 * nq * w * 4:].view(np.uint32)
+            e, b, be = edge.split(":")
+            settings.append(dict(op=op, k=k, epsilon=eps, result_expansion=float(e), explored_blobs=int(b),
+                                 blob_epsilon=float(be), mode=mode, nq=nq, width=w))
+        np.savez_compressed(os.path.join(out, "golden.npz"), **arrays)
+    meta = dict(name=name, kind="qbg", base=spec["base"], query=spec["query"], create=spec["create"],
+                build=spec["build"], settings=settings,
+                reference="NGT " + open(os.path.join(REF, "include", "NGT", "version_defs.h")).read().split('"')[-2])
+    with open(os.path.join(out, "meta.json"), "w") as f:
+        json.dump(meta, f, indent=1)
+    print("wrote", out)
+
+
 def gen(spec):
     name, kw = spec
     return getattr(synthetic, name)(**kw)
@@ -229,6 +293,9 @@ def make(name: str, spec: dict) -> None:
 
 
 if __name__ == "__main__":
-    names = sys.argv[1:] or list(FIXTURES)
+    names = sys.argv[1:] or list(FIXTURES) + list(QBG_FIXTURES)
     for n in names:
-        make(n, FIXTURES[n])
+        if n in QBG_FIXTURES:
+            make_qbg(n, QBG_FIXTURES[n])
+        else:
+            make(n, FIXTURES[n])

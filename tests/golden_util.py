@@ -18,8 +18,16 @@ INTEGER_FIXTURES = {"c1_f32_l2", "c1_f32_l2_onng", "u8_l2", "u8_l1", "u8_hamming
                     "f32_l2_graphonly", "f32_l2_resultsize", "qg_f32_l2_d32", "qg_f32_l2_d64_q2"}
 
 
-def fixture_names():
-    return sorted(d for d in os.listdir(GOLDEN) if os.path.isdir(os.path.join(GOLDEN, d)))
+def fixture_names(kind: str = "graph"):
+    """Fixtures of one kind: "graph" (NGT indexes, some with a quantized graph) or "qbg"."""
+    out = []
+    for d in sorted(os.listdir(GOLDEN)):
+        if not os.path.isdir(os.path.join(GOLDEN, d)):
+            continue
+        k = json.load(open(os.path.join(GOLDEN, d, "meta.json"))).get("kind", "graph")
+        if k == kind:
+            out.append(d)
+    return out
 
 
 def generate(spec):
@@ -28,10 +36,20 @@ def generate(spec):
 
 
 def materialize(name: str, root: str):
-    """Writes the index of fixture `name` under root/name; returns (path, meta, queries, golden)."""
+    """Writes the index of fixture `name` under root/name; returns (path, meta, queries, golden).
+    For a QBG fixture the path is the QBG index directory (its global index in path/global)."""
     src = os.path.join(GOLDEN, name)
     meta = json.load(open(os.path.join(src, "meta.json")))
     out = os.path.join(root, name)
+    if meta.get("kind") == "qbg":
+        if not os.path.exists(os.path.join(out, "grp")):
+            with tarfile.open(os.path.join(src, "qbg.tar.gz")) as tf:
+                for m in tf.getmembers():
+                    dst = os.path.join(out, m.name)
+                    os.makedirs(os.path.dirname(dst), exist_ok=True)
+                    with tf.extractfile(m) as fi, open(dst, "wb") as fo:
+                        fo.write(fi.read())
+        return out, meta, generate(meta["query"]), np.load(os.path.join(src, "golden.npz"))
     if not os.path.exists(os.path.join(out, "obj")):
         os.makedirs(out, exist_ok=True)
         shutil.copy(os.path.join(src, "prf"), out)

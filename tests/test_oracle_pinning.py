@@ -103,3 +103,18 @@ def test_oracle_linear_search_matches_readme_known_answer(tmp_path):
         for (gi, gd), (ei, ed) in zip(got, expect[q]):
             assert gi == ei
             assert abs(gd - ed) <= 1e-3 * max(1.0, ed)
+
+
+@pytest.mark.parametrize("name", fixture_names("qbg"))
+def test_oracle_qbg_matches_reference_golden(name, workdir):
+    """QBG (qbg_search_index_float): ids, quantized distances and counts identical."""
+    path, meta, queries, golden = materialize(name, workdir)
+    o = oracle.Oracle(oracle.IndexFiles(os.path.join(path, "global")))
+    for i, s in enumerate(meta["settings"]):
+        ids, ds, n, _ = o.qbg_search(queries[:s["nq"]], path, k=s["k"], epsilon=s["epsilon"],
+                                     blob_epsilon=s["blob_epsilon"], result_expansion=s["result_expansion"],
+                                     explored_blobs=s["explored_blobs"], threads=4)
+        gi, gd, gc = golden["ids_%d" % i], golden["dist_%d" % i], golden["count_%d" % i]
+        assert np.array_equal(n, gc), (name, s)
+        assert np.array_equal(ids[:, :s["width"]], gi), (name, s)
+        assert np.array_equal(ds[:, :s["width"]].view(np.uint32), gd.view(np.uint32)), (name, s)
