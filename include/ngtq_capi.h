@@ -6,8 +6,11 @@
  * and error conventions.  An index is quantized with the reference tools
  * (`qbg create-qg` + `qbg build-qg`, or ngtqg_quantize) and opened here
  * unchanged; the search runs on the GPU and returns the reference's results
- * (same ids and distances, in the same order).  ngtqg_quantize and the QBG
- * functions of that header are not provided.
+ * (same ids and distances, in the same order).  The QBG search subset
+ * (qbg_open_index .. qbg_get_dimension) follows the same rule for indexes built
+ * by `qbg create` / `qbg append` / `qbg build`.  Index construction
+ * (ngtqg_quantize, qbg_create, qbg_append_object, qbg_build_index, ...) stays
+ * with the reference.
  */
 #pragma once
 
@@ -88,6 +91,83 @@ bool ngtqg_gpu_search_batch_float(NGTQGIndex index, const float *queries, size_t
 bool ngtqg_gpu_search_batch_device(NGTQGIndex index, const void *d_rows, size_t nq,
                                    const NGTQGQueryParameters *params, size_t nparams, NGTObjectDistance *d_results,
                                    size_t kmax, uint32_t *d_counts, void *d_stats, void *stream, NGTQGError error);
+
+/* ---- quantized blob graph (QBG) search, lib/NGT/NGTQ/Capi.h ---------------- */
+
+/* lib/NGT/NGTQ/Capi.h:101-103 */
+typedef void *QBGIndex;
+typedef NGTError QBGError;
+typedef NGTObjectDistances QBGObjectDistances;
+
+/* lib/NGT/NGTQ/Capi.h:129-137 */
+typedef struct {
+  size_t number_of_results;
+  float epsilon;
+  float blob_epsilon;
+  float result_expansion;          /* >= 1: number_of_results x this many results (quantized distances) */
+  size_t number_of_explored_blobs;
+  size_t number_of_edges;
+  float radius;                    /* accepted and ignored, as by the reference */
+} QBGQueryParameters;
+
+/* lib/NGT/NGTQ/Capi.h:139-148 */
+typedef struct {
+  float *query;
+  size_t number_of_results;
+  float epsilon;
+  float blob_epsilon;
+  float result_expansion;
+  size_t number_of_explored_blobs;
+  size_t number_of_edges;
+  float radius;
+} QBGQuery;
+
+/* lib/NGT/NGTQ/Capi.h:150-163 */
+typedef struct {
+  float *query;
+  QBGQueryParameters params;
+} QBGQueryFloat;
+
+typedef struct {
+  uint8_t *query;
+  QBGQueryParameters params;
+} QBGQueryUint8;
+
+typedef struct {
+  NGTFloat16 *query;
+  QBGQueryParameters params;
+} QBGQueryFloat16;
+
+/* Opens a built QBG index (its blobs and the global index in <path>/global);
+ * replaces lib/NGT/NGTQ/Capi.h:183 / Capi.cpp:239-250.  An index that has not
+ * been built is rejected here whatever `prebuilt` says. */
+QBGIndex qbg_open_index(const char *index_path, bool prebuilt, QBGError error);
+/* lib/NGT/NGTQ/Capi.h:185 */
+void qbg_close_index(QBGIndex index);
+/* Defaults: 20 results, epsilon 0.1, blob_epsilon 0, result_expansion 3,
+ * 256 explored blobs, 0 edges (all), radius 0 (lib/NGT/NGTQ/Capi.cpp:528-547). */
+void qbg_initialize_query_parameters(QBGQueryParameters *parameters);
+void qbg_initialize_query(QBGQuery *query);
+/* lib/NGT/NGTQ/Capi.h:205-211: one query of the genuine dimension; results
+ * ascending by (distance, id), quantized distances. */
+bool qbg_search_index(QBGIndex index, QBGQuery query, QBGObjectDistances results, QBGError error);
+bool qbg_search_index_float(QBGIndex index, QBGQueryFloat query, QBGObjectDistances results, QBGError error);
+bool qbg_search_index_uint8(QBGIndex index, QBGQueryUint8 query, QBGObjectDistances results, QBGError error);
+bool qbg_search_index_float16(QBGIndex index, QBGQueryFloat16 query, QBGObjectDistances results, QBGError error);
+/* lib/NGT/NGTQ/Capi.h:115-119 */
+uint32_t qbg_get_result_size(QBGObjectDistances results, NGTError error);
+NGTObjectDistance qbg_get_result(const QBGObjectDistances results, const uint32_t idx, NGTError error);
+void qbg_destroy_results(QBGObjectDistances results);
+/* lib/NGT/NGTQ/Capi.h:226: the genuine (query) dimension. */
+size_t qbg_get_dimension(QBGIndex index, QBGError error);
+
+/* Extension: many queries in one launch (replaces a loop over
+ * qbg_search_index_float): results nq x kmax with kmax >= every query's
+ * number_of_results x result_expansion; counts nq; stats NULL or nq
+ * NGTGPUQueryStats (the visited counter holds the blobs judged). */
+bool qbg_gpu_search_batch_float(QBGIndex index, const float *queries, size_t nq, int32_t dim,
+                                const QBGQueryParameters *params, size_t nparams, NGTObjectDistance *results,
+                                size_t kmax, uint32_t *counts, void *stats, QBGError error);
 
 #ifdef __cplusplus
 }

@@ -54,6 +54,18 @@ class QGQueryFloat(ctypes.Structure):
     _fields_ = [("query", POINTER(c_float)), ("params", QGQueryParameters)]
 
 
+class QBGQueryParameters(ctypes.Structure):
+    """QBGQueryParameters (lib/NGT/NGTQ/Capi.h:129-137)."""
+    _fields_ = [("number_of_results", c_size_t), ("epsilon", c_float), ("blob_epsilon", c_float),
+                ("result_expansion", c_float), ("number_of_explored_blobs", c_size_t),
+                ("number_of_edges", c_size_t), ("radius", c_float)]
+
+
+class QBGQueryFloat(ctypes.Structure):
+    """QBGQueryFloat (lib/NGT/NGTQ/Capi.h:150-153)."""
+    _fields_ = [("query", POINTER(c_float)), ("params", QBGQueryParameters)]
+
+
 class QueryStats(ctypes.Structure):
     _fields_ = [("distance_computations", c_uint32), ("expansions", c_uint32), ("visited", c_uint32),
                 ("edges_read", c_uint32), ("status", c_uint32)]
@@ -120,6 +132,13 @@ def load_library() -> ctypes.CDLL:
                                           c_size_t, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p], c_bool),
         "ngtqg_gpu_search_batch_device": ([c_void_p, c_void_p, c_size_t, POINTER(QGQueryParameters), c_size_t,
                                            c_void_p, c_size_t, c_void_p, c_void_p, c_void_p, c_void_p], c_bool),
+        "qbg_open_index": ([c_char_p, c_bool, c_void_p], c_void_p),
+        "qbg_close_index": ([c_void_p], None),
+        "qbg_get_dimension": ([c_void_p, c_void_p], c_size_t),
+        "qbg_initialize_query_parameters": ([POINTER(QBGQueryParameters)], None),
+        "qbg_search_index_float": ([c_void_p, QBGQueryFloat, c_void_p, c_void_p], c_bool),
+        "qbg_gpu_search_batch_float": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QBGQueryParameters),
+                                        c_size_t, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p], c_bool),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -365,6 +384,93 @@ class QuantizedIndex:
     def close(self):
         if getattr(self, "_index", None):
             self._lib.ngtqg_close_index(self._index)
+            self._index = None
+        if getattr(self, "_results", None):
+            self._lib.ngt_destroy_results(self._results)
+            self._results = None
+        if getattr(self, "_err", None):
+            self._lib.ngt_destroy_error_object(self._err)
+            self._err = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class QBGIndex:
+    """A quantized-blob-graph index opened on the GPU through the reference's QBG
+    C API (qbg_open_index / qbg_search_index_float, lib/NGT/NGTQ/Capi.h).
+
+    ``search(query, k, ...)`` returns a list of ObjectDistance (1-based ids,
+    ascending), k x result_expansion of them with quantized distances when the
+    expansion is >= 1, exactly as qbg_search_index_float does.
+    """
+
+    def __init__(self, path: str):
+        self._lib = load_library()
+        self._err = self._lib.ngt_create_error_object()
+        self._index = self._lib.qbg_open_index(path.encode(), True, self._err)
+        if not self._index:
+            raise NativeError(self._lib.ngt_get_error_string(self._err).decode())
+        self._results = self._lib.ngt_create_empty_results(self._err)
+        self.dimension = int(self._lib.qbg_get_dimension(self._index, self._err))
+
+    def _check(self, ok):
+        if not ok:
+            msg = self._lib.ngt_get_error_string(self._err).decode()
+            self._lib.ngt_clear_error_string(self._err)
+            raise NativeError(msg)
+
+    @staticmethod
+    def params(k=20, epsilon=0.1, blob_epsilon=0.0, result_expansion=3.0, explored_blobs=256, edges=0):
+        p = QBGQueryParameters()
+        p.number_of_results, p.epsilon, p.blob_epsilon = int(k), float(epsilon), float(blob_epsilon)
+        p.result_expansion, p.number_of_explored_blobs = float(result_expansion), int(explored_blobs)
+        p.number_of_edges, p.radius = int(edges), 0.0
+        return p
+
+    @staticmethod
+    def result_size(p) -> int:
+        return int(np.float32(p.number_of_results) * np.float32(p.result_expansion)) \
+            if p.result_expansion >= 1.0 else int(p.number_of_results)
+
+    def search(self, query, k=20, epsilon=0.1, blob_epsilon=0.0, result_expansion=3.0, explored_blobs=256, edges=0):
+        q = np.ascontiguousarray(query, dtype=np.float32)
+        qq = QBGQueryFloat()
+        qq.query = q.ctypes.data_as(POINTER(c_float))
+        qq.params = self.params(k, epsilon, blob_epsilon, result_expansion, explored_blobs, edges)
+        self._check(self._lib.qbg_search_index_float(self._index, qq, self._results, self._err))
+        n = self._lib.ngt_get_result_size(self._results, self._err)
+        return [self._lib.ngt_get_result(self._results, i, self._err) for i in range(n)]
+
+    def batch_search(self, queries, k=20, epsilon=0.1, blob_epsilon=0.0, result_expansion=3.0, explored_blobs=256,
+                     edges=0, with_stats: bool = False):
+        """Every row in one launch: (ids[nq, m], distances[nq, m], counts[nq])."""
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        nq = q.shape[0]
+        p = self.params(k, epsilon, blob_epsilon, result_expansion, explored_blobs, edges)
+        kmax = max(self.result_size(p), 1)
+        res = np.zeros((nq, kmax), RESULT_DTYPE)
+        counts = np.zeros(nq, np.uint32)
+        stats = np.zeros(nq, QUERY_STATS_DTYPE)
+        self._check(self._lib.qbg_gpu_search_batch_float(self._index, q.ctypes.data, nq, q.shape[1],
+                                                         ctypes.byref(p), 1, res.ctypes.data, kmax,
+                                                         counts.ctypes.data, stats.ctypes.data, self._err))
+        m = int(counts.max()) if nq else 0
+        out = (res["id"][:, :m].copy(), res["distance"][:, :m].copy(), counts)
+        return out + (stats,) if with_stats else out
+
+    def close(self):
+        if getattr(self, "_index", None):
+            self._lib.qbg_close_index(self._index)
             self._index = None
         if getattr(self, "_results", None):
             self._lib.ngt_destroy_results(self._results)

@@ -23,6 +23,7 @@ extern "C" {
 }
 
 using ngtg::GraphEngine;
+using ngtg::QBGArgs;
 using ngtg::QGArgs;
 using ngtg::GraphMode;
 using ngtg::QueryType;
@@ -585,6 +586,156 @@ bool ngtqg_gpu_search_batch_device(NGTQGIndex index, const void* d_rows, size_t 
     e->qg_search_device(static_cast<const uint4*>(d_rows), nq, a.data(), a.size(),
                         reinterpret_cast<ngtg::ObjDist*>(d_results), d_counts,
                         static_cast<ngtg::QueryStats*>(d_stats), kmax, s);
+    return true;
+  }
+  CAPI_CATCH(error, false)
+}
+
+// ---- quantized blob graph (lib/NGT/NGTQ/Capi.cpp) ------------------------------
+
+QBGIndex qbg_open_index(const char* index_path, bool prebuilt, QBGError error) {
+  (void)prebuilt;
+  try {
+    if (index_path == nullptr) throw std::runtime_error("index path is NULL");
+    return static_cast<QBGIndex>(new GraphEngine(index_path, true));
+  }
+  CAPI_CATCH(error, nullptr)
+}
+
+void qbg_close_index(QBGIndex index) {
+  if (index == nullptr) return;
+  delete engine(index);
+}
+
+void qbg_initialize_query_parameters(QBGQueryParameters* parameters) {
+  if (parameters == nullptr) return;
+  parameters->number_of_results = 20;
+  parameters->epsilon = 0.1f;
+  parameters->blob_epsilon = 0.0f;
+  parameters->result_expansion = 3.0f;
+  parameters->number_of_explored_blobs = 256;
+  parameters->number_of_edges = 0;
+  parameters->radius = 0;
+}
+
+void qbg_initialize_query(QBGQuery* query) {
+  if (query == nullptr) return;
+  query->query = nullptr;
+  query->number_of_results = 20;
+  query->epsilon = 0.1f;
+  query->blob_epsilon = 0.0f;
+  query->result_expansion = 3.0f;
+  query->number_of_explored_blobs = 256;
+  query->number_of_edges = 0;
+  query->radius = 0;
+}
+
+uint32_t qbg_get_result_size(QBGObjectDistances results, NGTError error) {
+  return ngt_get_result_size(results, error);
+}
+
+NGTObjectDistance qbg_get_result(const QBGObjectDistances results, const uint32_t idx, NGTError error) {
+  return ngt_get_result(results, idx, error);
+}
+
+void qbg_destroy_results(QBGObjectDistances results) { ngt_destroy_results(results); }
+
+size_t qbg_get_dimension(QBGIndex index, QBGError error) {
+  if (index == nullptr) {
+    CAPI_PARAM_ERROR(error, "index = " << index);
+    return 0;
+  }
+  return engine(index)->qbg_genuine_dimension();
+}
+
+}  // extern "C"
+
+namespace {
+
+QBGArgs qbg_args(const QBGQueryParameters& p) {
+  QBGArgs a;
+  a.size = p.number_of_results;
+  a.epsilon = p.epsilon;
+  a.blob_epsilon = p.blob_epsilon;
+  a.result_expansion = p.result_expansion;
+  a.explored_blobs = p.number_of_explored_blobs;
+  a.edges = p.number_of_edges;
+  return a;
+}
+
+bool qbg_search_common(QBGIndex index, const void* query, QueryType qt, const QBGQueryParameters& p,
+                       QBGObjectDistances results, QBGError error, const char* fn) {
+  if (index == nullptr || query == nullptr || results == nullptr) {
+    std::stringstream ss;
+    ss << "Capi : " << fn << "() : parametor error: index = " << index << " query = " << query
+       << " results = " << results;
+    set_error(ss, error);
+    return false;
+  }
+  try {
+    GraphEngine* e = engine(index);
+    QBGArgs a = qbg_args(p);
+    SearchOutput out;
+    e->qbg_search(query, qt, 1, e->qbg_genuine_dimension(), &a, 1, out);
+    fill_results(out, 0, results);
+    return true;
+  } catch (std::exception& err) {
+    std::stringstream ss;
+    ss << "Capi : " << fn << "() : Error: " << err.what();
+    set_error(ss, error);
+    return false;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+bool qbg_search_index(QBGIndex index, QBGQuery query, QBGObjectDistances results, QBGError error) {
+  QBGQueryParameters p{query.number_of_results, query.epsilon, query.blob_epsilon, query.result_expansion,
+                       query.number_of_explored_blobs, query.number_of_edges, query.radius};
+  return qbg_search_common(index, query.query, QueryType::Float32, p, results, error, __FUNCTION__);
+}
+
+bool qbg_search_index_float(QBGIndex index, QBGQueryFloat query, QBGObjectDistances results, QBGError error) {
+  return qbg_search_common(index, query.query, QueryType::Float32, query.params, results, error, __FUNCTION__);
+}
+
+bool qbg_search_index_uint8(QBGIndex index, QBGQueryUint8 query, QBGObjectDistances results, QBGError error) {
+  return qbg_search_common(index, query.query, QueryType::Uint8, query.params, results, error, __FUNCTION__);
+}
+
+bool qbg_search_index_float16(QBGIndex index, QBGQueryFloat16 query, QBGObjectDistances results,
+                              QBGError error) {
+  return qbg_search_common(index, query.query, QueryType::Float16, query.params, results, error, __FUNCTION__);
+}
+
+bool qbg_gpu_search_batch_float(QBGIndex index, const float* queries, size_t nq, int32_t dim,
+                                const QBGQueryParameters* params, size_t nparams, NGTObjectDistance* results,
+                                size_t kmax, uint32_t* counts, void* stats, QBGError error) {
+  if (index == nullptr || (nq && (queries == nullptr || results == nullptr || counts == nullptr)) ||
+      params == nullptr || dim <= 0 || !(nparams == 1 || nparams == nq)) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " queries = " << queries << " nq = " << nq
+                                       << " nparams = " << nparams << " dim = " << dim);
+    return false;
+  }
+  try {
+    std::vector<QBGArgs> a;
+    for (size_t i = 0; i < nparams; i++) {
+      a.push_back(qbg_args(params[i]));
+      if (GraphEngine::qbg_result_size(a.back()) > kmax)
+        throw std::runtime_error("a query asks for more results than kmax");
+    }
+    SearchOutput out;
+    engine(index)->qbg_search(queries, QueryType::Float32, nq, (size_t)dim, a.data(), a.size(), out);
+    for (size_t q = 0; q < nq; q++) {
+      counts[q] = out.counts[q];
+      for (uint32_t i = 0; i < out.counts[q]; i++) {
+        const ngtg::ObjDist& o = out.results[q * out.kmax + i];
+        results[q * kmax + i] = NGTObjectDistance{o.id, o.distance};
+      }
+      if (stats) std::memcpy(static_cast<NGTGPUQueryStats*>(stats) + q, &out.stats[q], sizeof(NGTGPUQueryStats));
+    }
     return true;
   }
   CAPI_CATCH(error, false)

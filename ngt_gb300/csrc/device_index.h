@@ -87,6 +87,21 @@ struct QGParams {
   uint32_t out_off;
 };
 
+// Per-query parameters of a quantized-blob-graph search (QBG::SearchContainer
+// after qbg_search_index_, lib/NGT/NGTQ/Capi.cpp:549-574).
+struct QBGParams {
+  uint32_t size;         // result size: number_of_results x result_expansion when that is >= 1
+  float coef;            // 1 + epsilon
+  float bcoef;           // 1 + blob_epsilon
+  uint32_t explored;     // number_of_explored_blobs
+  uint32_t edge_size;    // global-graph neighbours read per expanded node
+  uint32_t seed_off;     // tree-seed table of the global index (seed_cnt 0xffffffff)
+  uint32_t seed_cnt;
+  uint32_t fb_off;       // the fixed random seeds used when the tree gives none
+  uint32_t fb_cnt;
+  uint32_t out_off;
+};
+
 // Per-query counters written by the kernels.
 struct QueryStats {
   uint32_t distance_computations;

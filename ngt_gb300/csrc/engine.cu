@@ -16,6 +16,7 @@
 #include "graph_exact.cuh"
 #include "graph_fast.cuh"
 #include "qg_search.cuh"
+#include "qbg_search.cuh"
 #include "kernels.h"
 #include "linear_select.cuh"
 #include "seed_rng.h"
@@ -95,6 +96,70 @@ GraphEngine::GraphEngine(const std::string& path, GraphMode mode, bool quantized
   if (quantized) upload_qg();
 }
 
+GraphEngine::GraphEngine(const std::string& qbg_dir, bool blobs) : mode_(GraphMode::Updatable) {
+  if (!blobs) throw std::runtime_error("invalid QBG open");
+  load_index(qbg_dir + "/global", host_);
+  if (host_.prop.otype != ObjType::Float || host_.prop.metric != Metric::L2)
+    throw std::runtime_error("the QBG global index must hold float L2 centroids");
+  load_qbg(qbg_dir, host_.nrows, qb_);
+  {
+    Property qp = load_property_raw(qbg_dir);
+    try {
+      qbg_genuine_dim_ = (uint32_t)std::stoul(qp.get("GenuineDimension", std::to_string(qb_.dim)));
+    } catch (...) {
+      qbg_genuine_dim_ = 0;
+    }
+    if (qbg_genuine_dim_ == 0 || qbg_genuine_dim_ > host_.dim)
+      throw std::runtime_error("invalid GenuineDimension in " + qbg_dir + "/prf");
+  }
+  if (!qg_kernel(qb_.m)) throw std::runtime_error("too many subspaces in the QBG index");
+  uint32_t mx = 1;
+  for (uint32_t b = 0; b < qb_.nnodes; b++) mx = std::max(mx, qb_.offsets[b + 1] - qb_.offsets[b]);
+  blob_cap_ = (mx + 15) / 16 * 16;
+  // getRandomSeeds(repository, seeds, 20) (lib/NGT/Index.h:1270-1302) for a query whose
+  // tree leaf is empty, drawn from a generator seeded with 1
+  {
+    size_t n = host_.nrows ? host_.nrows - 1 : 0;
+    size_t ss = std::min<size_t>(n, 20);
+    GlibcRand rng(1);
+    size_t empty = 0;
+    while (qbg_fallback_seeds_.size() < ss) {
+      size_t idx = (size_t)std::floor((double)n * rng.unit()) + 1;
+      if (!host_.present[idx]) {
+        if (++empty > n) break;
+        continue;
+      }
+      if (std::find(qbg_fallback_seeds_.begin(), qbg_fallback_seeds_.end(), (uint32_t)idx) !=
+          qbg_fallback_seeds_.end())
+        continue;
+      qbg_fallback_seeds_.push_back((uint32_t)idx);
+    }
+  }
+  NGT_CUDA(cudaGetDevice(&device_));
+  NGT_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+  upload();
+  auto up = [&](const void* src, size_t bytes) {
+    void* p = dmalloc_copy<void>(src, bytes);
+    qg_buffers_.push_back(p);
+    return p;
+  };
+  dqb_.rotation = qb_.rotation.empty() ? nullptr
+                                       : static_cast<const float*>(up(qb_.rotation.data(), qb_.rotation.size() * 4));
+  dqb_.gcentroid = static_cast<const float*>(up(qb_.gcentroid.data(), qb_.gcentroid.size() * 4));
+  dqb_.lcentroids = static_cast<const float*>(up(qb_.lcentroids.data(), qb_.lcentroids.size() * 4));
+  dqb_.offsets = static_cast<const uint32_t*>(up(qb_.offsets.data(), qb_.offsets.size() * 4));
+  dqb_.ids = static_cast<const uint32_t*>(up(qb_.ids.data(), qb_.ids.size() * 4));
+  dqb_.code_off16 = static_cast<const uint32_t*>(up(qb_.code_off16.data(), qb_.code_off16.size() * 4));
+  dqb_.codes = static_cast<const uint8_t*>(up(qb_.codes.data(), qb_.codes.size()));
+  dqb_.dim = qb_.dim;
+  dqb_.m = qb_.m;
+  dqb_.ld = qb_.ld;
+  dqb_.ma = qb_.ma;
+  dqb_.nnodes = qb_.nnodes;
+  d_blob_sid_ = static_cast<uint32_t*>(up(qb_.sid.data(), qb_.sid.size() * 4));
+  qbg_loaded_ = true;
+}
+
 GraphEngine::~GraphEngine() {
   cudaSetDevice(device_);
   cudaFree(d_objects_);
@@ -114,6 +179,8 @@ GraphEngine::~GraphEngine() {
   }
   cudaFree(d_bf16_);
   for (void* p : qg_buffers_) cudaFree(p);
+  cudaFree(d_qbg_ovf_);
+  cudaFree(d_blob_dist_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 
@@ -824,6 +891,139 @@ void GraphEngine::qg_search(const void* queries, QueryType qt, size_t nq, size_t
   NGT_CUDA(cudaMallocAsync(&d_stats, nq * sizeof(QueryStats), s));
   NGT_CUDA(cudaMemcpyAsync(d_rows, rows.data(), rows.size(), cudaMemcpyHostToDevice, s));
   qg_search_device(d_rows, nq, args, nargs, d_out, d_counts, d_stats, kmax, s);
+  NGT_CUDA(cudaMemcpyAsync(out.results.data(), d_out, nq * kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, s));
+  NGT_CUDA(cudaMemcpyAsync(out.counts.data(), d_counts, nq * 4, cudaMemcpyDeviceToHost, s));
+  NGT_CUDA(cudaMemcpyAsync(out.stats.data(), d_stats, nq * sizeof(QueryStats), cudaMemcpyDeviceToHost, s));
+  NGT_CUDA(cudaFreeAsync(d_rows, s));
+  NGT_CUDA(cudaFreeAsync(d_out, s));
+  NGT_CUDA(cudaFreeAsync(d_counts, s));
+  NGT_CUDA(cudaFreeAsync(d_stats, s));
+  NGT_CUDA(cudaStreamSynchronize(s));
+}
+
+// ---- quantized blob graph ---------------------------------------------------
+
+void GraphEngine::qbg_search_device(const uint4* d_rows, size_t nq, const QBGArgs* args, size_t nargs,
+                                    ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, size_t kmax,
+                                    cudaStream_t stream) {
+  if (!qbg_loaded_) throw std::runtime_error("not a QBG index");
+  std::lock_guard<std::mutex> lock(mu_);
+  NGT_CUDA(cudaSetDevice(device_));
+  if (nq == 0) return;
+  // qbg_search_index_ (lib/NGT/NGTQ/Capi.cpp:549-574) and searchInOneStep
+  // (lib/NGT/NGTQ/QuantizedBlobGraph.h:1332-1381)
+  std::vector<QBGParams> params(nq);
+  std::vector<uint32_t> seeds(qbg_fallback_seeds_);
+  uint32_t max_size = 1;
+  for (size_t i = 0; i < nq; i++) {
+    const QBGArgs& a = args[nargs == 1 ? 0 : i];
+    const size_t size = qbg_result_size(a);
+    if (size > kmax) throw std::runtime_error("result size larger than the output capacity");
+    if (size > 4096) throw std::runtime_error("number_of_results x result_expansion above 4096 is not supported");
+    QBGParams qp{};
+    qp.size = (uint32_t)size;
+    float coef = a.epsilon + 1.0f;
+    if (coef == 0.0f) coef = 1.1f;
+    qp.coef = coef;
+    qp.bcoef = a.blob_epsilon + 1.0f;
+    qp.explored = (uint32_t)std::min<size_t>(a.explored_blobs, 0xffffffffu);
+    SearchArgs sa;
+    sa.size = size;
+    sa.epsilon = a.epsilon;
+    sa.edge_size = (int64_t)(int)a.edges;
+    qp.edge_size = (uint32_t)std::min<size_t>(edge_size_for(sa), 0xffffffffu);
+    qp.fb_off = 0;
+    qp.fb_cnt = (uint32_t)qbg_fallback_seeds_.size();
+    qp.out_off = (uint32_t)(i * kmax);
+    if (size > 0) {
+      if (host_.prop.has_tree) seed_params(size, qp.seed_off, qp.seed_cnt, seeds);
+      else { qp.seed_off = 0; qp.seed_cnt = 0; }
+    }
+    params[i] = qp;
+    max_size = std::max<uint32_t>(max_size, qp.size);
+  }
+  if (seeds.empty()) seeds.push_back(0);
+  QBGConfig cfg{};
+  cfg.rcap = max_size;
+  cfg.qcap = 1024;
+  cfg.ocap = (uint32_t)std::min<size_t>(65536, 2 * (size_t)host_.nrows + 256);
+  cfg.bitmap_words = (host_.nrows + 31) / 32;
+  cfg.blob_cap = blob_cap_;
+  cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));
+  int max_smem = 0;
+  NGT_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
+  size_t smem = qbg_kernel_smem_bytes(dev_.row_chunks, qb_.dim, qb_.m, cfg);
+  while (smem > (size_t)max_smem && cfg.qcap > 256) {
+    cfg.qcap >>= 1;
+    smem = qbg_kernel_smem_bytes(dev_.row_chunks, qb_.dim, qb_.m, cfg);
+  }
+  if (smem > (size_t)max_smem) throw std::runtime_error("QBG search state does not fit in shared memory");
+  QBGKernelFn fn = qbg_kernel(qb_.m);
+  NGT_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0, sms = 0;
+  NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kExactThreads, smem));
+  NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+  size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
+  ensure_scratch(grid);
+  if (grid > qbg_grid_ || cfg.ocap != qbg_ocap_) {
+    NGT_CUDA(cudaStreamSynchronize(stream));
+    cudaFree(d_qbg_ovf_);
+    cudaFree(d_blob_dist_);
+    d_qbg_ovf_ = nullptr;
+    d_blob_dist_ = nullptr;
+    size_t g2 = std::max(grid, qbg_grid_);
+    NGT_CUDA(cudaMalloc(&d_qbg_ovf_, g2 * 4 * (size_t)cfg.ocap * 8));
+    NGT_CUDA(cudaMalloc(&d_blob_dist_, g2 * (size_t)blob_cap_ * 4));
+    qbg_grid_ = g2;
+    qbg_ocap_ = cfg.ocap;
+  }
+  QBGParams* d_params = nullptr;
+  uint32_t* d_seeds = nullptr;
+  NGT_CUDA(cudaMallocAsync(&d_params, nq * sizeof(QBGParams), stream));
+  NGT_CUDA(cudaMallocAsync(&d_seeds, seeds.size() * 4, stream));
+  NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QBGParams), cudaMemcpyHostToDevice, stream));
+  NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, stream));
+  fn<<<(unsigned)grid, kExactThreads, smem, stream>>>(dev_, dqb_, d_blob_sid_, d_rows, (uint32_t)nq, d_params,
+                                                       d_seeds, d_out, d_counts, d_stats, d_bitmaps_, d_qbg_ovf_,
+                                                       d_blob_dist_, cfg);
+  NGT_CUDA(cudaGetLastError());
+  launches_++;
+  NGT_CUDA(cudaFreeAsync(d_params, stream));
+  NGT_CUDA(cudaFreeAsync(d_seeds, stream));
+}
+
+void GraphEngine::qbg_search(const void* queries, QueryType qt, size_t nq, size_t qdim, const QBGArgs* args,
+                             size_t nargs, SearchOutput& out) {
+  if (!qbg_loaded_) throw std::runtime_error("not a QBG index");
+  NGT_CUDA(cudaSetDevice(device_));
+  if (qdim != qbg_genuine_dim_)
+    throw std::runtime_error("the query dimension " + std::to_string(qdim) + " differs from the index dimension " +
+                             std::to_string(qbg_genuine_dim_));
+  // the query as floats, zero-padded to the global index dimension
+  // (searchInOneStep resizes the object vector, QuantizedBlobGraph.h:1336-1339)
+  std::vector<float> padded(nq * host_.dim, 0.f);
+  for (size_t q = 0; q < nq; q++)
+    for (size_t i = 0; i < qdim; i++) padded[q * host_.dim + i] = (float)query_elem(queries, qt, q * qdim + i);
+  std::vector<uint8_t> rows;
+  convert_queries(padded.data(), QueryType::Float32, nq, host_.dim, rows);
+  size_t kmax = 1;
+  for (size_t i = 0; i < nargs; i++) kmax = std::max(kmax, qbg_result_size(args[i]));
+  out.kmax = kmax;
+  out.results.assign(nq * kmax, ObjDist{0, 0.f});
+  out.counts.assign(nq, 0);
+  out.stats.assign(nq, QueryStats{});
+  if (nq == 0) return;
+  uint4* d_rows = nullptr;
+  ObjDist* d_out = nullptr;
+  uint32_t* d_counts = nullptr;
+  QueryStats* d_stats = nullptr;
+  cudaStream_t s = stream_;
+  NGT_CUDA(cudaMallocAsync(&d_rows, rows.size(), s));
+  NGT_CUDA(cudaMallocAsync(&d_out, nq * kmax * sizeof(ObjDist), s));
+  NGT_CUDA(cudaMallocAsync(&d_counts, nq * 4, s));
+  NGT_CUDA(cudaMallocAsync(&d_stats, nq * sizeof(QueryStats), s));
+  NGT_CUDA(cudaMemcpyAsync(d_rows, rows.data(), rows.size(), cudaMemcpyHostToDevice, s));
+  qbg_search_device(d_rows, nq, args, nargs, d_out, d_counts, d_stats, kmax, s);
   NGT_CUDA(cudaMemcpyAsync(out.results.data(), d_out, nq * kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, s));
   NGT_CUDA(cudaMemcpyAsync(out.counts.data(), d_counts, nq * 4, cudaMemcpyDeviceToHost, s));
   NGT_CUDA(cudaMemcpyAsync(out.stats.data(), d_stats, nq * sizeof(QueryStats), cudaMemcpyDeviceToHost, s));

@@ -46,6 +46,17 @@ struct QGArgs {
   float radius = -1.0f;            // < 0 means FLT_MAX
 };
 
+// Parameters of one quantized-blob-graph query (QBGQueryParameters,
+// lib/NGT/NGTQ/Capi.h; defaults of qbg_initialize_query_parameters).
+struct QBGArgs {
+  size_t size = 20;                 // number_of_results
+  float epsilon = 0.1f;
+  float blob_epsilon = 0.0f;
+  float result_expansion = 3.0f;
+  size_t explored_blobs = 256;
+  size_t edges = 0;                 // global-graph edge size (0: all)
+};
+
 struct SearchOutput {
   std::vector<ObjDist> results;    // nq * kmax
   std::vector<uint32_t> counts;    // nq
@@ -60,6 +71,9 @@ class GraphEngine {
   // quantized = true also reads the quantized graph (<path>/qg) before any
   // device work, so that a damaged one is reported like a damaged index.
   GraphEngine(const std::string& path, GraphMode mode, bool quantized = false);
+  // A QBG index: `qbg_dir` holds the blobs, qbg_dir/global the global index
+  // (blob centroids, their graph and tree) that this engine searches.
+  GraphEngine(const std::string& qbg_dir, bool blobs);
   ~GraphEngine();
   GraphEngine(const GraphEngine&) = delete;
   GraphEngine& operator=(const GraphEngine&) = delete;
@@ -86,6 +100,18 @@ class GraphEngine {
   // The same over converted query rows resident on the device.
   void qg_search_device(const uint4* d_rows, size_t nq, const QGArgs* args, size_t nargs, ObjDist* d_out,
                         uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream);
+  // qbg_search_index over host queries (nq x qdim, qdim = the QBG genuine
+  // dimension); results ascending (distance, id) with quantized distances,
+  // size x result_expansion of them when the expansion is >= 1.
+  void qbg_search(const void* queries, QueryType qt, size_t nq, size_t qdim, const QBGArgs* args, size_t nargs,
+                  SearchOutput& out);
+  void qbg_search_device(const uint4* d_rows, size_t nq, const QBGArgs* args, size_t nargs, ObjDist* d_out,
+                         uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream);
+  bool is_qbg() const { return qbg_loaded_; }
+  uint32_t qbg_genuine_dimension() const { return qbg_genuine_dim_; }
+  static size_t qbg_result_size(const QBGArgs& a) {
+    return a.result_expansion >= 1.0f ? (size_t)((float)a.size * a.result_expansion) : a.size;
+  }
   // Exhaustive search (exact ids, ties broken by id).
   void linear_search(const void* queries, QueryType qt, size_t nq, size_t qdim, size_t size, SearchOutput& out);
 
@@ -156,6 +182,18 @@ class GraphEngine {
 
   HostIndex host_;
   GraphMode mode_;
+  // quantized blob graph
+  HostQG qb_;
+  bool qbg_loaded_ = false;
+  uint32_t qbg_genuine_dim_ = 0;
+  DevQG dqb_;
+  uint32_t* d_blob_sid_ = nullptr;
+  uint32_t blob_cap_ = 16;
+  std::vector<uint32_t> qbg_fallback_seeds_;
+  unsigned long long* d_qbg_ovf_ = nullptr;
+  float* d_blob_dist_ = nullptr;
+  size_t qbg_grid_ = 0;
+  uint32_t qbg_ocap_ = 0;
   // quantized graph
   HostQG qg_;
   bool qg_loaded_ = false;

@@ -85,6 +85,19 @@ std::string Property::get(const std::string& k, const std::string& dflt) const {
   return it == kv.end() ? dflt : it->second;
 }
 
+Property load_property_raw(const std::string& dir) {
+  Property p;
+  std::ifstream f(dir + "/prf");
+  if (!f.is_open()) fail("cannot open " + dir + "/prf");
+  std::string line;
+  while (std::getline(f, line)) {
+    if (!line.empty() && line.back() == '\r') line.pop_back();
+    auto tab = line.find('\t');
+    if (tab != std::string::npos) p.kv[line.substr(0, tab)] = line.substr(tab + 1);
+  }
+  return p;
+}
+
 Property load_property(const std::string& dir) {
   Property p;
   std::ifstream f(dir + "/prf");
@@ -279,19 +292,22 @@ std::vector<float> read_float_rows(const std::string& path, uint32_t dim, uint32
 
 }  // namespace
 
+static void load_quantized(const std::string& dir, uint32_t id_bound, uint32_t node_bound, bool blobs, HostQG& q);
+
 void load_qg(const std::string& index_dir, uint32_t nrows, HostQG& q) {
-  const std::string dir = index_dir + "/qg";
-  Property p;
+  load_quantized(index_dir + "/qg", nrows, nrows, false, q);
+}
+
+void load_qbg(const std::string& qbg_dir, uint32_t nblobs, HostQG& q) {
+  load_quantized(qbg_dir, 0xFFFFFFFFu, nblobs, true, q);
+}
+
+static void load_quantized(const std::string& dir, uint32_t nrows, uint32_t node_bound, bool blobs, HostQG& q) {
   {
     std::ifstream f(dir + "/prf");
     if (!f.is_open()) fail("no quantized graph: cannot open " + dir + "/prf");
-    std::string line;
-    while (std::getline(f, line)) {
-      if (!line.empty() && line.back() == '\r') line.pop_back();
-      auto tab = line.find('\t');
-      if (tab != std::string::npos) p.kv[line.substr(0, tab)] = line.substr(tab + 1);
-    }
   }
+  Property p = load_property_raw(dir);
   int dim = to_int(p.get("Dimension", "0"), "Dimension");
   int m = to_int(p.get("LocalDivisionNo", "0"), "LocalDivisionNo");
   if (dim <= 0 || m <= 0 || dim % m != 0) fail("invalid Dimension / LocalDivisionNo in " + dir + "/prf");
@@ -321,10 +337,12 @@ void load_qg(const std::string& index_dir, uint32_t nrows, HostQG& q) {
     uint32_t size = r.get<uint32_t>();
     (void)r.get<uint32_t>();
     uint32_t pdim = r.get<uint32_t>();
-    if (pdim == 0 || size < pdim) fail("invalid global codebook in " + dir + "/rqcb");
+    if (pdim == 0 || size < pdim || size % pdim != 0) fail("invalid global codebook in " + dir + "/rqcb");
     const char* src = r.take((size_t)size * 4);
-    q.gcentroid.assign(q.dim, 0.f);
-    std::memcpy(q.gcentroid.data(), src, (size_t)std::min(pdim, q.dim) * 4);
+    q.ncentroids = blobs ? size / pdim : 1u;
+    q.gcentroid.assign((size_t)q.ncentroids * q.dim, 0.f);
+    for (uint32_t c = 0; c < q.ncentroids; c++)
+      std::memcpy(q.gcentroid.data() + (size_t)c * q.dim, src + (size_t)c * pdim * 4, (size_t)std::min(pdim, q.dim) * 4);
   }
   q.lcentroids.assign((size_t)q.m * 16 * q.ld, 0.f);
   for (uint32_t i = 0; i < q.m; i++) {
@@ -337,14 +355,17 @@ void load_qg(const std::string& index_dir, uint32_t nrows, HostQG& q) {
     Reader r(dir + "/grp");
     (void)r.get<uint64_t>();
     uint64_t n = r.get<uint64_t>();
-    if (n > nrows) fail("quantized graph has more nodes than the object repository in " + dir);
+    if (n > node_bound) fail("quantized graph has more nodes than the object repository in " + dir);
     q.nnodes = (uint32_t)n;
     q.offsets.assign(n + 1, 0);
     q.code_off16.assign(n, 0);
+    q.sid.assign(n, 0);
     q.ids.clear();
     q.codes.clear();
     for (uint64_t i = 0; i < n; i++) {
-      (void)r.get<uint32_t>();
+      uint32_t sid = r.get<uint32_t>();
+      if (blobs && sid >= q.ncentroids) fail("blob subspace id beyond the codebook in " + dir + "/grp");
+      q.sid[i] = blobs ? sid : 0u;
       uint32_t cnt = r.get<uint32_t>();
       const char* src = r.take((size_t)cnt * 4);
       size_t base = q.ids.size();

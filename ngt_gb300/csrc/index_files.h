@@ -94,8 +94,10 @@ struct HostQG {
   uint32_t ld = 0;                  // dimensions per subspace
   uint32_t ma = 0;                  // m rounded up to even
   std::vector<float> rotation;      // dim*dim, [p*dim + c]; empty = none
-  std::vector<float> gcentroid;     // dim
+  std::vector<float> gcentroid;     // [ncentroids][dim]: QG has one, QBG one per blob subspace id
+  uint32_t ncentroids = 1;
   std::vector<float> lcentroids;    // [m][16][ld]
+  std::vector<uint32_t> sid;        // per node: its subspace id (the codebook centroid of its table)
   uint32_t nnodes = 0;
   std::vector<uint32_t> offsets;    // nnodes+1
   std::vector<uint32_t> ids;
@@ -106,8 +108,14 @@ struct HostQG {
 
 // Throws std::runtime_error with a message on any format or I/O error.
 Property load_property(const std::string& dir);
+// The key/value pairs of <dir>/prf without interpreting them (NGTQ property files).
+Property load_property_raw(const std::string& dir);
 void load_index(const std::string& dir, HostIndex& out);
 // Reads <index_dir>/qg; nrows bounds the neighbour ids.
 void load_qg(const std::string& index_dir, uint32_t nrows, HostQG& out);
+// Reads the blobs of a QBG index directory (same files at its top level:
+// prf, qr, rqcb, local-*/obj, grp); blobs = nodes of its global index, at most
+// nblobs of them; the object ids in a blob are not bounded here.
+void load_qbg(const std::string& qbg_dir, uint32_t nblobs, HostQG& out);
 
 }  // namespace ngtg

@@ -22,6 +22,13 @@ typedef void (*QGKernelFn)(DevGraph, DevQG, const uint4*, uint32_t, const QGPara
 QGKernelFn qg_kernel(uint32_t m);
 size_t qg_kernel_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, const ExactConfig& c);
 
+struct QBGConfig;
+typedef void (*QBGKernelFn)(DevGraph, DevQG, const uint32_t*, const uint4*, uint32_t, const QBGParams*,
+                            const uint32_t*, ObjDist*, uint32_t*, QueryStats*, uint32_t*, unsigned long long*, float*,
+                            QBGConfig);
+QBGKernelFn qbg_kernel(uint32_t m);
+size_t qbg_kernel_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, const QBGConfig& c);
+
 // Batched kernel for (object type, metric); bf16_rows selects the bf16 search
 // rows for float objects.  nullptr when unsupported.
 FastKernelFn fast_kernel(ObjType ot, Metric m, bool bf16_rows);

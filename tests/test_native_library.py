@@ -142,3 +142,32 @@ def test_qg_loader_rejects_damaged_quantized_graph(lib, tmp_path, damage):
     assert h is None
     assert msg.startswith("Capi : ngtqg_open_index() : Error:"), msg
     assert "CUDA" not in msg, msg
+
+
+@pytest.mark.parametrize("damage", ["missing_rqcb", "bad_sid", "truncate_grp", "no_global"])
+def test_qbg_loader_rejects_damaged_index(lib, tmp_path, damage):
+    from golden_util import fixture_names
+    path, meta, _, _ = materialize(fixture_names("qbg")[0], str(tmp_path))
+    if damage == "missing_rqcb":
+        os.remove(os.path.join(path, "rqcb"))
+    elif damage == "bad_sid":
+        data = bytearray(open(os.path.join(path, "grp"), "rb").read())
+        pos = 16 + 8                                  # node 1's subspace id (node 0 is empty)
+        data[pos:pos + 4] = np.uint32(10 ** 6).tobytes()
+        open(os.path.join(path, "grp"), "wb").write(bytes(data))
+    elif damage == "truncate_grp":
+        data = open(os.path.join(path, "grp"), "rb").read()
+        open(os.path.join(path, "grp"), "wb").write(data[: len(data) - 5])
+    elif damage == "no_global":
+        shutil.rmtree(os.path.join(path, "global"))
+    lib.qbg_open_index.restype = ctypes.c_void_p
+    lib.qbg_open_index.argtypes = [ctypes.c_char_p, ctypes.c_bool, ctypes.c_void_p]
+    lib.ngt_create_error_object.restype = ctypes.c_void_p
+    lib.ngt_get_error_string.restype = ctypes.c_char_p
+    lib.ngt_get_error_string.argtypes = [ctypes.c_void_p]
+    err = lib.ngt_create_error_object()
+    h = lib.qbg_open_index(path.encode(), True, ctypes.c_void_p(err))
+    msg = lib.ngt_get_error_string(ctypes.c_void_p(err)).decode()
+    assert h is None
+    assert msg.startswith("Capi : qbg_open_index() : Error:"), msg
+    assert "CUDA" not in msg, msg
