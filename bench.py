@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--served-rates", type=lambda s: [int(x) for x in s.split(",")], default=[5000, 20000, 50000],
                     help="offered query rates of the serving measurement")
     ap.add_argument("--served-seconds", type=float, default=2.0, help="length of each served-rate run")
+    ap.add_argument("--fixed", default=None,
+                    help="EPS_PLAIN:EPS_BATCHED:LIST:PARENTS -- skip the epsilon / tuning sweeps (profiling runs)")
     return ap.parse_args()
 
 
@@ -384,20 +386,27 @@ def main():
 
     runs = {}
     curves = {}
-    eps, curves[KERNEL_EXACT] = calibrate(KERNEL_EXACT)
-    runs[KERNEL_EXACT] = timed(KERNEL_EXACT, eps)
-    # batched kernel: pick the candidate-list length whose recall-target epsilon runs fastest
-    best = None
-    for L in LIST_SWEEP:
-        for P in PARENT_SWEEP:
-            ix.set_batched_tuning(list_capacity=L, parents=P)
-            eps_l, curve_l = calibrate(KERNEL_BATCHED)
-            probe = timed(KERNEL_BATCHED, eps_l, steps=2)
-            log("batched L=%d P=%d: epsilon %g recall %.4f %.1f q/s" % (L, P, eps_l, probe["recall"], probe["qps"]))
-            if probe["recall"] >= RECALL_TARGET and (best is None or probe["qps"] > best[3]):
-                best = (L, P, eps_l, probe["qps"], curve_l)
-    if best is None:
-        best = (LIST_SWEEP[-1], PARENT_SWEEP[0], EPS_SWEEP[-1], 0.0, curve_l)
+    if args.fixed:
+        ep, eb, L, P = args.fixed.split(":")
+        curves[KERNEL_EXACT] = []
+        runs[KERNEL_EXACT] = timed(KERNEL_EXACT, float(ep))
+        best = (int(L), int(P), float(eb), 0.0, [])
+    else:
+        eps, curves[KERNEL_EXACT] = calibrate(KERNEL_EXACT)
+        runs[KERNEL_EXACT] = timed(KERNEL_EXACT, eps)
+        # batched kernel: pick the candidate-list length whose recall-target epsilon runs fastest
+        best = None
+        for L in LIST_SWEEP:
+            for P in PARENT_SWEEP:
+                ix.set_batched_tuning(list_capacity=L, parents=P)
+                eps_l, curve_l = calibrate(KERNEL_BATCHED)
+                probe = timed(KERNEL_BATCHED, eps_l, steps=2)
+                log("batched L=%d P=%d: epsilon %g recall %.4f %.1f q/s"
+                    % (L, P, eps_l, probe["recall"], probe["qps"]))
+                if probe["recall"] >= RECALL_TARGET and (best is None or probe["qps"] > best[3]):
+                    best = (L, P, eps_l, probe["qps"], curve_l)
+        if best is None:
+            best = (LIST_SWEEP[-1], PARENT_SWEEP[0], EPS_SWEEP[-1], 0.0, curve_l)
     ix.set_batched_tuning(list_capacity=best[0], parents=best[1])
     curves[KERNEL_BATCHED] = best[4]
     runs[KERNEL_BATCHED] = timed(KERNEL_BATCHED, best[2])
