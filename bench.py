@@ -43,6 +43,7 @@ EPS_SWEEP = [0.0, 0.02, 0.04, 0.06, 0.07, 0.08, 0.09, 0.1, 0.12, 0.15, 0.2, 0.3]
 RECALL_TARGET = 0.95
 LIST_SWEEP = [128, 256]
 PARENT_SWEEP = [2, 4, 8]
+ROWS_SWEEP = [4, 6, 8]            # rows per lane group in flight (results do not depend on it)
 
 
 def log(*a):
@@ -65,7 +66,7 @@ def parse():
                     help="offered query rates of the serving measurement")
     ap.add_argument("--served-seconds", type=float, default=2.0, help="length of each served-rate run")
     ap.add_argument("--fixed", default=None,
-                    help="EPS_PLAIN:EPS_BATCHED:LIST:PARENTS -- skip the epsilon / tuning sweeps (profiling runs)")
+                    help="EPS_PLAIN:EPS_BATCHED:LIST:PARENTS[:ROWS] -- skip the epsilon / tuning sweeps (profiling runs)")
     return ap.parse_args()
 
 
@@ -387,31 +388,35 @@ def main():
     runs = {}
     curves = {}
     if args.fixed:
-        ep, eb, L, P = args.fixed.split(":")
+        ep, eb, L, P, R = (args.fixed.split(":") + ["4"])[:5]
         curves[KERNEL_EXACT] = []
         runs[KERNEL_EXACT] = timed(KERNEL_EXACT, float(ep))
-        best = (int(L), int(P), float(eb), 0.0, [])
+        best = (int(L), int(P), float(eb), 0.0, [], int(R))
     else:
         eps, curves[KERNEL_EXACT] = calibrate(KERNEL_EXACT)
         runs[KERNEL_EXACT] = timed(KERNEL_EXACT, eps)
-        # batched kernel: pick the candidate-list length whose recall-target epsilon runs fastest
+        # batched kernel: the (list length, parents, rows in flight) whose recall-target
+        # epsilon runs fastest
         best = None
         for L in LIST_SWEEP:
             for P in PARENT_SWEEP:
                 ix.set_batched_tuning(list_capacity=L, parents=P)
                 eps_l, curve_l = calibrate(KERNEL_BATCHED)
-                probe = timed(KERNEL_BATCHED, eps_l, steps=2)
-                log("batched L=%d P=%d: epsilon %g recall %.4f %.1f q/s"
-                    % (L, P, eps_l, probe["recall"], probe["qps"]))
-                if probe["recall"] >= RECALL_TARGET and (best is None or probe["qps"] > best[3]):
-                    best = (L, P, eps_l, probe["qps"], curve_l)
+                for R in ROWS_SWEEP:
+                    ix.set_batched_tuning(list_capacity=L, parents=P, rows_in_flight=R)
+                    probe = timed(KERNEL_BATCHED, eps_l, steps=2)
+                    log("batched L=%d P=%d R=%d: epsilon %g recall %.4f %.1f q/s"
+                        % (L, P, R, eps_l, probe["recall"], probe["qps"]))
+                    if probe["recall"] >= RECALL_TARGET and (best is None or probe["qps"] > best[3]):
+                        best = (L, P, eps_l, probe["qps"], curve_l, R)
         if best is None:
-            best = (LIST_SWEEP[-1], PARENT_SWEEP[0], EPS_SWEEP[-1], 0.0, curve_l)
-    ix.set_batched_tuning(list_capacity=best[0], parents=best[1])
+            best = (LIST_SWEEP[-1], PARENT_SWEEP[0], EPS_SWEEP[-1], 0.0, curve_l, 4)
+    ix.set_batched_tuning(list_capacity=best[0], parents=best[1], rows_in_flight=best[5])
     curves[KERNEL_BATCHED] = best[4]
     runs[KERNEL_BATCHED] = timed(KERNEL_BATCHED, best[2])
     runs[KERNEL_BATCHED]["list_capacity"] = best[0]
     runs[KERNEL_BATCHED]["parents"] = best[1]
+    runs[KERNEL_BATCHED]["rows_in_flight"] = best[5]
     for kernel in (KERNEL_EXACT, KERNEL_BATCHED):
         log("kernel %d: %.1f q/s at epsilon %g, recall %.4f, %.1f GB/s"
             % (kernel, runs[kernel]["qps"], runs[kernel]["epsilon"], runs[kernel]["recall"],
@@ -453,8 +458,9 @@ def main():
             "config": {"workload": "graph search, %d x %d float32 L2 ONNG, %d queries per step, k=%d"
                                    % (args.n, args.dim, nq, k),
                        "headline": "batched kernel (warp per query, bf16 rows, exact fp32 re-rank), epsilon=%g, "
-                                   "candidate list %d, %d parents per step"
-                                   % (head["epsilon"], head["list_capacity"], head["parents"]),
+                                   "candidate list %d, %d parents per step, %d rows in flight per lane group"
+                                   % (head["epsilon"], head["list_capacity"], head["parents"],
+                                      head["rows_in_flight"]),
                        "recall_at_k": round(head["recall"], 4), "epsilon_curve": curves[KERNEL_BATCHED],
                        "plain_fp32": {"qps": round(plain["qps"], 1), "epsilon": plain["epsilon"],
                                       "recall_at_k": round(plain["recall"], 4),

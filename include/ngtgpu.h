@@ -64,6 +64,10 @@ bool ngtgpu_search_batch_device(NGTIndex, const void *d_rows, size_t nq, const N
  * expanded per iteration (<= 16), and re-ranked candidates per query as a
  * multiple of size. */
 bool ngtgpu_set_batched_tuning(NGTIndex, uint32_t list_capacity, uint32_t parents, float rerank_factor, NGTError);
+/* Rows each lane group of the batched kernel keeps in flight while computing
+ * distances: 4 (default), 6 or 8 (float L2 indexes; deeper pipelines trade
+ * registers, so fewer CTAs per SM).  0 restores the default. */
+bool ngtgpu_set_batched_rows_in_flight(NGTIndex, uint32_t rows, NGTError);
 
 /* Exact graph search (results equal ngtgpu_search_batch_device with
  * NGTGPU_KERNEL_EXACT) that allocates no device memory, for callers that cannot

@@ -118,6 +118,7 @@ def load_library() -> ctypes.CDLL:
                                         c_size_t, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p], c_bool),
         "ngtgpu_kernel_launches": ([c_void_p, c_void_p], c_uint64),
         "ngtgpu_set_batched_tuning": ([c_void_p, c_uint32, c_uint32, c_float, c_void_p], c_bool),
+        "ngtgpu_set_batched_rows_in_flight": ([c_void_p, c_uint32, c_void_p], c_bool),
         "ngtgpu_server_create": ([c_void_p, c_uint32, c_uint32, c_uint32, c_void_p], c_void_p),
         "ngtgpu_server_submit": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QueryParameters), c_size_t,
                                   c_void_p], ctypes.c_int64),
@@ -257,9 +258,11 @@ class Index:
         out = (res["id"][:, :m].copy(), res["distance"][:, :m].copy(), counts)
         return out + (stats,) if with_stats else out
 
-    def set_batched_tuning(self, list_capacity: int = 0, parents: int = 0, rerank_factor: float = 0.0):
+    def set_batched_tuning(self, list_capacity: int = 0, parents: int = 0, rerank_factor: float = 0.0,
+                           rows_in_flight: int = 0):
         self._check(self._lib.ngtgpu_set_batched_tuning(self._index, list_capacity, parents, rerank_factor,
                                                         self._err))
+        self._check(self._lib.ngtgpu_set_batched_rows_in_flight(self._index, rows_in_flight, self._err))
 
     def kernel_launches(self) -> int:
         return int(self._lib.ngtgpu_kernel_launches(self._index, self._err))

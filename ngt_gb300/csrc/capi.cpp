@@ -429,10 +429,21 @@ bool ngtgpu_set_batched_tuning(NGTIndex index, uint32_t list_capacity, uint32_t 
                                        << " rerank_factor = " << rerank_factor);
     return false;
   }
-  ngtg::FastTuning t;
+  ngtg::FastTuning t = engine(index)->tuning();
   t.list_cap = list_capacity;
   t.parents = parents;
   t.rerank_factor = rerank_factor;
+  engine(index)->set_tuning(t);
+  return true;
+}
+
+bool ngtgpu_set_batched_rows_in_flight(NGTIndex index, uint32_t rows, NGTError error) {
+  if (index == nullptr || !(rows == 0 || rows == 4 || rows == 6 || rows == 8)) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " rows = " << rows);
+    return false;
+  }
+  ngtg::FastTuning t = engine(index)->tuning();
+  t.rows_in_flight = rows;
   engine(index)->set_tuning(t);
   return true;
 }

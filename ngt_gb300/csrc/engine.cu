@@ -545,7 +545,8 @@ void GraphEngine::launch_fast(const uint4* d_rows, size_t nq, const QueryParams*
                               uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats,
                               cudaStream_t stream, Kernel kernel, FastScratch& scratch) {
   const bool bf16 = kernel == Kernel::Fast && host_.prop.otype == ObjType::Float;
-  FastKernelFn fn = fast_kernel(host_.prop.otype, host_.prop.metric, bf16);
+  FastKernelFn fn = fast_kernel(host_.prop.otype, host_.prop.metric, bf16,
+                                tuning_.rows_in_flight ? tuning_.rows_in_flight : 4u);
   if (!fn) throw std::runtime_error("the batched kernel does not support this index type");
   if (bf16) ensure_bf16_rows();
   FastConfig cfg{};

@@ -35,6 +35,7 @@ struct FastTuning {
   uint32_t list_cap = 0;       // candidate list length (power of two)
   uint32_t parents = 0;        // nodes expanded per iteration
   float rerank_factor = 0.f;   // re-ranked entries = ceil(size * factor)
+  uint32_t rows_in_flight = 0; // rows per lane group in flight in the distance loop (4, 6 or 8)
 };
 
 // Parameters of one quantized-graph query (NGTQGQueryParameters,

@@ -143,8 +143,10 @@ struct PackedL2 {
   }
 };
 
-template <ObjType ST, ObjType OT, Metric M>
-__global__ void __launch_bounds__(kFastThreads, 5)
+// U: rows per lane group in flight in the distance loop; MINB: CTAs per SM the
+// register allocation is sized for.
+template <ObjType ST, ObjType OT, Metric M, int U = 4, int MINB = 5>
+__global__ void __launch_bounds__(kFastThreads, MINB)
 graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint4* __restrict__ queries, uint32_t nq,
                          const QueryParams* __restrict__ params, const uint32_t* __restrict__ seed_list,
                          ObjDist* __restrict__ out, uint32_t* __restrict__ out_count, QueryStats* __restrict__ stats,
@@ -447,7 +449,6 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       };
       if (sc <= (uint32_t)SG * 2) {
         // at most two 16-byte chunks per lane per row; U rows per group in flight
-        constexpr int U = 4;
         const uint32_t c0 = (uint32_t)sgl, c1 = (uint32_t)sgl + (uint32_t)SG;
         const uint4 zero = make_uint4(0, 0, 0, 0);
         const uint4 q0 = c0 < sc ? qs[c0] : zero, q1 = c1 < sc ? qs[c1] : zero;

@@ -10,8 +10,13 @@ namespace ngtg {
 #define NGT_FAST_CASE(ST, OT, M) \
   case Metric::M: return &graph_search_fast_kernel<ObjType::ST, ObjType::OT, Metric::M>;
 
-FastKernelFn fast_kernel(ObjType ot, Metric m, bool bf16_rows) {
+FastKernelFn fast_kernel(ObjType ot, Metric m, bool bf16_rows, uint32_t rows_in_flight) {
   m = kernel_metric(m);
+  if (ot == ObjType::Float && bf16_rows && m == Metric::L2 && rows_in_flight > 4) {
+    // deeper row pipelines for the L2 bf16 search (fewer CTAs per SM by registers)
+    if (rows_in_flight <= 6) return &graph_search_fast_kernel<ObjType::Bfloat16, ObjType::Float, Metric::L2, 6, 4>;
+    return &graph_search_fast_kernel<ObjType::Bfloat16, ObjType::Float, Metric::L2, 8, 4>;
+  }
   if (ot == ObjType::Float && bf16_rows) {
     switch (m) {
       NGT_FAST_CASE(Bfloat16, Float, L2) NGT_FAST_CASE(Bfloat16, Float, L1) NGT_FAST_CASE(Bfloat16, Float, Cosine)

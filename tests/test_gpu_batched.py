@@ -105,3 +105,18 @@ def test_batched_mixed_parameters_and_edge_cases(workdir):
         # a radius keeps only results within it
         ids, ds, n = ix.batch_search(queries[:200], k=10, epsilon=0.1, radius=300.0, kernel=KERNEL_BATCHED)
         assert all((ds[j, :n[j]] <= 300.0).all() for j in range(200))
+
+
+def test_rows_in_flight_does_not_change_results(tmp_path):
+    """The deeper-pipelined instantiations (6 or 8 rows per lane group) compute
+    the same distances in the same order: results identical to the default."""
+    from ngt_gb300 import Index
+    path, meta, queries, _ = materialize("c1_f32_l2", str(tmp_path))
+    with Index(path, read_only=True) as ix:
+        ix.set_batched_tuning(list_capacity=256, parents=4)
+        ref = ix.batch_search(queries[:300], k=10, epsilon=0.1, kernel=1, with_stats=True)
+        for rows in (6, 8):
+            ix.set_batched_tuning(list_capacity=256, parents=4, rows_in_flight=rows)
+            got = ix.batch_search(queries[:300], k=10, epsilon=0.1, kernel=1, with_stats=True)
+            for a, b in zip(ref, got):
+                assert np.array_equal(np.asarray(a).view(np.uint8), np.asarray(b).view(np.uint8)), rows
