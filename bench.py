@@ -44,6 +44,12 @@ RECALL_TARGET = 0.95
 LIST_SWEEP = [128, 256]
 PARENT_SWEEP = [2, 4, 8]
 ROWS_SWEEP = [4, 6, 8]            # rows per lane group in flight (results do not depend on it)
+# dram__bytes_read.sum + dram__bytes_write.sum of one graph_search_fast_kernel
+# launch of 2,000 queries on this workload (1M x 128, k=10, epsilon 0.08; ncu
+# capture summarised under profiles/), per query.  Scaled by the queries of one
+# launch to give roofline.traffic; the workload's DC per query is the same at
+# every batch size.
+FAST_KERNEL_DRAM_BYTES_PER_QUERY = 10.56e9 / 2000
 
 
 def log(*a):
@@ -475,7 +481,11 @@ def main():
                        "mean_expansions": round(head["expansions"], 1), "mean_edges_read": round(head["edges"], 1),
                        "status_bits": head["status"]},
             "roofline": {"bound": "hbm", "achieved": round(head["achieved_gbs"], 1), "peak": peak, "unit": "GB/s",
-                         "frac": round(head["achieved_gbs"] / peak, 4), "traffic": None, "peak_source": peak_kind,
+                         "frac": round(head["achieved_gbs"] / peak, 4),
+                         "traffic": (round(FAST_KERNEL_DRAM_BYTES_PER_QUERY * nq / 1e9, 3)
+                                     if (args.n, args.dim, k) == (1_000_000, 128, 10) else None),
+                         "traffic_unit": "GB per launch (ncu dram bytes per query x queries)",
+                         "peak_source": peak_kind,
                          "basis": "(%d*DC + 4*edges + %d query + re-rank %d*2k) bytes per query over the kernel's "
                                   "median event time" % (head["row_bytes"], row_bytes, row_bytes)},
             "served": served,

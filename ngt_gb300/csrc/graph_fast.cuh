@@ -111,6 +111,53 @@ __device__ __forceinline__ void warp_sort32(unsigned long long* a, uint32_t n, i
   __syncwarp();
 }
 
+// Ascending sort of a[0..n), n <= 32 * J, in registers: element e = j * 32 + lane
+// sits in k[j] of `lane`; bitonic network with compare-exchanges inside a lane for
+// strides >= 32 and shuffles below.  Written back to a.
+template <int J>
+__device__ __forceinline__ void warp_sort_reg(unsigned long long* a, uint32_t n, int lane) {
+  unsigned long long k[J];
+#pragma unroll
+  for (int j = 0; j < J; j++) {
+    const uint32_t e = (uint32_t)(j * 32 + lane);
+    k[j] = e < n ? a[e] : ~0ull;
+  }
+#pragma unroll
+  for (int size = 2; size <= 32 * J; size <<= 1) {
+#pragma unroll
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      if (stride >= 32) {
+        const int js = stride >> 5;
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+          if ((j & js) == 0) {
+            const uint32_t e = (uint32_t)(j * 32 + lane);
+            const bool up = (e & (uint32_t)size) == 0;
+            unsigned long long x = k[j], y = k[j + js];
+            if ((x > y) == up) { k[j] = y; k[j + js] = x; }
+          }
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+          const uint32_t e = (uint32_t)(j * 32 + lane);
+          const bool up = (e & (uint32_t)size) == 0;
+          const bool lower = (lane & stride) == 0;
+          unsigned long long y = __shfl_xor_sync(0xffffffffu, k[j], stride);
+          k[j] = (lower == up) ? (y < k[j] ? y : k[j]) : (y > k[j] ? y : k[j]);
+        }
+      }
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int j = 0; j < J; j++) {
+    const uint32_t e = (uint32_t)(j * 32 + lane);
+    if (e < n) a[e] = k[j];
+  }
+  __syncwarp();
+}
+
 // Number of entries of the sorted a[0..n) that are < x (ignoring the expanded bit of a's entries
 // is not needed: keys are ordered by distance first, the bit only reorders exact distance ties).
 __device__ __forceinline__ uint32_t warp_lower_bound(const unsigned long long* a, uint32_t n, unsigned long long x) {
@@ -129,14 +176,20 @@ template <ObjType ST, Metric M>
 struct PackedL2 {
   static constexpr bool kOn = (M == Metric::L2 || M == Metric::InnerProduct) &&
                               (ST == ObjType::Bfloat16 || ST == ObjType::Float || ST == ObjType::Float16);
-  __device__ __forceinline__ static float2 add(float2 acc, const uint4& q, const uint4& x) {
-    constexpr int P = ObjTraits<ST>::kPerChunk;
-    float a[P], b[P];
+  static constexpr int P = ObjTraits<ST>::kPerChunk;
+  // the query chunk negated and unpacked once per query
+  __device__ __forceinline__ static void prepare(const uint4& q, float2 (&nq)[P / 2]) {
+    float a[P];
     unpack<ST>(q, a);
+#pragma unroll
+    for (int i = 0; i < P; i += 2) nq[i / 2] = make_float2(-a[i], -a[i + 1]);
+  }
+  __device__ __forceinline__ static float2 add(float2 acc, const float2 (&nq)[P / 2], const uint4& x) {
+    float b[P];
     unpack<ST>(x, b);
 #pragma unroll
     for (int i = 0; i < P; i += 2) {
-      float2 dlt = __fadd2_rn(make_float2(b[i], b[i + 1]), make_float2(-a[i], -a[i + 1]));
+      float2 dlt = __fadd2_rn(make_float2(b[i], b[i + 1]), nq[i / 2]);
       acc = __ffma2_rn(dlt, dlt, acc);
     }
     return acc;
@@ -452,6 +505,11 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
         const uint32_t c0 = (uint32_t)sgl, c1 = (uint32_t)sgl + (uint32_t)SG;
         const uint4 zero = make_uint4(0, 0, 0, 0);
         const uint4 q0 = c0 < sc ? qs[c0] : zero, q1 = c1 < sc ? qs[c1] : zero;
+        float2 nq0[PackedL2<ST, M>::P / 2], nq1[PackedL2<ST, M>::P / 2];
+        if constexpr (PackedL2<ST, M>::kOn) {
+          PackedL2<ST, M>::prepare(q0, nq0);
+          PackedL2<ST, M>::prepare(q1, nq1);
+        }
         for (uint32_t b = 0; b < cnt; b += gpw * U) {
           uint4 x0[U], x1[U];
           uint32_t idu[U];
@@ -468,8 +526,8 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
             float d;
             if constexpr (PackedL2<ST, M>::kOn) {
               float2 acc = make_float2(0.f, 0.f);
-              if (c0 < sc) acc = PackedL2<ST, M>::add(acc, q0, x0[u]);
-              if (c1 < sc) acc = PackedL2<ST, M>::add(acc, q1, x1[u]);
+              if (c0 < sc) acc = PackedL2<ST, M>::add(acc, nq0, x0[u]);
+              if (c1 < sc) acc = PackedL2<ST, M>::add(acc, nq1, x1[u]);
               float v = acc.x + acc.y;
 #pragma unroll
               for (int off = 16; off > 0; off >>= 1)
@@ -522,6 +580,8 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       __syncwarp();
       if (kept == 0) continue;
       if (kept <= 32) warp_sort32(nkey, kept, lane);
+      else if (kept <= 64) warp_sort_reg<2>(nkey, kept, lane);
+      else if (kept <= 128) warp_sort_reg<4>(nkey, kept, lane);
       else warp_bitonic_sort(nkey, kept, lane);
       // In-place merge of nkey[0..kept) into list[0..n), keeping the first L.
       // 1. merged positions of the new keys (list entries compare without their
