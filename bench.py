@@ -42,8 +42,10 @@ sys.path.insert(0, ROOT)
 EPS_SWEEP = [0.0, 0.02, 0.04, 0.06, 0.07, 0.08, 0.09, 0.1, 0.12, 0.15, 0.2, 0.3]
 RECALL_TARGET = 0.95
 LIST_SWEEP = [128, 256]
-PARENT_SWEEP = [2, 4, 8]
-ROWS_SWEEP = [4, 6, 8]            # rows per lane group in flight (results do not depend on it)
+PARENT_SWEEP = [2, 4]
+# (rows per lane group in flight, CTAs per SM the registers are budgeted for,
+# neighbour slots per iteration; 0 = automatic).  Only the last can change results.
+VARIANT_SWEEP = [(4, 5, 0), (6, 4, 0), (6, 5, 0), (4, 6, 256), (2, 8, 256), (4, 5, 256)]
 # dram__bytes_read.sum + dram__bytes_write.sum of one graph_search_fast_kernel
 # launch of 2,000 queries on this workload (1M x 128, k=10, epsilon 0.08; ncu
 # capture summarised under profiles/), per query.  Scaled by the queries of one
@@ -72,7 +74,7 @@ def parse():
                     help="offered query rates of the serving measurement")
     ap.add_argument("--served-seconds", type=float, default=2.0, help="length of each served-rate run")
     ap.add_argument("--fixed", default=None,
-                    help="EPS_PLAIN:EPS_BATCHED:LIST:PARENTS[:ROWS] -- skip the epsilon / tuning sweeps (profiling runs)")
+                    help="EPS_PLAIN:EPS_BATCHED:LIST:PARENTS[:ROWS:CTAS:NBR] -- skip the epsilon / tuning sweeps")
     return ap.parse_args()
 
 
@@ -394,10 +396,10 @@ def main():
     runs = {}
     curves = {}
     if args.fixed:
-        ep, eb, L, P, R = (args.fixed.split(":") + ["4"])[:5]
+        ep, eb, L, P, R, C, NB = (args.fixed.split(":") + ["4", "5", "0"][len(args.fixed.split(":")) - 4:])[:7]
         curves[KERNEL_EXACT] = []
         runs[KERNEL_EXACT] = timed(KERNEL_EXACT, float(ep))
-        best = (int(L), int(P), float(eb), 0.0, [], int(R))
+        best = (int(L), int(P), float(eb), 0.0, [], (int(R), int(C), int(NB)))
     else:
         eps, curves[KERNEL_EXACT] = calibrate(KERNEL_EXACT)
         runs[KERNEL_EXACT] = timed(KERNEL_EXACT, eps)
@@ -408,21 +410,24 @@ def main():
             for P in PARENT_SWEEP:
                 ix.set_batched_tuning(list_capacity=L, parents=P)
                 eps_l, curve_l = calibrate(KERNEL_BATCHED)
-                for R in ROWS_SWEEP:
-                    ix.set_batched_tuning(list_capacity=L, parents=P, rows_in_flight=R)
+                for V in VARIANT_SWEEP:
+                    ix.set_batched_tuning(list_capacity=L, parents=P, rows_in_flight=V[0], ctas_per_sm=V[1],
+                                          neighbour_capacity=V[2])
                     probe = timed(KERNEL_BATCHED, eps_l, steps=2)
-                    log("batched L=%d P=%d R=%d: epsilon %g recall %.4f %.1f q/s"
-                        % (L, P, R, eps_l, probe["recall"], probe["qps"]))
+                    log("batched L=%d P=%d R=%d C=%d NB=%d: epsilon %g recall %.4f %.1f q/s"
+                        % (L, P, V[0], V[1], V[2], eps_l, probe["recall"], probe["qps"]))
                     if probe["recall"] >= RECALL_TARGET and (best is None or probe["qps"] > best[3]):
-                        best = (L, P, eps_l, probe["qps"], curve_l, R)
+                        best = (L, P, eps_l, probe["qps"], curve_l, V)
         if best is None:
-            best = (LIST_SWEEP[-1], PARENT_SWEEP[0], EPS_SWEEP[-1], 0.0, curve_l, 4)
-    ix.set_batched_tuning(list_capacity=best[0], parents=best[1], rows_in_flight=best[5])
+            best = (LIST_SWEEP[-1], PARENT_SWEEP[0], EPS_SWEEP[-1], 0.0, curve_l, VARIANT_SWEEP[0])
+    V = best[5]
+    ix.set_batched_tuning(list_capacity=best[0], parents=best[1], rows_in_flight=V[0], ctas_per_sm=V[1],
+                          neighbour_capacity=V[2])
     curves[KERNEL_BATCHED] = best[4]
     runs[KERNEL_BATCHED] = timed(KERNEL_BATCHED, best[2])
     runs[KERNEL_BATCHED]["list_capacity"] = best[0]
     runs[KERNEL_BATCHED]["parents"] = best[1]
-    runs[KERNEL_BATCHED]["rows_in_flight"] = best[5]
+    runs[KERNEL_BATCHED]["variant"] = best[5]
     for kernel in (KERNEL_EXACT, KERNEL_BATCHED):
         log("kernel %d: %.1f q/s at epsilon %g, recall %.4f, %.1f GB/s"
             % (kernel, runs[kernel]["qps"], runs[kernel]["epsilon"], runs[kernel]["recall"],
@@ -464,9 +469,10 @@ def main():
             "config": {"workload": "graph search, %d x %d float32 L2 ONNG, %d queries per step, k=%d"
                                    % (args.n, args.dim, nq, k),
                        "headline": "batched kernel (warp per query, bf16 rows, exact fp32 re-rank), epsilon=%g, "
-                                   "candidate list %d, %d parents per step, %d rows in flight per lane group"
+                                   "candidate list %d, %d parents per step, %d rows in flight per lane group, "
+                                   "registers for %d CTAs/SM, neighbour slots %s"
                                    % (head["epsilon"], head["list_capacity"], head["parents"],
-                                      head["rows_in_flight"]),
+                                      head["variant"][0], head["variant"][1], head["variant"][2] or "auto"),
                        "recall_at_k": round(head["recall"], 4), "epsilon_curve": curves[KERNEL_BATCHED],
                        "plain_fp32": {"qps": round(plain["qps"], 1), "epsilon": plain["epsilon"],
                                       "recall_at_k": round(plain["recall"], 4),

@@ -69,6 +69,22 @@ bool ngtgpu_set_batched_tuning(NGTIndex, uint32_t list_capacity, uint32_t parent
  * registers, so fewer CTAs per SM).  0 restores the default. */
 bool ngtgpu_set_batched_rows_in_flight(NGTIndex, uint32_t rows, NGTError);
 
+/* All knobs of the batched kernel at once (0 = automatic for each).  The
+ * (rows_in_flight, ctas_per_sm) pairs built are (4, 5) for every index type and
+ * (6, 4), (8, 4), (6, 5), (4, 6), (2, 8) for float L2 indexes; a search with a
+ * pair that is not built fails with an error.  neighbour_capacity bounds the
+ * neighbour slots of one iteration (each parent reads at most
+ * neighbour_capacity / parents edges) and sets the shared memory per query. */
+typedef struct {
+  uint32_t list_capacity;
+  uint32_t parents;
+  float rerank_factor;
+  uint32_t rows_in_flight;
+  uint32_t ctas_per_sm;
+  uint32_t neighbour_capacity;
+} NGTGPUBatchedTuning;
+bool ngtgpu_set_batched_tuning_ex(NGTIndex, const NGTGPUBatchedTuning *tuning, NGTError);
+
 /* Exact graph search (results equal ngtgpu_search_batch_device with
  * NGTGPU_KERNEL_EXACT) that allocates no device memory, for callers that cannot
  * call cudaMalloc while they search: hosts that own and budget all device

@@ -66,6 +66,12 @@ class QBGQueryFloat(ctypes.Structure):
     _fields_ = [("query", POINTER(c_float)), ("params", QBGQueryParameters)]
 
 
+class BatchedTuning(ctypes.Structure):
+    """NGTGPUBatchedTuning (include/ngtgpu.h)."""
+    _fields_ = [("list_capacity", c_uint32), ("parents", c_uint32), ("rerank_factor", c_float),
+                ("rows_in_flight", c_uint32), ("ctas_per_sm", c_uint32), ("neighbour_capacity", c_uint32)]
+
+
 class QueryStats(ctypes.Structure):
     _fields_ = [("distance_computations", c_uint32), ("expansions", c_uint32), ("visited", c_uint32),
                 ("edges_read", c_uint32), ("status", c_uint32)]
@@ -119,6 +125,7 @@ def load_library() -> ctypes.CDLL:
         "ngtgpu_kernel_launches": ([c_void_p, c_void_p], c_uint64),
         "ngtgpu_set_batched_tuning": ([c_void_p, c_uint32, c_uint32, c_float, c_void_p], c_bool),
         "ngtgpu_set_batched_rows_in_flight": ([c_void_p, c_uint32, c_void_p], c_bool),
+        "ngtgpu_set_batched_tuning_ex": ([c_void_p, POINTER(BatchedTuning), c_void_p], c_bool),
         "ngtgpu_server_create": ([c_void_p, c_uint32, c_uint32, c_uint32, c_void_p], c_void_p),
         "ngtgpu_server_submit": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QueryParameters), c_size_t,
                                   c_void_p], ctypes.c_int64),
@@ -259,10 +266,9 @@ class Index:
         return out + (stats,) if with_stats else out
 
     def set_batched_tuning(self, list_capacity: int = 0, parents: int = 0, rerank_factor: float = 0.0,
-                           rows_in_flight: int = 0):
-        self._check(self._lib.ngtgpu_set_batched_tuning(self._index, list_capacity, parents, rerank_factor,
-                                                        self._err))
-        self._check(self._lib.ngtgpu_set_batched_rows_in_flight(self._index, rows_in_flight, self._err))
+                           rows_in_flight: int = 0, ctas_per_sm: int = 0, neighbour_capacity: int = 0):
+        t = BatchedTuning(list_capacity, parents, rerank_factor, rows_in_flight, ctas_per_sm, neighbour_capacity)
+        self._check(self._lib.ngtgpu_set_batched_tuning_ex(self._index, ctypes.byref(t), self._err))
 
     def kernel_launches(self) -> int:
         return int(self._lib.ngtgpu_kernel_launches(self._index, self._err))

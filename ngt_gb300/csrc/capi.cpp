@@ -438,12 +438,32 @@ bool ngtgpu_set_batched_tuning(NGTIndex index, uint32_t list_capacity, uint32_t 
 }
 
 bool ngtgpu_set_batched_rows_in_flight(NGTIndex index, uint32_t rows, NGTError error) {
-  if (index == nullptr || !(rows == 0 || rows == 4 || rows == 6 || rows == 8)) {
+  if (index == nullptr || !(rows == 0 || rows == 2 || rows == 4 || rows == 6 || rows == 8)) {
     CAPI_PARAM_ERROR(error, "index = " << index << " rows = " << rows);
     return false;
   }
   ngtg::FastTuning t = engine(index)->tuning();
   t.rows_in_flight = rows;
+  engine(index)->set_tuning(t);
+  return true;
+}
+
+bool ngtgpu_set_batched_tuning_ex(NGTIndex index, const NGTGPUBatchedTuning* tuning, NGTError error) {
+  if (index == nullptr || tuning == nullptr || tuning->list_capacity > 1024 || tuning->parents > 16 ||
+      tuning->rerank_factor < 0.f || tuning->neighbour_capacity > 4096 ||
+      !(tuning->rows_in_flight == 0 || tuning->rows_in_flight == 2 || tuning->rows_in_flight == 4 ||
+        tuning->rows_in_flight == 6 || tuning->rows_in_flight == 8) ||
+      tuning->ctas_per_sm > 8) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " tuning = " << tuning);
+    return false;
+  }
+  ngtg::FastTuning t;
+  t.list_cap = tuning->list_capacity;
+  t.parents = tuning->parents;
+  t.rerank_factor = tuning->rerank_factor;
+  t.rows_in_flight = tuning->rows_in_flight;
+  t.ctas_per_sm = tuning->ctas_per_sm;
+  t.nbr_cap = tuning->neighbour_capacity;
   engine(index)->set_tuning(t);
   return true;
 }

@@ -545,9 +545,9 @@ void GraphEngine::launch_fast(const uint4* d_rows, size_t nq, const QueryParams*
                               uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats,
                               cudaStream_t stream, Kernel kernel, FastScratch& scratch) {
   const bool bf16 = kernel == Kernel::Fast && host_.prop.otype == ObjType::Float;
-  FastKernelFn fn = fast_kernel(host_.prop.otype, host_.prop.metric, bf16,
-                                tuning_.rows_in_flight ? tuning_.rows_in_flight : 4u);
-  if (!fn) throw std::runtime_error("the batched kernel does not support this index type");
+  FastKernelFn fn = fast_kernel(host_.prop.otype, host_.prop.metric, bf16, tuning_.rows_in_flight,
+                                tuning_.ctas_per_sm);
+  if (!fn) throw std::runtime_error("the batched kernel does not support this index type or tuning");
   if (bf16) ensure_bf16_rows();
   FastConfig cfg{};
   uint32_t L = tuning_.list_cap ? next_pow2(tuning_.list_cap) : next_pow2(std::max<uint32_t>(512, 4 * max_size));
@@ -558,7 +558,8 @@ void GraphEngine::launch_fast(const uint4* d_rows, size_t nq, const QueryParams*
   cfg.parents = tuning_.parents ? std::min<uint32_t>(tuning_.parents, 16) : 4;
   float rf0 = tuning_.rerank_factor > 0.f ? tuning_.rerank_factor : 2.0f;
   uint32_t rerank_max = std::min<uint32_t>(L, (uint32_t)std::ceil(rf0 * (float)max_size) + 1);
-  cfg.nbr_cap = std::max<uint32_t>({512u, next_pow2(rerank_max), L, next_pow2(cfg.parents * 128)});
+  cfg.nbr_cap = tuning_.nbr_cap ? std::max<uint32_t>({next_pow2(tuning_.nbr_cap), next_pow2(rerank_max), L})
+                                : std::max<uint32_t>({512u, next_pow2(rerank_max), L, next_pow2(cfg.parents * 128)});
   // nd doubles as the 256-bin refill histogram
   cfg.nbr_cap = std::max<uint32_t>(cfg.nbr_cap, 256u);
   cfg.search_chunks = bf16 ? dev_.row_chunks / 2 : dev_.row_chunks;

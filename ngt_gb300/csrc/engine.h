@@ -35,7 +35,9 @@ struct FastTuning {
   uint32_t list_cap = 0;       // candidate list length (power of two)
   uint32_t parents = 0;        // nodes expanded per iteration
   float rerank_factor = 0.f;   // re-ranked entries = ceil(size * factor)
-  uint32_t rows_in_flight = 0; // rows per lane group in flight in the distance loop (4, 6 or 8)
+  uint32_t rows_in_flight = 0; // rows per lane group in flight in the distance loop (2, 4, 6 or 8)
+  uint32_t ctas_per_sm = 0;    // register budget of the instantiation (4..8)
+  uint32_t nbr_cap = 0;        // neighbour slots per iteration (power of two >= 256)
 };
 
 // Parameters of one quantized-graph query (NGTQGQueryParameters,

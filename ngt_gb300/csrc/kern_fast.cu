@@ -10,13 +10,20 @@ namespace ngtg {
 #define NGT_FAST_CASE(ST, OT, M) \
   case Metric::M: return &graph_search_fast_kernel<ObjType::ST, ObjType::OT, Metric::M>;
 
-FastKernelFn fast_kernel(ObjType ot, Metric m, bool bf16_rows, uint32_t rows_in_flight) {
+FastKernelFn fast_kernel(ObjType ot, Metric m, bool bf16_rows, uint32_t rows_in_flight, uint32_t ctas_per_sm) {
   m = kernel_metric(m);
-  if (ot == ObjType::Float && bf16_rows && m == Metric::L2 && rows_in_flight > 4) {
-    // deeper row pipelines for the L2 bf16 search (fewer CTAs per SM by registers)
-    if (rows_in_flight <= 6) return &graph_search_fast_kernel<ObjType::Bfloat16, ObjType::Float, Metric::L2, 6, 4>;
-    return &graph_search_fast_kernel<ObjType::Bfloat16, ObjType::Float, Metric::L2, 8, 4>;
+  if (rows_in_flight == 0) rows_in_flight = 4;
+  if (ctas_per_sm == 0) ctas_per_sm = rows_in_flight > 4 ? 4 : 5;
+  if (ot == ObjType::Float && bf16_rows && m == Metric::L2 && !(rows_in_flight == 4 && ctas_per_sm == 5)) {
+    // other row pipelines / register budgets for the L2 bf16 search
+#define NGT_FAST_L2(U, B) \
+  if (rows_in_flight == U && ctas_per_sm == B) \
+    return &graph_search_fast_kernel<ObjType::Bfloat16, ObjType::Float, Metric::L2, U, B>;
+    NGT_FAST_L2(6, 4) NGT_FAST_L2(8, 4) NGT_FAST_L2(6, 5) NGT_FAST_L2(4, 6) NGT_FAST_L2(2, 8)
+#undef NGT_FAST_L2
+    return nullptr;
   }
+  if (!(rows_in_flight == 4 && ctas_per_sm == 5)) return nullptr;
   if (ot == ObjType::Float && bf16_rows) {
     switch (m) {
       NGT_FAST_CASE(Bfloat16, Float, L2) NGT_FAST_CASE(Bfloat16, Float, L1) NGT_FAST_CASE(Bfloat16, Float, Cosine)

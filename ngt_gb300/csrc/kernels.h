@@ -31,9 +31,12 @@ size_t qbg_kernel_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, cons
 
 // Batched kernel for (object type, metric); bf16_rows selects the bf16 search
 // rows for float objects.  nullptr when unsupported.
-// rows_in_flight (rows per lane group the distance loop keeps in flight) selects
-// a deeper-pipelined instantiation for the float/L2 bf16 search when above 4.
-FastKernelFn fast_kernel(ObjType ot, Metric m, bool bf16_rows, uint32_t rows_in_flight = 4);
+// rows_in_flight (rows per lane group the distance loop keeps in flight) and
+// ctas_per_sm (the register budget) select an instantiation: (4, 5) for every
+// type; (6, 4), (8, 4), (6, 5), (4, 6), (2, 8) for the float/L2 bf16 search.
+// 0 = default.  nullptr when the combination is not built.
+FastKernelFn fast_kernel(ObjType ot, Metric m, bool bf16_rows, uint32_t rows_in_flight = 4,
+                         uint32_t ctas_per_sm = 0);
 void launch_float_rows_to_bf16(const void* in, void* out, size_t nfloats, cudaStream_t s);
 
 // Return nullptr when the (type, metric) pair is not supported.

@@ -115,8 +115,22 @@ def test_rows_in_flight_does_not_change_results(tmp_path):
     with Index(path, read_only=True) as ix:
         ix.set_batched_tuning(list_capacity=256, parents=4)
         ref = ix.batch_search(queries[:300], k=10, epsilon=0.1, kernel=1, with_stats=True)
-        for rows in (6, 8):
-            ix.set_batched_tuning(list_capacity=256, parents=4, rows_in_flight=rows)
+        for rows, ctas in ((6, 4), (8, 4), (6, 5), (4, 6), (2, 8)):
+            ix.set_batched_tuning(list_capacity=256, parents=4, rows_in_flight=rows, ctas_per_sm=ctas)
             got = ix.batch_search(queries[:300], k=10, epsilon=0.1, kernel=1, with_stats=True)
             for a, b in zip(ref, got):
                 assert np.array_equal(np.asarray(a).view(np.uint8), np.asarray(b).view(np.uint8)), rows
+
+
+def test_smaller_neighbour_capacity_keeps_recall(tmp_path):
+    """neighbour_capacity 256 with 4 parents reads at most 64 edges per parent."""
+    from ngt_gb300 import Index
+    path, meta, queries, _ = materialize("c1_f32_l2_onng", str(tmp_path))
+    o = oracle.Oracle(oracle.IndexFiles(path))
+    q = queries[:200]
+    with Index(path, read_only=True) as ix:
+        ix.set_batched_tuning(list_capacity=256, parents=4, neighbour_capacity=256, rows_in_flight=4, ctas_per_sm=6)
+        ids, ds, n = ix.batch_search(q, k=10, epsilon=0.1, kernel=1)
+    li, ld, ln = o.linear_search(q, k=10, threads=8)
+    hit = sum(len(set(ids[j, :n[j]]) & set(li[j, :ln[j]])) for j in range(len(q)))
+    assert hit / (10 * len(q)) > 0.9
