@@ -19,6 +19,9 @@ extern "C" {
 #define NGTGPU_KERNEL_BATCHED 1u   /* warp per query, persistent, bf16 search rows for float objects,
                                       exact re-rank of the best candidates (checked by recall) */
 #define NGTGPU_KERNEL_BATCHED_FP32 2u  /* the batched kernel on the full-precision rows */
+#define NGTGPU_KERNEL_WIDE 3u      /* the same search with one query per 256-thread CTA: rows of an
+                                      iteration copied to shared memory all at once (low latency per
+                                      query; float L2 and uint8 L2 indexes) */
 
 /* Per-query statistics: distance computations, expanded nodes, visited ids,
  * adjacency entries read, and status bits (1: candidate overflow tier full,

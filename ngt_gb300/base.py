@@ -25,6 +25,7 @@ LIB_PATH = os.path.join(_HERE, "libngtgpu.so")
 KERNEL_EXACT = 0
 KERNEL_BATCHED = 1
 KERNEL_BATCHED_FP32 = 2
+KERNEL_WIDE = 3
 
 
 class NativeError(Exception):

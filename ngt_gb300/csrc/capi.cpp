@@ -343,6 +343,7 @@ static ngtg::Kernel check_kernel(uint32_t kernel) {
     case NGTGPU_KERNEL_EXACT: return ngtg::Kernel::Exact;
     case NGTGPU_KERNEL_BATCHED: return ngtg::Kernel::Fast;
     case NGTGPU_KERNEL_BATCHED_FP32: return ngtg::Kernel::FastFp32;
+    case NGTGPU_KERNEL_WIDE: return ngtg::Kernel::Wide;
     default: throw std::runtime_error("unknown kernel selector " + std::to_string(kernel));
   }
 }

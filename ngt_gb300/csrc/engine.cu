@@ -15,6 +15,7 @@
 
 #include "graph_exact.cuh"
 #include "graph_fast.cuh"
+#include "graph_wide.cuh"
 #include "qg_search.cuh"
 #include "qbg_search.cuh"
 #include "kernels.h"
@@ -416,6 +417,7 @@ void GraphEngine::ensure_scratch(size_t grid) {
 
 bool GraphEngine::fast_supported(Kernel k) const {
   if (k == Kernel::Exact) return true;
+  if (k == Kernel::Wide) return wide_kernel(host_.prop.otype, host_.prop.metric, true) != nullptr;
   return fast_kernel(host_.prop.otype, host_.prop.metric, k == Kernel::Fast) != nullptr;
 }
 
@@ -473,6 +475,8 @@ void GraphEngine::search_device(const uint4* d_rows, size_t nq, const SearchArgs
   NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, stream));
   if (kernel == Kernel::Exact)
     launch_exact(d_rows, nq, d_params, d_seeds, max_size, d_out, d_counts, d_stats, stream);
+  else if (kernel == Kernel::Wide)
+    launch_wide(d_rows, nq, d_params, d_seeds, max_size, d_out, d_counts, d_stats, stream, fast_scratch_[0]);
   else
     launch_fast(d_rows, nq, d_params, d_seeds, max_size, d_out, d_counts, d_stats, stream, kernel,
                 fast_scratch_[0]);
@@ -537,6 +541,54 @@ void GraphEngine::launch_exact(const uint4* d_rows, size_t nq, const QueryParams
   ensure_scratch(grid);
   fn<<<(unsigned)grid, kExactThreads, smem, stream>>>(dev_, d_rows, (uint32_t)nq, d_params, d_seeds, d_out, d_counts,
                                                        d_stats, d_bitmaps_, d_overflow_, cfg);
+  NGT_CUDA(cudaGetLastError());
+  launches_++;
+}
+
+void GraphEngine::launch_wide(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
+                              uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats,
+                              cudaStream_t stream, FastScratch& scratch) {
+  const bool bf16 = host_.prop.otype == ObjType::Float;
+  WideKernelFn fn = wide_kernel(host_.prop.otype, host_.prop.metric, bf16);
+  if (!fn) throw std::runtime_error("the wide kernel does not support this index type");
+  if (bf16) ensure_bf16_rows();
+  WideConfig cfg{};
+  uint32_t L = tuning_.list_cap ? next_pow2(tuning_.list_cap) : next_pow2(std::max<uint32_t>(256, 4 * max_size));
+  L = std::max<uint32_t>(L, next_pow2(max_size + 1));
+  if (L > 1024) throw std::runtime_error("result size too large for the wide kernel (at most 1023)");
+  cfg.list_cap = L;
+  cfg.parents = tuning_.parents ? std::min<uint32_t>(tuning_.parents, 32) : 8;
+  float rf = tuning_.rerank_factor > 0.f ? tuning_.rerank_factor : 2.0f;
+  uint32_t rerank_max = std::min<uint32_t>(L, (uint32_t)std::ceil(rf * (float)max_size) + 1);
+  cfg.nbr_cap = tuning_.nbr_cap ? std::max<uint32_t>({next_pow2(tuning_.nbr_cap), next_pow2(rerank_max), L})
+                                : std::max<uint32_t>({512u, next_pow2(rerank_max), L,
+                                                      std::min<uint32_t>(4096, next_pow2(cfg.parents * 100))});
+  cfg.search_chunks = bf16 ? dev_.row_chunks / 2 : dev_.row_chunks;
+  cfg.stage_rows = std::max<uint32_t>(32, std::min<uint32_t>(512, (96u * 1024u) / (cfg.search_chunks * 16)));
+  cfg.sgroup = std::min<uint32_t>(32, next_pow2((cfg.search_chunks + 1) / 2));
+  cfg.ngroup = std::min<uint32_t>(32, next_pow2(dev_.row_chunks));
+  cfg.rerank_x16 = (uint32_t)std::ceil(rf * 16.0f);
+  cfg.bitmap_words = ((host_.nrows + 31) / 32 + 3) / 4 * 4;
+  cfg.max_iters = 1u << 22;
+  cfg.spill_cap = kSpillCapacity;
+  size_t smem = wide_kernel_smem_bytes(dev_.row_chunks, cfg);
+  int max_smem = 0, per_sm = 0, sms = 0;
+  NGT_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
+  while (smem > (size_t)max_smem && cfg.stage_rows > 32) {
+    cfg.stage_rows /= 2;
+    smem = wide_kernel_smem_bytes(dev_.row_chunks, cfg);
+  }
+  if (smem > (size_t)max_smem) throw std::runtime_error("wide search state does not fit in shared memory");
+  NGT_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kWideThreads, smem));
+  NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+  size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
+  ensure_fast_scratch(scratch, grid, stream);
+  NGT_CUDA(cudaMemsetAsync(scratch.work, 0, 4, stream));
+  const uint4* srows = bf16 ? static_cast<const uint4*>(d_bf16_) : dev_.objects;
+  fn<<<(unsigned)grid, kWideThreads, smem, stream>>>(dev_, srows, d_rows, (uint32_t)nq, d_params, d_seeds, d_out,
+                                                      d_counts, d_stats, scratch.bitmaps, scratch.work,
+                                                      scratch.spill, cfg);
   NGT_CUDA(cudaGetLastError());
   launches_++;
 }

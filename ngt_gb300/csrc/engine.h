@@ -28,7 +28,9 @@ enum class QueryType { Float32 = 0, Float64 = 1, Uint8 = 2, Float16 = 3 };
 // Exact: reference-order search, one query per CTA (results equal the reference's).
 // Fast: batched warp-per-query search on bf16 rows (float objects) or the native
 //       rows (other types), with an exact re-rank.  FastFp32: the same on fp32 rows.
-enum class Kernel { Exact = 0, Fast = 1, FastFp32 = 2 };
+// Wide: the batched search with one query per CTA (rows of an iteration staged in
+//       shared memory at once), for low per-query latency.
+enum class Kernel { Exact = 0, Fast = 1, FastFp32 = 2, Wide = 3 };
 
 // Knobs of the batched kernel (0 = automatic).
 struct FastTuning {
@@ -182,6 +184,9 @@ class GraphEngine {
   void launch_fast(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
                    uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, cudaStream_t stream,
                    Kernel kernel, FastScratch& scratch);
+  void launch_wide(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
+                   uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, cudaStream_t stream,
+                   FastScratch& scratch);
 
   HostIndex host_;
   GraphMode mode_;

@@ -1,0 +1,549 @@
+// Batched graph search with one query per CTA ("wide"): the same relaxed
+// best-first search as graph_fast.cuh (sorted candidate list with expanded
+// bits, P parents per iteration within (1+epsilon) x r_k, spill tier, exact
+// re-rank of the best candidates), with every phase of an iteration spread
+// over the CTA so that one query moves many rows at once:
+//   * the P parents' edge slots are read, filtered against the query's
+//     visited bitmap and compacted by all 256 threads;
+//   * the new neighbours' search rows are copied into shared memory with
+//     asynchronous 16-byte copies (cp.async), all of a round in flight at once,
+//     and their distances computed from shared memory;
+//   * the survivors are sorted (bitonic, CTA-wide) and merged into the list by
+//     per-entry binary searches into a second buffer.
+// One warp (warp 0) owns the control decisions (parent selection, the refill
+// from the spill tier), exactly as the warp-per-query kernel makes them.
+// Per-query latency is set by a few memory round trips per iteration instead of
+// one per 16 rows, which is what a lightly loaded server needs.
+#pragma once
+#include <cuda_bf16.h>
+#include <cfloat>
+#include "distance.cuh"
+#include "device_index.h"
+#include "graph_fast.cuh"
+
+namespace ngtg {
+
+constexpr int kWideThreads = 256;
+constexpr int kWideWarps = kWideThreads / 32;
+
+struct WideConfig {
+  uint32_t list_cap;       // L: power of two
+  uint32_t nbr_cap;        // neighbour slots per iteration (power of two >= L)
+  uint32_t parents;        // P (<= 32)
+  uint32_t stage_rows;     // search rows staged in shared memory per round
+  uint32_t sgroup;         // lanes per search distance (power of two <= 32)
+  uint32_t ngroup;         // lanes per full-precision distance
+  uint32_t search_chunks;  // 16-byte chunks per search row
+  uint32_t rerank_x16;
+  uint32_t bitmap_words;   // per CTA, multiple of 4
+  uint32_t max_iters;
+  uint32_t spill_cap;
+};
+
+struct WideShared {
+  uint32_t q, n, cur, np, total, cnt, kept, scan0, spill_n, stop, done, refill, first_new;
+  uint32_t status, dc, expansions, edges, visited;
+  unsigned long long spill_min, worst;
+  float limit, insert_limit;
+  uint32_t parents[32], pexcl[32], pbase[32];
+  uint32_t wcnt[kWideWarps], wcnt2[kWideWarps];
+  unsigned long long wmin[kWideWarps];
+};
+
+inline size_t wide_smem_bytes(uint32_t row_chunks, const WideConfig& c) {
+  size_t b = (size_t)row_chunks * 16 + (size_t)c.search_chunks * 16;
+  b += (size_t)c.list_cap * 16;                                   // list, double-buffered
+  b += (size_t)c.nbr_cap * 16;                                    // nkey, nid, nd
+  b += (size_t)c.stage_rows * c.search_chunks * 16;               // row staging
+  b += sizeof(WideShared) + 16;
+  return b;
+}
+
+__device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n" ::: "memory");
+  asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+}
+
+// CTA-wide ascending bitonic sort of a[0..n) (shared memory), padded with ~0 to
+// the next power of two (<= cap).
+__device__ __forceinline__ void cta_bitonic_sort(unsigned long long* a, uint32_t n, uint32_t cap) {
+  if (n <= 1) return;
+  uint32_t p = 1;
+  while (p < n) p <<= 1;
+  for (uint32_t i = n + threadIdx.x; i < p && i < cap; i += blockDim.x) a[i] = ~0ull;
+  __syncthreads();
+  for (uint32_t k = 2; k <= p; k <<= 1) {
+    for (uint32_t j = k >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = threadIdx.x; i < p; i += blockDim.x) {
+        uint32_t l = i ^ j;
+        if (l > i) {
+          unsigned long long x = a[i], y = a[l];
+          bool up = (i & k) == 0;
+          if ((x > y) == up) { a[i] = y; a[l] = x; }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Order-preserving CTA compaction of one round of flags: returns the position of
+// this thread's element among the flagged ones of the round (valid when flag)
+// and the round's total in *round_total.
+__device__ __forceinline__ uint32_t cta_compact(bool flag, uint32_t* wcnt, uint32_t* round_total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned bal = __ballot_sync(0xffffffffu, flag);
+  if (lane == 0) wcnt[warp] = __popc(bal);
+  __syncthreads();
+  uint32_t base = 0, tot = 0;
+#pragma unroll
+  for (int w = 0; w < kWideWarps; w++) {
+    uint32_t c = wcnt[w];
+    if (w < warp) base += c;
+    tot += c;
+  }
+  __syncthreads();
+  *round_total = tot;
+  return base + __popc(bal & ((1u << lane) - 1u));
+}
+
+template <ObjType ST, ObjType OT, Metric M>
+__global__ void __launch_bounds__(kWideThreads, 1)
+graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint4* __restrict__ queries,
+                         uint32_t nq, const QueryParams* __restrict__ params, const uint32_t* __restrict__ seed_list,
+                         ObjDist* __restrict__ out, uint32_t* __restrict__ out_count, QueryStats* __restrict__ stats,
+                         uint32_t* __restrict__ bitmaps, uint32_t* __restrict__ work,
+                         unsigned long long* __restrict__ spills, WideConfig cfg) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t rc = g.row_chunks, sc = cfg.search_chunks;
+  const uint32_t L = cfg.list_cap, NB = cfg.nbr_cap, SR = cfg.stage_rows;
+  uint4* qn = reinterpret_cast<uint4*>(smem);
+  uint4* qs = qn + rc;
+  unsigned long long* lists = reinterpret_cast<unsigned long long*>(qs + sc);   // 2 x L
+  unsigned long long* nkey = lists + 2 * (size_t)L;
+  uint32_t* nid = reinterpret_cast<uint32_t*>(nkey + NB);
+  float* nd = reinterpret_cast<float*>(nid + NB);
+  uint4* stage = reinterpret_cast<uint4*>(nd + NB);
+  WideShared& s = *reinterpret_cast<WideShared*>(stage + (size_t)SR * sc);
+  uint32_t* bitmap = bitmaps + (size_t)blockIdx.x * cfg.bitmap_words;
+  unsigned long long* spill = spills + (size_t)blockIdx.x * 2 * cfg.spill_cap;
+  unsigned long long* spill_tmp = spill + cfg.spill_cap;
+  const int SG = (int)cfg.sgroup, NG = (int)cfg.ngroup;
+  const int sgl = lane & (SG - 1), ngl = lane & (NG - 1);
+
+  // distances of nid[0..cnt) into nd[], rows staged through shared memory
+  auto score = [&](uint32_t cnt) {
+    for (uint32_t r0 = 0; r0 < cnt; r0 += SR) {
+      const uint32_t nr = min(SR, cnt - r0);
+      for (uint32_t idx = tid; idx < nr * sc; idx += blockDim.x) {
+        const uint32_t i = idx / sc, c = idx - i * sc;
+        cp_async16(stage + idx, srows + (size_t)nid[r0 + i] * sc + c);
+      }
+      cp_async_wait_all();
+      __syncthreads();
+      const uint32_t gpb = kWideThreads / SG;
+      for (uint32_t b = 0; b < nr; b += gpb) {          // uniform trip count per warp
+        const uint32_t i = b + (uint32_t)(tid / SG);
+        const bool valid = i < nr;
+        const uint4* row = stage + (size_t)(valid ? i : 0u) * sc;
+        float d;
+        if constexpr (PackedL2<ST, M>::kOn) {
+          float2 acc = make_float2(0.f, 0.f);
+          for (uint32_t c = (uint32_t)sgl; c < sc; c += (uint32_t)SG) {
+            float2 nq[PackedL2<ST, M>::P / 2];
+            PackedL2<ST, M>::prepare(qs[c], nq);
+            acc = PackedL2<ST, M>::add(acc, nq, row[c]);
+          }
+          float v = acc.x + acc.y;
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1)
+            if (off < SG) v += __shfl_xor_sync(0xffffffffu, v, off);
+          d = sqrtf(v);
+        } else {
+          Acc<ST, M> acc;
+          for (uint32_t c = (uint32_t)sgl; c < sc; c += (uint32_t)SG) acc.add(qs[c], row[c], (int)c);
+          acc.reduce(SG);
+          d = acc.finish();
+        }
+        if (valid && sgl == 0) nd[r0 + i] = d;
+      }
+      __syncthreads();
+    }
+  };
+
+  while (true) {
+    if (tid == 0) s.q = atomicAdd(work, 1u);
+    __syncthreads();
+    const uint32_t q = s.q;
+    if (q >= nq) break;
+    const QueryParams P = params[q];
+    for (uint32_t i = tid; i < rc; i += blockDim.x) qn[i] = queries[(size_t)q * rc + i];
+    __syncthreads();
+    if constexpr (ST != OT) {
+      const float* qf = reinterpret_cast<const float*>(qn);
+      uint32_t* qb = reinterpret_cast<uint32_t*>(qs);
+      for (uint32_t i = tid; i < sc * 4; i += blockDim.x) {
+        uint32_t lo = __bfloat16_as_ushort(__float2bfloat16_rn(qf[2 * i]));
+        uint32_t hi = __bfloat16_as_ushort(__float2bfloat16_rn(qf[2 * i + 1]));
+        qb[i] = lo | (hi << 16);
+      }
+    } else {
+      for (uint32_t i = tid; i < sc; i += blockDim.x) qs[i] = qn[i];
+    }
+    if (tid == 0) {
+      s.n = 0; s.cur = 0; s.scan0 = 0; s.spill_n = 0; s.spill_min = ~0ull; s.refill = 0; s.done = 0;
+      s.status = 0; s.dc = 0; s.expansions = 0; s.edges = 0; s.visited = 0;
+    }
+    __syncthreads();
+    if (P.size == 0) {
+      if (tid == 0) { out_count[q] = 0; stats[q] = QueryStats{0, 0, 0, 0, 0}; }
+      __syncthreads();
+      continue;
+    }
+    // ---- seeds (warp 0): tree leaf or explicit list, marked visited, compacted ----
+    if (warp == 0) {
+      const uint32_t* seeds = nullptr;
+      uint32_t nseeds = 0, st = 0;
+      if (P.seed_cnt == 0xffffffffu) {
+        uint32_t node = g.root;
+        int depth = 0;
+        while (!(node & 0x80000000u) && depth < 64) {
+          const DevInternal& in = g.internals[node];
+          float d = group_distance<OT, M>(qn, g.pivots + (size_t)in.pivot * rc, (int)rc, lane, 32);
+          uint32_t bsize = in.nchildren - 1, mid;
+          for (mid = 0; mid < bsize; mid++)
+            if (d < in.borders[mid]) break;
+          node = in.children[mid];
+          depth++;
+        }
+        if (node & 0x80000000u) {
+          uint32_t leaf = node & 0x7fffffffu;
+          if (leaf < g.nleaves) {
+            const uint32_t* off = g.leaf_seed_off + P.seed_off;
+            seeds = g.leaf_seed_ids + off[leaf];
+            nseeds = off[leaf + 1] - off[leaf];
+          }
+        } else {
+          st |= kStatusTreeError;
+        }
+      } else {
+        seeds = seed_list + P.seed_off;
+        nseeds = P.seed_cnt;
+      }
+      nseeds = min(nseeds, NB);
+      if (nseeds == 0) st |= kStatusEmptySeeds;
+      uint32_t m = 0;
+      for (uint32_t b = 0; b < nseeds; b += 32) {
+        uint32_t i = b + lane;
+        bool fresh = false;
+        uint32_t id = 0;
+        if (i < nseeds) {
+          id = seeds[i];
+          if (id < g.nrows) {
+            uint32_t bit = 1u << (id & 31u);
+            fresh = (atomicOr(&bitmap[id >> 5], bit) & bit) == 0u;
+          }
+        }
+        unsigned bal = __ballot_sync(0xffffffffu, fresh);
+        if (fresh) nid[m + __popc(bal & ((1u << lane) - 1u))] = id;
+        m += __popc(bal);
+      }
+      if (lane == 0) { s.cnt = m; s.status |= st; s.dc = m; s.visited = m; }
+    }
+    __syncthreads();
+    {
+      const uint32_t m = s.cnt;
+      score(m);
+      for (uint32_t i = tid; i < m; i += blockDim.x) nkey[i] = pack_key(nd[i], nid[i]);
+      __syncthreads();
+      cta_bitonic_sort(nkey, m, NB);
+      const uint32_t n0 = min(m, L);
+      for (uint32_t i = tid; i < n0; i += blockDim.x) lists[i] = nkey[i];
+      if (tid == 0) s.n = n0;
+      __syncthreads();
+    }
+    const float user_radius = P.radius;
+
+    // ---- best-first iterations ---------------------------------------------------------
+    for (uint32_t it = 0; it < cfg.max_iters; it++) {
+      // control (warp 0): refill from the spill tier when flagged, then pick parents
+      if (warp == 0) {
+        unsigned long long* list = lists + (size_t)s.cur * L;
+        uint32_t n = s.n, scan0 = s.scan0, spill_n = s.spill_n;
+        unsigned long long spill_min = s.spill_min;
+        bool refill = s.refill != 0;
+        float rk = (n >= P.size) ? fminf(key_dist(list[P.size - 1]), user_radius) : user_radius;
+        const float limit = P.coef * rk;
+        if (refill) {
+          n = min(n, P.size);
+          const uint32_t room = L - n;
+          uint32_t r = 0;
+          for (uint32_t b = 0; b < spill_n; b += 32) {
+            uint32_t i = b + lane;
+            unsigned long long k = i < spill_n ? spill[i] : ~0ull;
+            bool live = i < spill_n && key_dist(k) <= limit;
+            unsigned bal = __ballot_sync(0xffffffffu, live);
+            if (live) spill_tmp[r + __popc(bal & ((1u << lane) - 1u))] = k;
+            r += __popc(bal);
+          }
+          __syncwarp();
+          unsigned long long thr = ~0ull;
+          if (r > room) {
+            unsigned long long prefix = 0, mask = 0;
+            uint32_t need = room;
+            uint32_t* hist = reinterpret_cast<uint32_t*>(nd);
+            for (int shift = 56; shift >= 0; shift -= 8) {
+              for (uint32_t i = lane; i < 256; i += 32) hist[i] = 0;
+              __syncwarp();
+              for (uint32_t i = lane; i < r; i += 32) {
+                unsigned long long k = spill_tmp[i];
+                if ((k & mask) == prefix) atomicAdd(&hist[(uint32_t)(k >> shift) & 255u], 1u);
+              }
+              __syncwarp();
+              uint32_t acc = 0, bsel = 255;
+              for (uint32_t b = 0; b < 256; b++) {
+                uint32_t h = hist[b];
+                if (acc + h >= need) { bsel = b; break; }
+                acc += h;
+              }
+              prefix |= (unsigned long long)bsel << shift;
+              need -= acc;
+              mask |= 255ull << shift;
+              __syncwarp();
+            }
+            thr = prefix;
+          }
+          uint32_t moved = 0, stay = 0;
+          unsigned long long smin = ~0ull;
+          for (uint32_t b = 0; b < r; b += 32) {
+            uint32_t i = b + lane;
+            unsigned long long k = i < r ? spill_tmp[i] : ~0ull;
+            bool take = i < r && k <= thr;
+            bool keep = i < r && k > thr;
+            unsigned bt = __ballot_sync(0xffffffffu, take), bk = __ballot_sync(0xffffffffu, keep);
+            if (take) nkey[moved + __popc(bt & ((1u << lane) - 1u))] = k;
+            if (keep) { spill[stay + __popc(bk & ((1u << lane) - 1u))] = k; smin = k < smin ? k : smin; }
+            moved += __popc(bt);
+            stay += __popc(bk);
+          }
+          for (int off = 16; off > 0; off >>= 1) {
+            unsigned long long o = __shfl_xor_sync(0xffffffffu, smin, off);
+            smin = o < smin ? o : smin;
+          }
+          __syncwarp();
+          warp_bitonic_sort(nkey, moved, lane);
+          for (uint32_t i = lane; i < moved; i += 32) list[n + i] = nkey[i];
+          __syncwarp();
+          scan0 = n;
+          n += moved;
+          spill_n = stay;
+          spill_min = smin;
+          refill = false;
+        }
+        uint32_t np = 0;
+        bool stop = false;
+        for (uint32_t b = scan0 & ~31u; b < n && !stop && np < cfg.parents; b += 32) {
+          uint32_t i = b + lane;
+          unsigned long long k = i < n ? list[i] : ~0ull;
+          unsigned ball = __ballot_sync(0xffffffffu, i < n && !key_expanded(k));
+          while (ball && np < cfg.parents) {
+            int j = __ffs(ball) - 1;
+            unsigned long long kj = __shfl_sync(0xffffffffu, k, j);
+            if (key_dist(kj) > limit) { stop = true; break; }
+            if (lane == j) list[i] = k | kExpandedBit;
+            if (lane == 0) s.parents[np] = key_rawid(kj);
+            np++;
+            scan0 = b + (uint32_t)j + 1;
+            ball &= ball - 1;
+          }
+        }
+        __syncwarp();
+        uint32_t done = 0, next_refill = 0;
+        if (np == 0) {
+          if (!stop && spill_n > 0 && key_dist(spill_min) <= limit) {
+            scan0 = n;
+            next_refill = 1;
+          } else {
+            done = 1;
+          }
+        } else {
+          // edge slots of the parents
+          const uint32_t per_parent = min(P.edge_size, NB / np);
+          uint32_t pe0 = 0, pne = 0;
+          if ((uint32_t)lane < np) {
+            const uint32_t v = s.parents[lane];
+            const uint32_t a = g.offsets[v];
+            pe0 = a;
+            pne = min(g.offsets[v + 1] - a, per_parent);
+          }
+          uint32_t incl = pne;
+#pragma unroll
+          for (int off = 1; off < 32; off <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, incl, off);
+            if (lane >= off) incl += t;
+          }
+          const uint32_t total = __shfl_sync(0xffffffffu, incl, np - 1);
+          if ((uint32_t)lane < np) {
+            s.pexcl[lane] = incl - pne;
+            s.pbase[lane] = pe0;
+          }
+          if (lane == 0) { s.total = total; s.edges += total; s.expansions += np; }
+        }
+        if (lane == 0) {
+          s.n = n; s.scan0 = scan0; s.spill_n = spill_n; s.spill_min = spill_min;
+          s.refill = next_refill; s.done = done; s.np = np; s.limit = limit;
+        }
+      }
+      __syncthreads();
+      const uint32_t done = s.done, refill_next = s.refill, np = s.np, total = s.total;
+      __syncthreads();              // everyone has read the decision before warp 0 writes the next one
+      if (done) break;
+      if (refill_next) continue;
+      // ---- gather: unvisited neighbours of the parents, in edge order -----------------
+      uint32_t cnt = 0;
+      for (uint32_t base0 = 0; base0 < total; base0 += blockDim.x) {
+        const uint32_t t = base0 + tid;
+        uint32_t id = 0;
+        bool fresh = false;
+        if (t < total) {
+          uint32_t p2 = 0;
+          for (uint32_t c = 1; c < np; c++)
+            if (t >= s.pexcl[c]) p2 = c;
+          id = __ldg(g.edges + s.pbase[p2] + (t - s.pexcl[p2]));
+          const uint32_t bit = 1u << (id & 31u);
+          fresh = (atomicOr(&bitmap[id >> 5], bit) & bit) == 0u;
+        }
+        uint32_t rt;
+        const uint32_t pos = cta_compact(fresh, s.wcnt, &rt);
+        if (fresh) nid[cnt + pos] = id;
+        cnt += rt;
+      }
+      __syncthreads();
+      if (tid == 0) { s.dc += cnt; s.visited += cnt; }
+      // ---- distances ------------------------------------------------------------------------
+      score(cnt);
+      // ---- placement: below the list's worst -> merged; else within the limit -> spill ---
+      const unsigned long long* list = lists + (size_t)s.cur * L;
+      const uint32_t n = s.n;
+      const unsigned long long worst = (n >= L) ? (list[L - 1] & ~(unsigned long long)kExpandedBit) : ~0ull;
+      const float rk2 = (n >= P.size) ? fminf(key_dist(list[P.size - 1]), user_radius) : user_radius;
+      const float insert_limit = P.coef * rk2;
+      uint32_t kept = 0;
+      unsigned long long smin = ~0ull;
+      for (uint32_t base0 = 0; base0 < cnt; base0 += blockDim.x) {
+        const uint32_t i = base0 + tid;
+        unsigned long long key = ~0ull;
+        bool live = false;
+        if (i < cnt) {
+          key = pack_key(nd[i], nid[i]);
+          live = nd[i] <= insert_limit;
+        }
+        const bool keep = live && key < worst;
+        const bool spl = live && key >= worst;
+        uint32_t rt;
+        const uint32_t pos = cta_compact(keep, s.wcnt, &rt);
+        if (keep) nkey[kept + pos] = key;
+        kept += rt;
+        if (spl) {
+          const uint32_t o = atomicAdd(&s.spill_n, 1u);
+          if (o < cfg.spill_cap) spill[o] = key;
+          smin = key < smin ? key : smin;
+        }
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        unsigned long long o = __shfl_xor_sync(0xffffffffu, smin, off);
+        smin = o < smin ? o : smin;
+      }
+      if (lane == 0) s.wmin[warp] = smin;
+      __syncthreads();
+      if (tid == 0) {
+        unsigned long long mn = s.spill_min;
+        for (int w = 0; w < kWideWarps; w++) mn = s.wmin[w] < mn ? s.wmin[w] : mn;
+        s.spill_min = mn;
+        if (s.spill_n > cfg.spill_cap) { s.spill_n = cfg.spill_cap; s.status |= kStatusCandidateOverflow; }
+        s.first_new = 0xffffffffu;
+      }
+      __syncthreads();
+      if (kept == 0) continue;
+      cta_bitonic_sort(nkey, kept, NB);
+      // ---- merge into the other list buffer (entries compare without the expanded bit) ---
+      unsigned long long* dst = lists + (size_t)(s.cur ^ 1u) * L;
+      for (uint32_t i = tid; i < n; i += blockDim.x) {
+        const unsigned long long k = list[i];
+        const uint32_t pos = i + warp_lower_bound(nkey, kept, k & ~(unsigned long long)kExpandedBit);
+        if (pos < L) dst[pos] = k;
+        else if (!key_expanded(k)) {
+          const uint32_t o = atomicAdd(&s.spill_n, 1u);
+          if (o < cfg.spill_cap) spill[o] = k;
+          atomicMin(&s.spill_min, k);
+        }
+      }
+      for (uint32_t j = tid; j < kept; j += blockDim.x) {
+        const unsigned long long k = nkey[j];
+        uint32_t lo = 0, hi = n;
+        while (lo < hi) {
+          uint32_t mid = (lo + hi) >> 1;
+          if ((list[mid] & ~(unsigned long long)kExpandedBit) < k) lo = mid + 1; else hi = mid;
+        }
+        const uint32_t pos = j + lo;
+        if (pos < L) {
+          dst[pos] = k;
+          atomicMin(&s.first_new, pos);
+        } else {
+          const uint32_t o = atomicAdd(&s.spill_n, 1u);
+          if (o < cfg.spill_cap) spill[o] = k;
+          atomicMin(&s.spill_min, k);
+        }
+      }
+      __syncthreads();
+      if (tid == 0) {
+        s.cur ^= 1u;
+        s.n = min(n + kept, L);
+        if (s.first_new < s.scan0) s.scan0 = s.first_new;
+        if (s.spill_n > cfg.spill_cap) { s.spill_n = cfg.spill_cap; s.status |= kStatusCandidateOverflow; }
+      }
+      __syncthreads();
+    }
+    // ---- exact re-rank of the best entries with the full-precision rows --------------------
+    {
+      const unsigned long long* list = lists + (size_t)s.cur * L;
+      const uint32_t n = s.n;
+      const uint32_t R = min(n, max(P.size, (uint32_t)((P.size * cfg.rerank_x16 + 15) / 16)));
+      const uint32_t gpb = kWideThreads / NG;
+      for (uint32_t b = 0; b < R; b += gpb) {
+        const uint32_t i = b + (uint32_t)(tid / NG);
+        const bool valid = i < R;
+        const uint32_t id = valid ? key_rawid(list[i]) : 0u;
+        float d = group_distance<OT, M>(qn, g.objects + (size_t)id * rc, (int)rc, ngl, NG);
+        if (valid && ngl == 0) nkey[i] = pack_key(d, id);
+      }
+      __syncthreads();
+      cta_bitonic_sort(nkey, R, NB);
+      if (warp == 0) {
+        uint32_t nout = 0;
+        for (uint32_t b = 0; b < R && nout < P.size_out; b += 32) {
+          uint32_t i = b + lane;
+          bool ok = i < R && key_dist(nkey[i]) <= user_radius;
+          unsigned bal = __ballot_sync(0xffffffffu, ok);
+          uint32_t pos = nout + __popc(bal & ((1u << lane) - 1u));
+          if (ok && pos < P.size_out) out[P.out_off + pos] = ObjDist{key_id(nkey[i]), key_dist(nkey[i])};
+          nout = min(P.size_out, nout + __popc(bal));
+        }
+        if (lane == 0) {
+          out_count[q] = nout;
+          stats[q] = QueryStats{s.dc, s.expansions, s.visited, s.edges, s.status};
+        }
+      }
+    }
+    uint4* bm4 = reinterpret_cast<uint4*>(bitmap);
+    for (uint32_t i = tid; i < cfg.bitmap_words / 4; i += blockDim.x) bm4[i] = make_uint4(0, 0, 0, 0);
+    __syncthreads();
+  }
+}
+
+}  // namespace ngtg

@@ -1,0 +1,19 @@
+// Instantiations of the CTA-per-query ("wide") batched graph search kernel.
+#include "graph_wide.cuh"
+#include "kernels.h"
+
+namespace ngtg {
+
+WideKernelFn wide_kernel(ObjType ot, Metric m, bool bf16_rows) {
+  m = kernel_metric(m);
+  if (ot == ObjType::Float && bf16_rows && m == Metric::L2)
+    return &graph_search_wide_kernel<ObjType::Bfloat16, ObjType::Float, Metric::L2>;
+  if (ot == ObjType::Float && !bf16_rows && m == Metric::L2)
+    return &graph_search_wide_kernel<ObjType::Float, ObjType::Float, Metric::L2>;
+  if (ot == ObjType::Uint8 && m == Metric::L2) return &graph_search_wide_kernel<ObjType::Uint8, ObjType::Uint8, Metric::L2>;
+  return nullptr;
+}
+
+size_t wide_kernel_smem_bytes(uint32_t row_chunks, const WideConfig& c) { return wide_smem_bytes(row_chunks, c); }
+
+}  // namespace ngtg

@@ -29,6 +29,13 @@ typedef void (*QBGKernelFn)(DevGraph, DevQG, const uint32_t*, const uint4*, uint
 QBGKernelFn qbg_kernel(uint32_t m);
 size_t qbg_kernel_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, const QBGConfig& c);
 
+struct WideConfig;
+typedef void (*WideKernelFn)(DevGraph, const uint4*, const uint4*, uint32_t, const QueryParams*, const uint32_t*,
+                             ObjDist*, uint32_t*, QueryStats*, uint32_t*, uint32_t*, unsigned long long*, WideConfig);
+// CTA-per-query batched kernel (float L2 with bf16 or fp32 search rows, uint8 L2); nullptr otherwise.
+WideKernelFn wide_kernel(ObjType ot, Metric m, bool bf16_rows);
+size_t wide_kernel_smem_bytes(uint32_t row_chunks, const WideConfig& c);
+
 // Batched kernel for (object type, metric); bf16_rows selects the bf16 search
 // rows for float objects.  nullptr when unsupported.
 // rows_in_flight (rows per lane group the distance loop keeps in flight) and

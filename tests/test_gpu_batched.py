@@ -1,4 +1,5 @@
-"""GPU tests of the batched (warp-per-query, bf16 + exact re-rank) graph search.
+"""GPU tests of the batched graph search (bf16 + exact re-rank): the
+warp-per-query kernel and the CTA-per-query ("wide") kernel.
 
 Its visit order is parallel, so its ids are judged by recall: against the
 exact ground truth (the reference's own linear-search golden results, ties by
@@ -15,6 +16,8 @@ from golden_util import is_integer_fixture, materialize
 pytestmark = pytest.mark.gpu
 
 KERNEL_BATCHED = 1
+KERNEL_WIDE = 3
+WIDE_CASES = {"c1_f32_l2", "c1_f32_l2_onng", "u8_l2"}      # float L2 and uint8 L2 indexes
 
 
 @pytest.fixture(scope="module")
@@ -38,9 +41,12 @@ CASES = [("c1_f32_l2", 0, 10), ("c1_f32_l2", 2, 10), ("c1_f32_l2_onng", 0, 11), 
          ("u8_l1", 0, 1), ("f32_cosine", 0, 1), ("f32_ncosine", 0, 1), ("f16_l2", 0, 1)]
 
 
+@pytest.mark.parametrize("kernel", [KERNEL_BATCHED, KERNEL_WIDE])
 @pytest.mark.parametrize("name,graph_setting,linear_setting", CASES)
-def test_batched_recall_not_below_reference(name, graph_setting, linear_setting, workdir):
+def test_batched_recall_not_below_reference(name, graph_setting, linear_setting, kernel, workdir):
     from ngt_gb300 import Index
+    if kernel == KERNEL_WIDE and name not in WIDE_CASES:
+        pytest.skip("the wide kernel is built for float L2 and uint8 L2 indexes")
     path, meta, queries, golden = materialize(name, workdir)
     s = meta["settings"][graph_setting]
     k, eps, nq = s["k"], s["epsilon"], s["nq"]
@@ -58,7 +64,7 @@ def test_batched_recall_not_below_reference(name, graph_setting, linear_setting,
 
     ref_ids, ref_n = golden["ids_%d" % graph_setting], golden["count_%d" % graph_setting]
     with Index(path, read_only=True) as ix:
-        ids, ds, n = ix.batch_search(queries[:nq], k=k, epsilon=eps, kernel=KERNEL_BATCHED)
+        ids, ds, n = ix.batch_search(queries[:nq], k=k, epsilon=eps, kernel=kernel)
     r_ref = _tie_aware_recall(ref_ids, ref_n, gt_d, k, qrows, files.objects, dist)
     r_ours = _tie_aware_recall(ids, n, gt_d, k, qrows, files.objects, dist)
     assert r_ours >= r_ref - 1e-12, (name, r_ours, r_ref)
@@ -91,20 +97,24 @@ def oracle_dist(files, a, b):
     return np.float32(lib.oracle_distance(files.otype, files.metric, a.ctypes.data, b.ctypes.data, files.dpad))
 
 
-def test_batched_mixed_parameters_and_edge_cases(workdir):
+@pytest.mark.parametrize("kernel", [KERNEL_BATCHED, KERNEL_WIDE])
+def test_batched_mixed_parameters_and_edge_cases(kernel, workdir):
     from ngt_gb300 import Index
     path, meta, queries, golden = materialize("c1_f32_l2", workdir)
     with Index(path, read_only=True) as ix:
-        ids, ds, n = ix.batch_search(queries[:50], k=0, epsilon=0.1, kernel=KERNEL_BATCHED)
+        ids, ds, n = ix.batch_search(queries[:50], k=0, epsilon=0.1, kernel=kernel)
         assert (n == 0).all()
-        ids, ds, n = ix.batch_search(queries[:50], k=10, epsilon=0.1, radius=0.0, kernel=KERNEL_BATCHED)
+        ids, ds, n = ix.batch_search(queries[:50], k=10, epsilon=0.1, radius=0.0, kernel=kernel)
         assert (n == 0).all()
         ks = np.array([1, 5, 10, 50, 100] * 40)
-        ids, ds, n = ix.batch_search(queries[:200], k=ks, epsilon=0.1, kernel=KERNEL_BATCHED)
+        ids, ds, n = ix.batch_search(queries[:200], k=ks, epsilon=0.1, kernel=kernel)
         assert (n == ks).all()
         # a radius keeps only results within it
-        ids, ds, n = ix.batch_search(queries[:200], k=10, epsilon=0.1, radius=300.0, kernel=KERNEL_BATCHED)
+        ids, ds, n = ix.batch_search(queries[:200], k=10, epsilon=0.1, radius=300.0, kernel=kernel)
         assert all((ds[j, :n[j]] <= 300.0).all() for j in range(200))
+        # a large epsilon drives the spill tier and its refills
+        ids, ds, n, st = ix.batch_search(queries[:100], k=100, epsilon=0.3, kernel=kernel, with_stats=True)
+        assert (n == 100).all() and (st["status"] & 1 == 0).all()
 
 
 def test_rows_in_flight_does_not_change_results(tmp_path):
