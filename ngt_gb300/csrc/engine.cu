@@ -564,7 +564,8 @@ void GraphEngine::launch_wide(const uint4* d_rows, size_t nq, const QueryParams*
                                 : std::max<uint32_t>({512u, next_pow2(rerank_max), L,
                                                       std::min<uint32_t>(4096, next_pow2(cfg.parents * 100))});
   cfg.search_chunks = bf16 ? dev_.row_chunks / 2 : dev_.row_chunks;
-  cfg.stage_rows = std::max<uint32_t>(32, std::min<uint32_t>(512, (96u * 1024u) / (cfg.search_chunks * 16)));
+  // about 64 KB of staged rows, so that two CTAs share an SM
+  cfg.stage_rows = std::max<uint32_t>(32, std::min<uint32_t>(256, (64u * 1024u) / (cfg.search_chunks * 16)));
   cfg.sgroup = std::min<uint32_t>(32, next_pow2((cfg.search_chunks + 1) / 2));
   cfg.ngroup = std::min<uint32_t>(32, next_pow2(dev_.row_chunks));
   cfg.rerank_x16 = (uint32_t)std::ceil(rf * 16.0f);
