@@ -45,7 +45,8 @@ LIST_SWEEP = [128, 256]
 PARENT_SWEEP = [2, 4]
 # (rows per lane group in flight, CTAs per SM the registers are budgeted for,
 # neighbour slots per iteration; 0 = automatic).  Only the last can change results.
-VARIANT_SWEEP = [(4, 5, 0), (6, 4, 0), (6, 5, 0), (4, 6, 256), (2, 8, 256), (4, 5, 256)]
+VARIANT_SWEEP = [(4, 5, 0), (6, 4, 0), (4, 6, 256), (4, 5, 256)]
+WIDE_PARENTS = 8                  # parents per step of the CTA-per-query kernel the serving loop uses
 # dram__bytes_read.sum + dram__bytes_write.sum of one graph_search_fast_kernel
 # launch of 2,000 queries on this workload (1M x 128, k=10, epsilon 0.08; ncu
 # capture summarised under profiles/), per query.  Scaled by the queries of one
@@ -184,14 +185,14 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def served_latency(ix, queries, k, eps, rates, seconds):
+def served_latency(ix, queries, k, eps, rates, seconds, kernel=1, inflight=3):
     """Poisson arrivals of requests (sizes geometric on 1..256, mean ~16 queries) at each
     target query rate through the serving loop; p50/p99 request latency (submit to completion)."""
     import threading
     from ngt_gb300 import Server
     out = []
     rng = np.random.default_rng(43)
-    with Server(ix, max_batch=4096, inflight=3, max_k=max(16, k)) as srv:
+    with Server(ix, max_batch=4096, inflight=inflight, max_k=max(16, k), kernel=kernel) as srv:
         for rate in rates:
             sizes, gaps = [], []
             t = 0.0
@@ -236,7 +237,7 @@ def served_latency(ix, queries, k, eps, rates, seconds):
             out.append({"offered_qps": rate, "achieved_qps": round(total / wall, 1), "requests": len(sizes),
                         "p50_ms": round(float(np.percentile(lat_np, 50)), 3),
                         "p99_ms": round(float(np.percentile(lat_np, 99)), 3)})
-            log("served at %d q/s offered: %s" % (rate, out[-1]))
+            log("served (kernel %d) at %d q/s offered: %s" % (kernel, rate, out[-1]))
     return out
 
 
@@ -311,7 +312,7 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     from ngt_gb300 import Index
-    from ngt_gb300.base import KERNEL_BATCHED, KERNEL_EXACT, QUERY_STATS_DTYPE
+    from ngt_gb300.base import KERNEL_BATCHED, KERNEL_EXACT, KERNEL_WIDE, QUERY_STATS_DTYPE
 
     t_setup = time.time()
     base, queries = workload(args, rank)
@@ -380,7 +381,7 @@ def main():
         cnt_np = cnt.cpu().numpy().astype(np.int64)
         stats = st.cpu().numpy().view(QUERY_STATS_DTYPE).reshape(nq)
         rec = recall(base, queries, ids_np, cnt_np, kth, k)
-        srow = row_bytes // 2 if kernel == KERNEL_BATCHED else row_bytes
+        srow = row_bytes // 2 if kernel in (KERNEL_BATCHED, KERNEL_WIDE) else row_bytes
         rerank = 0 if kernel == KERNEL_EXACT else 2 * k * row_bytes
         bytes_pq = (srow * stats["distance_computations"].astype(np.float64) + 4.0 * stats["edges_read"]
                     + row_bytes + rerank)
@@ -452,8 +453,17 @@ def main():
     d2h = nq * (int(np.ceil(k * (1 + head["epsilon"]))) + 1) * 8 + nq * 4 + nq * QUERY_STATS_DTYPE.itemsize
 
     # ---- served: continuous batching under a Poisson request stream ------------------------------
-    served = served_latency(ix, queries, k, head["epsilon"], args.served_rates, args.served_seconds) \
-        if args.served_seconds > 0 else None
+    # the serving loop launches the CTA-per-query kernel (lowest latency per query); the
+    # warp-per-query kernel's serving figures are reported beside it
+    served = served_warp = wide = None
+    if args.served_seconds > 0:
+        served_warp = served_latency(ix, queries, k, head["epsilon"], args.served_rates, args.served_seconds,
+                                     kernel=KERNEL_BATCHED)
+        ix.set_batched_tuning(list_capacity=256, parents=WIDE_PARENTS)
+        wide = timed(KERNEL_WIDE, head["epsilon"])
+        log("wide kernel: %.1f q/s at epsilon %g, recall %.4f" % (wide["qps"], wide["epsilon"], wide["recall"]))
+        served = served_latency(ix, queries, k, head["epsilon"], args.served_rates, args.served_seconds,
+                                kernel=KERNEL_WIDE, inflight=4)
 
     # ---- CPU baseline (oracle port on a bounded sample) ------------------------------------------
     cpu = None
@@ -494,7 +504,12 @@ def main():
                          "peak_source": peak_kind,
                          "basis": "(%d*DC + 4*edges + %d query + re-rank %d*2k) bytes per query over the kernel's "
                                   "median event time" % (head["row_bytes"], row_bytes, row_bytes)},
-            "served": served,
+            "served": {"kernel": "CTA per query (bf16 rows, rows of a step staged in shared memory), "
+                                 "%d parents per step" % WIDE_PARENTS,
+                       "qps_10000_batch": round(wide["qps"], 1) if wide else None,
+                       "recall_at_k": round(wide["recall"], 4) if wide else None,
+                       "rates": served,
+                       "warp_per_query_kernel_rates": served_warp} if served else None,
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

@@ -85,6 +85,8 @@ typedef struct {
   uint32_t rows_in_flight;
   uint32_t ctas_per_sm;
   uint32_t neighbour_capacity;
+  uint32_t cta_threads;        /* NGTGPU_KERNEL_WIDE: 128 or 256 threads per query (float L2: both) */
+  uint32_t stage_kilobytes;    /* NGTGPU_KERNEL_WIDE: shared memory for staged rows (default 64) */
 } NGTGPUBatchedTuning;
 bool ngtgpu_set_batched_tuning_ex(NGTIndex, const NGTGPUBatchedTuning *tuning, NGTError);
 
@@ -120,6 +122,10 @@ bool ngtgpu_search_exact_noalloc(NGTIndex, const void *d_rows, size_t nq, const 
 typedef void *NGTGPUServer;
 NGTGPUServer ngtgpu_server_create(NGTIndex, uint32_t max_batch_queries, uint32_t inflight, uint32_t max_k,
                                   NGTError);
+/* The same with the kernel the launches use: NGTGPU_KERNEL_BATCHED (throughput),
+ * NGTGPU_KERNEL_BATCHED_FP32, or NGTGPU_KERNEL_WIDE (lowest latency per query). */
+NGTGPUServer ngtgpu_server_create_ex(NGTIndex, uint32_t max_batch_queries, uint32_t inflight, uint32_t max_k,
+                                     uint32_t kernel, NGTError);
 int64_t ngtgpu_server_submit(NGTGPUServer, const float *queries, size_t nq, int32_t dim,
                              const NGTQueryParameters *params, size_t nparams, NGTError);
 bool ngtgpu_server_wait(NGTGPUServer, int64_t ticket, NGTObjectDistance *results, size_t kmax, uint32_t *counts,

@@ -70,7 +70,8 @@ class QBGQueryFloat(ctypes.Structure):
 class BatchedTuning(ctypes.Structure):
     """NGTGPUBatchedTuning (include/ngtgpu.h)."""
     _fields_ = [("list_capacity", c_uint32), ("parents", c_uint32), ("rerank_factor", c_float),
-                ("rows_in_flight", c_uint32), ("ctas_per_sm", c_uint32), ("neighbour_capacity", c_uint32)]
+                ("rows_in_flight", c_uint32), ("ctas_per_sm", c_uint32), ("neighbour_capacity", c_uint32),
+                ("cta_threads", c_uint32), ("stage_kilobytes", c_uint32)]
 
 
 class QueryStats(ctypes.Structure):
@@ -128,6 +129,7 @@ def load_library() -> ctypes.CDLL:
         "ngtgpu_set_batched_rows_in_flight": ([c_void_p, c_uint32, c_void_p], c_bool),
         "ngtgpu_set_batched_tuning_ex": ([c_void_p, POINTER(BatchedTuning), c_void_p], c_bool),
         "ngtgpu_server_create": ([c_void_p, c_uint32, c_uint32, c_uint32, c_void_p], c_void_p),
+        "ngtgpu_server_create_ex": ([c_void_p, c_uint32, c_uint32, c_uint32, c_uint32, c_void_p], c_void_p),
         "ngtgpu_server_submit": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QueryParameters), c_size_t,
                                   c_void_p], ctypes.c_int64),
         "ngtgpu_server_wait": ([c_void_p, ctypes.c_int64, c_void_p, c_size_t, c_void_p, POINTER(ctypes.c_double),
@@ -267,8 +269,10 @@ class Index:
         return out + (stats,) if with_stats else out
 
     def set_batched_tuning(self, list_capacity: int = 0, parents: int = 0, rerank_factor: float = 0.0,
-                           rows_in_flight: int = 0, ctas_per_sm: int = 0, neighbour_capacity: int = 0):
-        t = BatchedTuning(list_capacity, parents, rerank_factor, rows_in_flight, ctas_per_sm, neighbour_capacity)
+                           rows_in_flight: int = 0, ctas_per_sm: int = 0, neighbour_capacity: int = 0,
+                           cta_threads: int = 0, stage_kilobytes: int = 0):
+        t = BatchedTuning(list_capacity, parents, rerank_factor, rows_in_flight, ctas_per_sm, neighbour_capacity,
+                          cta_threads, stage_kilobytes)
         self._check(self._lib.ngtgpu_set_batched_tuning_ex(self._index, ctypes.byref(t), self._err))
 
     def kernel_launches(self) -> int:
@@ -505,11 +509,12 @@ class QBGIndex:
 class Server:
     """Continuous-batching serving loop over an open Index (ngtgpu_server_*)."""
 
-    def __init__(self, index: Index, max_batch: int = 4096, inflight: int = 3, max_k: int = 128):
+    def __init__(self, index: Index, max_batch: int = 4096, inflight: int = 3, max_k: int = 128,
+                 kernel: int = KERNEL_BATCHED):
         self._ix = index
         self._lib = index._lib
         self._err = self._lib.ngt_create_error_object()
-        self._srv = self._lib.ngtgpu_server_create(index._index, max_batch, inflight, max_k, self._err)
+        self._srv = self._lib.ngtgpu_server_create_ex(index._index, max_batch, inflight, max_k, kernel, self._err)
         if not self._srv:
             raise NativeError(self._lib.ngt_get_error_string(self._err).decode())
         self.max_k = max_k

@@ -454,7 +454,8 @@ bool ngtgpu_set_batched_tuning_ex(NGTIndex index, const NGTGPUBatchedTuning* tun
       tuning->rerank_factor < 0.f || tuning->neighbour_capacity > 4096 ||
       !(tuning->rows_in_flight == 0 || tuning->rows_in_flight == 2 || tuning->rows_in_flight == 4 ||
         tuning->rows_in_flight == 6 || tuning->rows_in_flight == 8) ||
-      tuning->ctas_per_sm > 8) {
+      tuning->ctas_per_sm > 8 || !(tuning->cta_threads == 0 || tuning->cta_threads == 128 ||
+                                   tuning->cta_threads == 256) || tuning->stage_kilobytes > 200) {
     CAPI_PARAM_ERROR(error, "index = " << index << " tuning = " << tuning);
     return false;
   }
@@ -465,6 +466,8 @@ bool ngtgpu_set_batched_tuning_ex(NGTIndex index, const NGTGPUBatchedTuning* tun
   t.rows_in_flight = tuning->rows_in_flight;
   t.ctas_per_sm = tuning->ctas_per_sm;
   t.nbr_cap = tuning->neighbour_capacity;
+  t.cta_threads = tuning->cta_threads;
+  t.stage_kb = tuning->stage_kilobytes;
   engine(index)->set_tuning(t);
   return true;
 }

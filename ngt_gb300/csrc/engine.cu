@@ -417,7 +417,7 @@ void GraphEngine::ensure_scratch(size_t grid) {
 
 bool GraphEngine::fast_supported(Kernel k) const {
   if (k == Kernel::Exact) return true;
-  if (k == Kernel::Wide) return wide_kernel(host_.prop.otype, host_.prop.metric, true) != nullptr;
+  if (k == Kernel::Wide) return wide_kernel(host_.prop.otype, host_.prop.metric, true, 256) != nullptr;
   return fast_kernel(host_.prop.otype, host_.prop.metric, k == Kernel::Fast) != nullptr;
 }
 
@@ -486,12 +486,13 @@ void GraphEngine::search_device(const uint4* d_rows, size_t nq, const SearchArgs
 
 void GraphEngine::search_device_slot(const uint4* d_rows, size_t nq, const SearchArgs* args, size_t nargs,
                                      ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, size_t kmax,
-                                     cudaStream_t stream, size_t slot) {
+                                     cudaStream_t stream, size_t slot, Kernel kernel) {
   std::lock_guard<std::mutex> lock(mu_);
   NGT_CUDA(cudaSetDevice(device_));
   if (nq == 0) return;
   if (slot == 0 || slot >= fast_scratch_.size()) throw std::runtime_error("invalid scratch set");
-  if (!fast_supported(Kernel::Fast)) throw std::runtime_error("the batched kernel does not support this index type");
+  if (kernel == Kernel::Exact || !fast_supported(kernel))
+    throw std::runtime_error("the batched kernel does not support this index type");
   std::vector<QueryParams> params;
   std::vector<uint32_t> seeds;
   uint32_t max_size = 0;
@@ -502,8 +503,11 @@ void GraphEngine::search_device_slot(const uint4* d_rows, size_t nq, const Searc
   NGT_CUDA(cudaMallocAsync(&d_seeds, seeds.size() * 4, stream));
   NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QueryParams), cudaMemcpyHostToDevice, stream));
   NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, stream));
-  launch_fast(d_rows, nq, d_params, d_seeds, max_size, d_out, d_counts, d_stats, stream, Kernel::Fast,
-              fast_scratch_[slot]);
+  if (kernel == Kernel::Wide)
+    launch_wide(d_rows, nq, d_params, d_seeds, max_size, d_out, d_counts, d_stats, stream, fast_scratch_[slot]);
+  else
+    launch_fast(d_rows, nq, d_params, d_seeds, max_size, d_out, d_counts, d_stats, stream, kernel,
+                fast_scratch_[slot]);
   NGT_CUDA(cudaFreeAsync(d_params, stream));
   NGT_CUDA(cudaFreeAsync(d_seeds, stream));
   // the pageable host parameter copies above are complete once they return
@@ -549,8 +553,9 @@ void GraphEngine::launch_wide(const uint4* d_rows, size_t nq, const QueryParams*
                               uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats,
                               cudaStream_t stream, FastScratch& scratch) {
   const bool bf16 = host_.prop.otype == ObjType::Float;
-  WideKernelFn fn = wide_kernel(host_.prop.otype, host_.prop.metric, bf16);
-  if (!fn) throw std::runtime_error("the wide kernel does not support this index type");
+  const uint32_t threads = tuning_.cta_threads ? tuning_.cta_threads : 256u;
+  WideKernelFn fn = wide_kernel(host_.prop.otype, host_.prop.metric, bf16, threads);
+  if (!fn) throw std::runtime_error("the wide kernel does not support this index type or CTA size");
   if (bf16) ensure_bf16_rows();
   WideConfig cfg{};
   uint32_t L = tuning_.list_cap ? next_pow2(tuning_.list_cap) : next_pow2(std::max<uint32_t>(256, 4 * max_size));
@@ -564,8 +569,9 @@ void GraphEngine::launch_wide(const uint4* d_rows, size_t nq, const QueryParams*
                                 : std::max<uint32_t>({512u, next_pow2(rerank_max), L,
                                                       std::min<uint32_t>(4096, next_pow2(cfg.parents * 100))});
   cfg.search_chunks = bf16 ? dev_.row_chunks / 2 : dev_.row_chunks;
-  // about 64 KB of staged rows, so that two CTAs share an SM
-  cfg.stage_rows = std::max<uint32_t>(32, std::min<uint32_t>(256, (64u * 1024u) / (cfg.search_chunks * 16)));
+  // 64 KB of staged rows by default (two 256-thread CTAs share an SM)
+  const uint32_t stage_bytes = (tuning_.stage_kb ? tuning_.stage_kb : 64u) * 1024u;
+  cfg.stage_rows = std::max<uint32_t>(16, std::min<uint32_t>(512, stage_bytes / (cfg.search_chunks * 16)));
   cfg.sgroup = std::min<uint32_t>(32, next_pow2((cfg.search_chunks + 1) / 2));
   cfg.ngroup = std::min<uint32_t>(32, next_pow2(dev_.row_chunks));
   cfg.rerank_x16 = (uint32_t)std::ceil(rf * 16.0f);
@@ -575,19 +581,19 @@ void GraphEngine::launch_wide(const uint4* d_rows, size_t nq, const QueryParams*
   size_t smem = wide_kernel_smem_bytes(dev_.row_chunks, cfg);
   int max_smem = 0, per_sm = 0, sms = 0;
   NGT_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
-  while (smem > (size_t)max_smem && cfg.stage_rows > 32) {
+  while (smem > (size_t)max_smem && cfg.stage_rows > 16) {
     cfg.stage_rows /= 2;
     smem = wide_kernel_smem_bytes(dev_.row_chunks, cfg);
   }
   if (smem > (size_t)max_smem) throw std::runtime_error("wide search state does not fit in shared memory");
   NGT_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kWideThreads, smem));
+  NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, (int)threads, smem));
   NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
   size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
   ensure_fast_scratch(scratch, grid, stream);
   NGT_CUDA(cudaMemsetAsync(scratch.work, 0, 4, stream));
   const uint4* srows = bf16 ? static_cast<const uint4*>(d_bf16_) : dev_.objects;
-  fn<<<(unsigned)grid, kWideThreads, smem, stream>>>(dev_, srows, d_rows, (uint32_t)nq, d_params, d_seeds, d_out,
+  fn<<<(unsigned)grid, threads, smem, stream>>>(dev_, srows, d_rows, (uint32_t)nq, d_params, d_seeds, d_out,
                                                       d_counts, d_stats, scratch.bitmaps, scratch.work,
                                                       scratch.spill, cfg);
   NGT_CUDA(cudaGetLastError());

@@ -40,6 +40,8 @@ struct FastTuning {
   uint32_t rows_in_flight = 0; // rows per lane group in flight in the distance loop (2, 4, 6 or 8)
   uint32_t ctas_per_sm = 0;    // register budget of the instantiation (4..8)
   uint32_t nbr_cap = 0;        // neighbour slots per iteration (power of two >= 256)
+  uint32_t cta_threads = 0;    // wide kernel: threads per CTA (128 or 256)
+  uint32_t stage_kb = 0;       // wide kernel: shared memory for staged rows (KB)
 };
 
 // Parameters of one quantized-graph query (NGTQGQueryParameters,
@@ -133,7 +135,8 @@ class GraphEngine {
   // The batched kernel with scratch set `slot` (1 .. scratch_sets-1 are free for
   // concurrent launches on different streams; slot 0 belongs to search_device).
   void search_device_slot(const uint4* d_rows, size_t nq, const SearchArgs* args, size_t nargs, ObjDist* d_out,
-                          uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream, size_t slot);
+                          uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream, size_t slot,
+                          Kernel kernel = Kernel::Fast);
   void reserve_scratch_sets(size_t n);
   // Bytes of device scratch one batched launch of nq queries uses (admission).
   size_t batched_scratch_bytes(size_t nq) const;

@@ -4,7 +4,7 @@
 // re-rank of the best candidates), with every phase of an iteration spread
 // over the CTA so that one query moves many rows at once:
 //   * the P parents' edge slots are read, filtered against the query's
-//     visited bitmap and compacted by all 256 threads;
+//     visited bitmap and compacted by all threads of the CTA (128 or 256);
 //   * the new neighbours' search rows are copied into shared memory with
 //     asynchronous 16-byte copies (cp.async), all of a round in flight at once,
 //     and their distances computed from shared memory;
@@ -23,8 +23,8 @@
 
 namespace ngtg {
 
-constexpr int kWideThreads = 256;
-constexpr int kWideWarps = kWideThreads / 32;
+constexpr int kWideMaxThreads = 256;
+constexpr int kWideMaxWarps = kWideMaxThreads / 32;
 
 struct WideConfig {
   uint32_t list_cap;       // L: power of two
@@ -46,8 +46,8 @@ struct WideShared {
   unsigned long long spill_min, worst;
   float limit, insert_limit;
   uint32_t parents[32], pexcl[32], pbase[32];
-  uint32_t wcnt[kWideWarps], wcnt2[kWideWarps];
-  unsigned long long wmin[kWideWarps];
+  uint32_t wcnt[kWideMaxWarps], wcnt2[kWideMaxWarps];
+  unsigned long long wmin[kWideMaxWarps];
 };
 
 inline size_t wide_smem_bytes(uint32_t row_chunks, const WideConfig& c) {
@@ -100,8 +100,8 @@ __device__ __forceinline__ uint32_t cta_compact(bool flag, uint32_t* wcnt, uint3
   if (lane == 0) wcnt[warp] = __popc(bal);
   __syncthreads();
   uint32_t base = 0, tot = 0;
-#pragma unroll
-  for (int w = 0; w < kWideWarps; w++) {
+  const int nw = (int)(blockDim.x >> 5);
+  for (int w = 0; w < nw; w++) {
     uint32_t c = wcnt[w];
     if (w < warp) base += c;
     tot += c;
@@ -111,8 +111,9 @@ __device__ __forceinline__ uint32_t cta_compact(bool flag, uint32_t* wcnt, uint3
   return base + __popc(bal & ((1u << lane) - 1u));
 }
 
-template <ObjType ST, ObjType OT, Metric M>
-__global__ void __launch_bounds__(kWideThreads, 1)
+// T: threads per CTA (128 or 256), one query per CTA.
+template <ObjType ST, ObjType OT, Metric M, int T>
+__global__ void __launch_bounds__(T, 1)
 graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint4* __restrict__ queries,
                          uint32_t nq, const QueryParams* __restrict__ params, const uint32_t* __restrict__ seed_list,
                          ObjDist* __restrict__ out, uint32_t* __restrict__ out_count, QueryStats* __restrict__ stats,
@@ -146,7 +147,7 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       }
       cp_async_wait_all();
       __syncthreads();
-      const uint32_t gpb = kWideThreads / SG;
+      const uint32_t gpb = (uint32_t)T / SG;
       for (uint32_t b = 0; b < nr; b += gpb) {          // uniform trip count per warp
         const uint32_t i = b + (uint32_t)(tid / SG);
         const bool valid = i < nr;
@@ -463,7 +464,7 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       __syncthreads();
       if (tid == 0) {
         unsigned long long mn = s.spill_min;
-        for (int w = 0; w < kWideWarps; w++) mn = s.wmin[w] < mn ? s.wmin[w] : mn;
+        for (int w = 0; w < T / 32; w++) mn = s.wmin[w] < mn ? s.wmin[w] : mn;
         s.spill_min = mn;
         if (s.spill_n > cfg.spill_cap) { s.spill_n = cfg.spill_cap; s.status |= kStatusCandidateOverflow; }
         s.first_new = 0xffffffffu;
@@ -514,7 +515,7 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       const unsigned long long* list = lists + (size_t)s.cur * L;
       const uint32_t n = s.n;
       const uint32_t R = min(n, max(P.size, (uint32_t)((P.size * cfg.rerank_x16 + 15) / 16)));
-      const uint32_t gpb = kWideThreads / NG;
+      const uint32_t gpb = (uint32_t)T / NG;
       for (uint32_t b = 0; b < R; b += gpb) {
         const uint32_t i = b + (uint32_t)(tid / NG);
         const bool valid = i < R;

@@ -4,13 +4,17 @@
 
 namespace ngtg {
 
-WideKernelFn wide_kernel(ObjType ot, Metric m, bool bf16_rows) {
+WideKernelFn wide_kernel(ObjType ot, Metric m, bool bf16_rows, uint32_t threads) {
   m = kernel_metric(m);
+  if (threads != 128 && threads != 256) return nullptr;
   if (ot == ObjType::Float && bf16_rows && m == Metric::L2)
-    return &graph_search_wide_kernel<ObjType::Bfloat16, ObjType::Float, Metric::L2>;
+    return threads == 128 ? &graph_search_wide_kernel<ObjType::Bfloat16, ObjType::Float, Metric::L2, 128>
+                          : &graph_search_wide_kernel<ObjType::Bfloat16, ObjType::Float, Metric::L2, 256>;
+  if (threads != 256) return nullptr;
   if (ot == ObjType::Float && !bf16_rows && m == Metric::L2)
-    return &graph_search_wide_kernel<ObjType::Float, ObjType::Float, Metric::L2>;
-  if (ot == ObjType::Uint8 && m == Metric::L2) return &graph_search_wide_kernel<ObjType::Uint8, ObjType::Uint8, Metric::L2>;
+    return &graph_search_wide_kernel<ObjType::Float, ObjType::Float, Metric::L2, 256>;
+  if (ot == ObjType::Uint8 && m == Metric::L2)
+    return &graph_search_wide_kernel<ObjType::Uint8, ObjType::Uint8, Metric::L2, 256>;
   return nullptr;
 }
 

@@ -32,8 +32,9 @@ size_t qbg_kernel_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, cons
 struct WideConfig;
 typedef void (*WideKernelFn)(DevGraph, const uint4*, const uint4*, uint32_t, const QueryParams*, const uint32_t*,
                              ObjDist*, uint32_t*, QueryStats*, uint32_t*, uint32_t*, unsigned long long*, WideConfig);
-// CTA-per-query batched kernel (float L2 with bf16 or fp32 search rows, uint8 L2); nullptr otherwise.
-WideKernelFn wide_kernel(ObjType ot, Metric m, bool bf16_rows);
+// CTA-per-query batched kernel with `threads` per CTA: 256 for float L2 (bf16 or
+// fp32 search rows) and uint8 L2, 128 also for float L2 on bf16 rows; nullptr otherwise.
+WideKernelFn wide_kernel(ObjType ot, Metric m, bool bf16_rows, uint32_t threads = 256);
 size_t wide_kernel_smem_bytes(uint32_t row_chunks, const WideConfig& c);
 
 // Batched kernel for (object type, metric); bf16_rows selects the bf16 search

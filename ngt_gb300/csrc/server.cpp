@@ -82,8 +82,8 @@ struct Lane {
 
 class Server {
  public:
-  Server(GraphEngine* e, size_t max_batch, size_t inflight, size_t max_k)
-      : e_(e), max_batch_(max_batch), max_k_(max_k), row_bytes_(e->host().row_bytes()) {
+  Server(GraphEngine* e, size_t max_batch, size_t inflight, size_t max_k, Kernel kernel = Kernel::Fast)
+      : e_(e), max_batch_(max_batch), max_k_(max_k), row_bytes_(e->host().row_bytes()), kernel_(kernel) {
     if (max_batch == 0 || inflight == 0 || max_k == 0) throw std::runtime_error("invalid server sizes");
     SRV_CUDA(cudaSetDevice(e->device()));
     e->reserve_scratch_sets(inflight + 1);
@@ -222,7 +222,7 @@ class Server {
     try {
       SRV_CUDA(cudaMemcpyAsync(l.d_rows, l.h_rows, nq * row_bytes_, cudaMemcpyHostToDevice, l.stream));
       e_->search_device_slot(l.d_rows, nq, args.data(), args.size(), l.d_out, l.d_counts, l.d_stats, l.kmax,
-                             l.stream, l.slot);
+                             l.stream, l.slot, kernel_);
       SRV_CUDA(cudaMemcpyAsync(l.h_out, l.d_out, nq * l.kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, l.stream));
       SRV_CUDA(cudaMemcpyAsync(l.h_counts, l.d_counts, nq * 4, cudaMemcpyDeviceToHost, l.stream));
       SRV_CUDA(cudaEventRecord(l.done_event, l.stream));
@@ -262,6 +262,7 @@ class Server {
 
   GraphEngine* e_;
   size_t max_batch_, max_k_, row_bytes_;
+  Kernel kernel_;
   std::vector<Lane> lanes_;
   std::deque<std::shared_ptr<Request>> pending_;
   std::map<int64_t, std::shared_ptr<Request>> tickets_;
@@ -298,12 +299,20 @@ extern "C" {
 
 NGTGPUServer ngtgpu_server_create(NGTIndex index, uint32_t max_batch_queries, uint32_t inflight, uint32_t max_k,
                                   NGTError error) {
-  if (index == nullptr) {
-    server_error(__FUNCTION__, "parametor error: index is NULL", error);
+  return ngtgpu_server_create_ex(index, max_batch_queries, inflight, max_k, NGTGPU_KERNEL_BATCHED, error);
+}
+
+NGTGPUServer ngtgpu_server_create_ex(NGTIndex index, uint32_t max_batch_queries, uint32_t inflight, uint32_t max_k,
+                                     uint32_t kernel, NGTError error) {
+  if (index == nullptr || !(kernel == NGTGPU_KERNEL_BATCHED || kernel == NGTGPU_KERNEL_BATCHED_FP32 ||
+                            kernel == NGTGPU_KERNEL_WIDE)) {
+    server_error(__FUNCTION__, "parametor error: index is NULL or the kernel is not a batched one", error);
     return nullptr;
   }
   try {
-    return new ngtg::Server(static_cast<ngtg::GraphEngine*>(index), max_batch_queries, inflight, max_k);
+    ngtg::Kernel k = kernel == NGTGPU_KERNEL_WIDE ? ngtg::Kernel::Wide
+                     : kernel == NGTGPU_KERNEL_BATCHED_FP32 ? ngtg::Kernel::FastFp32 : ngtg::Kernel::Fast;
+    return new ngtg::Server(static_cast<ngtg::GraphEngine*>(index), max_batch_queries, inflight, max_k, k);
   } catch (std::exception& ex) {
     server_error(__FUNCTION__, ex.what(), error);
     return nullptr;
