@@ -454,7 +454,7 @@ graph_search_fast_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       __syncwarp();
       edges_read += total;
       uint32_t cnt = 0;
-      constexpr int J = 8;
+      constexpr int J = 12;     // 384 edge slots per round: four parents of an ONNG node in one pass
       for (uint32_t base0 = 0; base0 < total; base0 += 32 * J) {
         uint32_t ids[J];
         bool fresh[J];

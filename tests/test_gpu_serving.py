@@ -22,7 +22,8 @@ def index_path(tmp_path_factory):
     return path, queries
 
 
-def test_results_in_the_mix_equal_results_alone(index_path):
+@pytest.mark.parametrize("kernel", [1, 3])
+def test_results_in_the_mix_equal_results_alone(index_path, kernel):
     from ngt_gb300 import Index, Server
     path, queries = index_path
     rng = np.random.default_rng(7)
@@ -34,8 +35,8 @@ def test_results_in_the_mix_equal_results_alone(index_path):
         start += n
         reqs.append((q, int(rng.choice([5, 10, 20])), float(rng.choice([0.05, 0.1, 0.15]))))
     with Index(path, read_only=True) as ix:
-        alone = [ix.batch_search(q, k=k, epsilon=e, kernel=KERNEL_BATCHED) for q, k, e in reqs]
-        with Server(ix, max_batch=256, inflight=3, max_k=64) as srv:
+        alone = [ix.batch_search(q, k=k, epsilon=e, kernel=kernel) for q, k, e in reqs]
+        with Server(ix, max_batch=256, inflight=3, max_k=64, kernel=kernel) as srv:
             tickets = [None] * len(reqs)
 
             def submitter(part):
