@@ -74,6 +74,7 @@ def parse():
     ap.add_argument("--served-rates", type=lambda s: [int(x) for x in s.split(",")], default=[5000, 20000, 50000],
                     help="offered query rates of the serving measurement")
     ap.add_argument("--served-seconds", type=float, default=2.0, help="length of each served-rate run")
+    ap.add_argument("--qg", type=int, default=1, help="also measure the quantized-graph search (1) or not (0)")
     ap.add_argument("--fixed", default=None,
                     help="EPS_PLAIN:EPS_BATCHED:LIST:PARENTS[:ROWS:CTAS:NBR] -- skip the epsilon / tuning sweeps")
     return ap.parse_args()
@@ -238,6 +239,71 @@ def served_latency(ix, queries, k, eps, rates, seconds, kernel=1, inflight=3, ma
                         "p50_ms": round(float(np.percentile(lat_np, 50)), 3),
                         "p99_ms": round(float(np.percentile(lat_np, 99)), 3)})
             log("served (kernel %d) at %d q/s offered: %s" % (kernel, rate, out[-1]))
+    return out
+
+
+QG_EPS_SWEEP = [0.0, 0.02, 0.04, 0.06, 0.08, 0.1, 0.12, 0.15, 0.2]
+
+
+def qg_measurement(path, base, queries, kth, k, steps, warmup, log_fn):
+    """Quantized-graph search (ngtqg_* C API, the exact-order QG kernel) on the same index:
+    a 4-bit PQ with 2-dimensional subvectors (64 subspaces), each node's first 128 edges;
+    the smallest epsilon of a sweep whose recall@k (result expansion 3, exact re-rank)
+    reaches the target, timed with queries resident in HBM."""
+    import torch
+    from ngt_gb300 import QuantizedIndex, qg_build
+    from ngt_gb300.base import QGQueryParameters, QUERY_STATS_DTYPE
+    if not os.path.exists(os.path.join(path, "qg", "grp")):
+        qg_build.build_qg(path, base, dsv=2, max_edges=128, log=log_fn)
+    t0 = time.time()
+    ix = QuantizedIndex(path, zero_based_numbering=False)
+    log_fn("qg: opened in %.1f s" % (time.time() - t0))
+    nq = len(queries)
+    cal = min(2000, nq)
+    eps_sel, curve = QG_EPS_SWEEP[-1], []
+    for eps in QG_EPS_SWEEP:
+        ids, ds, n = ix.batch_search(queries[:cal], size=k, epsilon=eps, result_expansion=3.0)
+        r = recall(base, queries[:cal], ids, n, kth[:cal], k)
+        curve.append((eps, round(r, 4)))
+        log_fn("qg epsilon %.2f recall@%d %.4f" % (eps, k, r))
+        if r >= RECALL_TARGET:
+            eps_sel = eps
+            break
+    rows = torch.from_numpy(ix.convert_queries(queries)).cuda()
+    res = torch.zeros((nq, k, 2), dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(nq, dtype=torch.int32, device="cuda")
+    st = torch.zeros((nq, QUERY_STATS_DTYPE.itemsize // 4), dtype=torch.int32, device="cuda")
+    p = QGQueryParameters(k, eps_sel, 3.0, -1.0)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        for _ in range(warmup):
+            ix.search_device(rows.data_ptr(), nq, p, res.data_ptr(), k, cnt.data_ptr(), st.data_ptr(),
+                             stream.cuda_stream)
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with torch.cuda.stream(stream):
+        for a, b in ev:
+            a.record(stream)
+            ix.search_device(rows.data_ptr(), nq, p, res.data_ptr(), k, cnt.data_ptr(), st.data_ptr(),
+                             stream.cuda_stream)
+            b.record(stream)
+    torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in ev]
+    ids = res[:, :, 0].cpu().numpy().view(np.uint32)
+    c = cnt.cpu().numpy().astype(np.int64)
+    stats = st.cpu().numpy().view(QUERY_STATS_DTYPE).reshape(nq)
+    rec = recall(base, queries, ids, c, kth, k)
+    # algorithmic bytes: per scanned neighbour 32 code bytes + a 4-byte id, the query,
+    # and the fp32 rows of the k x 3 re-ranked results
+    bytes_q = 36.0 * stats["edges_read"].astype(np.float64) + 512 + 512 * 3 * k
+    out = {"qps": round(nq * steps / (sum(ms) / 1e3), 1), "epsilon": eps_sel, "result_expansion": 3.0,
+           "recall_at_k": round(rec, 4), "epsilon_curve": curve,
+           "kernel": "exact-order QG kernel, one query per CTA (results equal the reference's)",
+           "quantizer": "64 subspaces x 16 centroids (2-dim subvectors), no rotation, 128 edges per node",
+           "mean_expansions": round(float(stats["expansions"].mean()), 1),
+           "mean_quantized_distances": round(float(stats["distance_computations"].mean()), 1),
+           "achieved_gbs": round(float(bytes_q.sum() / (statistics.median(ms) / 1e3) / 1e9), 1)}
+    ix.close()
     return out
 
 
@@ -467,6 +533,16 @@ def main():
         served = served_latency(ix, queries, k, head["epsilon"], args.served_rates, args.served_seconds,
                                 kernel=KERNEL_WIDE, inflight=8, max_batch=512)
 
+    # ---- quantized graph on the same index (rank 0) ---------------------------------------------
+    qg = None
+    if args.qg and rank == 0 and world == 1:
+        try:
+            qg = qg_measurement(path, base, queries, kth, k, max(3, args.steps // 3), args.warmup, log)
+            log("qg: %s" % qg)
+        except Exception as ex:                 # reported, never fatal to the headline measurement
+            qg = {"error": str(ex)}
+            log("qg measurement failed: %s" % ex)
+
     # ---- CPU baseline (oracle port on a bounded sample) ------------------------------------------
     cpu = None
     if rank == 0:
@@ -513,6 +589,7 @@ def main():
                        "recall_at_k": round(wide["recall"], 4) if wide else None,
                        "rates": served,
                        "warp_per_query_kernel_rates": served_warp} if served else None,
+            "quantized_graph": qg,
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
