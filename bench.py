@@ -41,11 +41,15 @@ sys.path.insert(0, ROOT)
 
 EPS_SWEEP = [0.0, 0.02, 0.04, 0.06, 0.07, 0.075, 0.08, 0.085, 0.09, 0.1, 0.12, 0.15, 0.2, 0.3]
 RECALL_TARGET = 0.95
-LIST_SWEEP = [128, 256]
-PARENT_SWEEP = [3, 4]
-# (rows per lane group in flight, CTAs per SM the registers are budgeted for,
-# neighbour slots per iteration; 0 = automatic).  Only the last can change results.
-VARIANT_SWEEP = [(4, 5, 0), (6, 4, 0), (4, 6, 256), (4, 5, 256)]
+# Batched-kernel candidates of the autotuner.  kernel 1: warp per query (R rows per
+# lane group in flight, registers budgeted for C CTAs per SM, NB neighbour slots per
+# step; 0 = automatic); kernel 3: CTA per query (T threads, `stage` KB of staged rows).
+BATCHED_CANDIDATES = [
+    dict(kernel=1, L=256, P=3, R=4, C=5, NB=256), dict(kernel=1, L=256, P=4, R=4, C=5, NB=0),
+    dict(kernel=1, L=256, P=4, R=6, C=4, NB=0), dict(kernel=1, L=128, P=3, R=4, C=5, NB=256),
+    dict(kernel=3, L=256, P=8, T=128, stage=16), dict(kernel=3, L=256, P=16, T=128, stage=16),
+    dict(kernel=3, L=128, P=8, T=128, stage=16), dict(kernel=3, L=256, P=8, T=128, stage=32),
+    dict(kernel=3, L=256, P=8, T=256, stage=64)]
 WIDE_PARENTS = 16                 # parents per step of the CTA-per-query kernel the serving loop uses
 # dram__bytes_read.sum + dram__bytes_write.sum of one graph_search_fast_kernel
 # launch of 2,000 queries on this workload (1M x 128, k=10, epsilon 0.08; ncu
@@ -447,7 +451,7 @@ def main():
         cnt_np = cnt.cpu().numpy().astype(np.int64)
         stats = st.cpu().numpy().view(QUERY_STATS_DTYPE).reshape(nq)
         rec = recall(base, queries, ids_np, cnt_np, kth, k)
-        srow = row_bytes // 2 if kernel in (KERNEL_BATCHED, KERNEL_WIDE) else row_bytes
+        srow = row_bytes // 2 if kernel in (1, 3) else row_bytes
         rerank = 0 if kernel == KERNEL_EXACT else 2 * k * row_bytes
         bytes_pq = (srow * stats["distance_computations"].astype(np.float64) + 4.0 * stats["edges_read"]
                     + row_bytes + rerank)
@@ -462,41 +466,50 @@ def main():
 
     runs = {}
     curves = {}
+    def apply(c):
+        ix.set_batched_tuning(list_capacity=c["L"], parents=c["P"], rows_in_flight=c.get("R", 0),
+                              ctas_per_sm=c.get("C", 0), neighbour_capacity=c.get("NB", 0),
+                              cta_threads=c.get("T", 0), stage_kilobytes=c.get("stage", 0))
+
     if args.fixed:
         ep, eb, L, P, R, C, NB = (args.fixed.split(":") + ["4", "5", "0"][len(args.fixed.split(":")) - 4:])[:7]
         curves[KERNEL_EXACT] = []
         runs[KERNEL_EXACT] = timed(KERNEL_EXACT, float(ep))
-        best = (int(L), int(P), float(eb), 0.0, [], (int(R), int(C), int(NB)))
+        best_cfg = dict(kernel=KERNEL_BATCHED, L=int(L), P=int(P), R=int(R), C=int(C), NB=int(NB))
+        best_eps, best_curve = float(eb), []
     else:
         eps, curves[KERNEL_EXACT] = calibrate(KERNEL_EXACT)
         runs[KERNEL_EXACT] = timed(KERNEL_EXACT, eps)
-        # batched kernel: the (list length, parents, rows in flight) whose recall-target
-        # epsilon runs fastest
-        best = None
-        for L in LIST_SWEEP:
-            for P in PARENT_SWEEP:
-                cal = {}
-                for V in VARIANT_SWEEP:
-                    ix.set_batched_tuning(list_capacity=L, parents=P, rows_in_flight=V[0], ctas_per_sm=V[1],
-                                          neighbour_capacity=V[2])
-                    if V[2] not in cal:                       # only the neighbour capacity changes results
-                        cal[V[2]] = calibrate(KERNEL_BATCHED)
-                    eps_l, curve_l = cal[V[2]]
-                    probe = timed(KERNEL_BATCHED, eps_l, steps=2)
-                    log("batched L=%d P=%d R=%d C=%d NB=%d: epsilon %g recall %.4f %.1f q/s"
-                        % (L, P, V[0], V[1], V[2], eps_l, probe["recall"], probe["qps"]))
-                    if probe["recall"] >= RECALL_TARGET and (best is None or probe["qps"] > best[3]):
-                        best = (L, P, eps_l, probe["qps"], curve_l, V)
-        if best is None:
-            best = (LIST_SWEEP[-1], PARENT_SWEEP[0], EPS_SWEEP[-1], 0.0, curve_l, VARIANT_SWEEP[0])
-    V = best[5]
-    ix.set_batched_tuning(list_capacity=best[0], parents=best[1], rows_in_flight=V[0], ctas_per_sm=V[1],
-                          neighbour_capacity=V[2])
-    curves[KERNEL_BATCHED] = best[4]
-    runs[KERNEL_BATCHED] = timed(KERNEL_BATCHED, best[2])
-    runs[KERNEL_BATCHED]["list_capacity"] = best[0]
-    runs[KERNEL_BATCHED]["parents"] = best[1]
-    runs[KERNEL_BATCHED]["variant"] = best[5]
+        # autotuner: every candidate at the smallest epsilon reaching the recall target
+        # (calibrated once per result-determining setting), three timed steps each; the two
+        # fastest are timed again with the full step count
+        cal, probes = {}, []
+        for c in BATCHED_CANDIDATES:
+            apply(c)
+            key = (c["kernel"], c["L"], c["P"], c.get("NB", 0))
+            if key not in cal:
+                cal[key] = calibrate(c["kernel"])
+            eps_c, curve_c = cal[key]
+            probe = timed(c["kernel"], eps_c, steps=3)
+            log("candidate %s: epsilon %g recall %.4f %.1f q/s" % (c, eps_c, probe["recall"], probe["qps"]))
+            if probe["recall"] >= RECALL_TARGET:
+                probes.append((probe["qps"], c, eps_c, curve_c))
+        probes.sort(key=lambda t: -t[0])
+        finals = []
+        for qps, c, eps_c, curve_c in probes[:2]:
+            apply(c)
+            r = timed(c["kernel"], eps_c)
+            log("final %s: %.1f q/s" % (c, r["qps"]))
+            finals.append((r["qps"], c, eps_c, curve_c))
+        finals.sort(key=lambda t: -t[0])
+        if finals:
+            _, best_cfg, best_eps, best_curve = finals[0]
+        else:
+            best_cfg, best_eps, best_curve = BATCHED_CANDIDATES[0], EPS_SWEEP[-1], []
+    apply(best_cfg)
+    curves[KERNEL_BATCHED] = best_curve
+    runs[KERNEL_BATCHED] = timed(best_cfg["kernel"], best_eps)
+    runs[KERNEL_BATCHED]["config"] = best_cfg
     for kernel in (KERNEL_EXACT, KERNEL_BATCHED):
         log("kernel %d: %.1f q/s at epsilon %g, recall %.4f, %.1f GB/s"
             % (kernel, runs[kernel]["qps"], runs[kernel]["epsilon"], runs[kernel]["recall"],
@@ -513,7 +526,7 @@ def main():
     e2e_times = []
     for i in range(args.warmup + args.steps):
         t1 = time.time()
-        ix.batch_search(hq, k=k, epsilon=head["epsilon"], kernel=KERNEL_BATCHED)
+        ix.batch_search(hq, k=k, epsilon=head["epsilon"], kernel=head["config"]["kernel"])
         if i >= args.warmup:
             e2e_times.append(time.time() - t1)
     e2e_qps = world * nq * len(e2e_times) / sum(e2e_times)
@@ -556,11 +569,11 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32-rerank", "data": "synthetic",
             "config": {"workload": "graph search, %d x %d float32 L2 ONNG, %d queries per step, k=%d"
                                    % (args.n, args.dim, nq, k),
-                       "headline": "batched kernel (warp per query, bf16 rows, exact fp32 re-rank), epsilon=%g, "
-                                   "candidate list %d, %d parents per step, %d rows in flight per lane group, "
-                                   "registers for %d CTAs/SM, neighbour slots %s"
-                                   % (head["epsilon"], head["list_capacity"], head["parents"],
-                                      head["variant"][0], head["variant"][1], head["variant"][2] or "auto"),
+                       "headline": ("batched kernel (%s, bf16 rows, exact fp32 re-rank), epsilon=%g, "
+                                    "autotuned settings %s"
+                                    % ("warp per query" if head["config"]["kernel"] == KERNEL_BATCHED
+                                       else "CTA per query, rows of a step staged in shared memory",
+                                       head["epsilon"], json.dumps(head["config"], sort_keys=True))),
                        "recall_at_k": round(head["recall"], 4), "epsilon_curve": curves[KERNEL_BATCHED],
                        "plain_fp32": {"qps": round(plain["qps"], 1), "epsilon": plain["epsilon"],
                                       "recall_at_k": round(plain["recall"], 4),
