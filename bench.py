@@ -270,10 +270,10 @@ def qg_measurement(path, base, queries, kth, k, steps, warmup, log_fn):
     st = torch.zeros((nq, QUERY_STATS_DTYPE.itemsize // 4), dtype=torch.int32, device="cuda")
     stream = torch.cuda.Stream()
 
-    def run(eps, exp, nsteps, n):
+    def run(eps, exp, nsteps, n, warm):
         p = QGQueryParameters(k, eps, exp, -1.0)
         with torch.cuda.stream(stream):
-            for _ in range(warmup):
+            for _ in range(warm):
                 ix.search_device(rows.data_ptr(), n, p, res.data_ptr(), k, cnt.data_ptr(), st.data_ptr(),
                                  stream.cuda_stream)
         torch.cuda.synchronize()
@@ -295,7 +295,7 @@ def qg_measurement(path, base, queries, kth, k, steps, warmup, log_fn):
     best, curve = None, []
     for exp in QG_EXPANSIONS:
         for eps in QG_EPS_SWEEP:
-            qps, r, _, _ = run(eps, exp, 1, cal)
+            qps, r, _, _ = run(eps, exp, 1, cal, 1)
             curve.append((exp, eps, round(r, 4), round(qps, 1)))
             log_fn("qg expansion %.0f epsilon %.2f recall@%d %.4f %.1f q/s" % (exp, eps, k, r, qps))
             if r >= RECALL_TARGET:
@@ -305,7 +305,7 @@ def qg_measurement(path, base, queries, kth, k, steps, warmup, log_fn):
     if best is None:
         best = (0.0, QG_EPS_SWEEP[-1], QG_EXPANSIONS[-1])
     _, eps_sel, exp_sel = best
-    qps, rec, stats, ms = run(eps_sel, exp_sel, steps, nq)
+    qps, rec, stats, ms = run(eps_sel, exp_sel, steps, nq, warmup)
     # algorithmic bytes: per scanned neighbour 64 code bytes + a 4-byte id, the query,
     # and the fp32 rows of the re-ranked results
     bytes_q = 68.0 * stats["edges_read"].astype(np.float64) + 512 + 512 * exp_sel * k
