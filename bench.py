@@ -51,12 +51,12 @@ BATCHED_CANDIDATES = [
     dict(kernel=3, L=128, P=8, T=128, stage=16), dict(kernel=3, L=256, P=8, T=128, stage=32),
     dict(kernel=3, L=256, P=8, T=256, stage=64)]
 WIDE_PARENTS = 16                 # parents per step of the CTA-per-query kernel the serving loop uses
-# dram__bytes_read.sum + dram__bytes_write.sum of one graph_search_fast_kernel
-# launch of 2,000 queries on this workload (1M x 128, k=10, epsilon 0.08; ncu
-# capture summarised under profiles/), per query.  Scaled by the queries of one
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of 2,000 queries on
+# this workload (1M x 128, k=10, epsilon 0.08; ncu captures summarised under
+# profiles/), per query, for each batched kernel.  Scaled by the queries of one
 # launch to give roofline.traffic; the workload's DC per query is the same at
 # every batch size.
-FAST_KERNEL_DRAM_BYTES_PER_QUERY = 10.56e9 / 2000
+DRAM_BYTES_PER_QUERY = {1: 10.56e9 / 2000}      # batched kernel id -> measured bytes per query
 
 
 def log(*a):
@@ -80,7 +80,9 @@ def parse():
     ap.add_argument("--served-seconds", type=float, default=2.0, help="length of each served-rate run")
     ap.add_argument("--qg", type=int, default=1, help="also measure the quantized-graph search (1) or not (0)")
     ap.add_argument("--fixed", default=None,
-                    help="EPS_PLAIN:EPS_BATCHED:LIST:PARENTS[:ROWS:CTAS:NBR] -- skip the epsilon / tuning sweeps")
+                    help="EPS_PLAIN:EPS_BATCHED -- skip the epsilon / tuning sweeps (profiling runs)")
+    ap.add_argument("--fixed-config", default='{"kernel": 3, "L": 256, "P": 8, "T": 128, "stage": 16}',
+                    help="batched-kernel settings (JSON) used with --fixed")
     return ap.parse_args()
 
 
@@ -481,10 +483,10 @@ def main():
                               cta_threads=c.get("T", 0), stage_kilobytes=c.get("stage", 0))
 
     if args.fixed:
-        ep, eb, L, P, R, C, NB = (args.fixed.split(":") + ["4", "5", "0"][len(args.fixed.split(":")) - 4:])[:7]
+        ep, eb = args.fixed.split(":")[:2]
         curves[KERNEL_EXACT] = []
         runs[KERNEL_EXACT] = timed(KERNEL_EXACT, float(ep))
-        best_cfg = dict(kernel=KERNEL_BATCHED, L=int(L), P=int(P), R=int(R), C=int(C), NB=int(NB))
+        best_cfg = json.loads(args.fixed_config)
         best_eps, best_curve = float(eb), []
     else:
         eps, curves[KERNEL_EXACT] = calibrate(KERNEL_EXACT)
@@ -598,8 +600,9 @@ def main():
                        "status_bits": head["status"]},
             "roofline": {"bound": "hbm", "achieved": round(head["achieved_gbs"], 1), "peak": peak, "unit": "GB/s",
                          "frac": round(head["achieved_gbs"] / peak, 4),
-                         "traffic": (round(FAST_KERNEL_DRAM_BYTES_PER_QUERY * nq / 1e9, 3)
-                                     if (args.n, args.dim, k) == (1_000_000, 128, 10) else None),
+                         "traffic": (round(DRAM_BYTES_PER_QUERY[head["config"]["kernel"]] * nq / 1e9, 3)
+                                     if (args.n, args.dim, k) == (1_000_000, 128, 10)
+                                     and head["config"]["kernel"] in DRAM_BYTES_PER_QUERY else None),
                          "traffic_unit": "GB per launch (ncu dram bytes per query x queries)",
                          "peak_source": peak_kind,
                          "basis": "(%d*DC + 4*edges + %d query + re-rank %d*2k) bytes per query over the kernel's "
