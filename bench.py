@@ -47,8 +47,8 @@ RECALL_TARGET = 0.95
 BATCHED_CANDIDATES = [
     dict(kernel=1, L=256, P=3, R=4, C=5, NB=256), dict(kernel=1, L=256, P=4, R=4, C=5, NB=0),
     dict(kernel=1, L=256, P=4, R=6, C=4, NB=0), dict(kernel=1, L=128, P=3, R=4, C=5, NB=256),
-    dict(kernel=3, L=256, P=8, T=128, stage=16), dict(kernel=3, L=256, P=16, T=128, stage=16),
-    dict(kernel=3, L=128, P=8, T=128, stage=16), dict(kernel=3, L=256, P=8, T=128, stage=32),
+    dict(kernel=3, L=256, P=8, T=128, stage=16), dict(kernel=3, L=256, P=8, T=128, stage=32),
+    dict(kernel=3, L=128, P=8, T=128, stage=32), dict(kernel=3, L=256, P=16, T=128, stage=32),
     dict(kernel=3, L=256, P=8, T=256, stage=64)]
 WIDE_PARENTS = 16                 # parents per step of the CTA-per-query kernel the serving loop uses
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of 2,000 queries on

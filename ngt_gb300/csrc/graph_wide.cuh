@@ -138,20 +138,33 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
   const int sgl = lane & (SG - 1), ngl = lane & (NG - 1);
 
   // distances of nid[0..cnt) into nd[], rows staged through shared memory
+  // distances of nid[0..cnt) into nd[]: rows staged through shared memory in two
+  // halves, the next half's copies in flight while the current half is scored
+  const uint32_t SRH = SR / 2;
+  auto issue = [&](uint32_t r0, uint32_t nr, uint4* buf) {
+    for (uint32_t idx = tid; idx < nr * sc; idx += blockDim.x) {
+      const uint32_t i = idx / sc, c = idx - i * sc;
+      cp_async16(buf + idx, srows + (size_t)nid[r0 + i] * sc + c);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
   auto score = [&](uint32_t cnt) {
-    for (uint32_t r0 = 0; r0 < cnt; r0 += SR) {
-      const uint32_t nr = min(SR, cnt - r0);
-      for (uint32_t idx = tid; idx < nr * sc; idx += blockDim.x) {
-        const uint32_t i = idx / sc, c = idx - i * sc;
-        cp_async16(stage + idx, srows + (size_t)nid[r0 + i] * sc + c);
-      }
-      cp_async_wait_all();
+    if (cnt == 0) return;
+    uint4* buf[2] = {stage, stage + (size_t)SRH * sc};
+    issue(0, min(SRH, cnt), buf[0]);
+    if (cnt > SRH) issue(SRH, min(SRH, cnt - SRH), buf[1]);
+    uint32_t h = 0;
+    for (uint32_t r0 = 0; r0 < cnt; r0 += SRH, h ^= 1u) {
+      const uint32_t nr = min(SRH, cnt - r0);
+      if (r0 + SRH < cnt) asm volatile("cp.async.wait_group 1;\n" ::: "memory");   // this half landed
+      else asm volatile("cp.async.wait_group 0;\n" ::: "memory");
       __syncthreads();
+      const uint4* stg = buf[h];
       const uint32_t gpb = (uint32_t)T / SG;
       for (uint32_t b = 0; b < nr; b += gpb) {          // uniform trip count per warp
         const uint32_t i = b + (uint32_t)(tid / SG);
         const bool valid = i < nr;
-        const uint4* row = stage + (size_t)(valid ? i : 0u) * sc;
+        const uint4* row = stg + (size_t)(valid ? i : 0u) * sc;
         float d;
         if constexpr (PackedL2<ST, M>::kOn) {
           float2 acc = make_float2(0.f, 0.f);
@@ -173,7 +186,8 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
         }
         if (valid && sgl == 0) nd[r0 + i] = d;
       }
-      __syncthreads();
+      __syncthreads();                                   // the half is free again
+      if (r0 + 2 * SRH < cnt) issue(r0 + 2 * SRH, min(SRH, cnt - (r0 + 2 * SRH)), buf[h]);
     }
   };
 
@@ -405,26 +419,55 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       __syncthreads();              // everyone has read the decision before warp 0 writes the next one
       if (done) break;
       if (refill_next) continue;
-      // ---- gather: unvisited neighbours of the parents, in edge order -----------------
+      // ---- gather: unvisited neighbours of the parents ----------------------------------
+      // Every thread takes up to kGatherSlots edge slots (t = base + j*T + tid): all
+      // edge loads, then all visited-bit atomics, then one CTA scan of the per-thread
+      // counts places the new ids (their order does not matter to this search).
+      constexpr int kGatherSlots = 8;
       uint32_t cnt = 0;
-      for (uint32_t base0 = 0; base0 < total; base0 += blockDim.x) {
-        const uint32_t t = base0 + tid;
-        uint32_t id = 0;
-        bool fresh = false;
-        if (t < total) {
-          uint32_t p2 = 0;
-          for (uint32_t c = 1; c < np; c++)
-            if (t >= s.pexcl[c]) p2 = c;
-          id = __ldg(g.edges + s.pbase[p2] + (t - s.pexcl[p2]));
-          const uint32_t bit = 1u << (id & 31u);
-          fresh = (atomicOr(&bitmap[id >> 5], bit) & bit) == 0u;
+      for (uint32_t base0 = 0; base0 < total; base0 += kGatherSlots * (uint32_t)T) {
+        uint32_t ids[kGatherSlots];
+        uint32_t fm = 0, p2 = 0;
+#pragma unroll
+        for (int j = 0; j < kGatherSlots; j++) {
+          const uint32_t t = base0 + (uint32_t)j * (uint32_t)T + (uint32_t)tid;
+          ids[j] = 0;
+          if (t < total) {
+            while (p2 + 1 < np && t >= s.pexcl[p2 + 1]) p2++;       // slots increase with j
+            ids[j] = __ldg(g.edges + s.pbase[p2] + (t - s.pexcl[p2]));
+          }
         }
-        uint32_t rt;
-        const uint32_t pos = cta_compact(fresh, s.wcnt, &rt);
-        if (fresh) nid[cnt + pos] = id;
-        cnt += rt;
+#pragma unroll
+        for (int j = 0; j < kGatherSlots; j++) {
+          const uint32_t t = base0 + (uint32_t)j * (uint32_t)T + (uint32_t)tid;
+          if (t < total) {
+            const uint32_t bit = 1u << (ids[j] & 31u);
+            if ((atomicOr(&bitmap[ids[j] >> 5], bit) & bit) == 0u) fm |= 1u << j;
+          }
+        }
+        // CTA exclusive scan of the per-thread counts
+        const uint32_t c = (uint32_t)__popc(fm);
+        uint32_t incl = c;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          uint32_t v = __shfl_up_sync(0xffffffffu, incl, off);
+          if (lane >= off) incl += v;
+        }
+        if (lane == 31) s.wcnt[warp] = incl;
+        __syncthreads();
+        uint32_t wbase = 0, tot = 0;
+        for (int w = 0; w < T / 32; w++) {
+          const uint32_t x = s.wcnt[w];
+          if (w < warp) wbase += x;
+          tot += x;
+        }
+        uint32_t pos = cnt + wbase + incl - c;
+#pragma unroll
+        for (int j = 0; j < kGatherSlots; j++)
+          if (fm & (1u << j)) nid[pos++] = ids[j];
+        cnt += tot;
+        __syncthreads();
       }
-      __syncthreads();
       if (tid == 0) { s.dc += cnt; s.visited += cnt; }
       // ---- distances ------------------------------------------------------------------------
       score(cnt);
