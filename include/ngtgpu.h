@@ -77,7 +77,10 @@ bool ngtgpu_set_batched_rows_in_flight(NGTIndex, uint32_t rows, NGTError);
  * (6, 4), (8, 4), (6, 5), (4, 6), (2, 8) for float L2 indexes; a search with a
  * pair that is not built fails with an error.  neighbour_capacity bounds the
  * neighbour slots of one iteration (each parent reads at most
- * neighbour_capacity / parents edges) and sets the shared memory per query. */
+ * neighbour_capacity / parents edges) and sets the shared memory per query.
+ * parents: at most 32 (the warp-per-query kernel uses at most 16 of them).
+ * NGTGPU_KERNEL_WIDE reads rows_in_flight as the rows each lane group scores at
+ * once from shared memory (1, 2 or 4; default 4). */
 typedef struct {
   uint32_t list_capacity;
   uint32_t parents;
@@ -87,6 +90,8 @@ typedef struct {
   uint32_t neighbour_capacity;
   uint32_t cta_threads;        /* NGTGPU_KERNEL_WIDE: 128 or 256 threads per query (float L2: both) */
   uint32_t stage_kilobytes;    /* NGTGPU_KERNEL_WIDE: shared memory for staged rows (default 64) */
+  uint32_t l2_policy;          /* NGTGPU_KERNEL_WIDE: 1 plain caching, 2 visited bitmaps kept in L2,
+                                  3 (default) as 2 and staged rows streamed through L2 (evict-first) */
 } NGTGPUBatchedTuning;
 bool ngtgpu_set_batched_tuning_ex(NGTIndex, const NGTGPUBatchedTuning *tuning, NGTError);
 

@@ -71,7 +71,7 @@ class BatchedTuning(ctypes.Structure):
     """NGTGPUBatchedTuning (include/ngtgpu.h)."""
     _fields_ = [("list_capacity", c_uint32), ("parents", c_uint32), ("rerank_factor", c_float),
                 ("rows_in_flight", c_uint32), ("ctas_per_sm", c_uint32), ("neighbour_capacity", c_uint32),
-                ("cta_threads", c_uint32), ("stage_kilobytes", c_uint32)]
+                ("cta_threads", c_uint32), ("stage_kilobytes", c_uint32), ("l2_policy", c_uint32)]
 
 
 class QueryStats(ctypes.Structure):
@@ -270,9 +270,9 @@ class Index:
 
     def set_batched_tuning(self, list_capacity: int = 0, parents: int = 0, rerank_factor: float = 0.0,
                            rows_in_flight: int = 0, ctas_per_sm: int = 0, neighbour_capacity: int = 0,
-                           cta_threads: int = 0, stage_kilobytes: int = 0):
+                           cta_threads: int = 0, stage_kilobytes: int = 0, l2_policy: int = 0):
         t = BatchedTuning(list_capacity, parents, rerank_factor, rows_in_flight, ctas_per_sm, neighbour_capacity,
-                          cta_threads, stage_kilobytes)
+                          cta_threads, stage_kilobytes, l2_policy)
         self._check(self._lib.ngtgpu_set_batched_tuning_ex(self._index, ctypes.byref(t), self._err))
 
     def kernel_launches(self) -> int:

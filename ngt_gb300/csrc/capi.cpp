@@ -450,12 +450,12 @@ bool ngtgpu_set_batched_rows_in_flight(NGTIndex index, uint32_t rows, NGTError e
 }
 
 bool ngtgpu_set_batched_tuning_ex(NGTIndex index, const NGTGPUBatchedTuning* tuning, NGTError error) {
-  if (index == nullptr || tuning == nullptr || tuning->list_capacity > 1024 || tuning->parents > 16 ||
+  if (index == nullptr || tuning == nullptr || tuning->list_capacity > 1024 || tuning->parents > 32 ||
       tuning->rerank_factor < 0.f || tuning->neighbour_capacity > 4096 ||
-      !(tuning->rows_in_flight == 0 || tuning->rows_in_flight == 2 || tuning->rows_in_flight == 4 ||
+      !(tuning->rows_in_flight <= 2 || tuning->rows_in_flight == 4 ||
         tuning->rows_in_flight == 6 || tuning->rows_in_flight == 8) ||
       tuning->ctas_per_sm > 8 || !(tuning->cta_threads == 0 || tuning->cta_threads == 128 ||
-                                   tuning->cta_threads == 256) || tuning->stage_kilobytes > 200) {
+                                   tuning->cta_threads == 256) || tuning->stage_kilobytes > 200 || tuning->l2_policy > 3) {
     CAPI_PARAM_ERROR(error, "index = " << index << " tuning = " << tuning);
     return false;
   }
@@ -468,6 +468,7 @@ bool ngtgpu_set_batched_tuning_ex(NGTIndex index, const NGTGPUBatchedTuning* tun
   t.nbr_cap = tuning->neighbour_capacity;
   t.cta_threads = tuning->cta_threads;
   t.stage_kb = tuning->stage_kilobytes;
+  t.l2_policy = tuning->l2_policy;
   engine(index)->set_tuning(t);
   return true;
 }

@@ -578,6 +578,10 @@ void GraphEngine::launch_wide(const uint4* d_rows, size_t nq, const QueryParams*
   cfg.bitmap_words = ((host_.nrows + 31) / 32 + 3) / 4 * 4;
   cfg.max_iters = 1u << 22;
   cfg.spill_cap = kSpillCapacity;
+  // default: visited bitmaps kept in L2, staged rows streamed through it
+  cfg.l2_policy = tuning_.l2_policy ? tuning_.l2_policy - 1 : 2u;
+  // rows_in_flight: rows per lane group scored at once (1, 2 or 4; default 4)
+  cfg.score_rows = tuning_.rows_in_flight ? std::min<uint32_t>(tuning_.rows_in_flight, 4) : 4u;
   size_t smem = wide_kernel_smem_bytes(dev_.row_chunks, cfg);
   int max_smem = 0, per_sm = 0, sms = 0;
   NGT_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
@@ -594,8 +598,7 @@ void GraphEngine::launch_wide(const uint4* d_rows, size_t nq, const QueryParams*
   NGT_CUDA(cudaMemsetAsync(scratch.work, 0, 4, stream));
   const uint4* srows = bf16 ? static_cast<const uint4*>(d_bf16_) : dev_.objects;
   fn<<<(unsigned)grid, threads, smem, stream>>>(dev_, srows, d_rows, (uint32_t)nq, d_params, d_seeds, d_out,
-                                                      d_counts, d_stats, scratch.bitmaps, scratch.work,
-                                                      scratch.spill, cfg);
+                                                d_counts, d_stats, scratch.bitmaps, scratch.work, scratch.spill, cfg);
   NGT_CUDA(cudaGetLastError());
   launches_++;
 }

@@ -42,6 +42,7 @@ struct FastTuning {
   uint32_t nbr_cap = 0;        // neighbour slots per iteration (power of two >= 256)
   uint32_t cta_threads = 0;    // wide kernel: threads per CTA (128 or 256)
   uint32_t stage_kb = 0;       // wide kernel: shared memory for staged rows (KB)
+  uint32_t l2_policy = 0;      // wide kernel: 0 automatic, else WideConfig::l2_policy + 1
 };
 
 // Parameters of one quantized-graph query (NGTQGQueryParameters,

@@ -17,6 +17,7 @@
 #pragma once
 #include <cuda_bf16.h>
 #include <cfloat>
+#include <type_traits>
 #include "distance.cuh"
 #include "device_index.h"
 #include "graph_fast.cuh"
@@ -38,6 +39,9 @@ struct WideConfig {
   uint32_t bitmap_words;   // per CTA, multiple of 4
   uint32_t max_iters;
   uint32_t spill_cap;
+  uint32_t l2_policy;      // 0: default caching; 1: visited bitmap kept in L2 (evict_last);
+                           // 2: as 1, and staged rows streamed through L2 (evict_first)
+  uint32_t score_rows;     // rows per lane group scored at once (1, 2 or 4)
 };
 
 struct WideShared {
@@ -62,6 +66,34 @@ inline size_t wide_smem_bytes(uint32_t row_chunks, const WideConfig& c) {
 __device__ __forceinline__ void cp_async16(void* smem_dst, const void* gmem_src) {
   const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
   asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gmem_src) : "memory");
+}
+__device__ __forceinline__ void cp_async16_hint(void* smem_dst, const void* gmem_src, uint64_t policy) {
+  const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gmem_src), "l"(policy)
+               : "memory");
+}
+// atomicOr on a visited-bitmap word, with an L2 eviction-priority hint when `hint`
+__device__ __forceinline__ uint32_t visit_or(uint32_t* word, uint32_t bit, bool hint, uint64_t policy) {
+  if (!hint) return atomicOr(word, bit);
+  uint32_t old;
+  asm volatile("atom.global.or.L2::cache_hint.b32 %0, [%1], %2, %3;\n"
+               : "=r"(old) : "l"(word), "r"(bit), "l"(policy) : "memory");
+  return old;
+}
+__device__ __forceinline__ void store_zero16(uint4* p, bool hint, uint64_t policy) {
+  if (!hint) { *p = make_uint4(0, 0, 0, 0); return; }
+  asm volatile("st.global.L2::cache_hint.v4.u32 [%0], {%1, %1, %1, %1}, %2;\n" ::"l"(p), "r"(0u), "l"(policy)
+               : "memory");
+}
+__device__ __forceinline__ uint64_t l2_policy_evict_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_evict_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
 }
 __device__ __forceinline__ void cp_async_wait_all() {
   asm volatile("cp.async.commit_group;\n" ::: "memory");
@@ -113,7 +145,7 @@ __device__ __forceinline__ uint32_t cta_compact(bool flag, uint32_t* wcnt, uint3
 
 // T: threads per CTA (128 or 256), one query per CTA.
 template <ObjType ST, ObjType OT, Metric M, int T>
-__global__ void __launch_bounds__(T, 1)
+__global__ void __launch_bounds__(T, T == 128 ? 5 : 2)
 graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint4* __restrict__ queries,
                          uint32_t nq, const QueryParams* __restrict__ params, const uint32_t* __restrict__ seed_list,
                          ObjDist* __restrict__ out, uint32_t* __restrict__ out_count, QueryStats* __restrict__ stats,
@@ -136,55 +168,135 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
   unsigned long long* spill_tmp = spill + cfg.spill_cap;
   const int SG = (int)cfg.sgroup, NG = (int)cfg.ngroup;
   const int sgl = lane & (SG - 1), ngl = lane & (NG - 1);
+  const bool keep_visited = cfg.l2_policy >= 1, stream_rows = cfg.l2_policy >= 2;
+  const uint64_t pol_keep = keep_visited ? l2_policy_evict_last() : 0ull;
+  const uint64_t pol_stream = stream_rows ? l2_policy_evict_first() : 0ull;
 
   // distances of nid[0..cnt) into nd[], rows staged through shared memory
   // distances of nid[0..cnt) into nd[]: rows staged through shared memory in two
   // halves, the next half's copies in flight while the current half is scored
   const uint32_t SRH = SR / 2;
+  // each thread copies chunk (tid % sc) of every (T / sc)-th row when sc divides T
+  const bool rows_split = ((uint32_t)T % sc) == 0;
+  const uint32_t my_chunk = (uint32_t)tid % sc, my_row = (uint32_t)tid / sc, row_step = (uint32_t)T / sc;
   auto issue = [&](uint32_t r0, uint32_t nr, uint4* buf) {
-    for (uint32_t idx = tid; idx < nr * sc; idx += blockDim.x) {
-      const uint32_t i = idx / sc, c = idx - i * sc;
-      cp_async16(buf + idx, srows + (size_t)nid[r0 + i] * sc + c);
+    if (rows_split) {
+      if (stream_rows) {
+        for (uint32_t i = my_row; i < nr; i += row_step)
+          cp_async16_hint(buf + (size_t)i * sc + my_chunk, srows + (size_t)nid[r0 + i] * sc + my_chunk, pol_stream);
+      } else {
+        for (uint32_t i = my_row; i < nr; i += row_step)
+          cp_async16(buf + (size_t)i * sc + my_chunk, srows + (size_t)nid[r0 + i] * sc + my_chunk);
+      }
+    } else {
+      for (uint32_t idx = tid; idx < nr * sc; idx += blockDim.x) {
+        const uint32_t i = idx / sc, c = idx - i * sc;
+        cp_async16(buf + idx, srows + (size_t)nid[r0 + i] * sc + c);
+      }
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
   };
   auto score = [&](uint32_t cnt) {
     if (cnt == 0) return;
+    // the query chunks this lane reads (c = sgl + j * SG), negated and unpacked once
+    constexpr int kQC = 2;   // the host sets sgroup so that every lane reads at most two chunks
+    float2 nqc[kQC][PackedL2<ST, M>::P / 2];
+    if constexpr (PackedL2<ST, M>::kOn) {
+#pragma unroll
+      for (int j = 0; j < kQC; j++) {
+        const uint32_t c = (uint32_t)sgl + (uint32_t)(j * SG);
+        PackedL2<ST, M>::prepare(c < sc ? qs[c] : make_uint4(0, 0, 0, 0), nqc[j]);
+      }
+    }
     uint4* buf[2] = {stage, stage + (size_t)SRH * sc};
     issue(0, min(SRH, cnt), buf[0]);
     if (cnt > SRH) issue(SRH, min(SRH, cnt - SRH), buf[1]);
     uint32_t h = 0;
     for (uint32_t r0 = 0; r0 < cnt; r0 += SRH, h ^= 1u) {
       const uint32_t nr = min(SRH, cnt - r0);
-      if (r0 + SRH < cnt) asm volatile("cp.async.wait_group 1;\n" ::: "memory");   // this half landed
-      else asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+      if (r0 + SRH < cnt) {
+        asm volatile("cp.async.wait_group 1;\n" ::: "memory");   // this half landed
+      } else {
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+      }
       __syncthreads();
       const uint4* stg = buf[h];
       const uint32_t gpb = (uint32_t)T / SG;
-      for (uint32_t b = 0; b < nr; b += gpb) {          // uniform trip count per warp
-        const uint32_t i = b + (uint32_t)(tid / SG);
-        const bool valid = i < nr;
-        const uint4* row = stg + (size_t)(valid ? i : 0u) * sc;
-        float d;
-        if constexpr (PackedL2<ST, M>::kOn) {
-          float2 acc = make_float2(0.f, 0.f);
-          for (uint32_t c = (uint32_t)sgl; c < sc; c += (uint32_t)SG) {
-            float2 nq[PackedL2<ST, M>::P / 2];
-            PackedL2<ST, M>::prepare(qs[c], nq);
-            acc = PackedL2<ST, M>::add(acc, nq, row[c]);
-          }
-          float v = acc.x + acc.y;
+      const uint32_t gi = (uint32_t)(tid / SG);
+      if (PackedL2<ST, M>::kOn && sc <= (uint32_t)(kQC * SG)) {
+        // KR rows per lane group at once: their shared-memory loads first, then 2 x KR
+        // independent accumulations (one per chunk) and interleaved shuffle reductions
+        auto rows_at_once = [&](auto kr_tag) {
+          constexpr int KR = decltype(kr_tag)::value;
+          for (uint32_t b = 0; b < nr; b += gpb * KR) {    // uniform trip count per warp
+            uint4 x[KR][kQC];
 #pragma unroll
-          for (int off = 16; off > 0; off >>= 1)
-            if (off < SG) v += __shfl_xor_sync(0xffffffffu, v, off);
-          d = sqrtf(v);
-        } else {
-          Acc<ST, M> acc;
-          for (uint32_t c = (uint32_t)sgl; c < sc; c += (uint32_t)SG) acc.add(qs[c], row[c], (int)c);
-          acc.reduce(SG);
-          d = acc.finish();
+            for (int u = 0; u < KR; u++) {
+              const uint32_t i = b + (uint32_t)u * gpb + gi;
+              const uint4* row = stg + (size_t)(i < nr ? i : 0u) * sc;
+#pragma unroll
+              for (int j = 0; j < kQC; j++) {
+                const uint32_t c = (uint32_t)sgl + (uint32_t)(j * SG);
+                x[u][j] = c < sc ? row[c] : make_uint4(0, 0, 0, 0);
+              }
+            }
+            float v[KR];
+#pragma unroll
+            for (int u = 0; u < KR; u++) {
+              float2 acc[kQC];
+#pragma unroll
+              for (int j = 0; j < kQC; j++) {
+                acc[j] = make_float2(0.f, 0.f);
+                if ((uint32_t)sgl + (uint32_t)(j * SG) < sc) acc[j] = PackedL2<ST, M>::add(acc[j], nqc[j], x[u][j]);
+              }
+              float t = acc[0].x + acc[0].y;
+#pragma unroll
+              for (int j = 1; j < kQC; j++) t += acc[j].x + acc[j].y;
+              v[u] = t;
+            }
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1)
+              if (off < SG) {
+#pragma unroll
+                for (int u = 0; u < KR; u++) v[u] += __shfl_xor_sync(0xffffffffu, v[u], off);
+              }
+#pragma unroll
+            for (int u = 0; u < KR; u++) {
+              const uint32_t i = b + (uint32_t)u * gpb + gi;
+              if (i < nr && sgl == 0) nd[r0 + i] = sqrtf(v[u]);
+            }
+          }
+        };
+        const uint32_t kr = min(cfg.score_rows, (nr + gpb - 1) / gpb);   // uniform
+        if (kr >= 4) rows_at_once(std::integral_constant<int, 4>{});
+        else if (kr >= 2) rows_at_once(std::integral_constant<int, 2>{});
+        else rows_at_once(std::integral_constant<int, 1>{});
+      } else {
+        for (uint32_t b = 0; b < nr; b += gpb) {          // uniform trip count per warp
+          const uint32_t i = b + gi;
+          const bool valid = i < nr;
+          const uint4* row = stg + (size_t)(valid ? i : 0u) * sc;
+          float d;
+          if constexpr (PackedL2<ST, M>::kOn) {
+            float2 acc = make_float2(0.f, 0.f);
+            for (uint32_t c = (uint32_t)sgl; c < sc; c += (uint32_t)SG) {
+              float2 nq[PackedL2<ST, M>::P / 2];
+              PackedL2<ST, M>::prepare(qs[c], nq);
+              acc = PackedL2<ST, M>::add(acc, nq, row[c]);
+            }
+            float v = acc.x + acc.y;
+#pragma unroll
+            for (int off = 16; off > 0; off >>= 1)
+              if (off < SG) v += __shfl_xor_sync(0xffffffffu, v, off);
+            d = sqrtf(v);
+          } else {
+            Acc<ST, M> acc;
+            for (uint32_t c = (uint32_t)sgl; c < sc; c += (uint32_t)SG) acc.add(qs[c], row[c], (int)c);
+            acc.reduce(SG);
+            d = acc.finish();
+          }
+          if (valid && sgl == 0) nd[r0 + i] = d;
         }
-        if (valid && sgl == 0) nd[r0 + i] = d;
       }
       __syncthreads();                                   // the half is free again
       if (r0 + 2 * SRH < cnt) issue(r0 + 2 * SRH, min(SRH, cnt - (r0 + 2 * SRH)), buf[h]);
@@ -261,7 +373,7 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
           id = seeds[i];
           if (id < g.nrows) {
             uint32_t bit = 1u << (id & 31u);
-            fresh = (atomicOr(&bitmap[id >> 5], bit) & bit) == 0u;
+            fresh = (visit_or(&bitmap[id >> 5], bit, keep_visited, pol_keep) & bit) == 0u;
           }
         }
         unsigned bal = __ballot_sync(0xffffffffu, fresh);
@@ -442,7 +554,7 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
           const uint32_t t = base0 + (uint32_t)j * (uint32_t)T + (uint32_t)tid;
           if (t < total) {
             const uint32_t bit = 1u << (ids[j] & 31u);
-            if ((atomicOr(&bitmap[ids[j] >> 5], bit) & bit) == 0u) fm |= 1u << j;
+            if ((visit_or(&bitmap[ids[j] >> 5], bit, keep_visited, pol_keep) & bit) == 0u) fm |= 1u << j;
           }
         }
         // CTA exclusive scan of the per-thread counts
@@ -585,7 +697,7 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       }
     }
     uint4* bm4 = reinterpret_cast<uint4*>(bitmap);
-    for (uint32_t i = tid; i < cfg.bitmap_words / 4; i += blockDim.x) bm4[i] = make_uint4(0, 0, 0, 0);
+    for (uint32_t i = tid; i < cfg.bitmap_words / 4; i += blockDim.x) store_zero16(bm4 + i, keep_visited, pol_keep);
     __syncthreads();
   }
 }
