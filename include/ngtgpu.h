@@ -92,6 +92,8 @@ typedef struct {
   uint32_t stage_kilobytes;    /* NGTGPU_KERNEL_WIDE: shared memory for staged rows (default 64) */
   uint32_t l2_policy;          /* NGTGPU_KERNEL_WIDE: 1 plain caching, 2 visited bitmaps kept in L2,
                                   3 (default) as 2 and staged rows streamed through L2 (evict-first) */
+  uint32_t search_rows;        /* NGTGPU_KERNEL_WIDE, float L2 objects: 0 automatic (8-bit codes when they
+                                  are lossless, else bf16), 1 bf16, 2 8-bit codes */
 } NGTGPUBatchedTuning;
 bool ngtgpu_set_batched_tuning_ex(NGTIndex, const NGTGPUBatchedTuning *tuning, NGTError);
 
@@ -139,6 +141,12 @@ void ngtgpu_server_destroy(NGTGPUServer);
 
 /* Number of kernel launches issued by this index since it was opened. */
 uint64_t ngtgpu_kernel_launches(NGTIndex, NGTError);
+
+/* Search rows NGTGPU_KERNEL_WIDE uses for this index under its tuning: 0 the
+ * objects themselves, 1 bf16 copies, 2 8-bit codes rint((x - min) / s) with s = 1
+ * when every coordinate is an integer and they span at most 256 values (the
+ * codes are then lossless), else (max - min) / 255.  UINT32_MAX on error. */
+uint32_t ngtgpu_get_wide_search_rows(NGTIndex, NGTError);
 
 #ifdef __cplusplus
 }

@@ -71,7 +71,8 @@ class BatchedTuning(ctypes.Structure):
     """NGTGPUBatchedTuning (include/ngtgpu.h)."""
     _fields_ = [("list_capacity", c_uint32), ("parents", c_uint32), ("rerank_factor", c_float),
                 ("rows_in_flight", c_uint32), ("ctas_per_sm", c_uint32), ("neighbour_capacity", c_uint32),
-                ("cta_threads", c_uint32), ("stage_kilobytes", c_uint32), ("l2_policy", c_uint32)]
+                ("cta_threads", c_uint32), ("stage_kilobytes", c_uint32), ("l2_policy", c_uint32),
+                ("search_rows", c_uint32)]
 
 
 class QueryStats(ctypes.Structure):
@@ -125,6 +126,7 @@ def load_library() -> ctypes.CDLL:
         "ngtgpu_search_batch_device": ([c_void_p, c_void_p, c_size_t, POINTER(QueryParameters), c_size_t, c_void_p,
                                         c_size_t, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p], c_bool),
         "ngtgpu_kernel_launches": ([c_void_p, c_void_p], c_uint64),
+        "ngtgpu_get_wide_search_rows": ([c_void_p, c_void_p], c_uint32),
         "ngtgpu_set_batched_tuning": ([c_void_p, c_uint32, c_uint32, c_float, c_void_p], c_bool),
         "ngtgpu_set_batched_rows_in_flight": ([c_void_p, c_uint32, c_void_p], c_bool),
         "ngtgpu_set_batched_tuning_ex": ([c_void_p, POINTER(BatchedTuning), c_void_p], c_bool),
@@ -270,13 +272,21 @@ class Index:
 
     def set_batched_tuning(self, list_capacity: int = 0, parents: int = 0, rerank_factor: float = 0.0,
                            rows_in_flight: int = 0, ctas_per_sm: int = 0, neighbour_capacity: int = 0,
-                           cta_threads: int = 0, stage_kilobytes: int = 0, l2_policy: int = 0):
+                           cta_threads: int = 0, stage_kilobytes: int = 0, l2_policy: int = 0,
+                           search_rows: int = 0):
         t = BatchedTuning(list_capacity, parents, rerank_factor, rows_in_flight, ctas_per_sm, neighbour_capacity,
-                          cta_threads, stage_kilobytes, l2_policy)
+                          cta_threads, stage_kilobytes, l2_policy, search_rows)
         self._check(self._lib.ngtgpu_set_batched_tuning_ex(self._index, ctypes.byref(t), self._err))
 
     def kernel_launches(self) -> int:
         return int(self._lib.ngtgpu_kernel_launches(self._index, self._err))
+
+    def wide_search_rows(self) -> str:
+        """Search rows of the CTA-per-query kernel: "native", "bf16" or "u8"."""
+        v = int(self._lib.ngtgpu_get_wide_search_rows(self._index, self._err))
+        if v == 0xFFFFFFFF:
+            self._check(False)
+        return ("native", "bf16", "u8")[v]
 
     # device-resident path (used by bench.py for the HBM-resident measurement)
     def query_row_bytes(self) -> int:

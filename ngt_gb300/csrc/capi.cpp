@@ -455,7 +455,8 @@ bool ngtgpu_set_batched_tuning_ex(NGTIndex index, const NGTGPUBatchedTuning* tun
       !(tuning->rows_in_flight <= 2 || tuning->rows_in_flight == 4 ||
         tuning->rows_in_flight == 6 || tuning->rows_in_flight == 8) ||
       tuning->ctas_per_sm > 8 || !(tuning->cta_threads == 0 || tuning->cta_threads == 128 ||
-                                   tuning->cta_threads == 256) || tuning->stage_kilobytes > 200 || tuning->l2_policy > 3) {
+                                   tuning->cta_threads == 256) || tuning->stage_kilobytes > 200 || tuning->l2_policy > 3 ||
+      tuning->search_rows > 2) {
     CAPI_PARAM_ERROR(error, "index = " << index << " tuning = " << tuning);
     return false;
   }
@@ -469,8 +470,20 @@ bool ngtgpu_set_batched_tuning_ex(NGTIndex index, const NGTGPUBatchedTuning* tun
   t.cta_threads = tuning->cta_threads;
   t.stage_kb = tuning->stage_kilobytes;
   t.l2_policy = tuning->l2_policy;
+  t.search_rows = tuning->search_rows;
   engine(index)->set_tuning(t);
   return true;
+}
+
+uint32_t ngtgpu_get_wide_search_rows(NGTIndex index, NGTError error) {
+  if (index == nullptr) {
+    CAPI_PARAM_ERROR(error, "index = " << index);
+    return UINT32_MAX;
+  }
+  try {
+    return (uint32_t)engine(index)->wide_search_rows();
+  }
+  CAPI_CATCH(error, UINT32_MAX)
 }
 
 uint64_t ngtgpu_kernel_launches(NGTIndex index, NGTError error) {

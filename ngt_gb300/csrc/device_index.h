@@ -111,6 +111,10 @@ struct QueryStats {
   uint32_t status;       // bit flags below
 };
 
+// Search rows of the CTA-per-query kernel: the objects themselves, bf16 copies of
+// float objects, or 8-bit codes of float objects (WideConfig::sq8).
+enum class SearchRows : uint32_t { Native = 0, Bf16 = 1, Sq8 = 2 };
+
 enum StatusBits : uint32_t {
   kStatusCandidateOverflow = 1u,   // candidate list hit its capacity (result may differ)
   kStatusVisitedSpill = 2u,        // visited set moved to the global bitmap

@@ -179,6 +179,7 @@ GraphEngine::~GraphEngine() {
     cudaFree(sc.work);
   }
   cudaFree(d_bf16_);
+  cudaFree(d_sq8_);
   for (void* p : qg_buffers_) cudaFree(p);
   cudaFree(d_qbg_ovf_);
   cudaFree(d_blob_dist_);
@@ -417,7 +418,9 @@ void GraphEngine::ensure_scratch(size_t grid) {
 
 bool GraphEngine::fast_supported(Kernel k) const {
   if (k == Kernel::Exact) return true;
-  if (k == Kernel::Wide) return wide_kernel(host_.prop.otype, host_.prop.metric, true, 256) != nullptr;
+  if (k == Kernel::Wide)
+    return wide_kernel(host_.prop.otype, host_.prop.metric,
+                       host_.prop.otype == ObjType::Float ? SearchRows::Bf16 : SearchRows::Native, 256) != nullptr;
   return fast_kernel(host_.prop.otype, host_.prop.metric, k == Kernel::Fast) != nullptr;
 }
 
@@ -454,6 +457,46 @@ void GraphEngine::ensure_bf16_rows() {
   launch_float_rows_to_bf16(d_objects_, d_bf16_, nfloats, stream_);
   NGT_CUDA(cudaGetLastError());
   NGT_CUDA(cudaStreamSynchronize(stream_));
+}
+
+void GraphEngine::ensure_sq8_stats() {
+  if (sq8_stats_) return;
+  const float* x = reinterpret_cast<const float*>(host_.objects.data());
+  const uint32_t dim = host_.prop.dimension, dpad = host_.dpad;
+  float lo = FLT_MAX, hi = -FLT_MAX;
+  bool integral = true;
+  for (size_t r = 1; r < host_.nrows; r++) {          // row 0 is the unused slot
+    const float* row = x + r * dpad;
+    for (uint32_t d = 0; d < dim; d++) {
+      const float v = row[d];
+      lo = std::min(lo, v);
+      hi = std::max(hi, v);
+      integral = integral && std::nearbyint(v) == v;
+    }
+  }
+  if (!(lo <= hi)) { lo = 0.f; hi = 0.f; }
+  sq8_lossless_ = integral && hi - lo <= 255.f;
+  sq8_offset_ = lo;
+  sq8_scale_ = sq8_lossless_ || hi == lo ? 1.f : (hi - lo) / 255.f;
+  sq8_stats_ = true;
+}
+
+void GraphEngine::ensure_sq8_rows() {
+  if (d_sq8_ || host_.prop.otype != ObjType::Float) return;
+  ensure_sq8_stats();
+  NGT_CUDA(cudaMalloc(&d_sq8_, (size_t)host_.nrows * host_.dpad));
+  launch_float_rows_to_sq8(static_cast<const float*>(d_objects_), static_cast<uint8_t*>(d_sq8_), host_.nrows,
+                           host_.dpad, host_.prop.dimension, sq8_offset_, sq8_scale_, stream_);
+  NGT_CUDA(cudaGetLastError());
+  NGT_CUDA(cudaStreamSynchronize(stream_));
+}
+
+SearchRows GraphEngine::wide_search_rows() {
+  if (host_.prop.otype != ObjType::Float || kernel_metric(host_.prop.metric) != Metric::L2) return SearchRows::Native;
+  if (tuning_.search_rows == 1) return SearchRows::Bf16;
+  if (tuning_.search_rows == 2) return SearchRows::Sq8;
+  ensure_sq8_stats();
+  return sq8_lossless_ ? SearchRows::Sq8 : SearchRows::Bf16;
 }
 
 void GraphEngine::search_device(const uint4* d_rows, size_t nq, const SearchArgs* args, size_t nargs, ObjDist* d_out,
@@ -552,11 +595,13 @@ void GraphEngine::launch_exact(const uint4* d_rows, size_t nq, const QueryParams
 void GraphEngine::launch_wide(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
                               uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats,
                               cudaStream_t stream, FastScratch& scratch) {
-  const bool bf16 = host_.prop.otype == ObjType::Float;
+  const SearchRows rows = wide_search_rows();
+  const bool bf16 = rows == SearchRows::Bf16, sq8 = rows == SearchRows::Sq8;
   const uint32_t threads = tuning_.cta_threads ? tuning_.cta_threads : 256u;
-  WideKernelFn fn = wide_kernel(host_.prop.otype, host_.prop.metric, bf16, threads);
+  WideKernelFn fn = wide_kernel(host_.prop.otype, host_.prop.metric, rows, threads);
   if (!fn) throw std::runtime_error("the wide kernel does not support this index type or CTA size");
   if (bf16) ensure_bf16_rows();
+  if (sq8) ensure_sq8_rows();
   WideConfig cfg{};
   uint32_t L = tuning_.list_cap ? next_pow2(tuning_.list_cap) : next_pow2(std::max<uint32_t>(256, 4 * max_size));
   L = std::max<uint32_t>(L, next_pow2(max_size + 1));
@@ -568,7 +613,14 @@ void GraphEngine::launch_wide(const uint4* d_rows, size_t nq, const QueryParams*
   cfg.nbr_cap = tuning_.nbr_cap ? std::max<uint32_t>({next_pow2(tuning_.nbr_cap), next_pow2(rerank_max), L})
                                 : std::max<uint32_t>({512u, next_pow2(rerank_max), L,
                                                       std::min<uint32_t>(4096, next_pow2(cfg.parents * 100))});
-  cfg.search_chunks = bf16 ? dev_.row_chunks / 2 : dev_.row_chunks;
+  cfg.search_chunks = bf16 ? dev_.row_chunks / 2 : sq8 ? dev_.row_chunks / 4 : dev_.row_chunks;
+  if (sq8) {
+    cfg.sq8 = 1;
+    cfg.dim = host_.prop.dimension;
+    cfg.sq_offset = sq8_offset_;
+    cfg.sq_in = 256.f / sq8_scale_;
+    cfg.sq_out = sq8_scale_ / 256.f;
+  }
   // 64 KB of staged rows by default (two 256-thread CTAs share an SM)
   const uint32_t stage_bytes = (tuning_.stage_kb ? tuning_.stage_kb : 64u) * 1024u;
   cfg.stage_rows = std::max<uint32_t>(16, std::min<uint32_t>(512, stage_bytes / (cfg.search_chunks * 16)));
@@ -596,7 +648,8 @@ void GraphEngine::launch_wide(const uint4* d_rows, size_t nq, const QueryParams*
   size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
   ensure_fast_scratch(scratch, grid, stream);
   NGT_CUDA(cudaMemsetAsync(scratch.work, 0, 4, stream));
-  const uint4* srows = bf16 ? static_cast<const uint4*>(d_bf16_) : dev_.objects;
+  const uint4* srows = bf16 ? static_cast<const uint4*>(d_bf16_) : sq8 ? static_cast<const uint4*>(d_sq8_)
+                                                                       : dev_.objects;
   fn<<<(unsigned)grid, threads, smem, stream>>>(dev_, srows, d_rows, (uint32_t)nq, d_params, d_seeds, d_out,
                                                 d_counts, d_stats, scratch.bitmaps, scratch.work, scratch.spill, cfg);
   NGT_CUDA(cudaGetLastError());

@@ -43,6 +43,8 @@ struct FastTuning {
   uint32_t cta_threads = 0;    // wide kernel: threads per CTA (128 or 256)
   uint32_t stage_kb = 0;       // wide kernel: shared memory for staged rows (KB)
   uint32_t l2_policy = 0;      // wide kernel: 0 automatic, else WideConfig::l2_policy + 1
+  uint32_t search_rows = 0;    // wide kernel, float objects: 0 automatic (8-bit when lossless, else bf16),
+                               // 1 bf16, 2 8-bit codes
 };
 
 // Parameters of one quantized-graph query (NGTQGQueryParameters,
@@ -183,6 +185,14 @@ class GraphEngine {
   void ensure_scratch(size_t grid);
   void ensure_fast_scratch(FastScratch& sc, size_t slots, cudaStream_t stream);
   void ensure_bf16_rows();
+  // 8-bit codes of float objects; the affine map is lossless when every
+  // coordinate is an integer and they span at most 256 values
+  void ensure_sq8_stats();
+  void ensure_sq8_rows();
+ public:
+  // search rows the wide kernel uses for this index and tuning
+  SearchRows wide_search_rows();
+ private:
   void launch_exact(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
                     uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, cudaStream_t stream);
   void launch_fast(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
@@ -235,6 +245,9 @@ class GraphEngine {
   static constexpr uint32_t kSpillCapacity = 32768;
   std::vector<FastScratch> fast_scratch_ = std::vector<FastScratch>(1);
   void* d_bf16_ = nullptr;                                // bf16 copy of float object rows
+  void* d_sq8_ = nullptr;                                 // 8-bit codes of float object rows
+  bool sq8_stats_ = false, sq8_lossless_ = false;
+  float sq8_offset_ = 0.f, sq8_scale_ = 1.f;
   FastTuning tuning_;
   DevGraph dev_;
 };

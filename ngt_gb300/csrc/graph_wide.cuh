@@ -42,6 +42,10 @@ struct WideConfig {
   uint32_t l2_policy;      // 0: default caching; 1: visited bitmap kept in L2 (evict_last);
                            // 2: as 1, and staged rows streamed through L2 (evict_first)
   uint32_t score_rows;     // rows per lane group scored at once (1, 2 or 4)
+  // 8-bit search rows of float objects: code = rint((x - sq_offset) / s), the query
+  // mapped the same way in 1/256 steps; distance = sqrt(sum) * sq_out (s / 256)
+  uint32_t sq8, dim;
+  float sq_offset, sq_in, sq_out;   // sq_in = 256 / s
 };
 
 struct WideShared {
@@ -55,7 +59,7 @@ struct WideShared {
 };
 
 inline size_t wide_smem_bytes(uint32_t row_chunks, const WideConfig& c) {
-  size_t b = (size_t)row_chunks * 16 + (size_t)c.search_chunks * 16;
+  size_t b = (size_t)row_chunks * 16 + (size_t)c.search_chunks * (c.sq8 ? 64 : 16);
   b += (size_t)c.list_cap * 16;                                   // list, double-buffered
   b += (size_t)c.nbr_cap * 16;                                    // nkey, nid, nd
   b += (size_t)c.stage_rows * c.search_chunks * 16;               // row staging
@@ -143,6 +147,54 @@ __device__ __forceinline__ uint32_t cta_compact(bool flag, uint32_t* wcnt, uint3
   return base + __popc(bal & ((1u << lane) - 1u));
 }
 
+// (row - query)^2 of one 16-byte row chunk, two float lanes at a time, against the
+// query chunk prepared once per query: bf16 / fp32 rows through PackedL2, 8-bit
+// rows of float objects (Sq8) by placing each code in the mantissa of 2^23
+// (2^23 + 256 c, one byte permute) and adding the negated 2^23 + rint(256 q'),
+// so that the difference 256 (c - q') is exact.
+template <ObjType ST, ObjType OT, Metric M>
+struct WideDot {
+  typedef PackedL2<ST, M> PL;
+  static constexpr bool kSq8 = ST == ObjType::Uint8 && OT == ObjType::Float && M == Metric::L2;
+  static constexpr bool kOn = kSq8 || PL::kOn;
+  static constexpr int NQ = kSq8 ? 8 : (PL::P / 2 > 0 ? PL::P / 2 : 1);
+  // query chunk c: qs holds the search-type query (4 uint4 of floats per chunk for Sq8)
+  __device__ __forceinline__ static void prepare(const uint4* qs, uint32_t c, float2 (&nq)[NQ]) {
+    if constexpr (kSq8) {
+      const float2* f = reinterpret_cast<const float2*>(qs + 4 * (size_t)c);
+#pragma unroll
+      for (int i = 0; i < 8; i++) nq[i] = f[i];
+    } else if constexpr (PL::kOn) {
+      PL::prepare(qs[c], nq);
+    }
+  }
+  __device__ __forceinline__ static void zero(float2 (&nq)[NQ]) {
+#pragma unroll
+    for (int i = 0; i < NQ; i++) nq[i] = make_float2(0.f, 0.f);
+  }
+  __device__ __forceinline__ static float2 add(float2 acc, const float2 (&nq)[NQ], const uint4& x) {
+    if constexpr (kSq8) {
+      const uint32_t w[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        const float a = __uint_as_float(__byte_perm(w[i], 0x4B000000u, 0x7504u));
+        const float b = __uint_as_float(__byte_perm(w[i], 0x4B000000u, 0x7514u));
+        const float c = __uint_as_float(__byte_perm(w[i], 0x4B000000u, 0x7524u));
+        const float d = __uint_as_float(__byte_perm(w[i], 0x4B000000u, 0x7534u));
+        const float2 d0 = __fadd2_rn(make_float2(a, b), nq[2 * i]);
+        const float2 d1 = __fadd2_rn(make_float2(c, d), nq[2 * i + 1]);
+        acc = __ffma2_rn(d0, d0, acc);
+        acc = __ffma2_rn(d1, d1, acc);
+      }
+      return acc;
+    } else if constexpr (PL::kOn) {
+      return PL::add(acc, nq, x);
+    } else {
+      return acc;
+    }
+  }
+};
+
 // T: threads per CTA (128 or 256), one query per CTA.
 template <ObjType ST, ObjType OT, Metric M, int T>
 __global__ void __launch_bounds__(T, T == 128 ? 5 : 2)
@@ -156,8 +208,9 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
   const uint32_t rc = g.row_chunks, sc = cfg.search_chunks;
   const uint32_t L = cfg.list_cap, NB = cfg.nbr_cap, SR = cfg.stage_rows;
   uint4* qn = reinterpret_cast<uint4*>(smem);
-  uint4* qs = qn + rc;
-  unsigned long long* lists = reinterpret_cast<unsigned long long*>(qs + sc);   // 2 x L
+  typedef WideDot<ST, OT, M> Dot;
+  uint4* qs = qn + rc;                                                           // sc (x 4 for Sq8) chunks
+  unsigned long long* lists = reinterpret_cast<unsigned long long*>(qs + (Dot::kSq8 ? 4 * sc : sc));   // 2 x L
   unsigned long long* nkey = lists + 2 * (size_t)L;
   uint32_t* nid = reinterpret_cast<uint32_t*>(nkey + NB);
   float* nd = reinterpret_cast<float*>(nid + NB);
@@ -200,12 +253,13 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
     if (cnt == 0) return;
     // the query chunks this lane reads (c = sgl + j * SG), negated and unpacked once
     constexpr int kQC = 2;   // the host sets sgroup so that every lane reads at most two chunks
-    float2 nqc[kQC][PackedL2<ST, M>::P / 2];
-    if constexpr (PackedL2<ST, M>::kOn) {
+    float2 nqc[kQC][Dot::NQ];
+    if constexpr (Dot::kOn) {
 #pragma unroll
       for (int j = 0; j < kQC; j++) {
         const uint32_t c = (uint32_t)sgl + (uint32_t)(j * SG);
-        PackedL2<ST, M>::prepare(c < sc ? qs[c] : make_uint4(0, 0, 0, 0), nqc[j]);
+        if (c < sc) Dot::prepare(qs, c, nqc[j]);
+        else Dot::zero(nqc[j]);
       }
     }
     uint4* buf[2] = {stage, stage + (size_t)SRH * sc};
@@ -223,7 +277,7 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       const uint4* stg = buf[h];
       const uint32_t gpb = (uint32_t)T / SG;
       const uint32_t gi = (uint32_t)(tid / SG);
-      if (PackedL2<ST, M>::kOn && sc <= (uint32_t)(kQC * SG)) {
+      if (Dot::kOn && sc <= (uint32_t)(kQC * SG)) {
         // KR rows per lane group at once: their shared-memory loads first, then 2 x KR
         // independent accumulations (one per chunk) and interleaved shuffle reductions
         auto rows_at_once = [&](auto kr_tag) {
@@ -247,7 +301,7 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
 #pragma unroll
               for (int j = 0; j < kQC; j++) {
                 acc[j] = make_float2(0.f, 0.f);
-                if ((uint32_t)sgl + (uint32_t)(j * SG) < sc) acc[j] = PackedL2<ST, M>::add(acc[j], nqc[j], x[u][j]);
+                if ((uint32_t)sgl + (uint32_t)(j * SG) < sc) acc[j] = Dot::add(acc[j], nqc[j], x[u][j]);
               }
               float t = acc[0].x + acc[0].y;
 #pragma unroll
@@ -263,7 +317,7 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
 #pragma unroll
             for (int u = 0; u < KR; u++) {
               const uint32_t i = b + (uint32_t)u * gpb + gi;
-              if (i < nr && sgl == 0) nd[r0 + i] = sqrtf(v[u]);
+              if (i < nr && sgl == 0) nd[r0 + i] = Dot::kSq8 ? sqrtf(v[u]) * cfg.sq_out : sqrtf(v[u]);
             }
           }
         };
@@ -277,18 +331,18 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
           const bool valid = i < nr;
           const uint4* row = stg + (size_t)(valid ? i : 0u) * sc;
           float d;
-          if constexpr (PackedL2<ST, M>::kOn) {
+          if constexpr (Dot::kOn) {
             float2 acc = make_float2(0.f, 0.f);
             for (uint32_t c = (uint32_t)sgl; c < sc; c += (uint32_t)SG) {
-              float2 nq[PackedL2<ST, M>::P / 2];
-              PackedL2<ST, M>::prepare(qs[c], nq);
-              acc = PackedL2<ST, M>::add(acc, nq, row[c]);
+              float2 nq[Dot::NQ];
+              Dot::prepare(qs, c, nq);
+              acc = Dot::add(acc, nq, row[c]);
             }
             float v = acc.x + acc.y;
 #pragma unroll
             for (int off = 16; off > 0; off >>= 1)
               if (off < SG) v += __shfl_xor_sync(0xffffffffu, v, off);
-            d = sqrtf(v);
+            d = Dot::kSq8 ? sqrtf(v) * cfg.sq_out : sqrtf(v);
           } else {
             Acc<ST, M> acc;
             for (uint32_t c = (uint32_t)sgl; c < sc; c += (uint32_t)SG) acc.add(qs[c], row[c], (int)c);
@@ -311,7 +365,16 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
     const QueryParams P = params[q];
     for (uint32_t i = tid; i < rc; i += blockDim.x) qn[i] = queries[(size_t)q * rc + i];
     __syncthreads();
-    if constexpr (ST != OT) {
+    if constexpr (Dot::kSq8) {
+      // 16 negated values per row chunk: -(2^23 + rint(256 (q - offset) / s)), 0 past dim
+      const float* qf = reinterpret_cast<const float*>(qn);
+      float* qv = reinterpret_cast<float*>(qs);
+      for (uint32_t i = tid; i < sc * 16; i += blockDim.x) {
+        float v = 0.f;
+        if (i < cfg.dim) v = fminf(fmaxf(rintf((qf[i] - cfg.sq_offset) * cfg.sq_in), -8388607.f), 8388607.f);
+        qv[i] = -(8388608.f + v);
+      }
+    } else if constexpr (ST != OT) {
       const float* qf = reinterpret_cast<const float*>(qn);
       uint32_t* qb = reinterpret_cast<uint32_t*>(qs);
       for (uint32_t i = tid; i < sc * 4; i += blockDim.x) {
