@@ -45,11 +45,10 @@ RECALL_TARGET = 0.95
 # lane group in flight, registers budgeted for C CTAs per SM, NB neighbour slots per
 # step; 0 = automatic); kernel 3: CTA per query (T threads, `stage` KB of staged rows).
 BATCHED_CANDIDATES = [
-    dict(kernel=1, L=256, P=3, R=4, C=5, NB=256), dict(kernel=1, L=256, P=4, R=4, C=5, NB=0),
-    dict(kernel=1, L=256, P=4, R=6, C=4, NB=0), dict(kernel=1, L=128, P=3, R=4, C=5, NB=256),
-    dict(kernel=3, L=256, P=8, T=128, stage=16), dict(kernel=3, L=256, P=8, T=128, stage=32),
-    dict(kernel=3, L=128, P=8, T=128, stage=32), dict(kernel=3, L=256, P=16, T=128, stage=32),
-    dict(kernel=3, L=256, P=8, T=256, stage=64)]
+    dict(kernel=1, L=256, P=3, R=4, C=5, NB=256), dict(kernel=1, L=256, P=4, R=6, C=4, NB=0),
+    dict(kernel=3, L=256, P=8, T=128, stage=16), dict(kernel=3, L=256, P=8, T=128, stage=8),
+    dict(kernel=3, L=256, P=8, T=128, stage=32), dict(kernel=3, L=256, P=16, T=128, stage=16),
+    dict(kernel=3, L=256, P=16, T=256, stage=32), dict(kernel=3, L=256, P=8, T=256, stage=32)]
 WIDE_PARENTS = 16                 # parents per step of the CTA-per-query kernel the serving loop uses
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of 2,000 queries on
 # this workload (1M x 128, k=10, epsilon 0.08; ncu captures summarised under
@@ -462,7 +461,8 @@ def main():
         cnt_np = cnt.cpu().numpy().astype(np.int64)
         stats = st.cpu().numpy().view(QUERY_STATS_DTYPE).reshape(nq)
         rec = recall(base, queries, ids_np, cnt_np, kth, k)
-        srow = row_bytes // 2 if kernel in (1, 3) else row_bytes
+        srow = (row_bytes // 4 if kernel == 3 and wide_rows == "u8" else
+                row_bytes // 2 if kernel in (1, 3) else row_bytes)
         rerank = 0 if kernel == KERNEL_EXACT else 2 * k * row_bytes
         bytes_pq = (srow * stats["distance_computations"].astype(np.float64) + 4.0 * stats["edges_read"]
                     + row_bytes + rerank)
@@ -477,6 +477,8 @@ def main():
 
     runs = {}
     curves = {}
+    wide_rows = ix.wide_search_rows()       # search rows of the CTA-per-query kernel: "u8" or "bf16"
+
     def apply(c):
         ix.set_batched_tuning(list_capacity=c["L"], parents=c["P"], rows_in_flight=c.get("R", 0),
                               ctas_per_sm=c.get("C", 0), neighbour_capacity=c.get("NB", 0),
@@ -572,19 +574,22 @@ def main():
     if rank == 0:
         cpu = cpu_baseline(path, queries, plain["epsilon"], k, args.cpu_sample, os.cpu_count() or 1)
 
+    head_rows = wide_rows if head["config"]["kernel"] == KERNEL_WIDE else "bf16"
+    rows_text = ("8-bit (lossless: the objects' coordinates are 8-bit integers)" if head_rows == "u8"
+                 else head_rows)
     if rank == 0:
         line = {
             "metric": "queries/s at recall@10>=0.95 (1M x 128 L2 ONNG)",
             "value": round(head["qps"], 1), "unit": "queries/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(head["ms_per_step"], 4), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "bf16+f32-rerank", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "%s+f32-rerank" % head_rows, "data": "synthetic",
             "config": {"workload": "graph search, %d x %d float32 L2 ONNG, %d queries per step, k=%d"
                                    % (args.n, args.dim, nq, k),
-                       "headline": ("batched kernel (%s, bf16 rows, exact fp32 re-rank), epsilon=%g, "
+                       "headline": ("batched kernel (%s, %s search rows, exact fp32 re-rank), epsilon=%g, "
                                     "autotuned settings %s"
                                     % ("warp per query" if head["config"]["kernel"] == KERNEL_BATCHED
                                        else "CTA per query, rows of a step staged in shared memory",
-                                       head["epsilon"], json.dumps(head["config"], sort_keys=True))),
+                                       rows_text, head["epsilon"], json.dumps(head["config"], sort_keys=True))),
                        "recall_at_k": round(head["recall"], 4), "epsilon_curve": curves[KERNEL_BATCHED],
                        "plain_fp32": {"qps": round(plain["qps"], 1), "epsilon": plain["epsilon"],
                                       "recall_at_k": round(plain["recall"], 4),
@@ -607,9 +612,9 @@ def main():
                          "peak_source": peak_kind,
                          "basis": "(%d*DC + 4*edges + %d query + re-rank %d*2k) bytes per query over the kernel's "
                                   "median event time" % (head["row_bytes"], row_bytes, row_bytes)},
-            "served": {"kernel": "CTA per query (bf16 rows, rows of a step staged in shared memory), "
+            "served": {"kernel": "CTA per query (%s search rows, rows of a step staged in shared memory), "
                                  "%d parents per step; up to 8 launches of at most 512 queries in flight"
-                                 % WIDE_PARENTS,
+                                 % (wide_rows, WIDE_PARENTS),
                        "qps_10000_batch": round(wide["qps"], 1) if wide else None,
                        "recall_at_k": round(wide["recall"], 4) if wide else None,
                        "rates": served,

@@ -144,3 +144,52 @@ def test_smaller_neighbour_capacity_keeps_recall(tmp_path):
     li, ld, ln = o.linear_search(q, k=10, threads=8)
     hit = sum(len(set(ids[j, :n[j]]) & set(li[j, :ln[j]])) for j in range(len(q)))
     assert hit / (10 * len(q)) > 0.9
+
+
+def test_wide_u8_rows_of_integer_objects_equal_bf16_rows(tmp_path):
+    """On objects whose coordinates are 8-bit integers both search-row formats
+    give every distance exactly (the 8-bit codes are lossless, and the automatic
+    choice takes them): results and statistics identical."""
+    from ngt_gb300 import Index
+    path, meta, queries, _ = materialize("c1_f32_l2", str(tmp_path))
+    with Index(path, read_only=True) as ix:
+        assert ix.wide_search_rows() == "u8"
+        out = {}
+        for rows in (1, 2, 0):
+            ix.set_batched_tuning(list_capacity=256, parents=8, cta_threads=128, stage_kilobytes=16, search_rows=rows)
+            out[rows] = ix.batch_search(queries[:300], k=10, epsilon=0.1, kernel=KERNEL_WIDE, with_stats=True)
+        ix.set_batched_tuning(search_rows=1)
+        assert ix.wide_search_rows() == "bf16"
+    for rows in (2, 0):
+        for a, b in zip(out[1], out[rows]):
+            assert np.array_equal(np.asarray(a).view(np.uint8), np.asarray(b).view(np.uint8)), rows
+
+
+def test_wide_lossy_u8_rows_keep_recall(tmp_path):
+    """Non-integer float objects: the automatic choice stays bf16; 8-bit codes
+    with a range-wide scale (requested explicitly) stay within 0.02 of its recall
+    after the exact re-rank, and the returned distances stay exact."""
+    import torch
+    from ngt_gb300 import Index, graph_build
+    # points near an 8-dimensional subspace of R^64 (searchable, non-integer coordinates)
+    rng = np.random.default_rng(4)
+    basis = rng.standard_normal((8, 64)).astype(np.float32)
+    pts = (rng.standard_normal((20500, 8)).astype(np.float32) @ basis
+           + 0.05 * rng.standard_normal((20500, 64)).astype(np.float32)).astype(np.float32)
+    x, q = pts[:20000], pts[20000:]
+    path = str(tmp_path / "gm")
+    graph_build.build_onng_index(path, x, k=40, outgoing=10, incoming=40, log=lambda *a: None)
+    X = torch.from_numpy(x).double()
+    d2 = torch.cdist(torch.from_numpy(q).double(), X) ** 2
+    gt = torch.topk(d2, 10, largest=False).indices.numpy() + 1          # object ids start at 1
+    recall = {}
+    with Index(path, read_only=True) as ix:
+        assert ix.wide_search_rows() == "bf16"
+        for rows in (1, 2):
+            ix.set_batched_tuning(cta_threads=256, search_rows=rows)
+            ids, ds, n = ix.batch_search(q, k=10, epsilon=0.15, kernel=KERNEL_WIDE)
+            recall[rows] = np.mean([len(set(ids[j, :n[j]]) & set(gt[j])) / 10 for j in range(len(q))])
+            exact = np.sqrt(((x[ids[:, 0] - 1] - q) ** 2).sum(1))
+            assert np.allclose(ds[:, 0], exact, rtol=1e-5, atol=1e-5)
+    assert recall[1] > 0.9
+    assert recall[2] >= recall[1] - 0.02, recall
