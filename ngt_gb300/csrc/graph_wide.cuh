@@ -689,12 +689,23 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       }
       __syncthreads();
       if (kept == 0) continue;
-      cta_bitonic_sort(nkey, kept, NB);
       // ---- merge into the other list buffer (entries compare without the expanded bit) ---
+      // Every key's place is its rank among the new keys plus its rank among the list's:
+      // up to T new keys are ranked by counting (no sort, no barrier), more are sorted
+      // first and ranked by binary search.
+      const bool by_count = kept <= (uint32_t)T;
+      if (!by_count) cta_bitonic_sort(nkey, kept, NB);
+      auto rank_new = [&](unsigned long long x, uint32_t j_hint) -> uint32_t {
+        if (!by_count) return j_hint;
+        uint32_t r = 0;
+        for (uint32_t t = 0; t < kept; t++) r += nkey[t] < x ? 1u : 0u;
+        return r;
+      };
       unsigned long long* dst = lists + (size_t)(s.cur ^ 1u) * L;
       for (uint32_t i = tid; i < n; i += blockDim.x) {
         const unsigned long long k = list[i];
-        const uint32_t pos = i + warp_lower_bound(nkey, kept, k & ~(unsigned long long)kExpandedBit);
+        const unsigned long long km = k & ~(unsigned long long)kExpandedBit;
+        const uint32_t pos = i + (by_count ? rank_new(km, 0u) : warp_lower_bound(nkey, kept, km));
         if (pos < L) dst[pos] = k;
         else if (!key_expanded(k)) {
           const uint32_t o = atomicAdd(&s.spill_n, 1u);
@@ -709,7 +720,7 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
           uint32_t mid = (lo + hi) >> 1;
           if ((list[mid] & ~(unsigned long long)kExpandedBit) < k) lo = mid + 1; else hi = mid;
         }
-        const uint32_t pos = j + lo;
+        const uint32_t pos = rank_new(k, j) + lo;
         if (pos < L) {
           dst[pos] = k;
           atomicMin(&s.first_new, pos);
