@@ -193,3 +193,29 @@ def test_wide_lossy_u8_rows_keep_recall(tmp_path):
             assert np.allclose(ds[:, 0], exact, rtol=1e-5, atol=1e-5)
     assert recall[1] > 0.9
     assert recall[2] >= recall[1] - 0.02, recall
+
+
+def test_wide_tuning_knobs_do_not_change_results(tmp_path):
+    """Threads per CTA, staged rows, rows scored at once and the L2 policy change
+    how a step is executed, never which candidates it keeps: results and
+    statistics identical.  Out-of-range knobs are rejected."""
+    from ngt_gb300 import Index
+    from ngt_gb300.base import NativeError
+    path, meta, queries, _ = materialize("c1_f32_l2_onng", str(tmp_path))
+    with Index(path, read_only=True) as ix:
+        ix.set_batched_tuning(list_capacity=256, parents=8, search_rows=1)
+        ref = ix.batch_search(queries[:300], k=10, epsilon=0.1, kernel=KERNEL_WIDE, with_stats=True)
+        for T, stage, rows, l2 in ((128, 8, 1, 1), (128, 32, 2, 2), (256, 64, 4, 3), (256, 16, 2, 1), (128, 200, 4, 3)):
+            ix.set_batched_tuning(list_capacity=256, parents=8, search_rows=1, cta_threads=T, stage_kilobytes=stage,
+                                  rows_in_flight=rows, l2_policy=l2)
+            got = ix.batch_search(queries[:300], k=10, epsilon=0.1, kernel=KERNEL_WIDE, with_stats=True)
+            for a, b in zip(ref, got):
+                assert np.array_equal(np.asarray(a).view(np.uint8), np.asarray(b).view(np.uint8)), (T, stage, rows, l2)
+        # 32 parents per step (the largest) still reaches the reference-level recall
+        ix.set_batched_tuning(list_capacity=256, parents=32)
+        ids, ds, n = ix.batch_search(queries[:300], k=10, epsilon=0.1, kernel=KERNEL_WIDE)
+        assert (n == 10).all()
+        for bad in (dict(parents=33), dict(l2_policy=4), dict(search_rows=3), dict(cta_threads=192),
+                    dict(stage_kilobytes=201), dict(rows_in_flight=3)):
+            with pytest.raises(NativeError):
+                ix.set_batched_tuning(**bad)
