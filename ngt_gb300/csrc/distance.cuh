@@ -20,6 +20,7 @@ template <> struct ObjTraits<ObjType::Float> { typedef float T; static constexpr
 template <> struct ObjTraits<ObjType::Float16> { typedef __half T; static constexpr int kPerChunk = 8; };
 template <> struct ObjTraits<ObjType::Uint8> { typedef uint8_t T; static constexpr int kPerChunk = 16; };
 template <> struct ObjTraits<ObjType::Bfloat16> { typedef uint16_t T; static constexpr int kPerChunk = 8; };
+template <> struct ObjTraits<ObjType::Qsint8> { typedef int8_t T; static constexpr int kPerChunk = 16; };
 
 template <ObjType OT>
 __device__ __forceinline__ void unpack(const uint4& v, float* f);
@@ -47,6 +48,12 @@ __device__ __forceinline__ void unpack<ObjType::Bfloat16>(const uint4& v, float*
   }
 }
 template <>
+__device__ __forceinline__ void unpack<ObjType::Qsint8>(const uint4& v, float* f) {
+  const uint32_t w[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+  for (int i = 0; i < 16; i++) f[i] = (float)(int8_t)((w[i >> 2] >> ((i & 3) * 8)) & 0xffu);
+}
+template <>
 __device__ __forceinline__ void unpack<ObjType::Uint8>(const uint4& v, float* f) {
   const uint32_t w[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
@@ -69,6 +76,14 @@ struct Acc {
         // (a-b)^2 = a^2 + b^2 - 2ab, all in exact unsigned 32-bit arithmetic.
         i0 += __dp4a(qa[i], qa[i], 0u) + __dp4a(xa[i], xa[i], 0u);
         i1 += __dp4a(qa[i], xa[i], 0u);
+      }
+    } else if constexpr (OT == ObjType::Qsint8 && M == Metric::L2) {
+      const int qa[4] = {(int)q.x, (int)q.y, (int)q.z, (int)q.w}, xa[4] = {(int)x.x, (int)x.y, (int)x.z, (int)x.w};
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        // (a-b)^2 = a^2 + b^2 - 2ab over signed bytes, exact 32-bit arithmetic
+        i0 += (uint32_t)(__dp4a(qa[i], qa[i], 0) + __dp4a(xa[i], xa[i], 0));
+        i1 += (uint32_t)__dp4a(qa[i], xa[i], 0);
       }
     } else if constexpr (OT == ObjType::Uint8 && M == Metric::L1) {
       i0 += __vsadu4(q.x, x.x) + __vsadu4(q.y, x.y) + __vsadu4(q.z, x.z) + __vsadu4(q.w, x.w);
@@ -110,7 +125,8 @@ struct Acc {
   }
 
   // Which accumulators a metric uses (only those are reduced across lanes).
-  static constexpr bool kUint8Sq = OT == ObjType::Uint8 && (M == Metric::L2 || M == Metric::InnerProduct);
+  static constexpr bool kUint8Sq = (OT == ObjType::Uint8 && (M == Metric::L2 || M == Metric::InnerProduct)) ||
+                                   (OT == ObjType::Qsint8 && M == Metric::L2);
   static constexpr bool kUseI0 = kUint8Sq || (OT == ObjType::Uint8 && M == Metric::L1) || M == Metric::Hamming ||
                                  M == Metric::Jaccard;
   static constexpr bool kUseI1 = kUint8Sq || M == Metric::Jaccard;
@@ -133,7 +149,11 @@ struct Acc {
   }
 
   __device__ __forceinline__ float finish() const {
-    if constexpr (OT == ObjType::Uint8 && (M == Metric::L2 || M == Metric::InnerProduct)) {
+    if constexpr (OT == ObjType::Qsint8 && M == Metric::L2) {
+      // the squared sum itself: PrimitiveComparator::compareL2(qsint8) of the x86
+      // build (lib/NGT/PrimitiveComparatorX86.h:341-431) takes no square root
+      return (float)(int)(i0 - 2u * i1);
+    } else if constexpr (OT == ObjType::Uint8 && (M == Metric::L2 || M == Metric::InnerProduct)) {
       return sqrtf((float)(i0 - 2u * i1));
     } else if constexpr (OT == ObjType::Uint8 && M == Metric::L1) {
       return (float)i0;

@@ -54,6 +54,7 @@ ExactKernelFn exact_kernel(ObjType t, Metric m) {
     case ObjType::Float: return exact_kernel_float(m);
     case ObjType::Float16: return exact_kernel_half(m);
     case ObjType::Uint8: return exact_kernel_u8(m);
+    case ObjType::Qsint8: return exact_kernel_qs8(m);
     default: return nullptr;
   }
 }
@@ -64,6 +65,7 @@ LinearKernelFn linear_kernel(ObjType t, Metric m) {
     case ObjType::Float: return linear_kernel_float(m);
     case ObjType::Float16: return linear_kernel_half(m);
     case ObjType::Uint8: return linear_kernel_u8(m);
+    case ObjType::Qsint8: return linear_kernel_qs8(m);
     default: return nullptr;
   }
 }
@@ -271,7 +273,7 @@ void GraphEngine::build_params(const SearchArgs* args, size_t nargs, size_t nq, 
     if (coef == 0.0f) coef = 1.1f;                     // NGT_EXPLORATION_COEFFICIENT
     size_t size = a.size;
     size_t size_out = size;
-    bool size_backup = p.epsilon_type == 2;            // EpsilonTypeResultSize
+    bool size_backup = result_size_rule();
     if (size_backup) {
       size = (size_t)std::round(coef * (float)size);
       coef = 1.0f;
@@ -336,8 +338,17 @@ void GraphEngine::seed_params(size_t k, uint32_t& seed_off, uint32_t& seed_cnt, 
   seed_cnt = (uint32_t)(seed_list.size() - seed_off);
 }
 
+// EpsilonType ResultSize: search for round((1+epsilon) x k) results with the
+// exploration coefficient 1; the updatable search applies it to quantized
+// objects under EpsilonType None too (lib/NGT/Graph.cpp:845-852).
+bool GraphEngine::result_size_rule() const {
+  const Property& p = host_.prop;
+  return p.epsilon_type == 2 ||
+         (mode_ == GraphMode::Updatable && p.epsilon_type == 0 && p.otype == ObjType::Qsint8);
+}
+
 size_t GraphEngine::output_size(const SearchArgs& a) const {
-  if (host_.prop.epsilon_type == 2 && mode_ == GraphMode::Updatable) {
+  if (result_size_rule() && mode_ == GraphMode::Updatable) {
     float coef = a.epsilon + 1.0f;
     if (coef == 0.0f) coef = 1.1f;
     return (size_t)std::round(coef * (float)a.size);
@@ -393,6 +404,19 @@ void GraphEngine::convert_queries(const void* queries, QueryType qt, size_t nq, 
         for (size_t i = 0; i < qdim; i++) {
           double v = query_elem(queries, qt, q * qdim + i);
           dst[i] = (uint8_t)(int)v;       // static_cast<uint8_t> truncates toward zero
+        }
+        break;
+      }
+      case ObjType::Qsint8: {
+        // ObjectSpace::quantizeSymmetrically (lib/NGT/ObjectSpace.h:432-441): the
+        // division in float, the product with 127.5 and the rounding in double
+        const float scale = host_.prop.quantization_scale;
+        for (size_t i = 0; i < qdim; i++) {
+          float fv = tmp[i];
+          fv = (float)std::round((double)(fv / scale) * 127.5);
+          fv = fv < -127.0f ? -127.0f : fv;
+          fv = fv > 127.0f ? 127.0f : fv;
+          dst[i] = (uint8_t)(int8_t)fv;
         }
         break;
       }

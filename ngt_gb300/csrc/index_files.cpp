@@ -65,7 +65,8 @@ ObjType parse_objtype(const std::string& s) {
   if (s == "Float-4") return ObjType::Float;
   if (s == "Integer-1") return ObjType::Uint8;
   if (s == "Float-2") return ObjType::Float16;
-  fail("unsupported ObjectType '" + s + "' (quantized object types are not supported)");
+  if (s == "QSUInteger-8B") return ObjType::Qsint8;
+  fail("unsupported ObjectType '" + s + "'");
 }
 
 int to_int(const std::string& s, const char* key) {
@@ -124,6 +125,17 @@ Property load_property(const std::string& dir) {
   p.epsilon_type = et == "ByQuery" ? 1 : et == "ResultSize" ? 2 : 0;
   p.graph_type = p.get("GraphType", "ANNG");
   if (p.metric == Metric::SparseJaccard) fail("SparseJaccard indexes are not supported");
+  if (p.otype == ObjType::Qsint8) {
+    // the quantized objects' search comparators other than L2 compare against
+    // differently coded queries (lib/NGT/PrimitiveComparator.h:376-404); L2 only here
+    if (p.metric != Metric::L2) fail("QSUInteger-8B objects are supported with the L2 distance only");
+    try {
+      p.quantization_scale = std::stof(p.get("QuantizationScale", "0"));
+    } catch (...) {
+      fail("invalid QuantizationScale in " + dir + "/prf");
+    }
+    if (!(p.quantization_scale > 0.f)) fail("QSUInteger-8B index without a positive QuantizationScale");
+  }
   return p;
 }
 

@@ -33,6 +33,7 @@ struct Property {
   int seed_size = 10;
   int seed_type = 0;               // SeedType (lib/NGT/Graph.h:297-304)
   int epsilon_type = 0;            // EpsilonType (lib/NGT/Graph.h:306)
+  float quantization_scale = 0.f;  // QuantizationScale (Qsint8 objects)
   std::string graph_type;
   std::string get(const std::string& k, const std::string& dflt = "") const;
 };

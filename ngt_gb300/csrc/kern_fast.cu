@@ -45,6 +45,9 @@ FastKernelFn fast_kernel(ObjType ot, Metric m, bool bf16_rows, uint32_t rows_in_
   if (ot == ObjType::Float16) {
     switch (m) { NGT_FAST_CASE(Float16, Float16, L2) NGT_FAST_CASE(Float16, Float16, L1) default: return nullptr; }
   }
+  if (ot == ObjType::Qsint8) {
+    switch (m) { NGT_FAST_CASE(Qsint8, Qsint8, L2) default: return nullptr; }
+  }
   return nullptr;
 }
 

@@ -19,6 +19,8 @@ WideKernelFn wide_kernel(ObjType ot, Metric m, SearchRows rows, uint32_t threads
     return &graph_search_wide_kernel<ObjType::Float, ObjType::Float, Metric::L2, 256>;
   if (ot == ObjType::Uint8 && m == Metric::L2)
     return &graph_search_wide_kernel<ObjType::Uint8, ObjType::Uint8, Metric::L2, 256>;
+  if (ot == ObjType::Qsint8 && m == Metric::L2)
+    return &graph_search_wide_kernel<ObjType::Qsint8, ObjType::Qsint8, Metric::L2, 256>;
   return nullptr;
 }
 

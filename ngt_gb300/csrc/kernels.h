@@ -54,9 +54,11 @@ void launch_float_rows_to_bf16(const void* in, void* out, size_t nfloats, cudaSt
 ExactKernelFn exact_kernel_float(Metric m);
 ExactKernelFn exact_kernel_half(Metric m);
 ExactKernelFn exact_kernel_u8(Metric m);
+ExactKernelFn exact_kernel_qs8(Metric m);
 LinearKernelFn linear_kernel_float(Metric m);
 LinearKernelFn linear_kernel_half(Metric m);
 LinearKernelFn linear_kernel_u8(Metric m);
+LinearKernelFn linear_kernel_qs8(Metric m);
 
 // Metric used by the kernels: inner product runs as L2 over the augmented rows.
 inline Metric kernel_metric(Metric m) { return m == Metric::InnerProduct ? Metric::L2 : m; }

@@ -24,12 +24,15 @@ enum class Metric : int32_t {
   Lorentz = 101,
 };
 
-enum class ObjType : int32_t { Float = 0, Uint8 = 1, Float16 = 2, Bfloat16 = 3 };
+// Qsint8: NGT's scalar-quantized objects (ObjectType "QSUInteger-8B",
+// lib/NGT/ObjectSpace.h:250): int8 codes rint(x / QuantizationScale x 127.5).
+enum class ObjType : int32_t { Float = 0, Uint8 = 1, Float16 = 2, Bfloat16 = 3, Qsint8 = 4 };
 
 inline size_t objtype_size(ObjType t) {
   switch (t) {
     case ObjType::Float: return 4;
-    case ObjType::Uint8: return 1;
+    case ObjType::Uint8:
+    case ObjType::Qsint8: return 1;
     default: return 2;
   }
 }

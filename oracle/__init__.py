@@ -32,8 +32,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
 
-OBJTYPES = {"Float-4": 0, "Integer-1": 1, "Float-2": 2}
-ELEM = {0: np.float32, 1: np.uint8, 2: np.float16}
+OBJTYPES = {"Float-4": 0, "Integer-1": 1, "Float-2": 2, "QSUInteger-8B": 3}
+ELEM = {0: np.float32, 1: np.uint8, 2: np.float16, 3: np.int8}
 METRICS = {"L1": 0, "L2": 1, "Hamming": 2, "Angle": 3, "Cosine": 4, "NormalizedAngle": 5,
            "NormalizedCosine": 6, "Jaccard": 7, "NormalizedL2": 9, "InnerProduct": 10,
            "Poincare": 100, "Lorentz": 101}
@@ -297,6 +297,8 @@ class Oracle:
         L.oracle_prepare_queries.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_uint32, ctypes.c_void_p,
                                              ctypes.c_size_t, ctypes.c_size_t, ctypes.c_void_p]
         L.oracle_rand_sequence.argtypes = [ctypes.c_uint32, ctypes.c_size_t, ctypes.c_void_p]
+        L.oracle_prepare_qsint8.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
+                                            ctypes.c_float, ctypes.c_void_p]
         L.oracle_distance.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
         L.oracle_distance.restype = ctypes.c_float
         L.oracle_qg_search.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
@@ -346,6 +348,10 @@ class Oracle:
     def prepare(self, queries: np.ndarray) -> np.ndarray:
         q = np.ascontiguousarray(queries, np.float32)
         rows = np.zeros((q.shape[0], self.f.dpad), self.f.dtype)
+        if self.f.otype == 3:
+            self.lib.oracle_prepare_qsint8(self.f.dpad, q.ctypes.data, q.shape[0], q.shape[1],
+                                           ctypes.c_float(float(self.f.prop["QuantizationScale"])), rows.ctypes.data)
+            return rows
         self.lib.oracle_prepare_queries(self.f.otype, self.f.metric, self.f.dpad, q.ctypes.data, q.shape[0],
                                         q.shape[1], rows.ctypes.data)
         return rows

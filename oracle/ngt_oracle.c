@@ -19,6 +19,11 @@
  *   glibc rand()      random_r TYPE_3 (degree 31, separation 3) as published
  *   query conversion  ObjectRepository::setObject lib/NGT/ObjectRepository.h:238-282,
  *                     ObjectSpace::normalize lib/NGT/ObjectSpace.h:356-384
+ *   qsint8 objects    ObjectSpace::quantizeSymmetrically lib/NGT/ObjectSpace.h:432-441
+ *                     (query codes), PrimitiveComparator::compareL2(qsint8)
+ *                     lib/NGT/PrimitiveComparatorX86.h:341-431 (the squared sum,
+ *                     no square root, in the x86 build), the updatable search's
+ *                     result-size rule for quantized objects lib/NGT/Graph.cpp:845-852
  */
 #include <float.h>
 #include <limits.h>
@@ -27,7 +32,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-enum { OT_FLOAT = 0, OT_UINT8 = 1, OT_HALF = 2 };
+enum { OT_FLOAT = 0, OT_UINT8 = 1, OT_HALF = 2, OT_QSINT8 = 3 };
 enum {
   M_L1 = 0, M_L2 = 1, M_HAMMING = 2, M_ANGLE = 3, M_COSINE = 4, M_NANGLE = 5, M_NCOSINE = 6,
   M_JACCARD = 7, M_NL2 = 9, M_IP = 10, M_POINCARE = 100, M_LORENTZ = 101
@@ -94,11 +99,12 @@ static inline double elem(const void *row, int ot, size_t i) {
   switch (ot) {
     case OT_FLOAT: return ((const float *)row)[i];
     case OT_UINT8: return ((const uint8_t *)row)[i];
+    case OT_QSINT8: return ((const int8_t *)row)[i];
     default: return half_to_double(((const uint16_t *)row)[i]);
   }
 }
 
-static size_t elem_size(int ot) { return ot == OT_FLOAT ? 4 : ot == OT_UINT8 ? 1 : 2; }
+static size_t elem_size(int ot) { return ot == OT_FLOAT ? 4 : (ot == OT_UINT8 || ot == OT_QSINT8) ? 1 : 2; }
 
 /* ---------------- comparators ---------------- */
 static float compare(int ot, int metric, const void *a, const void *b, size_t n) {
@@ -110,6 +116,7 @@ static float compare(int ot, int metric, const void *a, const void *b, size_t n)
         double x = elem(a, ot, i) - elem(b, ot, i);
         d += x * x;
       }
+      if (ot == OT_QSINT8) return (float)d;     /* squared sum of the codes' differences */
       return (float)sqrt(d);
     }
     case M_L1: {
@@ -358,7 +365,12 @@ static size_t graph_one(const OracleIndex *ix, const void *q, size_t k, size_t k
   float coef = epsilon + 1.0f;
   if (coef == 0.0f) coef = 1.1f;
   size_t size = k, size_backup = 0;
-  if (ix->epsilon_type == 2) { size_backup = k; size = (size_t)roundf(coef * (float)k); }
+  /* EpsilonType ResultSize, and the updatable search over quantized objects with
+   * EpsilonType None (lib/NGT/Graph.cpp:845-852) */
+  if (ix->epsilon_type == 2 || (mode != 0 && ix->epsilon_type == 0 && ix->otype == OT_QSINT8)) {
+    size_backup = k;
+    size = (size_t)roundf(coef * (float)k);
+  }
   float radius = radius0 < 0.0f ? FLT_MAX : radius0;
   size_t esz = edge_size_for(ix, edge_size, coef);
   float expcoef = size_backup ? 1.0f : coef;
@@ -479,6 +491,20 @@ static uint16_t float_to_half(float f) {
 
 /* Query conversion: cast to the object type, normalise (float sum, sqrt,
  * divide, in the object type) for the normalised metrics. */
+/* qsint8 query codes: round(v / scale x 127.5) clamped to [-127, 127], the division in
+ * float and the product and rounding in double (lib/NGT/ObjectSpace.h:432-441). */
+void oracle_prepare_qsint8(uint32_t dpad, const float *q, size_t nq, size_t dim, float scale, int8_t *rows) {
+  memset(rows, 0, nq * dpad);
+  for (size_t i = 0; i < nq; i++)
+    for (size_t j = 0; j < dim; j++) {
+      float fv = q[i * dim + j];
+      fv = (float)round((double)(fv / scale) * 127.5);
+      fv = fv < -127.0f ? -127.0f : fv;
+      fv = fv > 127.0f ? 127.0f : fv;
+      rows[i * dpad + j] = (int8_t)fv;
+    }
+}
+
 void oracle_prepare_queries(int ot, int metric, uint32_t dpad, const float *q, size_t nq, size_t dim, void *rows) {
   size_t rb = (size_t)dpad * elem_size(ot);
   memset(rows, 0, nq * rb);

@@ -124,6 +124,14 @@ FIXTURES = {
         create="-d 32 -o f -D 2 -E 10 -S 40 -i t", regenerate_obj=True, otype="f",
         prf_set={"EpsilonType": "ResultSize"},
         settings=[("graph", 10, 0.1, None, "ro"), ("graph", 10, 0.2, None, "rw")]),
+    # Scalar-quantized objects (ObjectType QSUInteger-8B): int8 codes
+    # rint(x / QuantizationScale x 127.5), the query quantized the same way
+    "qs8_l2": dict(
+        base=("gaussian_mixture", dict(n=2000, dim=32, nclusters=16, seed_means=191, seed=192)),
+        query=("gaussian_mixture", dict(n=200, dim=32, nclusters=16, seed_means=191, seed=193)),
+        create="-d 32 -o qsu8 -D 2 -E 10 -S 40 -i t", regenerate_obj=False, otype="q",
+        settings=[("graph", 10, 0.1, None, "ro"), ("graph", 10, 0.02, None, "ro"), ("graph", 20, 0.2, None, "rw"),
+                  ("linear", 10, 0.0, None, "ro")]),
     # Quantized graphs (ngtqg_search_index_float); for "qg" settings the edge
     # column holds the result expansion.
     "qg_f32_l2_d32": dict(

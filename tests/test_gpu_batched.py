@@ -17,7 +17,7 @@ pytestmark = pytest.mark.gpu
 
 KERNEL_BATCHED = 1
 KERNEL_WIDE = 3
-WIDE_CASES = {"c1_f32_l2", "c1_f32_l2_onng", "u8_l2"}      # float L2 and uint8 L2 indexes
+WIDE_CASES = {"c1_f32_l2", "c1_f32_l2_onng", "u8_l2", "qs8_l2"}      # float, uint8 and int8-code L2 indexes
 
 
 @pytest.fixture(scope="module")
@@ -38,7 +38,7 @@ def _tie_aware_recall(ids, counts, gt_d, k, qrows, objects, metric_fn):
 # (fixture, graph setting, linear setting).  Epsilon <= 0.2: with its bounded
 # candidate list the batched kernel explores at least what the reference does.
 CASES = [("c1_f32_l2", 0, 10), ("c1_f32_l2", 2, 10), ("c1_f32_l2_onng", 0, 11), ("u8_l2", 0, 2),
-         ("u8_l1", 0, 1), ("f32_cosine", 0, 1), ("f32_ncosine", 0, 1), ("f16_l2", 0, 1)]
+         ("u8_l1", 0, 1), ("f32_cosine", 0, 1), ("f32_ncosine", 0, 1), ("f16_l2", 0, 1), ("qs8_l2", 0, 3)]
 
 
 @pytest.mark.parametrize("kernel", [KERNEL_BATCHED, KERNEL_WIDE])
@@ -46,7 +46,7 @@ CASES = [("c1_f32_l2", 0, 10), ("c1_f32_l2", 2, 10), ("c1_f32_l2_onng", 0, 11), 
 def test_batched_recall_not_below_reference(name, graph_setting, linear_setting, kernel, workdir):
     from ngt_gb300 import Index
     if kernel == KERNEL_WIDE and name not in WIDE_CASES:
-        pytest.skip("the wide kernel is built for float L2 and uint8 L2 indexes")
+        pytest.skip("the wide kernel is built for L2 indexes of float, uint8 and int8-code objects")
     path, meta, queries, golden = materialize(name, workdir)
     s = meta["settings"][graph_setting]
     k, eps, nq = s["k"], s["epsilon"], s["nq"]

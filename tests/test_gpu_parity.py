@@ -61,7 +61,7 @@ def test_batch_search_matches_reference(name, workdir):
         _check(name, s, ids, ds, n, gi, gd, gc)
 
 
-@pytest.mark.parametrize("name", ["c1_f32_l2", "u8_l2"])
+@pytest.mark.parametrize("name", ["c1_f32_l2", "u8_l2", "qs8_l2"])
 def test_single_query_capi_matches_reference(name, workdir):
     """ngt_search_index_as_float one query at a time (the reference's own call)."""
     from ngt_gb300 import Index
