@@ -9,9 +9,13 @@ Workload (the benchmark's plain-vs-batched graph-search configuration):
            opened read-only through the C ABI (ngt_open_index_as_read_only)
   search   k = 10, each kernel at the smallest epsilon of a sweep (0 .. 0.3)
            whose recall@10 against the exact ground truth is >= 0.95:
-           the batched kernel (warp per query, bf16 rows, exact fp32 re-rank; the
-           headline `value`) and the plain fp32 one-query-per-CTA kernel (the
-           reference-order search; reported in config.plain_fp32)
+           the batched kernel (the autotuner's fastest of the warp-per-query and
+           CTA-per-query kernels and their settings; 8-bit or bf16 search rows,
+           exact fp32 re-rank; the headline `value`) and the plain fp32
+           one-query-per-CTA kernel (the reference-order search; reported in
+           config.plain_fp32).  Also reported: the serving loop's latency, the
+           quantized-graph search and scalar-quantized (QSUInteger-8B) objects
+           over the same graph.
 
 A step is one pass of all queries through the search.  `value` is queries/s
 with queries resident in HBM (ngtgpu_search_batch_device); `e2e` is the same
@@ -41,6 +45,9 @@ sys.path.insert(0, ROOT)
 
 EPS_SWEEP = [0.0, 0.02, 0.04, 0.06, 0.07, 0.075, 0.08, 0.085, 0.09, 0.1, 0.12, 0.15, 0.2, 0.3]
 RECALL_TARGET = 0.95
+# epsilon sweep of the scalar-quantized objects (their distances are squared, so the
+# exploration coefficient bites later)
+QS8_EPS_SWEEP = [0.08, 0.1, 0.11, 0.12, 0.13, 0.14, 0.15, 0.17, 0.2, 0.25, 0.3]
 # Batched-kernel candidates of the autotuner.  kernel 1: warp per query (R rows per
 # lane group in flight, registers budgeted for C CTAs per SM, NB neighbour slots per
 # step; 0 = automatic); kernel 3: CTA per query (T threads, `stage` KB of staged rows).
@@ -79,6 +86,8 @@ def parse():
                     help="offered query rates of the serving measurement")
     ap.add_argument("--served-seconds", type=float, default=2.0, help="length of each served-rate run")
     ap.add_argument("--qg", type=int, default=1, help="also measure the quantized-graph search (1) or not (0)")
+    ap.add_argument("--qs8", type=int, default=1,
+                    help="also measure scalar-quantized (QSUInteger-8B) objects on the same graph (1) or not (0)")
     ap.add_argument("--fixed", default=None,
                     help="EPS_PLAIN:EPS_BATCHED -- skip the epsilon / tuning sweeps (profiling runs)")
     ap.add_argument("--fixed-config", default='{"kernel": 3, "L": 256, "P": 8, "T": 128, "stage": 16}',
@@ -318,6 +327,72 @@ def qg_measurement(path, base, queries, kth, k, steps, warmup, log_fn):
            "mean_expansions": round(float(stats["expansions"].mean()), 1),
            "mean_quantized_distances": round(float(stats["distance_computations"].mean()), 1),
            "achieved_gbs": round(float(bytes_q.sum() / (statistics.median(ms) / 1e3) / 1e9), 1)}
+    ix.close()
+    return out
+
+
+def qs8_measurement(path, base, queries, k, steps, warmup, log_fn):
+    """Scalar-quantized objects (ObjectType QSUInteger-8B, L2) over the same graph: int8
+    codes with the reference's symmetric quantization (scale = max |x|), queries coded the
+    same way, distances = squared code differences.  Recall against the exact k-NN in the
+    code space (what the reference's own linear search returns for this index); the plain
+    exact-order kernel and the CTA-per-query kernel, each at the smallest epsilon of the
+    sweep reaching the target, timed with queries in HBM."""
+    import torch
+    from ngt_gb300 import Index, graph_build
+    from ngt_gb300.base import KERNEL_EXACT, KERNEL_WIDE, QUERY_STATS_DTYPE
+    qpath = path + "_qs8"
+    if not os.path.exists(os.path.join(qpath, "grp")):
+        graph_build.write_qsint8_index(qpath, path, base, log=log_fn)
+    with open(os.path.join(qpath, "prf")) as f:
+        scale = float(dict(l.rstrip("\n").split("\t", 1) for l in f if "\t" in l)["QuantizationScale"])
+    cb = graph_build.quantize_symmetric(base, scale).astype(np.float32)
+    cq = graph_build.quantize_symmetric(queries, scale).astype(np.float32)
+    kth = ground_truth(cb, cq, k)
+    ix = Index(qpath, read_only=True)
+    nq = len(queries)
+    rows = torch.from_numpy(ix.convert_queries(queries)).cuda()
+    res = torch.zeros((nq, k, 2), dtype=torch.int32, device="cuda")
+    cnt = torch.zeros(nq, dtype=torch.int32, device="cuda")
+    st = torch.zeros((nq, QUERY_STATS_DTYPE.itemsize // 4), dtype=torch.int32, device="cuda")
+    stream = torch.cuda.Stream()
+
+    def run(kernel, eps, nsteps, n, warm):
+        params, nparams = ix.make_params(k, eps)
+        with torch.cuda.stream(stream):
+            for _ in range(warm):
+                ix.search_device(rows.data_ptr(), n, params, nparams, res.data_ptr(), k, cnt.data_ptr(),
+                                 st.data_ptr(), stream=stream.cuda_stream, kernel=kernel)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(nsteps)]
+        with torch.cuda.stream(stream):
+            for a, b in ev:
+                a.record(stream)
+                ix.search_device(rows.data_ptr(), n, params, nparams, res.data_ptr(), k, cnt.data_ptr(),
+                                 st.data_ptr(), stream=stream.cuda_stream, kernel=kernel)
+                b.record(stream)
+        torch.cuda.synchronize()
+        ms = statistics.median([a.elapsed_time(b) for a, b in ev])
+        ids = res[:n, :, 0].cpu().numpy().view(np.uint32)
+        c = cnt[:n].cpu().numpy().astype(np.int64)
+        return n / (ms / 1e3), recall(cb, cq[:n], ids, c, kth[:n], k)
+
+    out = {"object_type": "QSUInteger-8B (int8 codes, scale %g)" % scale,
+           "recall_basis": "exact k-NN over the codes", "graph": "the float index's ONNG"}
+    cal = min(2000, nq)
+    ix.set_batched_tuning(list_capacity=256, parents=8, cta_threads=128, stage_kilobytes=16)
+    for name, kernel in (("plain_exact", KERNEL_EXACT), ("batched", KERNEL_WIDE)):
+        eps_sel = QS8_EPS_SWEEP[-1]
+        for eps in QS8_EPS_SWEEP:
+            qps, r = run(kernel, eps, 1, cal, 1)
+            log_fn("qs8 kernel %d epsilon %.3f recall@%d %.4f" % (kernel, eps, k, r))
+            if r >= RECALL_TARGET:
+                eps_sel = eps
+                break
+        qps, r = run(kernel, eps_sel, steps, nq, warmup)
+        out[name] = {"qps": round(qps, 1), "epsilon": eps_sel, "recall_at_k": round(r, 4)}
+        log_fn("qs8 %s: %.1f q/s at epsilon %g, recall %.4f" % (name, qps, eps_sel, r))
+    out["speedup_batched_vs_plain"] = round(out["batched"]["qps"] / max(out["plain_exact"]["qps"], 1e-9), 3)
     ix.close()
     return out
 
@@ -570,6 +645,16 @@ def main():
             qg = {"error": str(ex)}
             log("qg measurement failed: %s" % ex)
 
+    # ---- scalar-quantized objects on the same graph (rank 0) -----------------------------------
+    qs8 = None
+    if args.qs8 and rank == 0 and world == 1:
+        try:
+            qs8 = qs8_measurement(path, base, queries, k, max(3, args.steps // 3), args.warmup, log)
+            log("qs8: %s" % qs8)
+        except Exception as ex:                 # reported, never fatal to the headline measurement
+            qs8 = {"error": str(ex)}
+            log("qs8 measurement failed: %s" % ex)
+
     # ---- CPU baseline (oracle port on a bounded sample) ------------------------------------------
     cpu = None
     if rank == 0:
@@ -621,6 +706,7 @@ def main():
                        "rates": served,
                        "warp_per_query_kernel_rates": served_warp} if served else None,
             "quantized_graph": qg,
+            "scalar_quantized": qs8,
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

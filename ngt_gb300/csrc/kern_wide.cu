@@ -14,13 +14,14 @@ WideKernelFn wide_kernel(ObjType ot, Metric m, SearchRows rows, uint32_t threads
   if (ot == ObjType::Float && rows == SearchRows::Sq8 && m == Metric::L2)
     return threads == 128 ? &graph_search_wide_kernel<ObjType::Uint8, ObjType::Float, Metric::L2, 128>
                           : &graph_search_wide_kernel<ObjType::Uint8, ObjType::Float, Metric::L2, 256>;
+  if (ot == ObjType::Qsint8 && rows == SearchRows::Native && m == Metric::L2)
+    return threads == 128 ? &graph_search_wide_kernel<ObjType::Qsint8, ObjType::Qsint8, Metric::L2, 128>
+                          : &graph_search_wide_kernel<ObjType::Qsint8, ObjType::Qsint8, Metric::L2, 256>;
   if (threads != 256 || rows != SearchRows::Native) return nullptr;
   if (ot == ObjType::Float && m == Metric::L2)
     return &graph_search_wide_kernel<ObjType::Float, ObjType::Float, Metric::L2, 256>;
   if (ot == ObjType::Uint8 && m == Metric::L2)
     return &graph_search_wide_kernel<ObjType::Uint8, ObjType::Uint8, Metric::L2, 256>;
-  if (ot == ObjType::Qsint8 && m == Metric::L2)
-    return &graph_search_wide_kernel<ObjType::Qsint8, ObjType::Qsint8, Metric::L2, 256>;
   return nullptr;
 }
 

@@ -32,8 +32,9 @@ size_t qbg_kernel_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, cons
 struct WideConfig;
 typedef void (*WideKernelFn)(DevGraph, const uint4*, const uint4*, uint32_t, const QueryParams*, const uint32_t*,
                              ObjDist*, uint32_t*, QueryStats*, uint32_t*, uint32_t*, unsigned long long*, WideConfig);
-// CTA-per-query batched kernel with `threads` per CTA: 256 for float L2 (bf16 or
-// fp32 search rows) and uint8 L2, 128 also for float L2 on bf16 rows; nullptr otherwise.
+// CTA-per-query batched kernel with `threads` per CTA: 256 for float L2 (bf16,
+// 8-bit or fp32 search rows), uint8 L2 and int8-code L2; 128 also for float L2 on
+// bf16 or 8-bit rows and for int8-code L2; nullptr otherwise.
 WideKernelFn wide_kernel(ObjType ot, Metric m, SearchRows rows, uint32_t threads = 256);
 // float rows (dpad per row, `dim` valid) -> 8-bit codes rint((x - offset) / scale), 0 past dim
 void launch_float_rows_to_sq8(const float* in, uint8_t* out, size_t nrows, uint32_t dpad, uint32_t dim, float offset,

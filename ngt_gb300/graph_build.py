@@ -26,6 +26,7 @@ reference ONNG it searches with the dynamic edge size (EdgeSizeForSearch -2:
 from __future__ import annotations
 
 import os
+import shutil
 import time
 
 import numpy as np
@@ -154,3 +155,42 @@ def build_onng_index(path: str, x: np.ndarray, k: int = 100, outgoing: int = 10,
     write_index(path, x, offsets, edges, dists)
     log("index written to %s in %.1f s total" % (path, time.time() - t0))
     return ids
+
+
+def quantize_symmetric(x: np.ndarray, scale: float) -> np.ndarray:
+    """int8 codes of NGT's scalar quantization (ObjectSpace::quantizeSymmetrically,
+    lib/NGT/ObjectSpace.h:432-441): the division in float32, the product with 127.5
+    and the rounding (half away from zero) in float64, clamped to [-127, 127]."""
+    v = (np.asarray(x, np.float32) / np.float32(scale)).astype(np.float64) * 127.5
+    r = np.sign(v) * np.floor(np.abs(v) + 0.5)
+    return np.clip(r, -127, 127).astype(np.int8)
+
+
+def write_qsint8_index(path: str, float_index: str, x: np.ndarray, log=print) -> float:
+    """A QSUInteger-8B (scalar-quantized, L2) graph-only index at `path` over the
+    objects x, with the graph of the float index at `float_index`.  The scale is
+    max(|max|, |min|) of the objects (NGT::Index::setQuantizationFromMaxMin,
+    lib/NGT/Index.cpp:864-875, clipping rate 0).  Returns the scale."""
+    t0 = time.time()
+    os.makedirs(path, exist_ok=True)
+    scale = float(max(abs(float(x.max())), abs(float(x.min()))))
+    n, dim = x.shape
+    with open(os.path.join(float_index, "prf")) as f:
+        prf = dict(line.rstrip("\n").split("\t", 1) for line in f if "\t" in line)
+    prf.update({"ObjectType": "QSUInteger-8B", "QuantizationScale": "%.9g" % scale, "QuantizationOffset": "0",
+                "QuantizationClippingRate": "0"})
+    with open(os.path.join(path, "prf"), "w") as f:
+        for kk in sorted(prf):
+            f.write("%s\t%s\n" % (kk, prf[kk]))
+    rec = np.empty((n, 1 + dim), np.uint8)
+    rec[:, 0] = ord("+")
+    for a in range(0, n, 1 << 18):
+        rec[a:a + (1 << 18), 1:] = quantize_symmetric(x[a:a + (1 << 18)], scale).view(np.uint8)
+    with open(os.path.join(path, "obj"), "wb") as f:
+        f.write(np.uint64(n + 1).tobytes())
+        f.write(b"-")
+        f.write(rec.tobytes())
+    shutil.copyfile(os.path.join(float_index, "grp"), os.path.join(path, "grp"))
+    log("qsint8 index written to %s in %.1f s (scale %g)" % (path, time.time() - t0, scale))
+    return scale
+
