@@ -5,11 +5,13 @@
 // over the CTA so that one query moves many rows at once:
 //   * the P parents' edge slots are read, filtered against the query's
 //     visited bitmap and compacted by all threads of the CTA (128 or 256);
-//   * the new neighbours' search rows are copied into shared memory with
-//     asynchronous 16-byte copies (cp.async), all of a round in flight at once,
-//     and their distances computed from shared memory;
-//   * the survivors are sorted (bitonic, CTA-wide) and merged into the list by
-//     per-entry binary searches into a second buffer.
+//   * the new neighbours' search rows (bf16 or 8-bit copies of float objects, or
+//     the objects themselves) are copied into a shared-memory stage with 16-byte
+//     cp.async in two halves, the next half in flight while the current one is
+//     scored, several rows per lane group at once;
+//   * every survivor's place in the list is its rank among the new keys (counted
+//     when there are at most T of them, else after a CTA bitonic sort) plus its
+//     rank in the list; keys land in a second list buffer.
 // One warp (warp 0) owns the control decisions (parent selection, the refill
 // from the spill tier), exactly as the warp-per-query kernel makes them.
 // Per-query latency is set by a few memory round trips per iteration instead of
