@@ -165,6 +165,7 @@ GraphEngine::GraphEngine(const std::string& qbg_dir, bool blobs) : mode_(GraphMo
 
 GraphEngine::~GraphEngine() {
   cudaSetDevice(device_);
+  if (staging_) cudaFreeHost(staging_);
   cudaFree(d_objects_);
   cudaFree(d_offsets_);
   cudaFree(d_edges_);
@@ -358,16 +359,27 @@ size_t GraphEngine::output_size(const SearchArgs& a) const {
 
 void GraphEngine::convert_queries(const void* queries, QueryType qt, size_t nq, size_t qdim,
                                   std::vector<uint8_t>& rows) const {
+  rows.resize(nq * host_.row_bytes());
+  convert_queries(queries, qt, nq, qdim, rows.data());
+}
+
+void GraphEngine::convert_queries(const void* queries, QueryType qt, size_t nq, size_t qdim, uint8_t* rows) const {
   const size_t user_dim = (size_t)host_.prop.dimension;
   if (qdim != host_.dim && !(host_.prop.metric == Metric::InnerProduct && qdim == user_dim))
     throw std::runtime_error("the query dimension " + std::to_string(qdim) + " differs from the index dimension " +
                              std::to_string(user_dim));
   const size_t rb = host_.row_bytes();
-  rows.assign(nq * rb, 0);
+  std::memset(rows, 0, nq * rb);
   const bool norm = is_normalized(host_.prop.metric);
+  if (host_.prop.otype == ObjType::Float && qt == QueryType::Float32 && !norm) {
+    // float rows are the queries themselves, zero padded
+    const float* src = static_cast<const float*>(queries);
+    for (size_t q = 0; q < nq; q++) std::memcpy(rows + q * rb, src + q * qdim, qdim * sizeof(float));
+    return;
+  }
   std::vector<float> tmp(qdim);
   for (size_t q = 0; q < nq; q++) {
-    uint8_t* dst = rows.data() + q * rb;
+    uint8_t* dst = rows + q * rb;
     for (size_t i = 0; i < qdim; i++) tmp[i] = (float)query_elem(queries, qt, q * qdim + i);
     switch (host_.prop.otype) {
       case ObjType::Float: {
@@ -730,8 +742,17 @@ void GraphEngine::launch_fast(const uint4* d_rows, size_t nq, const QueryParams*
 void GraphEngine::search(const void* queries, QueryType qt, size_t nq, size_t qdim, const SearchArgs* args,
                          size_t nargs, SearchOutput& out, Kernel kernel) {
   NGT_CUDA(cudaSetDevice(device_));
-  std::vector<uint8_t> rows;
-  convert_queries(queries, qt, nq, qdim, rows);
+  std::lock_guard<std::mutex> staging(staging_mu_);
+  // the query rows are converted straight into a pinned staging buffer (kept between calls)
+  const size_t row_total = nq * host_.row_bytes();
+  if (staging_bytes_ < row_total) {
+    if (staging_) NGT_CUDA(cudaFreeHost(staging_));
+    staging_ = nullptr;
+    staging_bytes_ = 0;
+    NGT_CUDA(cudaMallocHost(&staging_, std::max<size_t>(row_total, 1)));
+    staging_bytes_ = std::max<size_t>(row_total, 1);
+  }
+  convert_queries(queries, qt, nq, qdim, static_cast<uint8_t*>(staging_));
   size_t kmax = 1;
   for (size_t i = 0; i < nargs; i++) kmax = std::max(kmax, output_size(args[i]));
   out.kmax = kmax;
@@ -744,11 +765,11 @@ void GraphEngine::search(const void* queries, QueryType qt, size_t nq, size_t qd
   uint32_t* d_counts = nullptr;
   QueryStats* d_stats = nullptr;
   cudaStream_t s = stream_;
-  NGT_CUDA(cudaMallocAsync(&d_rows, rows.size(), s));
+  NGT_CUDA(cudaMallocAsync(&d_rows, row_total, s));
   NGT_CUDA(cudaMallocAsync(&d_out, nq * kmax * sizeof(ObjDist), s));
   NGT_CUDA(cudaMallocAsync(&d_counts, nq * 4, s));
   NGT_CUDA(cudaMallocAsync(&d_stats, nq * sizeof(QueryStats), s));
-  NGT_CUDA(cudaMemcpyAsync(d_rows, rows.data(), rows.size(), cudaMemcpyHostToDevice, s));
+  NGT_CUDA(cudaMemcpyAsync(d_rows, staging_, row_total, cudaMemcpyHostToDevice, s));
   search_device(d_rows, nq, args, nargs, d_out, d_counts, d_stats, kmax, s, kernel);
   NGT_CUDA(cudaMemcpyAsync(out.results.data(), d_out, nq * kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, s));
   NGT_CUDA(cudaMemcpyAsync(out.counts.data(), d_counts, nq * 4, cudaMemcpyDeviceToHost, s));

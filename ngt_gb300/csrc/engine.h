@@ -129,6 +129,7 @@ class GraphEngine {
   // allocateObject does (cast to the object type, normalisation for the
   // normalised metrics, zero augmentation for inner product).
   void convert_queries(const void* queries, QueryType qt, size_t nq, size_t qdim, std::vector<uint8_t>& rows) const;
+  void convert_queries(const void* queries, QueryType qt, size_t nq, size_t qdim, uint8_t* rows) const;
 
   // Device-side entry used by the batched extension: queries already converted
   // and resident on the device.
@@ -225,6 +226,9 @@ class GraphEngine {
   int device_ = 0;
   cudaStream_t stream_ = nullptr;
   std::mutex mu_;
+  std::mutex staging_mu_;                                 // the pinned query staging of search()
+  void* staging_ = nullptr;
+  size_t staging_bytes_ = 0;
   uint64_t launches_ = 0;
   // device data
   void* d_objects_ = nullptr;
