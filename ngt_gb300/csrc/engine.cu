@@ -267,6 +267,7 @@ void GraphEngine::build_params(const SearchArgs* args, size_t nargs, size_t nq, 
   seed_list.clear();
   max_size = 0;
   const Property& p = host_.prop;
+  uint32_t shared_seeds = UINT32_MAX;
   for (size_t i = 0; i < nq; i++) {
     const SearchArgs& a = args[nargs == 1 ? 0 : i];
     QueryParams qp{};
@@ -289,14 +290,15 @@ void GraphEngine::build_params(const SearchArgs* args, size_t nargs, size_t nq, 
     qp.coef = coef;
     qp.edge_size = (uint32_t)std::min<size_t>(edge_size_for(a), 0xffffffffu);
     qp.out_off = (uint32_t)(i * kmax);
-    seed_params(a.size, qp.seed_off, qp.seed_cnt, seed_list);
+    seed_params(a.size, qp.seed_off, qp.seed_cnt, seed_list, &shared_seeds);
     params[i] = qp;
     max_size = std::max<uint32_t>(max_size, qp.size);
   }
   if (seed_list.empty()) seed_list.push_back(0);
 }
 
-void GraphEngine::seed_params(size_t k, uint32_t& seed_off, uint32_t& seed_cnt, std::vector<uint32_t>& seed_list) {
+void GraphEngine::seed_params(size_t k, uint32_t& seed_off, uint32_t& seed_cnt, std::vector<uint32_t>& seed_list,
+                              uint32_t* shared_off) {
   const Property& p = host_.prop;
   if (p.has_tree) {
     // GraphAndTreeIndex::getSeedsFromTree: seedSize = SeedSize or size, capped by size;
@@ -320,21 +322,28 @@ void GraphEngine::seed_params(size_t k, uint32_t& seed_off, uint32_t& seed_cnt, 
   } else {
     // getRandomSeeds draws from the process-global rand() without reseeding;
     // here every query draws from a generator seeded with 1 so that results
-    // are reproducible.
-    GlibcRand rng(1);
-    std::vector<uint32_t> chosen;
-    size_t empty = 0;
-    while (chosen.size() < ss) {
-      double r = rng.unit();
-      size_t idx = (size_t)std::floor((double)n * r) + 1;
-      if (!host_.present[idx]) {
-        if (++empty > n) break;
-        continue;
+    // are reproducible -- the same seeds for every query, drawn once.
+    std::call_once(random_seeds_once_, [&] {
+      GlibcRand rng(1);
+      size_t empty = 0;
+      while (random_seeds_.size() < ss) {
+        double r = rng.unit();
+        size_t idx = (size_t)std::floor((double)n * r) + 1;
+        if (!host_.present[idx]) {
+          if (++empty > n) break;
+          continue;
+        }
+        if (std::find(random_seeds_.begin(), random_seeds_.end(), (uint32_t)idx) != random_seeds_.end()) continue;
+        random_seeds_.push_back((uint32_t)idx);
       }
-      if (std::find(chosen.begin(), chosen.end(), (uint32_t)idx) != chosen.end()) continue;
-      chosen.push_back((uint32_t)idx);
+    });
+    if (shared_off && *shared_off != UINT32_MAX) {
+      seed_off = *shared_off;
+      seed_cnt = (uint32_t)random_seeds_.size();
+      return;
     }
-    seed_list.insert(seed_list.end(), chosen.begin(), chosen.end());
+    seed_list.insert(seed_list.end(), random_seeds_.begin(), random_seeds_.end());
+    if (shared_off) *shared_off = seed_off;
   }
   seed_cnt = (uint32_t)(seed_list.size() - seed_off);
 }

@@ -181,7 +181,12 @@ class GraphEngine {
   void build_params(const SearchArgs* args, size_t nargs, size_t nq, size_t kmax, std::vector<QueryParams>& params,
                     std::vector<uint32_t>& seed_list, uint32_t& max_size);
   // Seeds of one query of requested size k: tree seeds thinned to k, or graph seeds.
-  void seed_params(size_t k, uint32_t& seed_off, uint32_t& seed_cnt, std::vector<uint32_t>& seed_list);
+  // shared_off: when given, queries of one launch share one copy of the graph-only
+  // random seeds (UINT32_MAX before the first)
+  void seed_params(size_t k, uint32_t& seed_off, uint32_t& seed_cnt, std::vector<uint32_t>& seed_list,
+                   uint32_t* shared_off = nullptr);
+  std::once_flag random_seeds_once_;
+  std::vector<uint32_t> random_seeds_;                    // graph-only index: the seeds of rand() seeded with 1
   size_t edge_size_for(const SearchArgs& a) const;
   void ensure_scratch(size_t grid);
   void ensure_fast_scratch(FastScratch& sc, size_t slots, cudaStream_t stream);
