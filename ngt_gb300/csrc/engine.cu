@@ -601,13 +601,19 @@ void GraphEngine::search_device_slot(const uint4* d_rows, size_t nq, const Searc
   // the pageable host parameter copies above are complete once they return
 }
 
+// Shared-memory visited hash of the exact-order kernels (QG included): a query moves
+// its visited set to the global bitmap once the hash is half full, which every
+// query of a large index does after a few thousand visits, so large indexes get a
+// small hash (more CTAs per SM) and small ones a large hash (no bitmap at all).
+uint32_t GraphEngine::visited_hash_capacity() const { return host_.nrows >= (1u << 18) ? 2048u : 8192u; }
+
 void GraphEngine::launch_exact(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
                                uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats,
                                cudaStream_t stream) {
   ExactConfig cfg{};
   cfg.kcap = max_size + 1;
   cfg.ccap = 1024;
-  cfg.hcap = 8192;
+  cfg.hcap = visited_hash_capacity();
   cfg.mode = (uint32_t)mode_;
   cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));
   cfg.bitmap_words = (host_.nrows + 31) / 32;
@@ -875,7 +881,7 @@ void GraphEngine::search_device_noalloc(void* scratch, size_t scratch_bytes, con
   ExactConfig cfg{};
   cfg.kcap = max_size + 1;
   cfg.ccap = 1024;
-  cfg.hcap = 8192;
+  cfg.hcap = visited_hash_capacity();
   cfg.mode = (uint32_t)mode_;
   cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));
   cfg.bitmap_words = (host_.nrows + 31) / 32;
@@ -1002,7 +1008,7 @@ void GraphEngine::qg_search_device(const uint4* d_rows, size_t nq, const QGArgs*
   ExactConfig cfg{};
   cfg.kcap = max_size + 1;
   cfg.ccap = 1024;
-  cfg.hcap = 8192;
+  cfg.hcap = visited_hash_capacity();
   cfg.mode = (uint32_t)GraphMode::Updatable;
   cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));
   cfg.bitmap_words = (host_.nrows + 31) / 32;
