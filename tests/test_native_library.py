@@ -99,6 +99,23 @@ def test_loader_rejects_damaged_index(lib, tmp_path, damage):
     assert "CUDA" not in msg, msg
 
 
+@pytest.mark.parametrize("damage", ["cosine", "no_scale", "zero_scale"])
+def test_loader_rejects_unsupported_scalar_quantized_index(lib, tmp_path, damage):
+    """QSUInteger-8B objects: L2 only, and a positive QuantizationScale is required."""
+    path, meta, _, _ = materialize("qs8_l2", str(tmp_path))
+    prf = open(os.path.join(path, "prf")).read().splitlines()
+    if damage == "cosine":
+        prf = [l if not l.startswith("DistanceType\t") else "DistanceType\tCosine" for l in prf]
+    elif damage == "no_scale":
+        prf = [l for l in prf if not l.startswith("QuantizationScale\t")]
+    else:
+        prf = [l if not l.startswith("QuantizationScale\t") else "QuantizationScale\t0" for l in prf]
+    open(os.path.join(path, "prf"), "w").write("\n".join(prf) + "\n")
+    h, msg = _error_string(lib, "ngt_open_index_as_read_only", path)
+    assert h is None
+    assert "QSUInteger-8B" in msg, msg
+
+
 def test_null_arguments_return_false_with_message(lib):
     lib.ngt_create_error_object.restype = ctypes.c_void_p
     lib.ngt_get_error_string.restype = ctypes.c_char_p
