@@ -675,7 +675,8 @@ void GraphEngine::launch_wide(const uint4* d_rows, size_t nq, const QueryParams*
   // 64 KB of staged rows by default (two 256-thread CTAs share an SM)
   const uint32_t stage_bytes = (tuning_.stage_kb ? tuning_.stage_kb : 64u) * 1024u;
   cfg.stage_rows = std::max<uint32_t>(16, std::min<uint32_t>(512, stage_bytes / (cfg.search_chunks * 16)));
-  cfg.sgroup = std::min<uint32_t>(32, next_pow2((cfg.search_chunks + 1) / 2));
+  // two chunks per lane; one for 8-bit rows (whose unpacked query chunk is 16 floats)
+  cfg.sgroup = std::min<uint32_t>(32, next_pow2(sq8 ? cfg.search_chunks : (cfg.search_chunks + 1) / 2));
   cfg.ngroup = std::min<uint32_t>(32, next_pow2(dev_.row_chunks));
   cfg.rerank_x16 = (uint32_t)std::ceil(rf * 16.0f);
   cfg.bitmap_words = ((host_.nrows + 31) / 32 + 3) / 4 * 4;

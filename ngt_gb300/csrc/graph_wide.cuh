@@ -60,11 +60,17 @@ struct WideShared {
   unsigned long long wmin[kWideMaxWarps];
 };
 
+// 16-byte chunks of the row stage, which also holds the NB candidate keys
+__host__ __device__ inline size_t wide_stage_chunks(uint32_t search_chunks, uint32_t stage_rows, uint32_t nbr_cap) {
+  const size_t rows = (size_t)stage_rows * search_chunks, keys = ((size_t)nbr_cap * 8 + 15) / 16;
+  return rows > keys ? rows : keys;
+}
+
 inline size_t wide_smem_bytes(uint32_t row_chunks, const WideConfig& c) {
   size_t b = (size_t)row_chunks * 16 + (size_t)c.search_chunks * (c.sq8 ? 64 : 16);
   b += (size_t)c.list_cap * 16;                                   // list, double-buffered
-  b += (size_t)c.nbr_cap * 16;                                    // nkey, nid, nd
-  b += (size_t)c.stage_rows * c.search_chunks * 16;               // row staging
+  b += (size_t)c.nbr_cap * 8;                                     // nid, nd
+  b += wide_stage_chunks(c.search_chunks, c.stage_rows, c.nbr_cap) * 16;   // row staging / nkey
   b += sizeof(WideShared) + 16;
   return b;
 }
@@ -195,7 +201,7 @@ struct WideDot {
 
 // T: threads per CTA (128 or 256), one query per CTA.
 template <ObjType ST, ObjType OT, Metric M, int T>
-__global__ void __launch_bounds__(T, T == 128 ? 5 : 2)
+__global__ void __launch_bounds__(T, T == 128 ? 6 : 2)
 graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint4* __restrict__ queries,
                          uint32_t nq, const QueryParams* __restrict__ params, const uint32_t* __restrict__ seed_list,
                          ObjDist* __restrict__ out, uint32_t* __restrict__ out_count, QueryStats* __restrict__ stats,
@@ -209,11 +215,13 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
   typedef WideDot<ST, OT, M> Dot;
   uint4* qs = qn + rc;                                                           // sc (x 4 for Sq8) chunks
   unsigned long long* lists = reinterpret_cast<unsigned long long*>(qs + (Dot::kSq8 ? 4 * sc : sc));   // 2 x L
-  unsigned long long* nkey = lists + 2 * (size_t)L;
-  uint32_t* nid = reinterpret_cast<uint32_t*>(nkey + NB);
+  uint32_t* nid = reinterpret_cast<uint32_t*>(lists + 2 * (size_t)L);
   float* nd = reinterpret_cast<float*>(nid + NB);
   uint4* stage = reinterpret_cast<uint4*>(nd + NB);
-  WideShared& s = *reinterpret_cast<WideShared*>(stage + (size_t)SR * sc);
+  // the candidate keys share the row stage: rows are staged only inside a score
+  // phase, keys are built after it and consumed before the next one
+  unsigned long long* nkey = reinterpret_cast<unsigned long long*>(stage);
+  WideShared& s = *reinterpret_cast<WideShared*>(stage + wide_stage_chunks(sc, SR, NB));
   uint32_t* bitmap = bitmaps + (size_t)blockIdx.x * cfg.bitmap_words;
   unsigned long long* spill = spills + (size_t)blockIdx.x * 2 * cfg.spill_cap;
   unsigned long long* spill_tmp = spill + cfg.spill_cap;
@@ -250,7 +258,8 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
   auto score = [&](uint32_t cnt) {
     if (cnt == 0) return;
     // the query chunks this lane reads (c = sgl + j * SG), negated and unpacked once
-    constexpr int kQC = 2;   // the host sets sgroup so that every lane reads at most two chunks
+    // the host sets sgroup so that every lane reads at most two chunks (one for 8-bit rows)
+    constexpr int kQC = Dot::kSq8 ? 1 : 2;
     float2 nqc[kQC][Dot::NQ];
     if constexpr (Dot::kOn) {
 #pragma unroll
