@@ -64,7 +64,7 @@ WIDE_PARENTS = 24                 # parents per step of the CTA-per-query kernel
 # launch to give roofline.traffic; the workload's DC per query is the same at
 # every batch size.
 DRAM_BYTES_PER_QUERY = {1: 10.56e9 / 2000,      # batched kernel id -> measured bytes per query
-                        3: 5.086e9 / 2000}      # (kernel 3: 8-bit search rows, its default configuration)
+                        3: 5.893e9 / 2000}      # (kernel 3: 8-bit search rows, its default configuration)
 
 
 def log(*a):
