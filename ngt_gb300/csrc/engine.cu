@@ -490,6 +490,13 @@ void GraphEngine::reserve_scratch_sets(size_t n) {
   if (fast_scratch_.size() < n) fast_scratch_.resize(n);
 }
 
+void GraphEngine::reserve_scratch_slots(size_t set, size_t slots) {
+  std::lock_guard<std::mutex> lock(mu_);
+  if (set >= fast_scratch_.size()) fast_scratch_.resize(set + 1);
+  NGT_CUDA(cudaSetDevice(device_));
+  ensure_fast_scratch(fast_scratch_[set], slots, stream_);
+}
+
 size_t GraphEngine::batched_scratch_bytes(size_t nq) const {
   size_t words = ((host_.nrows + 31) / 32 + 3) / 4 * 4;
   return nq * (words * 4 + 2 * (size_t)kSpillCapacity * 8) + nq * (sizeof(QueryParams) + 64);

@@ -142,6 +142,9 @@ class GraphEngine {
                           uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream, size_t slot,
                           Kernel kernel = Kernel::Fast);
   void reserve_scratch_sets(size_t n);
+  // sizes scratch set `set` for launches of up to `slots` CTAs now, so that no
+  // later launch reallocates it (a reallocation waits for the whole device)
+  void reserve_scratch_slots(size_t set, size_t slots);
   // Bytes of device scratch one batched launch of nq queries uses (admission).
   size_t batched_scratch_bytes(size_t nq) const;
   // The exact search with every scratch buffer carved from the caller-provided

@@ -100,6 +100,9 @@ class Server {
       SRV_CUDA(cudaMallocHost(&l.h_rows, max_batch * row_bytes_));
       SRV_CUDA(cudaMallocHost(&l.h_out, max_batch * max_k * sizeof(ObjDist)));
       SRV_CUDA(cudaMallocHost(&l.h_counts, max_batch * 4));
+      // a launch uses at most one scratch slot per query (plus the rounding of its
+      // last CTA's warps): no reallocation while serving
+      e->reserve_scratch_slots(l.slot, max_batch + 8);
     }
     worker_ = std::thread([this] { run(); });
   }
