@@ -613,13 +613,17 @@ void GraphEngine::search_device_slot(const uint4* d_rows, size_t nq, const Searc
 // query of a large index does after a few thousand visits, so large indexes get a
 // small hash (more CTAs per SM) and small ones a large hash (no bitmap at all).
 uint32_t GraphEngine::visited_hash_capacity() const { return host_.nrows >= (1u << 18) ? 2048u : 8192u; }
+// Shared-memory tier of the exact-order kernels' candidate queue: 512 keys on large
+// indexes (the overflow tier behind it keeps the queue exact; a smaller tier means
+// more CTAs per SM: 1M x 128: plain kernel +17 %, QG +18 %, results unchanged).
+uint32_t GraphEngine::candidate_list_capacity() const { return host_.nrows >= (1u << 18) ? 512u : 1024u; }
 
 void GraphEngine::launch_exact(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
                                uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats,
                                cudaStream_t stream) {
   ExactConfig cfg{};
   cfg.kcap = max_size + 1;
-  cfg.ccap = 1024;
+  cfg.ccap = std::max<uint32_t>(candidate_list_capacity(), std::min<uint32_t>(1024, next_pow2(cfg.kcap)));
   cfg.hcap = visited_hash_capacity();
   cfg.mode = (uint32_t)mode_;
   cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));
@@ -888,7 +892,7 @@ void GraphEngine::search_device_noalloc(void* scratch, size_t scratch_bytes, con
   build_params(args, nargs, nq, kmax, params, seeds, max_size);
   ExactConfig cfg{};
   cfg.kcap = max_size + 1;
-  cfg.ccap = 1024;
+  cfg.ccap = std::max<uint32_t>(candidate_list_capacity(), std::min<uint32_t>(1024, next_pow2(cfg.kcap)));
   cfg.hcap = visited_hash_capacity();
   cfg.mode = (uint32_t)mode_;
   cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));
@@ -1015,7 +1019,7 @@ void GraphEngine::qg_search_device(const uint4* d_rows, size_t nq, const QGArgs*
   if (seeds.empty()) seeds.push_back(0);
   ExactConfig cfg{};
   cfg.kcap = max_size + 1;
-  cfg.ccap = 1024;
+  cfg.ccap = std::max<uint32_t>(candidate_list_capacity(), std::min<uint32_t>(1024, next_pow2(cfg.kcap)));
   cfg.hcap = visited_hash_capacity();
   cfg.mode = (uint32_t)GraphMode::Updatable;
   cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));

@@ -196,6 +196,7 @@ class GraphEngine {
   void ensure_bf16_rows();
   bool result_size_rule() const;
   uint32_t visited_hash_capacity() const;
+  uint32_t candidate_list_capacity() const;
   // 8-bit codes of float objects; the affine map is lossless when every
   // coordinate is an integer and they span at most 256 values
   void ensure_sq8_stats();
