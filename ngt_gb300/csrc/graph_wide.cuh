@@ -56,7 +56,6 @@ struct WideShared {
   unsigned long long spill_min, worst;
   float limit, insert_limit;
   uint32_t parents[32], pexcl[32], pbase[32];
-  uint32_t wcnt[kWideMaxWarps], wcnt2[kWideMaxWarps];
   unsigned long long wmin[kWideMaxWarps];
 };
 
@@ -129,26 +128,6 @@ __device__ __forceinline__ void cta_bitonic_sort(unsigned long long* a, uint32_t
       __syncthreads();
     }
   }
-}
-
-// Order-preserving CTA compaction of one round of flags: returns the position of
-// this thread's element among the flagged ones of the round (valid when flag)
-// and the round's total in *round_total.
-__device__ __forceinline__ uint32_t cta_compact(bool flag, uint32_t* wcnt, uint32_t* round_total) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  unsigned bal = __ballot_sync(0xffffffffu, flag);
-  if (lane == 0) wcnt[warp] = __popc(bal);
-  __syncthreads();
-  uint32_t base = 0, tot = 0;
-  const int nw = (int)(blockDim.x >> 5);
-  for (int w = 0; w < nw; w++) {
-    uint32_t c = wcnt[w];
-    if (w < warp) base += c;
-    tot += c;
-  }
-  __syncthreads();
-  *round_total = tot;
-  return base + __popc(bal & ((1u << lane) - 1u));
 }
 
 // (row - query)^2 of one 16-byte row chunk, two float lanes at a time, against the
@@ -594,6 +573,7 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
         if (lane == 0) {
           s.n = n; s.scan0 = scan0; s.spill_n = spill_n; s.spill_min = spill_min;
           s.refill = next_refill; s.done = done; s.np = np; s.limit = limit;
+          s.cnt = 0; s.kept = 0;              // counters of this step's gather and placement
         }
       }
       __syncthreads();
@@ -606,7 +586,6 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       // edge loads, then all visited-bit atomics, then one CTA scan of the per-thread
       // counts places the new ids (their order does not matter to this search).
       constexpr int kGatherSlots = 8;
-      uint32_t cnt = 0;
       for (uint32_t base0 = 0; base0 < total; base0 += kGatherSlots * (uint32_t)T) {
         uint32_t ids[kGatherSlots];
         uint32_t fm = 0, p2 = 0;
@@ -627,7 +606,8 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
             if ((visit_or(&bitmap[ids[j] >> 5], bit, keep_visited, pol_keep) & bit) == 0u) fm |= 1u << j;
           }
         }
-        // CTA exclusive scan of the per-thread counts
+        // places in nid: a warp scan of the per-thread counts and one counter
+        // increment per warp (the order of the new ids does not matter to this search)
         const uint32_t c = (uint32_t)__popc(fm);
         uint32_t incl = c;
 #pragma unroll
@@ -635,21 +615,16 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
           uint32_t v = __shfl_up_sync(0xffffffffu, incl, off);
           if (lane >= off) incl += v;
         }
-        if (lane == 31) s.wcnt[warp] = incl;
-        __syncthreads();
-        uint32_t wbase = 0, tot = 0;
-        for (int w = 0; w < T / 32; w++) {
-          const uint32_t x = s.wcnt[w];
-          if (w < warp) wbase += x;
-          tot += x;
-        }
-        uint32_t pos = cnt + wbase + incl - c;
+        uint32_t wbase = 0;
+        if (lane == 31 && incl) wbase = atomicAdd(&s.cnt, incl);
+        wbase = __shfl_sync(0xffffffffu, wbase, 31);
+        uint32_t pos = wbase + incl - c;
 #pragma unroll
         for (int j = 0; j < kGatherSlots; j++)
           if (fm & (1u << j)) nid[pos++] = ids[j];
-        cnt += tot;
-        __syncthreads();
       }
+      __syncthreads();
+      const uint32_t cnt = s.cnt;
       if (tid == 0) { s.dc += cnt; s.visited += cnt; }
       // ---- distances ------------------------------------------------------------------------
       score(cnt);
@@ -659,7 +634,8 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       const unsigned long long worst = (n >= L) ? (list[L - 1] & ~(unsigned long long)kExpandedBit) : ~0ull;
       const float rk2 = (n >= P.size) ? fminf(key_dist(list[P.size - 1]), user_radius) : user_radius;
       const float insert_limit = P.coef * rk2;
-      uint32_t kept = 0;
+      // kept keys are appended through one counter increment per warp and round
+      // (their order does not matter: they are ranked or sorted before the merge)
       unsigned long long smin = ~0ull;
       for (uint32_t base0 = 0; base0 < cnt; base0 += blockDim.x) {
         const uint32_t i = base0 + tid;
@@ -671,10 +647,11 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
         }
         const bool keep = live && key < worst;
         const bool spl = live && key >= worst;
-        uint32_t rt;
-        const uint32_t pos = cta_compact(keep, s.wcnt, &rt);
-        if (keep) nkey[kept + pos] = key;
-        kept += rt;
+        const unsigned kb = __ballot_sync(0xffffffffu, keep);
+        uint32_t kbase = 0;
+        if (lane == 0 && kb) kbase = atomicAdd(&s.kept, (uint32_t)__popc(kb));
+        kbase = __shfl_sync(0xffffffffu, kbase, 0);
+        if (keep) nkey[kbase + __popc(kb & ((1u << lane) - 1u))] = key;
         if (spl) {
           const uint32_t o = atomicAdd(&s.spill_n, 1u);
           if (o < cfg.spill_cap) spill[o] = key;
@@ -687,6 +664,7 @@ graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint
       }
       if (lane == 0) s.wmin[warp] = smin;
       __syncthreads();
+      const uint32_t kept = s.kept;
       if (tid == 0) {
         unsigned long long mn = s.spill_min;
         for (int w = 0; w < T / 32; w++) mn = s.wmin[w] < mn ? s.wmin[w] : mn;
