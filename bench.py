@@ -54,7 +54,7 @@ QS8_EPS_SWEEP = [0.08, 0.1, 0.11, 0.12, 0.13, 0.14, 0.15, 0.17, 0.2, 0.25, 0.3]
 BATCHED_CANDIDATES = [
     dict(kernel=1, L=256, P=3, R=4, C=5, NB=256), dict(kernel=1, L=256, P=4, R=6, C=4, NB=0),
     dict(kernel=3, L=256, P=8, T=128, stage=16), dict(kernel=3, L=256, P=8, T=128, stage=8),
-    dict(kernel=3, L=256, P=12, T=128, stage=16),
+    dict(kernel=3, L=256, P=10, T=128, stage=16), dict(kernel=3, L=256, P=12, T=128, stage=16),
     dict(kernel=3, L=256, P=8, T=128, stage=32), dict(kernel=3, L=256, P=16, T=128, stage=16),
     dict(kernel=3, L=256, P=16, T=256, stage=32), dict(kernel=3, L=256, P=8, T=256, stage=32)]
 WIDE_PARENTS = 32                 # parents per step of the CTA-per-query kernel the serving loop uses
@@ -91,7 +91,7 @@ def parse():
                     help="also measure scalar-quantized (QSUInteger-8B) objects on the same graph (1) or not (0)")
     ap.add_argument("--fixed", default=None,
                     help="EPS_PLAIN:EPS_BATCHED -- skip the epsilon / tuning sweeps (profiling runs)")
-    ap.add_argument("--fixed-config", default='{"kernel": 3, "L": 256, "P": 8, "T": 128, "stage": 16}',
+    ap.add_argument("--fixed-config", default='{"kernel": 3, "L": 256, "P": 10, "T": 128, "stage": 16}',
                     help="batched-kernel settings (JSON) used with --fixed")
     return ap.parse_args()
 
