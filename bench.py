@@ -103,6 +103,27 @@ def dist_env():
     return rank, world, local
 
 
+def reduce_max(x: float, world: int, device="cuda") -> float:
+    """The largest x over all ranks (one replica per rank; the job is as slow as its slowest)."""
+    if world == 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def broadcast_choice(obj, world: int):
+    """Rank 0's value on every rank (the autotuner's decisions, so that all ranks time
+    the same candidates and run the same configuration)."""
+    if world == 1:
+        return obj
+    import torch
+    box = [obj]
+    torch.distributed.broadcast_object_list(box, src=0)
+    return box[0]
+
+
 def workload(args, rank):
     from ngt_gb300 import synthetic
     base = synthetic.clipped_exponential(args.n, args.dim, seed=11)
@@ -530,10 +551,7 @@ def main():
         launches = ix.kernel_launches() - launches0
         kernel_ms = [a.elapsed_time(b) for a, b in ev]
         total_ms = sum(kernel_ms)
-        if world > 1:
-            t = torch.tensor([total_ms], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            total_ms = float(t.item())
+        total_ms = reduce_max(total_ms, world)
         ids_np = res[:, :, 0].cpu().numpy().view(np.uint32)
         cnt_np = cnt.cpu().numpy().astype(np.int64)
         stats = st.cpu().numpy().view(QUERY_STATS_DTYPE).reshape(nq)
@@ -568,7 +586,7 @@ def main():
         best_cfg = json.loads(args.fixed_config)
         best_eps, best_curve = float(eb), []
     else:
-        eps, curves[KERNEL_EXACT] = calibrate(KERNEL_EXACT)
+        eps, curves[KERNEL_EXACT] = broadcast_choice(calibrate(KERNEL_EXACT), world)
         runs[KERNEL_EXACT] = timed(KERNEL_EXACT, eps)
         # autotuner: every candidate at the smallest epsilon reaching the recall target
         # (calibrated once per result-determining setting), three timed steps each; the two
@@ -585,6 +603,7 @@ def main():
             if probe["recall"] >= RECALL_TARGET:
                 probes.append((probe["qps"], c, eps_c, curve_c))
         probes.sort(key=lambda t: -t[0])
+        probes = broadcast_choice(probes, world)      # every rank times rank 0's finalists
         finals = []
         for qps, c, eps_c, curve_c in probes[:2]:
             apply(c)
@@ -619,7 +638,7 @@ def main():
         ix.batch_search(hq, k=k, epsilon=head["epsilon"], kernel=head["config"]["kernel"])
         if i >= args.warmup:
             e2e_times.append(time.time() - t1)
-    e2e_qps = world * nq * len(e2e_times) / sum(e2e_times)
+    e2e_qps = world * nq * len(e2e_times) / reduce_max(sum(e2e_times), world)
     h2d = hq.nbytes
     d2h = nq * (int(np.ceil(k * (1 + head["epsilon"]))) + 1) * 8 + nq * 4 + nq * QUERY_STATS_DTYPE.itemsize
 
