@@ -512,7 +512,10 @@ void GraphEngine::ensure_bf16_rows() {
 }
 
 void GraphEngine::ensure_sq8_stats() {
-  if (sq8_stats_) return;
+  std::call_once(sq8_once_, [this] { compute_sq8_stats(); });
+}
+
+void GraphEngine::compute_sq8_stats() {
   const float* x = reinterpret_cast<const float*>(host_.objects.data());
   const uint32_t dim = host_.prop.dimension, dpad = host_.dpad;
   float lo = FLT_MAX, hi = -FLT_MAX;
@@ -530,7 +533,6 @@ void GraphEngine::ensure_sq8_stats() {
   sq8_lossless_ = integral && hi - lo <= 255.f;
   sq8_offset_ = lo;
   sq8_scale_ = sq8_lossless_ || hi == lo ? 1.f : (hi - lo) / 255.f;
-  sq8_stats_ = true;
 }
 
 void GraphEngine::ensure_sq8_rows() {

@@ -200,6 +200,7 @@ class GraphEngine {
   // 8-bit codes of float objects; the affine map is lossless when every
   // coordinate is an integer and they span at most 256 values
   void ensure_sq8_stats();
+  void compute_sq8_stats();
   void ensure_sq8_rows();
  public:
   // search rows the wide kernel uses for this index and tuning
@@ -261,7 +262,8 @@ class GraphEngine {
   std::vector<FastScratch> fast_scratch_ = std::vector<FastScratch>(1);
   void* d_bf16_ = nullptr;                                // bf16 copy of float object rows
   void* d_sq8_ = nullptr;                                 // 8-bit codes of float object rows
-  bool sq8_stats_ = false, sq8_lossless_ = false;
+  std::once_flag sq8_once_;                               // the statistics are computed once
+  bool sq8_lossless_ = false;
   float sq8_offset_ = 0.f, sq8_scale_ = 1.f;
   FastTuning tuning_;
   DevGraph dev_;
