@@ -521,6 +521,7 @@ void GraphEngine::compute_sq8_stats() {
   float lo = FLT_MAX, hi = -FLT_MAX;
   bool integral = true;
   for (size_t r = 1; r < host_.nrows; r++) {          // row 0 is the unused slot
+    if (!host_.present[r]) continue;                   // removed objects
     const float* row = x + r * dpad;
     for (uint32_t d = 0; d < dim; d++) {
       const float v = row[d];
