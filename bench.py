@@ -231,6 +231,10 @@ def served_latency(ix, queries, k, eps, rates, seconds, kernel=1, inflight=3, ma
     out = []
     rng = np.random.default_rng(43)
     with Server(ix, max_batch=max_batch, inflight=inflight, max_k=max(16, k), kernel=kernel) as srv:
+        # warm-up (untimed): every lane launches a few times before the first rate
+        warm = [srv.submit(queries[i * 64:(i + 1) * 64], k=k, epsilon=eps) for i in range(4 * inflight)]
+        for t_ in warm:
+            srv.wait(t_)
         for rate in rates:
             sizes, gaps = [], []
             t = 0.0
