@@ -269,6 +269,13 @@ void GraphEngine::build_params(const SearchArgs* args, size_t nargs, size_t nq, 
   const Property& p = host_.prop;
   uint32_t shared_seeds = UINT32_MAX;
   for (size_t i = 0; i < nq; i++) {
+    if (nargs == 1 && i > 0) {
+      // one parameter set for the whole batch: every query's parameters (seeds
+      // included) equal the first one's but for its output slot
+      params[i] = params[0];
+      params[i].out_off = (uint32_t)(i * kmax);
+      continue;
+    }
     const SearchArgs& a = args[nargs == 1 ? 0 : i];
     QueryParams qp{};
     float coef = a.epsilon + 1.0f;                     // SearchContainer::setEpsilon
