@@ -2,7 +2,6 @@
 index writer codes objects exactly as the oracle (pinned to the reference) codes
 queries, its files read back through the oracle's independent reader, and the
 tie-aware recall counts what it should."""
-import os
 
 import numpy as np
 
