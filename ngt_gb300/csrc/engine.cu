@@ -675,7 +675,9 @@ void GraphEngine::launch_wide(const uint4* d_rows, size_t nq, const QueryParams*
   if (bf16) ensure_bf16_rows();
   if (sq8) ensure_sq8_rows();
   WideConfig cfg{};
-  uint32_t L = tuning_.list_cap ? next_pow2(tuning_.list_cap) : next_pow2(std::max<uint32_t>(256, 4 * max_size));
+  // automatic list: 4 x the result size, at least 256, at most 1024 (and never below size + 1)
+  uint32_t L = tuning_.list_cap ? next_pow2(tuning_.list_cap)
+                                : std::min<uint32_t>(1024, next_pow2(std::max<uint32_t>(256, 4 * max_size)));
   L = std::max<uint32_t>(L, next_pow2(max_size + 1));
   if (L > 1024) throw std::runtime_error("result size too large for the wide kernel (at most 1023)");
   cfg.list_cap = L;
@@ -738,7 +740,9 @@ void GraphEngine::launch_fast(const uint4* d_rows, size_t nq, const QueryParams*
   if (!fn) throw std::runtime_error("the batched kernel does not support this index type or tuning");
   if (bf16) ensure_bf16_rows();
   FastConfig cfg{};
-  uint32_t L = tuning_.list_cap ? next_pow2(tuning_.list_cap) : next_pow2(std::max<uint32_t>(512, 4 * max_size));
+  // automatic list: 4 x the result size, at least 512, at most 1024 (and never below size + 1)
+  uint32_t L = tuning_.list_cap ? next_pow2(tuning_.list_cap)
+                                : std::min<uint32_t>(1024, next_pow2(std::max<uint32_t>(512, 4 * max_size)));
   L = std::max<uint32_t>(L, next_pow2(max_size + 1));
   if (L > 1024) throw std::runtime_error("result size too large for the batched kernel (at most 1023)");
   cfg.list_cap = L;

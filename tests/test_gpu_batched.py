@@ -219,3 +219,27 @@ def test_wide_tuning_knobs_do_not_change_results(tmp_path):
                     dict(stage_kilobytes=201), dict(rows_in_flight=3)):
             with pytest.raises(NativeError):
                 ix.set_batched_tuning(**bad)
+
+
+@pytest.mark.parametrize("kernel", [KERNEL_BATCHED, KERNEL_WIDE])
+def test_batched_large_result_sizes(kernel, tmp_path):
+    """Result sizes above 256 (up to the list's 1024 entries) run, return that many
+    results ascending by (distance, id), every distance exact, and find most of
+    the exact k-NN."""
+    from ngt_gb300 import Index
+    path, meta, queries, _ = materialize("c1_f32_l2", str(tmp_path))
+    o = oracle.Oracle(oracle.IndexFiles(path))
+    q = queries[:20]
+    li, ld, ln = o.linear_search(q, k=600, threads=8)
+    with Index(path, read_only=True) as ix:
+        for k in (300, 600):
+            ids, ds, n = ix.batch_search(q, k=k, epsilon=0.2, kernel=kernel)
+            assert (n == k).all()
+            for j in range(len(q)):
+                pairs = list(zip(ds[j, :k], ids[j, :k]))
+                assert pairs == sorted(pairs)
+                rows = o.f.objects[ids[j, :k].astype(np.int64), :128].astype(np.float64)
+                exact = np.sqrt(((rows - q[j].astype(np.float64)) ** 2).sum(1)).astype(np.float32)
+                assert np.array_equal(ds[j, :k], exact)
+                kth = ld[j, k - 1]
+                assert (ds[j, :k] <= kth).mean() > 0.9
