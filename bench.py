@@ -173,38 +173,53 @@ def recall(base, queries, ids, counts, kth, k):
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks / throttle reasons sampled every 50 ms; the summary keeps the
+    samples whose own timestamps fall inside the region (the sampler starts first)."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
-    def __init__(self, gpu_index=0):
+    def __init__(self, gpu_index=0, period_ms=50):
         self.gpu = gpu_index
+        self.period = period_ms
         self.proc = None
 
     def __enter__(self):
+        import datetime
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", str(self.period)],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            time.sleep(0.3)                       # the tool's start-up, outside the region
         except FileNotFoundError:
             self.proc = None
+        self.t0 = datetime.datetime.now()
         return self
 
     def __exit__(self, *a):
-        self.rows = []
+        import datetime
+        self.t1 = datetime.datetime.now()
+        self.rows, self.window = [], []
         if self.proc is None:
             return
+        time.sleep(self.period / 1000.0)          # one more sample after the region
         self.proc.terminate()
         out, _ = self.proc.communicate(timeout=10)
         for line in out.strip().splitlines():
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) >= 9:
-                self.rows.append(parts)
+            if len(parts) < 10:
+                continue
+            self.rows.append(parts[1:])
+            try:
+                t = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
+            except ValueError:
+                continue
+            if self.t0 <= t <= self.t1:
+                self.window.append(parts[1:])
 
     def summary(self):
-        rows = getattr(self, "rows", [])
+        rows = getattr(self, "window", []) or getattr(self, "rows", [])
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
@@ -212,7 +227,8 @@ class ClockSampler:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows),
+                "samples_in_region": len(getattr(self, "window", [])), "period_ms": self.period}
 
 
 def measured_peaks():

@@ -57,3 +57,28 @@ def test_tie_aware_recall():
     assert bench.recall(base, queries, np.array([[1, 3]], np.uint32), np.array([2]), kth, 2) == 1.0
     assert bench.recall(base, queries, np.array([[1, 4]], np.uint32), np.array([2]), kth, 2) == 0.5
     assert bench.recall(base, queries, np.array([[1, 0]], np.uint32), np.array([1]), kth, 2) == 0.5
+
+
+def test_clock_sampler_keeps_the_samples_of_its_region(tmp_path, monkeypatch):
+    """A stand-in nvidia-smi prints a sample every period with its own timestamp; the
+    summary counts the samples inside the region and reports an active reason."""
+    import os
+    import time
+    import bench
+    fake = tmp_path / "nvidia-smi"
+    fake.write_text(
+        "#!" + __import__("sys").executable + "\n"
+        "import datetime, sys, time\n"
+        "period = int(sys.argv[sys.argv.index('-lms') + 1]) / 1000.0\n"
+        "while True:\n"
+        "    t = datetime.datetime.now().strftime('%Y/%m/%d %H:%M:%S.%f')[:-3]\n"
+        "    print(t + ', 0, 1965, 2070, 900.1, 0x4, Not Active, Not Active, Not Active, Active', flush=True)\n"
+        "    time.sleep(period)\n")
+    fake.chmod(0o755)
+    monkeypatch.setenv("PATH", str(tmp_path) + os.pathsep + os.environ["PATH"])
+    with bench.ClockSampler(0, period_ms=20) as c:
+        time.sleep(0.3)
+    s = c.summary()
+    assert s["sm_mhz"] == 1965.0 and s["sm_max_mhz"] == 2070.0
+    assert s["reasons"] == ["sw_power_cap"]
+    assert 5 <= s["samples_in_region"] <= 20 and s["samples_in_region"] < len(c.rows)   # lead-in dropped
