@@ -63,7 +63,9 @@ bool ngtgpu_search_batch_device(NGTIndex, const void *d_rows, size_t nq, const N
                                 NGTGPUQueryStats *d_stats, void *stream, uint32_t kernel, NGTError);
 
 /* Tuning of the batched kernel for this index (0 = automatic): candidate
- * list length (rounded up to a power of two, >= size+1, <= 1024), nodes
+ * list length (rounded up to a power of two, >= size+1, <= 1024; automatic:
+ * 4 x size, at least 256 for NGTGPU_KERNEL_WIDE and 512 for the warp kernel,
+ * at most 1024, so the batched kernels take result sizes up to 1023), nodes
  * expanded per iteration (<= 16), and re-ranked candidates per query as a
  * multiple of size. */
 bool ngtgpu_set_batched_tuning(NGTIndex, uint32_t list_capacity, uint32_t parents, float rerank_factor, NGTError);
