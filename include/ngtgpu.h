@@ -117,6 +117,44 @@ bool ngtgpu_search_exact_noalloc(NGTIndex, const void *d_rows, size_t nq, const 
                                  size_t nparams, NGTObjectDistance *d_results, size_t kmax, uint32_t *d_counts,
                                  NGTGPUQueryStats *d_stats, void *stream, NGTError);
 
+/* Exhaustive k-NN with a tensor-core pre-selection (the precision path of
+ * ngt_linear_search_index, lib/NGT/Capi.cpp; exact search semantics of
+ * ObjectSpaceRepository::linearSearch, lib/NGT/ObjectSpaceRepository.h:860-922).
+ * Float objects with L2, inner product, cosine, angle or their normalized forms.
+ * Every (query, object) pair is scored on the tensor cores from bf16 copies with
+ * fp32 accumulation; the `candidates` best scores per query (0: max(4 x size,
+ * 64); at most 4096, at least size) are re-ranked with the index's exact
+ * comparator on the fp32 objects, and the `size` nearest are returned ascending
+ * by (distance, id), with the distances of the plain linear search.  The ids
+ * equal the plain linear search's whenever the true nearest objects are among
+ * the candidates.  d_status[q] bit 1: the query's candidate list overflowed (the
+ * result may miss objects).  Device buffers; d_rows holds nq rows converted by
+ * ngtgpu_convert_queries_float; queued on `stream` (NULL = the index's stream),
+ * returns after completion. */
+bool ngtgpu_linear_search_tc_device(NGTIndex, const void *d_rows, size_t nq, size_t size, size_t candidates,
+                                    NGTObjectDistance *d_results, size_t kmax, uint32_t *d_counts,
+                                    uint32_t *d_status, void *stream, NGTError);
+/* The same over host buffers: nq float queries (row-major nq x dim), results of
+ * query i in results[i*kmax ..], counts[i], status[i]. */
+bool ngtgpu_linear_search_tc_float(NGTIndex, const float *queries, size_t nq, int32_t dim, size_t size,
+                                   size_t candidates, NGTObjectDistance *results, size_t kmax, uint32_t *counts,
+                                   uint32_t *status, NGTError);
+/* The approximate scores of the tensor-core pre-selection alone:
+ * d_scores[q * ld + id] (ld >= the number of object slots, id 0 unused), larger
+ * = closer: a * (q . x) + b over bf16 copies with a = 1, b = -|x|^2 / 2 for L2
+ * and inner product, a = 1 / |x| for cosine and angle, a = 1 for the normalized
+ * forms; -inf for id 0 and removed objects. */
+bool ngtgpu_tc_scores_device(NGTIndex, const void *d_rows, size_t nq, float *d_scores, size_t ld, void *stream,
+                             NGTError);
+/* CUDA-event times in milliseconds of the last query batch (up to 16384
+ * queries) of ngtgpu_linear_search_tc_*: [0] query conversion, dense part and
+ * its selection, [1] the score kernel over the remaining objects (the
+ * threshold filter), [2] the final exact re-rank. */
+bool ngtgpu_tc_phase_times(NGTIndex, float *ms3, NGTError);
+/* Objects scored densely before the per-query threshold filter of the
+ * tensor-core search (rounded up to a multiple of 128, at least `candidates`,
+ * at most 16384; 0 = automatic, 16384).  Results do not depend on it. */
+bool ngtgpu_set_tc_first_rows(NGTIndex, size_t rows, NGTError);
 /* Serving loop (continuous batching).  A server keeps up to `inflight`
  * batched-kernel launches on the GPU at once, each on its own stream and
  * scratch set; requests submitted from any thread while others run join the

@@ -125,6 +125,14 @@ def load_library() -> ctypes.CDLL:
         "ngtgpu_convert_queries_float": ([c_void_p, c_void_p, c_size_t, c_int32, c_void_p, c_void_p], c_bool),
         "ngtgpu_search_batch_device": ([c_void_p, c_void_p, c_size_t, POINTER(QueryParameters), c_size_t, c_void_p,
                                         c_size_t, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p], c_bool),
+        "ngtgpu_linear_search_tc_device": ([c_void_p, c_void_p, c_size_t, c_size_t, c_size_t, c_void_p, c_size_t,
+                                            c_void_p, c_void_p, c_void_p, c_void_p], c_bool),
+        "ngtgpu_linear_search_tc_float": ([c_void_p, c_void_p, c_size_t, c_int32, c_size_t, c_size_t, c_void_p,
+                                           c_size_t, c_void_p, c_void_p, c_void_p], c_bool),
+        "ngtgpu_tc_scores_device": ([c_void_p, c_void_p, c_size_t, c_void_p, c_size_t, c_void_p, c_void_p],
+                                    c_bool),
+        "ngtgpu_set_tc_first_rows": ([c_void_p, c_size_t, c_void_p], c_bool),
+        "ngtgpu_tc_phase_times": ([c_void_p, c_void_p, c_void_p], c_bool),
         "ngtgpu_kernel_launches": ([c_void_p, c_void_p], c_uint64),
         "ngtgpu_get_wide_search_rows": ([c_void_p, c_void_p], c_uint32),
         "ngtgpu_set_batched_tuning": ([c_void_p, c_uint32, c_uint32, c_float, c_void_p], c_bool),
@@ -277,6 +285,45 @@ class Index:
         t = BatchedTuning(list_capacity, parents, rerank_factor, rows_in_flight, ctas_per_sm, neighbour_capacity,
                           cta_threads, stage_kilobytes, l2_policy, search_rows)
         self._check(self._lib.ngtgpu_set_batched_tuning_ex(self._index, ctypes.byref(t), self._err))
+
+    def linear_search_tc(self, queries, k: int = 10, candidates: int = 0, first_rows: int = 0):
+        """Exhaustive k-NN of every row of `queries` with the tensor-core
+        pre-selection (bf16 scores, `candidates` re-ranked exactly).
+
+        Returns (ids[nq, k], distances[nq, k], counts[nq], status[nq]); status
+        bit 1 marks a query whose candidate list overflowed.
+        """
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        nq = q.shape[0]
+        self._check(self._lib.ngtgpu_set_tc_first_rows(self._index, first_rows, self._err))
+        res = np.zeros((nq, k), RESULT_DTYPE)
+        counts = np.zeros(nq, np.uint32)
+        status = np.zeros(nq, np.uint32)
+        ok = self._lib.ngtgpu_linear_search_tc_float(self._index, q.ctypes.data, nq, q.shape[1], k, candidates,
+                                                     res.ctypes.data, k, counts.ctypes.data, status.ctypes.data,
+                                                     self._err)
+        self._check(ok)
+        return res["id"].copy(), res["distance"].copy(), counts, status
+
+    def tc_phase_times(self):
+        """CUDA-event milliseconds of the last tensor-core search batch: (dense
+        part + selection, filtered part, final re-rank)."""
+        ms = np.zeros(3, np.float32)
+        self._check(self._lib.ngtgpu_tc_phase_times(self._index, ms.ctypes.data, self._err))
+        return tuple(float(v) for v in ms)
+
+    def tc_scores(self, queries) -> np.ndarray:
+        """Approximate scores [nq, number of object slots] of the tensor-core
+        pre-selection (larger = closer; -inf for id 0 and removed objects)."""
+        import torch
+        rows = torch.from_numpy(self.convert_queries(queries)).cuda()
+        nq = rows.shape[0]
+        nslots = self.number_of_objects() + 1
+        out = torch.empty((nq, nslots), dtype=torch.float32, device="cuda")
+        ok = self._lib.ngtgpu_tc_scores_device(self._index, rows.data_ptr(), nq, out.data_ptr(), nslots, None,
+                                               self._err)
+        self._check(ok)
+        return out.cpu().numpy()
 
     def kernel_launches(self) -> int:
         return int(self._lib.ngtgpu_kernel_launches(self._index, self._err))

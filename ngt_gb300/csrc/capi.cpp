@@ -423,6 +423,99 @@ bool ngtgpu_search_batch_device(NGTIndex index, const void* d_rows, size_t nq, c
   CAPI_CATCH(error, false)
 }
 
+bool ngtgpu_linear_search_tc_device(NGTIndex index, const void* d_rows, size_t nq, size_t size, size_t candidates,
+                                    NGTObjectDistance* d_results, size_t kmax, uint32_t* d_counts, uint32_t* d_status,
+                                    void* stream, NGTError error) {
+  if (index == nullptr ||
+      (nq && (d_rows == nullptr || d_results == nullptr || d_counts == nullptr || d_status == nullptr))) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " rows = " << d_rows << " nq = " << nq);
+    return false;
+  }
+  try {
+    GraphEngine* e = engine(index);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : e->stream();
+    e->linear_search_tc_device(static_cast<const uint4*>(d_rows), nq, size, candidates,
+                               reinterpret_cast<ngtg::ObjDist*>(d_results), kmax, d_counts, d_status, s);
+    return true;
+  }
+  CAPI_CATCH(error, false)
+}
+
+bool ngtgpu_linear_search_tc_float(NGTIndex index, const float* queries, size_t nq, int32_t dim, size_t size,
+                                   size_t candidates, NGTObjectDistance* results, size_t kmax, uint32_t* counts,
+                                   uint32_t* status, NGTError error) {
+  if (index == nullptr || dim <= 0 ||
+      (nq && (queries == nullptr || results == nullptr || counts == nullptr || status == nullptr))) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " queries = " << queries << " nq = " << nq << " dim = " << dim);
+    return false;
+  }
+  // device buffers of this call, freed on every exit
+  struct Buffers {
+    void* p[4] = {nullptr, nullptr, nullptr, nullptr};
+    ~Buffers() {
+      for (void* x : p) cudaFree(x);
+    }
+  } b;
+  try {
+    GraphEngine* e = engine(index);
+    if (nq == 0) return true;
+    std::vector<uint8_t> rows;
+    e->convert_queries(queries, QueryType::Float32, nq, (size_t)dim, rows);
+    cudaStream_t s = e->stream();
+    auto ck = [](cudaError_t c) {
+      if (c != cudaSuccess) throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(c));
+    };
+    ck(cudaSetDevice(e->device()));
+    ck(cudaMalloc(&b.p[0], rows.size()));
+    ck(cudaMalloc(&b.p[1], nq * kmax * sizeof(NGTObjectDistance)));
+    ck(cudaMalloc(&b.p[2], nq * 4));
+    ck(cudaMalloc(&b.p[3], nq * 4));
+    ck(cudaMemcpyAsync(b.p[0], rows.data(), rows.size(), cudaMemcpyHostToDevice, s));
+    e->linear_search_tc_device(static_cast<const uint4*>(b.p[0]), nq, size, candidates,
+                               static_cast<ngtg::ObjDist*>(b.p[1]), kmax, static_cast<uint32_t*>(b.p[2]),
+                               static_cast<uint32_t*>(b.p[3]), s);
+    ck(cudaMemcpyAsync(results, b.p[1], nq * kmax * sizeof(NGTObjectDistance), cudaMemcpyDeviceToHost, s));
+    ck(cudaMemcpyAsync(counts, b.p[2], nq * 4, cudaMemcpyDeviceToHost, s));
+    ck(cudaMemcpyAsync(status, b.p[3], nq * 4, cudaMemcpyDeviceToHost, s));
+    ck(cudaStreamSynchronize(s));
+    return true;
+  }
+  CAPI_CATCH(error, false)
+}
+
+bool ngtgpu_tc_scores_device(NGTIndex index, const void* d_rows, size_t nq, float* d_scores, size_t ld, void* stream,
+                             NGTError error) {
+  if (index == nullptr || (nq && (d_rows == nullptr || d_scores == nullptr))) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " rows = " << d_rows << " scores = " << d_scores);
+    return false;
+  }
+  try {
+    GraphEngine* e = engine(index);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : e->stream();
+    e->tc_scores_device(static_cast<const uint4*>(d_rows), nq, d_scores, ld, s);
+    return true;
+  }
+  CAPI_CATCH(error, false)
+}
+
+bool ngtgpu_tc_phase_times(NGTIndex index, float* ms3, NGTError error) {
+  if (index == nullptr || ms3 == nullptr) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " ms = " << ms3);
+    return false;
+  }
+  engine(index)->tc_phase_ms(ms3);
+  return true;
+}
+
+bool ngtgpu_set_tc_first_rows(NGTIndex index, size_t rows, NGTError error) {
+  if (index == nullptr) {
+    CAPI_PARAM_ERROR(error, "index = " << index);
+    return false;
+  }
+  engine(index)->set_tc_first_rows(rows);
+  return true;
+}
+
 bool ngtgpu_set_batched_tuning(NGTIndex index, uint32_t list_capacity, uint32_t parents, float rerank_factor,
                                NGTError error) {
   if (index == nullptr || list_capacity > 1024 || parents > 16 || rerank_factor < 0.f) {

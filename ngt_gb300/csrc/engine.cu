@@ -186,6 +186,7 @@ GraphEngine::~GraphEngine() {
   for (void* p : qg_buffers_) cudaFree(p);
   cudaFree(d_qbg_ovf_);
   cudaFree(d_blob_dist_);
+  tc_release(tc_);
   if (stream_) cudaStreamDestroy(stream_);
 }
 

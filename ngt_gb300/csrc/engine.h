@@ -75,6 +75,8 @@ struct SearchOutput {
 };
 
 class CudaError;
+struct TcState;                     // tensor-core linear search state (tc_linear.cu)
+void tc_release(TcState* s);
 
 class GraphEngine {
  public:
@@ -122,6 +124,23 @@ class GraphEngine {
   static size_t qbg_result_size(const QBGArgs& a) {
     return a.result_expansion >= 1.0f ? (size_t)((float)a.size * a.result_expansion) : a.size;
   }
+  // Exhaustive search with a tensor-core pre-selection (tc_linear.cu): bf16
+  // scores of every (query, row) with fp32 accumulation, the `candidates` best
+  // per query re-ranked with the exact comparator, the first `size` returned
+  // ascending by (distance, id).  d_rows: nq converted query rows; d_status[q]
+  // bit 1 = candidate list overflow.  Float objects; L2, inner product, cosine,
+  // angle and their normalized forms.
+  void linear_search_tc_device(const uint4* d_rows, size_t nq, size_t size, size_t candidates, ObjDist* d_out,
+                               size_t kmax, uint32_t* d_counts, uint32_t* d_status, cudaStream_t stream);
+  // The approximate scores alone: d_scores[q * ld + row] (-inf for the unused
+  // row 0 and removed objects).
+  void tc_scores_device(const uint4* d_rows, size_t nq, float* d_scores, size_t ld, cudaStream_t stream);
+  bool tc_supported() const;
+  // CUDA-event times (ms) of the last query batch of linear_search_tc_device:
+  // dense part with its selection, filtered part, final re-rank
+  void tc_phase_ms(float* out) const;
+  // rows scored densely before the threshold filter (0: automatic, 16384)
+  void set_tc_first_rows(size_t rows) { tc_first_rows_ = rows; }
   // Exhaustive search (exact ids, ties broken by id).
   void linear_search(const void* queries, QueryType qt, size_t nq, size_t qdim, size_t size, SearchOutput& out);
 
@@ -267,6 +286,9 @@ class GraphEngine {
   float sq8_offset_ = 0.f, sq8_scale_ = 1.f;
   FastTuning tuning_;
   DevGraph dev_;
+  void ensure_tc_rows();
+  TcState* tc_ = nullptr;
+  size_t tc_first_rows_ = 0;
 };
 
 }  // namespace ngtg

@@ -1,0 +1,908 @@
+// Exhaustive k-NN with a tensor-core pre-selection: the precision path of the
+// linear search over float objects.
+//
+// The reference's exhaustive search (ObjectSpaceRepository::linearSearch,
+// lib/NGT/ObjectSpaceRepository.h:860-922) compares the query with every
+// object and keeps the `size` smallest (distance, id) keys.  Here the bulk of
+// that work is a dense product Q x X^T on the tensor cores:
+//
+//   1. every row x gets a bf16 copy (K padded to a multiple of 64) and an
+//      affine pair (a, b) so that score = a * (q . x) + b orders rows like the
+//      metric does (larger score = closer):
+//        L2, normalized L2, inner product (L2 over the augmented rows):
+//            a = 1, b = -|x|^2 / 2          (|q - x|^2 = |q|^2 - 2 (q.x - |x|^2/2))
+//        cosine, angle:                     a = 1 / |x|, b = 0
+//        normalized cosine, normalized angle: a = 1, b = 0 (rows are unit length)
+//   2. tc_score_kernel: bf16 x bf16 -> fp32 GEMM with tcgen05.mma (M = 128 rows,
+//      N = 256 queries, K = 16 per instruction), operands staged by TMA
+//      (cp.async.bulk.tensor, 128-byte swizzle) through a 4-stage mbarrier
+//      pipeline, accumulators double-buffered in TMEM (2 x 256 columns) and
+//      read back with tcgen05.ld by four epilogue warps.  The first
+//      `first_rows` rows are written out densely; on the remaining rows the
+//      epilogue keeps only scores that beat the query's threshold.
+//   3. tc_first_select_kernel: per query, the C best scores of the dense part
+//      (exact radix select on 64-bit (score key, row) keys); the C-th becomes
+//      the threshold, and the C keys the first candidates.  Every row past the
+//      dense part has a larger id, so a row whose score key equals the
+//      threshold's can never displace it: the filter keeps strictly better keys.
+//   4. tc_final_kernel: per query, the C best approximate keys among the
+//      candidates (the global top C by approximate score, ties by id), their
+//      exact distances with the index's comparator on the fp32 rows (the same
+//      lane grouping as the plain linear search, hence the same rounding), a
+//      bitonic sort by (distance, id), and the first `size` of them.
+//
+// The result equals the plain linear search whenever the true `size` nearest
+// rows are among the C best approximate scores; the candidate oversampling C
+// is the caller's choice.  A query whose candidate list overflowed reports
+// status bit 1.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+#include <algorithm>
+#include <cfloat>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include "engine.h"
+#include "distance.cuh"
+#include "kernels.h"
+
+namespace ngtg {
+
+#define TC_CUDA(x)                                                                                  \
+  do {                                                                                              \
+    cudaError_t e_ = (x);                                                                           \
+    if (e_ != cudaSuccess)                                                                          \
+      throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(e_) + " in " #x);     \
+  } while (0)
+
+namespace tc {
+
+constexpr uint32_t BM = 128;            // rows per tile (TMEM lanes)
+constexpr uint32_t BN = 256;            // queries per tile (TMEM columns per accumulator)
+constexpr uint32_t BK = 64;             // bf16 elements per k-block: one 128-byte swizzle row
+constexpr uint32_t STAGES = 4;
+constexpr uint32_t A_BYTES = BM * BK * 2;
+constexpr uint32_t B_BYTES = BN * BK * 2;
+constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr uint32_t SMEM_BYTES = STAGES * STAGE_BYTES + 1024;   // + slack for 1024-byte alignment
+constexpr uint32_t EPI_WARPS = 8;       // two per TMEM lane quadrant, each half of the columns
+constexpr uint32_t THREADS = 64 + 32 * EPI_WARPS;   // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
+constexpr uint32_t TMEM_COLS = 2 * BN;
+constexpr uint32_t kInvalidKey = 0xff800000u;   // score key of -inf; valid keys are smaller
+constexpr uint64_t kWaitNs = 2000000000ull;     // bound of every wait (2 s)
+
+// Instruction descriptor of tcgen05.mma kind::f16: D fp32 (bits 4-5 = 1), A and
+// B bf16 (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
+// 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((BN >> 3) << 17) | ((BM >> 4) << 24);
+
+struct ScoreArgs {
+  uint32_t row_begin, row_end;          // rows [row_begin, row_end); row_begin % BM == 0
+  uint32_t nq, kblocks;
+  const float* row_scale;
+  const float* row_bias;
+  const uint8_t* present;
+  float* dense;                         // dense mode: dense[q * dense_ld + (row - row_begin)]
+  uint32_t dense_ld;
+  const float* thr;                     // filter mode: keep scores > thr[q]
+  unsigned long long* cand;             // [nq][cap] (key << 32 | row)
+  uint32_t* cand_count;
+  uint32_t cap;
+  uint32_t* status;                     // bit 1: candidate list overflow
+  uint32_t* error;                      // bit 1: producer wait, 2: MMA wait, 4: epilogue wait ran out
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Waits until the phase of parity `parity` completed; false when the wait ran
+// out (kWaitNs) or another role aborted (abort may be null: no abort check).
+__device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, const volatile uint32_t* abort) {
+  if (mbar_try(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  while (true) {
+    if (mbar_try(bar, parity)) return true;
+    if (abort && *abort) return false;
+    if (global_ns() - t0 > kWaitNs) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4}], [%2];"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor of a K-major tile with 128-byte swizzle:
+// start address >> 4 (bits 0-13), leading offset 16 B (ignored for swizzled
+// K-major), stride 1024 B between 8-row groups (bits 32-45), descriptor version
+// 1 (bits 46-47), layout SWIZZLE_128B = 2 (bits 61-63).
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}"
+      ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+// 32 consecutive fp32 columns of this warp's 32 TMEM lanes, one lane per thread.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+        "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15]),
+        "=r"(v[16]), "=r"(v[17]), "=r"(v[18]), "=r"(v[19]), "=r"(v[20]), "=r"(v[21]), "=r"(v[22]), "=r"(v[23]),
+        "=r"(v[24]), "=r"(v[25]), "=r"(v[26]), "=r"(v[27]), "=r"(v[28]), "=r"(v[29]), "=r"(v[30]), "=r"(v[31])
+      : "r"(taddr));
+}
+// Waits for the loads above; the registers are operands so that no use of them
+// is scheduled before the wait.
+__device__ __forceinline__ void tmem_ld_wait(uint32_t (&v)[32]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(v[0]), "+r"(v[1]), "+r"(v[2]), "+r"(v[3]), "+r"(v[4]), "+r"(v[5]), "+r"(v[6]), "+r"(v[7]),
+                 "+r"(v[8]), "+r"(v[9]), "+r"(v[10]), "+r"(v[11]), "+r"(v[12]), "+r"(v[13]), "+r"(v[14]),
+                 "+r"(v[15]), "+r"(v[16]), "+r"(v[17]), "+r"(v[18]), "+r"(v[19]), "+r"(v[20]), "+r"(v[21]),
+                 "+r"(v[22]), "+r"(v[23]), "+r"(v[24]), "+r"(v[25]), "+r"(v[26]), "+r"(v[27]), "+r"(v[28]),
+                 "+r"(v[29]), "+r"(v[30]), "+r"(v[31])
+               :
+               : "memory");
+}
+
+// Larger score -> smaller key (unsigned order); NaN and -inf -> kInvalidKey or
+// above.  -0 is folded to +0, so that "key < key(t)" and "s > t" agree.
+__device__ __forceinline__ uint32_t score_key(float s) {
+  if (s != s) return 0xffffffffu;
+  uint32_t f = __float_as_uint(s + 0.0f);
+  uint32_t asc = (f & 0x80000000u) ? ~f : (f | 0x80000000u);
+  return ~asc;
+}
+// The score of a key (inverse of score_key on valid keys).
+__device__ __forceinline__ float key_score(uint32_t key) {
+  const uint32_t asc = ~key;
+  return __uint_as_float((asc & 0x80000000u) ? (asc & 0x7fffffffu) : ~asc);
+}
+
+template <bool kDense>
+__global__ void __launch_bounds__(THREADS, 1)
+tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, ScoreArgs a) {
+  extern __shared__ __align__(1024) unsigned char dsmem[];
+  __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], bar_tfull[2], bar_tempty[2], bar_drain;
+  __shared__ uint32_t tmem_base_sh;
+  __shared__ volatile uint32_t abort_sh;
+  const uint32_t base = (smem_u32(dsmem) + 1023u) & ~1023u;
+  const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t mtiles = (a.row_end - a.row_begin + BM - 1) / BM;
+  const uint32_t ntiles = (a.nq + BN - 1) / BN;
+  const uint32_t tiles = mtiles * ntiles;
+
+  if (threadIdx.x == 0) {
+    for (uint32_t s = 0; s < STAGES; s++) {
+      mbar_init(smem_u32(&bar_full[s]), 1);
+      mbar_init(smem_u32(&bar_empty[s]), 1);
+    }
+    for (uint32_t b = 0; b < 2; b++) {
+      mbar_init(smem_u32(&bar_tfull[b]), 1);
+      mbar_init(smem_u32(&bar_tempty[b]), 32 * EPI_WARPS);
+    }
+    mbar_init(smem_u32(&bar_drain), 1);
+    abort_sh = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base_sh;
+
+  if (warp == 0) {
+    if (lane == 0) {
+      // TMA producer
+      uint32_t stage = 0, phase = 0;
+      uint32_t pending = 0, last_parity = 0;     // per stage: a load in flight, parity of its phase
+      for (uint32_t t = blockIdx.x; t < tiles && !abort_sh; t += gridDim.x) {
+        const int row0 = (int)(a.row_begin + (t / ntiles) * BM);
+        const int q0 = (int)((t % ntiles) * BN);
+        for (uint32_t kb = 0; kb < a.kblocks; kb++) {
+          if (!mbar_wait(smem_u32(&bar_empty[stage]), phase ^ 1u, &abort_sh)) {
+            atomicOr(a.error, 1u);
+            abort_sh = 1;
+            break;
+          }
+          const uint32_t sA = base + stage * STAGE_BYTES, sB = sA + A_BYTES;
+          const uint32_t fb = smem_u32(&bar_full[stage]);
+          mbar_expect_tx(fb, STAGE_BYTES);
+          tma_load_2d(sA, &mapA, fb, (int)(kb * BK), row0);
+          tma_load_2d(sB, &mapB, fb, (int)(kb * BK), q0);
+          pending |= 1u << stage;
+          last_parity = (last_parity & ~(1u << stage)) | (phase << stage);
+          if (++stage == STAGES) {
+            stage = 0;
+            phase ^= 1u;
+          }
+        }
+      }
+      // no copy may land in shared memory after the CTA exits
+      for (uint32_t s = 0; s < STAGES; s++)
+        if (pending & (1u << s)) mbar_wait(smem_u32(&bar_full[s]), (last_parity >> s) & 1u, nullptr);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      // MMA issuer
+      uint32_t stage = 0, phase = 0, local = 0;
+      for (uint32_t t = blockIdx.x; t < tiles && !abort_sh; t += gridDim.x, local++) {
+        const uint32_t buf = local & 1u, tphase = (local >> 1) & 1u;
+        if (!mbar_wait(smem_u32(&bar_tempty[buf]), tphase ^ 1u, &abort_sh)) {
+          atomicOr(a.error, 2u);
+          abort_sh = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t d = tmem + buf * BN;
+        bool ok = true;
+        for (uint32_t kb = 0; kb < a.kblocks; kb++) {
+          if (!mbar_wait(smem_u32(&bar_full[stage]), phase, &abort_sh)) {
+            atomicOr(a.error, 2u);
+            abort_sh = 1;
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t sA = base + stage * STAGE_BYTES, sB = sA + A_BYTES;
+#pragma unroll
+          for (uint32_t k = 0; k < BK / 16; k++)
+            mma_bf16(d, sw128_desc(sA + k * 32), sw128_desc(sB + k * 32), (kb | k) != 0 ? 1u : 0u);
+          mma_commit(smem_u32(&bar_empty[stage]));
+          if (++stage == STAGES) {
+            stage = 0;
+            phase ^= 1u;
+          }
+        }
+        if (!ok) break;
+        mma_commit(smem_u32(&bar_tfull[buf]));
+      }
+      // every MMA issued has completed before TMEM is released
+      mma_commit(smem_u32(&bar_drain));
+      mbar_wait(smem_u32(&bar_drain), 0, nullptr);
+    }
+  } else {
+    // epilogue: warp w reads TMEM lanes 32 * (w % 4) .. + 31 (one row per
+    // thread) and one half of the 256 columns
+    const uint32_t quad = warp & 3u;
+    const uint32_t half = (warp - 2u) >> 2;
+    uint32_t local = 0;
+    for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x, local++) {
+      const uint32_t buf = local & 1u, tphase = (local >> 1) & 1u;
+      uint32_t ok = 1;
+      if (lane == 0) ok = mbar_wait(smem_u32(&bar_tfull[buf]), tphase, &abort_sh) ? 1u : 0u;
+      ok = __shfl_sync(0xffffffffu, ok, 0);     // the warp stays converged for tcgen05.ld
+      if (!ok) {
+        if (lane == 0) atomicOr(a.error, 4u);
+        abort_sh = 1;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t row0 = a.row_begin + (t / ntiles) * BM;
+      const uint32_t q0 = (t % ntiles) * BN;
+      const uint32_t row = row0 + quad * 32 + lane;
+      const bool in_range = row < a.row_end;
+      const bool rvalid = in_range && row != 0 && a.present[row];
+      const float sc = rvalid ? a.row_scale[row] : 0.f;
+      const float bi = rvalid ? a.row_bias[row] : 0.f;
+      for (uint32_t c = half * (BN / 64); c < (half + 1) * (BN / 64); c++) {
+        const uint32_t qb = q0 + c * 32;
+        if (qb >= a.nq) break;                   // warp-uniform
+        // lane j holds the threshold of query qb + j (+inf past the last query)
+        float my_thr = INFINITY;
+        if (!kDense && qb + lane < a.nq) my_thr = __ldg(a.thr + qb + lane);
+        uint32_t v[32];
+        tmem_ld32(tmem + ((quad * 32u) << 16) + buf * BN + c * 32, v);
+        tmem_ld_wait(v);
+        if (kDense) {
+          if (in_range) {
+#pragma unroll
+            for (uint32_t j = 0; j < 32; j++) {
+              const uint32_t q = qb + j;
+              const float s = fmaf(__uint_as_float(v[j]), sc, bi) + 0.0f;
+              if (q < a.nq) a.dense[(size_t)q * a.dense_ld + (row - a.row_begin)] = rvalid ? s : -INFINITY;
+            }
+          }
+        } else {
+#pragma unroll
+          for (uint32_t j = 0; j < 32; j++) {
+            const float t = __shfl_sync(0xffffffffu, my_thr, j);
+            const float s = fmaf(__uint_as_float(v[j]), sc, bi);
+            if (rvalid && s > t) {
+              const uint32_t q = qb + j;
+              const uint32_t slot = atomicAdd(a.cand_count + q, 1u);
+              if (slot < a.cap)
+                a.cand[(size_t)q * a.cap + slot] = ((unsigned long long)score_key(s) << 32) | row;
+              else
+                atomicOr(a.status + q, 1u);
+            }
+          }
+        }
+      }
+      tc_fence_before();
+      mbar_arrive(smem_u32(&bar_tempty[buf]));
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+  }
+}
+
+// The k-th smallest (1-based, 1 <= k <= n) of n distinct 64-bit keys in shared
+// memory: eight 8-bit radix passes; warp 0 scans the 256-bin histogram.
+__device__ unsigned long long block_select_u64(const unsigned long long* keys, uint32_t n, uint32_t k,
+                                               uint32_t* hist) {
+  __shared__ unsigned long long sh_prefix;
+  __shared__ uint32_t sh_need;
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  unsigned long long prefix = 0, mask = 0;
+  uint32_t need = k;
+  for (int shift = 56; shift >= 0; shift -= 8) {
+    for (uint32_t i = threadIdx.x; i < 256; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+      const unsigned long long x = keys[i];
+      if ((x & mask) == prefix) atomicAdd(&hist[(uint32_t)(x >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t c[8], sum = 0;
+#pragma unroll
+      for (int j = 0; j < 8; j++) {
+        c[j] = hist[lane * 8 + j];
+        sum += c[j];
+      }
+      uint32_t incl = sum;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, incl, off);
+        if (lane >= (uint32_t)off) incl += y;
+      }
+      const uint32_t excl = incl - sum;
+      const unsigned here = __ballot_sync(0xffffffffu, excl < need && incl >= need);
+      if (lane == (uint32_t)(__ffs(here) - 1)) {
+        uint32_t acc = excl, j = 0;
+        for (j = 0; j < 7; j++) {
+          if (acc + c[j] >= need) break;
+          acc += c[j];
+        }
+        sh_prefix = prefix | ((unsigned long long)(lane * 8 + j) << shift);
+        sh_need = need - acc;
+      }
+    }
+    __syncthreads();
+    prefix = sh_prefix;
+    need = sh_need;
+    mask |= 255ull << shift;
+    __syncthreads();
+  }
+  return prefix;
+}
+
+// Per query: the C best keys of the dense part -> first candidates and threshold.
+__global__ void __launch_bounds__(512)
+tc_first_select_kernel(const float* __restrict__ dense, uint32_t ld, uint32_t nrows, uint32_t C,
+                       float* __restrict__ thr, unsigned long long* __restrict__ cand,
+                       uint32_t* __restrict__ cand_count, uint32_t cap) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem);   // ld
+  __shared__ uint32_t hist[256];
+  __shared__ uint32_t sh_n, sh_m;
+  const uint32_t q = blockIdx.x;
+  if (threadIdx.x == 0) sh_n = sh_m = 0;
+  __syncthreads();
+  const float* S = dense + (size_t)q * ld;
+  for (uint32_t r = threadIdx.x; r < nrows; r += blockDim.x) {
+    const uint32_t key = score_key(S[r]);
+    if (key < kInvalidKey) keys[atomicAdd(&sh_n, 1u)] = ((unsigned long long)key << 32) | r;
+  }
+  __syncthreads();
+  const uint32_t n = sh_n;
+  unsigned long long kth = ~0ull;
+  if (n > C) kth = block_select_u64(keys, n, C, hist);
+  unsigned long long* out = cand + (size_t)q * cap;
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
+    const unsigned long long x = keys[i];
+    if (x <= kth) out[atomicAdd(&sh_m, 1u)] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    cand_count[q] = sh_m;
+    thr[q] = n > C ? key_score((uint32_t)(kth >> 32)) : -INFINITY;
+  }
+}
+
+// Per query, between two parts of the filtered rows: the C best candidate keys
+// are kept (written back in place) and the threshold moves up to the C-th.  The
+// rows still to come have larger ids, so the strict filter stays exact.
+__global__ void __launch_bounds__(512)
+tc_compact_kernel(unsigned long long* __restrict__ cand, uint32_t* __restrict__ cand_count, uint32_t cap, uint32_t C,
+                  float* __restrict__ thr, uint32_t* __restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem);   // cap
+  __shared__ uint32_t hist[256];
+  __shared__ uint32_t sh_m;
+  const uint32_t q = blockIdx.x;
+  uint32_t n = cand_count[q];
+  if (n <= C) return;                                   // uniform over the CTA
+  if (n > cap) {
+    if (threadIdx.x == 0) status[q] |= 1u;
+    n = cap;
+  }
+  unsigned long long* list = cand + (size_t)q * cap;
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) keys[i] = list[i];
+  if (threadIdx.x == 0) sh_m = 0;
+  __syncthreads();
+  const unsigned long long kth = block_select_u64(keys, n, C, hist);
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+    if (keys[i] <= kth) list[atomicAdd(&sh_m, 1u)] = keys[i];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    cand_count[q] = C;
+    thr[q] = key_score((uint32_t)(kth >> 32));
+  }
+}
+
+// Per query: top C approximate candidates, exact distances, sorted, first `size`.
+template <Metric M>
+__global__ void __launch_bounds__(256)
+tc_final_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_t q0, const unsigned long long* __restrict__ cand,
+                const uint32_t* __restrict__ cand_count, uint32_t cap, uint32_t C, uint32_t P, uint32_t size,
+                uint32_t group, ObjDist* __restrict__ out, uint32_t kmax, uint32_t* __restrict__ out_count,
+                uint32_t* __restrict__ status) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint4* qv = reinterpret_cast<uint4*>(smem);                                        // row_chunks
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(qv + g.row_chunks);  // cap
+  unsigned long long* sel = keys + cap;                                               // P
+  __shared__ uint32_t hist[256];
+  __shared__ uint32_t sh_m;
+  const uint32_t qi = blockIdx.x, q = q0 + qi;
+  const uint32_t rc = g.row_chunks;
+  for (uint32_t i = threadIdx.x; i < rc; i += blockDim.x) qv[i] = queries[(size_t)q * rc + i];
+  uint32_t n = cand_count[qi];
+  if (n > cap) n = cap;
+  const unsigned long long* src = cand + (size_t)qi * cap;
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) keys[i] = src[i];
+  if (threadIdx.x == 0) sh_m = 0;
+  __syncthreads();
+  unsigned long long kth = ~0ull;
+  if (n > C) kth = block_select_u64(keys, n, C, hist);
+  for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+    if (keys[i] <= kth) sel[atomicAdd(&sh_m, 1u)] = keys[i];
+  __syncthreads();
+  const uint32_t m = sh_m;
+  for (uint32_t i = m + threadIdx.x; i < P; i += blockDim.x) sel[i] = ~0ull;
+  // exact distances: groups of `group` lanes per row, as the plain linear search
+  const int G = (int)group;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int gl = lane & (G - 1);
+  const uint32_t gpw = 32 / G, ngroups = blockDim.x / G;
+  for (uint32_t b = warp * gpw; b < m; b += ngroups) {
+    const uint32_t i = b + (uint32_t)(lane / G);
+    const bool valid = i < m;
+    const uint32_t row = valid ? (uint32_t)sel[i] : 0u;
+    const float d = group_distance<ObjType::Float, M>(qv, g.objects + (size_t)row * rc, (int)rc, gl, G);
+    if (valid && gl == 0) sel[i] = pack_key(d, row);
+  }
+  __syncthreads();
+  // bitonic sort of P keys (P a power of two)
+  for (uint32_t k2 = 2; k2 <= P; k2 <<= 1) {
+    for (uint32_t j = k2 >> 1; j > 0; j >>= 1) {
+      for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+        const uint32_t l = i ^ j;
+        if (l > i) {
+          const unsigned long long x = sel[i], y = sel[l];
+          const bool up = (i & k2) == 0;
+          if ((x > y) == up) {
+            sel[i] = y;
+            sel[l] = x;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  const uint32_t kk = min(size, m);
+  for (uint32_t i = threadIdx.x; i < kk; i += blockDim.x)
+    out[(size_t)q * kmax + i] = ObjDist{key_id(sel[i]), key_dist(sel[i])};
+  if (threadIdx.x == 0) {
+    out_count[q] = kk;
+    if (status && cand_count[qi] > cap) status[q] |= 1u;
+  }
+}
+
+// bf16 rows (K padded to kpad) and the affine pair of each row.
+__global__ void tc_rows_kernel(const float* __restrict__ x, uint32_t nrows, uint32_t dpad, uint32_t kpad, int mode,
+                               __nv_bfloat16* __restrict__ out, float* __restrict__ scale, float* __restrict__ bias) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t row = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (row >= nrows) return;
+  const float* xr = x + (size_t)row * dpad;
+  __nv_bfloat16* o = out + (size_t)row * kpad;
+  float n2 = 0.f;
+  for (uint32_t c = lane; c < kpad; c += 32) {
+    const float v = c < dpad ? xr[c] : 0.f;
+    n2 = fmaf(v, v, n2);
+    o[c] = __float2bfloat16_rn(v);
+  }
+  for (int off = 16; off > 0; off >>= 1) n2 += __shfl_xor_sync(0xffffffffu, n2, off);
+  if (lane == 0) {
+    if (mode == 0) {            // L2 family
+      scale[row] = 1.f;
+      bias[row] = -0.5f * n2;
+    } else if (mode == 1) {     // cosine, angle
+      scale[row] = n2 > 0.f ? rsqrtf(n2) : 0.f;
+      bias[row] = 0.f;
+    } else {                    // rows of unit length
+      scale[row] = 1.f;
+      bias[row] = 0.f;
+    }
+  }
+}
+
+// bf16 query rows [nq_pad][kpad]; rows past nq and columns past dpad are zero.
+__global__ void tc_queries_kernel(const float* __restrict__ rows, uint32_t dpad, uint32_t nq, uint32_t nq_pad,
+                                  uint32_t kpad, __nv_bfloat16* __restrict__ out) {
+  const size_t n = (size_t)nq_pad * kpad;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t q = (uint32_t)(i / kpad), c = (uint32_t)(i % kpad);
+    out[i] = __float2bfloat16_rn(q < nq && c < dpad ? rows[(size_t)q * dpad + c] : 0.f);
+  }
+}
+
+typedef void (*FinalFn)(DevGraph, const uint4*, uint32_t, const unsigned long long*, const uint32_t*, uint32_t,
+                        uint32_t, uint32_t, uint32_t, uint32_t, ObjDist*, uint32_t, uint32_t*, uint32_t*);
+
+FinalFn final_kernel(Metric m) {
+  switch (m) {
+    case Metric::L2: return &tc_final_kernel<Metric::L2>;
+    case Metric::NormalizedL2: return &tc_final_kernel<Metric::NormalizedL2>;
+    case Metric::Cosine: return &tc_final_kernel<Metric::Cosine>;
+    case Metric::Angle: return &tc_final_kernel<Metric::Angle>;
+    case Metric::NormalizedCosine: return &tc_final_kernel<Metric::NormalizedCosine>;
+    case Metric::NormalizedAngle: return &tc_final_kernel<Metric::NormalizedAngle>;
+    default: return nullptr;
+  }
+}
+
+int row_mode(Metric m) {
+  switch (m) {
+    case Metric::L2:
+    case Metric::NormalizedL2:
+    case Metric::InnerProduct: return 0;
+    case Metric::Cosine:
+    case Metric::Angle: return 1;
+    case Metric::NormalizedCosine:
+    case Metric::NormalizedAngle: return 2;
+    default: return -1;
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess || q != cudaDriverEntryPointSuccess || p == nullptr)
+      throw std::runtime_error("cuTensorMapEncodeTiled is not available from the driver");
+    return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }();
+  return fn;
+}
+
+// 2-D bf16 tensor map over rows x kpad (row stride kpad * 2 bytes), box
+// BK x box_rows, 128-byte swizzle; reads past the last row return zeros.
+CUtensorMap make_map(const void* base, uint64_t rows, uint64_t kpad, uint32_t box_rows) {
+  CUtensorMap m;
+  cuuint64_t dims[2] = {kpad, rows};
+  cuuint64_t strides[1] = {kpad * 2};
+  cuuint32_t box[2] = {BK, box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return m;
+}
+
+uint32_t pow2_at_least(uint32_t v) {
+  uint32_t p = 1;
+  while (p < v) p <<= 1;
+  return p;
+}
+
+}  // namespace tc
+
+// Device state of the tensor-core linear search (built on first use).
+struct TcState {
+  __nv_bfloat16* rows = nullptr;   // [nrows][kpad]
+  float* scale = nullptr;
+  float* bias = nullptr;
+  uint32_t kpad = 0;
+  CUtensorMap mapA;
+  // scratch, grown on demand
+  void* scratch = nullptr;
+  size_t scratch_bytes = 0;
+  uint32_t* error = nullptr;
+  // phase timing of the last query batch: dense part + selection, filtered
+  // part (the score kernel over the remaining rows), final re-rank
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  float phase_ms[3] = {0.f, 0.f, 0.f};
+};
+
+void tc_release(TcState* s) {
+  if (!s) return;
+  cudaFree(s->rows);
+  cudaFree(s->scale);
+  cudaFree(s->bias);
+  cudaFree(s->scratch);
+  cudaFree(s->error);
+  for (cudaEvent_t e : s->ev)
+    if (e) cudaEventDestroy(e);
+  delete s;
+}
+
+bool GraphEngine::tc_supported() const {
+  return host_.prop.otype == ObjType::Float && tc::row_mode(host_.prop.metric) >= 0;
+}
+
+void GraphEngine::ensure_tc_rows() {
+  if (tc_) return;
+  if (!tc_supported())
+    throw std::runtime_error("the tensor-core linear search needs float objects and an L2, inner-product, cosine or "
+                             "angle distance");
+  std::unique_ptr<TcState> s(new TcState());
+  const uint32_t dpad = host_.dpad;
+  s->kpad = (dpad + tc::BK - 1) / tc::BK * tc::BK;
+  const size_t nrows = host_.nrows;
+  TC_CUDA(cudaMalloc(&s->rows, nrows * s->kpad * 2));
+  TC_CUDA(cudaMalloc(&s->scale, nrows * 4));
+  TC_CUDA(cudaMalloc(&s->bias, nrows * 4));
+  TC_CUDA(cudaMalloc(&s->error, 4));
+  for (cudaEvent_t& e : s->ev) TC_CUDA(cudaEventCreate(&e));
+  TC_CUDA(cudaMemsetAsync(s->error, 0, 4, stream_));
+  const unsigned blocks = (unsigned)((nrows + 7) / 8);
+  tc::tc_rows_kernel<<<blocks, 256, 0, stream_>>>(static_cast<const float*>(d_objects_), (uint32_t)nrows, dpad,
+                                                  s->kpad, tc::row_mode(host_.prop.metric), s->rows, s->scale,
+                                                  s->bias);
+  TC_CUDA(cudaGetLastError());
+  launches_++;
+  s->mapA = tc::make_map(s->rows, nrows, s->kpad, tc::BM);
+  TC_CUDA(cudaStreamSynchronize(stream_));
+  tc_ = s.release();
+}
+
+namespace {
+
+void launch_scores(const TcState& st, const CUtensorMap& mapB, tc::ScoreArgs a, bool dense, cudaStream_t s,
+                   int sms) {
+  const uint32_t mtiles = (a.row_end - a.row_begin + tc::BM - 1) / tc::BM;
+  const uint32_t tiles = mtiles * ((a.nq + tc::BN - 1) / tc::BN);
+  if (tiles == 0) return;
+  const unsigned grid = (unsigned)std::min<uint32_t>(tiles, (uint32_t)sms);
+  if (dense) {
+    TC_CUDA(cudaFuncSetAttribute((const void*)tc::tc_score_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc::SMEM_BYTES));
+    tc::tc_score_kernel<true><<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(st.mapA, mapB, a);
+  } else {
+    TC_CUDA(cudaFuncSetAttribute((const void*)tc::tc_score_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)tc::SMEM_BYTES));
+    tc::tc_score_kernel<false><<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(st.mapA, mapB, a);
+  }
+  TC_CUDA(cudaGetLastError());
+}
+
+void check_error(const TcState& st, cudaStream_t s) {
+  uint32_t err = 0;
+  TC_CUDA(cudaMemcpyAsync(&err, st.error, 4, cudaMemcpyDeviceToHost, s));
+  TC_CUDA(cudaStreamSynchronize(s));
+  if (err) {
+    TC_CUDA(cudaMemsetAsync(st.error, 0, 4, s));
+    throw std::runtime_error("tensor-core score kernel: a pipeline wait ran out (code " + std::to_string(err) + ")");
+  }
+}
+
+}  // namespace
+
+void GraphEngine::tc_scores_device(const uint4* d_rows, size_t nq, float* d_scores, size_t ld, cudaStream_t stream) {
+  std::lock_guard<std::mutex> lock(mu_);
+  TC_CUDA(cudaSetDevice(device_));
+  ensure_tc_rows();
+  if (nq == 0) return;
+  if (ld < host_.nrows) throw std::runtime_error("score stride smaller than the number of rows");
+  if (nq > (1u << 20)) throw std::runtime_error("at most 2^20 queries per call");
+  const TcState& st = *tc_;
+  int sms = 0;
+  TC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+  __nv_bfloat16* qb = nullptr;
+  const size_t nq_pad = (nq + tc::BN - 1) / tc::BN * tc::BN;
+  TC_CUDA(cudaMallocAsync(&qb, nq_pad * st.kpad * 2, stream));
+  tc::tc_queries_kernel<<<1024, 256, 0, stream>>>(reinterpret_cast<const float*>(d_rows), host_.dpad, (uint32_t)nq,
+                                                  (uint32_t)nq_pad, st.kpad, qb);
+  TC_CUDA(cudaGetLastError());
+  CUtensorMap mapB = tc::make_map(qb, nq_pad, st.kpad, tc::BN);
+  tc::ScoreArgs a{};
+  a.row_begin = 0;
+  a.row_end = (uint32_t)host_.nrows;
+  a.nq = (uint32_t)nq;
+  a.kblocks = st.kpad / tc::BK;
+  a.row_scale = st.scale;
+  a.row_bias = st.bias;
+  a.present = d_present_;
+  a.dense = d_scores;
+  a.dense_ld = (uint32_t)ld;
+  a.error = st.error;
+  launch_scores(st, mapB, a, true, stream, sms);
+  launches_ += 2;
+  TC_CUDA(cudaFreeAsync(qb, stream));
+  check_error(st, stream);
+}
+
+void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t size, size_t candidates,
+                                          ObjDist* d_out, size_t kmax, uint32_t* d_counts, uint32_t* d_status,
+                                          cudaStream_t stream) {
+  std::lock_guard<std::mutex> lock(mu_);
+  TC_CUDA(cudaSetDevice(device_));
+  ensure_tc_rows();
+  if (nq == 0) return;
+  if (size == 0) throw std::runtime_error("result size must be at least 1");
+  if (kmax < size) throw std::runtime_error("kmax smaller than the result size");
+  if (!d_status) throw std::runtime_error("a status buffer is required");
+  size_t C = candidates ? candidates : std::max<size_t>(4 * size, 64);
+  if (C < size) C = size;
+  if (C > 4096) throw std::runtime_error("at most 4096 candidates per query (and results <= candidates)");
+  const tc::FinalFn fin = tc::final_kernel(kernel_metric(host_.prop.metric));
+  if (!fin) throw std::runtime_error("unsupported distance for the tensor-core linear search");
+  const TcState& st = *tc_;
+  const uint32_t nrows = (uint32_t)host_.nrows;
+  // rows of the dense first part: >= C, a multiple of the tile height, <= 16384
+  size_t first = tc_first_rows_ ? tc_first_rows_ : 16384;
+  first = std::max<size_t>(first, C);
+  first = std::min<size_t>((first + tc::BM - 1) / tc::BM * tc::BM, 16384);
+  if (first < C) throw std::runtime_error("too many candidates for the dense first part");
+  const uint32_t r0 = (uint32_t)std::min<size_t>(first, nrows);
+  const uint32_t cap = std::min<uint32_t>(16384, std::max<uint32_t>(8192, tc::pow2_at_least((uint32_t)(4 * C))));
+  const uint32_t P = tc::pow2_at_least((uint32_t)C);
+  int sms = 0;
+  TC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+  const size_t qbmax = std::min<size_t>(nq, 16384);
+  // scratch: bf16 queries | dense scores | candidates | counts | thresholds
+  const size_t qbpad = (qbmax + tc::BN - 1) / tc::BN * tc::BN;
+  const size_t b_q = qbpad * st.kpad * 2;
+  const size_t b_d = (qbmax * (size_t)first * 4 + 255) / 256 * 256;
+  const size_t b_c = qbmax * (size_t)cap * 8;
+  const size_t need = b_q + b_d + b_c + 2 * qbmax * 4 + 512;
+  if (tc_->scratch_bytes < need) {
+    TC_CUDA(cudaStreamSynchronize(stream));
+    TC_CUDA(cudaFree(tc_->scratch));
+    tc_->scratch = nullptr;
+    tc_->scratch_bytes = 0;
+    TC_CUDA(cudaMalloc(&tc_->scratch, need));
+    tc_->scratch_bytes = need;
+  }
+  uint8_t* sp = static_cast<uint8_t*>(tc_->scratch);
+  __nv_bfloat16* qbuf = reinterpret_cast<__nv_bfloat16*>(sp);
+  float* dense = reinterpret_cast<float*>(sp + b_q);
+  unsigned long long* cand = reinterpret_cast<unsigned long long*>(sp + b_q + b_d);
+  uint32_t* ccount = reinterpret_cast<uint32_t*>(sp + b_q + b_d + b_c);
+  float* thr = reinterpret_cast<float*>(ccount + qbmax);
+  const uint32_t rc = dev_.row_chunks;
+  uint32_t group = 1;
+  while (group < rc && group < 32) group <<= 1;
+  const size_t fin_smem = (size_t)rc * 16 + (size_t)cap * 8 + (size_t)P * 8;
+  TC_CUDA(cudaFuncSetAttribute((const void*)fin, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fin_smem));
+  TC_CUDA(cudaFuncSetAttribute((const void*)tc::tc_first_select_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(first * 8)));
+  TC_CUDA(cudaFuncSetAttribute((const void*)tc::tc_compact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(cap * 8)));
+  TC_CUDA(cudaMemsetAsync(d_status, 0, nq * 4, stream));
+  for (size_t q0 = 0; q0 < nq; q0 += qbmax) {
+    const uint32_t nb = (uint32_t)std::min(qbmax, nq - q0);
+    const uint32_t nbpad = (nb + tc::BN - 1) / tc::BN * tc::BN;
+    TC_CUDA(cudaEventRecord(st.ev[0], stream));
+    const float* qrows = reinterpret_cast<const float*>(d_rows) + q0 * host_.dpad;
+    tc::tc_queries_kernel<<<1024, 256, 0, stream>>>(qrows, host_.dpad, nb, nbpad, st.kpad, qbuf);
+    TC_CUDA(cudaGetLastError());
+    CUtensorMap mapB = tc::make_map(qbuf, nbpad, st.kpad, tc::BN);
+    tc::ScoreArgs a{};
+    a.nq = nb;
+    a.kblocks = st.kpad / tc::BK;
+    a.row_scale = st.scale;
+    a.row_bias = st.bias;
+    a.present = d_present_;
+    a.error = st.error;
+    // dense first part
+    a.row_begin = 0;
+    a.row_end = r0;
+    a.dense = dense;
+    a.dense_ld = (uint32_t)first;
+    launch_scores(st, mapB, a, true, stream, sms);
+    tc::tc_first_select_kernel<<<nb, 512, first * 8, stream>>>(dense, (uint32_t)first, r0, (uint32_t)C, thr, cand,
+                                                               ccount, cap);
+    TC_CUDA(cudaGetLastError());
+    launches_ += 3;
+    TC_CUDA(cudaEventRecord(st.ev[1], stream));
+    // filtered rest, in parts that double in size; between two parts the
+    // candidate lists are cut back to C and the thresholds move up
+    a.dense = nullptr;
+    a.thr = thr;
+    a.cand = cand;
+    a.cand_count = ccount;
+    a.cap = cap;
+    a.status = d_status + q0;
+    for (uint32_t row = r0, part = std::max<uint32_t>(r0, tc::BM); row < nrows; part *= 2) {
+      const uint32_t end = (uint32_t)std::min<uint64_t>(nrows, (uint64_t)row + part);
+      a.row_begin = row;
+      a.row_end = end;
+      launch_scores(st, mapB, a, false, stream, sms);
+      launches_++;
+      if (end < nrows) {
+        tc::tc_compact_kernel<<<nb, 512, cap * 8, stream>>>(cand, ccount, cap, (uint32_t)C, thr, d_status + q0);
+        TC_CUDA(cudaGetLastError());
+        launches_++;
+      }
+      row = end;
+    }
+    TC_CUDA(cudaEventRecord(st.ev[2], stream));
+    fin<<<nb, 256, fin_smem, stream>>>(dev_, d_rows, (uint32_t)q0, cand, ccount, cap, (uint32_t)C, P,
+                                       (uint32_t)size, group, d_out, (uint32_t)kmax, d_counts, d_status);
+    TC_CUDA(cudaGetLastError());
+    TC_CUDA(cudaEventRecord(st.ev[3], stream));
+    launches_++;
+  }
+  check_error(st, stream);
+  for (int i = 0; i < 3; i++) TC_CUDA(cudaEventElapsedTime(&tc_->phase_ms[i], st.ev[i], st.ev[i + 1]));
+}
+
+void GraphEngine::tc_phase_ms(float* out) const {
+  for (int i = 0; i < 3; i++) out[i] = tc_ ? tc_->phase_ms[i] : 0.f;
+}
+
+}  // namespace ngtg

@@ -1,0 +1,161 @@
+"""Exhaustive search with the tensor-core pre-selection (tc_linear.cu) through the C ABI.
+
+The approximate scores are checked against numpy on the same bf16-rounded
+inputs (exactly on integer-valued data, where every product and partial sum is
+an integer below 2^24); the searches against the reference's own linear-search
+results of the golden fixtures (ObjectSpaceRepository::linearSearch,
+lib/NGT/ObjectSpaceRepository.h:860-922) and, on Gaussian-cluster data of the
+precision-path shape, against an FP64 exhaustive ground truth.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from golden_util import materialize
+
+pytestmark = pytest.mark.gpu
+
+FLOAT_LINEAR = ["c1_f32_l2", "f32_cosine", "f32_angle", "f32_ncosine", "f32_nl2"]
+
+
+@pytest.fixture(scope="module")
+def workdir(tmp_path_factory):
+    return str(tmp_path_factory.mktemp("gpu_tc"))
+
+
+def _bf16(x):
+    """Round float32 to bf16 (round to nearest even), returned as float64."""
+    b = np.ascontiguousarray(x, np.float32).view(np.uint32).astype(np.uint64)
+    b = ((b + 0x7FFF + ((b >> 16) & 1)) >> 16) << 16
+    return b.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def _linear_settings(meta):
+    return [(i, s) for i, s in enumerate(meta["settings"]) if s["op"] == "linear"]
+
+
+def _object_rows(path):
+    import oracle
+    f = oracle.IndexFiles(path)
+    return f, f.objects
+
+
+def test_scores_exact_on_integer_data(workdir):
+    from ngt_gb300 import Index
+    path, meta, queries, golden = materialize("c1_f32_l2", workdir)
+    f, obj = _object_rows(path)
+    x = obj[:, :128].astype(np.float64)
+    with Index(path, read_only=True) as ix:
+        s = ix.tc_scores(queries[:300])
+    q = queries[:300].astype(np.float64)
+    ref = q @ x[1:].T - 0.5 * (x[1:] ** 2).sum(1)[None, :]
+    assert np.isneginf(s[:, 0]).all()
+    assert np.array_equal(s[:, 1:], ref.astype(np.float32))
+
+
+@pytest.mark.parametrize("name", ["f32_cosine", "f32_ncosine", "f32_nl2"])
+def test_scores_float_metrics(name, workdir):
+    from ngt_gb300 import Index
+    path, meta, queries, golden = materialize(name, workdir)
+    with Index(path, read_only=True) as ix:
+        rows = ix.convert_queries(queries[:100]).view(np.float32)
+        s = ix.tc_scores(queries[:100])
+    f, obj = _object_rows(path)
+    x = obj[1:].astype(np.float32)
+    d = x.shape[1]
+    qb, xb = _bf16(rows[:, :d]), _bf16(x)
+    dot = qb @ xb.T
+    x64 = x.astype(np.float64)
+    n2 = (x64 ** 2).sum(1)
+    if name == "f32_cosine":
+        ref = dot / np.sqrt(n2)[None, :]
+    elif name == "f32_nl2":
+        ref = dot - 0.5 * n2[None, :]
+    else:
+        ref = dot
+    tol = 1e-5 * np.abs(ref).max() + 1e-6
+    assert np.abs(s[:, 1:] - ref).max() <= tol
+
+
+@pytest.mark.parametrize("first_rows", [0, 256])
+@pytest.mark.parametrize("name", FLOAT_LINEAR)
+def test_linear_search_matches_reference(name, first_rows, workdir):
+    """Both the dense-only path (0: every row of these indexes is scored densely)
+    and the threshold filter (256 dense rows) return the reference's results."""
+    from ngt_gb300 import Index
+    path, meta, queries, golden = materialize(name, workdir)
+    for i, s in _linear_settings(meta):
+        nq, k = s["nq"], s["k"]
+        gi, gd, gc = golden["ids_%d" % i], golden["dist_%d" % i], golden["count_%d" % i]
+        with Index(path, read_only=True) as ix:
+            ids, ds, n, status = ix.linear_search_tc(queries[:nq], k=k, candidates=max(64, 4 * k),
+                                                     first_rows=first_rows)
+        assert (status == 0).all()
+        assert np.array_equal(n, gc)
+        if name == "c1_f32_l2":
+            assert np.array_equal(ids, gi) and np.array_equal(ds.view(np.uint32), gd.view(np.uint32))
+        else:
+            # float metrics: the reference sums with AVX lanes; distances within
+            # 1e-5 relative (floor 0.1), ids equal except across near-ties
+            tol = 1e-5 * np.maximum(np.abs(gd), 0.1)
+            assert (np.abs(ds - gd) <= tol).mean() > 0.99, name
+            assert (ids == gi).all(1).mean() >= 0.98, name
+
+
+def test_linear_search_equals_plain_linear_search(workdir):
+    """Ids and distances equal the plain GPU linear search bit for bit."""
+    from ngt_gb300 import Index
+    path, meta, queries, golden = materialize("f32_cosine", workdir)
+    with Index(path, read_only=True) as ix:
+        ids, ds, n, status = ix.linear_search_tc(queries[:50], k=20, candidates=128, first_rows=128)
+        for j in range(50):
+            r = ix.linear_search(queries[j], k=20)
+            assert [o.id for o in r] == list(ids[j, : n[j]])
+            assert np.array_equal(np.array([o.distance for o in r], np.float32), ds[j, : n[j]])
+
+
+def test_query_batches_and_repeats(workdir):
+    """More queries than one batch (8192): every copy of a query gets the same result."""
+    from ngt_gb300 import Index
+    path, meta, queries, golden = materialize("c1_f32_l2", workdir)
+    reps = np.tile(queries[:100], (90, 1))            # 9000 queries
+    with Index(path, read_only=True) as ix:
+        ids, ds, n, status = ix.linear_search_tc(reps, k=10, candidates=64, first_rows=512)
+    assert (status == 0).all()
+    gi = golden["ids_10"][:100]
+    for r in range(90):
+        assert np.array_equal(ids[r * 100:(r + 1) * 100], gi)
+
+
+def _cluster_index(tmp, n=20000, dim=768, nq=200, seed=21):
+    """Gaussian-cluster float rows (64 means ~ N(0,1), sigma 0.5), L2-normalised,
+    written as a NormalizedCosine index; queries from the same mixture."""
+    from ngt_gb300.graph_build import write_index
+    rng = np.random.default_rng(seed)
+    means = rng.standard_normal((64, dim)).astype(np.float32)
+    x = means[rng.integers(0, 64, n)] + 0.5 * rng.standard_normal((n, dim)).astype(np.float32)
+    q = means[rng.integers(0, 64, nq)] + 0.5 * rng.standard_normal((nq, dim)).astype(np.float32)
+    x /= np.linalg.norm(x, axis=1, keepdims=True)
+    path = os.path.join(tmp, "clusters")
+    ring = np.concatenate([[0], np.arange(2, n + 1), [1]]).astype(np.uint32)[1:]   # node i -> i % n + 1
+    offsets = np.concatenate([[0, 0], np.arange(1, n + 1)]).astype(np.int64)
+    write_index(path, x, offsets, ring, np.zeros(n, np.float32),
+                extra_prf={"DistanceType": "NormalizedCosine", "EdgeSizeForSearch": "10"})
+    return path, x, q
+
+
+def test_fp64_ground_truth_on_clusters(workdir):
+    """k=100 with 400 candidates on 20,000 x 768 normalised cluster data: every
+    returned id is within the FP64 top 100 (ties at the cut allowed)."""
+    from ngt_gb300 import Index
+    path, x, q = _cluster_index(workdir)
+    qn = q.astype(np.float64) / np.linalg.norm(q.astype(np.float64), axis=1, keepdims=True)
+    d64 = 1.0 - qn @ x.astype(np.float64).T
+    kth = np.sort(d64, axis=1)[:, 99]
+    with Index(path, read_only=True) as ix:
+        ids, ds, n, status = ix.linear_search_tc(q, k=100, candidates=400, first_rows=2048)
+    assert (status == 0).all() and (n == 100).all()
+    got = np.take_along_axis(d64, ids.astype(np.int64) - 1, axis=1)
+    assert (got <= kth[:, None] + 1e-6).all()
+    assert (np.diff(ds, axis=1) >= 0).all()
