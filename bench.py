@@ -15,7 +15,12 @@ Workload (the benchmark's plain-vs-batched graph-search configuration):
            one-query-per-CTA kernel (the reference-order search; reported in
            config.plain_fp32).  Also reported: the serving loop's latency, the
            quantized-graph search and scalar-quantized (QSUInteger-8B) objects
-           over the same graph.
+           over the same graph, and (`brute_force_precision`) the exact
+           brute-force k=100 search of 1,000,000 x 768 Gaussian-cluster rows
+           (NormalizedCosine) with the tensor-core pre-selection: bf16 scores
+           on tcgen05 with fp32 accumulation, 400 candidates re-ranked in fp32,
+           ids checked against an FP64 ground truth.  --precision-path prints
+           that measurement alone as its own line.
 
 A step is one pass of all queries through the search.  `value` is queries/s
 with queries resident in HBM (ngtgpu_search_batch_device); `e2e` is the same
@@ -92,6 +97,8 @@ def parse():
     ap.add_argument("--precision-path", action="store_true",
                     help="measure the exact brute-force k-NN with the tensor-core pre-selection instead "
                          "(Gaussian-cluster rows, NormalizedCosine, k=100, 400 candidates)")
+    ap.add_argument("--precision", type=int, default=1,
+                    help="also measure the tensor-core brute-force search (1) or not (0) in the default run")
     ap.add_argument("--pp-n", type=int, default=1_000_000, help="rows of the brute-force workload")
     ap.add_argument("--pp-nq", type=int, default=10_000, help="queries of the brute-force workload")
     ap.add_argument("--pp-first-rows", type=int, default=0, help="dense rows before the threshold filter (0 auto)")
@@ -504,7 +511,7 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def precision_path(args):
+def precision_path(args, steps=None, warmup=None):
     """Exact brute-force k-NN with the tensor-core pre-selection.
 
     Workload: n x 768 float32 rows drawn from 64 Gaussian clusters (means N(0,1),
@@ -551,13 +558,15 @@ def precision_path(args):
                                                     ix._err)
         ix._check(ok)
 
-    for _ in range(max(3, args.warmup)):
+    steps = steps or args.steps
+    warmup = max(3, warmup or args.warmup)
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
     times, phases = [], []
     launches0 = ix.kernel_launches()
     with ClockSampler(0) as clocks:
-        for _ in range(args.steps):
+        for _ in range(steps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             step()
@@ -565,12 +574,12 @@ def precision_path(args):
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
             phases.append(ix.tc_phase_times())
-    launches = (ix.kernel_launches() - launches0) // max(1, args.steps)
+    launches = (ix.kernel_launches() - launches0) // max(1, steps)
     ms = statistics.median(times)
     ph = [statistics.median(p[i] for p in phases) for i in range(3)]
     # e2e: host queries in, host results out, through the host-buffer call
     e2e = []
-    for _ in range(max(2, args.steps // 2)):
+    for _ in range(max(2, steps // 2)):
         torch.cuda.synchronize()
         t = time.perf_counter()
         ix.linear_search_tc(q, k=k, candidates=C, first_rows=args.pp_first_rows)
@@ -595,7 +604,7 @@ def precision_path(args):
         ix.linear_search(q[j], k=k)
         plain.append(time.perf_counter() - t)
     plain_qps = 1.0 / statistics.median(plain)
-    first = args.pp_first_rows or 16384
+    first = args.pp_first_rows or 8192
     flops_filter = 2.0 * nq * max(0, n + 1 - first) * dim
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
@@ -604,7 +613,7 @@ def precision_path(args):
     return {
         "metric": "queries/s, exact brute-force k=100 (1M x 768 cosine, bf16 tensor-core scores + fp32 re-rank "
                   "of 400)" if n == 1_000_000 else "queries/s, exact brute-force k=100 (n=%d x 768 cosine)" % n,
-        "value": nq / (ms * 1e-3), "unit": "queries/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "value": nq / (ms * 1e-3), "unit": "queries/s", "n_gpus": 1, "steps": steps, "warmup": warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "replicas only", "vs_baseline": None,
         "dtype": "bf16+f32-rerank", "data": "synthetic (seeded Gaussian clusters)",
         "config": {"workload": "brute-force %d x %d NormalizedCosine, %d queries, k=%d, candidates=%d" % (
@@ -823,6 +832,18 @@ def main():
             qs8 = {"error": str(ex)}
             log("qs8 measurement failed: %s" % ex)
 
+    # ---- exact brute force with the tensor-core pre-selection (rank 0) ---------------------------
+    pp = None
+    if args.precision and rank == 0 and world == 1:
+        try:
+            pp = precision_path(args, steps=max(3, args.steps // 3), warmup=args.warmup)
+            for key in ("metric", "unit", "n_gpus", "higher_is_better", "scaling", "vs_baseline", "data"):
+                pp.pop(key, None)
+            log("brute force: %s" % pp)
+        except Exception as ex:                 # reported, never fatal to the headline measurement
+            pp = {"error": str(ex)}
+            log("brute-force measurement failed: %s" % ex)
+
     # ---- CPU baseline (oracle port on a bounded sample) ------------------------------------------
     cpu = None
     if rank == 0:
@@ -875,6 +896,7 @@ def main():
                        "warp_per_query_kernel_rates": served_warp} if served else None,
             "quantized_graph": qg,
             "scalar_quantized": qs8,
+            "brute_force_precision": pp,
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

@@ -153,7 +153,7 @@ bool ngtgpu_tc_scores_device(NGTIndex, const void *d_rows, size_t nq, float *d_s
 bool ngtgpu_tc_phase_times(NGTIndex, float *ms3, NGTError);
 /* Objects scored densely before the per-query threshold filter of the
  * tensor-core search (rounded up to a multiple of 128, at least `candidates`,
- * at most 16384; 0 = automatic, 16384).  Results do not depend on it. */
+ * at most 16384; 0 = automatic, 8192).  Results do not depend on it. */
 bool ngtgpu_set_tc_first_rows(NGTIndex, size_t rows, NGTError);
 /* Serving loop (continuous batching).  A server keeps up to `inflight`
  * batched-kernel launches on the GPU at once, each on its own stream and

@@ -139,7 +139,7 @@ class GraphEngine {
   // CUDA-event times (ms) of the last query batch of linear_search_tc_device:
   // dense part with its selection, filtered part, final re-rank
   void tc_phase_ms(float* out) const;
-  // rows scored densely before the threshold filter (0: automatic, 16384)
+  // rows scored densely before the threshold filter (0: automatic, 8192)
   void set_tc_first_rows(size_t rows) { tc_first_rows_ = rows; }
   // Exhaustive search (exact ids, ties broken by id).
   void linear_search(const void* queries, QueryType qt, size_t nq, size_t qdim, size_t size, SearchOutput& out);

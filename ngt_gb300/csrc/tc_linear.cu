@@ -17,9 +17,11 @@
 //      N = 256 queries, K = 16 per instruction), operands staged by TMA
 //      (cp.async.bulk.tensor, 128-byte swizzle) through a 4-stage mbarrier
 //      pipeline, accumulators double-buffered in TMEM (2 x 256 columns) and
-//      read back with tcgen05.ld by four epilogue warps.  The first
-//      `first_rows` rows are written out densely; on the remaining rows the
-//      epilogue keeps only scores that beat the query's threshold.
+//      read back with tcgen05.ld by eight epilogue warps (two per TMEM lane
+//      quadrant).  The first `first_rows` rows are written out densely; on the
+//      remaining rows, taken in parts that double in size, the epilogue keeps
+//      only scores that beat the query's threshold, and tc_compact_kernel cuts
+//      each list back to the C best and raises the threshold between two parts.
 //   3. tc_first_select_kernel: per query, the C best scores of the dense part
 //      (exact radix select on 64-bit (score key, row) keys); the C-th becomes
 //      the threshold, and the C keys the first candidates.  Every row past the
@@ -313,6 +315,14 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
     uint32_t local = 0;
     for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x, local++) {
       const uint32_t buf = local & 1u, tphase = (local >> 1) & 1u;
+      // what does not depend on the accumulator is loaded before the wait
+      const uint32_t row0 = a.row_begin + (t / ntiles) * BM;
+      const uint32_t q0 = (t % ntiles) * BN;
+      const uint32_t row = row0 + quad * 32 + lane;
+      const bool in_range = row < a.row_end;
+      const bool rvalid = in_range && row != 0 && a.present[row];
+      const float sc = rvalid ? a.row_scale[row] : 0.f;
+      const float bi = rvalid ? a.row_bias[row] : 0.f;
       uint32_t ok = 1;
       if (lane == 0) ok = mbar_wait(smem_u32(&bar_tfull[buf]), tphase, &abort_sh) ? 1u : 0u;
       ok = __shfl_sync(0xffffffffu, ok, 0);     // the warp stays converged for tcgen05.ld
@@ -322,13 +332,6 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
         break;
       }
       tc_fence_after();
-      const uint32_t row0 = a.row_begin + (t / ntiles) * BM;
-      const uint32_t q0 = (t % ntiles) * BN;
-      const uint32_t row = row0 + quad * 32 + lane;
-      const bool in_range = row < a.row_end;
-      const bool rvalid = in_range && row != 0 && a.present[row];
-      const float sc = rvalid ? a.row_scale[row] : 0.f;
-      const float bi = rvalid ? a.row_bias[row] : 0.f;
       for (uint32_t c = half * (BN / 64); c < (half + 1) * (BN / 64); c++) {
         const uint32_t qb = q0 + c * 32;
         if (qb >= a.nq) break;                   // warp-uniform
@@ -803,7 +806,8 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
   const TcState& st = *tc_;
   const uint32_t nrows = (uint32_t)host_.nrows;
   // rows of the dense first part: >= C, a multiple of the tile height, <= 16384
-  size_t first = tc_first_rows_ ? tc_first_rows_ : 16384;
+  // (automatic: 8192; the threshold then tightens between the doubling parts)
+  size_t first = tc_first_rows_ ? tc_first_rows_ : 8192;
   first = std::max<size_t>(first, C);
   first = std::min<size_t>((first + tc::BM - 1) / tc::BM * tc::BM, 16384);
   if (first < C) throw std::runtime_error("too many candidates for the dense first part");
