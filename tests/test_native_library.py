@@ -129,6 +129,31 @@ def test_null_arguments_return_false_with_message(lib):
     assert "parametor error" in lib.ngt_get_error_string(err).decode()
 
 
+def test_tensor_core_search_rejects_null_arguments(lib):
+    """The tensor-core exhaustive search entry points check their handles and
+    buffers before any device work."""
+    lib.ngt_create_error_object.restype = ctypes.c_void_p
+    lib.ngt_get_error_string.restype = ctypes.c_char_p
+    lib.ngt_get_error_string.argtypes = [ctypes.c_void_p]
+    vp, sz = ctypes.c_void_p, ctypes.c_size_t
+    calls = {
+        "ngtgpu_linear_search_tc_float": ([vp, vp, sz, ctypes.c_int32, sz, sz, vp, sz, vp, vp, vp],
+                                          (None, None, 4, 8, 10, 0, None, 10, None, None)),
+        "ngtgpu_linear_search_tc_device": ([vp, vp, sz, sz, sz, vp, sz, vp, vp, vp, vp],
+                                           (None, None, 4, 10, 0, None, 10, None, None, None)),
+        "ngtgpu_tc_scores_device": ([vp, vp, sz, vp, sz, vp, vp], (None, None, 4, None, 100, None)),
+        "ngtgpu_set_tc_first_rows": ([vp, sz, vp], (None, 0)),
+        "ngtgpu_tc_phase_times": ([vp, vp, vp], (None, None)),
+    }
+    for name, (argtypes, args) in calls.items():
+        fn = getattr(lib, name)
+        fn.argtypes = argtypes
+        fn.restype = ctypes.c_bool
+        err = ctypes.c_void_p(lib.ngt_create_error_object())
+        assert not fn(*args, err), name
+        assert "parametor error" in lib.ngt_get_error_string(err).decode(), name
+
+
 @pytest.mark.parametrize("damage", ["truncate_qg_grp", "missing_qr", "short_codebook", "bad_qg_edge", "no_qg",
                                     "wrong_metric"])
 def test_qg_loader_rejects_damaged_quantized_graph(lib, tmp_path, damage):
