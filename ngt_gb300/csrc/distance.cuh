@@ -117,8 +117,13 @@ struct Acc {
           f1 = __fmaf_rn(a[i], a[i], f1);
           f2 = __fmaf_rn(b[i], b[i], f2);
         } else if constexpr (M == Metric::Lorentz) {
+          // compensated (float-float) sum of the exact products: the reference sums
+          // them in double, and acosh near 1 magnifies the error of a plain float sum
           float p = a[i] * b[i];
-          if (chunk_index == 0 && i == 0) f0 += p; else f0 -= p;
+          float pe = __fmaf_rn(a[i], b[i], -p);
+          if (!(chunk_index == 0 && i == 0)) { p = -p; pe = -pe; }
+          two_sum_acc(f0, f1, p);
+          f1 += pe;
         }
       }
     }
@@ -133,10 +138,26 @@ struct Acc {
   static constexpr bool kUseF0 = !kUseI0;
   static constexpr bool kUseF12 = !kUseI0 && (M == Metric::Cosine || M == Metric::Angle || M == Metric::Poincare);
 
+  // hi += x with the rounding error of the addition carried into lo (Knuth's TwoSum)
+  static __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+    float s = hi + x;
+    float bb = s - hi;
+    float err = (hi - (s - bb)) + (x - bb);
+    hi = s;
+    lo += err;
+  }
+
   __device__ __forceinline__ void reduce(int width) {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       if (off < width) {
+        if constexpr (M == Metric::Lorentz) {
+          float h = __shfl_xor_sync(0xffffffffu, f0, off), l = __shfl_xor_sync(0xffffffffu, f1, off);
+          // the same partner order on both lanes of a pair: the two lanes end equal
+          two_sum_acc(f0, f1, h);
+          f1 += l;
+          continue;
+        }
         if constexpr (kUseF0) f0 += __shfl_xor_sync(0xffffffffu, f0, off);
         if constexpr (kUseF12) {
           f1 += __shfl_xor_sync(0xffffffffu, f1, off);
@@ -183,10 +204,15 @@ struct Acc {
       float c = f0 / sqrtf(f1 * f2);
       return c >= 1.f ? 0.f : (c <= -1.f ? acosf(-1.f) : acosf(c));
     } else if constexpr (M == Metric::Poincare) {
-      float c2 = sqrtf(f0);
-      return acoshf(1.f + 2.f * c2 * c2 / (1.f - f1) / (1.f - f2));
+      // acosh(1 + x) = log1p(x + sqrt(x (x + 2))): keeps the precision of small x,
+      // which 1 + x in float would round away (the reference evaluates it in double)
+      float x = 2.f * f0 / (1.f - f1) / (1.f - f2);
+      return log1pf(x + sqrtf(x * (x + 2.f)));
     } else if constexpr (M == Metric::Lorentz) {
-      return acoshf(f0);
+      // s - 1 from the float-float sum (s >= 1 on the hyperboloid), then acosh as above
+      float e = (f0 - 1.f) + f1;
+      if (!(e >= 0.f)) return e != e ? e : 0.f;
+      return log1pf(e + sqrtf(e * (e + 2.f)));
     } else {
       return 0.f;
     }

@@ -97,6 +97,10 @@ GraphEngine::GraphEngine(const std::string& path, GraphMode mode, bool quantized
   NGT_CUDA(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
   upload();
   if (quantized) upload_qg();
+  // The no-allocation search's fixed scratch and the exact kernel live in modules
+  // that CUDA loads lazily; loading them here, while the index opens, keeps that
+  // search's first call free of the module loads (and the reservation they make).
+  noalloc_prepare_device(device_, (const void*)exact_kernel(host_.prop.otype, host_.prop.metric));
 }
 
 GraphEngine::GraphEngine(const std::string& qbg_dir, bool blobs) : mode_(GraphMode::Updatable) {
@@ -629,10 +633,8 @@ uint32_t GraphEngine::visited_hash_capacity() const { return host_.nrows >= (1u 
 // more CTAs per SM: 1M x 128: plain kernel +17 %, QG +18 %, results unchanged).
 uint32_t GraphEngine::candidate_list_capacity() const { return host_.nrows >= (1u << 18) ? 512u : 1024u; }
 
-void GraphEngine::launch_exact(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
-                               uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats,
-                               cudaStream_t stream) {
-  ExactConfig cfg{};
+size_t GraphEngine::exact_launch_config(uint32_t max_size, ExactConfig& cfg) const {
+  cfg = ExactConfig{};
   cfg.kcap = max_size + 1;
   cfg.ccap = std::max<uint32_t>(candidate_list_capacity(), std::min<uint32_t>(1024, next_pow2(cfg.kcap)));
   cfg.hcap = visited_hash_capacity();
@@ -652,6 +654,14 @@ void GraphEngine::launch_exact(const uint4* d_rows, size_t nq, const QueryParams
     smem = exact_smem_bytes(dev_.row_chunks, cfg);
   }
   if (smem > (size_t)max_smem) throw std::runtime_error("result size too large for the on-chip search state");
+  return smem;
+}
+
+void GraphEngine::launch_exact(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
+                               uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats,
+                               cudaStream_t stream) {
+  ExactConfig cfg;
+  const size_t smem = exact_launch_config(max_size, cfg);
   ExactKernelFn fn = exact_kernel(host_.prop.otype, host_.prop.metric);
   NGT_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   int per_sm = 0, sms = 0;
@@ -735,7 +745,10 @@ void GraphEngine::launch_wide(const uint4* d_rows, size_t nq, const QueryParams*
 void GraphEngine::launch_fast(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
                               uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats,
                               cudaStream_t stream, Kernel kernel, FastScratch& scratch) {
-  const bool bf16 = kernel == Kernel::Fast && host_.prop.otype == ObjType::Float;
+  // hyperbolic metrics search on the fp32 rows: acosh near 1 magnifies bf16 rounding
+  // of the coordinates far beyond what the exact re-rank of a few candidates can repair
+  const bool hyperbolic = host_.prop.metric == Metric::Poincare || host_.prop.metric == Metric::Lorentz;
+  const bool bf16 = kernel == Kernel::Fast && host_.prop.otype == ObjType::Float && !hyperbolic;
   FastKernelFn fn = fast_kernel(host_.prop.otype, host_.prop.metric, bf16, tuning_.rows_in_flight,
                                 tuning_.ctas_per_sm);
   if (!fn) throw std::runtime_error("the batched kernel does not support this index type or tuning");
@@ -905,26 +918,8 @@ void GraphEngine::search_device_noalloc(void* scratch, size_t scratch_bytes, con
   std::vector<uint32_t> seeds;
   uint32_t max_size = 0;
   build_params(args, nargs, nq, kmax, params, seeds, max_size);
-  ExactConfig cfg{};
-  cfg.kcap = max_size + 1;
-  cfg.ccap = std::max<uint32_t>(candidate_list_capacity(), std::min<uint32_t>(1024, next_pow2(cfg.kcap)));
-  cfg.hcap = visited_hash_capacity();
-  cfg.mode = (uint32_t)mode_;
-  cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));
-  cfg.bitmap_words = (host_.nrows + 31) / 32;
-  cfg.ocap = kOverflowCapacity;
-  int max_smem = 0;
-  NGT_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
-  size_t smem = exact_smem_bytes(dev_.row_chunks, cfg);
-  while (smem > (size_t)max_smem && cfg.hcap > 2048) {
-    cfg.hcap >>= 1;
-    smem = exact_smem_bytes(dev_.row_chunks, cfg);
-  }
-  while (smem > (size_t)max_smem && cfg.ccap > 256) {
-    cfg.ccap >>= 1;
-    smem = exact_smem_bytes(dev_.row_chunks, cfg);
-  }
-  if (smem > (size_t)max_smem) throw std::runtime_error("result size too large for the on-chip search state");
+  ExactConfig cfg;
+  const size_t smem = exact_launch_config(max_size, cfg);
   // scratch layout: params | seeds | bitmaps[grid] | overflow[grid], each 256-byte aligned
   auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
   const size_t params_bytes = up(nq * sizeof(QueryParams));

@@ -34,3 +34,19 @@ def random_bytes(n: int, dim: int, seed: int, p_one: float = 0.5) -> np.ndarray:
     rng = np.random.default_rng(seed)
     bits = (rng.random((n, dim * 8)) < p_one).astype(np.uint8)
     return np.packbits(bits, axis=1, bitorder="little").astype(np.float32)
+
+
+def poincare_ball(n: int, dim: int, nclusters: int, seed_means: int, seed: int) -> np.ndarray:
+    """Gaussian-mixture points mapped into the open unit ball (x / (1 + |x|) x 0.9),
+    valid objects of a Poincare index."""
+    x = gaussian_mixture(n, dim, nclusters, seed_means, seed).astype(np.float64)
+    x *= 0.9 / (1.0 + np.linalg.norm(x, axis=1, keepdims=True))
+    return x.astype(np.float32)
+
+
+def lorentz_hyperboloid(n: int, dim: int, nclusters: int, seed_means: int, seed: int) -> np.ndarray:
+    """Points of the hyperboloid x0 = sqrt(1 + |x_rest|^2) (x_rest a scaled Gaussian
+    mixture of dim - 1 coordinates), valid objects of a Lorentz index."""
+    y = 0.5 * gaussian_mixture(n, dim - 1, nclusters, seed_means, seed).astype(np.float64)
+    x0 = np.sqrt(1.0 + (y * y).sum(1, keepdims=True))
+    return np.concatenate([x0, y], axis=1).astype(np.float32)

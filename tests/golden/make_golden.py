@@ -141,12 +141,45 @@ FIXTURES = {
         regenerate_obj=True, otype="f", qg=dict(create="", build="-E 64"),
         settings=[("qg", 10, 0.1, 3.0, "rw"), ("qg", 10, 0.02, 3.0, "rw"), ("qg", 10, 0.1, 0.0, "rw"),
                   ("qg", 20, 0.1, 1.5, "rw"), ("qg", 10, 0.1, 1.0, "rw")]),
+    # Inner product: stored as L2 over (D+1)-dimensional rows whose last element is
+    # sqrt(MaxMagnitude - |x|^2) (lib/NGT/Index.cpp:455-640).  `ngt create` with a data
+    # file stops with "Index is unavailable" for this distance (its createIndex reaches
+    # getIndex() on a bare GraphAndTreeIndex, lib/NGT/Index.cpp:189-214,914-930), so the
+    # index is created empty and filled by `ngt append`, the path that computes the
+    # magnitudes.  The object file holds the augmented rows, so it is stored.
+    "f32_ip": dict(
+        base=("gaussian_mixture", dict(n=2000, dim=32, nclusters=16, seed_means=201, seed=202)),
+        query=("gaussian_mixture", dict(n=200, dim=32, nclusters=16, seed_means=201, seed=203)),
+        create="-d 32 -o f -D i -E 10 -S 40 -i t", append=True, regenerate_obj=False, otype="f",
+        settings=[("graph", 10, 0.1, None, "ro"), ("graph", 10, 0.1, None, "rw"), ("graph", 20, 0.2, None, "ro"),
+                  ("linear", 10, 0.0, None, "ro")]),
+    "f32_poincare": dict(
+        base=("poincare_ball", dict(n=2000, dim=16, nclusters=16, seed_means=211, seed=212)),
+        query=("poincare_ball", dict(n=200, dim=16, nclusters=16, seed_means=211, seed=213)),
+        create="-d 16 -o f -D p -E 10 -S 40 -i t", regenerate_obj=True, otype="f",
+        settings=[("graph", 10, 0.1, None, "ro"), ("linear", 10, 0.0, None, "ro")]),
+    "f32_lorentz": dict(
+        base=("lorentz_hyperboloid", dict(n=2000, dim=16, nclusters=16, seed_means=221, seed=222)),
+        query=("lorentz_hyperboloid", dict(n=200, dim=16, nclusters=16, seed_means=221, seed=223)),
+        create="-d 16 -o f -D l -E 10 -S 40 -i t", regenerate_obj=True, otype="f",
+        settings=[("graph", 10, 0.1, None, "ro"), ("linear", 10, 0.0, None, "ro")]),
     "qg_f32_l2_d64_q2": dict(
         base=("clipped_exponential", dict(n=2000, dim=64, seed=171)),
         query=("clipped_exponential", dict(n=200, dim=64, seed=172)),
         create="-d 64 -o f -D 2 -E 16 -S 40 -i t",
         regenerate_obj=True, otype="f", qg=dict(create="-Q 2", build="-Q 2 -E 48"),
         settings=[("qg", 10, 0.1, 3.0, "rw"), ("qg", 10, 0.1, 0.0, "rw")]),
+    # The quantized-graph shape of the 1M x 100 angular workload at small scale:
+    # unit-normalised Gaussian-cluster vectors of dimension 100 (pseudo-dimension
+    # 112, so 56 two-dimensional subspaces of which 6 are zero padding), an ONNG
+    # (10 outgoing / 100 incoming edges), rotation by the optimizer's default.
+    "qg_f32_l2_d100_q2": dict(
+        base=("gaussian_mixture", dict(n=3000, dim=100, nclusters=30, seed_means=231, seed=232, normalize=True)),
+        query=("gaussian_mixture", dict(n=200, dim=100, nclusters=30, seed_means=231, seed=233, normalize=True)),
+        create="-d 100 -o f -D 2 -E 100 -S 0 -e 0.1 -i t", reconstruct="-m S -o 10 -i 100",
+        regenerate_obj=True, otype="f", qg=dict(create="-Q 2", build="-Q 2"),
+        settings=[("qg", 10, 0.02, 2.0, "rw"), ("qg", 10, 0.05, 3.0, "rw"), ("qg", 10, 0.1, 2.0, "rw"),
+                  ("qg", 10, 0.1, 0.0, "rw")]),
 }
 
 
@@ -234,7 +267,11 @@ def make(name: str, spec: dict) -> None:
         tsv = os.path.join(tmp, "base.tsv")
         np.savetxt(tsv, base, fmt="%.9g", delimiter="\t")
         idx = os.path.join(tmp, "idx")
-        run([os.path.join(REF, "ngt"), "create"] + spec["create"].split() + [idx, tsv])
+        if spec.get("append"):
+            run([os.path.join(REF, "ngt"), "create"] + spec["create"].split() + [idx])
+            run([os.path.join(REF, "ngt"), "append", idx, tsv])
+        else:
+            run([os.path.join(REF, "ngt"), "create"] + spec["create"].split() + [idx, tsv])
         if "reconstruct" in spec:
             idx2 = os.path.join(tmp, "idx2")
             run([os.path.join(REF, "ngt"), "reconstruct-graph"] + spec["reconstruct"].split() + [idx, idx2])

@@ -38,7 +38,8 @@ def _tie_aware_recall(ids, counts, gt_d, k, qrows, objects, metric_fn):
 # (fixture, graph setting, linear setting).  Epsilon <= 0.2: with its bounded
 # candidate list the batched kernel explores at least what the reference does.
 CASES = [("c1_f32_l2", 0, 10), ("c1_f32_l2", 2, 10), ("c1_f32_l2_onng", 0, 11), ("u8_l2", 0, 2),
-         ("u8_l1", 0, 1), ("f32_cosine", 0, 1), ("f32_ncosine", 0, 1), ("f16_l2", 0, 1), ("qs8_l2", 0, 3)]
+         ("u8_l1", 0, 1), ("f32_cosine", 0, 1), ("f32_ncosine", 0, 1), ("f16_l2", 0, 1), ("qs8_l2", 0, 3),
+         ("f32_ip", 0, 3), ("f32_ip", 2, 3), ("f32_poincare", 0, 1), ("f32_lorentz", 0, 1)]
 
 
 @pytest.mark.parametrize("kernel", [KERNEL_BATCHED, KERNEL_WIDE])
