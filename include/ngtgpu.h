@@ -105,14 +105,15 @@ bool ngtgpu_set_batched_tuning_ex(NGTIndex, const NGTGPUBatchedTuning *tuning, N
  * memory themselves, and serving paths that must never enter the allocator.
  * No counterpart in the reference.  Its scratch (query parameters, seed lists,
  * per-CTA visited bitmaps and candidate overflow tiers) lives in one fixed
- * 32 MiB device array that the library reserves on every GPU that loads it,
- * until the process exits.  The first call on a device looks up that array's
- * address (no allocation), so make it before any stream capture.  Calls share
+ * 32 MiB device array.  The library reserves that array on a GPU when it opens
+ * the first index there (the array's address lookup loads its module) and holds
+ * it until the process exits; the search itself reserves nothing.  Calls share
  * the array: calls that overlap on the GPU race.  A call is rejected with an
  * error when its parameters plus one CTA's scratch exceed 32 MiB, and when a
  * query's result size has no seed table yet (run one regular search with that
  * size on the index first).  Buffers are device memory, as in
- * ngtgpu_search_batch_device; the call returns after the search completed. */
+ * ngtgpu_search_batch_device.  The call is synchronous: it copies its
+ * parameters from host memory and returns after the search completed. */
 bool ngtgpu_search_exact_noalloc(NGTIndex, const void *d_rows, size_t nq, const NGTQueryParameters *params,
                                  size_t nparams, NGTObjectDistance *d_results, size_t kmax, uint32_t *d_counts,
                                  NGTGPUQueryStats *d_stats, void *stream, NGTError);

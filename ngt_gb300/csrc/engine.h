@@ -12,6 +12,13 @@
 #include "index_files.h"
 
 namespace ngtg {
+struct ExactConfig;
+// Resolves the no-allocation search's fixed scratch on `device` (current) and loads
+// the module of `exact_fn` (defined in noalloc.cu; called when an index opens).
+void noalloc_prepare_device(int device, const void* exact_fn);
+}  // namespace ngtg
+
+namespace ngtg {
 
 // Search parameters of one query, as the reference's C API receives them
 // (ngt_search_index_ in lib/NGT/Capi.cpp:514-532).
@@ -174,6 +181,9 @@ class GraphEngine {
   void search_device_noalloc(void* scratch, size_t scratch_bytes, const uint4* d_rows, size_t nq,
                              const SearchArgs* args, size_t nargs, ObjDist* d_out, uint32_t* d_counts,
                              QueryStats* d_stats, size_t kmax, cudaStream_t stream);
+  // The exact kernel's configuration for result sizes up to max_size: fills cfg and
+  // returns its dynamic shared memory (shared by every exact launch path).
+  size_t exact_launch_config(uint32_t max_size, ExactConfig& cfg) const;
   void set_tuning(const FastTuning& t) { tuning_ = t; }
   const FastTuning& tuning() const { return tuning_; }
   bool fast_supported(Kernel k) const;

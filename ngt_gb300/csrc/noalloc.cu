@@ -11,15 +11,17 @@
 // cudaMalloc.  The caller still passes (and owns) the query rows, the result
 // buffers and the stream.
 //
-// The array is a file-scope __device__ variable: every GPU that loads the
-// library reserves it until the process exits.  Host code cannot use the name
-// as a device pointer (it denotes a host-side shadow), so its device address is
-// looked up once per device with cudaGetSymbolAddress, with that device
-// current, on the first call made on that device (so make that first call
-// before any stream capture begins).  All calls share the array
-// and it keeps the previous call's contents, so each call clears what must
-// start at zero (the visited bitmaps); calls whose work overlaps on the GPU
-// (on different streams, or from different threads) race on it.
+// The array is a file-scope __device__ variable.  CUDA loads the module that
+// holds it lazily, so the 32 MiB are reserved on a GPU when the module is first
+// used there; the library does that while it opens an index on that GPU (the
+// array's address lookup below), so from then until the process exits the GPU
+// holds the array, and the search itself triggers no module load.  Host code
+// cannot use the name as a device pointer (it denotes a host-side shadow), so
+// the device address is looked up once per device with cudaGetSymbolAddress,
+// with that device current.  All calls share the array and it keeps the
+// previous call's contents, so each call clears what must start at zero (the
+// visited bitmaps); calls whose work overlaps on the GPU (on different
+// streams, or from different threads) race on it.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -48,7 +50,8 @@ void* g_scratch_addr[256] = {};
 }  // namespace
 
 // Device address of the scratch array on `device` (which must be current).
-// The first call on a device performs the lookup; it is not an allocation.
+// The first call on a device performs the lookup, which loads the array's module
+// and so reserves the array on that device.
 void* noalloc_scratch_address(int device) {
   std::lock_guard<std::mutex> lock(g_scratch_mu);
   if (device < 0 || device >= 256) throw std::runtime_error("device ordinal out of range");
@@ -64,6 +67,14 @@ void* noalloc_scratch_address(int device) {
 }
 
 size_t noalloc_scratch_bytes() { return kNoAllocScratchBytes; }
+
+void noalloc_prepare_device(int device, const void* exact_fn) {
+  noalloc_scratch_address(device);
+  cudaFuncAttributes attr;
+  cudaError_t e = cudaFuncGetAttributes(&attr, exact_fn);     // loads the kernel's module
+  if (e != cudaSuccess)
+    throw std::runtime_error(std::string("loading the exact search kernel failed: ") + cudaGetErrorString(e));
+}
 
 }  // namespace ngtg
 

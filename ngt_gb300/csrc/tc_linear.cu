@@ -881,8 +881,27 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
     a.cand_count = ccount;
     a.cap = cap;
     a.status = d_status + q0;
+    // Valid (present) rows seen so far.  While fewer than C, every query's threshold
+    // is still -inf and each valid row of the next part is appended on top of them,
+    // so such a part ends before it could pass the list capacity (an index with
+    // most low ids removed); the presence flags are the same for every query.
+    size_t valid = 0;
+    for (uint32_t i = 1; i < r0; i++) valid += host_.present[i] ? 1 : 0;
     for (uint32_t row = r0, part = std::max<uint32_t>(r0, tc::BM); row < nrows; part *= 2) {
-      const uint32_t end = (uint32_t)std::min<uint64_t>(nrows, (uint64_t)row + part);
+      uint32_t end = (uint32_t)std::min<uint64_t>(nrows, (uint64_t)row + part);
+      if (valid < C) {
+        const size_t room = cap - valid;          // >= 3 C and >= 6144: cap >= max(8192, 4 C), C <= 2048 there
+        size_t v = 0;
+        uint32_t e = row;
+        while (e < end && v + (host_.present[e] ? 1 : 0) <= room) v += host_.present[e++] ? 1 : 0;
+        if (e < end) {
+          e = std::max<uint32_t>(row + tc::BM, e / tc::BM * tc::BM);   // whole tiles; room >= one tile
+          v = 0;
+          for (uint32_t i = row; i < e; i++) v += host_.present[i] ? 1 : 0;
+        }
+        end = e;
+        valid += v;
+      }
       a.row_begin = row;
       a.row_end = end;
       launch_scores(st, mapB, a, false, stream, sms);

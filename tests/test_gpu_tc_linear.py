@@ -159,3 +159,41 @@ def test_fp64_ground_truth_on_clusters(workdir):
     got = np.take_along_axis(d64, ids.astype(np.int64) - 1, axis=1)
     assert (got <= kth[:, None] + 1e-6).all()
     assert (np.diff(ds, axis=1) >= 0).all()
+
+
+def test_low_ids_mostly_removed(workdir):
+    """An index whose first 8,000 ids are removed except 40: the dense first part holds
+    fewer valid rows than the candidates, so every query's threshold is still -inf in
+    the first filtered parts.  The parts are planned so that no candidate list
+    overflows (status 0), and the results equal the plain GPU linear search."""
+    from ngt_gb300 import Index
+    from ngt_gb300.graph_build import write_index
+    from ngt_gb300.synthetic import clipped_exponential
+    n, dim = 20000, 64
+    x = clipped_exponential(n, dim, seed=241)
+    q = clipped_exponential(60, dim, seed=242)
+    present = np.ones(n + 1, bool)
+    present[0] = False
+    present[1:8001] = False
+    present[1:8001:200] = True
+    ids_p = np.nonzero(present)[0]
+    deg = np.zeros(n + 1, np.int64)
+    deg[ids_p] = 1
+    offsets = np.concatenate([[0], np.cumsum(deg)])
+    edges = np.roll(ids_p, -1).astype(np.uint32)          # a ring over the present objects
+    path = os.path.join(workdir, "removed_low")
+    write_index(path, x, offsets, edges, np.ones(len(edges), np.float32), extra_prf={"EdgeSizeForSearch": "10"})
+    with open(os.path.join(path, "obj"), "wb") as f:       # removed objects are '-' records
+        f.write(np.uint64(n + 1).tobytes())
+        f.write(b"-")
+        raw = x.view(np.uint8).reshape(n, -1)
+        for i in range(1, n + 1):
+            f.write(b"+" + raw[i - 1].tobytes() if present[i] else b"-")
+    with Index(path, read_only=True) as ix:
+        ids, ds, cnt, status = ix.linear_search_tc(q, k=100, candidates=400)
+        assert (status == 0).all()
+        for j in range(len(q)):
+            r = ix.linear_search(q[j], k=100)
+            assert [o.id for o in r] == list(ids[j, :cnt[j]])
+            assert np.array_equal(np.array([o.distance for o in r], np.float32), ds[j, :cnt[j]])
+        assert present[ids[:, :1]].all()

@@ -19,6 +19,29 @@ from golden_util import materialize
 pytestmark = pytest.mark.gpu
 
 
+def _cudart():
+    """The CUDA runtime this process already loaded (for the memory queries)."""
+    for line in open("/proc/self/maps"):
+        path = line.split()[-1] if line.strip() else ""
+        if "libcudart.so" in path:
+            return ctypes.CDLL(path)
+    raise RuntimeError("libcudart is not loaded")
+
+
+def _device_memory_state(rt):
+    """(free device bytes, default pool reserved bytes, default pool used bytes)."""
+    free, total = ctypes.c_size_t(), ctypes.c_size_t()
+    assert rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+    pool = ctypes.c_void_p()
+    dev = ctypes.c_int()
+    assert rt.cudaGetDevice(ctypes.byref(dev)) == 0
+    assert rt.cudaDeviceGetDefaultMemPool(ctypes.byref(pool), dev) == 0
+    reserved, used = ctypes.c_uint64(), ctypes.c_uint64()
+    assert rt.cudaMemPoolGetAttribute(pool, 5, ctypes.byref(reserved)) == 0      # ReservedMemCurrent
+    assert rt.cudaMemPoolGetAttribute(pool, 7, ctypes.byref(used)) == 0          # UsedMemCurrent
+    return free.value, reserved.value, used.value
+
+
 def _noalloc(lib):
     fn = lib.ngtgpu_search_exact_noalloc
     fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
@@ -50,12 +73,18 @@ def test_noalloc_equals_regular_entry_point_on_consecutive_calls(tmp_path):
                          kernel=KERNEL_EXACT)
         torch.cuda.synchronize()
         fn = _noalloc(ix._lib)
-        for _ in range(2):
+        rt = _cudart()
+        for call in range(2):
             rb, cb, sb = buffers()
+            torch.cuda.synchronize()
+            before = _device_memory_state(rt)
             ok = fn(ix._index, rows.data_ptr(), nq, params, nparams, rb.data_ptr(), k, cb.data_ptr(), sb.data_ptr(),
                     None, ix._err)
             assert ok, ix._lib.ngt_get_error_string(ix._err)
             torch.cuda.synchronize()
+            # nothing reserved on the device by the call: free memory and the default
+            # pool unchanged (the fixed scratch was reserved when the index opened)
+            assert _device_memory_state(rt) == before, call
             assert torch.equal(ca, cb)
             assert torch.equal(ra, rb)          # ids and distance bits
             assert torch.equal(sa, sb)          # identical search work
