@@ -140,6 +140,23 @@ bool ngtgpu_linear_search_tc_device(NGTIndex, const void *d_rows, size_t nq, siz
 bool ngtgpu_linear_search_tc_float(NGTIndex, const float *queries, size_t nq, int32_t dim, size_t size,
                                    size_t candidates, NGTObjectDistance *results, size_t kmax, uint32_t *counts,
                                    uint32_t *status, NGTError);
+/* Precision of the tensor-core scores, and options, of the _ex calls below. */
+#define NGTGPU_TC_BF16 0u        /* bf16 copies, fp32 accumulation (kind::f16) */
+#define NGTGPU_TC_FP8 1u         /* per-row and per-query scaled E4M3 copies, fp32 accumulation
+                                    (kind::f8f6f4): half the bytes and twice the tensor rate of bf16,
+                                    coarser scores, so more candidates are needed for the same ids */
+#define NGTGPU_TC_FP64_TIES 1u   /* flag: the candidates whose fp32 distance ties the size-th one within
+                                    the fp32 evaluation error (1e-4 x max(d, 1)) are ordered by their FP64
+                                    distance at the cut, so the returned ids are the FP64 top `size` among
+                                    the candidates (status bit 4: more than 64 such ties, fp32 order kept) */
+/* ngtgpu_linear_search_tc_device / _float with a score precision and flags. */
+bool ngtgpu_linear_search_tc_ex(NGTIndex, const void *d_rows, size_t nq, size_t size, size_t candidates,
+                                uint32_t precision, uint32_t flags, NGTObjectDistance *d_results, size_t kmax,
+                                uint32_t *d_counts, uint32_t *d_status, void *stream, NGTError);
+bool ngtgpu_linear_search_tc_float_ex(NGTIndex, const float *queries, size_t nq, int32_t dim, size_t size,
+                                      size_t candidates, uint32_t precision, uint32_t flags,
+                                      NGTObjectDistance *results, size_t kmax, uint32_t *counts, uint32_t *status,
+                                      NGTError);
 /* The approximate scores of the tensor-core pre-selection alone:
  * d_scores[q * ld + id] (ld >= the number of object slots, id 0 unused), larger
  * = closer: a * (q . x) + b over bf16 copies with a = 1, b = -|x|^2 / 2 for L2

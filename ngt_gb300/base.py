@@ -26,6 +26,10 @@ KERNEL_EXACT = 0
 KERNEL_BATCHED = 1
 KERNEL_BATCHED_FP32 = 2
 KERNEL_WIDE = 3
+# tensor-core exhaustive search: score precision and flags (include/ngtgpu.h)
+TC_BF16 = 0
+TC_FP8 = 1
+TC_FP64_TIES = 1
 
 
 class NativeError(Exception):
@@ -129,6 +133,10 @@ def load_library() -> ctypes.CDLL:
                                             c_void_p, c_void_p, c_void_p, c_void_p], c_bool),
         "ngtgpu_linear_search_tc_float": ([c_void_p, c_void_p, c_size_t, c_int32, c_size_t, c_size_t, c_void_p,
                                            c_size_t, c_void_p, c_void_p, c_void_p], c_bool),
+        "ngtgpu_linear_search_tc_ex": ([c_void_p, c_void_p, c_size_t, c_size_t, c_size_t, c_uint32, c_uint32,
+                                        c_void_p, c_size_t, c_void_p, c_void_p, c_void_p, c_void_p], c_bool),
+        "ngtgpu_linear_search_tc_float_ex": ([c_void_p, c_void_p, c_size_t, c_int32, c_size_t, c_size_t, c_uint32,
+                                              c_uint32, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p], c_bool),
         "ngtgpu_tc_scores_device": ([c_void_p, c_void_p, c_size_t, c_void_p, c_size_t, c_void_p, c_void_p],
                                     c_bool),
         "ngtgpu_set_tc_first_rows": ([c_void_p, c_size_t, c_void_p], c_bool),
@@ -286,12 +294,15 @@ class Index:
                           cta_threads, stage_kilobytes, l2_policy, search_rows)
         self._check(self._lib.ngtgpu_set_batched_tuning_ex(self._index, ctypes.byref(t), self._err))
 
-    def linear_search_tc(self, queries, k: int = 10, candidates: int = 0, first_rows: int = 0):
+    def linear_search_tc(self, queries, k: int = 10, candidates: int = 0, first_rows: int = 0,
+                         precision: str = "bf16", fp64_ties: bool = False):
         """Exhaustive k-NN of every row of `queries` with the tensor-core
-        pre-selection (bf16 scores, `candidates` re-ranked exactly).
+        pre-selection (bf16 or per-row scaled fp8 scores, `candidates` re-ranked
+        exactly; fp64_ties: the ties at the cut ordered by FP64 distance).
 
         Returns (ids[nq, k], distances[nq, k], counts[nq], status[nq]); status
-        bit 1 marks a query whose candidate list overflowed.
+        bit 1 marks a query whose candidate list overflowed, bit 4 a tie window
+        too wide for the FP64 check.
         """
         q = np.ascontiguousarray(queries, dtype=np.float32)
         nq = q.shape[0]
@@ -299,9 +310,10 @@ class Index:
         res = np.zeros((nq, k), RESULT_DTYPE)
         counts = np.zeros(nq, np.uint32)
         status = np.zeros(nq, np.uint32)
-        ok = self._lib.ngtgpu_linear_search_tc_float(self._index, q.ctypes.data, nq, q.shape[1], k, candidates,
-                                                     res.ctypes.data, k, counts.ctypes.data, status.ctypes.data,
-                                                     self._err)
+        prec = {"bf16": TC_BF16, "fp8": TC_FP8}[precision]
+        ok = self._lib.ngtgpu_linear_search_tc_float_ex(self._index, q.ctypes.data, nq, q.shape[1], k, candidates,
+                                                        prec, TC_FP64_TIES if fp64_ties else 0, res.ctypes.data, k,
+                                                        counts.ctypes.data, status.ctypes.data, self._err)
         self._check(ok)
         return res["id"].copy(), res["distance"].copy(), counts, status
 

@@ -153,9 +153,11 @@ struct Acc {
       if (off < width) {
         if constexpr (M == Metric::Lorentz) {
           float h = __shfl_xor_sync(0xffffffffu, f0, off), l = __shfl_xor_sync(0xffffffffu, f1, off);
-          // the same partner order on both lanes of a pair: the two lanes end equal
-          two_sum_acc(f0, f1, h);
-          f1 += l;
+          // TwoSum's error term is exact whatever the operand order, and f1 + l is
+          // commutative, so both lanes of a pair end with the same (hi, lo)
+          float lo = f1 + l;
+          two_sum_acc(f0, lo, h);
+          f1 = lo;
           continue;
         }
         if constexpr (kUseF0) f0 += __shfl_xor_sync(0xffffffffu, f0, off);

@@ -478,7 +478,8 @@ bool GraphEngine::fast_supported(Kernel k) const {
   if (k == Kernel::Wide)
     return wide_kernel(host_.prop.otype, host_.prop.metric,
                        host_.prop.otype == ObjType::Float ? SearchRows::Bf16 : SearchRows::Native, 256) != nullptr;
-  return fast_kernel(host_.prop.otype, host_.prop.metric, k == Kernel::Fast) != nullptr;
+  const bool hyperbolic = host_.prop.metric == Metric::Poincare || host_.prop.metric == Metric::Lorentz;
+  return fast_kernel(host_.prop.otype, host_.prop.metric, k == Kernel::Fast && !hyperbolic) != nullptr;
 }
 
 void GraphEngine::ensure_fast_scratch(FastScratch& sc, size_t slots, cudaStream_t stream) {

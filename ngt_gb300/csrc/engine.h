@@ -137,8 +137,13 @@ class GraphEngine {
   // ascending by (distance, id).  d_rows: nq converted query rows; d_status[q]
   // bit 1 = candidate list overflow.  Float objects; L2, inner product, cosine,
   // angle and their normalized forms.
+  // fp8: scores from per-row / per-query scaled E4M3 copies (kind::f8f6f4) instead
+  // of bf16; fp64_ties: the candidates tied with the size-th one within the fp32
+  // evaluation error are ordered by FP64 distance at the cut (status bit 4: tie
+  // window too wide, fp32 order kept).
   void linear_search_tc_device(const uint4* d_rows, size_t nq, size_t size, size_t candidates, ObjDist* d_out,
-                               size_t kmax, uint32_t* d_counts, uint32_t* d_status, cudaStream_t stream);
+                               size_t kmax, uint32_t* d_counts, uint32_t* d_status, cudaStream_t stream,
+                               bool fp8 = false, bool fp64_ties = false);
   // The approximate scores alone: d_scores[q * ld + row] (-inf for the unused
   // row 0 and removed objects).
   void tc_scores_device(const uint4* d_rows, size_t nq, float* d_scores, size_t ld, cudaStream_t stream);
@@ -297,6 +302,7 @@ class GraphEngine {
   FastTuning tuning_;
   DevGraph dev_;
   void ensure_tc_rows();
+  void ensure_tc_rows8();
   TcState* tc_ = nullptr;
   size_t tc_first_rows_ = 0;
 };

@@ -33,7 +33,11 @@ FastKernelFn fast_kernel(ObjType ot, Metric m, bool bf16_rows, uint32_t rows_in_
     }
   }
   if (ot == ObjType::Float) {
-    switch (m) { NGT_FAST_CASE(Float, Float, L2) NGT_FAST_CASE(Float, Float, NormalizedCosine) default: return nullptr; }
+    switch (m) {
+      NGT_FAST_CASE(Float, Float, L2) NGT_FAST_CASE(Float, Float, NormalizedCosine)
+      NGT_FAST_CASE(Float, Float, Poincare) NGT_FAST_CASE(Float, Float, Lorentz)   // searched on the fp32 rows
+      default: return nullptr;
+    }
   }
   if (ot == ObjType::Uint8) {
     switch (m) {

@@ -40,6 +40,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 #include <algorithm>
 #include <cfloat>
 #include <memory>
@@ -78,6 +79,11 @@ constexpr uint64_t kWaitNs = 2000000000ull;     // bound of every wait (2 s)
 // B bf16 (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
 // 17-22, M >> 4 at bits 24-28.
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((BN >> 3) << 17) | ((BM >> 4) << 24);
+// kind::f8f6f4 with A and B E4M3 (format 0 at bits 7-9 and 10-12), D fp32.  One MMA
+// consumes K = 32 one-byte elements, the same 32 bytes of each 128-byte swizzle
+// row as a bf16 MMA's K = 16, so staging, descriptors and k-steps are shared.
+constexpr uint32_t kIdescF8 = (1u << 4) | ((BN >> 3) << 17) | ((BM >> 4) << 24);
+constexpr float kE4M3Max = 448.f;       // largest finite E4M3 value
 
 struct ScoreArgs {
   uint32_t row_begin, row_end;          // rows [row_begin, row_end); row_begin % BM == 0
@@ -93,6 +99,7 @@ struct ScoreArgs {
   uint32_t cap;
   uint32_t* status;                     // bit 1: candidate list overflow
   uint32_t* error;                      // bit 1: producer wait, 2: MMA wait, 4: epilogue wait ran out
+  const float* qscale;                  // fp8 scores: per-query dequantisation scale (bf16: unused)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -158,6 +165,12 @@ __device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64
       ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(kIdesc), "r"(accumulate)
       : "memory");
 }
+__device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}"
+      ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(kIdescF8), "r"(accumulate)
+      : "memory");
+}
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
@@ -200,7 +213,10 @@ __device__ __forceinline__ float key_score(uint32_t key) {
   return __uint_as_float((asc & 0x80000000u) ? (asc & 0x7fffffffu) : ~asc);
 }
 
-template <bool kDense>
+// kFp8: A (rows) and B (queries) hold per-row / per-query scaled E4M3 values; the
+// accumulator is multiplied by the query's scale in the epilogue (the row's scale
+// is folded into row_scale).
+template <bool kDense, bool kFp8>
 __global__ void __launch_bounds__(THREADS, 1)
 tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, ScoreArgs a) {
   extern __shared__ __align__(1024) unsigned char dsmem[];
@@ -292,8 +308,12 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
           tc_fence_after();
           const uint32_t sA = base + stage * STAGE_BYTES, sB = sA + A_BYTES;
 #pragma unroll
-          for (uint32_t k = 0; k < BK / 16; k++)
-            mma_bf16(d, sw128_desc(sA + k * 32), sw128_desc(sB + k * 32), (kb | k) != 0 ? 1u : 0u);
+          for (uint32_t k = 0; k < BK / 16; k++) {
+            if constexpr (kFp8)
+              mma_f8(d, sw128_desc(sA + k * 32), sw128_desc(sB + k * 32), (kb | k) != 0 ? 1u : 0u);
+            else
+              mma_bf16(d, sw128_desc(sA + k * 32), sw128_desc(sB + k * 32), (kb | k) != 0 ? 1u : 0u);
+          }
           mma_commit(smem_u32(&bar_empty[stage]));
           if (++stage == STAGES) {
             stage = 0;
@@ -336,25 +356,27 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
         const uint32_t qb = q0 + c * 32;
         if (qb >= a.nq) break;                   // warp-uniform
         // lane j holds the threshold of query qb + j (+inf past the last query)
-        float my_thr = INFINITY;
+        float my_thr = INFINITY, my_qs = 1.f;
         if (!kDense && qb + lane < a.nq) my_thr = __ldg(a.thr + qb + lane);
+        if (kFp8 && qb + lane < a.nq) my_qs = __ldg(a.qscale + qb + lane);
         uint32_t v[32];
         tmem_ld32(tmem + ((quad * 32u) << 16) + buf * BN + c * 32, v);
         tmem_ld_wait(v);
         if (kDense) {
-          if (in_range) {
 #pragma unroll
-            for (uint32_t j = 0; j < 32; j++) {
-              const uint32_t q = qb + j;
-              const float s = fmaf(__uint_as_float(v[j]), sc, bi) + 0.0f;
-              if (q < a.nq) a.dense[(size_t)q * a.dense_ld + (row - a.row_begin)] = rvalid ? s : -INFINITY;
-            }
+          for (uint32_t j = 0; j < 32; j++) {
+            const uint32_t q = qb + j;
+            // the shuffle runs on every lane of the warp, whatever its row
+            const float scj = kFp8 ? sc * __shfl_sync(0xffffffffu, my_qs, j) : sc;
+            const float s = fmaf(__uint_as_float(v[j]), scj, bi) + 0.0f;
+            if (in_range && q < a.nq) a.dense[(size_t)q * a.dense_ld + (row - a.row_begin)] = rvalid ? s : -INFINITY;
           }
         } else {
 #pragma unroll
           for (uint32_t j = 0; j < 32; j++) {
             const float t = __shfl_sync(0xffffffffu, my_thr, j);
-            const float s = fmaf(__uint_as_float(v[j]), sc, bi);
+            const float scj = kFp8 ? sc * __shfl_sync(0xffffffffu, my_qs, j) : sc;
+            const float s = fmaf(__uint_as_float(v[j]), scj, bi);
             if (rvalid && s > t) {
               const uint32_t q = qb + j;
               const uint32_t slot = atomicAdd(a.cand_count + q, 1u);
@@ -493,8 +515,44 @@ tc_compact_kernel(unsigned long long* __restrict__ cand, uint32_t* __restrict__ 
   }
 }
 
-// Per query: top C approximate candidates, exact distances, sorted, first `size`.
+// Distance between the query row q (shared memory) and object row x in FP64,
+// computed by one warp (lanes over the elements; every lane returns the value).
 template <Metric M>
+__device__ double fp64_distance(const float* q, const float* x, uint32_t n, uint32_t lane) {
+  double a = 0.0, b = 0.0, c = 0.0;
+  for (uint32_t i = lane; i < n; i += 32) {
+    const double u = q[i], v = x[i];
+    if constexpr (M == Metric::L2) {
+      a += (u - v) * (u - v);
+    } else {
+      a += u * v;
+      b += u * u;
+      c += v * v;
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, off);
+    b += __shfl_xor_sync(0xffffffffu, b, off);
+    c += __shfl_xor_sync(0xffffffffu, c, off);
+  }
+  if constexpr (M == Metric::L2) return sqrt(a);
+  if constexpr (M == Metric::NormalizedL2) return sqrt(fmax(0.0, 2.0 - 2.0 * a));
+  if constexpr (M == Metric::NormalizedCosine) return fabs(1.0 - a);
+  if constexpr (M == Metric::Cosine) return fabs(1.0 - a / sqrt(b * c));
+  const double cs = M == Metric::Angle ? a / sqrt(b * c) : a;
+  return cs >= 1.0 ? 0.0 : cs <= -1.0 ? acos(-1.0) : acos(cs);
+}
+
+constexpr uint32_t kTieWindow = 64;     // largest tie window the FP64 check resolves
+
+// Per query: top C approximate candidates, exact distances, sorted, first `size`.
+// kTies: the FP64 check at the cut.  The fp32 distances of the candidates next to
+// the size-th one (within 1e-4 x max(d, 1), well above the fp32 evaluation error
+// of these sums) are recomputed in FP64, and the ones that belong to the FP64 top
+// `size` are returned in those places (in fp32 (distance, id) order): the returned
+// set is then the FP64 ground truth's among the candidates.  A window wider than
+// kTieWindow entries keeps the fp32 result and sets status bit 4.
+template <Metric M, bool kTies>
 __global__ void __launch_bounds__(256)
 tc_final_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_t q0, const unsigned long long* __restrict__ cand,
                 const uint32_t* __restrict__ cand_count, uint32_t cap, uint32_t C, uint32_t P, uint32_t size,
@@ -553,6 +611,58 @@ tc_final_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_t q0, cons
     }
   }
   const uint32_t kk = min(size, m);
+  if constexpr (kTies) {
+    __shared__ uint32_t sh_lo, sh_hi;
+    __shared__ double wd[kTieWindow];
+    __shared__ unsigned long long wk[kTieWindow];
+    if (threadIdx.x == 0) {
+      sh_lo = sh_hi = kk;
+      if (kk > 0 && kk < m) {
+        const float dk = key_dist(sel[kk - 1]);
+        const float tol = 1e-4f * fmaxf(dk, 1.f);
+        uint32_t lo = kk - 1, hi = kk;
+        while (lo > 0 && key_dist(sel[lo - 1]) >= dk - tol) lo--;
+        while (hi < m && key_dist(sel[hi]) <= dk + tol) hi++;
+        if (hi > kk) {                       // the window crosses the cut
+          if (hi - lo <= kTieWindow) {
+            sh_lo = lo;
+            sh_hi = hi;
+          } else if (status) {
+            status[q] |= 4u;
+          }
+        }
+      }
+    }
+    __syncthreads();
+    const uint32_t lo = sh_lo, hi = sh_hi;
+    if (hi > kk) {
+      const float* qf = reinterpret_cast<const float*>(qv);
+      const uint32_t n = rc * 4;
+      for (uint32_t i = lo + warp; i < hi; i += blockDim.x / 32) {
+        const uint32_t row = key_id(sel[i]);
+        const double d = fp64_distance<M>(qf, reinterpret_cast<const float*>(g.objects + (size_t)row * rc), n,
+                                          (uint32_t)lane);
+        if (lane == 0) {
+          wd[i - lo] = d;
+          wk[i - lo] = sel[i];
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        // the (kk - lo) best of the window by (FP64 distance, id) take places lo..kk-1,
+        // in their fp32 (distance, id) order
+        const uint32_t w = hi - lo, need = kk - lo;
+        uint32_t put = lo;
+        for (uint32_t i = 0; i < w && put < kk; i++) {
+          uint32_t rank = 0;
+          for (uint32_t j = 0; j < w; j++)
+            rank += (wd[j] < wd[i] || (wd[j] == wd[i] && key_id(wk[j]) < key_id(wk[i]))) ? 1u : 0u;
+          if (rank < need) sel[put++] = wk[i];
+        }
+      }
+      __syncthreads();
+    }
+  }
   for (uint32_t i = threadIdx.x; i < kk; i += blockDim.x)
     out[(size_t)q * kmax + i] = ObjDist{key_id(sel[i]), key_dist(sel[i])};
   if (threadIdx.x == 0) {
@@ -590,6 +700,48 @@ __global__ void tc_rows_kernel(const float* __restrict__ x, uint32_t nrows, uint
   }
 }
 
+// Per-row scaled E4M3 rows (K padded to kpad8): row r holds x / s_r with
+// s_r = max|x| / 448 (1 for a zero row), rounded to nearest E4M3; scale8[r] = the
+// row's affine scale (as in tc_rows_kernel) times s_r, so that the accumulated
+// sum times scale8[r] times the query's own scale is the bf16 path's a (q . x).
+__global__ void tc_rows8_kernel(const float* __restrict__ x, uint32_t nrows, uint32_t dpad, uint32_t kpad8,
+                                const float* __restrict__ scale, uint8_t* __restrict__ out,
+                                float* __restrict__ scale8) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t row = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+  if (row >= nrows) return;
+  const float* xr = x + (size_t)row * dpad;
+  float mx = 0.f;
+  for (uint32_t c = lane; c < dpad; c += 32) mx = fmaxf(mx, fabsf(xr[c]));
+  for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+  const float sr = mx > 0.f ? mx / kE4M3Max : 1.f;
+  uint8_t* o = out + (size_t)row * kpad8;
+  for (uint32_t c = lane; c < kpad8; c += 32)
+    o[c] = c < dpad ? (uint8_t)__nv_cvt_float_to_fp8(xr[c] / sr, __NV_SATFINITE, __NV_E4M3) : (uint8_t)0;
+  if (lane == 0) scale8[row] = scale[row] * sr;
+}
+
+// Per-query scaled E4M3 query rows [nq_pad][kpad8] and their scales (one warp per
+// query; rows past nq and columns past dpad are zero).
+__global__ void tc_queries8_kernel(const float* __restrict__ rows, uint32_t dpad, uint32_t nq, uint32_t nq_pad,
+                                   uint32_t kpad8, uint8_t* __restrict__ out, float* __restrict__ qscale) {
+  const uint32_t lane = threadIdx.x & 31;
+  for (uint32_t q = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5); q < nq_pad;
+       q += gridDim.x * (blockDim.x / 32)) {
+    const float* xr = rows + (size_t)q * dpad;
+    float mx = 0.f;
+    if (q < nq)
+      for (uint32_t c = lane; c < dpad; c += 32) mx = fmaxf(mx, fabsf(xr[c]));
+    for (int off = 16; off > 0; off >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, off));
+    const float t = mx > 0.f ? mx / kE4M3Max : 1.f;
+    uint8_t* o = out + (size_t)q * kpad8;
+    for (uint32_t c = lane; c < kpad8; c += 32)
+      o[c] = (q < nq && c < dpad) ? (uint8_t)__nv_cvt_float_to_fp8(xr[c] / t, __NV_SATFINITE, __NV_E4M3)
+                                  : (uint8_t)0;
+    if (lane == 0) qscale[q] = t;
+  }
+}
+
 // bf16 query rows [nq_pad][kpad]; rows past nq and columns past dpad are zero.
 __global__ void tc_queries_kernel(const float* __restrict__ rows, uint32_t dpad, uint32_t nq, uint32_t nq_pad,
                                   uint32_t kpad, __nv_bfloat16* __restrict__ out) {
@@ -603,17 +755,19 @@ __global__ void tc_queries_kernel(const float* __restrict__ rows, uint32_t dpad,
 typedef void (*FinalFn)(DevGraph, const uint4*, uint32_t, const unsigned long long*, const uint32_t*, uint32_t,
                         uint32_t, uint32_t, uint32_t, uint32_t, ObjDist*, uint32_t, uint32_t*, uint32_t*);
 
-FinalFn final_kernel(Metric m) {
+template <bool kTies>
+FinalFn final_kernel_t(Metric m) {
   switch (m) {
-    case Metric::L2: return &tc_final_kernel<Metric::L2>;
-    case Metric::NormalizedL2: return &tc_final_kernel<Metric::NormalizedL2>;
-    case Metric::Cosine: return &tc_final_kernel<Metric::Cosine>;
-    case Metric::Angle: return &tc_final_kernel<Metric::Angle>;
-    case Metric::NormalizedCosine: return &tc_final_kernel<Metric::NormalizedCosine>;
-    case Metric::NormalizedAngle: return &tc_final_kernel<Metric::NormalizedAngle>;
+    case Metric::L2: return &tc_final_kernel<Metric::L2, kTies>;
+    case Metric::NormalizedL2: return &tc_final_kernel<Metric::NormalizedL2, kTies>;
+    case Metric::Cosine: return &tc_final_kernel<Metric::Cosine, kTies>;
+    case Metric::Angle: return &tc_final_kernel<Metric::Angle, kTies>;
+    case Metric::NormalizedCosine: return &tc_final_kernel<Metric::NormalizedCosine, kTies>;
+    case Metric::NormalizedAngle: return &tc_final_kernel<Metric::NormalizedAngle, kTies>;
     default: return nullptr;
   }
 }
+FinalFn final_kernel(Metric m, bool ties) { return ties ? final_kernel_t<true>(m) : final_kernel_t<false>(m); }
 
 int row_mode(Metric m) {
   switch (m) {
@@ -655,6 +809,20 @@ CUtensorMap make_map(const void* base, uint64_t rows, uint64_t kpad, uint32_t bo
   return m;
 }
 
+// The same over E4M3 rows: rows x kpad8 bytes, box 128 x box_rows.
+CUtensorMap make_map8(const void* base, uint64_t rows, uint64_t kpad8, uint32_t box_rows) {
+  CUtensorMap m;
+  cuuint64_t dims[2] = {kpad8, rows};
+  cuuint64_t strides[1] = {kpad8};
+  cuuint32_t box[2] = {128, box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<void*>(base), dims, strides, box, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw std::runtime_error("cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return m;
+}
+
 uint32_t pow2_at_least(uint32_t v) {
   uint32_t p = 1;
   while (p < v) p <<= 1;
@@ -670,6 +838,11 @@ struct TcState {
   float* bias = nullptr;
   uint32_t kpad = 0;
   CUtensorMap mapA;
+  // per-row scaled E4M3 rows (built on the first fp8 search)
+  uint8_t* rows8 = nullptr;        // [nrows][kpad8]
+  float* scale8 = nullptr;         // affine scale x the row's E4M3 scale
+  uint32_t kpad8 = 0;
+  CUtensorMap mapA8;
   // scratch, grown on demand
   void* scratch = nullptr;
   size_t scratch_bytes = 0;
@@ -683,6 +856,8 @@ struct TcState {
 void tc_release(TcState* s) {
   if (!s) return;
   cudaFree(s->rows);
+  cudaFree(s->rows8);
+  cudaFree(s->scale8);
   cudaFree(s->scale);
   cudaFree(s->bias);
   cudaFree(s->scratch);
@@ -722,22 +897,47 @@ void GraphEngine::ensure_tc_rows() {
   tc_ = s.release();
 }
 
+void GraphEngine::ensure_tc_rows8() {
+  ensure_tc_rows();
+  TcState& s = *tc_;
+  if (s.rows8) return;
+  const uint32_t dpad = host_.dpad;
+  const uint32_t kpad8 = (dpad + 127) / 128 * 128;
+  const size_t nrows = host_.nrows;
+  TC_CUDA(cudaMalloc(&s.rows8, nrows * kpad8));
+  TC_CUDA(cudaMalloc(&s.scale8, nrows * 4));
+  s.kpad8 = kpad8;
+  const unsigned blocks = (unsigned)((nrows + 7) / 8);
+  tc::tc_rows8_kernel<<<blocks, 256, 0, stream_>>>(static_cast<const float*>(d_objects_), (uint32_t)nrows, dpad,
+                                                   kpad8, s.scale, s.rows8, s.scale8);
+  TC_CUDA(cudaGetLastError());
+  launches_++;
+  s.mapA8 = tc::make_map8(s.rows8, nrows, kpad8, tc::BM);
+  TC_CUDA(cudaStreamSynchronize(stream_));
+}
+
 namespace {
 
+template <bool kFp8>
+void launch_scores_t(const CUtensorMap& mapA, const CUtensorMap& mapB, const tc::ScoreArgs& a, bool dense,
+                     cudaStream_t s, unsigned grid) {
+  auto fn = dense ? tc::tc_score_kernel<true, kFp8> : tc::tc_score_kernel<false, kFp8>;
+  TC_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_BYTES));
+  fn<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(mapA, mapB, a);
+}
+
 void launch_scores(const TcState& st, const CUtensorMap& mapB, tc::ScoreArgs a, bool dense, cudaStream_t s,
-                   int sms) {
+                   int sms, bool fp8 = false) {
   const uint32_t mtiles = (a.row_end - a.row_begin + tc::BM - 1) / tc::BM;
   const uint32_t tiles = mtiles * ((a.nq + tc::BN - 1) / tc::BN);
   if (tiles == 0) return;
   const unsigned grid = (unsigned)std::min<uint32_t>(tiles, (uint32_t)sms);
-  if (dense) {
-    TC_CUDA(cudaFuncSetAttribute((const void*)tc::tc_score_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)tc::SMEM_BYTES));
-    tc::tc_score_kernel<true><<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(st.mapA, mapB, a);
+  if (fp8) {
+    a.row_scale = st.scale8;
+    a.kblocks = st.kpad8 / 128;
+    launch_scores_t<true>(st.mapA8, mapB, a, dense, s, grid);
   } else {
-    TC_CUDA(cudaFuncSetAttribute((const void*)tc::tc_score_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)tc::SMEM_BYTES));
-    tc::tc_score_kernel<false><<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(st.mapA, mapB, a);
+    launch_scores_t<false>(st.mapA, mapB, a, dense, s, grid);
   }
   TC_CUDA(cudaGetLastError());
 }
@@ -790,10 +990,11 @@ void GraphEngine::tc_scores_device(const uint4* d_rows, size_t nq, float* d_scor
 
 void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t size, size_t candidates,
                                           ObjDist* d_out, size_t kmax, uint32_t* d_counts, uint32_t* d_status,
-                                          cudaStream_t stream) {
+                                          cudaStream_t stream, bool fp8, bool fp64_ties) {
   std::lock_guard<std::mutex> lock(mu_);
   TC_CUDA(cudaSetDevice(device_));
   ensure_tc_rows();
+  if (fp8) ensure_tc_rows8();
   if (nq == 0) return;
   if (size == 0) throw std::runtime_error("result size must be at least 1");
   if (kmax < size) throw std::runtime_error("kmax smaller than the result size");
@@ -801,7 +1002,7 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
   size_t C = candidates ? candidates : std::max<size_t>(4 * size, 64);
   if (C < size) C = size;
   if (C > 4096) throw std::runtime_error("at most 4096 candidates per query (and results <= candidates)");
-  const tc::FinalFn fin = tc::final_kernel(kernel_metric(host_.prop.metric));
+  const tc::FinalFn fin = tc::final_kernel(kernel_metric(host_.prop.metric), fp64_ties);
   if (!fin) throw std::runtime_error("unsupported distance for the tensor-core linear search");
   const TcState& st = *tc_;
   const uint32_t nrows = (uint32_t)host_.nrows;
@@ -817,12 +1018,12 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
   int sms = 0;
   TC_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
   const size_t qbmax = std::min<size_t>(nq, 16384);
-  // scratch: bf16 queries | dense scores | candidates | counts | thresholds
+  // scratch: bf16 or E4M3 queries | dense scores | candidates | counts | thresholds | query scales
   const size_t qbpad = (qbmax + tc::BN - 1) / tc::BN * tc::BN;
-  const size_t b_q = qbpad * st.kpad * 2;
+  const size_t b_q = (qbpad * std::max<size_t>(st.kpad * 2, st.kpad8) + 255) / 256 * 256;
   const size_t b_d = (qbmax * (size_t)first * 4 + 255) / 256 * 256;
   const size_t b_c = qbmax * (size_t)cap * 8;
-  const size_t need = b_q + b_d + b_c + 2 * qbmax * 4 + 512;
+  const size_t need = b_q + b_d + b_c + 2 * qbmax * 4 + qbpad * 4 + 512;
   if (tc_->scratch_bytes < need) {
     TC_CUDA(cudaStreamSynchronize(stream));
     TC_CUDA(cudaFree(tc_->scratch));
@@ -837,6 +1038,8 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
   unsigned long long* cand = reinterpret_cast<unsigned long long*>(sp + b_q + b_d);
   uint32_t* ccount = reinterpret_cast<uint32_t*>(sp + b_q + b_d + b_c);
   float* thr = reinterpret_cast<float*>(ccount + qbmax);
+  float* qscale = thr + qbmax;
+  uint8_t* qbuf8 = reinterpret_cast<uint8_t*>(sp);
   const uint32_t rc = dev_.row_chunks;
   uint32_t group = 1;
   while (group < rc && group < 32) group <<= 1;
@@ -852,12 +1055,19 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
     const uint32_t nbpad = (nb + tc::BN - 1) / tc::BN * tc::BN;
     TC_CUDA(cudaEventRecord(st.ev[0], stream));
     const float* qrows = reinterpret_cast<const float*>(d_rows) + q0 * host_.dpad;
-    tc::tc_queries_kernel<<<1024, 256, 0, stream>>>(qrows, host_.dpad, nb, nbpad, st.kpad, qbuf);
+    CUtensorMap mapB;
+    if (fp8) {
+      tc::tc_queries8_kernel<<<1024, 256, 0, stream>>>(qrows, host_.dpad, nb, nbpad, st.kpad8, qbuf8, qscale);
+      mapB = tc::make_map8(qbuf8, nbpad, st.kpad8, tc::BN);
+    } else {
+      tc::tc_queries_kernel<<<1024, 256, 0, stream>>>(qrows, host_.dpad, nb, nbpad, st.kpad, qbuf);
+      mapB = tc::make_map(qbuf, nbpad, st.kpad, tc::BN);
+    }
     TC_CUDA(cudaGetLastError());
-    CUtensorMap mapB = tc::make_map(qbuf, nbpad, st.kpad, tc::BN);
     tc::ScoreArgs a{};
     a.nq = nb;
     a.kblocks = st.kpad / tc::BK;
+    a.qscale = qscale;
     a.row_scale = st.scale;
     a.row_bias = st.bias;
     a.present = d_present_;
@@ -867,7 +1077,7 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
     a.row_end = r0;
     a.dense = dense;
     a.dense_ld = (uint32_t)first;
-    launch_scores(st, mapB, a, true, stream, sms);
+    launch_scores(st, mapB, a, true, stream, sms, fp8);
     tc::tc_first_select_kernel<<<nb, 512, first * 8, stream>>>(dense, (uint32_t)first, r0, (uint32_t)C, thr, cand,
                                                                ccount, cap);
     TC_CUDA(cudaGetLastError());
@@ -904,7 +1114,7 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
       }
       a.row_begin = row;
       a.row_end = end;
-      launch_scores(st, mapB, a, false, stream, sms);
+      launch_scores(st, mapB, a, false, stream, sms, fp8);
       launches_++;
       if (end < nrows) {
         tc::tc_compact_kernel<<<nb, 512, cap * 8, stream>>>(cand, ccount, cap, (uint32_t)C, thr, d_status + q0);

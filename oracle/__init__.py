@@ -31,6 +31,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+FAST_LIB_PATH = os.path.join(HERE, "_build", "liboracle_fast.so")
 
 OBJTYPES = {"Float-4": 0, "Integer-1": 1, "Float-2": 2, "QSUInteger-8B": 3}
 ELEM = {0: np.float32, 1: np.uint8, 2: np.float16, 3: np.int8}
@@ -50,6 +51,18 @@ def build(verbose: bool = False) -> str:
     if verbose:
         print(r.stdout)
     return LIB_PATH
+
+
+def build_fast() -> str:
+    """Compiles liboracle_fast.so: the same restatement with the reference's Release
+    flags (-Ofast -march=native), timed as the CPU baseline; never used to check."""
+    src = os.path.join(HERE, "ngt_oracle.c")
+    if os.path.exists(FAST_LIB_PATH) and os.path.getmtime(FAST_LIB_PATH) >= os.path.getmtime(src):
+        return FAST_LIB_PATH
+    r = subprocess.run(["make", "-C", HERE, "fast"], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle speed build failed:\n" + r.stdout + r.stderr)
+    return FAST_LIB_PATH
 
 
 class OracleIndexC(ctypes.Structure):
@@ -284,9 +297,10 @@ class QGFiles:
 class Oracle:
     """ctypes binding of ngt_oracle.c over one IndexFiles."""
 
-    def __init__(self, files: IndexFiles):
+    def __init__(self, files: IndexFiles, speed_build: bool = False):
+        """speed_build: load the -Ofast build (for timing the CPU baseline only)."""
         self.f = files
-        self.lib = ctypes.CDLL(build())
+        self.lib = ctypes.CDLL(build_fast() if speed_build else build())
         L = self.lib
         L.oracle_graph_search.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
                                           ctypes.c_size_t, ctypes.c_float, ctypes.c_float, ctypes.c_int64, ctypes.c_int,

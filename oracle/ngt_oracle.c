@@ -583,28 +583,31 @@ typedef struct {
 
 /* Rotation::mul (lib/NGT/NGTQ/Quantizer.h:117-160), y[c] = sum_p R[p][c] x[p].  The
  * reference hands it to BLAS sgemv('N'); the summation order here is the one the x86-64
- * OpenBLAS build the reference links uses, which this reproduces bit for bit for
- * dimensions <= 48 (one FMA chain over p) and for multiples of 32 up to 512 (blocks of 8
- * columns: first product, then FMAs, the block total added to y[c]).  For other
- * dimensions OpenBLAS's order depends on its thread partition of the rows, and single
- * elements can differ from it by an ulp. */
-void oracle_qg_rotate(const OracleQG *qg, const float *x, float *y) {
-  size_t d = qg->dim;
-  if (!qg->rotation) { memcpy(y, x, d * sizeof(float)); return; }
+ * OpenBLAS build the reference links uses: one FMA chain over p for dimensions <= 48,
+ * else blocks of 8 columns (first product, then FMAs, the block total added to y[c]).
+ * It equals that sgemv bit for bit at every multiple of 16 from 16 to 768, with one
+ * thread or eight (tests/test_oracle_rotation.py), and QG/QBG pseudo-dimensions are
+ * always multiples of 16 (lib/NGT/NGTQ/QuantizedGraph.h:640-657). */
+void oracle_rotate(const float *R, const float *x, float *y, size_t d) {
   for (size_t c = 0; c < d; c++) {
     float acc = 0.0f;
     if (d <= 48) {
-      for (size_t p = 0; p < d; p++) acc = fmaf(qg->rotation[p * d + c], x[p], acc);
+      for (size_t p = 0; p < d; p++) acc = fmaf(R[p * d + c], x[p], acc);
     } else {
       for (size_t p0 = 0; p0 < d; p0 += 8) {
         size_t p1 = p0 + 8 < d ? p0 + 8 : d;
-        float t = qg->rotation[p0 * d + c] * x[p0];
-        for (size_t p = p0 + 1; p < p1; p++) t = fmaf(qg->rotation[p * d + c], x[p], t);
+        float t = R[p0 * d + c] * x[p0];
+        for (size_t p = p0 + 1; p < p1; p++) t = fmaf(R[p * d + c], x[p], t);
         acc = acc + t;
       }
     }
     y[c] = acc;
   }
+}
+
+void oracle_qg_rotate(const OracleQG *qg, const float *x, float *y) {
+  if (!qg->rotation) { memcpy(y, x, qg->dim * sizeof(float)); return; }
+  oracle_rotate(qg->rotation, x, y, qg->dim);
 }
 
 /* createFloatL2DistanceLookup for the uint8 table (lib/NGT/NGTQ/Quantizer.h:1731-1810,

@@ -185,6 +185,11 @@ FIXTURES = {
 
 # Quantized blob graphs (qbg_search_index_float).  Settings: ("qbg", k, epsilon,
 # "expansion:explored_blobs:blob_epsilon", "rw").
+# ("qbg1", ...) and ("qbg2", ...) run the reference's searchInOneStep / searchInTwoSteps
+# through its C++ API (oracle/_ref/ref_qbg_dump) with "refinement_expansion:probes:blob_epsilon":
+# the one-step search judges at most `probes` blobs, the two-step search probes `probes`
+# blobs found by the global index; with an expansion >= 1 the k x expansion quantized
+# results are re-ranked by exact distances over the object file (refineDistances).
 QBG_FIXTURES = {
     "qbg_u8_l2_d32": dict(
         base=("clipped_exponential", dict(n=20000, dim=32, seed=181)),
@@ -193,6 +198,14 @@ QBG_FIXTURES = {
         settings=[("qbg", 10, 0.1, "3.0:16:0.0", "rw"), ("qbg", 10, 0.1, "3.0:256:0.0", "rw"),
                   ("qbg", 10, 0.0, "1.0:8:0.05", "rw"), ("qbg", 5, 0.2, "2.0:32:0.1", "rw"),
                   ("qbg", 10, 0.1, "0.5:16:0.0", "rw")]),
+    # with its object file (qbg_dir/obj), for the refined and two-step searches
+    "qbg_u8_l2_d64": dict(
+        base=("clipped_exponential", dict(n=20000, dim=64, seed=251)),
+        query=("clipped_exponential", dict(n=100, dim=64, seed=252)),
+        create="-d 64 -D 2 -N 32 -o c", build="-B 1000:10,1000:40,0:256", with_obj=True,
+        settings=[("qbg", 10, 0.1, "3.0:16:0.0", "rw"), ("qbg2", 10, 0.1, "0.0:8:0.0", "rw"),
+                  ("qbg2", 10, 0.1, "3.0:8:0.0", "rw"), ("qbg2", 20, 0.1, "2.0:32:0.05", "rw"),
+                  ("qbg1", 10, 0.1, "3.0:16:0.0", "rw"), ("qbg1", 10, 0.05, "1.5:64:0.1", "rw")]),
 }
 
 
@@ -210,7 +223,7 @@ def make_qbg(name: str, spec: dict) -> None:
         os.makedirs(out, exist_ok=True)
         members = ["prf", "qr", "rqcb", "grp"] + sorted(
             "%s/obj" % d for d in os.listdir(idx) if d.startswith("local-")) + [
-            "global/prf", "global/obj", "global/grp", "global/tre"]
+            "global/prf", "global/obj", "global/grp", "global/tre"] + (["obj"] if spec.get("with_obj") else [])
         with tarfile.open(os.path.join(out, "qbg.tar.gz"), "w:gz") as tf:
             for m in members:
                 info = tf.gettarinfo(os.path.join(idx, m), arcname=m)
@@ -223,10 +236,16 @@ def make_qbg(name: str, spec: dict) -> None:
         for i, (op, k, eps, edge, mode) in enumerate(spec["settings"]):
             nq = queries.shape[0]
             dump = os.path.join(tmp, "out%d" % i)
-            run([os.path.join(REF, "ref_dump"), op, idx, qf, str(nq), str(queries.shape[1]), str(k), repr(eps),
-                 edge, mode, dump])
-            exp = float(edge.split(":")[0])
-            w = int(np.float32(k) * np.float32(exp)) if exp >= 1.0 else k
+            if op == "qbg":
+                run([os.path.join(REF, "ref_dump"), op, idx, qf, str(nq), str(queries.shape[1]), str(k), repr(eps),
+                     edge, mode, dump])
+                exp = float(edge.split(":")[0])
+                w = int(np.float32(k) * np.float32(exp)) if exp >= 1.0 else k
+            else:
+                e_, b_, be_ = edge.split(":")
+                run([os.path.join(REF, "ref_qbg_dump"), "one" if op == "qbg1" else "two", idx, qf, str(nq),
+                     str(queries.shape[1]), str(k), repr(eps), be_, b_, e_, dump])
+                w = k
             raw = np.fromfile(dump, np.uint8)
             arrays["ids_%d" % i] = raw[:nq * w * 4].view(np.uint32).reshape(nq, w)
             arrays["dist_%d" % i] = raw[nq * w * 4:2 * nq * w * 4].view(np.float32).reshape(nq, w)

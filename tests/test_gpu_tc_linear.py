@@ -197,3 +197,41 @@ def test_low_ids_mostly_removed(workdir):
             assert [o.id for o in r] == list(ids[j, :cnt[j]])
             assert np.array_equal(np.array([o.distance for o in r], np.float32), ds[j, :cnt[j]])
         assert present[ids[:, :1]].all()
+
+
+@pytest.mark.parametrize("name", ["c1_f32_l2", "f32_cosine", "f32_ncosine", "f32_ip"])
+def test_fp8_scores_return_reference_linear_search(name, workdir):
+    """Per-row scaled E4M3 scores (kind::f8f6f4) with an oversampled exact re-rank
+    return the reference's recorded linear-search results (ids; distances exact)."""
+    from ngt_gb300 import Index
+    path, meta, queries, golden = materialize(name, workdir)
+    i, s = _linear_settings(meta)[0]
+    nq, k = s["nq"], s["k"]
+    with Index(path, read_only=True) as ix:
+        ids, ds, n, status = ix.linear_search_tc(queries[:nq], k=k, candidates=256, precision="fp8",
+                                                 first_rows=256)
+    assert (status == 0).all()
+    assert np.array_equal(n, golden["count_%d" % i][:nq])
+    assert (ids == golden["ids_%d" % i][:nq]).all(1).mean() >= 0.98
+    gd = golden["dist_%d" % i][:nq]
+    assert (np.abs(ds - gd) <= 1e-5 * np.maximum(np.abs(gd), 0.1)).mean() > 0.99
+
+
+def test_fp8_and_bf16_agree_with_fp64_ties_on_clusters(workdir):
+    """k=100 on 20,000 x 768 normalised cluster data: bf16 (400 candidates) and fp8
+    (1,024 candidates) with the FP64 tie check both return exactly the FP64 top 100
+    of every query (as a set; ties at the cut decided in FP64)."""
+    from ngt_gb300 import Index
+    path, x, q = _cluster_index(workdir)
+    qn = q.astype(np.float64) / np.linalg.norm(q.astype(np.float64), axis=1, keepdims=True)
+    d64 = 1.0 - qn @ x.astype(np.float64).T
+    order = np.lexsort((np.broadcast_to(np.arange(d64.shape[1]), d64.shape), d64), axis=1)[:, :100]
+    truth = [set((order[j] + 1).tolist()) for j in range(len(q))]
+    with Index(path, read_only=True) as ix:
+        for prec, C in (("bf16", 400), ("fp8", 1024)):
+            ids, ds, n, status = ix.linear_search_tc(q, k=100, candidates=C, first_rows=2048, precision=prec,
+                                                     fp64_ties=True)
+            assert (status == 0).all() and (n == 100).all(), prec
+            agree = np.mean([set(ids[j].tolist()) == truth[j] for j in range(len(q))])
+            assert agree == 1.0, (prec, agree)
+            assert (np.diff(ds, axis=1) >= 0).all()
