@@ -169,6 +169,30 @@ bool qbg_gpu_search_batch_float(QBGIndex index, const float *queries, size_t nq,
                                 const QBGQueryParameters *params, size_t nparams, NGTObjectDistance *results,
                                 size_t kmax, uint32_t *counts, void *stats, QBGError error);
 
+/* Extension flags: the searches of the reference's C++ API (QBG::Index, as its `qbg
+ * search` command and ngtpy drive it) rather than its C API's. */
+#define NGTGPU_QBG_TWO_STEP 1u   /* searchInTwoSteps (lib/NGT/NGTQ/QuantizedBlobGraph.h:1190-1330): the
+                                    number_of_explored_blobs blobs nearest the query, found by the global
+                                    index's graph search (epsilon = blob_epsilon), are all judged in order;
+                                    epsilon is not used.  Without it: searchInOneStep (:1332-1594). */
+#define NGTGPU_QBG_REFINE 2u     /* result_expansion is the refinement expansion: the search keeps
+                                    number_of_results x result_expansion (>= 1) quantized results, re-ranked by
+                                    exact distances over the index's object list (qbg_dir/obj, loaded on the
+                                    first refined call; refineDistances, QuantizedBlobGraph.h:1136-1185) to the
+                                    number_of_results best.  The one-step search then thins its tree seeds with
+                                    number_of_results, as the reference's container does. */
+/* qbg_gpu_search_batch_float with the flags above (0: identical to it). */
+bool qbg_gpu_search_batch_ex(QBGIndex index, const float *queries, size_t nq, int32_t dim,
+                             const QBGQueryParameters *params, size_t nparams, uint32_t flags,
+                             NGTObjectDistance *results, size_t kmax, uint32_t *counts, void *stats, QBGError error);
+/* The same on device memory: d_rows holds nq float rows of the global index's
+ * dimension (converted by ngtgpu_convert_queries_float on this handle), d_stats nq
+ * NGTGPUQueryStats; queued on `stream` (NULL: the index's stream); returns after
+ * completion. */
+bool qbg_gpu_search_batch_device(QBGIndex index, const void *d_rows, size_t nq, const QBGQueryParameters *params,
+                                 size_t nparams, uint32_t flags, NGTObjectDistance *d_results, size_t kmax,
+                                 uint32_t *d_counts, void *d_stats, void *stream, QBGError error);
+
 #ifdef __cplusplus
 }
 #endif

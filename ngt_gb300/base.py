@@ -30,6 +30,9 @@ KERNEL_WIDE = 3
 TC_BF16 = 0
 TC_FP8 = 1
 TC_FP64_TIES = 1
+# QBG search flags (include/ngtq_capi.h)
+QBG_TWO_STEP = 1
+QBG_REFINE = 2
 
 
 class NativeError(Exception):
@@ -168,6 +171,11 @@ def load_library() -> ctypes.CDLL:
         "qbg_search_index_float": ([c_void_p, QBGQueryFloat, c_void_p, c_void_p], c_bool),
         "qbg_gpu_search_batch_float": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QBGQueryParameters),
                                         c_size_t, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p], c_bool),
+        "qbg_gpu_search_batch_ex": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QBGQueryParameters),
+                                     c_size_t, c_uint32, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p], c_bool),
+        "qbg_gpu_search_batch_device": ([c_void_p, c_void_p, c_size_t, POINTER(QBGQueryParameters), c_size_t,
+                                         c_uint32, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p, c_void_p],
+                                        c_bool),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -535,18 +543,22 @@ class QBGIndex:
         return [self._lib.ngt_get_result(self._results, i, self._err) for i in range(n)]
 
     def batch_search(self, queries, k=20, epsilon=0.1, blob_epsilon=0.0, result_expansion=3.0, explored_blobs=256,
-                     edges=0, with_stats: bool = False):
-        """Every row in one launch: (ids[nq, m], distances[nq, m], counts[nq])."""
+                     edges=0, with_stats: bool = False, two_step: bool = False, refine: bool = False):
+        """Every row in one launch: (ids[nq, m], distances[nq, m], counts[nq]).
+
+        two_step: searchInTwoSteps (explored_blobs probes); refine: result_expansion is
+        the refinement expansion (exact re-rank over the object list to k results)."""
         q = np.ascontiguousarray(queries, dtype=np.float32)
         nq = q.shape[0]
         p = self.params(k, epsilon, blob_epsilon, result_expansion, explored_blobs, edges)
-        kmax = max(self.result_size(p), 1)
+        kmax = max(int(k) if refine and result_expansion >= 1.0 else self.result_size(p), 1)
         res = np.zeros((nq, kmax), RESULT_DTYPE)
         counts = np.zeros(nq, np.uint32)
         stats = np.zeros(nq, QUERY_STATS_DTYPE)
-        self._check(self._lib.qbg_gpu_search_batch_float(self._index, q.ctypes.data, nq, q.shape[1],
-                                                         ctypes.byref(p), 1, res.ctypes.data, kmax,
-                                                         counts.ctypes.data, stats.ctypes.data, self._err))
+        flags = (QBG_TWO_STEP if two_step else 0) | (QBG_REFINE if refine else 0)
+        self._check(self._lib.qbg_gpu_search_batch_ex(self._index, q.ctypes.data, nq, q.shape[1],
+                                                      ctypes.byref(p), 1, flags, res.ctypes.data, kmax,
+                                                      counts.ctypes.data, stats.ctypes.data, self._err))
         m = int(counts.max()) if nq else 0
         out = (res["id"][:, :m].copy(), res["distance"][:, :m].copy(), counts)
         return out + (stats,) if with_stats else out

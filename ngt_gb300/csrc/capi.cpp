@@ -899,16 +899,55 @@ bool qbg_search_index_float16(QBGIndex index, QBGQueryFloat16 query, QBGObjectDi
 bool qbg_gpu_search_batch_float(QBGIndex index, const float* queries, size_t nq, int32_t dim,
                                 const QBGQueryParameters* params, size_t nparams, NGTObjectDistance* results,
                                 size_t kmax, uint32_t* counts, void* stats, QBGError error) {
-  if (index == nullptr || (nq && (queries == nullptr || results == nullptr || counts == nullptr)) ||
-      params == nullptr || dim <= 0 || !(nparams == 1 || nparams == nq)) {
-    CAPI_PARAM_ERROR(error, "index = " << index << " queries = " << queries << " nq = " << nq
-                                       << " nparams = " << nparams << " dim = " << dim);
+  return qbg_gpu_search_batch_ex(index, queries, nq, dim, params, nparams, 0u, results, kmax, counts, stats, error);
+}
+
+bool qbg_gpu_search_batch_device(QBGIndex index, const void* d_rows, size_t nq, const QBGQueryParameters* params,
+                                 size_t nparams, uint32_t flags, NGTObjectDistance* d_results, size_t kmax,
+                                 uint32_t* d_counts, void* d_stats, void* stream, QBGError error) {
+  if (index == nullptr || (nq && (d_rows == nullptr || d_results == nullptr || d_counts == nullptr ||
+                                  d_stats == nullptr)) ||
+      params == nullptr || !(nparams == 1 || nparams == nq) ||
+      (flags & ~(NGTGPU_QBG_TWO_STEP | NGTGPU_QBG_REFINE)) != 0) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " rows = " << d_rows << " nq = " << nq << " nparams = " << nparams
+                                       << " flags = " << flags);
     return false;
   }
   try {
     std::vector<QBGArgs> a;
     for (size_t i = 0; i < nparams; i++) {
       a.push_back(qbg_args(params[i]));
+      a.back().two_step = (flags & NGTGPU_QBG_TWO_STEP) != 0;
+      a.back().refine = (flags & NGTGPU_QBG_REFINE) != 0;
+      if (GraphEngine::qbg_result_size(a.back()) > kmax)
+        throw std::runtime_error("a query asks for more results than kmax");
+    }
+    GraphEngine* e = engine(index);
+    cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : e->stream();
+    e->qbg_search_device(static_cast<const uint4*>(d_rows), nq, a.data(), a.size(),
+                         reinterpret_cast<ngtg::ObjDist*>(d_results), d_counts,
+                         static_cast<ngtg::QueryStats*>(d_stats), kmax, s);
+    return true;
+  }
+  CAPI_CATCH(error, false)
+}
+
+bool qbg_gpu_search_batch_ex(QBGIndex index, const float* queries, size_t nq, int32_t dim,
+                             const QBGQueryParameters* params, size_t nparams, uint32_t flags,
+                             NGTObjectDistance* results, size_t kmax, uint32_t* counts, void* stats, QBGError error) {
+  if (index == nullptr || (nq && (queries == nullptr || results == nullptr || counts == nullptr)) ||
+      params == nullptr || dim <= 0 || !(nparams == 1 || nparams == nq) ||
+      (flags & ~(NGTGPU_QBG_TWO_STEP | NGTGPU_QBG_REFINE)) != 0) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " queries = " << queries << " nq = " << nq
+                                       << " nparams = " << nparams << " dim = " << dim << " flags = " << flags);
+    return false;
+  }
+  try {
+    std::vector<QBGArgs> a;
+    for (size_t i = 0; i < nparams; i++) {
+      a.push_back(qbg_args(params[i]));
+      a.back().two_step = (flags & NGTGPU_QBG_TWO_STEP) != 0;
+      a.back().refine = (flags & NGTGPU_QBG_REFINE) != 0;
       if (GraphEngine::qbg_result_size(a.back()) > kmax)
         throw std::runtime_error("a query asks for more results than kmax");
     }

@@ -6,6 +6,8 @@
 #include <cuda_fp16.h>
 #include <algorithm>
 #include <cfloat>
+#include <cstdlib>
+#include <fstream>
 #include <climits>
 #include <cmath>
 #include <cstring>
@@ -109,6 +111,7 @@ GraphEngine::GraphEngine(const std::string& qbg_dir, bool blobs) : mode_(GraphMo
   if (host_.prop.otype != ObjType::Float || host_.prop.metric != Metric::L2)
     throw std::runtime_error("the QBG global index must hold float L2 centroids");
   load_qbg(qbg_dir, host_.nrows, qb_);
+  qbg_dir_ = qbg_dir;
   {
     Property qp = load_property_raw(qbg_dir);
     try {
@@ -190,6 +193,7 @@ GraphEngine::~GraphEngine() {
   for (void* p : qg_buffers_) cudaFree(p);
   cudaFree(d_qbg_ovf_);
   cudaFree(d_blob_dist_);
+  cudaFree(d_olist_);
   tc_release(tc_);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -1103,6 +1107,78 @@ void GraphEngine::qg_search(const void* queries, QueryType qt, size_t nq, size_t
 
 // ---- quantized blob graph ---------------------------------------------------
 
+void GraphEngine::ensure_object_list() {
+  if (d_olist_) return;
+  // the array file of the object list (lib/NGT/ArrayFile.h): a 16-byte head (record
+  // size, reserved), then per object a 16-byte flag block and the object; record 0
+  // is the unused slot.  GenuineDataType: 0 uint8, 1 float (ObjectFile::DataType).
+  Property qp = load_property_raw(qbg_dir_);
+  const int gdt = std::atoi(qp.get("GenuineDataType", "0").c_str());
+  if (gdt != 0 && gdt != 1) throw std::runtime_error("the object list's data type is neither uint8 nor float");
+  const std::string path = qbg_dir_ + "/obj";
+  std::ifstream f(path, std::ios::binary | std::ios::ate);
+  if (!f.is_open()) throw std::runtime_error("the refinement needs the object list " + path);
+  const size_t bytes = (size_t)f.tellg();
+  f.seekg(0);
+  uint64_t head[2] = {0, 0};
+  if (bytes < 16 || !f.read(reinterpret_cast<char*>(head), 16)) throw std::runtime_error("truncated " + path);
+  const size_t rs = head[0], es = gdt == 0 ? 1 : 4;
+  if (rs == 0 || rs % es != 0 || (bytes - 16) % (16 + rs) != 0) throw std::runtime_error("corrupted " + path);
+  const size_t n = (bytes - 16) / (16 + rs);
+  if (n > 0xffffffffull) throw std::runtime_error("object list too large");
+  const size_t chunks = (rs + 15) / 16;
+  std::vector<uint8_t> rows(n * chunks * 16, 0), rec(16 + rs);
+  for (size_t i = 0; i < n; i++) {
+    if (!f.read(reinterpret_cast<char*>(rec.data()), (std::streamsize)rec.size())) throw std::runtime_error("truncated " + path);
+    std::memcpy(rows.data() + i * chunks * 16, rec.data() + 16, rs);
+  }
+  d_olist_ = dmalloc_copy<void>(rows.data(), rows.size());
+  olist_chunks_ = (uint32_t)chunks;
+  olist_dim_ = (uint32_t)(rs / es);
+  olist_rows_ = (uint32_t)n;
+  olist_uint8_ = gdt == 0;
+}
+
+void GraphEngine::qbg_probe_blobs(const uint4* d_rows, size_t nq, const QBGArgs* args, size_t nargs,
+                                  ObjDist* d_blobs, uint32_t* d_bcounts, size_t bstride, cudaStream_t stream) {
+  // searchInTwoSteps' global search (QuantizedBlobGraph.h:1224-1237): NGT::Index::search
+  // of the read-only global index with size = the probes, epsilon = (1 + blob_epsilon) - 1
+  // and the index's own edge size
+  std::vector<SearchArgs> sa(nargs);
+  for (size_t i = 0; i < nargs; i++) {
+    sa[i].size = args[i].explored_blobs;
+    sa[i].epsilon = (args[i].blob_epsilon + 1.0f) - 1.0f;
+    sa[i].radius = FLT_MAX;
+    sa[i].edge_size = -1;
+  }
+  const GraphMode saved = mode_;
+  mode_ = GraphMode::ReadOnly;
+  try {
+    std::vector<QueryParams> params;
+    std::vector<uint32_t> seeds;
+    uint32_t max_size = 0;
+    build_params(sa.data(), nargs, nq, bstride, params, seeds, max_size);
+    QueryParams* d_params = nullptr;
+    uint32_t* d_seeds = nullptr;
+    QueryStats* d_st = nullptr;
+    NGT_CUDA(cudaMallocAsync(&d_params, nq * sizeof(QueryParams), stream));
+    NGT_CUDA(cudaMallocAsync(&d_seeds, seeds.size() * 4, stream));
+    NGT_CUDA(cudaMallocAsync(&d_st, nq * sizeof(QueryStats), stream));
+    NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QueryParams), cudaMemcpyHostToDevice, stream));
+    NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, stream));
+    launch_exact(d_rows, nq, d_params, d_seeds, max_size, d_blobs, d_bcounts, d_st, stream);
+    NGT_CUDA(cudaFreeAsync(d_params, stream));
+    NGT_CUDA(cudaFreeAsync(d_seeds, stream));
+    NGT_CUDA(cudaFreeAsync(d_st, stream));
+    // the host parameter vectors must outlive the copies above
+    NGT_CUDA(cudaStreamSynchronize(stream));
+  } catch (...) {
+    mode_ = saved;
+    throw;
+  }
+  mode_ = saved;
+}
+
 void GraphEngine::qbg_search_device(const uint4* d_rows, size_t nq, const QBGArgs* args, size_t nargs,
                                     ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, size_t kmax,
                                     cudaStream_t stream) {
@@ -1110,16 +1186,28 @@ void GraphEngine::qbg_search_device(const uint4* d_rows, size_t nq, const QBGArg
   std::lock_guard<std::mutex> lock(mu_);
   NGT_CUDA(cudaSetDevice(device_));
   if (nq == 0) return;
-  // qbg_search_index_ (lib/NGT/NGTQ/Capi.cpp:549-574) and searchInOneStep
-  // (lib/NGT/NGTQ/QuantizedBlobGraph.h:1332-1381)
+  if (nargs != 1 && nargs != nq) throw std::runtime_error("one parameter block, or one per query");
+  const bool two_step = args[0].two_step;
+  bool refine = false;
+  for (size_t i = 0; i < nargs; i++) {
+    if (args[i].two_step != two_step) throw std::runtime_error("one-step and two-step queries in one call");
+    refine = refine || (args[i].refine && args[i].result_expansion >= 1.0f);
+  }
+  if (refine) ensure_object_list();
+  // qbg_search_index_ (lib/NGT/NGTQ/Capi.cpp:549-574), searchInOneStep
+  // (lib/NGT/NGTQ/QuantizedBlobGraph.h:1332-1381) and searchInTwoSteps (:1190-1330)
   std::vector<QBGParams> params(nq);
   std::vector<uint32_t> seeds(qbg_fallback_seeds_);
+  std::vector<uint32_t> exact(nq, 0);
   uint32_t max_size = 1;
+  size_t max_probes = 1;
   for (size_t i = 0; i < nq; i++) {
     const QBGArgs& a = args[nargs == 1 ? 0 : i];
-    const size_t size = qbg_result_size(a);
-    if (size > kmax) throw std::runtime_error("result size larger than the output capacity");
+    const size_t size = qbg_search_size(a);
+    const bool ref = a.refine && a.result_expansion >= 1.0f;
+    if (qbg_result_size(a) > kmax) throw std::runtime_error("result size larger than the output capacity");
     if (size > 4096) throw std::runtime_error("number_of_results x result_expansion above 4096 is not supported");
+    exact[i] = ref ? (uint32_t)a.size : 0u;
     QBGParams qp{};
     qp.size = (uint32_t)size;
     float coef = a.epsilon + 1.0f;
@@ -1134,48 +1222,30 @@ void GraphEngine::qbg_search_device(const uint4* d_rows, size_t nq, const QBGArg
     qp.edge_size = (uint32_t)std::min<size_t>(edge_size_for(sa), 0xffffffffu);
     qp.fb_off = 0;
     qp.fb_cnt = (uint32_t)qbg_fallback_seeds_.size();
-    qp.out_off = (uint32_t)(i * kmax);
-    if (size > 0) {
-      if (host_.prop.has_tree) seed_params(size, qp.seed_off, qp.seed_cnt, seeds);
+    qp.out_off = 0;                                    // set below, once the stride is known
+    if (size > 0 && !two_step) {
+      // the tree seeds are thinned with the container's size: the result size before a
+      // refinement expansion (QuantizedBlobGraph.h:1336-1345)
+      if (host_.prop.has_tree) seed_params(ref ? a.size : size, qp.seed_off, qp.seed_cnt, seeds);
       else { qp.seed_off = 0; qp.seed_cnt = 0; }
     }
     params[i] = qp;
     max_size = std::max<uint32_t>(max_size, qp.size);
+    max_probes = std::max<size_t>(max_probes, a.explored_blobs);
   }
+  // refined results pass through a buffer as wide as the largest search size
+  const size_t stride = refine ? (size_t)max_size : kmax;
+  for (size_t i = 0; i < nq; i++) params[i].out_off = (uint32_t)(i * stride);
   if (seeds.empty()) seeds.push_back(0);
-  QBGConfig cfg{};
-  cfg.rcap = max_size;
-  cfg.qcap = 1024;
-  cfg.ocap = (uint32_t)std::min<size_t>(65536, 2 * (size_t)host_.nrows + 256);
-  cfg.bitmap_words = (host_.nrows + 31) / 32;
-  cfg.blob_cap = blob_cap_;
-  cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));
-  int max_smem = 0;
+  int max_smem = 0, sms = 0;
   NGT_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
-  size_t smem = qbg_kernel_smem_bytes(dev_.row_chunks, qb_.dim, qb_.m, cfg);
-  while (smem > (size_t)max_smem && cfg.qcap > 256) {
-    cfg.qcap >>= 1;
-    smem = qbg_kernel_smem_bytes(dev_.row_chunks, qb_.dim, qb_.m, cfg);
-  }
-  if (smem > (size_t)max_smem) throw std::runtime_error("QBG search state does not fit in shared memory");
-  QBGKernelFn fn = qbg_kernel(qb_.m);
-  NGT_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  int per_sm = 0, sms = 0;
-  NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kExactThreads, smem));
   NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
-  size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
-  ensure_scratch(grid);
-  if (grid > qbg_grid_ || cfg.ocap != qbg_ocap_) {
-    NGT_CUDA(cudaStreamSynchronize(stream));
-    cudaFree(d_qbg_ovf_);
-    cudaFree(d_blob_dist_);
-    d_qbg_ovf_ = nullptr;
-    d_blob_dist_ = nullptr;
-    size_t g2 = std::max(grid, qbg_grid_);
-    NGT_CUDA(cudaMalloc(&d_qbg_ovf_, g2 * 4 * (size_t)cfg.ocap * 8));
-    NGT_CUDA(cudaMalloc(&d_blob_dist_, g2 * (size_t)blob_cap_ * 4));
-    qbg_grid_ = g2;
-    qbg_ocap_ = cfg.ocap;
+  // the search's own output: the caller's buffers, or a temporary one before the refinement
+  ObjDist* d_sout = d_out;
+  uint32_t* d_scount = d_counts;
+  if (refine) {
+    NGT_CUDA(cudaMallocAsync(&d_sout, nq * stride * sizeof(ObjDist), stream));
+    NGT_CUDA(cudaMallocAsync(&d_scount, nq * 4, stream));
   }
   QBGParams* d_params = nullptr;
   uint32_t* d_seeds = nullptr;
@@ -1183,13 +1253,92 @@ void GraphEngine::qbg_search_device(const uint4* d_rows, size_t nq, const QBGArg
   NGT_CUDA(cudaMallocAsync(&d_seeds, seeds.size() * 4, stream));
   NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QBGParams), cudaMemcpyHostToDevice, stream));
   NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, stream));
-  fn<<<(unsigned)grid, kExactThreads, smem, stream>>>(dev_, dqb_, d_blob_sid_, d_rows, (uint32_t)nq, d_params,
-                                                       d_seeds, d_out, d_counts, d_stats, d_bitmaps_, d_qbg_ovf_,
-                                                       d_blob_dist_, cfg);
-  NGT_CUDA(cudaGetLastError());
-  launches_++;
+  auto ensure_blob_dist = [&](size_t grid, uint32_t ocap) {
+    if (grid > qbg_grid_ || ocap != qbg_ocap_) {
+      NGT_CUDA(cudaStreamSynchronize(stream));
+      cudaFree(d_qbg_ovf_);
+      cudaFree(d_blob_dist_);
+      d_qbg_ovf_ = nullptr;
+      d_blob_dist_ = nullptr;
+      size_t g2 = std::max(grid, qbg_grid_);
+      NGT_CUDA(cudaMalloc(&d_qbg_ovf_, g2 * 4 * (size_t)std::max<uint32_t>(ocap, 1) * 8));
+      NGT_CUDA(cudaMalloc(&d_blob_dist_, g2 * (size_t)blob_cap_ * 4));
+      qbg_grid_ = g2;
+      qbg_ocap_ = ocap;
+    }
+  };
+  if (two_step) {
+    ObjDist* d_blobs = nullptr;
+    uint32_t* d_bcounts = nullptr;
+    NGT_CUDA(cudaMallocAsync(&d_blobs, nq * max_probes * sizeof(ObjDist), stream));
+    NGT_CUDA(cudaMallocAsync(&d_bcounts, nq * 4, stream));
+    qbg_probe_blobs(d_rows, nq, args, nargs, d_blobs, d_bcounts, max_probes, stream);
+    QBGScanKernelFn fn = qbg_scan_kernel_for(qb_.m);
+    if (!fn) throw std::runtime_error("too many subspaces in the QBG index");
+    const size_t smem = qbg_scan_kernel_smem_bytes(dev_.row_chunks, qb_.dim, qb_.m, max_size);
+    if (smem > (size_t)max_smem) throw std::runtime_error("QBG search state does not fit in shared memory");
+    NGT_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kExactThreads, smem));
+    const size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
+    ensure_blob_dist(grid, qbg_ocap_);
+    fn<<<(unsigned)grid, kExactThreads, smem, stream>>>(dqb_, d_blob_sid_, d_rows, dev_.row_chunks, (uint32_t)nq,
+                                                         d_params, d_blobs, d_bcounts, (uint32_t)max_probes, d_sout,
+                                                         d_scount, d_stats, d_blob_dist_, blob_cap_, max_size);
+    NGT_CUDA(cudaGetLastError());
+    launches_++;
+    NGT_CUDA(cudaFreeAsync(d_blobs, stream));
+    NGT_CUDA(cudaFreeAsync(d_bcounts, stream));
+  } else {
+    QBGConfig cfg{};
+    cfg.rcap = max_size;
+    cfg.qcap = 1024;
+    cfg.ocap = (uint32_t)std::min<size_t>(65536, 2 * (size_t)host_.nrows + 256);
+    cfg.bitmap_words = (host_.nrows + 31) / 32;
+    cfg.blob_cap = blob_cap_;
+    cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));
+    size_t smem = qbg_kernel_smem_bytes(dev_.row_chunks, qb_.dim, qb_.m, cfg);
+    while (smem > (size_t)max_smem && cfg.qcap > 256) {
+      cfg.qcap >>= 1;
+      smem = qbg_kernel_smem_bytes(dev_.row_chunks, qb_.dim, qb_.m, cfg);
+    }
+    if (smem > (size_t)max_smem) throw std::runtime_error("QBG search state does not fit in shared memory");
+    QBGKernelFn fn = qbg_kernel(qb_.m);
+    NGT_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kExactThreads, smem));
+    size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
+    ensure_scratch(grid);
+    ensure_blob_dist(grid, cfg.ocap);
+    fn<<<(unsigned)grid, kExactThreads, smem, stream>>>(dev_, dqb_, d_blob_sid_, d_rows, (uint32_t)nq, d_params,
+                                                         d_seeds, d_sout, d_scount, d_stats, d_bitmaps_, d_qbg_ovf_,
+                                                         d_blob_dist_, cfg);
+    NGT_CUDA(cudaGetLastError());
+    launches_++;
+  }
+  if (refine) {
+    uint32_t* d_exact = nullptr;
+    NGT_CUDA(cudaMallocAsync(&d_exact, nq * 4, stream));
+    NGT_CUDA(cudaMemcpyAsync(d_exact, exact.data(), nq * 4, cudaMemcpyHostToDevice, stream));
+    const uint32_t P = next_pow2(std::max<uint32_t>(max_size, 2));
+    const size_t smem = (size_t)olist_chunks_ * 16 + (size_t)P * 8;
+    QBGRefineKernelFn rf = qbg_refine_kernel_for(olist_uint8_);
+    NGT_CUDA(cudaFuncSetAttribute((const void*)rf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const unsigned grid = (unsigned)std::min<size_t>(nq, (size_t)sms * 8);
+    rf<<<grid, 256, smem, stream>>>(d_sout, d_scount, (uint32_t)stride, reinterpret_cast<const float*>(d_rows),
+                                    (uint32_t)(dev_.row_chunks * 4), static_cast<const uint4*>(d_olist_),
+                                    olist_chunks_, olist_dim_, olist_rows_, d_exact, (uint32_t)nq, P, d_out,
+                                    (uint32_t)kmax, d_counts);
+    NGT_CUDA(cudaGetLastError());
+    launches_++;
+    NGT_CUDA(cudaFreeAsync(d_exact, stream));
+    NGT_CUDA(cudaFreeAsync(d_sout, stream));
+    NGT_CUDA(cudaFreeAsync(d_scount, stream));
+  }
   NGT_CUDA(cudaFreeAsync(d_params, stream));
   NGT_CUDA(cudaFreeAsync(d_seeds, stream));
+  // the host vectors (parameters, exact sizes) must outlive the copies above
+  NGT_CUDA(cudaStreamSynchronize(stream));
 }
 
 void GraphEngine::qbg_search(const void* queries, QueryType qt, size_t nq, size_t qdim, const QBGArgs* args,

@@ -72,6 +72,13 @@ struct QBGArgs {
   float result_expansion = 3.0f;
   size_t explored_blobs = 256;
   size_t edges = 0;                 // global-graph edge size (0: all)
+  // searchInTwoSteps (lib/NGT/NGTQ/QuantizedBlobGraph.h:1190-1330): explored_blobs
+  // blobs probed, found by the global index's graph search; else searchInOneStep
+  bool two_step = false;
+  // result_expansion read as the refinement expansion of the reference's search
+  // container: size x expansion quantized results re-ranked by exact distances over
+  // the object list (refineDistances, QuantizedBlobGraph.h:1136-1185) to `size`
+  bool refine = false;
 };
 
 struct SearchOutput {
@@ -128,8 +135,12 @@ class GraphEngine {
                          uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream);
   bool is_qbg() const { return qbg_loaded_; }
   uint32_t qbg_genuine_dimension() const { return qbg_genuine_dim_; }
-  static size_t qbg_result_size(const QBGArgs& a) {
+  // results the blob search keeps, and results returned
+  static size_t qbg_search_size(const QBGArgs& a) {
     return a.result_expansion >= 1.0f ? (size_t)((float)a.size * a.result_expansion) : a.size;
+  }
+  static size_t qbg_result_size(const QBGArgs& a) {
+    return a.refine && a.result_expansion >= 1.0f ? a.size : qbg_search_size(a);
   }
   // Exhaustive search with a tensor-core pre-selection (tc_linear.cu): bf16
   // scores of every (query, row) with fp32 accumulation, the `candidates` best
@@ -261,6 +272,16 @@ class GraphEngine {
   std::vector<uint32_t> qbg_fallback_seeds_;
   unsigned long long* d_qbg_ovf_ = nullptr;
   float* d_blob_dist_ = nullptr;
+  // the QBG object list (qbg_dir/obj), loaded on the first refined search: rows of
+  // olist_chunks_ 16-byte chunks (uint8 or float), row 0 unused
+  std::string qbg_dir_;
+  void* d_olist_ = nullptr;
+  uint32_t olist_chunks_ = 0, olist_dim_ = 0, olist_rows_ = 0;
+  bool olist_uint8_ = true;
+  void ensure_object_list();
+  // the global index's read-only graph search for the two-step search (mu_ held)
+  void qbg_probe_blobs(const uint4* d_rows, size_t nq, const QBGArgs* args, size_t nargs, ObjDist* d_blobs,
+                       uint32_t* d_bcounts, size_t bstride, cudaStream_t stream);
   size_t qbg_grid_ = 0;
   uint32_t qbg_ocap_ = 0;
   // quantized graph

@@ -18,4 +18,21 @@ size_t qbg_kernel_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, cons
   return qbg_smem_bytes(row_chunks, dim, m, c);
 }
 
+QBGScanKernelFn qbg_scan_kernel_for(uint32_t m) {
+  if (m <= 32) return &qbg_scan_kernel<1>;
+  if (m <= 64) return &qbg_scan_kernel<2>;
+  if (m <= 128) return &qbg_scan_kernel<4>;
+  if (m <= 256) return &qbg_scan_kernel<8>;
+  if (m <= 512) return &qbg_scan_kernel<16>;
+  return nullptr;
+}
+
+size_t qbg_scan_kernel_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, uint32_t rcap) {
+  return qbg_scan_smem_bytes(row_chunks, dim, m, rcap);
+}
+
+QBGRefineKernelFn qbg_refine_kernel_for(bool uint8_rows) {
+  return uint8_rows ? &qbg_refine_kernel<ObjType::Uint8> : &qbg_refine_kernel<ObjType::Float>;
+}
+
 }  // namespace ngtg

@@ -28,6 +28,16 @@ typedef void (*QBGKernelFn)(DevGraph, DevQG, const uint32_t*, const uint4*, uint
                             QBGConfig);
 QBGKernelFn qbg_kernel(uint32_t m);
 size_t qbg_kernel_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, const QBGConfig& c);
+// The two-step search's blob phase and the refinement (qbg_search.cuh).
+typedef void (*QBGScanKernelFn)(DevQG, const uint32_t*, const uint4*, uint32_t, uint32_t, const QBGParams*,
+                                const ObjDist*, const uint32_t*, uint32_t, ObjDist*, uint32_t*, QueryStats*, float*,
+                                uint32_t, uint32_t);
+QBGScanKernelFn qbg_scan_kernel_for(uint32_t m);
+size_t qbg_scan_kernel_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, uint32_t rcap);
+typedef void (*QBGRefineKernelFn)(const ObjDist*, const uint32_t*, uint32_t, const float*, uint32_t, const uint4*,
+                                  uint32_t, uint32_t, uint32_t, const uint32_t*, uint32_t, uint32_t, ObjDist*,
+                                  uint32_t, uint32_t*);
+QBGRefineKernelFn qbg_refine_kernel_for(bool uint8_rows);
 
 struct WideConfig;
 typedef void (*WideKernelFn)(DevGraph, const uint4*, const uint4*, uint32_t, const QueryParams*, const uint32_t*,

@@ -134,6 +134,111 @@ __device__ __forceinline__ void qbg_merge_results(unsigned long long* const* res
   __syncthreads();
 }
 
+// Rotation::mul of the query (the OpenBLAS sgemv order: one FMA chain for D <= 48,
+// else blocks of 8 columns), the query zero-padded to D.
+__device__ __forceinline__ void qbg_rotate(const DevQG& qb, const float* qf, uint32_t qlen, float* rq) {
+  const uint32_t D = qb.dim;
+  for (uint32_t c = threadIdx.x; c < D; c += blockDim.x) {
+    float acc = 0.f;
+    if (qb.rotation == nullptr) {
+      acc = c < qlen ? qf[c] : 0.f;
+    } else if (D <= 48) {
+      for (uint32_t p = 0; p < D; p++) acc = __fmaf_rn(qb.rotation[(size_t)p * D + c], p < qlen ? qf[p] : 0.f, acc);
+    } else {
+      for (uint32_t p0 = 0; p0 < D; p0 += 8) {
+        const uint32_t p1 = min(p0 + 8u, D);
+        float t = __fmul_rn(qb.rotation[(size_t)p0 * D + c], p0 < qlen ? qf[p0] : 0.f);
+        for (uint32_t p = p0 + 1; p < p1; p++) t = __fmaf_rn(qb.rotation[(size_t)p * D + c], p < qlen ? qf[p] : 0.f, t);
+        acc = __fadd_rn(acc, t);
+      }
+    }
+    rq[c] = acc;
+  }
+}
+
+// judge (lib/NGT/NGTQ/QuantizedBlobGraph.h:1033-1080) of one blob by the whole CTA:
+// the blob's LUT (rebuilt only when its subspace id differs from the last one),
+// the scan of its codes into bdist, its minimum into s.bmin; when that minimum is
+// below the radius, every object within the radius joins the result set (kept to
+// `size`), and the radius becomes the set's maximum once it is full.
+template <int SPL>
+__device__ __forceinline__ void qbg_judge_blob(const DevQG& qb, const uint32_t* __restrict__ blob_sid, uint32_t blob,
+                                               const float* rq, float* flut, uint8_t* lut, QBGShared& s,
+                                               float* bdist, unsigned long long* const* resb,
+                                               unsigned long long* bkeys, unsigned long long* bsorted,
+                                               uint32_t size) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t M = qb.m, LD = qb.ld, D = qb.dim;
+  if (tid == 0) s.bmin = FLT_MAX;
+  __syncthreads();
+  if (blob >= qb.nnodes) return;
+  const uint32_t a = qb.offsets[blob];
+  const uint32_t n = qb.offsets[blob + 1] - a;
+  const uint32_t sid = blob_sid[blob];
+  if (sid != s.lut_sid) {
+    qbg_build_lut(rq, qb.gcentroid + (size_t)sid * D, qb.lcentroids, flut, lut, M, LD, s);
+    if (tid == 0) s.lut_sid = sid;
+  }
+  uint32_t L[SPL][4];
+#pragma unroll
+  for (int j = 0; j < SPL; j++) {
+    const uint32_t sv = (uint32_t)lane + 32u * (uint32_t)j;
+    const uint4 v = sv < M ? reinterpret_cast<const uint4*>(lut)[sv] : make_uint4(0, 0, 0, 0);
+    L[j][0] = v.x; L[j][1] = v.y; L[j][2] = v.z; L[j][3] = v.w;
+  }
+  const float lscale = s.lut_scale, loffset = s.lut_offset;
+  const uint8_t* stream = qb.codes + (size_t)qb.code_off16[blob] * 16;
+  const uint32_t nblk = (n + 15) / 16;
+  float wmin = FLT_MAX;
+  for (uint32_t bi = (uint32_t)warp; bi < nblk; bi += kExactWarps) {
+    int o;
+    float d = qg_block_distance<SPL>(stream + (size_t)bi * 8 * qb.ma, L, M, qb.ma, lscale, loffset, lane, &o);
+    if (o >= 0 && bi * 16 + (uint32_t)o < n) {
+      bdist[bi * 16 + o] = d;
+      wmin = fminf(wmin, d);
+    }
+  }
+  for (int off = 16; off > 0; off >>= 1) wmin = fminf(wmin, __shfl_xor_sync(0xffffffffu, wmin, off));
+  if (lane == 0) s.wmin[warp] = wmin;
+  __threadfence_block();
+  __syncthreads();
+  if (tid == 0) {
+    float mn = s.wmin[0];
+    for (int w = 1; w < kExactWarps; w++) mn = fminf(mn, s.wmin[w]);
+    s.bmin = mn;
+    s.nblobs++;
+    s.dc += n;
+  }
+  __syncthreads();
+  const float radius0 = s.radius;
+  if (s.bmin < radius0) {
+    for (uint32_t c0 = 0; c0 < n; c0 += kExactChunk) {
+      const uint32_t clen = min((uint32_t)kExactChunk, n - c0);
+      bool acc = false;
+      float d = 0.f;
+      if ((uint32_t)tid < clen) {
+        d = bdist[c0 + tid];
+        acc = d <= radius0;
+      }
+      unsigned ballot = __ballot_sync(0xffffffffu, acc);
+      if (lane == 0) s.warp_cnt[warp] = __popc(ballot);
+      __syncthreads();
+      uint32_t base = 0, m = 0;
+      for (int w = 0; w < kExactWarps; w++) {
+        if (w < warp) base += s.warp_cnt[w];
+        m += s.warp_cnt[w];
+      }
+      if (acc) bkeys[base + __popc(ballot & ((1u << lane) - 1u))] = pack_key(d, qb.ids[a + c0 + tid]);
+      __syncthreads();
+      rank_sort(bkeys, bsorted, m);
+      __syncthreads();
+      qbg_merge_results(resb, s, bsorted, m, size);
+    }
+    if (tid == 0 && s.nres >= size) s.radius = key_dist(resb[s.rcur][s.nres - 1]);
+    __syncthreads();
+  }
+}
+
 template <int SPL>
 __global__ void __launch_bounds__(kExactThreads)
 qbg_search_kernel(DevGraph g, DevQG qb, const uint32_t* __restrict__ blob_sid, const uint4* __restrict__ queries,
@@ -191,24 +296,7 @@ qbg_search_kernel(DevGraph g, DevQG qb, const uint32_t* __restrict__ blob_sid, c
       continue;
     }
     // ---- rotation (Rotation::mul, the OpenBLAS sgemv order) ------------------
-    for (uint32_t c = tid; c < D; c += blockDim.x) {
-      float acc = 0.f;
-      if (qb.rotation == nullptr) {
-        acc = c < qlen ? qf[c] : 0.f;
-      } else if (D <= 48) {
-        for (uint32_t p = 0; p < D; p++)
-          acc = __fmaf_rn(qb.rotation[(size_t)p * D + c], p < qlen ? qf[p] : 0.f, acc);
-      } else {
-        for (uint32_t p0 = 0; p0 < D; p0 += 8) {
-          const uint32_t p1 = min(p0 + 8u, D);
-          float t = __fmul_rn(qb.rotation[(size_t)p0 * D + c], p0 < qlen ? qf[p0] : 0.f);
-          for (uint32_t p = p0 + 1; p < p1; p++)
-            t = __fmaf_rn(qb.rotation[(size_t)p * D + c], p < qlen ? qf[p] : 0.f, t);
-          acc = __fadd_rn(acc, t);
-        }
-      }
-      rq[c] = acc;
-    }
+    qbg_rotate(qb, qf, qlen, rq);
     // ---- seeds: tree leaf of the global index, else the fixed random list ---
     const uint32_t* seeds = nullptr;
     uint32_t nseeds = 0;
@@ -285,77 +373,8 @@ qbg_search_kernel(DevGraph g, DevQG qb, const uint32_t* __restrict__ blob_sid, c
       if (t == ~0ull || key_dist(t) > s.expR) {
         // ---- judge the current blob ----
         const uint32_t blob = key_id(s.current);
-        if (tid == 0) { s.exploration++; s.bmin = FLT_MAX; }
-        __syncthreads();
-        if (blob < qb.nnodes) {
-          const uint32_t a = qb.offsets[blob];
-          const uint32_t n = qb.offsets[blob + 1] - a;
-          const uint32_t sid = blob_sid[blob];
-          if (sid != s.lut_sid) {
-            qbg_build_lut(rq, qb.gcentroid + (size_t)sid * D, qb.lcentroids, flut, lut, M, LD, s);
-            if (tid == 0) s.lut_sid = sid;
-          }
-          uint32_t L[SPL][4];
-#pragma unroll
-          for (int j = 0; j < SPL; j++) {
-            const uint32_t sv = (uint32_t)lane + 32u * (uint32_t)j;
-            const uint4 v = sv < M ? reinterpret_cast<const uint4*>(lut)[sv] : make_uint4(0, 0, 0, 0);
-            L[j][0] = v.x; L[j][1] = v.y; L[j][2] = v.z; L[j][3] = v.w;
-          }
-          const float lscale = s.lut_scale, loffset = s.lut_offset;
-          const uint8_t* stream = qb.codes + (size_t)qb.code_off16[blob] * 16;
-          const uint32_t nblk = (n + 15) / 16;
-          float wmin = FLT_MAX;
-          for (uint32_t bi = (uint32_t)warp; bi < nblk; bi += kExactWarps) {
-            int o;
-            float d = qg_block_distance<SPL>(stream + (size_t)bi * 8 * qb.ma, L, M, qb.ma, lscale, loffset, lane,
-                                             &o);
-            if (o >= 0 && bi * 16 + (uint32_t)o < n) {
-              bdist[bi * 16 + o] = d;
-              wmin = fminf(wmin, d);
-            }
-          }
-          for (int off = 16; off > 0; off >>= 1) wmin = fminf(wmin, __shfl_xor_sync(0xffffffffu, wmin, off));
-          if (lane == 0) s.wmin[warp] = wmin;
-          __threadfence_block();
-          __syncthreads();
-          if (tid == 0) {
-            float mn = s.wmin[0];
-            for (int w = 1; w < kExactWarps; w++) mn = fminf(mn, s.wmin[w]);
-            s.bmin = mn;
-            s.nblobs++;
-            s.dc += n;
-          }
-          __syncthreads();
-          const float radius0 = s.radius;
-          if (s.bmin < radius0) {
-            // every object within the radius joins; the set keeps the `size` smallest
-            for (uint32_t c0 = 0; c0 < n; c0 += kExactChunk) {
-              const uint32_t clen = min((uint32_t)kExactChunk, n - c0);
-              bool acc = false;
-              float d = 0.f;
-              if ((uint32_t)tid < clen) {
-                d = bdist[c0 + tid];
-                acc = d <= radius0;
-              }
-              unsigned ballot = __ballot_sync(0xffffffffu, acc);
-              if (lane == 0) s.warp_cnt[warp] = __popc(ballot);
-              __syncthreads();
-              uint32_t base = 0, m = 0;
-              for (int w = 0; w < kExactWarps; w++) {
-                if (w < warp) base += s.warp_cnt[w];
-                m += s.warp_cnt[w];
-              }
-              if (acc) bkeys[base + __popc(ballot & ((1u << lane) - 1u))] = pack_key(d, qb.ids[a + c0 + tid]);
-              __syncthreads();
-              rank_sort(bkeys, bsorted, m);
-              __syncthreads();
-              qbg_merge_results(resb, s, bsorted, m, P.size);
-            }
-            if (tid == 0 && s.nres >= P.size) s.radius = key_dist(resb[s.rcur][s.nres - 1]);
-            __syncthreads();
-          }
-        }
+        if (tid == 0) s.exploration++;
+        qbg_judge_blob<SPL>(qb, blob_sid, blob, rq, flut, lut, s, bdist, resb, bkeys, bsorted, P.size);
         // ---- stop, or take the nearest waiting blob ----
         if (s.bmin > __fmul_rn(s.radius, P.coef) || s.exploration > P.explored) break;
         const unsigned long long nxt = tq_top(dq);
@@ -468,6 +487,139 @@ qbg_search_kernel(DevGraph g, DevQG qb, const uint32_t* __restrict__ blob_sid, c
     // leave the visited bitmap clean for the next query
     for (uint32_t i = tid; i < cfg.bitmap_words; i += blockDim.x) bitmap[i] = 0u;
     __threadfence();
+    __syncthreads();
+  }
+}
+
+// Shared memory of qbg_scan_kernel: query row, rotated query, float and uint8
+// tables, the double-buffered result set, the chunk keys, the shared state.
+inline size_t qbg_scan_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, uint32_t rcap) {
+  size_t b = (size_t)row_chunks * 16;
+  b += ((size_t)dim * 4 + 15) / 16 * 16;
+  b += (size_t)m * 16 * 4;
+  b += ((size_t)m * 16 + 15) / 16 * 16;
+  b += (size_t)rcap * 16;
+  b += (size_t)kExactChunk * 16;
+  b += sizeof(QBGShared) + 16;
+  return b;
+}
+
+// The blob phase of searchInTwoSteps (lib/NGT/NGTQ/QuantizedBlobGraph.h:1240-1306):
+// one query per CTA; its probed blobs (blobs[q * bstride ..], bcount[q] of them,
+// nearest first, from the global index's graph search) are judged in that order
+// with a result set of P.size.  Results: the quantized distances, ascending.
+template <int SPL>
+__global__ void __launch_bounds__(kExactThreads)
+qbg_scan_kernel(DevQG qb, const uint32_t* __restrict__ blob_sid, const uint4* __restrict__ queries,
+                uint32_t row_chunks, uint32_t nq, const QBGParams* __restrict__ params,
+                const ObjDist* __restrict__ blobs, const uint32_t* __restrict__ bcount, uint32_t bstride,
+                ObjDist* __restrict__ out, uint32_t* __restrict__ out_count, QueryStats* __restrict__ stats,
+                float* __restrict__ blob_dist, uint32_t blob_cap, uint32_t rcap) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int tid = threadIdx.x;
+  const uint32_t rc = row_chunks;
+  const uint32_t D = qb.dim, M = qb.m;
+  uint4* qv = reinterpret_cast<uint4*>(smem);
+  float* rq = reinterpret_cast<float*>(qv + rc);
+  float* flut = rq + (D + 3) / 4 * 4;
+  uint8_t* lut = reinterpret_cast<uint8_t*>(flut + (size_t)M * 16);
+  unsigned long long* res0 = reinterpret_cast<unsigned long long*>(lut + ((size_t)M * 16 + 15) / 16 * 16);
+  unsigned long long* res1 = res0 + rcap;
+  unsigned long long* bkeys = res1 + rcap;
+  unsigned long long* bsorted = bkeys + kExactChunk;
+  QBGShared& s = *reinterpret_cast<QBGShared*>(bsorted + kExactChunk);
+  unsigned long long* resb[2] = {res0, res1};
+  float* bdist = blob_dist + (size_t)blockIdx.x * blob_cap;
+  const float* qf = reinterpret_cast<const float*>(qv);
+  for (uint32_t q = blockIdx.x; q < nq; q += gridDim.x) {
+    const QBGParams P = params[q];
+    for (uint32_t i = tid; i < rc; i += blockDim.x) qv[i] = queries[(size_t)q * rc + i];
+    if (tid == 0) {
+      s.radius = FLT_MAX;
+      s.nres = 0; s.rcur = 0;
+      s.nblobs = 0; s.expansions = 0; s.dc = 0; s.status = 0;
+      s.lut_sid = 0xffffffffu;
+    }
+    __syncthreads();
+    const uint32_t nb = P.size == 0 ? 0u : bcount[q];
+    if (nb > 0) qbg_rotate(qb, qf, rc * 4, rq);
+    __syncthreads();
+    for (uint32_t b = 0; b < nb; b++)
+      qbg_judge_blob<SPL>(qb, blob_sid, blobs[(size_t)q * bstride + b].id, rq, flut, lut, s, bdist, resb, bkeys,
+                          bsorted, P.size);
+    __syncthreads();
+    const uint32_t n = s.nres;
+    const unsigned long long* res = resb[s.rcur];
+    for (uint32_t i = tid; i < n; i += blockDim.x) out[P.out_off + i] = ObjDist{key_id(res[i]), key_dist(res[i])};
+    if (tid == 0) {
+      out_count[q] = n;
+      stats[q] = QueryStats{s.dc, 0, s.nblobs, 0, s.status};
+    }
+    __syncthreads();
+  }
+}
+
+// refineDistances (lib/NGT/NGTQ/QuantizedBlobGraph.h:1136-1185): per query (one CTA)
+// the cand_count[q] candidates at cand[q * cstride ..] get their exact L2 distances
+// over the object list (rows of `orc` 16-byte chunks, row 0 unused; the float query
+// cast element-wise to the row type, as setObject does), are sorted by (distance,
+// id) and the first min(exact[q], n) written to out[q * kmax ..].
+template <ObjType OT>
+__global__ void __launch_bounds__(256)
+qbg_refine_kernel(const ObjDist* __restrict__ cand, const uint32_t* __restrict__ cand_count, uint32_t cstride,
+                  const float* __restrict__ qrows, uint32_t qdim, const uint4* __restrict__ olist, uint32_t orc,
+                  uint32_t odim, uint32_t nrows, const uint32_t* __restrict__ exact, uint32_t nq, uint32_t P,
+                  ObjDist* __restrict__ out, uint32_t kmax, uint32_t* __restrict__ out_count) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint4* qv = reinterpret_cast<uint4*>(smem);                                        // orc chunks
+  unsigned long long* keys = reinterpret_cast<unsigned long long*>(qv + orc);          // P
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t G = 1;
+  while (G < orc && G < 32) G <<= 1;
+  const uint32_t gl = lane & (G - 1), gpw = 32 / G, ngroups = blockDim.x / G;
+  for (uint32_t q = blockIdx.x; q < nq; q += gridDim.x) {
+    const uint32_t n = min(cand_count[q], P);
+    if constexpr (OT == ObjType::Uint8) {
+      uint8_t* qb = reinterpret_cast<uint8_t*>(qv);
+      for (uint32_t i = threadIdx.x; i < orc * 16; i += blockDim.x)
+        qb[i] = i < odim && i < qdim ? (uint8_t)__float2int_rz(qrows[(size_t)q * qdim + i]) : (uint8_t)0;
+    } else {
+      float* qb = reinterpret_cast<float*>(qv);
+      for (uint32_t i = threadIdx.x; i < orc * 4; i += blockDim.x)
+        qb[i] = i < odim && i < qdim ? qrows[(size_t)q * qdim + i] : 0.f;
+    }
+    for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) keys[i] = ~0ull;
+    __syncthreads();
+    for (uint32_t b = warp * gpw; b < n; b += ngroups) {
+      const uint32_t i = b + lane / G;
+      const bool valid = i < n;
+      const uint32_t id = valid ? cand[(size_t)q * cstride + i].id : 0u;
+      const bool inrange = id > 0 && id < nrows;
+      const float d = group_distance<OT, Metric::L2>(qv, olist + (size_t)(inrange ? id : 0u) * orc, (int)orc,
+                                                     (int)gl, (int)G);
+      if (valid && gl == 0) keys[i] = pack_key(inrange ? d : FLT_MAX, id);
+    }
+    __syncthreads();
+    for (uint32_t k2 = 2; k2 <= P; k2 <<= 1) {
+      for (uint32_t j = k2 >> 1; j > 0; j >>= 1) {
+        for (uint32_t i = threadIdx.x; i < P; i += blockDim.x) {
+          const uint32_t l = i ^ j;
+          if (l > i) {
+            const unsigned long long x = keys[i], y = keys[l];
+            const bool up = (i & k2) == 0;
+            if ((x > y) == up) {
+              keys[i] = y;
+              keys[l] = x;
+            }
+          }
+        }
+        __syncthreads();
+      }
+    }
+    const uint32_t m = min(exact[q], n);
+    for (uint32_t i = threadIdx.x; i < m; i += blockDim.x)
+      out[(size_t)q * kmax + i] = ObjDist{key_id(keys[i]), key_dist(keys[i])};
+    if (threadIdx.x == 0) out_count[q] = m;
     __syncthreads();
   }
 }

@@ -218,7 +218,21 @@ class OracleQGC(ctypes.Structure):
     _fields_ = [("dim", ctypes.c_uint32), ("m", ctypes.c_uint32), ("ld", ctypes.c_uint32), ("ma", ctypes.c_uint32),
                 ("rotation", ctypes.c_void_p), ("gcentroid", ctypes.c_void_p), ("lcentroids", ctypes.c_void_p),
                 ("nnodes", ctypes.c_uint32), ("offsets", ctypes.c_void_p), ("ids", ctypes.c_void_p),
-                ("code_off", ctypes.c_void_p), ("codes", ctypes.c_void_p), ("sid", ctypes.c_void_p)]
+                ("code_off", ctypes.c_void_p), ("codes", ctypes.c_void_p), ("sid", ctypes.c_void_p),
+                ("olist", ctypes.c_void_p), ("olist_dim", ctypes.c_uint32), ("olist_type", ctypes.c_int),
+                ("olist_n", ctypes.c_uint32)]
+
+
+def read_object_list(path: str, dtype) -> np.ndarray:
+    """Rows of a QBG object list (qbg_dir/obj): an array file with a 16-byte head
+    (record size, reserved) and records of a 16-byte flag block followed by the
+    object (lib/NGT/ArrayFile.h); row 0 is the unused slot."""
+    raw = np.fromfile(path, np.uint8)
+    rs = int(raw[:8].view(np.uint64)[0])
+    n = (len(raw) - 16) // (16 + rs)
+    assert (len(raw) - 16) % (16 + rs) == 0, "truncated object list " + path
+    rec = raw[16:16 + n * (16 + rs)].reshape(n, 16 + rs)[:, 16:]
+    return np.ascontiguousarray(rec).view(dtype)
 
 
 def _read_rows(path: str, dim: int) -> np.ndarray:
@@ -292,6 +306,13 @@ class QGFiles:
         self.codes = np.concatenate(chunks) if chunks else np.zeros(0, np.uint8)
         self.sid = np.array(sids, np.uint32)
         assert (self.sid < self.ncentroids).all(), "blob subspace id beyond the codebook"
+        # QBG: the object list the refinement reads (GenuineDataType 0 uint8, 1 float)
+        self.olist = None
+        olist = os.path.join(qg, "obj")
+        if blobs and os.path.exists(olist):
+            gdt = int(self.prop.get("GenuineDataType", "0"))
+            self.olist_type = {0: 1, 1: 0}[gdt]          # oracle object types: 1 uint8, 0 float
+            self.olist = read_object_list(olist, np.uint8 if gdt == 0 else np.float32)
 
 
 class Oracle:
@@ -323,6 +344,7 @@ class Oracle:
         L.oracle_qbg_search.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                         ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_size_t,
                                         ctypes.c_float, ctypes.c_float, ctypes.c_size_t, ctypes.c_int64,
+                                        ctypes.c_int, ctypes.c_size_t,
                                         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_int]
         L.oracle_qg_rotate.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
@@ -405,6 +427,9 @@ class Oracle:
             s.offsets, s.ids, s.code_off, s.codes = (self._p(g.offsets), self._p(g.ids), self._p(g.code_off),
                                                      self._p(g.codes))
             s.sid = self._p(g.sid) if blobs_path else None
+            if blobs_path and g.olist is not None:
+                s.olist, s.olist_dim, s.olist_type, s.olist_n = (self._p(g.olist), g.olist.shape[1], g.olist_type,
+                                                                 g.olist.shape[0])
             self.qg = s
         return self.qg
 
@@ -437,10 +462,18 @@ class Oracle:
         return ids, ds, n, dc
 
     def qbg_search(self, queries, qbg_path, k=20, epsilon=0.1, blob_epsilon=0.0, result_expansion=3.0,
-                   explored_blobs=256, edges=0, threads=1):
+                   explored_blobs=256, edges=0, threads=1, two_step=False, refinement_expansion=None):
         """qbg_search_index_float over a QBG index whose global index this Oracle
         was built on (defaults of qbg_initialize_query_parameters,
-        lib/NGT/NGTQ/Capi.cpp:528-536).  Returns ids, distances, counts, blobs judged."""
+        lib/NGT/NGTQ/Capi.cpp:528-536).  Returns ids, distances, counts, blobs judged.
+
+        two_step: searchInTwoSteps with explored_blobs probes.  refinement_expansion
+        (>= 1): the search keeps k x expansion results, re-ranked by exact distance
+        over the object list to the k best (the search containers of the reference's
+        CLI and ngtpy); it replaces result_expansion."""
+        refine = refinement_expansion is not None and refinement_expansion >= 1.0
+        if refinement_expansion is not None:
+            result_expansion = refinement_expansion
         qg = self._qg(qbg_path)
         qf = np.zeros((len(queries), self.f.dpad), np.float32)
         q = np.asarray(queries, np.float32)
@@ -453,8 +486,11 @@ class Oracle:
         ds = np.zeros((nq, kout), np.float32)
         n = np.zeros(nq, np.uint32)
         nb = np.zeros(nq, np.uint32)
+        if refine and not qg.olist:
+            raise ValueError("the refinement needs the QBG object list (qbg_dir/obj)")
         self.lib.oracle_qbg_search(ctypes.byref(self.s), ctypes.byref(qg), qf.ctypes.data, self.f.dpad,
                                    rows.ctypes.data, nq, size, kout, epsilon, blob_epsilon, explored_blobs, edges,
+                                   1 if two_step else 0, k if refine else 0,
                                    ids.ctypes.data, ds.ctypes.data, n.ctypes.data, nb.ctypes.data, threads)
         return ids, ds, n, nb
 

@@ -579,6 +579,10 @@ typedef struct {
   const uint64_t *code_off;  /* byte offset of each node's code stream in codes */
   const uint8_t *codes;
   const uint32_t *sid;       /* QBG: per blob, the codebook centroid of its LUT (NULL: centroid 0) */
+  const void *olist;         /* QBG: the object list (qbg_dir/obj), rows of olist_dim; row 0 unused */
+  uint32_t olist_dim;
+  int olist_type;            /* OT_UINT8 or OT_FLOAT */
+  uint32_t olist_n;          /* rows including row 0 */
 } OracleQG;
 
 /* Rotation::mul (lib/NGT/NGTQ/Quantizer.h:117-160), y[c] = sum_p R[p][c] x[p].  The
@@ -794,19 +798,20 @@ void oracle_qg_search(const OracleIndex *ix, const OracleQG *qg, const float *qf
  * refinementExpansion at 0), so the distances returned are the quantized ones.
  * ix is the global index (blob centroids, their graph and tree); qg the blobs. */
 static size_t qbg_one(const OracleIndex *ix, const OracleQG *qg, const float *qf, size_t qdim, const void *q,
-                      size_t size, float epsilon, float blob_epsilon, size_t explored, int64_t edge_size,
-                      uint32_t *ids, float *ds, uint32_t *blobs_out) {
+                      size_t size, size_t seed_size, float epsilon, float blob_epsilon, size_t explored,
+                      int64_t edge_size, uint32_t *ids, float *ds, uint32_t *blobs_out) {
   *blobs_out = 0;
   if (size == 0) return 0;
   float coef = epsilon + 1.0f;
   if (coef == 0.0f) coef = 1.1f;
   float bcoef = blob_epsilon + 1.0f;
   size_t esz = edge_size_for(ix, edge_size, coef);
-  /* seeds: getSeedsFromTree over the global graph with sc.size = size, else 20 random */
+  /* seeds: getSeedsFromTree over the global graph with the container's size (the result
+   * size before a refinement expansion, QuantizedBlobGraph.h:1336-1345), else 20 random */
   uint32_t *seeds = (uint32_t *)malloc(sizeof(uint32_t) * 65536);
   uint32_t tdc = 0;
   size_t ns = 0;
-  if (ix->has_tree) ns = tree_seeds(ix, q, size, seeds, &tdc);
+  if (ix->has_tree) ns = tree_seeds(ix, q, seed_size, seeds, &tdc);
   if (ns == 0) {
     OracleIndex tmp = *ix;
     tmp.seed_size = 20;
@@ -897,17 +902,104 @@ static size_t qbg_one(const OracleIndex *ix, const OracleQG *qg, const float *qf
   return nres;
 }
 
-/* qf: nq x qdim float queries; qrows: the same prepared as global-index rows.  kout >= size. */
+/* searchInTwoSteps (lib/NGT/NGTQ/QuantizedBlobGraph.h:1190-1330): the `probes` blobs
+ * nearest the query by the read-only graph search of the global index (epsilon =
+ * blob_epsilon as (1 + blob_epsilon) - 1, the index's edge size), then every probed
+ * blob judged in that order with a result set of `size` (judge,
+ * QuantizedBlobGraph.h:1033-1080: skipped when its minimum is not below the radius). */
+static size_t qbg_two(const OracleIndex *ix, const OracleQG *qg, const float *qf, size_t qdim, const void *q,
+                      size_t size, size_t probes, float blob_epsilon, uint32_t *ids, float *ds,
+                      uint32_t *blobs_out) {
+  *blobs_out = 0;
+  if (size == 0 || probes == 0) return 0;
+  uint32_t *bid = (uint32_t *)malloc(sizeof(uint32_t) * (probes + 1));
+  float *bdist = (float *)malloc(sizeof(float) * (probes + 1));
+  uint32_t dc = 0;
+  const float geps = (blob_epsilon + 1.0f) - 1.0f;
+  size_t nb = graph_one(ix, q, probes, probes, geps, FLT_MAX, -1, 0, bid, bdist, &dc, NULL, 0);
+  float *rq = (float *)calloc(qg->dim > qdim ? qg->dim : qdim, sizeof(float));
+  memcpy(rq, qf, qdim * sizeof(float));
+  float *rot = (float *)malloc(qg->dim * sizeof(float));
+  oracle_qg_rotate(qg, rq, rot);
+  uint8_t *lut = (uint8_t *)malloc((size_t)qg->m * 16);
+  float *bd = (float *)malloc(sizeof(float) * 65536);
+  od_t *res = (od_t *)malloc((size + 2) * sizeof(od_t));
+  size_t nres = 0;
+  float radius = FLT_MAX;
+  uint32_t judged = 0;
+  for (size_t b = 0; b < nb; b++) {
+    uint32_t blob = bid[b];
+    if (blob >= qg->nnodes) continue;
+    uint32_t a = qg->offsets[blob], n = qg->offsets[blob + 1] - a;
+    float scale, offset;
+    uint32_t c = qg->sid ? qg->sid[blob] : 0;
+    qg_lut_centroid(qg, rot, qg->gcentroid + (size_t)c * qg->dim, lut, &scale, &offset);
+    float bmin = n ? oracle_qg_scan(qg, lut, scale, offset, blob, bd) : FLT_MAX;
+    judged++;
+    if (bmin >= radius) continue;
+    for (uint32_t i = 0; i < n; i++) {
+      if (bd[i] <= radius) {
+        od_t x = {qg->ids[a + i], bd[i]};
+        maxheap_push(res, &nres, x);
+        if (nres > size) maxheap_pop(res, &nres);
+      }
+    }
+    if (nres >= size) radius = res[0].d;
+  }
+  qsort(res, nres, sizeof(od_t), od_cmp);
+  for (size_t i = 0; i < nres; i++) { ids[i] = res[i].id; ds[i] = res[i].d; }
+  free(res); free(bd); free(lut); free(rot); free(rq); free(bid); free(bdist);
+  *blobs_out = judged;
+  return nres;
+}
+
+/* refineDistances (lib/NGT/NGTQ/QuantizedBlobGraph.h:1136-1185): the results' exact
+ * distances to the query over the object list (its comparator: L2 over uint8 or float
+ * rows; a float query is cast element-wise to the row type, as setObject does,
+ * lib/NGT/ObjectRepository.h:237-246), then the `exact` best by (distance, id). */
+static size_t qbg_refine(const OracleQG *qg, const float *qf, size_t qdim, uint32_t *ids, float *ds, size_t n,
+                         size_t exact) {
+  size_t d = qg->olist_dim;
+  size_t es = qg->olist_type == OT_FLOAT ? 4 : 1;
+  uint8_t *qv = (uint8_t *)calloc(d, es);
+  for (size_t i = 0; i < d && i < qdim; i++) {
+    if (qg->olist_type == OT_FLOAT) ((float *)qv)[i] = qf[i];
+    else qv[i] = (uint8_t)qf[i];
+  }
+  od_t *r = (od_t *)malloc((n + 1) * sizeof(od_t));
+  for (size_t i = 0; i < n; i++) {
+    r[i].id = ids[i];
+    r[i].d = ids[i] < qg->olist_n
+                 ? compare(qg->olist_type, M_L2, qv, (const uint8_t *)qg->olist + (size_t)ids[i] * d * es, d)
+                 : FLT_MAX;
+  }
+  qsort(r, n, sizeof(od_t), od_cmp);
+  size_t m = n < exact ? n : exact;
+  for (size_t i = 0; i < m; i++) { ids[i] = r[i].id; ds[i] = r[i].d; }
+  free(r); free(qv);
+  return m;
+}
+
+/* qf: nq x qdim float queries; qrows: the same prepared as global-index rows.  kout >= size.
+ * two_step: searchInTwoSteps with `explored` probes, else searchInOneStep.  exact > 0:
+ * refinement to the `exact` best by exact distance (needs the object list). */
 void oracle_qbg_search(const OracleIndex *ix, const OracleQG *qg, const float *qf, size_t qdim, const void *qrows,
                        size_t nq, size_t size, size_t kout, float epsilon, float blob_epsilon, size_t explored,
-                       int64_t edge_size, uint32_t *out_ids, float *out_d, uint32_t *out_n, uint32_t *out_blobs,
-                       int nthreads) {
+                       int64_t edge_size, int two_step, size_t exact, uint32_t *out_ids, float *out_d,
+                       uint32_t *out_n, uint32_t *out_blobs, int nthreads) {
   size_t rb = (size_t)ix->dpad * elem_size(ix->otype);
 #pragma omp parallel for schedule(dynamic) num_threads(nthreads)
   for (long q = 0; q < (long)nq; q++) {
     uint32_t nb = 0;
-    out_n[q] = (uint32_t)qbg_one(ix, qg, qf + q * qdim, qdim, (const uint8_t *)qrows + q * rb, size, epsilon,
-                                 blob_epsilon, explored, edge_size, out_ids + q * kout, out_d + q * kout, &nb);
+    size_t n;
+    if (two_step)
+      n = qbg_two(ix, qg, qf + q * qdim, qdim, (const uint8_t *)qrows + q * rb, size, explored, blob_epsilon,
+                  out_ids + q * kout, out_d + q * kout, &nb);
+    else
+      n = qbg_one(ix, qg, qf + q * qdim, qdim, (const uint8_t *)qrows + q * rb, size, exact > 0 ? exact : size,
+                  epsilon, blob_epsilon, explored, edge_size, out_ids + q * kout, out_d + q * kout, &nb);
+    if (exact > 0 && qg->olist) n = qbg_refine(qg, qf + q * qdim, qdim, out_ids + q * kout, out_d + q * kout, n, exact);
+    out_n[q] = (uint32_t)n;
     if (out_blobs) out_blobs[q] = nb;
   }
 }

@@ -51,6 +51,7 @@ int main(int argc, char** argv) {
     sc.setEpsilon(eps);
     sc.setSize(k);
     sc.setBlobEpsilon(beps);
+    sc.setEdgeSize(0);                      // as qbg_search_index_ (NGTQ/Capi.cpp:570): every global edge
     if (mode == "two") index.searchInTwoSteps(sc);
     else index.searchInOneStep(sc);
     if (objects.size() > k) objects.resize(k);

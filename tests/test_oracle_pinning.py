@@ -114,9 +114,12 @@ def test_oracle_qbg_matches_reference_golden(name, workdir):
     path, meta, queries, golden = materialize(name, workdir)
     o = oracle.Oracle(oracle.IndexFiles(os.path.join(path, "global")))
     for i, s in enumerate(meta["settings"]):
+        # "qbg": the C API (one step, result expansion); "qbg1" / "qbg2": searchInOneStep /
+        # searchInTwoSteps with a refinement expansion (exact re-rank over the object list)
+        kw = {} if s["op"] == "qbg" else dict(refinement_expansion=s["result_expansion"], two_step=s["op"] == "qbg2")
         ids, ds, n, _ = o.qbg_search(queries[:s["nq"]], path, k=s["k"], epsilon=s["epsilon"],
                                      blob_epsilon=s["blob_epsilon"], result_expansion=s["result_expansion"],
-                                     explored_blobs=s["explored_blobs"], threads=4)
+                                     explored_blobs=s["explored_blobs"], threads=4, **kw)
         gi, gd, gc = golden["ids_%d" % i], golden["dist_%d" % i], golden["count_%d" % i]
         assert np.array_equal(n, gc), (name, s)
         assert np.array_equal(ids[:, :s["width"]], gi), (name, s)
