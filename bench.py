@@ -523,21 +523,62 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def _fp64_topk(xd, q, k, metric, M=0.0):
+    """FP64 ground truth on the GPU: per query the k-th smallest FP64 distance and the
+    FP64 distances of every object, for tie-aware checks (cosine: 1 - cos over unit
+    rows; inner product: the L2 over the augmented rows, sqrt(|q|^2 + M - 2 q.x))."""
+    import torch
+    out = []
+    for s0 in range(0, q.shape[0], 256):
+        qd = torch.from_numpy(q[s0:s0 + 256]).cuda().double()
+        if metric == "cosine":
+            qd = qd / qd.norm(dim=1, keepdim=True)
+            d = 1.0 - qd @ xd.T
+        else:
+            d = ((qd * qd).sum(1, keepdim=True) + M - 2.0 * (qd @ xd.T)).clamp_min(0).sqrt()
+        out.append(torch.topk(d, k, dim=1, largest=False).values[:, k - 1].cpu())
+    return torch.cat(out).numpy()
+
+
+def _fp64_agreement(xd, q, ids, kth, metric, M=0.0):
+    """Share of queries whose k returned ids all lie within the FP64 top k (ties at the
+    k-th FP64 distance allowed), i.e. the returned set is an FP64 exact answer."""
+    import torch
+    ok = 0
+    for s0 in range(0, q.shape[0], 256):
+        qd = torch.from_numpy(q[s0:s0 + 256]).cuda().double()
+        idx = torch.from_numpy(ids[s0:s0 + 256].astype(np.int64) - 1).cuda()
+        rows = xd[idx]                                             # [b, k, dim]
+        if metric == "cosine":
+            qd = qd / qd.norm(dim=1, keepdim=True)
+            d = 1.0 - torch.einsum("bd,bkd->bk", qd, rows)
+        else:
+            d = ((qd * qd).sum(1, keepdim=True) + M - 2.0 * torch.einsum("bd,bkd->bk", qd, rows)
+                 ).clamp_min(0).sqrt()
+        lim = torch.from_numpy(kth[s0:s0 + 256]).cuda()[:, None] * (1 + 1e-12) + 1e-15
+        ok += int((d <= lim).all(1).sum().item())
+    return ok / q.shape[0]
+
+
 def precision_path(args, steps=None, warmup=None):
     """Exact brute-force k-NN with the tensor-core pre-selection.
 
     Workload: n x 768 float32 rows drawn from 64 Gaussian clusters (means N(0,1),
-    within-cluster sigma 0.5; seeds 21 means, 22 rows, 23 queries), L2-normalised
-    and searched as a NormalizedCosine index; k=100; the 400 best bf16
-    tensor-core scores per query re-ranked with the exact fp32 comparator.  One
-    step = one device-resident call over all queries.  The rows (3 GB at 1M)
-    exceed L2, so no flush.  Ids are checked against an FP64 exhaustive ground
-    truth (torch fp64 on the GPU) for 200 queries."""
+    within-cluster sigma 0.5; seeds 21 means, 22 rows, 23 queries), searched two
+    ways: L2-normalised as a NormalizedCosine index, and raw as an InnerProduct
+    index (rows stored augmented to 769 dims with sqrt(M - |x|^2), M the largest
+    |x|^2); k=100.  Each runs with bf16 and with per-row scaled FP8 (E4M3) scores on
+    the tensor cores (fp32 accumulation), the best C candidates re-ranked with the
+    exact fp32 comparator and the ties at the cut decided in FP64.  C is the
+    smallest of 400, 800, 1600, 3200 whose results on the first 1,000 queries are
+    FP64-exact; every query's result is then checked against the FP64 ground truth
+    (torch fp64 on the GPU).  One step = one device-resident call over all queries.
+    The rows (3 GB) exceed L2, so no flush."""
     import torch
     from ngt_gb300 import Index
+    from ngt_gb300.base import TC_BF16, TC_FP8, TC_FP64_TIES
     from ngt_gb300.graph_build import write_index
-    n, dim, nq, k, C = args.pp_n, 768, args.pp_nq, 100, 400
-    path = os.path.join(args.workdir, "clusters_%d_%d" % (n, dim))
+    n, dim, nq, k = args.pp_n, 768, args.pp_nq, 100
     means = np.random.default_rng(21).standard_normal((64, dim)).astype(np.float32)
 
     def mixture(seed, m):
@@ -548,97 +589,136 @@ def precision_path(args, steps=None, warmup=None):
 
     t0 = time.time()
     x = mixture(22, n)
-    x /= np.linalg.norm(x, axis=1, keepdims=True)
     q = mixture(23, nq)
-    if not os.path.exists(os.path.join(path, "grp")):
-        ring = np.concatenate([np.arange(2, n + 1), [1]]).astype(np.uint32)      # node i -> i % n + 1
-        offsets = np.concatenate([[0, 0], np.arange(1, n + 1)]).astype(np.int64)
-        write_index(path, x, offsets, ring, np.zeros(n, np.float32),
-                    extra_prf={"DistanceType": "NormalizedCosine", "EdgeSizeForSearch": "10"})
-    ix = Index(path, read_only=True)
-    log("precision path setup %.1f s" % (time.time() - t0))
-    ix._check(ix._lib.ngtgpu_set_tc_first_rows(ix._index, args.pp_first_rows, ix._err))
-    rows = torch.from_numpy(ix.convert_queries(q)).cuda()
-    res = torch.zeros((nq, k, 2), dtype=torch.int32, device="cuda")
-    cnt = torch.zeros(nq, dtype=torch.int32, device="cuda")
-    status = torch.zeros(nq, dtype=torch.int32, device="cuda")
-    stream = torch.cuda.Stream()
-
-    def step():
-        ok = ix._lib.ngtgpu_linear_search_tc_device(ix._index, rows.data_ptr(), nq, k, C, res.data_ptr(), k,
-                                                    cnt.data_ptr(), status.data_ptr(), stream.cuda_stream,
-                                                    ix._err)
-        ix._check(ok)
-
-    steps = steps or args.steps
-    warmup = max(3, warmup or args.warmup)
-    for _ in range(warmup):
-        step()
-    torch.cuda.synchronize()
-    times, phases = [], []
-    launches0 = ix.kernel_launches()
-    with ClockSampler(0) as clocks:
-        for _ in range(steps):
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            step()
-            e1.record(stream)
-            e1.synchronize()
-            times.append(e0.elapsed_time(e1))
-            phases.append(ix.tc_phase_times())
-    launches = (ix.kernel_launches() - launches0) // max(1, steps)
-    ms = statistics.median(times)
-    ph = [statistics.median(p[i] for p in phases) for i in range(3)]
-    # e2e: host queries in, host results out, through the host-buffer call
-    e2e = []
-    for _ in range(max(2, steps // 2)):
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        ix.linear_search_tc(q, k=k, candidates=C, first_rows=args.pp_first_rows)
-        e2e.append(time.perf_counter() - t)
-    e2e_s = statistics.median(e2e)
-    # FP64 ground truth for 200 queries
-    ids = res[:, :, 0].cpu().numpy().astype(np.int64)
-    gt_q = min(200, nq)
-    xd = torch.from_numpy(x).cuda().double()
-    qd = torch.from_numpy(q[:gt_q]).cuda().double()
-    qd = qd / qd.norm(dim=1, keepdim=True)
-    d64 = 1.0 - qd @ xd.T
-    kth = torch.sort(d64, dim=1).values[:, k - 1]
-    got = torch.gather(d64, 1, torch.from_numpy(ids[:gt_q] - 1).cuda())
-    exact = (got <= kth[:, None] + 1e-9).all(1).float().mean().item()
-    del xd, d64
-    # plain fp32 linear search (one query per call through the reference's C API)
-    plain = []
-    for j in range(20):
-        torch.cuda.synchronize()
-        t = time.perf_counter()
-        ix.linear_search(q[j], k=k)
-        plain.append(time.perf_counter() - t)
-    plain_qps = 1.0 / statistics.median(plain)
-    first = args.pp_first_rows or 8192
-    flops_filter = 2.0 * nq * max(0, n + 1 - first) * dim
+    ring = np.concatenate([np.arange(2, n + 1), [1]]).astype(np.uint32)      # node i -> i % n + 1
+    offsets = np.concatenate([[0, 0], np.arange(1, n + 1)]).astype(np.int64)
     peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
         os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
-    peak = peaks.get("bf16_tflops", 1900.0)
-    achieved = flops_filter / (ph[1] * 1e-3) / 1e12 if ph[1] > 0 else None
+    bf16_peak = peaks.get("bf16_tflops", 1900.0)
+    steps = steps or args.steps
+    warmup = max(3, warmup or args.warmup)
+    first = args.pp_first_rows or 8192
+    out = {}
+    for metric in ("cosine", "inner_product"):
+        M = 0.0
+        if metric == "cosine":
+            rows_x = x / np.linalg.norm(x, axis=1, keepdims=True)
+            path = os.path.join(args.workdir, "clusters_%d_%d" % (n, dim))
+            prf = {"DistanceType": "NormalizedCosine", "EdgeSizeForSearch": "10"}
+        else:
+            n2 = (x.astype(np.float64) ** 2).sum(1)
+            M = float(n2.max())
+            rows_x = np.concatenate([x, np.sqrt(np.maximum(M - n2, 0.0))[:, None].astype(np.float32)], axis=1)
+            path = os.path.join(args.workdir, "clusters_ip_%d_%d" % (n, dim))
+            prf = {"DistanceType": "InnerProduct", "Dimension": str(dim), "MaxMagnitude": repr(M),
+                   "EdgeSizeForSearch": "10"}
+        if not os.path.exists(os.path.join(path, "grp")):
+            write_index(path, rows_x, offsets, ring, np.zeros(n, np.float32), extra_prf=prf)
+        ix = Index(path, read_only=True)
+        log("precision path %s setup %.1f s" % (metric, time.time() - t0))
+        ix._check(ix._lib.ngtgpu_set_tc_first_rows(ix._index, args.pp_first_rows, ix._err))
+        xd = torch.from_numpy(rows_x[:, :dim]).cuda().double()
+        kth = _fp64_topk(xd, q, k, metric, M)
+        log("precision path %s FP64 ground truth %.1f s" % (metric, time.time() - t0))
+        rows = torch.from_numpy(ix.convert_queries(q)).cuda()
+        cap_c = 3200
+        res = torch.zeros((nq, k, 2), dtype=torch.int32, device="cuda")
+        cnt = torch.zeros(nq, dtype=torch.int32, device="cuda")
+        status = torch.zeros(nq, dtype=torch.int32, device="cuda")
+        stream = torch.cuda.Stream()
+        for prec_name, prec in (("bf16", TC_BF16), ("fp8", TC_FP8)):
+
+            def step(C, nqq=nq):
+                ok = ix._lib.ngtgpu_linear_search_tc_ex(ix._index, rows.data_ptr(), nqq, k, C, prec, TC_FP64_TIES,
+                                                        res.data_ptr(), k, cnt.data_ptr(), status.data_ptr(),
+                                                        stream.cuda_stream, ix._err)
+                ix._check(ok)
+
+            cal = min(1000, nq)
+            C_sel = cap_c
+            for C in (400, 800, 1600, cap_c):
+                step(C, cal)
+                torch.cuda.synchronize()
+                agree = _fp64_agreement(xd, q[:cal], res[:cal, :, 0].cpu().numpy(), kth[:cal], metric, M)
+                log("precision %s %s C=%d: FP64-exact on %.4f of %d calibration queries" % (
+                    metric, prec_name, C, agree, cal))
+                if agree == 1.0:
+                    C_sel = C
+                    break
+            for _ in range(warmup):
+                step(C_sel)
+            torch.cuda.synchronize()
+            times, phases = [], []
+            launches0 = ix.kernel_launches()
+            with ClockSampler(0) as clocks:
+                for _ in range(steps):
+                    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                    e0.record(stream)
+                    step(C_sel)
+                    e1.record(stream)
+                    e1.synchronize()
+                    times.append(e0.elapsed_time(e1))
+                    phases.append(ix.tc_phase_times())
+            launches = (ix.kernel_launches() - launches0) // max(1, steps)
+            ms = statistics.median(times)
+            ph = [statistics.median(p[i] for p in phases) for i in range(3)]
+            agree_all = _fp64_agreement(xd, q, res[:, :, 0].cpu().numpy(), kth, metric, M)
+            # e2e: host queries in, host results out, through the host-buffer call
+            e2e = []
+            for _ in range(max(2, steps // 2)):
+                torch.cuda.synchronize()
+                t = time.perf_counter()
+                ix.linear_search_tc(q, k=k, candidates=C_sel, first_rows=args.pp_first_rows, precision=prec_name,
+                                    fp64_ties=True)
+                e2e.append(time.perf_counter() - t)
+            e2e_s = statistics.median(e2e)
+            kp = (dim + 63) // 64 * 64 if prec_name == "bf16" else (dim + 127) // 128 * 128
+            if metric == "inner_product":
+                kp = (dim + 1 + 63) // 64 * 64 if prec_name == "bf16" else (dim + 1 + 127) // 128 * 128
+            flops_filter = 2.0 * nq * max(0, n + 1 - first) * kp
+            peak = bf16_peak * (2.0 if prec_name == "fp8" else 1.0)
+            achieved = flops_filter / (ph[1] * 1e-3) / 1e12 if ph[1] > 0 else None
+            out["%s_%s" % (metric, prec_name)] = {
+                "value": nq / (ms * 1e-3), "unit": "queries/s", "ms_per_step": ms, "candidates": C_sel,
+                "dtype": "%s+f32-rerank+fp64-ties" % prec_name,
+                "phases_ms": {"dense_and_select": ph[0], "filtered_scores": ph[1], "rerank": ph[2]},
+                "roofline": {"bound": "tensor", "kernel": "tc_score_kernel (filtered part)",
+                             "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                             "frac": (achieved / peak) if achieved else None, "traffic": None,
+                             "peak_source": ("measured" if peaks else "fallback") + (
+                                 " bf16 x 2 (the nominal fp8:bf16 ratio)" if prec_name == "fp8" else "")},
+                "e2e": {"value": nq / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
+                        "d2h_bytes_per_step": int(nq * k * 8 + nq * 8)},
+                "exact_id_agreement_fp64": agree_all, "fp64_checked_queries": nq,
+                "overflow_queries": int(((status & 1) != 0).sum().item()),
+                "wide_tie_windows": int(((status & 4) != 0).sum().item()),
+                "gpu_launches": int(launches), "clocks": clocks.summary()}
+            log("precision %s %s: %.0f q/s at C=%d, FP64-exact on %.4f of %d queries" % (
+                metric, prec_name, nq / (ms * 1e-3), C_sel, agree_all, nq))
+        if metric == "cosine":
+            # plain fp32 linear search (one query per call through the reference's C API)
+            plain = []
+            for j in range(20):
+                torch.cuda.synchronize()
+                t = time.perf_counter()
+                ix.linear_search(q[j], k=k)
+                plain.append(time.perf_counter() - t)
+            out["plain_fp32_linear_qps"] = 1.0 / statistics.median(plain)
+        del xd
+        ix.close()
+        torch.cuda.empty_cache()
+    head = out["cosine_bf16"]
     return {
-        "metric": "queries/s, exact brute-force k=100 (1M x 768 cosine, bf16 tensor-core scores + fp32 re-rank "
-                  "of 400)" if n == 1_000_000 else "queries/s, exact brute-force k=100 (n=%d x 768 cosine)" % n,
-        "value": nq / (ms * 1e-3), "unit": "queries/s", "n_gpus": 1, "steps": steps, "warmup": warmup,
-        "ms_per_step": ms, "higher_is_better": True, "scaling": "replicas only", "vs_baseline": None,
-        "dtype": "bf16+f32-rerank", "data": "synthetic (seeded Gaussian clusters)",
-        "config": {"workload": "brute-force %d x %d NormalizedCosine, %d queries, k=%d, candidates=%d" % (
-            n, dim, nq, k, C), "l2": "rows exceed L2, no flush"},
-        "phases_ms": {"dense_and_select": ph[0], "filtered_scores": ph[1], "rerank": ph[2]},
-        "roofline": {"bound": "tensor", "kernel": "tc_score_kernel (filtered part)",
-                     "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": (achieved / peak) if achieved else None, "traffic": None,
-                     "peak_source": "measured" if peaks else "fallback"},
-        "e2e": {"value": nq / e2e_s, "unit": "queries/s", "h2d_bytes_per_step": int(q.nbytes),
-                "d2h_bytes_per_step": int(nq * k * 8 + nq * 8)},
-        "exact_id_agreement_fp64": exact, "overflow_queries": int((status != 0).sum().item()),
-        "plain_fp32_linear_qps": plain_qps, "gpu_launches": int(launches), "clocks": clocks.summary(),
+        "metric": "queries/s, exact brute-force k=100 (1M x 768 cosine, bf16 tensor-core scores + fp32 re-rank, "
+                  "FP64 ties)" if n == 1_000_000 else "queries/s, exact brute-force k=100 (n=%d x 768 cosine)" % n,
+        "value": head["value"], "unit": "queries/s", "n_gpus": 1, "steps": steps, "warmup": warmup,
+        "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak (row-range shards)",
+        "vs_baseline": None, "dtype": head["dtype"], "data": "synthetic (seeded Gaussian clusters)",
+        "config": {"workload": "brute-force %d x %d, %d queries, k=%d; cosine and inner product; bf16 and fp8 "
+                               "scores" % (n, dim, nq, k), "l2": "rows exceed L2, no flush"},
+        "roofline": head["roofline"], "e2e": head["e2e"], "gpu_launches": head["gpu_launches"],
+        "clocks": head["clocks"], "exact_id_agreement_fp64": head["exact_id_agreement_fp64"],
+        "variants": out,
     }
 
 
