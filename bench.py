@@ -88,7 +88,8 @@ def parse():
     ap.add_argument("--k", type=int, default=10)
     ap.add_argument("--workdir", default=os.environ.get("NGT_BENCH_DIR", "/tmp/ngt_bench"))
     ap.add_argument("--cpu-sample", type=int, default=2000, help="queries in the CPU-baseline sample")
-    ap.add_argument("--served-rates", type=lambda s: [int(x) for x in s.split(",")], default=[5000, 20000, 50000],
+    ap.add_argument("--served-rates", type=lambda s: [int(x) for x in s.split(",")],
+                    default=[20000, 100000, 200000, 400000],
                     help="offered query rates of the serving measurement")
     ap.add_argument("--served-seconds", type=float, default=2.0, help="length of each served-rate run")
     ap.add_argument("--qg", type=int, default=1, help="also measure the quantized-graph search (1) or not (0)")
@@ -102,6 +103,11 @@ def parse():
     ap.add_argument("--pp-n", type=int, default=1_000_000, help="rows of the brute-force workload")
     ap.add_argument("--pp-nq", type=int, default=10_000, help="queries of the brute-force workload")
     ap.add_argument("--pp-first-rows", type=int, default=0, help="dense rows before the threshold filter (0 auto)")
+    ap.add_argument("--qbg", type=int, default=1,
+                    help="also measure the quantized-blob-graph search on 10M x 128 uint8 objects (1) or not (0)")
+    ap.add_argument("--qbg-only", action="store_true", help="measure the quantized-blob-graph search alone")
+    ap.add_argument("--qbg-n", type=int, default=10_000_000, help="objects of the quantized-blob-graph workload")
+    ap.add_argument("--qbg-blobs", type=int, default=65536, help="blobs of the quantized-blob-graph workload")
     ap.add_argument("--fixed", default=None,
                     help="EPS_PLAIN:EPS_BATCHED -- skip the epsilon / tuning sweeps (profiling runs)")
     ap.add_argument("--fixed-config", default='{"kernel": 3, "L": 256, "P": 10, "T": 128, "stage": 16}',
@@ -252,64 +258,130 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def served_latency(ix, queries, k, eps, rates, seconds, kernel=1, inflight=3, max_batch=4096):
-    """Poisson arrivals of requests (sizes geometric on 1..256, mean ~16 queries) at each
-    target query rate through the serving loop; p50/p99 request latency (submit to completion)."""
+def poisson_stream(submit, wait, nqueries, rates, seconds, draw, rng, check=None, warm=None):
+    """Poisson request arrivals at each offered query rate (request sizes geometric on
+    1..256, mean ~16 queries; parameters drawn per request by draw(rng)) through a
+    serving loop; latency from submit to completion as the loop measures it.  check
+    (query rows, parameters, ids, counts) -> (hits, total) accumulates recall."""
     import threading
-    from ngt_gb300 import Server
     out = []
-    rng = np.random.default_rng(43)
-    with Server(ix, max_batch=max_batch, inflight=inflight, max_k=max(16, k), kernel=kernel) as srv:
-        # warm-up (untimed): every lane launches a few times before the first rate
-        warm = [srv.submit(queries[i * 64:(i + 1) * 64], k=k, epsilon=eps) for i in range(4 * inflight)]
-        for t_ in warm:
-            srv.wait(t_)
-        for rate in rates:
-            sizes, gaps = [], []
-            t = 0.0
-            while t < seconds:
-                n = int(min(256, rng.geometric(1.0 / 16.0)))
-                sizes.append(n)
-                gap = rng.exponential(n / rate)
-                gaps.append(gap)
-                t += gap
-            tickets = []
-            done = threading.Event()
-            lat = []
+    if warm:
+        warm()
+    for rate in rates:
+        reqs, t = [], 0.0
+        while t < seconds:
+            n = int(min(256, rng.geometric(1.0 / 16.0)))
+            gap = rng.exponential(n / rate)
+            s0 = int(rng.integers(0, nqueries - n + 1))
+            reqs.append((s0, n, draw(rng), gap))
+            t += gap
+        tickets, lat, hits = [], [], [0, 0]
+        done = threading.Event()
 
-            def waiter():
-                i = 0
-                while True:
-                    while i >= len(tickets):
-                        if done.is_set() and i >= len(tickets):
-                            return
-                        time.sleep(0.0002)
-                    lat.append(srv.wait(tickets[i])[3])
-                    i += 1
+        def waiter():
+            i = 0
+            while True:
+                while i >= len(tickets):
+                    if done.is_set() and i >= len(tickets):
+                        return
+                    time.sleep(0.0002)
+                ids, ds, cnt, l = wait(tickets[i])
+                lat.append(l)
+                if check:
+                    s0, n, prm, _ = reqs[i]
+                    h, tot = check(s0, n, prm, ids, cnt)
+                    hits[0] += h
+                    hits[1] += tot
+                i += 1
 
-            th = threading.Thread(target=waiter)
-            th.start()
-            t0 = time.perf_counter()
-            nxt = t0
-            pos = 0
-            total = 0
-            for n, gap in zip(sizes, gaps):
-                nxt += gap
-                while time.perf_counter() < nxt:
-                    pass
-                q = queries[pos:pos + n] if pos + n <= len(queries) else queries[:n]
-                pos = (pos + n) % max(1, len(queries) - 256)
-                tickets.append(srv.submit(q, k=k, epsilon=eps))
-                total += n
-            done.set()
-            th.join()
-            wall = time.perf_counter() - t0
-            lat_np = np.array(lat)
-            out.append({"offered_qps": rate, "achieved_qps": round(total / wall, 1), "requests": len(sizes),
-                        "p50_ms": round(float(np.percentile(lat_np, 50)), 3),
-                        "p99_ms": round(float(np.percentile(lat_np, 99)), 3)})
-            log("served (kernel %d) at %d q/s offered: %s" % (kernel, rate, out[-1]))
+        th = threading.Thread(target=waiter)
+        th.start()
+        t0 = time.perf_counter()
+        nxt = t0
+        total = 0
+        for s0, n, prm, gap in reqs:
+            nxt += gap
+            while time.perf_counter() < nxt:
+                pass
+            tickets.append(submit(s0, n, prm))
+            total += n
+        done.set()
+        th.join()
+        wall = time.perf_counter() - t0
+        lat_np = np.array(lat)
+        rec = {"offered_qps": rate, "achieved_qps": round(total / wall, 1), "requests": len(reqs),
+               "p50_ms": round(float(np.percentile(lat_np, 50)), 3),
+               "p99_ms": round(float(np.percentile(lat_np, 99)), 3)}
+        if check and hits[1]:
+            rec["recall_at_10"] = round(hits[0] / hits[1], 4)
+        out.append(rec)
+        log("served at %d q/s offered: %s" % (rate, rec))
     return out
+
+
+def served_latency(ix, queries, base, kth, rates, seconds, kernel=1, inflight=8, max_batch=512):
+    """The serving loop over the graph index under the mixed request stream: per
+    request k in {10 (3/4 of requests), 100}, epsilon in {0.02, 0.1, 0.2}; p50/p99 and
+    recall@10 (tie-aware, the first 10 results of each query) per offered rate."""
+    from ngt_gb300 import Server
+    rng = np.random.default_rng(43)
+    xt = None
+
+    def draw(r):
+        return (10 if r.random() < 0.75 else 100, float(r.choice([0.02, 0.1, 0.2])))
+
+    def check(s0, n, prm, ids, cnt):
+        d = np.sqrt(((base[np.maximum(ids[:, :10].astype(np.int64) - 1, 0)].astype(np.float64)
+                      - queries[s0:s0 + n, None, :].astype(np.float64)) ** 2).sum(2))
+        ok = (d <= kth[s0:s0 + n, None] + 1e-6) & (np.arange(10)[None, :] < np.minimum(cnt, 10)[:, None])
+        return int(ok.sum()), 10 * n
+
+    with Server(ix, max_batch=max_batch, inflight=inflight, max_k=128, kernel=kernel) as srv:
+        def warm():
+            t_ = [srv.submit(queries[i * 64:(i + 1) * 64], k=k_, epsilon=0.1)
+                  for i in range(2 * inflight) for k_ in (10, 100)]
+            for x in t_:
+                srv.wait(x)
+
+        return poisson_stream(lambda s0, n, prm: srv.submit(queries[s0:s0 + n], k=prm[0], epsilon=prm[1]),
+                              srv.wait, len(queries), rates, seconds, draw, rng, check, warm)
+
+
+def served_qbg(ix, q, k, probes_min, args, kth=None, x=None, ngt_q=0):
+    """The serving loop over the QBG index (two-step search with refinement, the
+    reference's CLI / ngtpy search) under the mixed request stream of the served QBG
+    configuration: k in {10, 100}, epsilon in {0.02, 0.1, 0.2}, probes in 8..64 (at
+    least the batched sweep's choice), Poisson arrivals at 1k-50k queries/s offered
+    (and beyond, to the saturation point)."""
+    from ngt_gb300 import QBGServer
+    rng = np.random.default_rng(44)
+    probe_set = [p for p in (8, 16, 32, 64) if p >= probes_min] or [64]
+
+    def draw(r):
+        return (10 if r.random() < 0.75 else 100, float(r.choice([0.02, 0.1, 0.2])), int(r.choice(probe_set)))
+
+    def check(s0, n, prm, ids, cnt):
+        if kth is None or s0 + n > ngt_q:
+            return 0, 0
+        import torch
+        idx = torch.from_numpy(np.maximum(ids[:, :10].astype(np.int64) - 1, 0)).cuda()
+        qq = torch.from_numpy(q[s0:s0 + n]).cuda()
+        d = ((x[idx] - qq[:, None, :]) ** 2).sum(2).sqrt().cpu().numpy()
+        ok = (d <= kth[s0:s0 + n, None] + 1e-6) & (np.arange(10)[None, :] < np.minimum(cnt, 10)[:, None])
+        return int(ok.sum()), 10 * n
+
+    with QBGServer(ix, max_batch=1024, inflight=4, max_k=128, two_step=True, refine=True) as srv:
+        def warm():
+            t_ = [srv.submit(q[i * 64:(i + 1) * 64], k=k_, result_expansion=2.0, explored_blobs=probe_set[0])
+                  for i in range(8) for k_ in (10, 100)]
+            for x_ in t_:
+                srv.wait(x_)
+
+        nqr = ngt_q if kth is not None else len(q)
+        return poisson_stream(lambda s0, n, prm: srv.submit(q[s0:s0 + n], k=prm[0], epsilon=prm[1],
+                                                             result_expansion=2.0, explored_blobs=prm[2]),
+                              srv.wait, nqr, [1000, 10000, 50000, 100000], args.served_seconds, draw, rng, check,
+                              warm)
 
 
 QG_EPS_SWEEP = [0.0, 0.02, 0.04, 0.06, 0.08, 0.1]
@@ -722,6 +794,130 @@ def precision_path(args, steps=None, warmup=None):
     }
 
 
+def qbg_workload(args, steps=None, warmup=None):
+    """The served quantized-blob-graph configuration: 10,000,000 x 128 uint8 objects
+    (clipped-exponential coordinates, seed 41; queries seed 42), a QBG index of 65,536
+    blobs with a rotation and 4-bit PQ over 64 two-dimensional subspaces, written by
+    ngt_gb300.qbg_build in the reference's format and opened with qbg_open_index.
+    The search is the reference's CLI / ngtpy one (searchInTwoSteps with a refinement
+    expansion: the probed blobs' 4-bit scans, then an exact uint8 L2 re-rank of k x
+    expansion candidates over the object list), k=10, the probe count the smallest of a
+    sweep whose recall@10 (tie-aware, exact ground truth) is >= 0.9.  The one-step
+    search of the C API (quantized distances) is reported beside it.  Queries resident
+    in HBM; the 1.3 GB object list and 0.4 GB of codes exceed L2, so no flush."""
+    import torch
+    from ngt_gb300 import QBGIndex
+    from ngt_gb300.base import QBG_REFINE, QBG_TWO_STEP, QUERY_STATS_DTYPE, RESULT_DTYPE
+    from ngt_gb300.qbg_build import build_qbg
+    from ngt_gb300.synthetic import clipped_exponential
+    n, d, nq, k = args.qbg_n, 128, args.nq, args.k
+    t0 = time.time()
+    x = clipped_exponential(n, d, seed=41).astype(np.uint8)
+    q = clipped_exponential(nq, d, seed=42)
+    path = os.path.join(args.workdir, "qbg_%d_%d_%d" % (n, d, args.qbg_blobs))
+    if not os.path.exists(os.path.join(path, "obj")):
+        build_qbg(path, x, nblobs=args.qbg_blobs, log=log)
+    log("qbg setup %.1f s" % (time.time() - t0))
+    # exact ground truth of the first queries (integer data: fp32 sums exact)
+    torch.backends.cuda.matmul.allow_tf32 = False
+    ngt_q = min(2000, nq)
+    X = torch.from_numpy(x).cuda().float()
+    xn = (X * X).sum(1)
+    kth = []
+    for s0 in range(0, ngt_q, 64):
+        qq = torch.from_numpy(q[s0:min(s0 + 64, ngt_q)]).cuda()
+        d2 = (qq * qq).sum(1, keepdim=True) + xn[None, :] - 2.0 * (qq @ X.T)
+        kth.append(torch.topk(d2, k, dim=1, largest=False).values[:, k - 1].clamp_min(0).sqrt().cpu())
+    kth = torch.cat(kth).numpy()
+
+    def recall_of(ids, cnt):
+        idx = torch.from_numpy(ids[:ngt_q].astype(np.int64) - 1).cuda().clamp_min(0)
+        qq = torch.from_numpy(q[:ngt_q]).cuda()
+        rows = X[idx]
+        dd = ((rows - qq[:, None, :]) ** 2).sum(2).sqrt().cpu().numpy()
+        valid = np.arange(k)[None, :] < cnt[:ngt_q, None]
+        return float(((dd <= kth[:, None] + 1e-6) & valid).sum() / (ngt_q * k))
+
+    ix = QBGIndex(path)
+    rows = np.zeros((nq, d), np.float32)
+    ok = ix._lib.ngtgpu_convert_queries_float(ix._index, np.ascontiguousarray(q).ctypes.data, nq, d,
+                                              rows.ctypes.data, ix._err)
+    ix._check(ok)
+    d_rows = torch.from_numpy(rows).cuda()
+    stream = torch.cuda.Stream()
+    out = {"workload": "QBG %d x %d uint8 L2, %d blobs, rotation + 4-bit PQ (64 two-dim subspaces), %d queries, k=%d"
+                       % (n, d, args.qbg_blobs, nq, k)}
+
+    def run(flags, probes, expansion, timed_steps, warm):
+        p = ix.params(k, 0.1, 0.0, expansion, probes, 0)
+        width = k if flags & QBG_REFINE else max(ix.result_size(p), 1)
+        res = torch.zeros((nq, width, 2), dtype=torch.int32, device="cuda")
+        cnt = torch.zeros(nq, dtype=torch.int32, device="cuda")
+        st = torch.zeros((nq, QUERY_STATS_DTYPE.itemsize // 4), dtype=torch.int32, device="cuda")
+
+        def step():
+            ix._check(ix._lib.qbg_gpu_search_batch_device(ix._index, d_rows.data_ptr(), nq, ctypes.byref(p), 1, flags,
+                                                          res.data_ptr(), width, cnt.data_ptr(), st.data_ptr(),
+                                                          stream.cuda_stream, ix._err))
+        for _ in range(warm):
+            step()
+        torch.cuda.synchronize()
+        times = []
+        with ClockSampler(0) as clocks:
+            for _ in range(timed_steps):
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                step()
+                e1.record(stream)
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1))
+        ms = statistics.median(times) if times else 0.0
+        ids = res[:, :k, 0].cpu().numpy().view(np.uint32)
+        c = np.minimum(cnt.cpu().numpy(), k)
+        stn = st.cpu().numpy()
+        return ms, recall_of(ids, c), stn, clocks.summary()
+
+    import ctypes
+    steps = steps or args.steps
+    warmup = max(3, warmup or args.warmup)
+    for name, flags, expansion in (("two_step_refined", QBG_TWO_STEP | QBG_REFINE, 2.0),
+                                   ("one_step_capi", 0, 3.0)):
+        sel = None
+        for probes in (8, 16, 32, 64, 128):
+            ms, r, stn, _ = run(flags, probes, expansion, 1, 1)
+            log("qbg %s probes %d: recall@%d %.4f, %.2f ms / %d queries" % (name, probes, k, r, ms, nq))
+            sel = (probes, r)
+            if r >= 0.9:
+                break
+        probes = sel[0]
+        ms, r, stn, clocks = run(flags, probes, expansion, steps, warmup)
+        scanned = float(stn[:, 0].mean())                   # objects scanned per query
+        blobs = float(stn[:, 2].mean())
+        # algorithmic bytes per query: ids + 4-bit codes of the scanned objects (4 + 32 B),
+        # the probed blob centroids' rows for the global search (~4 x probes visits x 512 B),
+        # the re-ranked uint8 rows (k x expansion x 128 B)
+        bytes_q = scanned * 36.0 + 4 * probes * 512.0 + (k * expansion * 128.0 if flags & QBG_REFINE else 0.0)
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))) if os.path.exists(
+            os.path.join(ROOT, "MEASURED_PEAKS.json")) else {}
+        peak = peaks.get("hbm_gbs", 6800.0)
+        achieved = bytes_q * nq / (ms * 1e-3) / 1e9
+        out[name] = {"qps": nq / (ms * 1e-3), "ms_per_step": ms, "probes_or_explored_blobs": probes,
+                     "expansion": expansion, "recall_at_k": r, "objects_scanned_per_query": scanned,
+                     "blobs_judged_per_query": blobs,
+                     "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                  "frac": achieved / peak, "basis": "36 B x objects scanned + 2 KB x probes + "
+                                                                    "128 B x re-ranked, per query"},
+                     "clocks": clocks}
+        log("qbg %s: %.0f q/s at %d probes, recall %.4f" % (name, nq / (ms * 1e-3), probes, r))
+    if args.served_seconds > 0:
+        out["served"] = served_qbg(ix, q, k, out["two_step_refined"]["probes_or_explored_blobs"], args, kth, X,
+                                   ngt_q)
+    ix.close()
+    del X
+    torch.cuda.empty_cache()
+    return out
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -731,6 +927,11 @@ def main():
         import torch
         torch.cuda.set_device(0)
         print(json.dumps(precision_path(args)), flush=True)
+        return
+    if args.qbg_only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(qbg_workload(args)), flush=True)
         return
     rank, world, local = dist_env()
     import torch
@@ -894,14 +1095,12 @@ def main():
     # ---- served: continuous batching under a Poisson request stream ------------------------------
     # the serving loop launches the CTA-per-query kernel (lowest latency per query); the
     # warp-per-query kernel's serving figures are reported beside it
-    served = served_warp = wide = None
-    if args.served_seconds > 0:
-        served_warp = served_latency(ix, queries, k, head["epsilon"], args.served_rates, args.served_seconds,
-                                     kernel=KERNEL_BATCHED)
-        ix.set_batched_tuning(list_capacity=256, parents=WIDE_PARENTS)
+    served = wide = None
+    if args.served_seconds > 0 and rank == 0:
+        ix.set_batched_tuning(list_capacity=0, parents=WIDE_PARENTS)
         wide = timed(KERNEL_WIDE, head["epsilon"])
         log("wide kernel: %.1f q/s at epsilon %g, recall %.4f" % (wide["qps"], wide["epsilon"], wide["recall"]))
-        served = served_latency(ix, queries, k, head["epsilon"], args.served_rates, args.served_seconds,
+        served = served_latency(ix, queries, base, kth, args.served_rates, args.served_seconds,
                                 kernel=KERNEL_WIDE, inflight=8, max_batch=512)
 
     # ---- quantized graph on the same index (rank 0) ---------------------------------------------
@@ -935,6 +1134,14 @@ def main():
         except Exception as ex:                 # reported, never fatal to the headline measurement
             pp = {"error": str(ex)}
             log("brute-force measurement failed: %s" % ex)
+    qbg = None
+    if args.qbg and rank == 0 and world == 1:
+        try:
+            qbg = qbg_workload(args, steps=max(3, args.steps // 3), warmup=args.warmup)
+            log("qbg: %s" % qbg)
+        except Exception as ex:                 # reported, never fatal to the headline measurement
+            qbg = {"error": str(ex)}
+            log("qbg measurement failed: %s" % ex)
 
     # ---- CPU baseline (oracle port on a bounded sample) ------------------------------------------
     cpu = None
@@ -980,15 +1187,17 @@ def main():
                          "basis": "(%d*DC + 4*edges + %d query + re-rank %d*2k) bytes per query over the kernel's "
                                   "median event time" % (head["row_bytes"], row_bytes, row_bytes)},
             "served": {"kernel": "CTA per query (%s search rows, rows of a step staged in shared memory), "
-                                 "%d parents per step; up to 8 launches of at most 512 queries in flight"
-                                 % (wide_rows, WIDE_PARENTS),
+                                 "%d parents per step; up to 8 launches of at most 512 queries in flight, "
+                                 "a launch holds requests of one shared-memory class" % (wide_rows, WIDE_PARENTS),
+                       "stream": "Poisson arrivals, request sizes geometric on 1..256 (mean ~16), k 10 (3/4) or "
+                                 "100, epsilon 0.02 / 0.1 / 0.2 per request",
                        "qps_10000_batch": round(wide["qps"], 1) if wide else None,
                        "recall_at_k": round(wide["recall"], 4) if wide else None,
-                       "rates": served,
-                       "warp_per_query_kernel_rates": served_warp} if served else None,
+                       "rates": served} if served else None,
             "quantized_graph": qg,
             "scalar_quantized": qs8,
             "brute_force_precision": pp,
+            "quantized_blob_graph": qbg,
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

@@ -193,6 +193,19 @@ bool qbg_gpu_search_batch_device(QBGIndex index, const void *d_rows, size_t nq, 
                                  size_t nparams, uint32_t flags, NGTObjectDistance *d_results, size_t kmax,
                                  uint32_t *d_counts, void *d_stats, void *stream, QBGError error);
 
+/* Extension: the serving loop of ngtgpu_server_create_ex over a QBG index.  Every
+ * request runs the search the flags above select (0: the C API's one-step search);
+ * up to `inflight` launches of up to max_batch_queries queries overlap on the
+ * device, each lane with scratch reserved at creation (and the object list loaded,
+ * with NGTGPU_QBG_REFINE).  Requests of 1..max_batch_queries queries with one
+ * parameter block or one per query; results up to max_k per query (with the
+ * refinement: number_of_results).  Returns an NGTGPUServer (ngtgpu.h): results are
+ * taken with ngtgpu_server_wait and the loop ends with ngtgpu_server_destroy. */
+void *ngtgpu_qbg_server_create(QBGIndex index, uint32_t max_batch_queries, uint32_t inflight, uint32_t max_k,
+                               uint32_t flags, QBGError error);
+int64_t ngtgpu_qbg_server_submit(void *server, const float *queries, size_t nq, int32_t dim,
+                                 const QBGQueryParameters *params, size_t nparams, QBGError error);
+
 #ifdef __cplusplus
 }
 #endif

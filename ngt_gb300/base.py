@@ -156,6 +156,9 @@ def load_library() -> ctypes.CDLL:
         "ngtgpu_server_wait": ([c_void_p, ctypes.c_int64, c_void_p, c_size_t, c_void_p, POINTER(ctypes.c_double),
                                 c_void_p], c_bool),
         "ngtgpu_server_destroy": ([c_void_p], None),
+        "ngtgpu_qbg_server_create": ([c_void_p, c_uint32, c_uint32, c_uint32, c_uint32, c_void_p], c_void_p),
+        "ngtgpu_qbg_server_submit": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QBGQueryParameters), c_size_t,
+                                      c_void_p], ctypes.c_int64),
         "ngtqg_open_index": ([c_char_p, c_void_p], c_void_p),
         "ngtqg_close_index": ([c_void_p], None),
         "ngtqg_initialize_query_parameters": ([POINTER(QGQueryParameters)], None),
@@ -584,6 +587,55 @@ class QBGIndex:
         return self
 
     def __exit__(self, *a):
+        self.close()
+
+
+class QBGServer:
+    """The continuous-batching serving loop over an open QBGIndex
+    (ngtgpu_qbg_server_*): every request runs the one-step search of the C API, or
+    with two_step / refine the reference's searchInTwoSteps / refinement."""
+
+    def __init__(self, index: "QBGIndex", max_batch: int = 1024, inflight: int = 3, max_k: int = 128,
+                 two_step: bool = False, refine: bool = False):
+        self._ix = index
+        self._lib = index._lib
+        self._err = self._lib.ngt_create_error_object()
+        flags = (QBG_TWO_STEP if two_step else 0) | (QBG_REFINE if refine else 0)
+        self._srv = self._lib.ngtgpu_qbg_server_create(index._index, max_batch, inflight, max_k, flags, self._err)
+        if not self._srv:
+            raise NativeError(self._lib.ngt_get_error_string(self._err).decode())
+        self.max_k = max_k
+        self._pending = {}
+
+    def submit(self, queries, k=20, epsilon=0.1, blob_epsilon=0.0, result_expansion=3.0, explored_blobs=256,
+               edges=0) -> int:
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        if q.ndim == 1:
+            q = q[None, :]
+        p = QBGIndex.params(k, epsilon, blob_epsilon, result_expansion, explored_blobs, edges)
+        t = self._lib.ngtgpu_qbg_server_submit(self._srv, q.ctypes.data, q.shape[0], q.shape[1], ctypes.byref(p), 1,
+                                               self._err)
+        if t < 0:
+            raise NativeError(self._lib.ngt_get_error_string(self._err).decode())
+        self._pending[t] = q.shape[0]
+        return t
+
+    def wait(self, ticket: int, kmax: int | None = None):
+        return Server.wait(self, ticket, kmax)
+
+    def close(self):
+        Server.close(self)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
         self.close()
 
 

@@ -194,6 +194,12 @@ GraphEngine::~GraphEngine() {
   cudaFree(d_qbg_ovf_);
   cudaFree(d_blob_dist_);
   cudaFree(d_olist_);
+  for (QbgScratch& q : qbg_scratch_) {
+    cudaFree(q.bitmaps);
+    cudaFree(q.exact_ovf);
+    cudaFree(q.qbg_ovf);
+    cudaFree(q.blob_dist);
+  }
   tc_release(tc_);
   if (stream_) cudaStreamDestroy(stream_);
 }
@@ -664,7 +670,8 @@ size_t GraphEngine::exact_launch_config(uint32_t max_size, ExactConfig& cfg) con
 
 void GraphEngine::launch_exact(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
                                uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats,
-                               cudaStream_t stream) {
+                               cudaStream_t stream, uint32_t* bitmaps, unsigned long long* overflow,
+                               size_t grid_cap) {
   ExactConfig cfg;
   const size_t smem = exact_launch_config(max_size, cfg);
   ExactKernelFn fn = exact_kernel(host_.prop.otype, host_.prop.metric);
@@ -673,9 +680,15 @@ void GraphEngine::launch_exact(const uint4* d_rows, size_t nq, const QueryParams
   NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kExactThreads, smem));
   NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
   size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
-  ensure_scratch(grid);
+  if (bitmaps) {
+    grid = std::min(grid, grid_cap);
+  } else {
+    ensure_scratch(grid);
+    bitmaps = d_bitmaps_;
+    overflow = d_overflow_;
+  }
   fn<<<(unsigned)grid, kExactThreads, smem, stream>>>(dev_, d_rows, (uint32_t)nq, d_params, d_seeds, d_out, d_counts,
-                                                       d_stats, d_bitmaps_, d_overflow_, cfg);
+                                                       d_stats, bitmaps, overflow, cfg);
   NGT_CUDA(cudaGetLastError());
   launches_++;
 }
@@ -1139,8 +1152,40 @@ void GraphEngine::ensure_object_list() {
   olist_uint8_ = gdt == 0;
 }
 
+GraphEngine::QbgScratch& GraphEngine::qbg_slot(size_t slot, size_t grid, cudaStream_t stream) {
+  if (slot >= qbg_scratch_.size()) qbg_scratch_.resize(slot + 1);
+  QbgScratch& q = qbg_scratch_[slot];
+  if (grid <= q.grid) return q;
+  NGT_CUDA(cudaStreamSynchronize(stream));     // earlier launches of this slot may still use the old buffers
+  cudaFree(q.bitmaps);
+  cudaFree(q.exact_ovf);
+  cudaFree(q.qbg_ovf);
+  cudaFree(q.blob_dist);
+  q = QbgScratch{};
+  const size_t words = (host_.nrows + 31) / 32;
+  const size_t qocap = std::min<size_t>(65536, 2 * (size_t)host_.nrows + 256);
+  NGT_CUDA(cudaMalloc(&q.bitmaps, grid * words * 4));
+  NGT_CUDA(cudaMemsetAsync(q.bitmaps, 0, grid * words * 4, stream));     // the kernels leave them clear
+  NGT_CUDA(cudaMalloc(&q.exact_ovf, grid * 2 * (size_t)kOverflowCapacity * 8));
+  NGT_CUDA(cudaMalloc(&q.qbg_ovf, grid * 4 * qocap * 8));
+  NGT_CUDA(cudaMalloc(&q.blob_dist, grid * (size_t)blob_cap_ * 4));
+  NGT_CUDA(cudaStreamSynchronize(stream));
+  q.grid = grid;
+  return q;
+}
+
+void GraphEngine::reserve_qbg_slot(size_t slot, size_t max_queries, cudaStream_t stream) {
+  std::lock_guard<std::mutex> lock(mu_);
+  NGT_CUDA(cudaSetDevice(device_));
+  int sms = 0;
+  NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+  // the largest grid any of the QBG kernels launches: one CTA per query, at most 16 per SM
+  qbg_slot(slot, std::min<size_t>(max_queries, (size_t)sms * 16), stream);
+}
+
 void GraphEngine::qbg_probe_blobs(const uint4* d_rows, size_t nq, const QBGArgs* args, size_t nargs,
-                                  ObjDist* d_blobs, uint32_t* d_bcounts, size_t bstride, cudaStream_t stream) {
+                                  ObjDist* d_blobs, uint32_t* d_bcounts, size_t bstride, cudaStream_t stream,
+                                  size_t slot) {
   // searchInTwoSteps' global search (QuantizedBlobGraph.h:1224-1237): NGT::Index::search
   // of the read-only global index with size = the probes, epsilon = (1 + blob_epsilon) - 1
   // and the index's own edge size
@@ -1166,12 +1211,17 @@ void GraphEngine::qbg_probe_blobs(const uint4* d_rows, size_t nq, const QBGArgs*
     NGT_CUDA(cudaMallocAsync(&d_st, nq * sizeof(QueryStats), stream));
     NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QueryParams), cudaMemcpyHostToDevice, stream));
     NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, stream));
-    launch_exact(d_rows, nq, d_params, d_seeds, max_size, d_blobs, d_bcounts, d_st, stream);
+    if (slot == 0) {
+      launch_exact(d_rows, nq, d_params, d_seeds, max_size, d_blobs, d_bcounts, d_st, stream);
+    } else {
+      QbgScratch& q = qbg_scratch_.at(slot);
+      launch_exact(d_rows, nq, d_params, d_seeds, max_size, d_blobs, d_bcounts, d_st, stream, q.bitmaps,
+                   q.exact_ovf, q.grid);
+    }
+    // (the copies above read pageable host memory: staged before they return)
     NGT_CUDA(cudaFreeAsync(d_params, stream));
     NGT_CUDA(cudaFreeAsync(d_seeds, stream));
     NGT_CUDA(cudaFreeAsync(d_st, stream));
-    // the host parameter vectors must outlive the copies above
-    NGT_CUDA(cudaStreamSynchronize(stream));
   } catch (...) {
     mode_ = saved;
     throw;
@@ -1181,7 +1231,7 @@ void GraphEngine::qbg_probe_blobs(const uint4* d_rows, size_t nq, const QBGArgs*
 
 void GraphEngine::qbg_search_device(const uint4* d_rows, size_t nq, const QBGArgs* args, size_t nargs,
                                     ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, size_t kmax,
-                                    cudaStream_t stream) {
+                                    cudaStream_t stream, size_t slot) {
   if (!qbg_loaded_) throw std::runtime_error("not a QBG index");
   std::lock_guard<std::mutex> lock(mu_);
   NGT_CUDA(cudaSetDevice(device_));
@@ -1272,7 +1322,7 @@ void GraphEngine::qbg_search_device(const uint4* d_rows, size_t nq, const QBGArg
     uint32_t* d_bcounts = nullptr;
     NGT_CUDA(cudaMallocAsync(&d_blobs, nq * max_probes * sizeof(ObjDist), stream));
     NGT_CUDA(cudaMallocAsync(&d_bcounts, nq * 4, stream));
-    qbg_probe_blobs(d_rows, nq, args, nargs, d_blobs, d_bcounts, max_probes, stream);
+    qbg_probe_blobs(d_rows, nq, args, nargs, d_blobs, d_bcounts, max_probes, stream, slot);
     QBGScanKernelFn fn = qbg_scan_kernel_for(qb_.m);
     if (!fn) throw std::runtime_error("too many subspaces in the QBG index");
     const size_t smem = qbg_scan_kernel_smem_bytes(dev_.row_chunks, qb_.dim, qb_.m, max_size);
@@ -1280,11 +1330,19 @@ void GraphEngine::qbg_search_device(const uint4* d_rows, size_t nq, const QBGArg
     NGT_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kExactThreads, smem));
-    const size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
-    ensure_blob_dist(grid, qbg_ocap_);
+    size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
+    float* bdist = nullptr;
+    if (slot == 0) {
+      ensure_blob_dist(grid, qbg_ocap_);
+      bdist = d_blob_dist_;
+    } else {
+      QbgScratch& q = qbg_scratch_.at(slot);
+      grid = std::min(grid, q.grid);
+      bdist = q.blob_dist;
+    }
     fn<<<(unsigned)grid, kExactThreads, smem, stream>>>(dqb_, d_blob_sid_, d_rows, dev_.row_chunks, (uint32_t)nq,
                                                          d_params, d_blobs, d_bcounts, (uint32_t)max_probes, d_sout,
-                                                         d_scount, d_stats, d_blob_dist_, blob_cap_, max_size);
+                                                         d_scount, d_stats, bdist, blob_cap_, max_size);
     NGT_CUDA(cudaGetLastError());
     launches_++;
     NGT_CUDA(cudaFreeAsync(d_blobs, stream));
@@ -1308,11 +1366,25 @@ void GraphEngine::qbg_search_device(const uint4* d_rows, size_t nq, const QBGArg
     int per_sm = 0;
     NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kExactThreads, smem));
     size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
-    ensure_scratch(grid);
-    ensure_blob_dist(grid, cfg.ocap);
+    uint32_t* bitmaps = nullptr;
+    unsigned long long* qovf = nullptr;
+    float* bdist = nullptr;
+    if (slot == 0) {
+      ensure_scratch(grid);
+      ensure_blob_dist(grid, cfg.ocap);
+      bitmaps = d_bitmaps_;
+      qovf = d_qbg_ovf_;
+      bdist = d_blob_dist_;
+    } else {
+      QbgScratch& q = qbg_scratch_.at(slot);
+      grid = std::min(grid, q.grid);
+      bitmaps = q.bitmaps;
+      qovf = q.qbg_ovf;
+      bdist = q.blob_dist;
+    }
     fn<<<(unsigned)grid, kExactThreads, smem, stream>>>(dev_, dqb_, d_blob_sid_, d_rows, (uint32_t)nq, d_params,
-                                                         d_seeds, d_sout, d_scount, d_stats, d_bitmaps_, d_qbg_ovf_,
-                                                         d_blob_dist_, cfg);
+                                                         d_seeds, d_sout, d_scount, d_stats, bitmaps, qovf, bdist,
+                                                         cfg);
     NGT_CUDA(cudaGetLastError());
     launches_++;
   }
@@ -1335,10 +1407,9 @@ void GraphEngine::qbg_search_device(const uint4* d_rows, size_t nq, const QBGArg
     NGT_CUDA(cudaFreeAsync(d_sout, stream));
     NGT_CUDA(cudaFreeAsync(d_scount, stream));
   }
+  // (the host vectors were read by copies from pageable memory, staged before they returned)
   NGT_CUDA(cudaFreeAsync(d_params, stream));
   NGT_CUDA(cudaFreeAsync(d_seeds, stream));
-  // the host vectors (parameters, exact sizes) must outlive the copies above
-  NGT_CUDA(cudaStreamSynchronize(stream));
 }
 
 void GraphEngine::qbg_search(const void* queries, QueryType qt, size_t nq, size_t qdim, const QBGArgs* args,

@@ -131,8 +131,17 @@ class GraphEngine {
   // size x result_expansion of them when the expansion is >= 1.
   void qbg_search(const void* queries, QueryType qt, size_t nq, size_t qdim, const QBGArgs* args, size_t nargs,
                   SearchOutput& out);
+  // slot 0: the engine's own scratch; slot >= 1: scratch set `slot`, reserved by
+  // reserve_qbg_slot (the serving loop's lanes, whose launches overlap)
+  void reserve_qbg_slot(size_t slot, size_t max_queries, cudaStream_t stream);
+  // loads the QBG object list the refinement reads (done on the first refined search)
+  void prepare_refinement() {
+    std::lock_guard<std::mutex> lock(mu_);
+    ensure_object_list();
+  }
   void qbg_search_device(const uint4* d_rows, size_t nq, const QBGArgs* args, size_t nargs, ObjDist* d_out,
-                         uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream);
+                         uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream,
+                         size_t slot = 0);
   bool is_qbg() const { return qbg_loaded_; }
   uint32_t qbg_genuine_dimension() const { return qbg_genuine_dim_; }
   // results the blob search keeps, and results returned
@@ -251,8 +260,10 @@ class GraphEngine {
   // search rows the wide kernel uses for this index and tuning
   SearchRows wide_search_rows();
  private:
+  // bitmaps / overflow: a caller's scratch for `grid_cap` CTAs (nullptr: the engine's own)
   void launch_exact(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
-                    uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, cudaStream_t stream);
+                    uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, cudaStream_t stream,
+                    uint32_t* bitmaps = nullptr, unsigned long long* overflow = nullptr, size_t grid_cap = 0);
   void launch_fast(const uint4* d_rows, size_t nq, const QueryParams* d_params, const uint32_t* d_seeds,
                    uint32_t max_size, ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, cudaStream_t stream,
                    Kernel kernel, FastScratch& scratch);
@@ -281,7 +292,18 @@ class GraphEngine {
   void ensure_object_list();
   // the global index's read-only graph search for the two-step search (mu_ held)
   void qbg_probe_blobs(const uint4* d_rows, size_t nq, const QBGArgs* args, size_t nargs, ObjDist* d_blobs,
-                       uint32_t* d_bcounts, size_t bstride, cudaStream_t stream);
+                       uint32_t* d_bcounts, size_t bstride, cudaStream_t stream, size_t slot);
+  // per-slot scratch of the QBG searches: the exact kernel's (probe search) visited
+  // bitmaps and overflow tiers, the one-step kernel's queue overflow, the blob distances
+  struct QbgScratch {
+    uint32_t* bitmaps = nullptr;
+    unsigned long long* exact_ovf = nullptr;
+    unsigned long long* qbg_ovf = nullptr;
+    float* blob_dist = nullptr;
+    size_t grid = 0;
+  };
+  std::vector<QbgScratch> qbg_scratch_;
+  QbgScratch& qbg_slot(size_t slot, size_t grid, cudaStream_t stream);
   size_t qbg_grid_ = 0;
   uint32_t qbg_ocap_ = 0;
   // quantized graph

@@ -13,6 +13,21 @@
 // A request's results depend only on its queries and parameters (the batched
 // kernel handles every query independently), so they are the same alone and
 // in any mix.
+//
+// Admission follows each request's footprint.  Scratch memory (visited bitmaps,
+// spill tiers, queue overflows, blob distances) is reserved per lane for
+// max_batch queries when the server starts, so a launch admits queries up to that
+// count and nothing is allocated while serving.  Shared memory per CTA grows with
+// a request's result size (the candidate list of the graph kernels, the result
+// set and sort width of the QBG kernels), and a launch runs with the largest one
+// it holds; so requests are grouped by that class: a launch takes the oldest
+// waiting request and, in arrival order, the waiting requests of the same class
+// that fit -- a small-k request never runs at a large-k request's occupancy, and
+// the oldest request always goes first (no starvation).
+//
+// The same loop serves quantized-blob-graph indexes (qbg_* handles): one-step or
+// two-step searches, optionally refined, with per-lane scratch sets so that the
+// launches overlap.
 #include <cuda_runtime.h>
 
 #include <atomic>
@@ -33,6 +48,7 @@
 
 extern "C" {
 #include "../../include/ngtgpu.h"
+#include "../../include/ngtq_capi.h"
 }
 
 namespace ngtg {
@@ -52,7 +68,9 @@ struct Request {
   int64_t ticket = 0;
   std::vector<uint8_t> rows;          // converted query rows
   size_t nq = 0;
-  std::vector<SearchArgs> args;       // 1 or nq entries
+  std::vector<SearchArgs> args;       // 1 or nq entries (graph search)
+  std::vector<QBGArgs> qargs;         // 1 or nq entries (quantized blob graph)
+  uint32_t cls = 0;                   // shared-memory class (admission groups a launch by it)
   size_t kmax = 0;
   Clock::time_point arrival;
   std::vector<ObjDist> results;       // nq * kmax
@@ -80,12 +98,23 @@ struct Lane {
 
 }  // namespace
 
+// Shared-memory class of a result size: powers of two from 16 (sizes up to 16 share one).
+uint32_t size_class(size_t size) {
+  uint32_t c = 0;
+  while (c < 31 && ((size_t)16 << c) < size) c++;
+  return c;
+}
+
 class Server {
  public:
-  Server(GraphEngine* e, size_t max_batch, size_t inflight, size_t max_k, Kernel kernel = Kernel::Fast)
-      : e_(e), max_batch_(max_batch), max_k_(max_k), row_bytes_(e->host().row_bytes()), kernel_(kernel) {
+  Server(GraphEngine* e, size_t max_batch, size_t inflight, size_t max_k, Kernel kernel = Kernel::Fast,
+         bool qbg = false, uint32_t qbg_flags = 0)
+      : e_(e), max_batch_(max_batch), max_k_(max_k), row_bytes_(e->host().row_bytes()), kernel_(kernel), qbg_(qbg),
+        qbg_flags_(qbg_flags) {
     if (max_batch == 0 || inflight == 0 || max_k == 0) throw std::runtime_error("invalid server sizes");
+    if (qbg && !e->is_qbg()) throw std::runtime_error("not a QBG index");
     SRV_CUDA(cudaSetDevice(e->device()));
+    if (qbg && (qbg_flags & 2u)) e->prepare_refinement();
     e->reserve_scratch_sets(inflight + 1);
     lanes_.resize(inflight);
     for (size_t i = 0; i < inflight; i++) {
@@ -102,7 +131,8 @@ class Server {
       SRV_CUDA(cudaMallocHost(&l.h_counts, max_batch * 4));
       // a launch uses at most one scratch slot per query (plus the rounding of its
       // last CTA's warps): no reallocation while serving
-      e->reserve_scratch_slots(l.slot, max_batch + 8);
+      if (qbg) e->reserve_qbg_slot(l.slot, max_batch, l.stream);
+      else e->reserve_scratch_slots(l.slot, max_batch + 8);
     }
     worker_ = std::thread([this] { run(); });
   }
@@ -130,6 +160,7 @@ class Server {
   }
 
   int64_t submit(const float* queries, size_t nq, size_t dim, const SearchArgs* args, size_t nargs) {
+    if (qbg_) throw std::runtime_error("this server serves a QBG index: submit QBG parameters");
     if (nq == 0 || nq > max_batch_)
       throw std::runtime_error("request size must be 1.." + std::to_string(max_batch_) + " queries");
     if (!(nargs == 1 || nargs == nq)) throw std::runtime_error("parameters must be 1 or one per query");
@@ -137,10 +168,47 @@ class Server {
     e_->convert_queries(queries, QueryType::Float32, nq, dim, r->rows);
     r->nq = nq;
     r->args.assign(args, args + nargs);
-    size_t kmax = 1;
-    for (const auto& a : r->args) kmax = std::max(kmax, e_->output_size(a));
+    size_t kmax = 1, smax = 1;
+    for (const auto& a : r->args) {
+      kmax = std::max(kmax, e_->output_size(a));
+      smax = std::max(smax, a.size);
+    }
     if (kmax > max_k_) throw std::runtime_error("result size above the server's maximum " + std::to_string(max_k_));
     r->kmax = kmax;
+    r->cls = size_class(smax);
+    return enqueue(r);
+  }
+
+  int64_t submit_qbg(const float* queries, size_t nq, size_t dim, const QBGArgs* args, size_t nargs) {
+    if (!qbg_) throw std::runtime_error("this server serves a graph index: submit graph parameters");
+    if (nq == 0 || nq > max_batch_)
+      throw std::runtime_error("request size must be 1.." + std::to_string(max_batch_) + " queries");
+    if (!(nargs == 1 || nargs == nq)) throw std::runtime_error("parameters must be 1 or one per query");
+    if (dim != e_->qbg_genuine_dimension())
+      throw std::runtime_error("the query dimension differs from the index dimension");
+    auto r = std::make_shared<Request>();
+    // the query zero-padded to the global index dimension, as the QBG searches resize it
+    const size_t gd = e_->host().dim;
+    std::vector<float> padded(nq * gd, 0.f);
+    for (size_t q = 0; q < nq; q++) std::memcpy(padded.data() + q * gd, queries + q * dim, dim * sizeof(float));
+    e_->convert_queries(padded.data(), QueryType::Float32, nq, gd, r->rows);
+    r->nq = nq;
+    r->qargs.assign(args, args + nargs);
+    size_t kmax = 1, smax = 1;
+    for (auto& a : r->qargs) {
+      a.two_step = (qbg_flags_ & 1u) != 0;
+      a.refine = (qbg_flags_ & 2u) != 0;
+      kmax = std::max(kmax, GraphEngine::qbg_result_size(a));
+      smax = std::max(smax, GraphEngine::qbg_search_size(a));
+    }
+    if (kmax > max_k_) throw std::runtime_error("result size above the server's maximum " + std::to_string(max_k_));
+    if (smax > 4096) throw std::runtime_error("number_of_results x result_expansion above 4096");
+    r->kmax = kmax;
+    r->cls = size_class(smax);
+    return enqueue(r);
+  }
+
+  int64_t enqueue(const std::shared_ptr<Request>& r) {
     r->arrival = Clock::now();
     std::lock_guard<std::mutex> lock(mu_);
     r->ticket = next_ticket_++;
@@ -192,11 +260,18 @@ class Server {
         for (Lane& l : lanes_)
           if (!l.busy) { free_lane = &l; break; }
         if (free_lane && !pending_.empty()) {
+          // the oldest request, and then in arrival order the waiting requests of its
+          // shared-memory class that fit the lane's query capacity
+          const uint32_t cls = pending_.front()->cls;
           size_t total = 0;
-          while (!pending_.empty() && total + pending_.front()->nq <= max_batch_) {
-            total += pending_.front()->nq;
-            batch.push_back(pending_.front());
-            pending_.pop_front();
+          for (auto it = pending_.begin(); it != pending_.end();) {
+            if ((*it)->cls == cls && total + (*it)->nq <= max_batch_) {
+              total += (*it)->nq;
+              batch.push_back(*it);
+              it = pending_.erase(it);
+            } else {
+              ++it;
+            }
           }
         } else if (!any_busy) {
           cv_.wait_for(lock, std::chrono::milliseconds(2), [&] { return stop_ || !pending_.empty(); });
@@ -216,16 +291,24 @@ class Server {
     l.kmax = 1;
     size_t nq = 0;
     std::vector<SearchArgs> args;
+    std::vector<QBGArgs> qargs;
     for (auto& r : batch) {
       std::memcpy(l.h_rows + nq * row_bytes_, r->rows.data(), r->nq * row_bytes_);
-      for (size_t q = 0; q < r->nq; q++) args.push_back(r->args[r->args.size() == 1 ? 0 : q]);
+      for (size_t q = 0; q < r->nq; q++) {
+        if (qbg_) qargs.push_back(r->qargs[r->qargs.size() == 1 ? 0 : q]);
+        else args.push_back(r->args[r->args.size() == 1 ? 0 : q]);
+      }
       nq += r->nq;
       l.kmax = std::max(l.kmax, r->kmax);
     }
     try {
       SRV_CUDA(cudaMemcpyAsync(l.d_rows, l.h_rows, nq * row_bytes_, cudaMemcpyHostToDevice, l.stream));
-      e_->search_device_slot(l.d_rows, nq, args.data(), args.size(), l.d_out, l.d_counts, l.d_stats, l.kmax,
-                             l.stream, l.slot, kernel_);
+      if (qbg_)
+        e_->qbg_search_device(l.d_rows, nq, qargs.data(), qargs.size(), l.d_out, l.d_counts, l.d_stats, l.kmax,
+                              l.stream, l.slot);
+      else
+        e_->search_device_slot(l.d_rows, nq, args.data(), args.size(), l.d_out, l.d_counts, l.d_stats, l.kmax,
+                               l.stream, l.slot, kernel_);
       SRV_CUDA(cudaMemcpyAsync(l.h_out, l.d_out, nq * l.kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, l.stream));
       SRV_CUDA(cudaMemcpyAsync(l.h_counts, l.d_counts, nq * 4, cudaMemcpyDeviceToHost, l.stream));
       SRV_CUDA(cudaEventRecord(l.done_event, l.stream));
@@ -266,6 +349,8 @@ class Server {
   GraphEngine* e_;
   size_t max_batch_, max_k_, row_bytes_;
   Kernel kernel_;
+  bool qbg_ = false;
+  uint32_t qbg_flags_ = 0;
   std::vector<Lane> lanes_;
   std::deque<std::shared_ptr<Request>> pending_;
   std::map<int64_t, std::shared_ptr<Request>> tickets_;
@@ -354,5 +439,43 @@ bool ngtgpu_server_wait(NGTGPUServer server, int64_t ticket, NGTObjectDistance* 
 }
 
 void ngtgpu_server_destroy(NGTGPUServer server) { delete static_cast<ngtg::Server*>(server); }
+
+void* ngtgpu_qbg_server_create(QBGIndex index, uint32_t max_batch_queries, uint32_t inflight, uint32_t max_k,
+                                      uint32_t flags, NGTError error) {
+  if (index == nullptr || (flags & ~(NGTGPU_QBG_TWO_STEP | NGTGPU_QBG_REFINE)) != 0) {
+    server_error(__FUNCTION__, "parametor error: index is NULL or unknown flags", error);
+    return nullptr;
+  }
+  try {
+    return new ngtg::Server(static_cast<ngtg::GraphEngine*>(index), max_batch_queries, inflight, max_k,
+                            ngtg::Kernel::Exact, true, flags);
+  } catch (std::exception& ex) {
+    server_error(__FUNCTION__, ex.what(), error);
+    return nullptr;
+  }
+}
+
+int64_t ngtgpu_qbg_server_submit(void* server, const float* queries, size_t nq, int32_t dim,
+                                 const QBGQueryParameters* params, size_t nparams, NGTError error) {
+  if (server == nullptr || queries == nullptr || params == nullptr || dim <= 0) {
+    server_error(__FUNCTION__, "parametor error: server, queries or params", error);
+    return -1;
+  }
+  try {
+    std::vector<ngtg::QBGArgs> a(nparams);
+    for (size_t i = 0; i < nparams; i++) {
+      a[i].size = params[i].number_of_results;
+      a[i].epsilon = params[i].epsilon;
+      a[i].blob_epsilon = params[i].blob_epsilon;
+      a[i].result_expansion = params[i].result_expansion;
+      a[i].explored_blobs = params[i].number_of_explored_blobs;
+      a[i].edges = params[i].number_of_edges;
+    }
+    return static_cast<ngtg::Server*>(server)->submit_qbg(queries, nq, (size_t)dim, a.data(), a.size());
+  } catch (std::exception& ex) {
+    server_error(__FUNCTION__, ex.what(), error);
+    return -1;
+  }
+}
 
 }  // extern "C"

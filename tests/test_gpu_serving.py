@@ -33,10 +33,10 @@ def test_results_in_the_mix_equal_results_alone(index_path, kernel):
         n = int(rng.integers(1, 48))
         q = queries[start % 900: start % 900 + n]
         start += n
-        reqs.append((q, int(rng.choice([5, 10, 20])), float(rng.choice([0.05, 0.1, 0.15]))))
+        reqs.append((q, int(rng.choice([5, 10, 20, 100])), float(rng.choice([0.02, 0.05, 0.1, 0.15, 0.2]))))
     with Index(path, read_only=True) as ix:
         alone = [ix.batch_search(q, k=k, epsilon=e, kernel=kernel) for q, k, e in reqs]
-        with Server(ix, max_batch=256, inflight=3, max_k=64, kernel=kernel) as srv:
+        with Server(ix, max_batch=256, inflight=3, max_k=128, kernel=kernel) as srv:
             tickets = [None] * len(reqs)
 
             def submitter(part):
@@ -71,3 +71,43 @@ def test_server_rejects_bad_requests(index_path):
             t = srv.submit(queries[:4], k=10)
             ids, ds, n, lat = srv.wait(t)
             assert (n == 10).all()
+
+
+@pytest.mark.parametrize("two_step,refine", [(False, False), (True, True), (False, True)])
+def test_qbg_results_in_the_mix_equal_results_alone(tmp_path, two_step, refine):
+    """The serving loop over a QBG index: requests with different k, epsilon, blob
+    epsilon, expansion and explored blobs / probes, submitted from several threads
+    while others run, each equal to the same queries searched alone."""
+    from ngt_gb300 import QBGIndex, QBGServer
+    path, meta, queries, golden = materialize("qbg_u8_l2_d64", str(tmp_path))
+    rng = np.random.default_rng(11)
+    reqs = []
+    for _ in range(40):
+        n = int(rng.integers(1, 24))
+        s0 = int(rng.integers(0, len(queries) - n))
+        reqs.append((queries[s0:s0 + n], int(rng.choice([5, 10, 20])), float(rng.choice([0.02, 0.1, 0.2])),
+                     float(rng.choice([0.0, 0.05])), float(rng.choice([1.0, 2.0, 3.0])), int(rng.choice([8, 16, 32]))))
+    with QBGIndex(path) as ix:
+        alone = [ix.batch_search(q, k=k, epsilon=e, blob_epsilon=b, result_expansion=x, explored_blobs=p,
+                                 two_step=two_step, refine=refine) for q, k, e, b, x, p in reqs]
+        with QBGServer(ix, max_batch=128, inflight=3, max_k=64, two_step=two_step, refine=refine) as srv:
+            tickets = [None] * len(reqs)
+
+            def submitter(part):
+                for i in part:
+                    q, k, e, b, x, p = reqs[i]
+                    tickets[i] = srv.submit(q, k=k, epsilon=e, blob_epsilon=b, result_expansion=x, explored_blobs=p)
+
+            threads = [threading.Thread(target=submitter, args=(range(t, len(reqs), 3),)) for t in range(3)]
+            for t in threads:
+                t.start()
+            for t in threads:
+                t.join()
+            for i in range(len(reqs)):
+                ids, ds, n, lat = srv.wait(tickets[i])
+                ai, ad, an = alone[i]
+                assert np.array_equal(n, an), i
+                for j in range(len(n)):
+                    assert np.array_equal(ids[j, :n[j]], ai[j, :an[j]]), (i, j)
+                    assert np.array_equal(ds[j, :n[j]].view(np.uint32), ad[j, :an[j]].view(np.uint32)), (i, j)
+                assert lat > 0.0
