@@ -331,9 +331,10 @@ def served_latency(ix, queries, base, kth, rates, seconds, kernel=1, inflight=8,
         return (10 if r.random() < 0.75 else 100, float(r.choice([0.02, 0.1, 0.2])))
 
     def check(s0, n, prm, ids, cnt):
-        d = np.sqrt(((base[np.maximum(ids[:, :10].astype(np.int64) - 1, 0)].astype(np.float64)
-                      - queries[s0:s0 + n, None, :].astype(np.float64)) ** 2).sum(2))
-        ok = (d <= kth[s0:s0 + n, None] + 1e-6) & (np.arange(10)[None, :] < np.minimum(cnt, 10)[:, None])
+        # kth holds the k-th exact squared distance
+        d2 = ((base[np.maximum(ids[:, :10].astype(np.int64) - 1, 0)].astype(np.float64)
+               - queries[s0:s0 + n, None, :].astype(np.float64)) ** 2).sum(2)
+        ok = (d2 <= kth[s0:s0 + n, None]) & (np.arange(10)[None, :] < np.minimum(cnt, 10)[:, None])
         return int(ok.sum()), 10 * n
 
     with Server(ix, max_batch=max_batch, inflight=inflight, max_k=128, kernel=kernel) as srv:
@@ -918,6 +919,46 @@ def qbg_workload(args, steps=None, warmup=None):
     return out
 
 
+def single_query_capi(ix, queries, base, kth, k, eps, threads=16, sample=4000):
+    """ngt_search_index_as_float, one query per call, from `threads` host threads at
+    once (the OpenMP loop of ngtpy's batch_search): the library coalesces the calls
+    that arrive while a launch runs into the next exact-kernel launch.  Wall-clock
+    queries/s over `sample` queries, the one-thread latency, and recall@k."""
+    import threading
+    q = queries[:sample]
+    got = [None] * len(q)
+
+    def worker(part):
+        for j in part:
+            got[j] = ix.search(q[j], k=k, epsilon=eps)
+
+    for j in range(32):                         # warm-up: seed tables, kernels loaded
+        ix.search(q[j], k=k, epsilon=eps)
+    q0, l0 = ix.coalescing_stats()
+    ths = [threading.Thread(target=worker, args=(range(t, len(q), threads),)) for t in range(threads)]
+    t0 = time.perf_counter()
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    wall = time.perf_counter() - t0
+    q1, l1 = ix.coalescing_stats()
+    lat = []
+    for j in range(50):
+        t = time.perf_counter()
+        ix.search(q[j], k=k, epsilon=eps)
+        lat.append(time.perf_counter() - t)
+    ids = np.zeros((len(q), k), np.uint32)
+    cnt = np.zeros(len(q), np.uint32)
+    for j, r in enumerate(got):
+        cnt[j] = len(r)
+        ids[j, :len(r)] = [o.id for o in r]
+    return {"qps": round(len(q) / wall, 1), "threads": threads, "queries": len(q), "epsilon": eps,
+            "queries_per_launch": round((q1 - q0) / max(1, l1 - l0), 1),
+            "one_thread_latency_ms": round(1e3 * statistics.median(lat), 3),
+            "recall_at_k": round(recall(base, q, ids, cnt, kth[:len(q)], k), 4)}
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -1148,6 +1189,15 @@ def main():
     if rank == 0:
         cpu = cpu_baseline(path, queries, plain["epsilon"], k, args.cpu_sample, os.cpu_count() or 1)
 
+    # ---- the drop-in single-query call from many host threads -----------------------------------
+    single = None
+    if rank == 0:
+        try:
+            single = single_query_capi(ix, queries, base, kth, k, plain["epsilon"])
+            log("single-query C API: %s" % single)
+        except Exception as ex:                 # reported, never fatal to the headline measurement
+            single = {"error": str(ex)}
+
     head_rows = wide_rows if head["config"]["kernel"] == KERNEL_WIDE else "bf16"
     rows_text = ("8-bit (lossless: the objects' coordinates are 8-bit integers)" if head_rows == "u8"
                  else head_rows)
@@ -1198,6 +1248,7 @@ def main():
             "scalar_quantized": qs8,
             "brute_force_precision": pp,
             "quantized_blob_graph": qbg,
+            "single_query_capi": single,
             "cpu_baseline": cpu,
             "e2e": {"value": round(e2e_qps, 1), "unit": "queries/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},

@@ -197,6 +197,14 @@ bool ngtgpu_server_wait(NGTGPUServer, int64_t ticket, NGTObjectDistance *results
                         double *latency_ms, NGTError);
 void ngtgpu_server_destroy(NGTGPUServer);
 
+/* The single-query graph searches (ngt_search_index, _as_float, _as_uint8,
+ * _as_float16, _with_query*) of concurrent host threads are coalesced: the first
+ * caller launches the exact-order kernel at once, callers arriving while a launch
+ * runs wait and are launched together by the next of them, so a loop of these calls
+ * over many threads (ngtpy's batch_search pattern) fills the GPU.  Every result equals
+ * a lone call's.  The queries coalesced so far, and the launches they took. */
+bool ngtgpu_coalescing_stats(NGTIndex, uint64_t *queries, uint64_t *launches, NGTError);
+
 /* Number of kernel launches issued by this index since it was opened. */
 uint64_t ngtgpu_kernel_launches(NGTIndex, NGTError);
 

@@ -145,6 +145,7 @@ def load_library() -> ctypes.CDLL:
         "ngtgpu_set_tc_first_rows": ([c_void_p, c_size_t, c_void_p], c_bool),
         "ngtgpu_tc_phase_times": ([c_void_p, c_void_p, c_void_p], c_bool),
         "ngtgpu_kernel_launches": ([c_void_p, c_void_p], c_uint64),
+        "ngtgpu_coalescing_stats": ([c_void_p, c_void_p, c_void_p, c_void_p], c_bool),
         "ngtgpu_get_wide_search_rows": ([c_void_p, c_void_p], c_uint32),
         "ngtgpu_set_batched_tuning": ([c_void_p, c_uint32, c_uint32, c_float, c_void_p], c_bool),
         "ngtgpu_set_batched_rows_in_flight": ([c_void_p, c_uint32, c_void_p], c_bool),
@@ -350,6 +351,12 @@ class Index:
 
     def kernel_launches(self) -> int:
         return int(self._lib.ngtgpu_kernel_launches(self._index, self._err))
+
+    def coalescing_stats(self):
+        """(queries, launches) of the coalesced single-query calls so far."""
+        q, n = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        self._check(self._lib.ngtgpu_coalescing_stats(self._index, ctypes.byref(q), ctypes.byref(n), self._err))
+        return int(q.value), int(n.value)
 
     def wide_search_rows(self) -> str:
         """Search rows of the CTA-per-query kernel: "native", "bf16" or "u8"."""

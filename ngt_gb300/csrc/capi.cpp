@@ -89,7 +89,7 @@ bool search_common(NGTIndex index, const void* query, QueryType qt, int32_t dim,
                    float radius, int64_t edge_size, NGTObjectDistances results) {
   SearchArgs a = make_args(size, epsilon, radius, edge_size);
   SearchOutput out;
-  engine(index)->search(query, qt, 1, (size_t)dim, &a, 1, out);
+  engine(index)->search_one(query, qt, (size_t)dim, a, out);
   fill_results(out, 0, results);
   return true;
 }
@@ -540,6 +540,16 @@ bool ngtgpu_tc_scores_device(NGTIndex index, const void* d_rows, size_t nq, floa
     return true;
   }
   CAPI_CATCH(error, false)
+}
+
+bool ngtgpu_coalescing_stats(NGTIndex index, uint64_t* queries, uint64_t* launches, NGTError error) {
+  if (index == nullptr || queries == nullptr || launches == nullptr) {
+    CAPI_PARAM_ERROR(error, "index = " << index);
+    return false;
+  }
+  *queries = engine(index)->coalesced_queries();
+  *launches = engine(index)->coalesced_launches();
+  return true;
 }
 
 bool ngtgpu_tc_phase_times(NGTIndex index, float* ms3, NGTError error) {

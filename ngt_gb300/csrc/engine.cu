@@ -854,6 +854,96 @@ void GraphEngine::search(const void* queries, QueryType qt, size_t nq, size_t qd
   NGT_CUDA(cudaStreamSynchronize(s));
 }
 
+void GraphEngine::search_one(const void* query, QueryType qt, size_t qdim, const SearchArgs& args,
+                             SearchOutput& out) {
+  auto call = std::make_shared<CoalescedCall>();
+  convert_queries(query, qt, 1, qdim, call->row);
+  call->args = args;
+  (void)output_size(args);
+  std::unique_lock<std::mutex> lock(co_mu_);
+  co_pending_.push_back(call);
+  while (!call->done) {
+    if (!co_busy_) {
+      // this caller launches everything waiting, its own query included
+      co_busy_ = true;
+      std::vector<std::shared_ptr<CoalescedCall>> batch;
+      batch.swap(co_pending_);
+      lock.unlock();
+      std::string err;
+      try {
+        run_coalesced(batch);
+      } catch (std::exception& ex) {
+        err = ex.what();
+      }
+      lock.lock();
+      for (auto& c : batch) {
+        c->error = err;
+        c->done = true;
+      }
+      co_busy_ = false;
+      co_cv_.notify_all();
+    } else {
+      co_cv_.wait(lock);
+    }
+  }
+  lock.unlock();
+  if (!call->error.empty()) throw std::runtime_error(call->error);
+  out = std::move(call->out);
+}
+
+void GraphEngine::run_coalesced(std::vector<std::shared_ptr<CoalescedCall>>& batch) {
+  NGT_CUDA(cudaSetDevice(device_));
+  const size_t nq = batch.size(), rb = host_.row_bytes();
+  std::vector<SearchArgs> args(nq);
+  size_t kmax = 1;
+  for (size_t i = 0; i < nq; i++) {
+    args[i] = batch[i]->args;
+    kmax = std::max(kmax, output_size(args[i]));
+  }
+  std::vector<ObjDist> res(nq * kmax);
+  std::vector<uint32_t> counts(nq);
+  std::vector<QueryStats> stats(nq);
+  {
+    std::lock_guard<std::mutex> staging(staging_mu_);
+    if (staging_bytes_ < nq * rb) {
+      if (staging_) NGT_CUDA(cudaFreeHost(staging_));
+      staging_ = nullptr;
+      staging_bytes_ = 0;
+      NGT_CUDA(cudaMallocHost(&staging_, nq * rb));
+      staging_bytes_ = nq * rb;
+    }
+    for (size_t i = 0; i < nq; i++) std::memcpy(static_cast<uint8_t*>(staging_) + i * rb, batch[i]->row.data(), rb);
+    uint4* d_rows = nullptr;
+    ObjDist* d_out = nullptr;
+    uint32_t* d_counts = nullptr;
+    QueryStats* d_stats = nullptr;
+    cudaStream_t s = stream_;
+    NGT_CUDA(cudaMallocAsync(&d_rows, nq * rb, s));
+    NGT_CUDA(cudaMallocAsync(&d_out, nq * kmax * sizeof(ObjDist), s));
+    NGT_CUDA(cudaMallocAsync(&d_counts, nq * 4, s));
+    NGT_CUDA(cudaMallocAsync(&d_stats, nq * sizeof(QueryStats), s));
+    NGT_CUDA(cudaMemcpyAsync(d_rows, staging_, nq * rb, cudaMemcpyHostToDevice, s));
+    search_device(d_rows, nq, args.data(), nq, d_out, d_counts, d_stats, kmax, s, Kernel::Exact);
+    NGT_CUDA(cudaMemcpyAsync(res.data(), d_out, nq * kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, s));
+    NGT_CUDA(cudaMemcpyAsync(counts.data(), d_counts, nq * 4, cudaMemcpyDeviceToHost, s));
+    NGT_CUDA(cudaMemcpyAsync(stats.data(), d_stats, nq * sizeof(QueryStats), cudaMemcpyDeviceToHost, s));
+    NGT_CUDA(cudaFreeAsync(d_rows, s));
+    NGT_CUDA(cudaFreeAsync(d_out, s));
+    NGT_CUDA(cudaFreeAsync(d_counts, s));
+    NGT_CUDA(cudaFreeAsync(d_stats, s));
+    NGT_CUDA(cudaStreamSynchronize(s));
+  }
+  co_queries_ += nq;
+  co_launches_++;
+  for (size_t i = 0; i < nq; i++) {
+    SearchOutput& o = batch[i]->out;
+    o.kmax = kmax;
+    o.results.assign(res.begin() + i * kmax, res.begin() + (i + 1) * kmax);
+    o.counts.assign(1, counts[i]);
+    o.stats.assign(1, stats[i]);
+  }
+}
+
 void GraphEngine::linear_search(const void* queries, QueryType qt, size_t nq, size_t qdim, size_t size,
                                 SearchOutput& out) {
   std::lock_guard<std::mutex> lock(mu_);

@@ -4,7 +4,10 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <atomic>
+#include <condition_variable>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -109,6 +112,16 @@ class GraphEngine {
   uint32_t dimension() const { return (uint32_t)host_.prop.dimension; }
 
   // Graph search over host queries (row-major nq x qdim).
+  // One query through the exact-order kernel, coalesced with the other single-query
+  // calls that arrive from other host threads while a launch is on the GPU (the
+  // OpenMP loop of ngtpy's batch_search over ngt_search_index_as_float): the first
+  // caller launches at once; callers arriving meanwhile wait and the next of them
+  // launches all waiting queries together.  Results equal a lone call's (the kernel
+  // handles every query independently).
+  void search_one(const void* query, QueryType qt, size_t qdim, const SearchArgs& args, SearchOutput& out);
+  // queries coalesced so far and launches they took (statistics)
+  uint64_t coalesced_queries() const { return co_queries_; }
+  uint64_t coalesced_launches() const { return co_launches_; }
   void search(const void* queries, QueryType qt, size_t nq, size_t qdim, const SearchArgs* args, size_t nargs,
               SearchOutput& out, Kernel kernel = Kernel::Exact);
   // Quantized graph (<index>/qg): loads it on first use; throws when the index
@@ -303,6 +316,20 @@ class GraphEngine {
     size_t grid = 0;
   };
   std::vector<QbgScratch> qbg_scratch_;
+  // coalescing of single-query calls
+  struct CoalescedCall {
+    std::vector<uint8_t> row;
+    SearchArgs args;
+    SearchOutput out;
+    bool done = false;
+    std::string error;
+  };
+  std::mutex co_mu_;
+  std::condition_variable co_cv_;
+  std::vector<std::shared_ptr<CoalescedCall>> co_pending_;
+  bool co_busy_ = false;
+  std::atomic<uint64_t> co_queries_{0}, co_launches_{0};
+  void run_coalesced(std::vector<std::shared_ptr<CoalescedCall>>& batch);
   QbgScratch& qbg_slot(size_t slot, size_t grid, cudaStream_t stream);
   size_t qbg_grid_ = 0;
   uint32_t qbg_ocap_ = 0;

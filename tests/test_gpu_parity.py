@@ -145,3 +145,31 @@ def test_negative_epsilon_matches_oracle(mode, workdir):
         for j in range(len(q)):
             assert np.array_equal(ids[j, :n[j]], oi[j, :n[j]]), (eps, j)
             assert np.array_equal(ds[j, :n[j]].view(np.uint32), od[j, :n[j]].view(np.uint32)), (eps, j)
+
+
+def test_concurrent_single_query_calls_are_coalesced(workdir):
+    """ngt_search_index_as_float from 16 host threads at once (ngtpy's batch_search
+    pattern): calls that arrive while a launch runs go together into the next one,
+    and every result still equals the reference's."""
+    import threading
+    from ngt_gb300 import Index
+    path, meta, queries, golden = materialize("c1_f32_l2", workdir)
+    s = meta["settings"][0]
+    nq = 400
+    got = [None] * nq
+    with Index(path, read_only=True) as ix:
+        def worker(part):
+            for j in part:
+                got[j] = ix.search(queries[j], k=s["k"], epsilon=s["epsilon"])
+
+        threads = [threading.Thread(target=worker, args=(range(t, nq, 16),)) for t in range(16)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        nqc, nlaunch = ix.coalescing_stats()
+    assert nqc == nq and 1 <= nlaunch <= nq
+    for j in range(nq):
+        r = got[j]
+        assert [o.id for o in r] == list(golden["ids_0"][j][: len(r)])
+        assert np.array_equal(np.array([o.distance for o in r], np.float32), golden["dist_0"][j][: len(r)])
