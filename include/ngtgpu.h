@@ -173,6 +173,12 @@ bool ngtgpu_tc_phase_times(NGTIndex, float *ms3, NGTError);
  * tensor-core search (rounded up to a multiple of 128, at least `candidates`,
  * at most 16384; 0 = automatic, 8192).  Results do not depend on it. */
 bool ngtgpu_set_tc_first_rows(NGTIndex, size_t rows, NGTError);
+/* Row-range shard of the tensor-core exhaustive search: later ngtgpu_linear_search_tc_*
+ * calls on this handle search objects [begin, end) only (begin a multiple of 128,
+ * end 0 = through the last object; 0, 0 restores the whole index).  Each GPU of a
+ * row-range split searches its shard for the size best and a host merge by
+ * (distance, id) gives the whole index's result (ngt_gb300/shard.py). */
+bool ngtgpu_set_tc_row_range(NGTIndex, size_t begin, size_t end, NGTError);
 /* Serving loop (continuous batching).  A server keeps up to `inflight`
  * batched-kernel launches on the GPU at once, each on its own stream and
  * scratch set; requests submitted from any thread while others run join the

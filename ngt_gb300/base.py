@@ -146,6 +146,7 @@ def load_library() -> ctypes.CDLL:
         "ngtgpu_tc_phase_times": ([c_void_p, c_void_p, c_void_p], c_bool),
         "ngtgpu_kernel_launches": ([c_void_p, c_void_p], c_uint64),
         "ngtgpu_coalescing_stats": ([c_void_p, c_void_p, c_void_p, c_void_p], c_bool),
+        "ngtgpu_set_tc_row_range": ([c_void_p, c_size_t, c_size_t, c_void_p], c_bool),
         "ngtgpu_get_wide_search_rows": ([c_void_p, c_void_p], c_uint32),
         "ngtgpu_set_batched_tuning": ([c_void_p, c_uint32, c_uint32, c_float, c_void_p], c_bool),
         "ngtgpu_set_batched_rows_in_flight": ([c_void_p, c_uint32, c_void_p], c_bool),

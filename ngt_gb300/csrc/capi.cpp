@@ -542,6 +542,18 @@ bool ngtgpu_tc_scores_device(NGTIndex index, const void* d_rows, size_t nq, floa
   CAPI_CATCH(error, false)
 }
 
+bool ngtgpu_set_tc_row_range(NGTIndex index, size_t begin, size_t end, NGTError error) {
+  if (index == nullptr) {
+    CAPI_PARAM_ERROR(error, "index = " << index);
+    return false;
+  }
+  try {
+    engine(index)->set_tc_row_range(begin, end);
+    return true;
+  }
+  CAPI_CATCH(error, false)
+}
+
 bool ngtgpu_coalescing_stats(NGTIndex index, uint64_t* queries, uint64_t* launches, NGTError error) {
   if (index == nullptr || queries == nullptr || launches == nullptr) {
     CAPI_PARAM_ERROR(error, "index = " << index);

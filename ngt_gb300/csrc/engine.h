@@ -9,6 +9,7 @@
 #include <map>
 #include <memory>
 #include <mutex>
+#include <stdexcept>
 #include <string>
 #include <vector>
 #include "device_index.h"
@@ -186,6 +187,14 @@ class GraphEngine {
   void tc_phase_ms(float* out) const;
   // rows scored densely before the threshold filter (0: automatic, 8192)
   void set_tc_first_rows(size_t rows) { tc_first_rows_ = rows; }
+  // the tensor-core search covers rows [begin, end) only (a shard of a row-range
+  // split; begin a multiple of 128; end 0 = the last row)
+  void set_tc_row_range(size_t begin, size_t end) {
+    if (begin % 128 != 0) throw std::runtime_error("a shard must begin at a multiple of 128 rows");
+    if (end != 0 && end <= begin) throw std::runtime_error("empty shard");
+    tc_row_begin_ = (uint32_t)begin;
+    tc_row_end_ = (uint32_t)end;
+  }
   // Exhaustive search (exact ids, ties broken by id).
   void linear_search(const void* queries, QueryType qt, size_t nq, size_t qdim, size_t size, SearchOutput& out);
 
@@ -375,6 +384,7 @@ class GraphEngine {
   void ensure_tc_rows8();
   TcState* tc_ = nullptr;
   size_t tc_first_rows_ = 0;
+  uint32_t tc_row_begin_ = 0, tc_row_end_ = 0;
 };
 
 }  // namespace ngtg

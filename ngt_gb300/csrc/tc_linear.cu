@@ -455,7 +455,7 @@ __device__ unsigned long long block_select_u64(const unsigned long long* keys, u
 __global__ void __launch_bounds__(512)
 tc_first_select_kernel(const float* __restrict__ dense, uint32_t ld, uint32_t nrows, uint32_t C,
                        float* __restrict__ thr, unsigned long long* __restrict__ cand,
-                       uint32_t* __restrict__ cand_count, uint32_t cap) {
+                       uint32_t* __restrict__ cand_count, uint32_t cap, uint32_t row_offset) {
   extern __shared__ __align__(16) unsigned char smem[];
   unsigned long long* keys = reinterpret_cast<unsigned long long*>(smem);   // ld
   __shared__ uint32_t hist[256];
@@ -466,7 +466,7 @@ tc_first_select_kernel(const float* __restrict__ dense, uint32_t ld, uint32_t nr
   const float* S = dense + (size_t)q * ld;
   for (uint32_t r = threadIdx.x; r < nrows; r += blockDim.x) {
     const uint32_t key = score_key(S[r]);
-    if (key < kInvalidKey) keys[atomicAdd(&sh_n, 1u)] = ((unsigned long long)key << 32) | r;
+    if (key < kInvalidKey) keys[atomicAdd(&sh_n, 1u)] = ((unsigned long long)key << 32) | (r + row_offset);
   }
   __syncthreads();
   const uint32_t n = sh_n;
@@ -1005,14 +1005,22 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
   const tc::FinalFn fin = tc::final_kernel(kernel_metric(host_.prop.metric), fp64_ties);
   if (!fin) throw std::runtime_error("unsupported distance for the tensor-core linear search");
   const TcState& st = *tc_;
-  const uint32_t nrows = (uint32_t)host_.nrows;
+  // the rows searched: the whole index, or the shard [tc_row_begin_, tc_row_end_)
+  const uint32_t rb = std::min<uint32_t>(tc_row_begin_, (uint32_t)host_.nrows);
+  const uint32_t nrows = tc_row_end_ ? std::min<uint32_t>(tc_row_end_, (uint32_t)host_.nrows) : (uint32_t)host_.nrows;
+  if (rb >= nrows) {
+    TC_CUDA(cudaMemsetAsync(d_counts, 0, nq * 4, stream));
+    TC_CUDA(cudaMemsetAsync(d_status, 0, nq * 4, stream));
+    TC_CUDA(cudaStreamSynchronize(stream));
+    return;
+  }
   // rows of the dense first part: >= C, a multiple of the tile height, <= 16384
   // (automatic: 8192; the threshold then tightens between the doubling parts)
   size_t first = tc_first_rows_ ? tc_first_rows_ : 8192;
   first = std::max<size_t>(first, C);
   first = std::min<size_t>((first + tc::BM - 1) / tc::BM * tc::BM, 16384);
   if (first < C) throw std::runtime_error("too many candidates for the dense first part");
-  const uint32_t r0 = (uint32_t)std::min<size_t>(first, nrows);
+  const uint32_t r0 = (uint32_t)std::min<size_t>((size_t)rb + first, nrows);
   const uint32_t cap = std::min<uint32_t>(16384, std::max<uint32_t>(8192, tc::pow2_at_least((uint32_t)(4 * C))));
   const uint32_t P = tc::pow2_at_least((uint32_t)C);
   int sms = 0;
@@ -1073,13 +1081,13 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
     a.present = d_present_;
     a.error = st.error;
     // dense first part
-    a.row_begin = 0;
+    a.row_begin = rb;
     a.row_end = r0;
     a.dense = dense;
     a.dense_ld = (uint32_t)first;
     launch_scores(st, mapB, a, true, stream, sms, fp8);
-    tc::tc_first_select_kernel<<<nb, 512, first * 8, stream>>>(dense, (uint32_t)first, r0, (uint32_t)C, thr, cand,
-                                                               ccount, cap);
+    tc::tc_first_select_kernel<<<nb, 512, first * 8, stream>>>(dense, (uint32_t)first, r0 - rb, (uint32_t)C, thr,
+                                                               cand, ccount, cap, rb);
     TC_CUDA(cudaGetLastError());
     launches_ += 3;
     TC_CUDA(cudaEventRecord(st.ev[1], stream));
@@ -1096,8 +1104,8 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
     // so such a part ends before it could pass the list capacity (an index with
     // most low ids removed); the presence flags are the same for every query.
     size_t valid = 0;
-    for (uint32_t i = 1; i < r0; i++) valid += host_.present[i] ? 1 : 0;
-    for (uint32_t row = r0, part = std::max<uint32_t>(r0, tc::BM); row < nrows; part *= 2) {
+    for (uint32_t i = std::max<uint32_t>(rb, 1); i < r0; i++) valid += host_.present[i] ? 1 : 0;
+    for (uint32_t row = r0, part = std::max<uint32_t>(r0 - rb, tc::BM); row < nrows; part *= 2) {
       uint32_t end = (uint32_t)std::min<uint64_t>(nrows, (uint64_t)row + part);
       if (valid < C) {
         const size_t room = cap - valid;          // >= 3 C and >= 6144: cap >= max(8192, 4 C), C <= 2048 there

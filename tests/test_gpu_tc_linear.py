@@ -235,3 +235,28 @@ def test_fp8_and_bf16_agree_with_fp64_ties_on_clusters(workdir):
             agree = np.mean([set(ids[j].tolist()) == truth[j] for j in range(len(q))])
             assert agree == 1.0, (prec, agree)
             assert (np.diff(ds, axis=1) >= 0).all()
+
+
+@pytest.mark.parametrize("nshards", [2, 3])
+def test_row_range_shards_merge_to_the_whole_search(workdir, nshards):
+    """The tensor-core search over each shard of a row-range split (the per-GPU part
+    of a multi-GPU exhaustive search), merged on the host by (distance, id), equals the
+    unsharded search: ids and distances bit for bit."""
+    from ngt_gb300 import Index
+    from ngt_gb300.shard import merge_topk, shard_ranges
+    path, meta, queries, golden = materialize("c1_f32_l2", workdir)
+    q = queries[:200]
+    with Index(path, read_only=True) as ix:
+        wi, wd, wn, ws = ix.linear_search_tc(q, k=10, candidates=64, first_rows=256)
+        il, dl, cl = [], [], []
+        for b, e in shard_ranges(ix.number_of_objects() + 1, nshards):
+            ix._check(ix._lib.ngtgpu_set_tc_row_range(ix._index, b, e, ix._err))
+            i, d, n, st = ix.linear_search_tc(q, k=10, candidates=64, first_rows=256)
+            assert (st == 0).all()
+            assert ((i[:, 0] >= max(b, 1)) & (i[:, 0] < e)).all()
+            il.append(i), dl.append(d), cl.append(n)
+        ix._check(ix._lib.ngtgpu_set_tc_row_range(ix._index, 0, 0, ix._err))
+    mi, md, mn = merge_topk(il, dl, cl, 10)
+    assert np.array_equal(mn, wn)
+    assert np.array_equal(mi, wi)
+    assert np.array_equal(md.view(np.uint32), wd.view(np.uint32))
