@@ -801,9 +801,11 @@ def qbg_workload(args, steps=None, warmup=None):
     blobs with a rotation and 4-bit PQ over 64 two-dimensional subspaces, written by
     ngt_gb300.qbg_build in the reference's format and opened with qbg_open_index.
     The search is the reference's CLI / ngtpy one (searchInTwoSteps with a refinement
-    expansion: the probed blobs' 4-bit scans, then an exact uint8 L2 re-rank of k x
-    expansion candidates over the object list), k=10, the probe count the smallest of a
-    sweep whose recall@10 (tie-aware, exact ground truth) is >= 0.9.  The one-step
+    expansion: the probed blobs' 4-bit scans, then an exact uint8 L2 re-rank of k x 10
+    candidates over the object list), k=10, the probe count the smallest of a sweep up
+    to 1024 whose recall@10 (tie-aware, exact ground truth) is >= 0.9, else the
+    largest; the sweep is reported as the recall / throughput frontier.  (The stated
+    coordinates are i.i.d., so a blob partition holds a query's neighbours poorly.)  The one-step
     search of the C API (quantized distances) is reported beside it.  Queries resident
     in HBM; the 1.3 GB object list and 0.4 GB of codes exceed L2, so no flush."""
     import torch
@@ -881,12 +883,15 @@ def qbg_workload(args, steps=None, warmup=None):
     import ctypes
     steps = steps or args.steps
     warmup = max(3, warmup or args.warmup)
-    for name, flags, expansion in (("two_step_refined", QBG_TWO_STEP | QBG_REFINE, 2.0),
-                                   ("one_step_capi", 0, 3.0)):
+    for name, flags, expansion, sweep in (("two_step_refined", QBG_TWO_STEP | QBG_REFINE, 10.0,
+                                           (8, 16, 32, 64, 128, 256, 512, 1024)),
+                                          ("one_step_capi", 0, 3.0, (8, 32, 128, 512))):
         sel = None
-        for probes in (8, 16, 32, 64, 128):
+        frontier = []
+        for probes in sweep:
             ms, r, stn, _ = run(flags, probes, expansion, 1, 1)
             log("qbg %s probes %d: recall@%d %.4f, %.2f ms / %d queries" % (name, probes, k, r, ms, nq))
+            frontier.append({"probes": probes, "recall_at_k": round(r, 4), "qps": round(nq / (ms * 1e-3), 1)})
             sel = (probes, r)
             if r >= 0.9:
                 break
@@ -903,6 +908,7 @@ def qbg_workload(args, steps=None, warmup=None):
         peak = peaks.get("hbm_gbs", 6800.0)
         achieved = bytes_q * nq / (ms * 1e-3) / 1e9
         out[name] = {"qps": nq / (ms * 1e-3), "ms_per_step": ms, "probes_or_explored_blobs": probes,
+                     "frontier": frontier,
                      "expansion": expansion, "recall_at_k": r, "objects_scanned_per_query": scanned,
                      "blobs_judged_per_query": blobs,
                      "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -99,6 +99,24 @@ typedef struct {
 } NGTGPUBatchedTuning;
 bool ngtgpu_set_batched_tuning_ex(NGTIndex, const NGTGPUBatchedTuning *tuning, NGTError);
 
+/* Autotuner of the batched kernels for this index, a result size k and an epsilon
+ * (or, epsilon < 0, the smallest epsilon of a sweep from 0 to 0.3 reaching the floor,
+ * chosen per configuration and returned in *best_epsilon, which may be NULL):
+ * a fixed list of configurations (the warp-per-query kernel's row pipelines and
+ * register budgets, the CTA-per-query kernel's threads, staged rows and parents per
+ * step) is timed on the nq sample queries (CUDA events, median of three launches),
+ * and the fastest whose tie-aware recall@k against the exhaustive search of the
+ * sample is >= recall_floor -- or, with recall_floor < 0, >= the exact-order kernel's
+ * recall at the same epsilon -- becomes the index's tuning.  *best and *best_kernel
+ * (NGTGPU_KERNEL_BATCHED or NGTGPU_KERNEL_WIDE) receive it, *best_qps (may be NULL)
+ * its queries/s on the sample.  With the environment variable NGTGPU_TUNE_CACHE
+ * naming a file, results are kept there as JSON keyed by (objects, dimension, object
+ * type, distance, k, epsilon) and reused without timing.  Fails when no configuration
+ * reaches the floor. */
+bool ngtgpu_autotune(NGTIndex, const float *queries, size_t nq, int32_t dim, size_t k, float epsilon,
+                     float recall_floor, NGTGPUBatchedTuning *best, uint32_t *best_kernel, float *best_qps,
+                     float *best_epsilon, NGTError);
+
 /* Exact graph search (results equal ngtgpu_search_batch_device with
  * NGTGPU_KERNEL_EXACT) that allocates no device memory, for callers that cannot
  * call cudaMalloc while they search: hosts that own and budget all device

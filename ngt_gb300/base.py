@@ -147,6 +147,8 @@ def load_library() -> ctypes.CDLL:
         "ngtgpu_kernel_launches": ([c_void_p, c_void_p], c_uint64),
         "ngtgpu_coalescing_stats": ([c_void_p, c_void_p, c_void_p, c_void_p], c_bool),
         "ngtgpu_set_tc_row_range": ([c_void_p, c_size_t, c_size_t, c_void_p], c_bool),
+        "ngtgpu_autotune": ([c_void_p, c_void_p, c_size_t, c_int32, c_size_t, c_float, c_float,
+                             POINTER(BatchedTuning), c_void_p, c_void_p, c_void_p, c_void_p], c_bool),
         "ngtgpu_get_wide_search_rows": ([c_void_p, c_void_p], c_uint32),
         "ngtgpu_set_batched_tuning": ([c_void_p, c_uint32, c_uint32, c_float, c_void_p], c_bool),
         "ngtgpu_set_batched_rows_in_flight": ([c_void_p, c_uint32, c_void_p], c_bool),
@@ -352,6 +354,21 @@ class Index:
 
     def kernel_launches(self) -> int:
         return int(self._lib.ngtgpu_kernel_launches(self._index, self._err))
+
+    def autotune(self, queries, k: int = 10, epsilon: float = 0.1, recall_floor: float = -1.0):
+        """ngtgpu_autotune: the fastest batched configuration for (k, epsilon) on these
+        sample queries whose recall reaches the floor (default: the exact-order
+        kernel's; epsilon < 0: each configuration at the smallest epsilon of a sweep
+        reaching the floor).  It becomes the index's tuning; returns (kernel, tuning
+        fields, qps on the sample, epsilon)."""
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        t = BatchedTuning()
+        kern, qps, eps = ctypes.c_uint32(0), ctypes.c_float(0.0), ctypes.c_float(0.0)
+        self._check(self._lib.ngtgpu_autotune(self._index, q.ctypes.data, q.shape[0], q.shape[1], k, epsilon,
+                                              recall_floor, ctypes.byref(t), ctypes.byref(kern), ctypes.byref(qps),
+                                              ctypes.byref(eps), self._err))
+        fields = {name: getattr(t, name) for name, _ in BatchedTuning._fields_}
+        return int(kern.value), fields, float(qps.value), float(eps.value)
 
     def coalescing_stats(self):
         """(queries, launches) of the coalesced single-query calls so far."""

@@ -277,3 +277,36 @@ def test_batched_lorentz_distances_exact(workdir):
             assert abs(ds[j, i] - want) <= 1e-5 * max(abs(want), 0.1), (j, i)
         pairs = list(zip(ds[j, :n[j]], ids[j, :n[j]]))
         assert pairs == sorted(pairs)
+
+
+def test_autotune_picks_a_configuration_no_worse_than_the_reference(workdir, tmp_path, monkeypatch):
+    """ngtgpu_autotune on the 5k fixture: the configuration it installs returns recall
+    no lower than the exact-order kernel at the same epsilon, and a second call reads
+    the same choice back from the JSON cache."""
+    import json
+    from ngt_gb300 import Index
+    cache = tmp_path / "tune.json"
+    monkeypatch.setenv("NGTGPU_TUNE_CACHE", str(cache))
+    path, meta, queries, golden = materialize("c1_f32_l2", workdir)
+    k, eps = 10, 0.1
+    gt_d = golden["dist_10"][:1000]                 # the reference's linear search, k = 10
+    files = oracle.IndexFiles(path)
+    o = oracle.Oracle(files)
+    qrows = o.prepare(queries[:1000])
+
+    def dist(a, b):
+        return oracle_dist(files, a, b)
+
+    with Index(path, read_only=True) as ix:
+        kernel, tuning, qps, _ = ix.autotune(queries[:1000], k=k, epsilon=eps)
+        assert kernel in (KERNEL_BATCHED, KERNEL_WIDE) and qps > 0
+        ids, ds, n = ix.batch_search(queries[:1000], k=k, epsilon=eps, kernel=kernel)
+        ei, ed, en = ix.batch_search(queries[:1000], k=k, epsilon=eps, kernel=0)
+    r = _tie_aware_recall(ids, n, gt_d, k, qrows, files.objects, dist)
+    r_exact = _tie_aware_recall(ei, en, gt_d, k, qrows, files.objects, dist)
+    assert r >= r_exact - 1e-12, (r, r_exact)
+    saved = json.loads(cache.read_text())
+    assert len(saved) == 1
+    with Index(path, read_only=True) as ix:
+        kernel2, tuning2, qps2, _ = ix.autotune(queries[:1000], k=k, epsilon=eps)
+    assert (kernel2, tuning2) == (kernel, tuning) and abs(qps2 - qps) <= 1e-3 * qps
