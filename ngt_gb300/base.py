@@ -245,12 +245,23 @@ class Index:
         return [self._lib.ngt_get_result(self._results, i, self._err) for i in range(n)]
 
     def search(self, query, k: int = 20, epsilon: float = 0.1, radius: float = -1.0):
-        """Graph search of one query: list of ObjectDistance (id, distance)."""
+        """Graph search of one query: list of ObjectDistance (id, distance).  Safe to call
+        from several threads at once: each call has its own result and error objects
+        (the library coalesces concurrent calls into one launch)."""
         q = np.ascontiguousarray(query, dtype=np.float32)
-        ok = self._lib.ngt_search_index_as_float(self._index, q.ctypes.data_as(POINTER(c_float)), q.shape[0], k,
-                                                 epsilon, radius, self._results, self._err)
-        self._check(ok)
-        return self._collect()
+        L = self._lib
+        err = L.ngt_create_error_object()
+        res = L.ngt_create_empty_results(err)
+        try:
+            ok = L.ngt_search_index_as_float(self._index, q.ctypes.data_as(POINTER(c_float)), q.shape[0], k,
+                                             epsilon, radius, res, err)
+            if not ok:
+                raise NativeError(L.ngt_get_error_string(err).decode())
+            n = L.ngt_get_result_size(res, err)
+            return [L.ngt_get_result(res, i, err) for i in range(n)]
+        finally:
+            L.ngt_destroy_results(res)
+            L.ngt_destroy_error_object(err)
 
     def linear_search(self, query, k: int = 20):
         q = np.ascontiguousarray(query, dtype=np.float32)
