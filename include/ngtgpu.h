@@ -46,6 +46,24 @@ bool ngtgpu_search_batch_float(NGTIndex, const float *queries, size_t nq, int32_
                                const NGTQueryParameters *params, size_t nparams, NGTObjectDistance *results,
                                size_t kmax, uint32_t *counts, NGTGPUQueryStats *stats, uint32_t kernel, NGTError);
 
+/* ngtgpu_search_batch_float with the search container's expected accuracy, as the
+ * reference's C++ API takes it (NGT::SearchContainer::setExpectedAccuracy; the C API
+ * has no way to pass it, and ignores NGTQuery.accuracy): accuracy > 0 replaces
+ * epsilon by the epsilon the index's AccuracyTable property gives for it
+ * (AccuracyTable::getEpsilon, lib/NGT/Index.h:442-472; GraphIndex::search,
+ * lib/NGT/Index.h:1700-1702), before the edge size and the exploration coefficient
+ * are derived from it.  An index without a table fails the call. */
+typedef struct {
+  size_t size;
+  float epsilon;
+  float accuracy;   /* expected accuracy; <= 0: use epsilon */
+  float radius;     /* < 0: no radius (FLT_MAX); a range search returns at most size objects within it */
+  size_t edge_size;
+} NGTGPUSearchParameters;
+bool ngtgpu_search_batch_ex_float(NGTIndex, const float *queries, size_t nq, int32_t dim,
+                                  const NGTGPUSearchParameters *params, size_t nparams, NGTObjectDistance *results,
+                                  size_t kmax, uint32_t *counts, NGTGPUQueryStats *stats, uint32_t kernel, NGTError);
+
 /* Size in bytes of one converted query row (padded object layout). */
 size_t ngtgpu_query_row_bytes(NGTIndex, NGTError);
 

@@ -52,6 +52,12 @@ class QueryParameters(ctypes.Structure):
     _fields_ = [("size", c_size_t), ("epsilon", c_float), ("radius", c_float), ("edge_size", c_size_t)]
 
 
+class SearchParameters(ctypes.Structure):
+    """NGTGPUSearchParameters (include/ngtgpu.h): NGTQueryParameters with the expected accuracy."""
+    _fields_ = [("size", c_size_t), ("epsilon", c_float), ("accuracy", c_float), ("radius", c_float),
+                ("edge_size", c_size_t)]
+
+
 class QGQueryParameters(ctypes.Structure):
     """NGTQGQueryParameters (lib/NGT/NGTQ/Capi.h:41-46)."""
     _fields_ = [("size", c_size_t), ("epsilon", c_float), ("result_expansion", c_float), ("radius", c_float)]
@@ -129,6 +135,8 @@ def load_library() -> ctypes.CDLL:
         "ngtgpu_search_batch_float": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QueryParameters), c_size_t,
                                        c_void_p, c_size_t, c_void_p, c_void_p, c_uint32, c_void_p], c_bool),
         "ngtgpu_query_row_bytes": ([c_void_p, c_void_p], c_size_t),
+        "ngtgpu_search_batch_ex_float": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(SearchParameters), c_size_t,
+                                          c_void_p, c_size_t, c_void_p, c_void_p, c_uint32, c_void_p], c_bool),
         "ngtgpu_convert_queries_float": ([c_void_p, c_void_p, c_size_t, c_int32, c_void_p, c_void_p], c_bool),
         "ngtgpu_search_batch_device": ([c_void_p, c_void_p, c_size_t, POINTER(QueryParameters), c_size_t, c_void_p,
                                         c_size_t, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p], c_bool),
@@ -311,6 +319,24 @@ class Index:
         m = int(counts.max()) if nq else 0
         out = (res["id"][:, :m].copy(), res["distance"][:, :m].copy(), counts)
         return out + (stats,) if with_stats else out
+
+    def batch_search_accuracy(self, queries, k=10, accuracy=0.9, epsilon=0.1, radius=-1.0, edge_size=None,
+                              kernel: int = KERNEL_EXACT):
+        """batch_search with the expected accuracy of the reference's C++ search container:
+        epsilon comes from the index's AccuracyTable (ngtgpu_search_batch_ex_float)."""
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        nq = q.shape[0]
+        p = SearchParameters(int(k), float(epsilon), float(accuracy), float(radius),
+                             _edge_field(-1 if edge_size is None else edge_size))
+        kmax = int(np.ceil(k * 1.4)) + 1
+        res = np.zeros((nq, kmax), RESULT_DTYPE)
+        counts = np.zeros(nq, np.uint32)
+        ok = self._lib.ngtgpu_search_batch_ex_float(self._index, q.ctypes.data, nq, q.shape[1], ctypes.byref(p), 1,
+                                                    res.ctypes.data, kmax, counts.ctypes.data, None, kernel,
+                                                    self._err)
+        self._check(ok)
+        m = int(counts.max()) if nq else 0
+        return res["id"][:, :m].copy(), res["distance"][:, :m].copy(), counts
 
     def set_batched_tuning(self, list_capacity: int = 0, parents: int = 0, rerank_factor: float = 0.0,
                            rows_in_flight: int = 0, ctas_per_sm: int = 0, neighbour_capacity: int = 0,

@@ -348,6 +348,46 @@ static ngtg::Kernel check_kernel(uint32_t kernel) {
   }
 }
 
+static bool search_batch_args(NGTIndex index, const float* queries, size_t nq, int32_t dim,
+                              const std::vector<SearchArgs>& a, NGTObjectDistance* results, size_t kmax,
+                              uint32_t* counts, NGTGPUQueryStats* stats, ngtg::Kernel kk) {
+  for (const auto& x : a)
+    if (engine(index)->output_size(x) > kmax) throw std::runtime_error("a query asks for more results than kmax");
+  SearchOutput out;
+  engine(index)->search(queries, QueryType::Float32, nq, (size_t)dim, a.data(), a.size(), out, kk);
+  for (size_t q = 0; q < nq; q++) {
+    counts[q] = out.counts[q];
+    for (uint32_t i = 0; i < out.counts[q]; i++) {
+      const ngtg::ObjDist& o = out.results[q * out.kmax + i];
+      results[q * kmax + i] = NGTObjectDistance{o.id, o.distance};
+    }
+    if (stats) std::memcpy(stats + q, &out.stats[q], sizeof(NGTGPUQueryStats));
+  }
+  return true;
+}
+
+bool ngtgpu_search_batch_ex_float(NGTIndex index, const float* queries, size_t nq, int32_t dim,
+                                  const NGTGPUSearchParameters* params, size_t nparams, NGTObjectDistance* results,
+                                  size_t kmax, uint32_t* counts, NGTGPUQueryStats* stats, uint32_t kernel,
+                                  NGTError error) {
+  if (index == nullptr || (nq && (queries == nullptr || results == nullptr || counts == nullptr)) ||
+      params == nullptr || dim <= 0 || !(nparams == 1 || nparams == nq)) {
+    CAPI_PARAM_ERROR(error, "index = " << index << " queries = " << queries << " nq = " << nq
+                                       << " nparams = " << nparams << " dim = " << dim);
+    return false;
+  }
+  try {
+    ngtg::Kernel kk = check_kernel(kernel);
+    std::vector<SearchArgs> a(nparams);
+    for (size_t i = 0; i < nparams; i++) {
+      a[i] = make_args(params[i].size, params[i].epsilon, params[i].radius, edge_size_from_field(params[i].edge_size));
+      a[i].accuracy = params[i].accuracy;
+    }
+    return search_batch_args(index, queries, nq, dim, a, results, kmax, counts, stats, kk);
+  }
+  CAPI_CATCH(error, false)
+}
+
 bool ngtgpu_search_batch_float(NGTIndex index, const float* queries, size_t nq, int32_t dim,
                                const NGTQueryParameters* params, size_t nparams, NGTObjectDistance* results,
                                size_t kmax, uint32_t* counts, NGTGPUQueryStats* stats, uint32_t kernel,

@@ -275,6 +275,35 @@ size_t GraphEngine::edge_size_for(const SearchArgs& a) const {
   throw std::runtime_error("invalid edge size parameter " + std::to_string(a.edge_size));
 }
 
+float GraphEngine::epsilon_for_accuracy(double accuracy) const {
+  // the table "eps:accuracy,eps:accuracy,..." (AccuracyTable::set, lib/NGT/Index.h:424-440)
+  std::vector<std::pair<float, double>> table;
+  const std::string str = host_.prop.get("AccuracyTable", "");
+  std::stringstream ss(str);
+  std::string tok;
+  while (std::getline(ss, tok, ',')) {
+    if (tok.empty()) continue;
+    const size_t c = tok.find(':');
+    if (c == std::string::npos || tok.find(':', c + 1) != std::string::npos)
+      throw std::runtime_error("AccuracyTable: invalid accuracy table string " + tok + ":" + str);
+    table.emplace_back((float)std::strtod(tok.substr(0, c).c_str(), nullptr),
+                       std::strtod(tok.substr(c + 1).c_str(), nullptr));
+  }
+  if (table.size() <= 2)
+    throw std::runtime_error("AccuracyTable: the accuracy table is not set yet. The table size=" +
+                             std::to_string(table.size()));
+  if (accuracy > 1.0) accuracy = 1.0;
+  size_t i = 0;
+  while (i < table.size() && table[i].second < accuracy) i++;
+  if (i == table.size()) i -= 2;
+  else if (i != 0) i--;
+  const std::pair<float, double> lower = table[i], upper = table[i + 1];
+  float e = (float)(lower.first + (upper.first - lower.first) * (accuracy - lower.second) /
+                                      (upper.second - lower.second));
+  if (e < -0.9f) e = -0.9f;
+  return e;
+}
+
 void GraphEngine::build_params(const SearchArgs* args, size_t nargs, size_t nq, size_t kmax,
                                std::vector<QueryParams>& params, std::vector<uint32_t>& seed_list,
                                uint32_t& max_size) {
@@ -291,7 +320,13 @@ void GraphEngine::build_params(const SearchArgs* args, size_t nargs, size_t nq, 
       params[i].out_off = (uint32_t)(i * kmax);
       continue;
     }
-    const SearchArgs& a = args[nargs == 1 ? 0 : i];
+    SearchArgs a = args[nargs == 1 ? 0 : i];
+    if (a.accuracy > 0.0f) {
+      // GraphIndex::search sets epsilon from the expected accuracy before the edge size
+      // and the exploration coefficient are derived from it (lib/NGT/Index.h:1700-1702)
+      a.epsilon = epsilon_for_accuracy(a.accuracy);
+      a.accuracy = -1.0f;
+    }
     QueryParams qp{};
     float coef = a.epsilon + 1.0f;                     // SearchContainer::setEpsilon
     if (coef == 0.0f) coef = 1.1f;                     // NGT_EXPLORATION_COEFFICIENT
@@ -381,7 +416,7 @@ bool GraphEngine::result_size_rule() const {
 
 size_t GraphEngine::output_size(const SearchArgs& a) const {
   if (result_size_rule() && mode_ == GraphMode::Updatable) {
-    float coef = a.epsilon + 1.0f;
+    float coef = (a.accuracy > 0.0f ? epsilon_for_accuracy(a.accuracy) : a.epsilon) + 1.0f;
     if (coef == 0.0f) coef = 1.1f;
     return (size_t)std::round(coef * (float)a.size);
   }

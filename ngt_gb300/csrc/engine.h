@@ -31,6 +31,10 @@ struct SearchArgs {
   float epsilon = 0.1f;
   float radius = -1.0f;            // < 0 means FLT_MAX
   int64_t edge_size = -1;          // -1: index default (EdgeSizeForSearch)
+  // > 0: the expected accuracy of the C++ API's search container, which replaces
+  // epsilon by the index's AccuracyTable (lib/NGT/Index.h:1700-1702); the reference's
+  // C API never passes it, so only the batched extensions set it
+  float accuracy = -1.0f;
 };
 
 // Query element type accepted at the boundary.
@@ -235,6 +239,9 @@ class GraphEngine {
   const FastTuning& tuning() const { return tuning_; }
   bool fast_supported(Kernel k) const;
 
+  // AccuracyTable::getEpsilon (lib/NGT/Index.h:442-472) over the index's
+  // AccuracyTable property: the epsilon expected to give `accuracy`
+  float epsilon_for_accuracy(double accuracy) const;
   // Number of results a query can return (larger than args.size only for the
   // updatable search on an index with EpsilonType ResultSize).
   size_t output_size(const SearchArgs& a) const;

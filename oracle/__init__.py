@@ -53,6 +53,31 @@ def build(verbose: bool = False) -> str:
     return LIB_PATH
 
 
+def epsilon_from_accuracy(table: str, accuracy: float) -> float:
+    """AccuracyTable::getEpsilon (lib/NGT/Index.h:442-472): epsilon interpolated
+    between the two table entries around the expected accuracy (float epsilons, double
+    accuracies, the difference of the epsilons in float)."""
+    t = []
+    for tok in table.split(","):
+        if not tok:
+            continue
+        a, b = tok.split(":")
+        t.append((np.float32(float(a)), float(b)))
+    if len(t) <= 2:
+        raise ValueError("the accuracy table is not set")
+    accuracy = min(accuracy, 1.0)
+    i = 0
+    while i < len(t) and t[i][1] < accuracy:
+        i += 1
+    if i == len(t):
+        i -= 2
+    elif i != 0:
+        i -= 1
+    lo, up = t[i], t[i + 1]
+    e = np.float32(float(lo[0]) + float(np.float32(up[0] - lo[0])) * (accuracy - lo[1]) / (up[1] - lo[1]))
+    return float(max(e, np.float32(-0.9)))
+
+
 def build_fast() -> str:
     """Compiles liboracle_fast.so: the same restatement with the reference's Release
     flags (-Ofast -march=native), timed as the CPU baseline; never used to check."""

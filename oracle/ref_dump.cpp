@@ -3,7 +3,7 @@
 // in this directory) through its own C API (lib/NGT/Capi.h) and dumps the
 // results in binary, so tests/golden/make_golden.py can record golden vectors.
 //
-// usage: ref_dump <graph|linear|qg|qbg> <index> <queries.f32> <nq> <dim> <k> <eps> <edge_size|x> <ro|rw> <out>
+// usage: ref_dump <graph|linear|range|graph_acc|qg|qbg> <index> <queries.f32> <nq> <dim> <k> <eps> <edge_size|x> <ro|rw> <out>
 //   out: nq x k uint32 ids, then nq x k float distances, then nq uint32 counts.
 //   For qg the edge_size argument is the result expansion (ngtqg_search_index_float).
 //   For qbg it is "expansion:explored_blobs:blob_epsilon" (qbg_search_index_float),
@@ -12,6 +12,7 @@
 //   For graph-only indexes srand(1) runs before every query, so that the
 //   random seeds the reference draws are reproducible.
 #include <NGT/Capi.h>
+#include <NGT/Index.h>
 #include <NGT/NGTQ/Capi.h>
 
 #include <climits>
@@ -122,6 +123,39 @@ int main(int argc, char** argv) {
     std::fclose(o);
     return 0;
   }
+  if (op == "graph_acc") {
+    // the C++ API's expected accuracy (SearchContainer::setExpectedAccuracy; the C API
+    // ignores NGTQuery::accuracy): epsilon from the index's AccuracyTable
+    // (lib/NGT/Index.h:1700-1702); the edge argument holds the accuracy
+    NGT::Index cindex(index_path, ro);
+    const float acc = std::strtof(argv[8], nullptr);
+    for (size_t i = 0; i < nq; i++) {
+      std::srand(1);
+      std::vector<float> qv(q.begin() + i * dim, q.begin() + (i + 1) * dim);
+      NGT::SearchQuery sc(qv);
+      sc.setSize(k);
+      sc.setEpsilon(eps);
+      sc.setExpectedAccuracy(acc);
+      cindex.search(sc);
+      auto& rs = sc.getWorkingResult();          // a max-heap of (distance, id)
+      std::vector<NGT::ObjectDistance> v;
+      while (!rs.empty()) {
+        v.push_back(rs.top());
+        rs.pop();
+      }
+      cnt[i] = (uint32_t)std::min(v.size(), k);
+      for (size_t j = 0; j < cnt[i]; j++) {
+        ids[i * k + j] = v[v.size() - 1 - j].id;
+        ds[i * k + j] = v[v.size() - 1 - j].distance;
+      }
+    }
+    FILE* o = std::fopen(argv[10], "wb");
+    std::fwrite(ids.data(), 4, ids.size(), o);
+    std::fwrite(ds.data(), 4, ds.size(), o);
+    std::fwrite(cnt.data(), 4, cnt.size(), o);
+    std::fclose(o);
+    return 0;
+  }
   NGTIndex index = ro ? ngt_open_index_as_read_only(index_path, err) : ngt_open_index(index_path, err);
   if (!index) {
     std::fprintf(stderr, "open failed: %s\n", ngt_get_error_string(err));
@@ -133,6 +167,10 @@ int main(int argc, char** argv) {
     std::srand(1);
     if (op == "linear") {
       ok = ngt_linear_search_index_as_float(index, &q[i * dim], (int32_t)dim, k, res, err);
+    } else if (op == "range") {
+      // range search: results within the radius (the edge argument), at most k
+      ok = ngt_search_index_as_float(index, &q[i * dim], (int32_t)dim, k, eps, std::strtof(argv[8], nullptr), res,
+                                     err);
     } else if (has_edge) {
       NGTQueryFloat qf;
       qf.query = &q[i * dim];

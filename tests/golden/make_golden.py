@@ -124,6 +124,17 @@ FIXTURES = {
         create="-d 32 -o f -D 2 -E 10 -S 40 -i t", regenerate_obj=True, otype="f",
         prf_set={"EpsilonType": "ResultSize"},
         settings=[("graph", 10, 0.1, None, "ro"), ("graph", 10, 0.2, None, "rw")]),
+    # Range search (radius in the edge column, ngt_search_index_as_float's radius) and
+    # the C++ API's expected accuracy (accuracy in the edge column; epsilon from the
+    # AccuracyTable property, lib/NGT/Index.h:418-486, 1700-1702)
+    "f32_l2_acc_range": dict(
+        base=("clipped_exponential", dict(n=2000, dim=32, seed=261)),
+        query=("clipped_exponential", dict(n=200, dim=32, seed=262)),
+        create="-d 32 -o f -D 2 -E 10 -S 40 -i t", regenerate_obj=True, otype="f",
+        prf_set={"AccuracyTable": "0:0.62,0.02:0.78,0.05:0.9,0.1:0.97,0.2:0.995,0.3:1"},
+        settings=[("range", 100, 0.1, 110.0, "ro"), ("range", 100, 0.1, 130.0, "rw"), ("range", 20, 0.0, 120.0, "ro"),
+                  ("graph_acc", 10, 0.1, 0.85, "ro"), ("graph_acc", 10, 0.1, 0.97, "ro"),
+                  ("graph_acc", 20, 0.1, 0.995, "rw"), ("graph_acc", 10, 0.1, 0.5, "ro")]),
     # Scalar-quantized objects (ObjectType QSUInteger-8B): int8 codes
     # rint(x / QuantizationScale x 127.5), the query quantized the same way
     "qs8_l2": dict(

@@ -45,7 +45,18 @@ def test_batch_search_matches_reference(name, workdir):
         nq, k = s["nq"], s["k"]
         gi, gd, gc = golden["ids_%d" % i], golden["dist_%d" % i], golden["count_%d" % i]
         with Index(path, read_only=(s["mode"] == "ro")) as ix:
-            if s["op"] == "linear":
+            if s["op"] == "graph_acc":
+                # the C++ API's expected accuracy: epsilon from the index's AccuracyTable
+                ids, ds, n = ix.batch_search_accuracy(queries[:nq], k=k, accuracy=s["edge_size"],
+                                                      epsilon=s["epsilon"])
+                ids = np.pad(ids, ((0, 0), (0, max(0, k - ids.shape[1]))))
+                ds = np.pad(ds, ((0, 0), (0, max(0, k - ds.shape[1]))))
+            elif s["op"] == "range":
+                # range search: at most k results within the radius (the edge column)
+                ids, ds, n = ix.batch_search(queries[:nq], k=k, epsilon=s["epsilon"], radius=s["edge_size"])
+                ids = np.pad(ids, ((0, 0), (0, max(0, k - ids.shape[1]))))
+                ds = np.pad(ds, ((0, 0), (0, max(0, k - ds.shape[1]))))
+            elif s["op"] == "linear":
                 res = [ix.linear_search(q, k=k) for q in queries[:nq]]
                 n = np.array([len(r) for r in res], np.uint32)
                 ids = np.zeros((nq, k), np.uint32)

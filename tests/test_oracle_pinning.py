@@ -32,6 +32,16 @@ def test_oracle_matches_reference_golden(name, workdir):
         gi, gd, gc = golden["ids_%d" % i], golden["dist_%d" % i], golden["count_%d" % i]
         if s["op"] == "linear":
             ids, ds, n = o.linear_search(queries[:nq], k=k, threads=4)
+        elif s["op"] in ("range", "graph_acc"):
+            # range search: the radius in the edge column; expected accuracy: the epsilon
+            # comes from the index's AccuracyTable
+            eps, radius = s["epsilon"], -1.0
+            if s["op"] == "range":
+                radius = s["edge_size"]
+            else:
+                eps = oracle.epsilon_from_accuracy(oracle.read_property(path)["AccuracyTable"], s["edge_size"])
+            ids, ds, n, _ = o.search(queries[:nq], k=k, epsilon=eps, radius=radius,
+                                     mode="read_only" if s["mode"] == "ro" else "updatable", threads=4)
         elif s["op"] == "qg":
             # quantized graph: the edge column holds the result expansion
             ids, ds, n, _ = o.qg_search(queries[:nq], k=k, epsilon=s["epsilon"], result_expansion=s["edge_size"],
