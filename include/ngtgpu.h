@@ -59,6 +59,11 @@ typedef struct {
   float accuracy;   /* expected accuracy; <= 0: use epsilon */
   float radius;     /* < 0: no radius (FLT_MAX); a range search returns at most size objects within it */
   size_t edge_size;
+  float refinement_expansion;  /* >= 1 (every query of the call): the search container's refinement
+                                  expansion of the C++ API (GraphIndex::search(SearchQuery&),
+                                  lib/NGT/Index.h:1146-1236): size x expansion results re-ranked by exact
+                                  distances over the index's float refinement objects (robj; L1, L2,
+                                  angle and cosine distances) to the size best; 0: none */
 } NGTGPUSearchParameters;
 bool ngtgpu_search_batch_ex_float(NGTIndex, const float *queries, size_t nq, int32_t dim,
                                   const NGTGPUSearchParameters *params, size_t nparams, NGTObjectDistance *results,

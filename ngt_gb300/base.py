@@ -53,9 +53,10 @@ class QueryParameters(ctypes.Structure):
 
 
 class SearchParameters(ctypes.Structure):
-    """NGTGPUSearchParameters (include/ngtgpu.h): NGTQueryParameters with the expected accuracy."""
+    """NGTGPUSearchParameters (include/ngtgpu.h): NGTQueryParameters with the expected
+    accuracy and the refinement expansion of the reference's C++ search container."""
     _fields_ = [("size", c_size_t), ("epsilon", c_float), ("accuracy", c_float), ("radius", c_float),
-                ("edge_size", c_size_t)]
+                ("edge_size", c_size_t), ("refinement_expansion", c_float)]
 
 
 class QGQueryParameters(ctypes.Structure):
@@ -327,14 +328,32 @@ class Index:
         q = np.ascontiguousarray(queries, dtype=np.float32)
         nq = q.shape[0]
         p = SearchParameters(int(k), float(epsilon), float(accuracy), float(radius),
-                             _edge_field(-1 if edge_size is None else edge_size))
-        kmax = int(np.ceil(k * 1.4)) + 1
+                             _edge_field(-1 if edge_size is None else edge_size), 0.0)
+        return self._search_ex(q, p, int(np.ceil(k * 1.4)) + 1, kernel)
+
+    def batch_search_refined(self, queries, k=10, expansion=2.0, epsilon=0.1, edge_size=None,
+                             kernel: int = KERNEL_EXACT):
+        """batch_search with the refinement expansion of the reference's C++ search
+        container: k x expansion results re-ranked by exact distances over the index's
+        refinement objects (robj) to the k best (ngtgpu_search_batch_ex_float)."""
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        p = SearchParameters(int(k), float(epsilon), -1.0, -1.0,
+                             _edge_field(-1 if edge_size is None else edge_size), float(expansion))
+        return self._search_ex(q, p, int(k), kernel)
+
+    def _search_ex(self, q, p, kmax, kernel):
+        nq = q.shape[0]
         res = np.zeros((nq, kmax), RESULT_DTYPE)
         counts = np.zeros(nq, np.uint32)
-        ok = self._lib.ngtgpu_search_batch_ex_float(self._index, q.ctypes.data, nq, q.shape[1], ctypes.byref(p), 1,
-                                                    res.ctypes.data, kmax, counts.ctypes.data, None, kernel,
-                                                    self._err)
-        self._check(ok)
+        L = self._lib
+        err = L.ngt_create_error_object()
+        try:
+            ok = L.ngtgpu_search_batch_ex_float(self._index, q.ctypes.data, nq, q.shape[1], ctypes.byref(p), 1,
+                                                res.ctypes.data, kmax, counts.ctypes.data, None, kernel, err)
+            if not ok:
+                raise NativeError(L.ngt_get_error_string(err).decode())
+        finally:
+            L.ngt_destroy_error_object(err)
         m = int(counts.max()) if nq else 0
         return res["id"][:, :m].copy(), res["distance"][:, :m].copy(), counts
 

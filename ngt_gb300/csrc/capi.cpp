@@ -352,7 +352,8 @@ static bool search_batch_args(NGTIndex index, const float* queries, size_t nq, i
                               const std::vector<SearchArgs>& a, NGTObjectDistance* results, size_t kmax,
                               uint32_t* counts, NGTGPUQueryStats* stats, ngtg::Kernel kk) {
   for (const auto& x : a)
-    if (engine(index)->output_size(x) > kmax) throw std::runtime_error("a query asks for more results than kmax");
+    if ((x.refinement_expansion >= 1.0f ? x.size : engine(index)->output_size(x)) > kmax)
+      throw std::runtime_error("a query asks for more results than kmax");
   SearchOutput out;
   engine(index)->search(queries, QueryType::Float32, nq, (size_t)dim, a.data(), a.size(), out, kk);
   for (size_t q = 0; q < nq; q++) {
@@ -382,6 +383,7 @@ bool ngtgpu_search_batch_ex_float(NGTIndex index, const float* queries, size_t n
     for (size_t i = 0; i < nparams; i++) {
       a[i] = make_args(params[i].size, params[i].epsilon, params[i].radius, edge_size_from_field(params[i].edge_size));
       a[i].accuracy = params[i].accuracy;
+      a[i].refinement_expansion = params[i].refinement_expansion;
     }
     return search_batch_args(index, queries, nq, dim, a, results, kmax, counts, stats, kk);
   }

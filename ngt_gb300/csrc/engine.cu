@@ -194,6 +194,7 @@ GraphEngine::~GraphEngine() {
   cudaFree(d_qbg_ovf_);
   cudaFree(d_blob_dist_);
   cudaFree(d_olist_);
+  cudaFree(d_robj_);
   for (QbgScratch& q : qbg_scratch_) {
     cudaFree(q.bitmaps);
     cudaFree(q.exact_ovf);
@@ -850,6 +851,12 @@ void GraphEngine::launch_fast(const uint4* d_rows, size_t nq, const QueryParams*
 void GraphEngine::search(const void* queries, QueryType qt, size_t nq, size_t qdim, const SearchArgs* args,
                          size_t nargs, SearchOutput& out, Kernel kernel) {
   NGT_CUDA(cudaSetDevice(device_));
+  bool refine = false;
+  for (size_t i = 0; i < nargs; i++) refine = refine || args[i].refinement_expansion >= 1.0f;
+  if (refine) {
+    search_refined(queries, qt, nq, qdim, args, nargs, out, kernel);
+    return;
+  }
   std::lock_guard<std::mutex> staging(staging_mu_);
   // the query rows are converted straight into a pinned staging buffer (kept between calls)
   const size_t row_total = nq * host_.row_bytes();
@@ -886,6 +893,77 @@ void GraphEngine::search(const void* queries, QueryType qt, size_t nq, size_t qd
   NGT_CUDA(cudaFreeAsync(d_out, s));
   NGT_CUDA(cudaFreeAsync(d_counts, s));
   NGT_CUDA(cudaFreeAsync(d_stats, s));
+  NGT_CUDA(cudaStreamSynchronize(s));
+}
+
+void GraphEngine::search_refined(const void* queries, QueryType qt, size_t nq, size_t qdim, const SearchArgs* args,
+                                 size_t nargs, SearchOutput& out, Kernel kernel) {
+  // GraphIndex::search(SearchQuery&) with a refinement expansion (lib/NGT/Index.h:1146-1236):
+  // the search keeps size x expansion results, whose exact distances over the float
+  // refinement objects (the comparator of the index's distance) order them, and the size
+  // best by (distance, id) are returned
+  if (host_.robj_rows == 0) throw std::runtime_error("the index has no refinement objects (robj)");
+  if (qt != QueryType::Float32 || qdim != (size_t)host_.prop.dimension)
+    throw std::runtime_error("a refined search takes float queries of the index dimension");
+  QBGRefineKernelFn rf = graph_refine_kernel_for(host_.prop.metric);
+  if (!rf) throw std::runtime_error("the refinement supports the L1, L2, angle and cosine distances");
+  std::vector<SearchArgs> exp(nargs);
+  std::vector<uint32_t> exact(nq);
+  uint32_t max_search = 1;
+  for (size_t i = 0; i < nargs; i++) {
+    if (args[i].refinement_expansion < 1.0f)
+      throw std::runtime_error("refined and unrefined queries in one call");
+    exp[i] = args[i];
+    exp[i].size = (size_t)((float)args[i].size * args[i].refinement_expansion);
+    exp[i].refinement_expansion = 0.0f;
+    max_search = std::max<uint32_t>(max_search, (uint32_t)output_size(exp[i]));
+  }
+  if (max_search > 4096) throw std::runtime_error("size x refinement expansion above 4096");
+  size_t kmax = 1;
+  for (size_t q = 0; q < nq; q++) {
+    exact[q] = (uint32_t)args[nargs == 1 ? 0 : q].size;
+    kmax = std::max<size_t>(kmax, exact[q]);
+  }
+  SearchOutput cand;
+  search(queries, qt, nq, qdim, exp.data(), nargs, cand, kernel);
+  {
+    std::lock_guard<std::mutex> lock(mu_);
+    if (!d_robj_) d_robj_ = dmalloc_copy<void>(host_.robj.data(), host_.robj.size() * 4);
+  }
+  cudaStream_t s = stream_;
+  ObjDist *d_cand = nullptr, *d_out = nullptr;
+  uint32_t *d_cc = nullptr, *d_exact = nullptr, *d_counts = nullptr;
+  float* d_q = nullptr;
+  NGT_CUDA(cudaMallocAsync(&d_cand, cand.results.size() * sizeof(ObjDist), s));
+  NGT_CUDA(cudaMallocAsync(&d_cc, nq * 4, s));
+  NGT_CUDA(cudaMallocAsync(&d_exact, nq * 4, s));
+  NGT_CUDA(cudaMallocAsync(&d_q, nq * qdim * 4, s));
+  NGT_CUDA(cudaMallocAsync(&d_out, nq * kmax * sizeof(ObjDist), s));
+  NGT_CUDA(cudaMallocAsync(&d_counts, nq * 4, s));
+  NGT_CUDA(cudaMemcpyAsync(d_cand, cand.results.data(), cand.results.size() * sizeof(ObjDist),
+                           cudaMemcpyHostToDevice, s));
+  NGT_CUDA(cudaMemcpyAsync(d_cc, cand.counts.data(), nq * 4, cudaMemcpyHostToDevice, s));
+  NGT_CUDA(cudaMemcpyAsync(d_exact, exact.data(), nq * 4, cudaMemcpyHostToDevice, s));
+  NGT_CUDA(cudaMemcpyAsync(d_q, queries, nq * qdim * 4, cudaMemcpyHostToDevice, s));
+  int sms = 0;
+  NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+  const uint32_t P = next_pow2(std::max<uint32_t>((uint32_t)cand.kmax, 2));
+  const uint32_t rchunks = host_.rdim_pad / 4;
+  const size_t smem = (size_t)rchunks * 16 + (size_t)P * 8;
+  NGT_CUDA(cudaFuncSetAttribute((const void*)rf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  rf<<<(unsigned)std::min<size_t>(nq, (size_t)sms * 8), 256, smem, s>>>(
+      d_cand, d_cc, (uint32_t)cand.kmax, d_q, (uint32_t)qdim, static_cast<const uint4*>(d_robj_), rchunks,
+      (uint32_t)host_.prop.dimension, host_.robj_rows, d_exact, (uint32_t)nq, P, d_out, (uint32_t)kmax, d_counts);
+  NGT_CUDA(cudaGetLastError());
+  launches_++;
+  out.kmax = kmax;
+  out.results.assign(nq * kmax, ObjDist{0, 0.f});
+  out.counts.assign(nq, 0);
+  out.stats = cand.stats;
+  NGT_CUDA(cudaMemcpyAsync(out.results.data(), d_out, nq * kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, s));
+  NGT_CUDA(cudaMemcpyAsync(out.counts.data(), d_counts, nq * 4, cudaMemcpyDeviceToHost, s));
+  for (void* p : {(void*)d_cand, (void*)d_cc, (void*)d_exact, (void*)d_q, (void*)d_out, (void*)d_counts})
+    NGT_CUDA(cudaFreeAsync(p, s));
   NGT_CUDA(cudaStreamSynchronize(s));
 }
 

@@ -35,6 +35,10 @@ struct SearchArgs {
   // epsilon by the index's AccuracyTable (lib/NGT/Index.h:1700-1702); the reference's
   // C API never passes it, so only the batched extensions set it
   float accuracy = -1.0f;
+  // >= 1: the C++ API's refinement expansion (GraphIndex::search(SearchQuery&),
+  // lib/NGT/Index.h:1146-1236): size x expansion results re-ranked by exact distances
+  // over the index's refinement objects (robj) to the size best
+  float refinement_expansion = 0.0f;
 };
 
 // Query element type accepted at the boundary.
@@ -127,6 +131,10 @@ class GraphEngine {
   // queries coalesced so far and launches they took (statistics)
   uint64_t coalesced_queries() const { return co_queries_; }
   uint64_t coalesced_launches() const { return co_launches_; }
+  // search() of arguments with a refinement expansion (all of them): the expanded
+  // search, then the exact re-rank over the refinement objects
+  void search_refined(const void* queries, QueryType qt, size_t nq, size_t qdim, const SearchArgs* args,
+                      size_t nargs, SearchOutput& out, Kernel kernel);
   void search(const void* queries, QueryType qt, size_t nq, size_t qdim, const SearchArgs* args, size_t nargs,
               SearchOutput& out, Kernel kernel = Kernel::Exact);
   // Quantized graph (<index>/qg): loads it on first use; throws when the index
@@ -332,6 +340,7 @@ class GraphEngine {
     size_t grid = 0;
   };
   std::vector<QbgScratch> qbg_scratch_;
+  void* d_robj_ = nullptr;                 // refinement objects on the device (uploaded on first use)
   // coalescing of single-query calls
   struct CoalescedCall {
     std::vector<uint8_t> row;

@@ -272,6 +272,30 @@ static void read_tree(const std::string& path, HostIndex& ix) {
     if (id == 0 || id >= ix.nrows) fail("tree leaf holds an invalid object id in " + path);
 }
 
+// The refinement object file robj (lib/NGT/Index.cpp:1207, ObjectSpace::deserialize): the
+// object-file layout of float rows of the user dimension.  Absent, or holding only the
+// count, when the index has no refinement objects.
+static void read_refinement(const std::string& path, HostIndex& ix) {
+  std::ifstream f(path, std::ios::binary | std::ios::ate);
+  if (!f.is_open() || (size_t)f.tellg() <= 8) return;
+  if (ix.prop.get("RefinementObjectType", "Float-4") != "Float-4") return;
+  f.close();
+  Reader r(path);
+  uint64_t n = r.get<uint64_t>();
+  if (n == 0 || n > 0xFFFFFFF0ull) fail("invalid object count in " + path);
+  const uint32_t d = (uint32_t)ix.prop.dimension;
+  ix.rdim_pad = (d + 3) / 4 * 4;
+  ix.robj.assign((size_t)n * ix.rdim_pad, 0.f);
+  for (uint64_t i = 0; i < n; i++) {
+    char t = r.get<char>();
+    if (t == '-') continue;
+    if (t != '+') fail("corrupted refinement object file " + path);
+    std::memcpy(ix.robj.data() + i * ix.rdim_pad, r.take((size_t)d * 4), (size_t)d * 4);
+  }
+  if (!r.at_end()) fail("trailing bytes in refinement object file " + path);
+  ix.robj_rows = (uint32_t)n;
+}
+
 void load_index(const std::string& dir, HostIndex& ix) {
   ix.path = dir;
   ix.prop = load_property(dir);
@@ -279,6 +303,7 @@ void load_index(const std::string& dir, HostIndex& ix) {
   ix.dpad = ((ix.dim - 1) / 16 + 1) * 16;
   read_objects(dir + "/obj", ix);
   read_graph(dir + "/grp", ix);
+  read_refinement(dir + "/robj", ix);
   if (ix.prop.has_tree) {
     read_tree(dir + "/tre", ix);
   }

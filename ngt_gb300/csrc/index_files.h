@@ -72,6 +72,10 @@ struct HostIndex {
   std::vector<uint32_t> offsets;    // CSR of the graph, nrows+1 entries
   std::vector<uint32_t> edges;
   HostTree tree;
+  // refinement objects (robj, RefinementObjectType Float-4): float rows of rdim_pad
+  // elements (the user dimension rounded up to 4), slot 0 unused; empty when absent
+  std::vector<float> robj;
+  uint32_t robj_rows = 0, rdim_pad = 0;
   size_t elem_size() const { return objtype_size(prop.otype); }
   size_t row_bytes() const { return (size_t)dpad * elem_size(); }
 };

@@ -35,4 +35,14 @@ QBGRefineKernelFn qbg_refine_kernel_for(bool uint8_rows) {
   return uint8_rows ? &qbg_refine_kernel<ObjType::Uint8> : &qbg_refine_kernel<ObjType::Float>;
 }
 
+QBGRefineKernelFn graph_refine_kernel_for(Metric m) {
+  switch (m) {
+    case Metric::L1: return &qbg_refine_kernel<ObjType::Float, Metric::L1>;
+    case Metric::L2: return &qbg_refine_kernel<ObjType::Float, Metric::L2>;
+    case Metric::Angle: return &qbg_refine_kernel<ObjType::Float, Metric::Angle>;
+    case Metric::Cosine: return &qbg_refine_kernel<ObjType::Float, Metric::Cosine>;
+    default: return nullptr;
+  }
+}
+
 }  // namespace ngtg

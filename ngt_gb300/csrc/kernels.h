@@ -38,6 +38,9 @@ typedef void (*QBGRefineKernelFn)(const ObjDist*, const uint32_t*, uint32_t, con
                                   uint32_t, uint32_t, uint32_t, const uint32_t*, uint32_t, uint32_t, ObjDist*,
                                   uint32_t, uint32_t*);
 QBGRefineKernelFn qbg_refine_kernel_for(bool uint8_rows);
+// The same re-rank over a graph index's float refinement objects with its distance
+// (L1, L2, angle, cosine; nullptr for the others).
+QBGRefineKernelFn graph_refine_kernel_for(Metric m);
 
 struct WideConfig;
 typedef void (*WideKernelFn)(DevGraph, const uint4*, const uint4*, uint32_t, const QueryParams*, const uint32_t*,

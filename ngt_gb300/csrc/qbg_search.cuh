@@ -564,7 +564,9 @@ qbg_scan_kernel(DevQG qb, const uint32_t* __restrict__ blob_sid, const uint4* __
 // over the object list (rows of `orc` 16-byte chunks, row 0 unused; the float query
 // cast element-wise to the row type, as setObject does), are sorted by (distance,
 // id) and the first min(exact[q], n) written to out[q * kmax ..].
-template <ObjType OT>
+// M: the comparator (L2 for QBG; the index's distance for a graph index's refinement
+// objects, lib/NGT/Index.h:1146-1236).
+template <ObjType OT, Metric M = Metric::L2>
 __global__ void __launch_bounds__(256)
 qbg_refine_kernel(const ObjDist* __restrict__ cand, const uint32_t* __restrict__ cand_count, uint32_t cstride,
                   const float* __restrict__ qrows, uint32_t qdim, const uint4* __restrict__ olist, uint32_t orc,
@@ -595,8 +597,8 @@ qbg_refine_kernel(const ObjDist* __restrict__ cand, const uint32_t* __restrict__
       const bool valid = i < n;
       const uint32_t id = valid ? cand[(size_t)q * cstride + i].id : 0u;
       const bool inrange = id > 0 && id < nrows;
-      const float d = group_distance<OT, Metric::L2>(qv, olist + (size_t)(inrange ? id : 0u) * orc, (int)orc,
-                                                     (int)gl, (int)G);
+      const float d = group_distance<OT, M>(qv, olist + (size_t)(inrange ? id : 0u) * orc, (int)orc, (int)gl,
+                                            (int)G);
       if (valid && gl == 0) keys[i] = pack_key(inrange ? d : FLT_MAX, id);
     }
     __syncthreads();

@@ -134,6 +134,14 @@ class IndexFiles:
         if self.has_tree:
             self._read_tre()
 
+    def refinement_objects(self):
+        """The float refinement objects (robj) of the index, or None: rows of the user
+        dimension, slot 0 unused (lib/NGT/Index.cpp:1207)."""
+        p = os.path.join(self.path, "robj")
+        if not os.path.exists(p) or os.path.getsize(p) <= 8:
+            return None
+        return _read_rows(p, self.dimension)
+
     def _read_obj(self):
         buf = open(os.path.join(self.path, "obj"), "rb").read()
         n = int(np.frombuffer(buf, np.uint64, 1, 0)[0])
@@ -440,6 +448,28 @@ class Oracle:
                                      sc.ctypes.data if sc is not None else None, threads)
         w = max(k, int(n.max()) if nq else 0, 1)
         return ids[:, :w], ds[:, :w], n, dc
+
+    def search_refined(self, queries, k=10, epsilon=0.1, expansion=2.0, mode="read_only", threads=1):
+        """GraphIndex::search(SearchQuery&) with a refinement expansion (lib/NGT/Index.h:
+        1146-1236): the search keeps k x expansion results, which are re-ranked by the
+        exact L2 distance over the float refinement objects; the k best by (distance, id)."""
+        R = self.f.refinement_objects()
+        size = int(np.float32(k) * np.float32(expansion))
+        ids, ds, n, dc = self.search(queries, k=size, epsilon=epsilon, mode=mode, threads=threads)
+        q = np.ascontiguousarray(queries, np.float32)
+        nq = q.shape[0]
+        out_i = np.zeros((nq, k), np.uint32)
+        out_d = np.zeros((nq, k), np.float32)
+        out_n = np.zeros(nq, np.uint32)
+        for j in range(nq):
+            c = ids[j, :n[j]]
+            d = np.array([self.lib.oracle_distance(0, 1, q[j].ctypes.data, np.ascontiguousarray(R[i]).ctypes.data,
+                                                   R.shape[1]) for i in c], np.float32)
+            order = np.lexsort((c, d))[:k]
+            out_n[j] = len(order)
+            out_i[j, :len(order)] = c[order]
+            out_d[j, :len(order)] = d[order]
+        return out_i, out_d, out_n
 
     def _qg(self, blobs_path=None):
         if self.qg is None:

@@ -3,7 +3,7 @@
 // in this directory) through its own C API (lib/NGT/Capi.h) and dumps the
 // results in binary, so tests/golden/make_golden.py can record golden vectors.
 //
-// usage: ref_dump <graph|linear|range|graph_acc|qg|qbg> <index> <queries.f32> <nq> <dim> <k> <eps> <edge_size|x> <ro|rw> <out>
+// usage: ref_dump <graph|linear|range|graph_acc|graph_refine|qg|qbg> <index> <queries.f32> <nq> <dim> <k> <eps> <edge_size|x> <ro|rw> <out>
 //   out: nq x k uint32 ids, then nq x k float distances, then nq uint32 counts.
 //   For qg the edge_size argument is the result expansion (ngtqg_search_index_float).
 //   For qbg it is "expansion:explored_blobs:blob_epsilon" (qbg_search_index_float),
@@ -123,10 +123,13 @@ int main(int argc, char** argv) {
     std::fclose(o);
     return 0;
   }
-  if (op == "graph_acc") {
+  if (op == "graph_acc" || op == "graph_refine") {
     // the C++ API's expected accuracy (SearchContainer::setExpectedAccuracy; the C API
     // ignores NGTQuery::accuracy): epsilon from the index's AccuracyTable
-    // (lib/NGT/Index.h:1700-1702); the edge argument holds the accuracy
+    // (lib/NGT/Index.h:1700-1702); or its refinement expansion (SearchQuery::
+    // setRefinementExpansion: k x expansion results re-ranked over the refinement
+    // objects, lib/NGT/Index.h:1146-1236); the edge argument holds the accuracy or the
+    // expansion
     NGT::Index cindex(index_path, ro);
     const float acc = std::strtof(argv[8], nullptr);
     for (size_t i = 0; i < nq; i++) {
@@ -135,7 +138,8 @@ int main(int argc, char** argv) {
       NGT::SearchQuery sc(qv);
       sc.setSize(k);
       sc.setEpsilon(eps);
-      sc.setExpectedAccuracy(acc);
+      if (op == "graph_refine") sc.setRefinementExpansion(acc);
+      else sc.setExpectedAccuracy(acc);
       cindex.search(sc);
       auto& rs = sc.getWorkingResult();          // a max-heap of (distance, id)
       std::vector<NGT::ObjectDistance> v;

@@ -135,6 +135,16 @@ FIXTURES = {
         settings=[("range", 100, 0.1, 110.0, "ro"), ("range", 100, 0.1, 130.0, "rw"), ("range", 20, 0.0, 120.0, "ro"),
                   ("graph_acc", 10, 0.1, 0.85, "ro"), ("graph_acc", 10, 0.1, 0.97, "ro"),
                   ("graph_acc", 20, 0.1, 0.995, "rw"), ("graph_acc", 10, 0.1, 0.5, "ro")]),
+    # Refinement objects (lib/NGT/Index.h:1146-1236): int8-code objects searched with
+    # k x expansion results, re-ranked by exact distances over float refinement objects
+    # (robj; `ngt create -R f` empty, then `ngt append -D r` fills objects and refinement
+    # objects); the edge column holds the refinement expansion (the C++ API only)
+    "qs8_l2_refine": dict(
+        base=("gaussian_mixture", dict(n=2000, dim=32, nclusters=16, seed_means=271, seed=272)),
+        query=("gaussian_mixture", dict(n=200, dim=32, nclusters=16, seed_means=271, seed=273)),
+        create="-d 32 -o qsu8 -R f -D 2 -E 10 -S 40 -i t", append="-D r", regenerate_obj=False, otype="q",
+        settings=[("graph_refine", 10, 0.1, 2.0, "ro"), ("graph_refine", 10, 0.05, 4.0, "ro"),
+                  ("graph_refine", 20, 0.1, 1.5, "rw"), ("graph", 10, 0.1, None, "ro")]),
     # Scalar-quantized objects (ObjectType QSUInteger-8B): int8 codes
     # rint(x / QuantizationScale x 127.5), the query quantized the same way
     "qs8_l2": dict(
@@ -299,7 +309,8 @@ def make(name: str, spec: dict) -> None:
         idx = os.path.join(tmp, "idx")
         if spec.get("append"):
             run([os.path.join(REF, "ngt"), "create"] + spec["create"].split() + [idx])
-            run([os.path.join(REF, "ngt"), "append", idx, tsv])
+            extra = spec["append"].split() if isinstance(spec["append"], str) else []
+            run([os.path.join(REF, "ngt"), "append"] + extra + [idx, tsv])
         else:
             run([os.path.join(REF, "ngt"), "create"] + spec["create"].split() + [idx, tsv])
         if "reconstruct" in spec:
@@ -327,8 +338,10 @@ def make(name: str, spec: dict) -> None:
                     info.mtime, info.uid, info.gid, info.uname, info.gname = 0, 0, 0, "", ""
                     with open(os.path.join(qgdir, m), "rb") as fi:
                         tf.addfile(info, fi)
-        for fn in ("grp", "tre", "obj"):
+        for fn in ("grp", "tre", "obj", "robj"):
             src = os.path.join(idx, fn)
+            if fn == "robj" and (not os.path.exists(src) or os.path.getsize(src) <= 8):
+                continue
             if not os.path.exists(src) or (fn == "obj" and spec["regenerate_obj"]):
                 continue
             with open(src, "rb") as fi, gzip.GzipFile(os.path.join(out, fn + ".gz"), "wb", mtime=0) as fo:

@@ -53,7 +53,7 @@ def materialize(name: str, root: str):
     if not os.path.exists(os.path.join(out, "obj")):
         os.makedirs(out, exist_ok=True)
         shutil.copy(os.path.join(src, "prf"), out)
-        for fn in ("grp", "tre", "obj"):
+        for fn in ("grp", "tre", "obj", "robj"):
             p = os.path.join(src, fn + ".gz")
             if os.path.exists(p):
                 with gzip.open(p) as fi, open(os.path.join(out, fn), "wb") as fo:

@@ -51,6 +51,13 @@ def test_batch_search_matches_reference(name, workdir):
                                                       epsilon=s["epsilon"])
                 ids = np.pad(ids, ((0, 0), (0, max(0, k - ids.shape[1]))))
                 ds = np.pad(ds, ((0, 0), (0, max(0, k - ds.shape[1]))))
+            elif s["op"] == "graph_refine":
+                # the C++ API's refinement expansion (the edge column): k x expansion results
+                # re-ranked by exact distances over the refinement objects
+                ids, ds, n = ix.batch_search_refined(queries[:nq], k=k, expansion=s["edge_size"],
+                                                     epsilon=s["epsilon"])
+                ids = np.pad(ids, ((0, 0), (0, max(0, k - ids.shape[1]))))
+                ds = np.pad(ds, ((0, 0), (0, max(0, k - ds.shape[1]))))
             elif s["op"] == "range":
                 # range search: at most k results within the radius (the edge column)
                 ids, ds, n = ix.batch_search(queries[:nq], k=k, epsilon=s["epsilon"], radius=s["edge_size"])
@@ -70,6 +77,16 @@ def test_batch_search_matches_reference(name, workdir):
                 ids = np.pad(ids, ((0, 0), (0, max(0, k - ids.shape[1]))))
                 ds = np.pad(ds, ((0, 0), (0, max(0, k - ds.shape[1]))))
         _check(name, s, ids, ds, n, gi, gd, gc)
+
+
+def test_refined_search_needs_refinement_objects(workdir):
+    """An index without refinement objects refuses a refined search with an error."""
+    from ngt_gb300 import Index
+    from ngt_gb300.base import NativeError
+    path, meta, queries, golden = materialize("c1_f32_l2", workdir)
+    with Index(path, read_only=True) as ix:
+        with pytest.raises(NativeError, match="refinement objects"):
+            ix.batch_search_refined(queries[:4], k=10, expansion=2.0)
 
 
 @pytest.mark.parametrize("name", ["c1_f32_l2", "u8_l2", "qs8_l2"])

@@ -32,6 +32,9 @@ def test_oracle_matches_reference_golden(name, workdir):
         gi, gd, gc = golden["ids_%d" % i], golden["dist_%d" % i], golden["count_%d" % i]
         if s["op"] == "linear":
             ids, ds, n = o.linear_search(queries[:nq], k=k, threads=4)
+        elif s["op"] == "graph_refine":
+            ids, ds, n = o.search_refined(queries[:nq], k=k, epsilon=s["epsilon"], expansion=s["edge_size"],
+                                          mode="read_only" if s["mode"] == "ro" else "updatable", threads=4)
         elif s["op"] in ("range", "graph_acc"):
             # range search: the radius in the edge column; expected accuracy: the epsilon
             # comes from the index's AccuracyTable
