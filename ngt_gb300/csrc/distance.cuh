@@ -85,6 +85,17 @@ struct Acc {
         i0 += (uint32_t)(__dp4a(qa[i], qa[i], 0) + __dp4a(xa[i], xa[i], 0));
         i1 += (uint32_t)__dp4a(qa[i], xa[i], 0);
       }
+    } else if constexpr (OT == ObjType::Qsint8 && (M == Metric::InnerProduct || M == Metric::NormalizedCosine)) {
+      // signed query codes . unsigned stored codes (the codes shifted by 127), exact;
+      // i0 counts the elements (the padded dimension the reference's constant uses)
+      const uint32_t qa[4] = {q.x, q.y, q.z, q.w}, xa[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+      for (int i = 0; i < 4; i++) {
+        int r;
+        asm("dp4a.s32.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(qa[i]), "r"(xa[i]), "r"(0));
+        i1 += (uint32_t)r;
+      }
+      i0 += 16u;
     } else if constexpr (OT == ObjType::Uint8 && M == Metric::L1) {
       i0 += __vsadu4(q.x, x.x) + __vsadu4(q.y, x.y) + __vsadu4(q.z, x.z) + __vsadu4(q.w, x.w);
     } else if constexpr (M == Metric::Hamming) {
@@ -130,11 +141,13 @@ struct Acc {
   }
 
   // Which accumulators a metric uses (only those are reduced across lanes).
-  static constexpr bool kUint8Sq = (OT == ObjType::Uint8 && (M == Metric::L2 || M == Metric::InnerProduct)) ||
-                                   (OT == ObjType::Qsint8 && M == Metric::L2);
-  static constexpr bool kUseI0 = kUint8Sq || (OT == ObjType::Uint8 && M == Metric::L1) || M == Metric::Hamming ||
-                                 M == Metric::Jaccard;
-  static constexpr bool kUseI1 = kUint8Sq || M == Metric::Jaccard;
+  static constexpr bool kUint8Sq =
+      (OT == ObjType::Uint8 && (M == Metric::L2 || M == Metric::InnerProduct || M == Metric::Quint8L2)) ||
+      (OT == ObjType::Qsint8 && M == Metric::L2);
+  static constexpr bool kQsDot = OT == ObjType::Qsint8 && (M == Metric::InnerProduct || M == Metric::NormalizedCosine);
+  static constexpr bool kUseI0 = kUint8Sq || kQsDot || (OT == ObjType::Uint8 && M == Metric::L1) ||
+                                 M == Metric::Hamming || M == Metric::Jaccard;
+  static constexpr bool kUseI1 = kUint8Sq || kQsDot || M == Metric::Jaccard;
   static constexpr bool kUseF0 = !kUseI0;
   static constexpr bool kUseF12 = !kUseI0 && (M == Metric::Cosine || M == Metric::Angle || M == Metric::Poincare);
 
@@ -176,6 +189,14 @@ struct Acc {
       // the squared sum itself: PrimitiveComparator::compareL2(qsint8) of the x86
       // build (lib/NGT/PrimitiveComparatorX86.h:341-431) takes no square root
       return (float)(int)(i0 - 2u * i1);
+    } else if constexpr (kQsDot) {
+      // 127*127*n (inner product) or 127*255*n (normalized cosine) minus the dot product,
+      // n the padded dimension (PrimitiveComparator::InnerProductQsint8,
+      // NormalizedCosineSimilarityQsint8, lib/NGT/PrimitiveComparator.h:376-404)
+      const long long c = (M == Metric::InnerProduct ? 127ll * 127ll : 127ll * 255ll) * (long long)i0;
+      return (float)(c - (long long)(int)i1);
+    } else if constexpr (OT == ObjType::Uint8 && M == Metric::Quint8L2) {
+      return (float)(i0 - 2u * i1);    // the squared sum (the reference's quint8 L2 takes no root)
     } else if constexpr (OT == ObjType::Uint8 && (M == Metric::L2 || M == Metric::InnerProduct)) {
       return sqrtf((float)(i0 - 2u * i1));
     } else if constexpr (OT == ObjType::Uint8 && M == Metric::L1) {
@@ -237,13 +258,31 @@ __device__ __forceinline__ float group_distance(const uint4* __restrict__ q, con
   return acc.finish();
 }
 
-// Orderable 64-bit key for (distance, id): distances are >= 0 for every metric,
-// so their IEEE bits order like unsigned integers (-0 is folded to +0).
-__device__ __forceinline__ unsigned long long pack_key(float d, uint32_t id) {
-  uint32_t b = (d == 0.0f) ? 0u : __float_as_uint(d);
-  return ((unsigned long long)b << 32) | id;
+// Monotone map of a float to unsigned bits (negative distances occur: the
+// scalar-quantized inner product), -0 folded to +0; +inf maps to 0xff800000.
+__device__ __forceinline__ uint32_t order_bits(float d) {
+  const uint32_t b = __float_as_uint(d == 0.0f ? 0.0f : d);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
 }
-__device__ __forceinline__ float key_dist(unsigned long long k) { return __uint_as_float((uint32_t)(k >> 32)); }
+__device__ __forceinline__ float order_float(uint32_t o) {
+  return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
+}
+
+// Orderable 64-bit key for (distance, id).
+__device__ __forceinline__ unsigned long long pack_key(float d, uint32_t id) {
+  return ((unsigned long long)order_bits(d) << 32) | id;
+}
+__device__ __forceinline__ float key_dist(unsigned long long k) { return order_float((uint32_t)(k >> 32)); }
+
+// The comparator of the DVP tree: the search comparator, except for scalar-quantized
+// inner-product and normalized-cosine indexes (ObjectSpaceRepository.h:727-745: the
+// squared L2 over unsigned bytes, the query's signed codes read as unsigned).
+template <ObjType OT, Metric M>
+struct TreeSpace {
+  static constexpr bool kQuint8 = OT == ObjType::Qsint8 && (M == Metric::InnerProduct || M == Metric::NormalizedCosine);
+  static constexpr ObjType ot = kQuint8 ? ObjType::Uint8 : OT;
+  static constexpr Metric m = kQuint8 ? Metric::Quint8L2 : M;
+};
 __device__ __forceinline__ uint32_t key_id(unsigned long long k) { return (uint32_t)k; }
 
 }  // namespace ngtg

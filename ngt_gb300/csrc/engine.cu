@@ -51,7 +51,7 @@ uint32_t next_pow2(uint32_t v) {
 }
 
 ExactKernelFn exact_kernel(ObjType t, Metric m) {
-  m = kernel_metric(m);
+  if (t != ObjType::Qsint8) m = kernel_metric(m);   // qsint8 inner product: its own comparator
   switch (t) {
     case ObjType::Float: return exact_kernel_float(m);
     case ObjType::Float16: return exact_kernel_half(m);
@@ -62,7 +62,7 @@ ExactKernelFn exact_kernel(ObjType t, Metric m) {
 }
 
 LinearKernelFn linear_kernel(ObjType t, Metric m) {
-  m = kernel_metric(m);
+  if (t != ObjType::Qsint8) m = kernel_metric(m);   // qsint8 inner product: its own comparator
   switch (t) {
     case ObjType::Float: return linear_kernel_float(m);
     case ObjType::Float16: return linear_kernel_half(m);
@@ -173,6 +173,13 @@ GraphEngine::GraphEngine(const std::string& qbg_dir, bool blobs) : mode_(GraphMo
 GraphEngine::~GraphEngine() {
   cudaSetDevice(device_);
   if (staging_) cudaFreeHost(staging_);
+  for (auto& l : co_lanes_) {
+    if (l.stream) cudaStreamSynchronize(l.stream);
+    cudaFree(l.bitmaps);
+    cudaFree(l.overflow);
+    if (l.staging) cudaFreeHost(l.staging);
+    if (l.stream) cudaStreamDestroy(l.stream);
+  }
   cudaFree(d_objects_);
   cudaFree(d_offsets_);
   cudaFree(d_edges_);
@@ -488,8 +495,17 @@ void GraphEngine::convert_queries(const void* queries, QueryType qt, size_t nq, 
       }
       case ObjType::Qsint8: {
         // ObjectSpace::quantizeSymmetrically (lib/NGT/ObjectSpace.h:432-441): the
-        // division in float, the product with 127.5 and the rounding in double
+        // division in float, the product with 127.5 and the rounding in double; under a
+        // normalized distance the float query is normalized first
+        // (ObjectSpaceRepository::allocateNormalizedObject, ObjectSpaceRepository.h:1120-1160)
         const float scale = host_.prop.quantization_scale;
+        if (norm) {
+          float sum = 0.0f;
+          for (size_t i = 0; i < qdim; i++) sum += tmp[i] * tmp[i];
+          if (sum == 0.0f) throw std::runtime_error("the query is a zero vector; it cannot be normalized");
+          sum = (float)std::sqrt(sum);
+          for (size_t i = 0; i < qdim; i++) tmp[i] = tmp[i] / sum;
+        }
         for (size_t i = 0; i < qdim; i++) {
           float fv = tmp[i];
           fv = (float)std::round((double)(fv / scale) * 127.5);
@@ -976,15 +992,23 @@ void GraphEngine::search_one(const void* query, QueryType qt, size_t qdim, const
   std::unique_lock<std::mutex> lock(co_mu_);
   co_pending_.push_back(call);
   while (!call->done) {
-    if (!co_busy_) {
-      // this caller launches everything waiting, its own query included
-      co_busy_ = true;
+    CoLane* lane = nullptr;
+    if (!co_pending_.empty())
+      for (auto& l : co_lanes_)
+        if (!l.busy) {
+          lane = &l;
+          break;
+        }
+    if (lane) {
+      // a free lane: this caller launches everything waiting (its own query, unless a
+      // caller before it took that one already)
+      lane->busy = true;
       std::vector<std::shared_ptr<CoalescedCall>> batch;
       batch.swap(co_pending_);
       lock.unlock();
       std::string err;
       try {
-        run_coalesced(batch);
+        run_coalesced(batch, *lane);
       } catch (std::exception& ex) {
         err = ex.what();
       }
@@ -993,7 +1017,7 @@ void GraphEngine::search_one(const void* query, QueryType qt, size_t qdim, const
         c->error = err;
         c->done = true;
       }
-      co_busy_ = false;
+      lane->busy = false;
       co_cv_.notify_all();
     } else {
       co_cv_.wait(lock);
@@ -1004,9 +1028,23 @@ void GraphEngine::search_one(const void* query, QueryType qt, size_t qdim, const
   out = std::move(call->out);
 }
 
-void GraphEngine::run_coalesced(std::vector<std::shared_ptr<CoalescedCall>>& batch) {
+void GraphEngine::run_coalesced(std::vector<std::shared_ptr<CoalescedCall>>& batch, CoLane& lane) {
   NGT_CUDA(cudaSetDevice(device_));
   const size_t nq = batch.size(), rb = host_.row_bytes();
+  const size_t words = (host_.nrows + 31) / 32;
+  if (!lane.stream) {
+    NGT_CUDA(cudaStreamCreateWithFlags(&lane.stream, cudaStreamNonBlocking));
+    NGT_CUDA(cudaMalloc(&lane.bitmaps, kLaneCtas * words * 4));
+    NGT_CUDA(cudaMemsetAsync(lane.bitmaps, 0, kLaneCtas * words * 4, lane.stream));
+    NGT_CUDA(cudaMalloc(&lane.overflow, kLaneCtas * 2 * (size_t)kOverflowCapacity * 8));
+  }
+  if (lane.staging_bytes < nq * rb) {
+    if (lane.staging) NGT_CUDA(cudaFreeHost(lane.staging));
+    lane.staging = nullptr;
+    lane.staging_bytes = 0;
+    NGT_CUDA(cudaMallocHost(&lane.staging, nq * rb));
+    lane.staging_bytes = nq * rb;
+  }
   std::vector<SearchArgs> args(nq);
   size_t kmax = 1;
   for (size_t i = 0; i < nq; i++) {
@@ -1017,26 +1055,35 @@ void GraphEngine::run_coalesced(std::vector<std::shared_ptr<CoalescedCall>>& bat
   std::vector<uint32_t> counts(nq);
   std::vector<QueryStats> stats(nq);
   {
-    std::lock_guard<std::mutex> staging(staging_mu_);
-    if (staging_bytes_ < nq * rb) {
-      if (staging_) NGT_CUDA(cudaFreeHost(staging_));
-      staging_ = nullptr;
-      staging_bytes_ = 0;
-      NGT_CUDA(cudaMallocHost(&staging_, nq * rb));
-      staging_bytes_ = nq * rb;
-    }
-    for (size_t i = 0; i < nq; i++) std::memcpy(static_cast<uint8_t*>(staging_) + i * rb, batch[i]->row.data(), rb);
+    for (size_t i = 0; i < nq; i++)
+      std::memcpy(static_cast<uint8_t*>(lane.staging) + i * rb, batch[i]->row.data(), rb);
     uint4* d_rows = nullptr;
     ObjDist* d_out = nullptr;
     uint32_t* d_counts = nullptr;
     QueryStats* d_stats = nullptr;
-    cudaStream_t s = stream_;
+    QueryParams* d_params = nullptr;
+    uint32_t* d_seeds = nullptr;
+    cudaStream_t s = lane.stream;
+    std::vector<QueryParams> params;
+    std::vector<uint32_t> seeds;
+    uint32_t max_size = 0;
+    build_params(args.data(), nq, nq, kmax, params, seeds, max_size);
     NGT_CUDA(cudaMallocAsync(&d_rows, nq * rb, s));
     NGT_CUDA(cudaMallocAsync(&d_out, nq * kmax * sizeof(ObjDist), s));
     NGT_CUDA(cudaMallocAsync(&d_counts, nq * 4, s));
     NGT_CUDA(cudaMallocAsync(&d_stats, nq * sizeof(QueryStats), s));
-    NGT_CUDA(cudaMemcpyAsync(d_rows, staging_, nq * rb, cudaMemcpyHostToDevice, s));
-    search_device(d_rows, nq, args.data(), nq, d_out, d_counts, d_stats, kmax, s, Kernel::Exact);
+    NGT_CUDA(cudaMallocAsync(&d_params, nq * sizeof(QueryParams), s));
+    NGT_CUDA(cudaMallocAsync(&d_seeds, seeds.size() * 4, s));
+    NGT_CUDA(cudaMemcpyAsync(d_rows, lane.staging, nq * rb, cudaMemcpyHostToDevice, s));
+    NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QueryParams), cudaMemcpyHostToDevice, s));
+    NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, s));
+    {
+      std::lock_guard<std::mutex> lock(mu_);
+      launch_exact(d_rows, nq, d_params, d_seeds, max_size, d_out, d_counts, d_stats, s, lane.bitmaps,
+                   lane.overflow, kLaneCtas);
+    }
+    NGT_CUDA(cudaFreeAsync(d_params, s));
+    NGT_CUDA(cudaFreeAsync(d_seeds, s));
     NGT_CUDA(cudaMemcpyAsync(res.data(), d_out, nq * kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, s));
     NGT_CUDA(cudaMemcpyAsync(counts.data(), d_counts, nq * 4, cudaMemcpyDeviceToHost, s));
     NGT_CUDA(cudaMemcpyAsync(stats.data(), d_stats, nq * sizeof(QueryStats), cudaMemcpyDeviceToHost, s));

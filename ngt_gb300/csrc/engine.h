@@ -349,12 +349,24 @@ class GraphEngine {
     bool done = false;
     std::string error;
   };
+  // A lane is one exact-kernel launch in flight: its own stream, visited bitmaps and
+  // overflow lists (kLaneCtas CTAs), and pinned query staging.  Several lanes run at
+  // once, so one slow query does not hold back the calls that arrive after it.
+  struct CoLane {
+    cudaStream_t stream = nullptr;
+    uint32_t* bitmaps = nullptr;
+    unsigned long long* overflow = nullptr;
+    void* staging = nullptr;
+    size_t staging_bytes = 0;
+    bool busy = false;
+  };
+  static constexpr size_t kCoLanes = 8, kLaneCtas = 16;
   std::mutex co_mu_;
   std::condition_variable co_cv_;
   std::vector<std::shared_ptr<CoalescedCall>> co_pending_;
-  bool co_busy_ = false;
+  CoLane co_lanes_[kCoLanes];
   std::atomic<uint64_t> co_queries_{0}, co_launches_{0};
-  void run_coalesced(std::vector<std::shared_ptr<CoalescedCall>>& batch);
+  void run_coalesced(std::vector<std::shared_ptr<CoalescedCall>>& batch, CoLane& lane);
   QbgScratch& qbg_slot(size_t slot, size_t grid, cudaStream_t stream);
   size_t qbg_grid_ = 0;
   uint32_t qbg_ocap_ = 0;

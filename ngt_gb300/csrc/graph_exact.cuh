@@ -246,7 +246,7 @@ graph_search_exact_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_
         int depth = 0;
         while (!(node & 0x80000000u) && depth < 64) {
           const DevInternal& in = g.internals[node];
-          float d = group_distance<OT, M>(qv, g.pivots + (size_t)in.pivot * rc, (int)rc, lane, 32);
+          float d = group_distance<TreeSpace<OT, M>::ot, TreeSpace<OT, M>::m>(qv, g.pivots + (size_t)in.pivot * rc, (int)rc, lane, 32);
           uint32_t bsize = in.nchildren - 1, mid;
           for (mid = 0; mid < bsize; mid++)
             if (d < in.borders[mid]) break;

@@ -126,9 +126,10 @@ Property load_property(const std::string& dir) {
   p.graph_type = p.get("GraphType", "ANNG");
   if (p.metric == Metric::SparseJaccard) fail("SparseJaccard indexes are not supported");
   if (p.otype == ObjType::Qsint8) {
-    // the quantized objects' search comparators other than L2 compare against
-    // differently coded queries (lib/NGT/PrimitiveComparator.h:376-404); L2 only here
-    if (p.metric != Metric::L2) fail("QSUInteger-8B objects are supported with the L2 distance only");
+    // the read-only search specializes L2, the inner product and the normalized cosine
+    // for these objects (lib/NGT/Graph.h:357-363); the others are not supported here
+    if (p.metric != Metric::L2 && p.metric != Metric::InnerProduct && p.metric != Metric::NormalizedCosine)
+      fail("QSUInteger-8B objects are supported with the L2, inner-product and normalized-cosine distances");
     try {
       p.quantization_scale = std::stof(p.get("QuantizationScale", "0"));
     } catch (...) {
@@ -283,7 +284,9 @@ static void read_refinement(const std::string& path, HostIndex& ix) {
   Reader r(path);
   uint64_t n = r.get<uint64_t>();
   if (n == 0 || n > 0xFFFFFFF0ull) fail("invalid object count in " + path);
-  const uint32_t d = (uint32_t)ix.prop.dimension;
+  // an inner-product index's refinement objects are augmented like its objects
+  // (GraphIndex::constructObjectSpace, lib/NGT/Index.cpp:1127-1189)
+  const uint32_t d = (uint32_t)ix.prop.dimension + (ix.prop.metric == Metric::InnerProduct ? 1u : 0u);
   ix.rdim_pad = (d + 3) / 4 * 4;
   ix.robj.assign((size_t)n * ix.rdim_pad, 0.f);
   for (uint64_t i = 0; i < n; i++) {

@@ -11,7 +11,7 @@ namespace ngtg {
   case Metric::M: return &graph_search_fast_kernel<ObjType::ST, ObjType::OT, Metric::M>;
 
 FastKernelFn fast_kernel(ObjType ot, Metric m, bool bf16_rows, uint32_t rows_in_flight, uint32_t ctas_per_sm) {
-  m = kernel_metric(m);
+  if (ot != ObjType::Qsint8) m = kernel_metric(m);   // qsint8 inner product: its own comparator
   if (rows_in_flight == 0) rows_in_flight = 4;
   if (ctas_per_sm == 0) ctas_per_sm = rows_in_flight > 4 ? 4 : 5;
   if (ot == ObjType::Float && bf16_rows && m == Metric::L2 && !(rows_in_flight == 4 && ctas_per_sm == 5)) {

@@ -5,7 +5,7 @@
 
 namespace ngtg {
 #define NGT_OT ObjType::Qsint8
-#define NGT_METRICS(X) X(L2)
+#define NGT_METRICS(X) X(L2) X(InnerProduct) X(NormalizedCosine)
 #define NGT_SUFFIX qs8
 #include "kern_table.inc"
 }  // namespace ngtg

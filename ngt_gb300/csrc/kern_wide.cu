@@ -6,7 +6,7 @@
 namespace ngtg {
 
 WideKernelFn wide_kernel(ObjType ot, Metric m, SearchRows rows, uint32_t threads) {
-  m = kernel_metric(m);
+  if (ot != ObjType::Qsint8) m = kernel_metric(m);   // qsint8 inner product: its own comparator
   if (threads != 128 && threads != 256) return nullptr;
   if (ot == ObjType::Float && rows == SearchRows::Bf16 && m == Metric::L2)
     return threads == 128 ? &graph_search_wide_kernel<ObjType::Bfloat16, ObjType::Float, Metric::L2, 128>

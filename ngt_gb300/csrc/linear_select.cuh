@@ -5,7 +5,7 @@
 
 namespace ngtg {
 
-__device__ __forceinline__ uint32_t dist_bits(float d) { return d == 0.0f ? 0u : __float_as_uint(d); }
+__device__ __forceinline__ uint32_t dist_bits(float d) { return order_bits(d); }
 
 __global__ void __launch_bounds__(512)
 linear_select_kernel(const float* __restrict__ dist, uint32_t nrows, uint32_t q0, uint32_t nqb, uint32_t k,
@@ -18,7 +18,7 @@ linear_select_kernel(const float* __restrict__ dist, uint32_t nrows, uint32_t q0
   const uint32_t qi = blockIdx.x;
   const uint32_t q = q0 + qi;
   const float* D = dist + (size_t)qi * nrows;
-  const uint32_t inf_bits = 0x7f800000u;
+  const uint32_t inf_bits = 0xff800000u;   // order_bits(+inf); NaN orders above it
   const bool use_radius = radius >= 0.0f;
   auto valid_bits = [&](uint32_t row, uint32_t& bits) -> bool {
     float d = D[row];
@@ -105,7 +105,7 @@ linear_select_kernel(const float* __restrict__ dist, uint32_t nrows, uint32_t q0
   __syncthreads();
   for (uint32_t i = threadIdx.x; i < kk; i += blockDim.x) {
     unsigned long long x = sorted[i];
-    out[(size_t)q * k + i] = ObjDist{(uint32_t)x, __uint_as_float((uint32_t)(x >> 32))};
+    out[(size_t)q * k + i] = ObjDist{(uint32_t)x, order_float((uint32_t)(x >> 32))};
   }
   if (threadIdx.x == 0) out_count[q] = kk;
 }

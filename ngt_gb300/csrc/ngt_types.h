@@ -22,6 +22,10 @@ enum class Metric : int32_t {
   InnerProduct = 10,  // stored as L2 over the (D+1) augmented space
   Poincare = 100,
   Lorentz = 101,
+  // internal only: the squared L2 over unsigned bytes, the tree comparator of
+  // scalar-quantized inner-product and normalized-cosine indexes
+  // (ComparatorL2Quint8Quint8, lib/NGT/ObjectSpaceRepository.h:514-533)
+  Quint8L2 = 200,
 };
 
 // Qsint8: NGT's scalar-quantized objects (ObjectType "QSUInteger-8B",

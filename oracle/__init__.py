@@ -366,7 +366,7 @@ class Oracle:
                                              ctypes.c_size_t, ctypes.c_size_t, ctypes.c_void_p]
         L.oracle_rand_sequence.argtypes = [ctypes.c_uint32, ctypes.c_size_t, ctypes.c_void_p]
         L.oracle_prepare_qsint8.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
-                                            ctypes.c_float, ctypes.c_void_p]
+                                            ctypes.c_float, ctypes.c_int, ctypes.c_void_p]
         L.oracle_distance.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]
         L.oracle_distance.restype = ctypes.c_float
         L.oracle_qg_search.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
@@ -419,7 +419,8 @@ class Oracle:
         rows = np.zeros((q.shape[0], self.f.dpad), self.f.dtype)
         if self.f.otype == 3:
             self.lib.oracle_prepare_qsint8(self.f.dpad, q.ctypes.data, q.shape[0], q.shape[1],
-                                           ctypes.c_float(float(self.f.prop["QuantizationScale"])), rows.ctypes.data)
+                                           ctypes.c_float(float(self.f.prop["QuantizationScale"])),
+                                           1 if self.f.metric_name == "NormalizedCosine" else 0, rows.ctypes.data)
             return rows
         self.lib.oracle_prepare_queries(self.f.otype, self.f.metric, self.f.dpad, q.ctypes.data, q.shape[0],
                                         q.shape[1], rows.ctypes.data)

@@ -108,6 +108,16 @@ static size_t elem_size(int ot) { return ot == OT_FLOAT ? 4 : (ot == OT_UINT8 ||
 
 /* ---------------- comparators ---------------- */
 static float compare(int ot, int metric, const void *a, const void *b, size_t n) {
+  if (ot == OT_QSINT8 && (metric == M_IP || metric == M_NCOSINE)) {
+    /* the signed query codes against the stored codes shifted to unsigned (code + 127):
+     * 127*127*n (inner product) or 127*255*n (normalized cosine) minus their integer dot
+     * product over the n padded elements (PrimitiveComparator::InnerProductQsint8 and
+     * NormalizedCosineSimilarityQsint8, lib/NGT/PrimitiveComparator.h:376-404) */
+    int64_t s = 0;
+    for (size_t i = 0; i < n; i++) s += (int64_t)((const int8_t *)a)[i] * (int64_t)((const uint8_t *)b)[i];
+    double c = metric == M_IP ? 127.0 * 127.0 * (double)n : 127.0 * 255.0 * (double)n;
+    return (float)(c - (double)s);
+  }
   switch (metric) {
     case M_L2:
     case M_IP: {
@@ -295,10 +305,27 @@ void oracle_linear_search(const OracleIndex *ix, const void *qrows, size_t nq, s
 }
 
 /* ---------------- seeds ---------------- */
+/* The tree's comparator (ObjectSpace::getComparator, lib/NGT/Tree.cpp:403-491): the
+ * search comparator, except for scalar-quantized inner-product and normalized-cosine
+ * indexes, whose comparator is the squared L2 over unsigned bytes (ComparatorL2Quint8Quint8,
+ * lib/NGT/ObjectSpaceRepository.h:514-533, 727-745), the query's signed codes read as
+ * unsigned. */
+static float tree_compare(const OracleIndex *ix, const void *q, const void *pivot) {
+  if (ix->otype == OT_QSINT8 && (ix->metric == M_IP || ix->metric == M_NCOSINE)) {
+    int64_t s = 0;
+    for (size_t i = 0; i < ix->dpad; i++) {
+      int64_t x = (int64_t)((const uint8_t *)q)[i] - (int64_t)((const uint8_t *)pivot)[i];
+      s += x * x;
+    }
+    return (float)(double)s;
+  }
+  return compare(ix->otype, ix->metric, q, pivot, ix->dpad);
+}
+
 static size_t tree_seeds(const OracleIndex *ix, const void *q, size_t size, uint32_t *seeds, uint32_t *ndc) {
   uint32_t node = ix->root;
   while (!(node & 0x80000000u)) {
-    float d = compare(ix->otype, ix->metric, q, row_ptr(ix, ix->pivots, ix->in_pivot[node]), ix->dpad);
+    float d = tree_compare(ix, q, row_ptr(ix, ix->pivots, ix->in_pivot[node]));
     (*ndc)++;
     uint32_t bsize = ix->in_nchildren[node] - 1, mid;
     for (mid = 0; mid < bsize; mid++)
@@ -492,17 +519,27 @@ static uint16_t float_to_half(float f) {
 /* Query conversion: cast to the object type, normalise (float sum, sqrt,
  * divide, in the object type) for the normalised metrics. */
 /* qsint8 query codes: round(v / scale x 127.5) clamped to [-127, 127], the division in
- * float and the product and rounding in double (lib/NGT/ObjectSpace.h:432-441). */
-void oracle_prepare_qsint8(uint32_t dpad, const float *q, size_t nq, size_t dim, float scale, int8_t *rows) {
+ * float and the product and rounding in double (lib/NGT/ObjectSpace.h:432-441); under a
+ * normalized distance the float query is normalized first (ObjectSpaceRepository::
+ * allocateNormalizedObject, lib/NGT/ObjectSpaceRepository.h:1120-1160). */
+void oracle_prepare_qsint8(uint32_t dpad, const float *q, size_t nq, size_t dim, float scale, int normalize,
+                           int8_t *rows) {
   memset(rows, 0, nq * dpad);
-  for (size_t i = 0; i < nq; i++)
+  for (size_t i = 0; i < nq; i++) {
+    float s = 1.0f;
+    if (normalize) {
+      volatile float sum = 0.0f;
+      for (size_t j = 0; j < dim; j++) { float p = q[i * dim + j] * q[i * dim + j]; sum = sum + p; }
+      s = (float)sqrt((double)sum);
+    }
     for (size_t j = 0; j < dim; j++) {
-      float fv = q[i * dim + j];
+      float fv = normalize ? q[i * dim + j] / s : q[i * dim + j];
       fv = (float)round((double)(fv / scale) * 127.5);
       fv = fv < -127.0f ? -127.0f : fv;
       fv = fv > 127.0f ? 127.0f : fv;
       rows[i * dpad + j] = (int8_t)fv;
     }
+  }
 }
 
 void oracle_prepare_queries(int ot, int metric, uint32_t dpad, const float *q, size_t nq, size_t dim, void *rows) {

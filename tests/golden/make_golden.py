@@ -153,6 +153,24 @@ FIXTURES = {
         create="-d 32 -o qsu8 -D 2 -E 10 -S 40 -i t", regenerate_obj=False, otype="q",
         settings=[("graph", 10, 0.1, None, "ro"), ("graph", 10, 0.02, None, "ro"), ("graph", 20, 0.2, None, "rw"),
                   ("linear", 10, 0.0, None, "ro")]),
+    # Scalar-quantized objects under the inner product and the normalized cosine: the
+    # stored codes are shifted to unsigned (code + 127) and the search compares the
+    # signed query codes with them by one integer dot product
+    # (ObjectSpaceRepository::isQsint8Quint8, lib/NGT/ObjectSpaceRepository.h:1343-1347;
+    # PrimitiveComparator::InnerProductQsint8 / NormalizedCosineSimilarityQsint8,
+    # lib/NGT/PrimitiveComparator.h:376-404); the tree compares by the unsigned-byte L2.
+    "qs8_ip": dict(
+        base=("gaussian_mixture", dict(n=2000, dim=32, nclusters=16, seed_means=281, seed=282)),
+        query=("gaussian_mixture", dict(n=200, dim=32, nclusters=16, seed_means=281, seed=283)),
+        create="-d 32 -o qsu8 -D i -E 10 -S 40 -i t", append=True, regenerate_obj=False, otype="q",
+        settings=[("graph", 10, 0.1, None, "ro"), ("graph", 10, 0.1, None, "rw"), ("graph", 20, 0.2, None, "ro"),
+                  ("linear", 10, 0.0, None, "ro")]),
+    "qs8_ncosine": dict(
+        base=("gaussian_mixture", dict(n=2000, dim=32, nclusters=16, seed_means=291, seed=292)),
+        query=("gaussian_mixture", dict(n=200, dim=32, nclusters=16, seed_means=291, seed=293)),
+        create="-d 32 -o qsu8 -D C -E 10 -S 40 -i t", regenerate_obj=False, otype="q",
+        settings=[("graph", 10, 0.1, None, "ro"), ("graph", 10, 0.1, None, "rw"), ("graph", 20, 0.2, None, "ro"),
+                  ("linear", 10, 0.0, None, "ro")]),
     # Quantized graphs (ngtqg_search_index_float); for "qg" settings the edge
     # column holds the result expansion.
     "qg_f32_l2_d32": dict(

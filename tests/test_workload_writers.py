@@ -13,14 +13,14 @@ def test_symmetric_quantization_matches_the_oracle():
     from ngt_gb300 import graph_build
     L = ctypes.CDLL(oracle.build())
     L.oracle_prepare_qsint8.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
-                                        ctypes.c_float, ctypes.c_void_p]
+                                        ctypes.c_float, ctypes.c_int, ctypes.c_void_p]
     rng = np.random.default_rng(7)
     x = (rng.standard_normal((300, 32)) * 3).astype(np.float32)
     x[0, :4] = [0.5, -0.5, 2.5, -2.5]                       # halves: rounding away from zero
     for scale in (float(np.abs(x).max()), 127.5, 3.3):
         ours = graph_build.quantize_symmetric(x, scale)
         ref = np.zeros((len(x), 32), np.int8)
-        L.oracle_prepare_qsint8(32, x.ctypes.data, len(x), 32, ctypes.c_float(scale), ref.ctypes.data)
+        L.oracle_prepare_qsint8(32, x.ctypes.data, len(x), 32, ctypes.c_float(scale), 0, ref.ctypes.data)
         assert np.array_equal(ours, ref), scale
 
 
