@@ -243,12 +243,25 @@ int64_t ngtgpu_server_submit(NGTGPUServer, const float *queries, size_t nq, int3
 bool ngtgpu_server_wait(NGTGPUServer, int64_t ticket, NGTObjectDistance *results, size_t kmax, uint32_t *counts,
                         double *latency_ms, NGTError);
 void ngtgpu_server_destroy(NGTGPUServer);
+/* Admission deadlines and cancellation (any server).  A request not launched within
+ * deadline_ms of its submission completes unlaunched: its wait returns false with
+ * "deadline exceeded before launch".  ngtgpu_server_submit_deadline sets it per
+ * request; ngtgpu_server_set_deadline sets the default of later submits (<= 0: none).
+ * ngtgpu_server_cancel withdraws a request not yet launched (true; its wait returns
+ * false with "cancelled"); a request on the device runs to completion (false). */
+int64_t ngtgpu_server_submit_deadline(NGTGPUServer, const float *queries, size_t nq, int32_t dim,
+                                      const NGTQueryParameters *params, size_t nparams, double deadline_ms,
+                                      NGTError);
+bool ngtgpu_server_set_deadline(NGTGPUServer, double deadline_ms, NGTError);
+bool ngtgpu_server_cancel(NGTGPUServer, int64_t ticket, NGTError);
 
 /* The single-query graph searches (ngt_search_index, _as_float, _as_uint8,
- * _as_float16, _with_query*) of concurrent host threads are coalesced: the first
- * caller launches the exact-order kernel at once, callers arriving while a launch
- * runs wait and are launched together by the next of them, so a loop of these calls
- * over many threads (ngtpy's batch_search pattern) fills the GPU.  Every result equals
+ * _as_float16, _with_query*) of concurrent host threads are coalesced: up to eight
+ * exact-order launches run at once, each on its own stream and scratch; a caller
+ * that finds one of them free launches every waiting query at once, and callers
+ * arriving while all eight run wait and are launched together by the next free one,
+ * so a loop of these calls over many threads (ngtpy's batch_search pattern) fills
+ * the GPU.  Every result equals
  * a lone call's.  The queries coalesced so far, and the launches they took. */
 bool ngtgpu_coalescing_stats(NGTIndex, uint64_t *queries, uint64_t *launches, NGTError);
 

@@ -206,6 +206,16 @@ void *ngtgpu_qbg_server_create(QBGIndex index, uint32_t max_batch_queries, uint3
 int64_t ngtgpu_qbg_server_submit(void *server, const float *queries, size_t nq, int32_t dim,
                                  const QBGQueryParameters *params, size_t nparams, QBGError error);
 
+/* The serving loop over a quantized graph (no reference counterpart; it serves the
+ * requests of ngtqg_search_index_float, lib/NGT/NGTQ/Capi.h:68-83): each launch runs
+ * the exact-order quantized-graph kernel over the waiting requests of one
+ * shared-memory class, with per-lane visited bitmaps; results equal
+ * ngtqg_search_index_float's.  Returns an NGTGPUServer (ngtgpu.h). */
+void *ngtgpu_qg_server_create(NGTQGIndex index, uint32_t max_batch_queries, uint32_t inflight, uint32_t max_k,
+                              NGTQGError error);
+int64_t ngtgpu_qg_server_submit(void *server, const float *queries, size_t nq, int32_t dim,
+                                const NGTQGQueryParameters *params, size_t nparams, NGTQGError error);
+
 #ifdef __cplusplus
 }
 #endif

@@ -169,6 +169,13 @@ def load_library() -> ctypes.CDLL:
         "ngtgpu_server_wait": ([c_void_p, ctypes.c_int64, c_void_p, c_size_t, c_void_p, POINTER(ctypes.c_double),
                                 c_void_p], c_bool),
         "ngtgpu_server_destroy": ([c_void_p], None),
+        "ngtgpu_server_submit_deadline": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QueryParameters),
+                                           c_size_t, ctypes.c_double, c_void_p], ctypes.c_int64),
+        "ngtgpu_server_set_deadline": ([c_void_p, ctypes.c_double, c_void_p], c_bool),
+        "ngtgpu_server_cancel": ([c_void_p, ctypes.c_int64, c_void_p], c_bool),
+        "ngtgpu_qg_server_create": ([c_void_p, c_uint32, c_uint32, c_uint32, c_void_p], c_void_p),
+        "ngtgpu_qg_server_submit": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QGQueryParameters), c_size_t,
+                                     c_void_p], ctypes.c_int64),
         "ngtgpu_qbg_server_create": ([c_void_p, c_uint32, c_uint32, c_uint32, c_uint32, c_void_p], c_void_p),
         "ngtgpu_qbg_server_submit": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QBGQueryParameters), c_size_t,
                                       c_void_p], ctypes.c_int64),
@@ -704,6 +711,63 @@ class QBGServer:
     def wait(self, ticket: int, kmax: int | None = None):
         return Server.wait(self, ticket, kmax)
 
+    def cancel(self, ticket: int) -> bool:
+        return Server.cancel(self, ticket)
+
+    def set_deadline(self, deadline_ms: float):
+        Server.set_deadline(self, deadline_ms)
+
+    def close(self):
+        Server.close(self)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class QGServer:
+    """The continuous-batching serving loop over an open QuantizedIndex
+    (ngtgpu_qg_server_*): every request runs ngtqg_search_index_float's search."""
+
+    def __init__(self, index: "QuantizedIndex", max_batch: int = 1024, inflight: int = 3, max_k: int = 128):
+        self._ix = index
+        self._lib = index._lib
+        self._err = self._lib.ngt_create_error_object()
+        self._srv = self._lib.ngtgpu_qg_server_create(index._index, max_batch, inflight, max_k, self._err)
+        if not self._srv:
+            raise NativeError(self._lib.ngt_get_error_string(self._err).decode())
+        self.max_k = max_k
+        self._pending = {}
+
+    def submit(self, queries, k=20, epsilon=0.03, result_expansion=3.0, radius=-1.0) -> int:
+        q = np.ascontiguousarray(queries, dtype=np.float32)
+        if q.ndim == 1:
+            q = q[None, :]
+        p = QGQueryParameters(int(k), float(epsilon), float(result_expansion), float(radius))
+        t = self._lib.ngtgpu_qg_server_submit(self._srv, q.ctypes.data, q.shape[0], q.shape[1], ctypes.byref(p), 1,
+                                              self._err)
+        if t < 0:
+            raise NativeError(self._lib.ngt_get_error_string(self._err).decode())
+        self._pending[t] = q.shape[0]
+        return t
+
+    def wait(self, ticket: int, kmax: int | None = None):
+        return Server.wait(self, ticket, kmax)
+
+    def cancel(self, ticket: int) -> bool:
+        return Server.cancel(self, ticket)
+
+    def set_deadline(self, deadline_ms: float):
+        Server.set_deadline(self, deadline_ms)
+
     def close(self):
         Server.close(self)
 
@@ -734,19 +798,43 @@ class Server:
         self.max_k = max_k
         self._pending = {}
 
-    def submit(self, queries, k=10, epsilon=0.1, radius=-1.0, edge_size=None) -> int:
+    def submit(self, queries, k=10, epsilon=0.1, radius=-1.0, edge_size=None, deadline_ms=None) -> int:
+        """Queues a request; deadline_ms: it must be launched within that time of now,
+        else its wait raises "deadline exceeded before launch"."""
         q = np.ascontiguousarray(queries, dtype=np.float32)
         if q.ndim == 1:
             q = q[None, :]
         params, n = Index.make_params(k, epsilon, radius, edge_size)
-        t = self._lib.ngtgpu_server_submit(self._srv, q.ctypes.data, q.shape[0], q.shape[1], params, n, self._err)
+        if deadline_ms is None:
+            t = self._lib.ngtgpu_server_submit(self._srv, q.ctypes.data, q.shape[0], q.shape[1], params, n,
+                                               self._err)
+        else:
+            t = self._lib.ngtgpu_server_submit_deadline(self._srv, q.ctypes.data, q.shape[0], q.shape[1], params, n,
+                                                        float(deadline_ms), self._err)
         if t < 0:
             raise NativeError(self._lib.ngt_get_error_string(self._err).decode())
         self._pending[t] = q.shape[0]
         return t
 
+    def cancel(self, ticket: int) -> bool:
+        """Withdraws a request not yet launched (True; its wait then raises "cancelled")."""
+        self._lib.ngt_clear_error_string(self._err)
+        ok = self._lib.ngtgpu_server_cancel(self._srv, ticket, self._err)
+        if not ok:
+            msg = self._lib.ngt_get_error_string(self._err).decode()
+            self._lib.ngt_clear_error_string(self._err)
+            if msg:
+                raise NativeError(msg)
+        return bool(ok)
+
+    def set_deadline(self, deadline_ms: float):
+        """Default admission deadline of later submits (<= 0: none)."""
+        self._lib.ngtgpu_server_set_deadline(self._srv, float(deadline_ms), self._err)
+
     def wait(self, ticket: int, kmax: int | None = None):
         nq = self._pending.pop(ticket)
+        if self._err:
+            self._lib.ngt_clear_error_string(self._err)
         kmax = kmax or self.max_k
         res = np.zeros((nq, kmax), RESULT_DTYPE)
         counts = np.zeros(nq, np.uint32)

@@ -69,7 +69,7 @@ struct Acc {
   uint32_t i0 = 0, i1 = 0;
 
   __device__ __forceinline__ void add(const uint4& q, const uint4& x, int chunk_index) {
-    if constexpr (OT == ObjType::Uint8 && (M == Metric::L2 || M == Metric::InnerProduct)) {
+    if constexpr (OT == ObjType::Uint8 && (M == Metric::L2 || M == Metric::InnerProduct || M == Metric::Quint8L2)) {
       const uint32_t qa[4] = {q.x, q.y, q.z, q.w}, xa[4] = {x.x, x.y, x.z, x.w};
 #pragma unroll
       for (int i = 0; i < 4; i++) {

@@ -1266,7 +1266,8 @@ void GraphEngine::open_qg() {
 
 void GraphEngine::qg_search_device(const uint4* d_rows, size_t nq, const QGArgs* args, size_t nargs,
                                    ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, size_t kmax,
-                                   cudaStream_t stream) {
+                                   cudaStream_t stream, uint32_t* bitmaps, unsigned long long* overflow,
+                                   size_t grid_cap) {
   if (!qg_loaded_) open_qg();
   std::lock_guard<std::mutex> lock(mu_);
   NGT_CUDA(cudaSetDevice(device_));
@@ -1318,7 +1319,13 @@ void GraphEngine::qg_search_device(const uint4* d_rows, size_t nq, const QGArgs*
   NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, kExactThreads, smem));
   NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
   size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
-  ensure_scratch(grid);
+  if (bitmaps) {
+    grid = std::min(grid, grid_cap);
+  } else {
+    ensure_scratch(grid);
+    bitmaps = d_bitmaps_;
+    overflow = d_overflow_;
+  }
   QGParams* d_params = nullptr;
   uint32_t* d_seeds = nullptr;
   NGT_CUDA(cudaMallocAsync(&d_params, nq * sizeof(QGParams), stream));
@@ -1326,7 +1333,7 @@ void GraphEngine::qg_search_device(const uint4* d_rows, size_t nq, const QGArgs*
   NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QGParams), cudaMemcpyHostToDevice, stream));
   NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, stream));
   fn<<<(unsigned)grid, kExactThreads, smem, stream>>>(dev_, dqg_, d_rows, (uint32_t)nq, d_params, d_seeds, d_out,
-                                                       d_counts, d_stats, d_bitmaps_, d_overflow_, cfg);
+                                                       d_counts, d_stats, bitmaps, overflow, cfg);
   NGT_CUDA(cudaGetLastError());
   launches_++;
   NGT_CUDA(cudaFreeAsync(d_params, stream));

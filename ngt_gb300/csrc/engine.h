@@ -150,8 +150,15 @@ class GraphEngine {
   void qg_search(const void* queries, QueryType qt, size_t nq, size_t qdim, const QGArgs* args, size_t nargs,
                  SearchOutput& out);
   // The same over converted query rows resident on the device.
+  // bitmaps / overflow: a caller's own visited bitmaps and overflow lists for at most
+  // grid_cap CTAs (launches on several streams at once); null: the engine's own.
   void qg_search_device(const uint4* d_rows, size_t nq, const QGArgs* args, size_t nargs, ObjDist* d_out,
-                        uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream);
+                        uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream,
+                        uint32_t* bitmaps = nullptr, unsigned long long* overflow = nullptr, size_t grid_cap = 0);
+  // bytes of the visited bitmap and of the overflow lists of one CTA of the exact-order
+  // kernels (the quantized graph's included)
+  size_t cta_bitmap_bytes() const { return (host_.nrows + 31) / 32 * 4; }
+  static size_t cta_overflow_bytes() { return 2 * (size_t)kOverflowCapacity * 8; }
   // qbg_search_index over host queries (nq x qdim, qdim = the QBG genuine
   // dimension); results ascending (distance, id) with quantized distances,
   // size x result_expansion of them when the expansion is >= 1.

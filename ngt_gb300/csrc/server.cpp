@@ -27,10 +27,17 @@
 //
 // The same loop serves quantized-blob-graph indexes (qbg_* handles): one-step or
 // two-step searches, optionally refined, with per-lane scratch sets so that the
-// launches overlap.
+// launches overlap; and quantized-graph indexes (ngtqg_* handles), each lane with its
+// own visited bitmaps and overflow lists for the exact-order quantized-graph kernel.
+//
+// A request that waits longer than the server's admission deadline (if one is set)
+// completes unlaunched with a "deadline exceeded" error, and a waiting request can be
+// cancelled; a request already on the device always runs to completion.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
+#include <cfloat>
 #include <chrono>
 #include <condition_variable>
 #include <cstring>
@@ -70,9 +77,11 @@ struct Request {
   size_t nq = 0;
   std::vector<SearchArgs> args;       // 1 or nq entries (graph search)
   std::vector<QBGArgs> qargs;         // 1 or nq entries (quantized blob graph)
+  std::vector<QGArgs> gargs;          // 1 or nq entries (quantized graph)
   uint32_t cls = 0;                   // shared-memory class (admission groups a launch by it)
   size_t kmax = 0;
   Clock::time_point arrival;
+  Clock::time_point deadline = Clock::time_point::max();   // latest admission
   std::vector<ObjDist> results;       // nq * kmax
   std::vector<uint32_t> counts;
   bool done = false;
@@ -91,6 +100,8 @@ struct Lane {
   uint8_t* h_rows = nullptr;          // pinned staging
   ObjDist* h_out = nullptr;
   uint32_t* h_counts = nullptr;
+  uint32_t* bitmaps = nullptr;        // quantized graph: visited bitmaps of kQgLaneCtas CTAs
+  unsigned long long* overflow = nullptr;
   bool busy = false;
   size_t kmax = 0;
   std::vector<std::shared_ptr<Request>> batch;
@@ -105,16 +116,22 @@ uint32_t size_class(size_t size) {
   return c;
 }
 
+enum class ServedIndex { Graph, Qbg, Qg };
+
 class Server {
  public:
+  // CTAs of one quantized-graph launch (its lane holds their bitmaps and overflow lists)
+  static constexpr size_t kQgLaneCtas = 256;
+
   Server(GraphEngine* e, size_t max_batch, size_t inflight, size_t max_k, Kernel kernel = Kernel::Fast,
-         bool qbg = false, uint32_t qbg_flags = 0)
-      : e_(e), max_batch_(max_batch), max_k_(max_k), row_bytes_(e->host().row_bytes()), kernel_(kernel), qbg_(qbg),
-        qbg_flags_(qbg_flags) {
+         ServedIndex kind = ServedIndex::Graph, uint32_t qbg_flags = 0)
+      : e_(e), max_batch_(max_batch), max_k_(max_k), row_bytes_(e->host().row_bytes()), kernel_(kernel),
+        qbg_(kind == ServedIndex::Qbg), qg_(kind == ServedIndex::Qg), qbg_flags_(qbg_flags) {
     if (max_batch == 0 || inflight == 0 || max_k == 0) throw std::runtime_error("invalid server sizes");
-    if (qbg && !e->is_qbg()) throw std::runtime_error("not a QBG index");
+    if (qbg_ && !e->is_qbg()) throw std::runtime_error("not a QBG index");
     SRV_CUDA(cudaSetDevice(e->device()));
-    if (qbg && (qbg_flags & 2u)) e->prepare_refinement();
+    if (qg_) e->open_qg();
+    if (qbg_ && (qbg_flags & 2u)) e->prepare_refinement();
     e->reserve_scratch_sets(inflight + 1);
     lanes_.resize(inflight);
     for (size_t i = 0; i < inflight; i++) {
@@ -131,8 +148,16 @@ class Server {
       SRV_CUDA(cudaMallocHost(&l.h_counts, max_batch * 4));
       // a launch uses at most one scratch slot per query (plus the rounding of its
       // last CTA's warps): no reallocation while serving
-      if (qbg) e->reserve_qbg_slot(l.slot, max_batch, l.stream);
-      else e->reserve_scratch_slots(l.slot, max_batch + 8);
+      if (qbg_) {
+        e->reserve_qbg_slot(l.slot, max_batch, l.stream);
+      } else if (qg_) {
+        const size_t ctas = std::min(max_batch, kQgLaneCtas);
+        SRV_CUDA(cudaMalloc(&l.bitmaps, ctas * e->cta_bitmap_bytes()));
+        SRV_CUDA(cudaMemsetAsync(l.bitmaps, 0, ctas * e->cta_bitmap_bytes(), l.stream));
+        SRV_CUDA(cudaMalloc(&l.overflow, ctas * GraphEngine::cta_overflow_bytes()));
+      } else {
+        e->reserve_scratch_slots(l.slot, max_batch + 8);
+      }
     }
     worker_ = std::thread([this] { run(); });
   }
@@ -154,13 +179,16 @@ class Server {
       cudaFreeHost(l.h_rows);
       cudaFreeHost(l.h_out);
       cudaFreeHost(l.h_counts);
+      cudaFree(l.bitmaps);
+      cudaFree(l.overflow);
       if (l.done_event) cudaEventDestroy(l.done_event);
       if (l.stream) cudaStreamDestroy(l.stream);
     }
   }
 
-  int64_t submit(const float* queries, size_t nq, size_t dim, const SearchArgs* args, size_t nargs) {
-    if (qbg_) throw std::runtime_error("this server serves a QBG index: submit QBG parameters");
+  int64_t submit(const float* queries, size_t nq, size_t dim, const SearchArgs* args, size_t nargs,
+                 double deadline_ms = -1.0) {
+    if (qbg_ || qg_) throw std::runtime_error("this server serves a quantized index: submit its parameters");
     if (nq == 0 || nq > max_batch_)
       throw std::runtime_error("request size must be 1.." + std::to_string(max_batch_) + " queries");
     if (!(nargs == 1 || nargs == nq)) throw std::runtime_error("parameters must be 1 or one per query");
@@ -176,7 +204,49 @@ class Server {
     if (kmax > max_k_) throw std::runtime_error("result size above the server's maximum " + std::to_string(max_k_));
     r->kmax = kmax;
     r->cls = size_class(smax);
+    return enqueue(r, deadline_ms);
+  }
+
+  int64_t submit_qg(const float* queries, size_t nq, size_t dim, const QGArgs* args, size_t nargs) {
+    if (!qg_) throw std::runtime_error("this server does not serve a quantized graph");
+    if (nq == 0 || nq > max_batch_)
+      throw std::runtime_error("request size must be 1.." + std::to_string(max_batch_) + " queries");
+    if (!(nargs == 1 || nargs == nq)) throw std::runtime_error("parameters must be 1 or one per query");
+    auto r = std::make_shared<Request>();
+    e_->convert_queries(queries, QueryType::Float32, nq, dim, r->rows);
+    r->nq = nq;
+    r->gargs.assign(args, args + nargs);
+    size_t kmax = 1, smax = 1;
+    for (const auto& a : r->gargs) {
+      kmax = std::max(kmax, a.size);
+      smax = std::max(smax, a.result_expansion > 1.0f ? (size_t)((float)a.size * a.result_expansion) : a.size);
+    }
+    if (kmax > max_k_) throw std::runtime_error("result size above the server's maximum " + std::to_string(max_k_));
+    r->kmax = kmax;
+    r->cls = size_class(smax);
     return enqueue(r);
+  }
+
+  // Withdraws a request that has not been launched: true, and its wait reports
+  // "cancelled"; false when it is on the device or complete (its wait delivers it).
+  bool cancel(int64_t ticket) {
+    std::lock_guard<std::mutex> lock(mu_);
+    if (!tickets_.count(ticket)) throw std::runtime_error("unknown ticket " + std::to_string(ticket));
+    for (auto it = pending_.begin(); it != pending_.end(); ++it)
+      if ((*it)->ticket == ticket) {
+        (*it)->error = "cancelled";
+        (*it)->done = true;
+        pending_.erase(it);
+        done_cv_.notify_all();
+        return true;
+      }
+    return false;
+  }
+
+  // Admission deadline of later submits (ms from submission; <= 0: none).
+  void set_deadline(double ms) {
+    std::lock_guard<std::mutex> lock(mu_);
+    deadline_ms_ = ms;
   }
 
   int64_t submit_qbg(const float* queries, size_t nq, size_t dim, const QBGArgs* args, size_t nargs) {
@@ -208,9 +278,12 @@ class Server {
     return enqueue(r);
   }
 
-  int64_t enqueue(const std::shared_ptr<Request>& r) {
+  int64_t enqueue(const std::shared_ptr<Request>& r, double deadline_ms = -1.0) {
     r->arrival = Clock::now();
     std::lock_guard<std::mutex> lock(mu_);
+    const double ms = deadline_ms > 0.0 ? deadline_ms : deadline_ms_;
+    if (ms > 0.0)
+      r->deadline = r->arrival + std::chrono::duration_cast<Clock::duration>(std::chrono::duration<double, std::milli>(ms));
     r->ticket = next_ticket_++;
     pending_.push_back(r);
     tickets_[r->ticket] = r;
@@ -257,6 +330,7 @@ class Server {
       {
         std::unique_lock<std::mutex> lock(mu_);
         if (stop_ && pending_.empty() && !any_busy) break;
+        expire(Clock::now());
         for (Lane& l : lanes_)
           if (!l.busy) { free_lane = &l; break; }
         if (free_lane && !pending_.empty()) {
@@ -286,16 +360,36 @@ class Server {
     }
   }
 
+  // Completes, unlaunched, the waiting requests whose admission deadline has passed
+  // (called with mu_ held).
+  void expire(Clock::time_point now) {
+    bool any = false;
+    for (auto it = pending_.begin(); it != pending_.end();) {
+      if ((*it)->deadline < now) {
+        (*it)->error = "deadline exceeded before launch";
+        (*it)->latency_ms = std::chrono::duration<double, std::milli>(now - (*it)->arrival).count();
+        (*it)->done = true;
+        it = pending_.erase(it);
+        any = true;
+      } else {
+        ++it;
+      }
+    }
+    if (any) done_cv_.notify_all();
+  }
+
   void launch(Lane& l, std::vector<std::shared_ptr<Request>>& batch) {
     l.batch = batch;
     l.kmax = 1;
     size_t nq = 0;
     std::vector<SearchArgs> args;
     std::vector<QBGArgs> qargs;
+    std::vector<QGArgs> gargs;
     for (auto& r : batch) {
       std::memcpy(l.h_rows + nq * row_bytes_, r->rows.data(), r->nq * row_bytes_);
       for (size_t q = 0; q < r->nq; q++) {
         if (qbg_) qargs.push_back(r->qargs[r->qargs.size() == 1 ? 0 : q]);
+        else if (qg_) gargs.push_back(r->gargs[r->gargs.size() == 1 ? 0 : q]);
         else args.push_back(r->args[r->args.size() == 1 ? 0 : q]);
       }
       nq += r->nq;
@@ -306,6 +400,9 @@ class Server {
       if (qbg_)
         e_->qbg_search_device(l.d_rows, nq, qargs.data(), qargs.size(), l.d_out, l.d_counts, l.d_stats, l.kmax,
                               l.stream, l.slot);
+      else if (qg_)
+        e_->qg_search_device(l.d_rows, nq, gargs.data(), gargs.size(), l.d_out, l.d_counts, l.d_stats, l.kmax,
+                             l.stream, l.bitmaps, l.overflow, std::min(max_batch_, kQgLaneCtas));
       else
         e_->search_device_slot(l.d_rows, nq, args.data(), args.size(), l.d_out, l.d_counts, l.d_stats, l.kmax,
                                l.stream, l.slot, kernel_);
@@ -349,8 +446,9 @@ class Server {
   GraphEngine* e_;
   size_t max_batch_, max_k_, row_bytes_;
   Kernel kernel_;
-  bool qbg_ = false;
+  bool qbg_ = false, qg_ = false;
   uint32_t qbg_flags_ = 0;
+  double deadline_ms_ = -1.0;
   std::vector<Lane> lanes_;
   std::deque<std::shared_ptr<Request>> pending_;
   std::map<int64_t, std::shared_ptr<Request>> tickets_;
@@ -440,6 +538,80 @@ bool ngtgpu_server_wait(NGTGPUServer server, int64_t ticket, NGTObjectDistance* 
 
 void ngtgpu_server_destroy(NGTGPUServer server) { delete static_cast<ngtg::Server*>(server); }
 
+int64_t ngtgpu_server_submit_deadline(NGTGPUServer server, const float* queries, size_t nq, int32_t dim,
+                                      const NGTQueryParameters* params, size_t nparams, double deadline_ms,
+                                      NGTError error) {
+  if (server == nullptr || queries == nullptr || params == nullptr || dim <= 0) {
+    server_error(__FUNCTION__, "parametor error: server, queries or params", error);
+    return -1;
+  }
+  try {
+    auto a = server_args(params, nparams);
+    return static_cast<ngtg::Server*>(server)->submit(queries, nq, (size_t)dim, a.data(), a.size(), deadline_ms);
+  } catch (std::exception& ex) {
+    server_error(__FUNCTION__, ex.what(), error);
+    return -1;
+  }
+}
+
+bool ngtgpu_server_cancel(NGTGPUServer server, int64_t ticket, NGTError error) {
+  if (server == nullptr) {
+    server_error(__FUNCTION__, "parametor error: server is NULL", error);
+    return false;
+  }
+  try {
+    return static_cast<ngtg::Server*>(server)->cancel(ticket);
+  } catch (std::exception& ex) {
+    server_error(__FUNCTION__, ex.what(), error);
+    return false;
+  }
+}
+
+bool ngtgpu_server_set_deadline(NGTGPUServer server, double deadline_ms, NGTError error) {
+  if (server == nullptr) {
+    server_error(__FUNCTION__, "parametor error: server is NULL", error);
+    return false;
+  }
+  static_cast<ngtg::Server*>(server)->set_deadline(deadline_ms);
+  return true;
+}
+
+void* ngtgpu_qg_server_create(NGTQGIndex index, uint32_t max_batch_queries, uint32_t inflight, uint32_t max_k,
+                              NGTQGError error) {
+  if (index == nullptr) {
+    server_error(__FUNCTION__, "parametor error: index is NULL", error);
+    return nullptr;
+  }
+  try {
+    return new ngtg::Server(static_cast<ngtg::GraphEngine*>(index), max_batch_queries, inflight, max_k,
+                            ngtg::Kernel::Exact, ngtg::ServedIndex::Qg);
+  } catch (std::exception& ex) {
+    server_error(__FUNCTION__, ex.what(), error);
+    return nullptr;
+  }
+}
+
+int64_t ngtgpu_qg_server_submit(void* server, const float* queries, size_t nq, int32_t dim,
+                                const NGTQGQueryParameters* params, size_t nparams, NGTQGError error) {
+  if (server == nullptr || queries == nullptr || params == nullptr || dim <= 0) {
+    server_error(__FUNCTION__, "parametor error: server, queries or params", error);
+    return -1;
+  }
+  try {
+    std::vector<ngtg::QGArgs> a(nparams);
+    for (size_t i = 0; i < nparams; i++) {
+      a[i].size = params[i].size;
+      a[i].epsilon = params[i].epsilon;
+      a[i].result_expansion = params[i].result_expansion;
+      a[i].radius = params[i].radius < 0.0f ? FLT_MAX : params[i].radius;   // ngtqg_search_index_
+    }
+    return static_cast<ngtg::Server*>(server)->submit_qg(queries, nq, (size_t)dim, a.data(), a.size());
+  } catch (std::exception& ex) {
+    server_error(__FUNCTION__, ex.what(), error);
+    return -1;
+  }
+}
+
 void* ngtgpu_qbg_server_create(QBGIndex index, uint32_t max_batch_queries, uint32_t inflight, uint32_t max_k,
                                       uint32_t flags, NGTError error) {
   if (index == nullptr || (flags & ~(NGTGPU_QBG_TWO_STEP | NGTGPU_QBG_REFINE)) != 0) {
@@ -448,7 +620,7 @@ void* ngtgpu_qbg_server_create(QBGIndex index, uint32_t max_batch_queries, uint3
   }
   try {
     return new ngtg::Server(static_cast<ngtg::GraphEngine*>(index), max_batch_queries, inflight, max_k,
-                            ngtg::Kernel::Exact, true, flags);
+                            ngtg::Kernel::Exact, ngtg::ServedIndex::Qbg, flags);
   } catch (std::exception& ex) {
     server_error(__FUNCTION__, ex.what(), error);
     return nullptr;
