@@ -264,6 +264,8 @@ bool ngtgpu_server_cancel(NGTGPUServer, int64_t ticket, NGTError);
  * the GPU.  Every result equals
  * a lone call's.  The queries coalesced so far, and the launches they took. */
 bool ngtgpu_coalescing_stats(NGTIndex, uint64_t *queries, uint64_t *launches, NGTError);
+/* How many coalesced launches may run at once (1..8, default 8). */
+bool ngtgpu_set_coalescing_lanes(NGTIndex, uint32_t lanes, NGTError);
 
 /* Number of kernel launches issued by this index since it was opened. */
 uint64_t ngtgpu_kernel_launches(NGTIndex, NGTError);

@@ -17,6 +17,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libngtgpu.so")
+LOOP = os.path.join(PKG, "capi_loop")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
@@ -69,6 +70,14 @@ def build_native(verbose: bool = False, jobs: int | None = None) -> str:
                 print(err, flush=True)
     if cmds or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
         run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"])
+    # the native multi-threaded caller of the C API (benchmark of the drop-in path)
+    src = os.path.join(PKG, "capi_loop.c")
+    if not os.path.exists(LOOP) or os.path.getmtime(LOOP) < max(os.path.getmtime(src), os.path.getmtime(LIB)):
+        cc = shutil.which("gcc") or shutil.which("cc")
+        if cc is None:
+            raise RuntimeError("no C compiler for capi_loop.c")
+        run([cc, "-O2", "-std=gnu11", "-I" + os.path.join(ROOT, "include"), src, "-o", LOOP, "-L" + PKG,
+             "-lngtgpu", "-lpthread", "-Wl,-rpath,$ORIGIN"])
     return LIB
 
 

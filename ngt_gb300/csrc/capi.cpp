@@ -606,6 +606,18 @@ bool ngtgpu_coalescing_stats(NGTIndex index, uint64_t* queries, uint64_t* launch
   return true;
 }
 
+bool ngtgpu_set_coalescing_lanes(NGTIndex index, uint32_t lanes, NGTError error) {
+  if (index == nullptr) {
+    CAPI_PARAM_ERROR(error, "index = " << index);
+    return false;
+  }
+  try {
+    engine(index)->set_coalescing_lanes(lanes);
+    return true;
+  }
+  CAPI_CATCH(error, false)
+}
+
 bool ngtgpu_tc_phase_times(NGTIndex index, float* ms3, NGTError error) {
   if (index == nullptr || ms3 == nullptr) {
     CAPI_PARAM_ERROR(error, "index = " << index << " ms = " << ms3);

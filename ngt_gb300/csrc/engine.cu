@@ -994,9 +994,9 @@ void GraphEngine::search_one(const void* query, QueryType qt, size_t qdim, const
   while (!call->done) {
     CoLane* lane = nullptr;
     if (!co_pending_.empty())
-      for (auto& l : co_lanes_)
-        if (!l.busy) {
-          lane = &l;
+      for (size_t i = 0; i < co_nlanes_; i++)
+        if (!co_lanes_[i].busy) {
+          lane = &co_lanes_[i];
           break;
         }
     if (lane) {

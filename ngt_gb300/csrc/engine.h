@@ -131,6 +131,11 @@ class GraphEngine {
   // queries coalesced so far and launches they took (statistics)
   uint64_t coalesced_queries() const { return co_queries_; }
   uint64_t coalesced_launches() const { return co_launches_; }
+  void set_coalescing_lanes(size_t n) {
+    if (n < 1 || n > kCoLanes) throw std::runtime_error("coalescing lanes must be 1..8");
+    std::lock_guard<std::mutex> lock(co_mu_);
+    co_nlanes_ = n;
+  }
   // search() of arguments with a refinement expansion (all of them): the expanded
   // search, then the exact re-rank over the refinement objects
   void search_refined(const void* queries, QueryType qt, size_t nq, size_t qdim, const SearchArgs* args,
@@ -372,6 +377,7 @@ class GraphEngine {
   std::condition_variable co_cv_;
   std::vector<std::shared_ptr<CoalescedCall>> co_pending_;
   CoLane co_lanes_[kCoLanes];
+  size_t co_nlanes_ = kCoLanes;            // lanes in use (1..kCoLanes)
   std::atomic<uint64_t> co_queries_{0}, co_launches_{0};
   void run_coalesced(std::vector<std::shared_ptr<CoalescedCall>>& batch, CoLane& lane);
   QbgScratch& qbg_slot(size_t slot, size_t grid, cudaStream_t stream);
