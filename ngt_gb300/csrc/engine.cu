@@ -177,6 +177,7 @@ GraphEngine::~GraphEngine() {
     if (l.stream) cudaStreamSynchronize(l.stream);
     cudaFree(l.bitmaps);
     cudaFree(l.overflow);
+    cudaFree(l.dev);
     if (l.staging) cudaFreeHost(l.staging);
     if (l.stream) cudaStreamDestroy(l.stream);
   }
@@ -1029,6 +1030,9 @@ void GraphEngine::search_one(const void* query, QueryType qt, size_t qdim, const
 }
 
 void GraphEngine::run_coalesced(std::vector<std::shared_ptr<CoalescedCall>>& batch, CoLane& lane) {
+  // Every copy goes between the lane's pinned block and its device block (one upload
+  // of rows + parameters + seeds, one download of results + counts + statistics), so
+  // the lanes' launches and copies overlap; pageable copies would serialize them.
   NGT_CUDA(cudaSetDevice(device_));
   const size_t nq = batch.size(), rb = host_.row_bytes();
   const size_t words = (host_.nrows + 31) / 32;
@@ -1038,67 +1042,56 @@ void GraphEngine::run_coalesced(std::vector<std::shared_ptr<CoalescedCall>>& bat
     NGT_CUDA(cudaMemsetAsync(lane.bitmaps, 0, kLaneCtas * words * 4, lane.stream));
     NGT_CUDA(cudaMalloc(&lane.overflow, kLaneCtas * 2 * (size_t)kOverflowCapacity * 8));
   }
-  if (lane.staging_bytes < nq * rb) {
-    if (lane.staging) NGT_CUDA(cudaFreeHost(lane.staging));
-    lane.staging = nullptr;
-    lane.staging_bytes = 0;
-    NGT_CUDA(cudaMallocHost(&lane.staging, nq * rb));
-    lane.staging_bytes = nq * rb;
-  }
   std::vector<SearchArgs> args(nq);
   size_t kmax = 1;
   for (size_t i = 0; i < nq; i++) {
     args[i] = batch[i]->args;
     kmax = std::max(kmax, output_size(args[i]));
   }
-  std::vector<ObjDist> res(nq * kmax);
-  std::vector<uint32_t> counts(nq);
-  std::vector<QueryStats> stats(nq);
-  {
-    for (size_t i = 0; i < nq; i++)
-      std::memcpy(static_cast<uint8_t*>(lane.staging) + i * rb, batch[i]->row.data(), rb);
-    uint4* d_rows = nullptr;
-    ObjDist* d_out = nullptr;
-    uint32_t* d_counts = nullptr;
-    QueryStats* d_stats = nullptr;
-    QueryParams* d_params = nullptr;
-    uint32_t* d_seeds = nullptr;
-    cudaStream_t s = lane.stream;
-    std::vector<QueryParams> params;
-    std::vector<uint32_t> seeds;
-    uint32_t max_size = 0;
-    build_params(args.data(), nq, nq, kmax, params, seeds, max_size);
-    NGT_CUDA(cudaMallocAsync(&d_rows, nq * rb, s));
-    NGT_CUDA(cudaMallocAsync(&d_out, nq * kmax * sizeof(ObjDist), s));
-    NGT_CUDA(cudaMallocAsync(&d_counts, nq * 4, s));
-    NGT_CUDA(cudaMallocAsync(&d_stats, nq * sizeof(QueryStats), s));
-    NGT_CUDA(cudaMallocAsync(&d_params, nq * sizeof(QueryParams), s));
-    NGT_CUDA(cudaMallocAsync(&d_seeds, seeds.size() * 4, s));
-    NGT_CUDA(cudaMemcpyAsync(d_rows, lane.staging, nq * rb, cudaMemcpyHostToDevice, s));
-    NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QueryParams), cudaMemcpyHostToDevice, s));
-    NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, s));
-    {
-      std::lock_guard<std::mutex> lock(mu_);
-      launch_exact(d_rows, nq, d_params, d_seeds, max_size, d_out, d_counts, d_stats, s, lane.bitmaps,
-                   lane.overflow, kLaneCtas);
-    }
-    NGT_CUDA(cudaFreeAsync(d_params, s));
-    NGT_CUDA(cudaFreeAsync(d_seeds, s));
-    NGT_CUDA(cudaMemcpyAsync(res.data(), d_out, nq * kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, s));
-    NGT_CUDA(cudaMemcpyAsync(counts.data(), d_counts, nq * 4, cudaMemcpyDeviceToHost, s));
-    NGT_CUDA(cudaMemcpyAsync(stats.data(), d_stats, nq * sizeof(QueryStats), cudaMemcpyDeviceToHost, s));
-    NGT_CUDA(cudaFreeAsync(d_rows, s));
-    NGT_CUDA(cudaFreeAsync(d_out, s));
-    NGT_CUDA(cudaFreeAsync(d_counts, s));
-    NGT_CUDA(cudaFreeAsync(d_stats, s));
-    NGT_CUDA(cudaStreamSynchronize(s));
+  std::vector<QueryParams> params;
+  std::vector<uint32_t> seeds;
+  uint32_t max_size = 0;
+  build_params(args.data(), nq, nq, kmax, params, seeds, max_size);
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t o_par = al(nq * rb), o_seed = o_par + al(nq * sizeof(QueryParams));
+  const size_t o_out = o_seed + al(seeds.size() * 4), o_cnt = o_out + al(nq * kmax * sizeof(ObjDist));
+  const size_t o_st = o_cnt + al(nq * 4), total = o_st + al(nq * sizeof(QueryStats));
+  if (lane.staging_bytes < total) {
+    if (lane.staging) NGT_CUDA(cudaFreeHost(lane.staging));
+    if (lane.dev) NGT_CUDA(cudaFree(lane.dev));
+    lane.staging = nullptr;
+    lane.dev = nullptr;
+    lane.staging_bytes = 0;
+    const size_t bytes = std::max<size_t>(total, 64 << 10);
+    NGT_CUDA(cudaMallocHost(&lane.staging, bytes));
+    NGT_CUDA(cudaMalloc(&lane.dev, bytes));
+    lane.staging_bytes = bytes;
   }
+  uint8_t* h = static_cast<uint8_t*>(lane.staging);
+  uint8_t* d = static_cast<uint8_t*>(lane.dev);
+  for (size_t i = 0; i < nq; i++) std::memcpy(h + i * rb, batch[i]->row.data(), rb);
+  std::memcpy(h + o_par, params.data(), nq * sizeof(QueryParams));
+  std::memcpy(h + o_seed, seeds.data(), seeds.size() * 4);
+  cudaStream_t s = lane.stream;
+  NGT_CUDA(cudaMemcpyAsync(d, h, o_out, cudaMemcpyHostToDevice, s));
+  {
+    std::lock_guard<std::mutex> lock(mu_);
+    launch_exact(reinterpret_cast<const uint4*>(d), nq, reinterpret_cast<const QueryParams*>(d + o_par),
+                 reinterpret_cast<const uint32_t*>(d + o_seed), max_size, reinterpret_cast<ObjDist*>(d + o_out),
+                 reinterpret_cast<uint32_t*>(d + o_cnt), reinterpret_cast<QueryStats*>(d + o_st), s, lane.bitmaps,
+                 lane.overflow, kLaneCtas);
+  }
+  NGT_CUDA(cudaMemcpyAsync(h + o_out, d + o_out, total - o_out, cudaMemcpyDeviceToHost, s));
+  NGT_CUDA(cudaStreamSynchronize(s));
   co_queries_ += nq;
   co_launches_++;
+  const ObjDist* res = reinterpret_cast<const ObjDist*>(h + o_out);
+  const uint32_t* counts = reinterpret_cast<const uint32_t*>(h + o_cnt);
+  const QueryStats* stats = reinterpret_cast<const QueryStats*>(h + o_st);
   for (size_t i = 0; i < nq; i++) {
     SearchOutput& o = batch[i]->out;
     o.kmax = kmax;
-    o.results.assign(res.begin() + i * kmax, res.begin() + (i + 1) * kmax);
+    o.results.assign(res + i * kmax, res + (i + 1) * kmax);
     o.counts.assign(1, counts[i]);
     o.stats.assign(1, stats[i]);
   }

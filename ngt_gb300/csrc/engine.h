@@ -368,7 +368,8 @@ class GraphEngine {
     cudaStream_t stream = nullptr;
     uint32_t* bitmaps = nullptr;
     unsigned long long* overflow = nullptr;
-    void* staging = nullptr;
+    void* staging = nullptr;               // pinned: rows, parameters, seeds | results, counts, stats
+    void* dev = nullptr;                   // the same layout on the device
     size_t staging_bytes = 0;
     bool busy = false;
   };
