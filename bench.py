@@ -925,7 +925,7 @@ def qbg_workload(args, steps=None, warmup=None):
     return out
 
 
-def single_query_capi(path, queries, base, kth, k, eps, threads=16, sample=4000, lanes=(8, 1)):
+def single_query_capi(path, queries, base, kth, k, eps, threads=16, sample=4000, lanes=(16, 1)):
     """ngt_search_index_as_float, one query per call, from `threads` native threads at
     once (the OpenMP loop of ngtpy's batch_search, in C: ngt_gb300/capi_loop.c): the
     library coalesces the calls that meet into exact-kernel launches, up to `lanes` of

@@ -256,16 +256,28 @@ bool ngtgpu_server_set_deadline(NGTGPUServer, double deadline_ms, NGTError);
 bool ngtgpu_server_cancel(NGTGPUServer, int64_t ticket, NGTError);
 
 /* The single-query graph searches (ngt_search_index, _as_float, _as_uint8,
- * _as_float16, _with_query*) of concurrent host threads are coalesced: up to eight
+ * _as_float16, _with_query*) of concurrent host threads are coalesced: up to 16
  * exact-order launches run at once, each on its own stream and scratch; a caller
  * that finds one of them free launches every waiting query at once, and callers
- * arriving while all eight run wait and are launched together by the next free one,
+ * arriving while all 16 run wait and are launched together by the next free one,
  * so a loop of these calls over many threads (ngtpy's batch_search pattern) fills
  * the GPU.  Every result equals
  * a lone call's.  The queries coalesced so far, and the launches they took. */
 bool ngtgpu_coalescing_stats(NGTIndex, uint64_t *queries, uint64_t *launches, NGTError);
-/* How many coalesced launches may run at once (1..8, default 8). */
+/* How many coalesced launches may run at once (1..16, default 16). */
 bool ngtgpu_set_coalescing_lanes(NGTIndex, uint32_t lanes, NGTError);
+
+/* ONNG construction (replaces `ngt reconstruct-graph -m S -o outgoing -i incoming -E
+ * min_edges anng onng`, GraphOptimizer::execute, lib/NGT/GraphOptimizer.h:268-367):
+ * copies the index directory anng_index to onng_index (which must not exist), rebuilds
+ * its graph with GraphReconstructor::reconstructGraph and adjustPathsEffectively
+ * (lib/NGT/GraphReconstructor.h:200-409,645-813) -- the same graph, edge for edge --
+ * with the path-adjustment candidates found on the GPU, and sets GraphType ONNG.
+ * outgoing / incoming < 0 take the index's OutgoingEdge / IncomingEdge; both 0 only
+ * adjust the paths of the ANNG.  The reference command's later search-parameter
+ * optimization (ngt optimize-search-parameters) is not part of it. */
+bool ngtgpu_build_onng(const char *anng_index, const char *onng_index, int32_t outgoing, int32_t incoming,
+                       int64_t min_edges, NGTError);
 
 /* Number of kernel launches issued by this index since it was opened. */
 uint64_t ngtgpu_kernel_launches(NGTIndex, NGTError);

@@ -4,7 +4,7 @@ The compute path is the native library libngtgpu.so (hand-written CUDA for
 sm_103a behind NGT's C ABI); this package only loads it and offers a thin
 Python mirror of NGT's ctypes wrapper (``ngt.base.Index``).
 """
-from .base import Index, ObjectDistance, NativeError, QBGIndex, QBGServer, QGServer, QuantizedIndex, Server, load_library  # noqa: F401
+from .base import build_onng, Index, ObjectDistance, NativeError, QBGIndex, QBGServer, QGServer, QuantizedIndex, Server, load_library  # noqa: F401
 
 
-__all__ = ["Index", "ObjectDistance", "NativeError", "QBGIndex", "QBGServer", "QGServer", "QuantizedIndex", "Server", "load_library"]
+__all__ = ["build_onng", "Index", "ObjectDistance", "NativeError", "QBGIndex", "QBGServer", "QGServer", "QuantizedIndex", "Server", "load_library"]

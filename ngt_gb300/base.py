@@ -169,6 +169,8 @@ def load_library() -> ctypes.CDLL:
         "ngtgpu_server_wait": ([c_void_p, ctypes.c_int64, c_void_p, c_size_t, c_void_p, POINTER(ctypes.c_double),
                                 c_void_p], c_bool),
         "ngtgpu_server_destroy": ([c_void_p], None),
+        "ngtgpu_build_onng": ([c_char_p, c_char_p, c_int32, c_int32, ctypes.c_int64, c_void_p], c_bool),
+        "ngtgpu_set_coalescing_lanes": ([c_void_p, c_uint32, c_void_p], c_bool),
         "ngtgpu_server_submit_deadline": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QueryParameters),
                                            c_size_t, ctypes.c_double, c_void_p], ctypes.c_int64),
         "ngtgpu_server_set_deadline": ([c_void_p, ctypes.c_double, c_void_p], c_bool),
@@ -206,6 +208,19 @@ def load_library() -> ctypes.CDLL:
         fn.restype = res
     _lib = L
     return L
+
+
+def build_onng(anng_index: str, onng_index: str, outgoing: int = -1, incoming: int = -1, min_edges: int = 0):
+    """`ngt reconstruct-graph -m S -o outgoing -i incoming -E min_edges` on the GPU:
+    copies anng_index to onng_index (which must not exist) and rebuilds its graph as
+    the reference's ONNG reconstruction and path adjustment do (ngtgpu_build_onng)."""
+    L = load_library()
+    err = L.ngt_create_error_object()
+    try:
+        if not L.ngtgpu_build_onng(anng_index.encode(), onng_index.encode(), outgoing, incoming, min_edges, err):
+            raise NativeError(L.ngt_get_error_string(err).decode())
+    finally:
+        L.ngt_destroy_error_object(err)
 
 
 def _edge_field(edge_size):

@@ -132,7 +132,7 @@ class GraphEngine {
   uint64_t coalesced_queries() const { return co_queries_; }
   uint64_t coalesced_launches() const { return co_launches_; }
   void set_coalescing_lanes(size_t n) {
-    if (n < 1 || n > kCoLanes) throw std::runtime_error("coalescing lanes must be 1..8");
+    if (n < 1 || n > kCoLanes) throw std::runtime_error("coalescing lanes must be 1..16");
     std::lock_guard<std::mutex> lock(co_mu_);
     co_nlanes_ = n;
   }
@@ -373,7 +373,7 @@ class GraphEngine {
     size_t staging_bytes = 0;
     bool busy = false;
   };
-  static constexpr size_t kCoLanes = 8, kLaneCtas = 16;
+  static constexpr size_t kCoLanes = 16, kLaneCtas = 8;
   std::mutex co_mu_;
   std::condition_variable co_cv_;
   std::vector<std::shared_ptr<CoalescedCall>> co_pending_;

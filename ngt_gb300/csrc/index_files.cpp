@@ -199,6 +199,61 @@ static void read_graph(const std::string& path, HostIndex& ix) {
   ix.offsets[ix.nrows] = acc;
 }
 
+GraphEdges read_graph_edges(const std::string& path) {
+  Reader r(path);
+  GraphEdges g;
+  g.n = r.get<uint64_t>();
+  if (g.n > 0xFFFFFFF0ull) fail("invalid node count in " + path);
+  g.present.assign(g.n, 0);
+  g.off.assign(g.n + 1, 0);
+  for (uint64_t i = 0; i < g.n; i++) {
+    char t = r.get<char>();
+    if (t == '+') {
+      uint32_t cnt = r.get<uint32_t>();
+      const char* p = r.take((size_t)cnt * 8);
+      g.present[i] = 1;
+      for (uint32_t e = 0; e < cnt; e++) {
+        uint32_t id;
+        float d;
+        std::memcpy(&id, p + (size_t)e * 8, 4);
+        std::memcpy(&d, p + (size_t)e * 8 + 4, 4);
+        if (id == 0 || id >= g.n) fail("edge to an invalid node id in " + path);
+        g.ids.push_back(id);
+        g.dists.push_back(d);
+      }
+    } else if (t != '-') {
+      fail("corrupted graph file " + path);
+    }
+    g.off[i + 1] = g.ids.size();
+  }
+  g.trailer.assign(r.buf.begin() + (std::ptrdiff_t)r.pos, r.buf.end());
+  return g;
+}
+
+void write_graph_edges(const std::string& path, const GraphEdges& g) {
+  std::ofstream f(path, std::ios::binary | std::ios::trunc);
+  if (!f.is_open()) fail("cannot write " + path);
+  f.write(reinterpret_cast<const char*>(&g.n), 8);
+  std::vector<char> rec;
+  for (uint64_t i = 0; i < g.n; i++) {
+    if (!g.present[i]) {
+      f.put('-');
+      continue;
+    }
+    const uint32_t cnt = (uint32_t)(g.off[i + 1] - g.off[i]);
+    rec.resize(1 + 4 + (size_t)cnt * 8);
+    rec[0] = '+';
+    std::memcpy(rec.data() + 1, &cnt, 4);
+    for (uint32_t e = 0; e < cnt; e++) {
+      std::memcpy(rec.data() + 5 + (size_t)e * 8, &g.ids[g.off[i] + e], 4);
+      std::memcpy(rec.data() + 9 + (size_t)e * 8, &g.dists[g.off[i] + e], 4);
+    }
+    f.write(rec.data(), (std::streamsize)rec.size());
+  }
+  f.write(g.trailer.data(), (std::streamsize)g.trailer.size());
+  if (!f.good()) fail("cannot write " + path);
+}
+
 static void read_tree(const std::string& path, HostIndex& ix) {
   Reader r(path);
   HostTree& t = ix.tree;

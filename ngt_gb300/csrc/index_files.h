@@ -111,6 +111,20 @@ struct HostQG {
   size_t block_bytes() const { return (size_t)8 * ma; }   // 16 neighbours
 };
 
+// Every node of a graph file with its edges' distances (Repository<GraphNode>,
+// lib/NGT/Graph.h:153-160): slot count, presence, CSR offsets, ids and distances, and
+// the raw bytes of the trailing prevsize vector (GraphRepository::serialize).
+struct GraphEdges {
+  uint64_t n = 0;
+  std::vector<uint8_t> present;
+  std::vector<uint64_t> off;        // n+1
+  std::vector<uint32_t> ids;
+  std::vector<float> dists;
+  std::vector<char> trailer;
+};
+GraphEdges read_graph_edges(const std::string& path);
+void write_graph_edges(const std::string& path, const GraphEdges& g);
+
 // Throws std::runtime_error with a message on any format or I/O error.
 Property load_property(const std::string& dir);
 // The key/value pairs of <dir>/prf without interpreting them (NGTQ property files).

@@ -602,3 +602,59 @@ def write_objects(path: str, rows: np.ndarray) -> None:
         f.write(np.uint64(n + 1).tobytes())
         f.write(b"-")
         f.write(rec.tobytes())
+
+
+def read_graph_file(path: str) -> dict:
+    """Every node of an NGT graph file (Repository<GraphNode>, lib/NGT/Graph.h:153-160):
+    slot count n, presence, CSR offsets (uint64, n+1), edge ids and distances, and the
+    trailing prevsize vector's raw bytes (GraphRepository::serialize)."""
+    raw = open(path, "rb").read()
+    n = int(np.frombuffer(raw, np.uint64, 1, 0)[0])
+    pos = 8
+    present = np.zeros(n, np.uint8)
+    off = np.zeros(n + 1, np.uint64)
+    ids, ds = [], []
+    total = 0
+    for i in range(n):
+        t = raw[pos:pos + 1]
+        pos += 1
+        if t == b"+":
+            cnt = int(np.frombuffer(raw, np.uint32, 1, pos)[0])
+            pos += 4
+            e = np.frombuffer(raw, np.uint32, 2 * cnt, pos).reshape(cnt, 2)
+            ids.append(e[:, 0].copy())
+            ds.append(e[:, 1].copy().view(np.float32))
+            pos += 8 * cnt
+            present[i] = 1
+            total += cnt
+        elif t != b"-":
+            raise ValueError("corrupted graph file " + path)
+        off[i + 1] = total
+    return dict(n=n, present=present, off=off,
+                ids=np.concatenate(ids) if ids else np.zeros(0, np.uint32),
+                dists=np.concatenate(ds) if ds else np.zeros(0, np.float32), trailer=raw[pos:])
+
+
+def onng(graph: dict, outgoing: int, incoming: int, min_edges: int = 0, max_edges: int = 2 ** 63 - 1) -> dict:
+    """The ONNG of an ANNG graph (read_graph_file's form) as `ngt reconstruct-graph -m S
+    -o outgoing -i incoming -E min_edges` builds it (GraphReconstructor::reconstructGraph
+    and adjustPathsEffectively): CSR offsets, ids and distances of every node."""
+    lib = ctypes.CDLL(build())
+    lib.oracle_onng.argtypes = [ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64]
+    lib.oracle_onng.restype = ctypes.c_int64
+    n = graph["n"]
+    cap = len(graph["ids"]) + n * max(incoming, 0) + 1
+    off = np.zeros(n + 1, np.uint64)
+    ids = np.zeros(cap, np.uint32)
+    ds = np.zeros(cap, np.float32)
+    present = np.ascontiguousarray(graph["present"], np.uint8)
+    goff = np.ascontiguousarray(graph["off"], np.uint64)
+    gids = np.ascontiguousarray(graph["ids"], np.uint32)
+    gds = np.ascontiguousarray(graph["dists"], np.float32)
+    total = lib.oracle_onng(n, present.ctypes.data, goff.ctypes.data, gids.ctypes.data, gds.ctypes.data, outgoing,
+                            incoming, max_edges, min_edges, off.ctypes.data, ids.ctypes.data, ds.ctypes.data, cap)
+    if total < 0:
+        raise RuntimeError("oracle_onng: output buffer too small")
+    return dict(n=n, off=off, ids=ids[:total], dists=ds[:total])

@@ -1040,3 +1040,176 @@ void oracle_qbg_search(const OracleIndex *ix, const OracleQG *qg, const float *q
     if (out_blobs) out_blobs[q] = nb;
   }
 }
+
+/* ---------------- ONNG construction (`ngt reconstruct-graph -m S`) ----------------
+ * GraphOptimizer::execute (lib/NGT/GraphOptimizer.h:268-367) with shortcut reduction:
+ *   GraphReconstructor::reconstructGraph (lib/NGT/GraphReconstructor.h:645-813) and
+ *   GraphReconstructor::adjustPathsEffectively (lib/NGT/GraphReconstructor.h:200-409).
+ * Graphs are CSR over node slots 0..n-1 (slot 0 and removed objects absent); edges
+ * (id, distance).  The result is written into out_off (n+1) / out_ids / out_d, which
+ * must hold the input's edges plus n x incoming.  Returns the number of edges, or -1
+ * when an output buffer is too small. */
+typedef struct { uint32_t id; float d; } edge_t;
+typedef struct { edge_t *e; size_t n, cap; } elist_t;
+
+static void el_push(elist_t *l, edge_t x) {
+  if (l->n == l->cap) {
+    l->cap = l->cap ? 2 * l->cap : 8;
+    l->e = (edge_t *)realloc(l->e, l->cap * sizeof(edge_t));
+  }
+  l->e[l->n++] = x;
+}
+static int edge_cmp(const void *a, const void *b) {      /* ObjectDistance::operator< */
+  const edge_t *x = (const edge_t *)a, *y = (const edge_t *)b;
+  if (x->d != y->d) return x->d < y->d ? -1 : 1;
+  return x->id < y->id ? -1 : (x->id > y->id);
+}
+/* GraphReconstructor::insert / hasEdge keep a node sorted by id (edgeComp) */
+static size_t el_lower_id(const elist_t *l, uint32_t id) {
+  size_t lo = 0, hi = l->n;
+  while (lo < hi) {
+    size_t mid = (lo + hi) / 2;
+    if ((l->e[mid].id & 0x7FFFFFFFu) < (id & 0x7FFFFFFFu)) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+static int el_has(const elist_t *l, uint32_t id) {
+  size_t i = el_lower_id(l, id);
+  return i < l->n && l->e[i].id == id;
+}
+typedef struct { uint32_t rank, path, dst; } cand_t;
+static int cand_cmp_desc(const void *a, const void *b) {   /* std::greater over (rank, (path, dst)) */
+  const cand_t *x = (const cand_t *)a, *y = (const cand_t *)b;
+  if (x->rank != y->rank) return x->rank > y->rank ? -1 : 1;
+  if (x->path != y->path) return x->path > y->path ? -1 : 1;
+  return x->dst > y->dst ? -1 : (x->dst < y->dst);
+}
+
+int64_t oracle_onng(uint64_t n, const uint8_t *present, const uint64_t *off, const uint32_t *ids, const float *ds,
+                    int64_t outgoing, int64_t incoming, int64_t max_edges, int64_t min_edges, uint64_t *out_off,
+                    uint32_t *out_ids, float *out_d, uint64_t out_cap) {
+  elist_t *g = (elist_t *)calloc(n, sizeof(elist_t));       /* outGraph */
+  for (uint64_t id = 1; id < n; id++) {
+    if (!present[id]) continue;
+    uint64_t cnt = off[id + 1] - off[id];
+    /* a node with fewer edges than `outgoing` keeps its whole list (the warning path) */
+    uint64_t keep = outgoing == 0 ? 0 : (cnt < (uint64_t)outgoing ? cnt : (uint64_t)outgoing);
+    for (uint64_t e = 0; e < keep; e++) el_push(&g[id], (edge_t){ids[off[id] + e], ds[off[id] + e]});
+  }
+  if (max_edges == 0) max_edges = outgoing > incoming ? outgoing : incoming;
+  for (uint64_t id = 1; id < n; id++) {                    /* reverse edges */
+    uint64_t cnt = present[id] ? off[id + 1] - off[id] : 0;
+    uint64_t rsize = (uint64_t)incoming < cnt ? (uint64_t)incoming : cnt;
+    for (uint64_t i = 0; i < rsize; i++) {
+      uint32_t to = ids[off[id] + i];
+      float d = ds[off[id] + i];
+      if (to >= n || !present[to]) continue;
+      elist_t *l = &g[to];
+      if ((int64_t)l->n >= max_edges) {
+        edge_t b = l->e[l->n - 1];
+        if (b.d > d || (b.d == d && b.id > to)) {
+          edge_t x = {(uint32_t)id, d};
+          size_t pos = 0;
+          while (pos < l->n && edge_cmp(&l->e[pos], &x) < 0) pos++;
+          el_push(l, x);
+          memmove(l->e + pos + 1, l->e + pos, (l->n - 1 - pos) * sizeof(edge_t));
+          l->e[pos] = x;
+          l->n = (size_t)max_edges;
+        }
+      } else {
+        el_push(l, (edge_t){(uint32_t)id, d});
+        if ((int64_t)l->n >= max_edges) qsort(l->e, l->n, sizeof(edge_t), edge_cmp);
+      }
+    }
+  }
+  for (uint64_t id = 1; id < n; id++) {                    /* sort, drop repeated ids */
+    elist_t *l = &g[id];
+    if (!l->n) continue;
+    qsort(l->e, l->n, sizeof(edge_t), edge_cmp);
+    size_t w = 0;
+    uint32_t prev = 0;
+    for (size_t r = 0; r < l->n; r++) {
+      if (l->e[r].id == prev) continue;
+      prev = l->e[r].id;
+      l->e[w++] = l->e[r];
+    }
+    l->n = w;
+  }
+  /* adjustPathsEffectively: tmp = the reconstructed graph, out = empty */
+  elist_t *tmp = g;
+  elist_t *out = (elist_t *)calloc(n, sizeof(elist_t));
+  cand_t **cand = (cand_t **)calloc(n, sizeof(cand_t *));
+  size_t *ncand = (size_t *)calloc(n, sizeof(size_t));
+  for (uint64_t id = 1; id < n; id++) {
+    const elist_t *src = &tmp[id];
+    size_t cap = 0;
+    for (size_t s = 0; s < src->n; s++) {
+      const elist_t *pn = &tmp[src->e[s].id];
+      for (size_t p = 0; p < pn->n; p++) {
+        uint32_t dst = pn->e[p].id;
+        size_t r;                                          /* dst's rank in src (the neighbour map) */
+        for (r = src->n; r > 0; r--)
+          if (src->e[r - 1].id == dst) break;
+        if (r == 0) continue;
+        r--;
+        if (src->e[s].d < src->e[r].d && pn->e[p].d < src->e[r].d) {
+          if (ncand[id] == cap) {
+            cap = cap ? 2 * cap : 16;
+            cand[id] = (cand_t *)realloc(cand[id], cap * sizeof(cand_t));
+          }
+          cand[id][ncand[id]++] = (cand_t){(uint32_t)r, src->e[s].id, dst};
+        }
+      }
+    }
+    if (ncand[id]) qsort(cand[id], ncand[id], sizeof(cand_t), cand_cmp_desc);
+  }
+  uint32_t *active = (uint32_t *)malloc(n * sizeof(uint32_t));
+  size_t nact = 0;
+  for (uint64_t id = 1; id < n; id++) active[nact++] = (uint32_t)id;
+  for (size_t rank = 0; nact; rank++) {
+    size_t w = 0;
+    for (size_t a = 0; a < nact; a++) {
+      uint32_t id = active[a];
+      const elist_t *src = &tmp[id];
+      if (rank >= src->n) continue;                       /* finished: leaves the list */
+      active[w++] = id;
+      if (!present[id]) continue;                         /* getNode throws: skipped */
+      uint32_t dst = src->e[rank].id;
+      if (ncand[id] > 0 && (int64_t)(out[id].n + src->n - rank) > min_edges) {
+        int exist = 0;
+        while (ncand[id] > 0 && cand[id][ncand[id] - 1].dst == dst) {
+          cand_t c = cand[id][--ncand[id]];
+          if (el_has(&out[id], c.path) && el_has(&out[c.path], c.dst)) {
+            exist = 1;
+            while (ncand[id] > 0 && cand[id][ncand[id] - 1].dst == dst) ncand[id]--;
+            break;
+          }
+        }
+        if (exist) continue;
+      }
+      elist_t *l = &out[id];
+      size_t pos = el_lower_id(l, dst);
+      el_push(l, src->e[rank]);
+      memmove(l->e + pos + 1, l->e + pos, (l->n - 1 - pos) * sizeof(edge_t));
+      l->e[pos] = src->e[rank];
+    }
+    nact = w;
+  }
+  uint64_t total = 0;
+  int64_t ret = 0;
+  out_off[0] = 0;
+  for (uint64_t id = 0; id < n; id++) {
+    elist_t *l = &out[id];
+    if (l->n) qsort(l->e, l->n, sizeof(edge_t), edge_cmp);
+    if (total + l->n > out_cap) ret = -1;
+    for (size_t e = 0; e < l->n && ret == 0; e++) {
+      out_ids[total + e] = l->e[e].id;
+      out_d[total + e] = l->e[e].d;
+    }
+    total += l->n;
+    out_off[id + 1] = total;
+  }
+  for (uint64_t id = 0; id < n; id++) { free(g[id].e); free(out[id].e); free(cand[id]); }
+  free(g); free(out); free(cand); free(ncand); free(active);
+  return ret < 0 ? -1 : (int64_t)total;
+}

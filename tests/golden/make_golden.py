@@ -63,6 +63,20 @@ FIXTURES = {
         create="-d 128 -o f -D 2 -E 100 -S 0 -e 0.1 -i t", reconstruct="-m S -o 10 -i 100",
         regenerate_obj=True, otype="f",
         settings=[("graph", 10, 0.1, None, "ro"), ("graph", 10, 0.02, None, "ro"), ("graph", 100, 0.1, None, "ro:100")]),
+    # ONNG construction (`ngt reconstruct-graph -m S`): the reference's ANNG is kept
+    # (anng_grp.gz, anng_prf) so that the GPU construction can rebuild the ONNG from it
+    "onng_f32_l2": dict(
+        base=("clipped_exponential", dict(n=2000, dim=32, seed=301)),
+        query=("clipped_exponential", dict(n=200, dim=32, seed=302)),
+        create="-d 32 -o f -D 2 -E 50 -S 0 -e 0.1 -i t", reconstruct="-m S -o 10 -i 50", keep_anng=True,
+        regenerate_obj=True, otype="f",
+        settings=[("graph", 10, 0.1, None, "ro"), ("graph", 10, 0.02, None, "rw")]),
+    "onng_u8_l2_minedges": dict(
+        base=("clipped_exponential", dict(n=1500, dim=48, seed=311)),
+        query=("clipped_exponential", dict(n=150, dim=48, seed=312)),
+        create="-d 48 -o c -D 2 -E 40 -S 0 -e 0.1 -i t", reconstruct="-m S -o 16 -i 30 -E 12", keep_anng=True,
+        regenerate_obj=True, otype="c",
+        settings=[("graph", 10, 0.1, None, "ro")]),
     "u8_l2": dict(
         base=("clipped_exponential", dict(n=3000, dim=64, seed=31)),
         query=("clipped_exponential", dict(n=300, dim=64, seed=32)),
@@ -331,6 +345,13 @@ def make(name: str, spec: dict) -> None:
             run([os.path.join(REF, "ngt"), "append"] + extra + [idx, tsv])
         else:
             run([os.path.join(REF, "ngt"), "create"] + spec["create"].split() + [idx, tsv])
+        if spec.get("keep_anng"):
+            # the ANNG before the reconstruction: input of the ONNG construction tests
+            os.makedirs(out, exist_ok=True)
+            shutil.copy(os.path.join(idx, "prf"), os.path.join(out, "anng_prf"))
+            with open(os.path.join(idx, "grp"), "rb") as fi, \
+                    gzip.GzipFile(os.path.join(out, "anng_grp.gz"), "wb", mtime=0) as fo:
+                fo.write(fi.read())
         if "reconstruct" in spec:
             idx2 = os.path.join(tmp, "idx2")
             run([os.path.join(REF, "ngt"), "reconstruct-graph"] + spec["reconstruct"].split() + [idx, idx2])
@@ -389,7 +410,8 @@ def make(name: str, spec: dict) -> None:
             settings.append(dict(op=op, k=k, epsilon=eps, edge_size=edge, mode=mode, nq=nq))
         np.savez_compressed(os.path.join(out, "golden.npz"), **arrays)
     meta = dict(name=name, base=spec["base"], query=spec["query"], create=spec["create"],
-                reconstruct=spec.get("reconstruct"), prf_set=spec.get("prf_set"), qg=spec.get("qg"),
+                reconstruct=spec.get("reconstruct"), keep_anng=bool(spec.get("keep_anng")),
+                prf_set=spec.get("prf_set"), qg=spec.get("qg"),
                 otype=spec["otype"],
                 regenerate_obj=spec["regenerate_obj"], obj_sha256=obj_sha, settings=settings,
                 reference="NGT " + open(os.path.join(REF, "include", "NGT", "version_defs.h")).read().split('"')[-2])

@@ -14,7 +14,7 @@ import oracle
 from ngt_gb300 import synthetic
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-INTEGER_FIXTURES = {"c1_f32_l2", "c1_f32_l2_onng", "f32_l2_acc_range", "u8_l2", "u8_l1", "u8_hamming", "u8_jaccard", "f16_l2", "qs8_l2", "qs8_ip", "qs8_ncosine",
+INTEGER_FIXTURES = {"c1_f32_l2", "c1_f32_l2_onng", "f32_l2_acc_range", "u8_l2", "u8_l1", "u8_hamming", "u8_jaccard", "f16_l2", "qs8_l2", "qs8_ip", "qs8_ncosine", "onng_f32_l2", "onng_u8_l2_minedges",
                     "f32_l2_graphonly", "f32_l2_resultsize", "qg_f32_l2_d32", "qg_f32_l2_d64_q2"}
 
 
