@@ -15,7 +15,9 @@ Construction (ONNG, lib/NGT/GraphReconstructor.h:645-760 reconstructGraph):
   3. incoming edges: node u is added to the list of each of its first
      `incoming` neighbours (reverse edges), duplicates removed, every list
      sorted by (distance, id).
-The reference's path adjustment (shortcut reduction) is not applied.
+  4. the reference's path adjustment (shortcut reduction), by the library's GPU
+     ONNG construction (ngtgpu_build_onng), which also redoes steps 2-3 exactly as
+     GraphReconstructor::reconstructGraph does from the k-NN lists written as an ANNG.
 
 Written files: prf, obj (NGT Repository<Object>), grp (Repository<GraphNode>
 with the trailing per-node size vector), and no tree: the index is
@@ -146,13 +148,35 @@ def write_index(path: str, x: np.ndarray, offsets: np.ndarray, edges: np.ndarray
         f.write(np.zeros(nrows, np.uint16).tobytes())
 
 
-def build_onng_index(path: str, x: np.ndarray, k: int = 100, outgoing: int = 10, incoming: int = 100, log=print):
+def build_onng_index(path: str, x: np.ndarray, k: int = 100, outgoing: int = 10, incoming: int = 100, log=print,
+                     path_adjustment: bool = True):
+    """path_adjustment: the k-NN lists are written as an ANNG and turned into an ONNG
+    by the library's GPU construction (ngtgpu_build_onng: the reference's graph
+    reconstruction and path adjustment, `ngt reconstruct-graph -m S -o outgoing -i
+    incoming`); otherwise only the reconstruction, without path adjustment, here."""
     t0 = time.time()
     ids, dst = knn_graph(x, k, log=log)
-    offsets, edges, dists = onng_reconstruct(ids, dst, outgoing, incoming)
-    deg = np.diff(offsets)[1:]
-    log("onng reconstruction: %d edges, mean degree %.1f, max %d" % (len(edges), deg.mean(), deg.max()))
-    write_index(path, x, offsets, edges, dists)
+    if path_adjustment:
+        from .base import build_onng
+        n = ids.shape[0]
+        offsets = np.zeros(n + 2, np.int64)
+        offsets[2:] = np.cumsum(np.full(n, k, np.int64))
+        anng = path + "_anng"
+        if os.path.exists(anng):
+            shutil.rmtree(anng)
+        write_index(anng, x, offsets, ids.cpu().numpy().reshape(-1), dst.cpu().numpy().reshape(-1),
+                    extra_prf={"GraphType": "ANNG"})
+        if os.path.exists(path):
+            shutil.rmtree(path)
+        t1 = time.time()
+        build_onng(anng, path, outgoing, incoming, 0)
+        shutil.rmtree(anng)
+        log("onng construction (GPU path adjustment) in %.1f s" % (time.time() - t1))
+    else:
+        offsets, edges, dists = onng_reconstruct(ids, dst, outgoing, incoming)
+        deg = np.diff(offsets)[1:]
+        log("onng reconstruction: %d edges, mean degree %.1f, max %d" % (len(edges), deg.mean(), deg.max()))
+        write_index(path, x, offsets, edges, dists)
     log("index written to %s in %.1f s total" % (path, time.time() - t0))
     return ids
 

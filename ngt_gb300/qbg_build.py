@@ -123,7 +123,8 @@ def build_qbg(path: str, x: np.ndarray, nblobs: int = 65536, nsid: int = 1024, d
     finally:
         torch.backends.cuda.matmul.allow_tf32 = tf32
     # global index over the blob centroids (ids 1..nblobs, node b = blob b - 1)
-    build_onng_index(os.path.join(path, "global"), B_np, k=min(100, nblobs - 1), outgoing=10, incoming=100, log=log)
+    build_onng_index(os.path.join(path, "global"), B_np, k=min(100, nblobs - 1), outgoing=10, incoming=100, log=log,
+                     path_adjustment=False)
     # blobs: members in id order
     order = np.argsort(blob_np, kind="stable")
     counts = np.bincount(blob_np, minlength=nblobs)

@@ -57,23 +57,25 @@ def test_build_onng_with_hubs_equals_oracle(tmp_path):
     from ngt_gb300 import build_onng
     rng = np.random.default_rng(5)
     n = 6001                                       # slots: the dummy 0 and nodes 1..6000
-    x = rng.standard_normal((n, 6)).astype(np.float32)
-    x[1] *= 0.01                                   # node 1 near the centre: everyone's neighbour
-    x[2] *= 0.02
     lists = [None]
     for i in range(1, n):
-        d = np.sqrt(((x[1:] - x[i]) ** 2).sum(1)).astype(np.float32)
-        d[i - 1] = np.inf
-        nb = np.lexsort((np.arange(1, n), d))[:24]
-        lists.append((nb + 1, d[nb]))
+        # 24 edges sorted by (distance, id); every node but node 1 has node 1 among them
+        nb = rng.choice(np.arange(2, n), 24, replace=False)
+        nb = nb[nb != i][:23]
+        nb = np.concatenate([[1], nb]) if i != 1 else rng.choice(np.arange(2, n), 24, replace=False)
+        d = rng.random(len(nb)).astype(np.float32) * 10
+        if i != 1:
+            d[0] = np.float32(0.001 * (i % 97))
+        order = np.lexsort((nb, d))
+        lists.append((nb[order].astype(np.uint32), d[order]))
     anng = tmp_path / "anng"
     anng.mkdir()
     _write_graph(str(anng / "grp"), n, lists)
     (anng / "prf").write_text("Dimension\t6\nGraphType\tANNG\nIncomingEdge\t24\nOutgoingEdge\t6\n")
     g = oracle.read_graph_file(str(anng / "grp"))
-    # node 1 gets a reverse edge from every node that has it among its 24 nearest:
-    # more neighbours than the 4096 of the shared-memory hash
-    assert sum(1 in lists[i][0] for i in range(1, n)) > 4096
+    # node 1 gets a reverse edge from every other node: more neighbours than the 4096 of
+    # the shared-memory hash, and more candidates than the shared-memory sort holds
+    assert sum(1 in lists[i][0] for i in range(2, n)) > 4096
     want = oracle.onng(g, 6, 24, 0)
     out = str(tmp_path / "onng")
     build_onng(str(anng), out, -1, -1, 0)           # outgoing / incoming from the property file
