@@ -68,8 +68,8 @@ WIDE_PARENTS = 32                 # parents per step of the CTA-per-query kernel
 # profiles/), per query, for each batched kernel.  Scaled by the queries of one
 # launch to give roofline.traffic; the workload's DC per query is the same at
 # every batch size.
-DRAM_BYTES_PER_QUERY = {1: 10.56e9 / 2000,      # batched kernel id -> measured bytes per query
-                        3: 5.893e9 / 2000}      # (kernel 3: 8-bit search rows, its default configuration)
+DRAM_BYTES_PER_QUERY = {3: 6.133e9 / 2000}      # batched kernel id -> measured bytes per query
+                                                 # (kernel 3: 8-bit search rows, its default configuration)
 
 
 def log(*a):
