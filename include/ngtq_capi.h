@@ -91,6 +91,20 @@ bool ngtqg_gpu_search_batch_float(NGTQGIndex index, const float *queries, size_t
 bool ngtqg_gpu_search_batch_device(NGTQGIndex index, const void *d_rows, size_t nq,
                                    const NGTQGQueryParameters *params, size_t nparams, NGTObjectDistance *d_results,
                                    size_t kmax, uint32_t *d_counts, void *d_stats, void *stream, NGTQGError error);
+/* The same two with a kernel: NGTGPU_KERNEL_EXACT (the reference's expansion order,
+ * results equal ngtqg_search_index_float's) or NGTGPU_KERNEL_WIDE (relaxed order:
+ * several parents per step, the quantized distances and the exact re-rank
+ * unchanged; recall at a given epsilon at least the exact kernel's in the tests).
+ * The relaxed kernel takes its parents per step and list capacity from the
+ * index's batched tuning (ngtgpu_set_batched_tuning_ex; defaults 8 and 4 x the
+ * result-set size, at least 256). */
+bool ngtqg_gpu_search_batch_ex_float(NGTQGIndex index, const float *queries, size_t nq, int32_t dim,
+                                     const NGTQGQueryParameters *params, size_t nparams, NGTObjectDistance *results,
+                                     size_t kmax, uint32_t *counts, void *stats, uint32_t kernel, NGTQGError error);
+bool ngtqg_gpu_search_batch_ex_device(NGTQGIndex index, const void *d_rows, size_t nq,
+                                      const NGTQGQueryParameters *params, size_t nparams,
+                                      NGTObjectDistance *d_results, size_t kmax, uint32_t *d_counts, void *d_stats,
+                                      void *stream, uint32_t kernel, NGTQGError error);
 
 /* ---- quantized blob graph (QBG) search, lib/NGT/NGTQ/Capi.h ---------------- */
 

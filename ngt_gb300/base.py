@@ -187,6 +187,12 @@ def load_library() -> ctypes.CDLL:
         "ngtqg_search_index_float": ([c_void_p, QGQueryFloat, c_void_p, c_void_p], c_bool),
         "ngtqg_gpu_search_batch_float": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QGQueryParameters),
                                           c_size_t, c_void_p, c_size_t, c_void_p, c_void_p, c_void_p], c_bool),
+        "ngtqg_gpu_search_batch_ex_float": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QGQueryParameters),
+                                             c_size_t, c_void_p, c_size_t, c_void_p, c_void_p, c_uint32, c_void_p],
+                                            c_bool),
+        "ngtqg_gpu_search_batch_ex_device": ([c_void_p, c_void_p, c_size_t, POINTER(QGQueryParameters), c_size_t,
+                                              c_void_p, c_size_t, c_void_p, c_void_p, c_void_p, c_uint32, c_void_p],
+                                             c_bool),
         "ngtqg_gpu_search_batch_device": ([c_void_p, c_void_p, c_size_t, POINTER(QGQueryParameters), c_size_t,
                                            c_void_p, c_size_t, c_void_p, c_void_p, c_void_p, c_void_p], c_bool),
         "qbg_open_index": ([c_char_p, c_bool, c_void_p], c_void_p),
@@ -543,9 +549,11 @@ class QuantizedIndex:
             out.append((r.id - self.zero, r.distance))
         return out
 
-    def batch_search(self, queries, size=0, epsilon=None, result_expansion=None, with_stats: bool = False):
+    def batch_search(self, queries, size=0, epsilon=None, result_expansion=None, with_stats: bool = False,
+                     kernel: int = KERNEL_EXACT):
         """Every row of `queries` in one launch: (ids[nq, m], distances[nq, m], counts[nq]),
-        ids as stored (1-based)."""
+        ids as stored (1-based).  kernel: KERNEL_EXACT (the reference's order) or
+        KERNEL_WIDE (relaxed order, several parents per step)."""
         q = np.ascontiguousarray(queries, dtype=np.float32)
         nq = q.shape[0]
         p = self._params(size, epsilon, result_expansion)
@@ -553,19 +561,24 @@ class QuantizedIndex:
         res = np.zeros((nq, kmax), RESULT_DTYPE)
         counts = np.zeros(nq, np.uint32)
         stats = np.zeros(nq, QUERY_STATS_DTYPE)
-        ok = self._lib.ngtqg_gpu_search_batch_float(self._index, q.ctypes.data, nq, q.shape[1], ctypes.byref(p), 1,
-                                                    res.ctypes.data, kmax, counts.ctypes.data, stats.ctypes.data,
-                                                    self._err)
+        ok = self._lib.ngtqg_gpu_search_batch_ex_float(self._index, q.ctypes.data, nq, q.shape[1], ctypes.byref(p),
+                                                       1, res.ctypes.data, kmax, counts.ctypes.data,
+                                                       stats.ctypes.data, kernel, self._err)
         self._check(ok)
         m = int(counts.max()) if nq else 0
         out = (res["id"][:, :m].copy(), res["distance"][:, :m].copy(), counts)
         return out + (stats,) if with_stats else out
 
     def search_device(self, d_rows: int, nq: int, params, d_results: int, kmax: int, d_counts: int, d_stats: int,
-                      stream: int = 0):
-        ok = self._lib.ngtqg_gpu_search_batch_device(self._index, d_rows, nq, ctypes.byref(params), 1, d_results,
-                                                     kmax, d_counts, d_stats, stream or None, self._err)
+                      stream: int = 0, kernel: int = KERNEL_EXACT):
+        ok = self._lib.ngtqg_gpu_search_batch_ex_device(self._index, d_rows, nq, ctypes.byref(params), 1, d_results,
+                                                        kmax, d_counts, d_stats, stream or None, kernel, self._err)
         self._check(ok)
+
+    def set_batched_tuning(self, list_capacity: int = 0, parents: int = 0):
+        """Parents per step and list capacity of the relaxed-order kernel (0: automatic)."""
+        t = BatchedTuning(list_capacity, parents, 0.0, 0, 0, 0, 0, 0, 0, 0)
+        self._check(self._lib.ngtgpu_set_batched_tuning_ex(self._index, ctypes.byref(t), self._err))
 
     def convert_queries(self, queries) -> np.ndarray:
         q = np.ascontiguousarray(queries, dtype=np.float32)

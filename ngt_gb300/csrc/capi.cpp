@@ -804,6 +804,18 @@ bool ngtqg_search_index_float16(NGTQGIndex index, NGTQGQueryFloat16 query, NGTOb
 bool ngtqg_gpu_search_batch_float(NGTQGIndex index, const float* queries, size_t nq, int32_t dim,
                                   const NGTQGQueryParameters* params, size_t nparams, NGTObjectDistance* results,
                                   size_t kmax, uint32_t* counts, void* stats, NGTQGError error) {
+  return ngtqg_gpu_search_batch_ex_float(index, queries, nq, dim, params, nparams, results, kmax, counts, stats,
+                                         NGTGPU_KERNEL_EXACT, error);
+}
+
+bool ngtqg_gpu_search_batch_ex_float(NGTQGIndex index, const float* queries, size_t nq, int32_t dim,
+                                     const NGTQGQueryParameters* params, size_t nparams, NGTObjectDistance* results,
+                                     size_t kmax, uint32_t* counts, void* stats, uint32_t kernel,
+                                     NGTQGError error) {
+  if (kernel != NGTGPU_KERNEL_EXACT && kernel != NGTGPU_KERNEL_WIDE) {
+    CAPI_PARAM_ERROR(error, "kernel = " << kernel);
+    return false;
+  }
   if (index == nullptr || (nq && (queries == nullptr || results == nullptr || counts == nullptr)) ||
       params == nullptr || dim <= 0 || !(nparams == 1 || nparams == nq)) {
     CAPI_PARAM_ERROR(error, "index = " << index << " queries = " << queries << " nq = " << nq
@@ -817,7 +829,8 @@ bool ngtqg_gpu_search_batch_float(NGTQGIndex index, const float* queries, size_t
       if (a.back().size > kmax) throw std::runtime_error("a query asks for more results than kmax");
     }
     SearchOutput out;
-    engine(index)->qg_search(queries, QueryType::Float32, nq, (size_t)dim, a.data(), a.size(), out);
+    engine(index)->qg_search(queries, QueryType::Float32, nq, (size_t)dim, a.data(), a.size(), out,
+                             kernel == NGTGPU_KERNEL_WIDE);
     for (size_t q = 0; q < nq; q++) {
       counts[q] = out.counts[q];
       for (uint32_t i = 0; i < out.counts[q]; i++) {
@@ -834,6 +847,18 @@ bool ngtqg_gpu_search_batch_float(NGTQGIndex index, const float* queries, size_t
 bool ngtqg_gpu_search_batch_device(NGTQGIndex index, const void* d_rows, size_t nq,
                                    const NGTQGQueryParameters* params, size_t nparams, NGTObjectDistance* d_results,
                                    size_t kmax, uint32_t* d_counts, void* d_stats, void* stream, NGTQGError error) {
+  return ngtqg_gpu_search_batch_ex_device(index, d_rows, nq, params, nparams, d_results, kmax, d_counts, d_stats,
+                                          stream, NGTGPU_KERNEL_EXACT, error);
+}
+
+bool ngtqg_gpu_search_batch_ex_device(NGTQGIndex index, const void* d_rows, size_t nq,
+                                      const NGTQGQueryParameters* params, size_t nparams,
+                                      NGTObjectDistance* d_results, size_t kmax, uint32_t* d_counts, void* d_stats,
+                                      void* stream, uint32_t kernel, NGTQGError error) {
+  if (kernel != NGTGPU_KERNEL_EXACT && kernel != NGTGPU_KERNEL_WIDE) {
+    CAPI_PARAM_ERROR(error, "kernel = " << kernel);
+    return false;
+  }
   if (index == nullptr || (nq && (d_rows == nullptr || d_results == nullptr || d_counts == nullptr ||
                                   d_stats == nullptr)) ||
       params == nullptr || !(nparams == 1 || nparams == nq)) {
@@ -845,9 +870,14 @@ bool ngtqg_gpu_search_batch_device(NGTQGIndex index, const void* d_rows, size_t 
     for (size_t i = 0; i < nparams; i++) a.push_back(qg_args(params[i]));
     GraphEngine* e = engine(index);
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : e->stream();
-    e->qg_search_device(static_cast<const uint4*>(d_rows), nq, a.data(), a.size(),
-                        reinterpret_cast<ngtg::ObjDist*>(d_results), d_counts,
-                        static_cast<ngtg::QueryStats*>(d_stats), kmax, s);
+    if (kernel == NGTGPU_KERNEL_WIDE)
+      e->qg_search_device_relaxed(static_cast<const uint4*>(d_rows), nq, a.data(), a.size(),
+                                  reinterpret_cast<ngtg::ObjDist*>(d_results), d_counts,
+                                  static_cast<ngtg::QueryStats*>(d_stats), kmax, s);
+    else
+      e->qg_search_device(static_cast<const uint4*>(d_rows), nq, a.data(), a.size(),
+                          reinterpret_cast<ngtg::ObjDist*>(d_results), d_counts,
+                          static_cast<ngtg::QueryStats*>(d_stats), kmax, s);
     return true;
   }
   CAPI_CATCH(error, false)

@@ -19,6 +19,7 @@
 #include "graph_fast.cuh"
 #include "graph_wide.cuh"
 #include "qg_search.cuh"
+#include "qg_wide.cuh"
 #include "qbg_search.cuh"
 #include "kernels.h"
 #include "linear_select.cuh"
@@ -1334,8 +1335,83 @@ void GraphEngine::qg_search_device(const uint4* d_rows, size_t nq, const QGArgs*
   // the pageable host parameter copies above are complete once they return
 }
 
+void GraphEngine::qg_search_device_relaxed(const uint4* d_rows, size_t nq, const QGArgs* args, size_t nargs,
+                                           ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, size_t kmax,
+                                           cudaStream_t stream) {
+  if (!qg_loaded_) open_qg();
+  std::lock_guard<std::mutex> lock(mu_);
+  NGT_CUDA(cudaSetDevice(device_));
+  if (nq == 0) return;
+  std::vector<QGParams> params(nq);
+  std::vector<uint32_t> seeds;
+  uint32_t max_size = 1;
+  for (size_t i = 0; i < nq; i++) {
+    const QGArgs& a = args[nargs == 1 ? 0 : i];
+    if (a.size > kmax) throw std::runtime_error("result size larger than the output capacity");
+    QGParams qp{};
+    float coef = a.epsilon + 1.0f;
+    if (coef == 0.0f) coef = 1.1f;
+    size_t size = a.size;
+    if (a.result_expansion > 1.0f) size = (size_t)((float)a.size * a.result_expansion);
+    qp.size = (uint32_t)std::min<size_t>(size, 0xffffffffu);
+    qp.k = (uint32_t)a.size;
+    qp.radius = a.radius < 0.0f ? FLT_MAX : a.radius;
+    qp.coef = coef;
+    qp.rerank = a.result_expansion >= 1.0f ? 1u : 0u;
+    qp.out_off = (uint32_t)(i * kmax);
+    if (a.size > 0) seed_params(a.size, qp.seed_off, qp.seed_cnt, seeds);
+    params[i] = qp;
+    max_size = std::max<uint32_t>(max_size, qp.size);
+  }
+  if (seeds.empty()) seeds.push_back(0);
+  QGWideConfig cfg{};
+  uint32_t L = tuning_.list_cap ? next_pow2(tuning_.list_cap)
+                                : std::min<uint32_t>(1024, next_pow2(std::max<uint32_t>(256, 4 * max_size)));
+  L = std::max<uint32_t>(L, next_pow2(max_size + 1));
+  if (L > 1024) throw std::runtime_error("result set too large for the relaxed quantized graph search (at most 1023)");
+  cfg.list_cap = L;
+  cfg.parents = tuning_.parents ? std::min<uint32_t>(tuning_.parents, 32) : 8;
+  // neighbour slots: the code blocks of the largest node, and about P typical nodes
+  uint32_t maxdeg = 0;
+  for (uint32_t i = 0; i < qg_.nnodes; i++) maxdeg = std::max(maxdeg, qg_.offsets[i + 1] - qg_.offsets[i]);
+  const uint32_t meandeg = qg_.nnodes ? (uint32_t)(qg_.offsets[qg_.nnodes] / qg_.nnodes) : 0u;
+  uint32_t NB = next_pow2(std::max<uint32_t>({512u, (maxdeg + 15) / 16 * 16,
+                                              cfg.parents * ((meandeg + 15) / 16 * 16), L}));
+  cfg.nbr_cap = std::min<uint32_t>(NB, std::max<uint32_t>(4096u, L));
+  cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));
+  cfg.bitmap_words = ((host_.nrows + 31) / 32 + 3) / 4 * 4;
+  cfg.max_iters = 1u << 22;
+  QGWideKernelFn fn = qg_wide_kernel_for(qg_.m);
+  if (!fn) throw std::runtime_error("too many subspaces in the quantized graph");
+  const size_t smem = qg_wide_kernel_smem_bytes(dev_.row_chunks, qg_.dim, qg_.m, cfg);
+  int max_smem = 0, per_sm = 0, sms = 0;
+  NGT_CUDA(cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, device_));
+  if (smem > (size_t)max_smem) throw std::runtime_error("relaxed quantized graph search state does not fit in shared memory");
+  NGT_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, (int)kQGWideThreads, smem));
+  NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+  const size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
+  FastScratch& scratch = fast_scratch_[0];
+  ensure_fast_scratch(scratch, grid, stream);
+  NGT_CUDA(cudaMemsetAsync(scratch.work, 0, 4, stream));
+  QGParams* d_params = nullptr;
+  uint32_t* d_seeds = nullptr;
+  NGT_CUDA(cudaMallocAsync(&d_params, nq * sizeof(QGParams), stream));
+  NGT_CUDA(cudaMallocAsync(&d_seeds, seeds.size() * 4, stream));
+  NGT_CUDA(cudaMemcpyAsync(d_params, params.data(), nq * sizeof(QGParams), cudaMemcpyHostToDevice, stream));
+  NGT_CUDA(cudaMemcpyAsync(d_seeds, seeds.data(), seeds.size() * 4, cudaMemcpyHostToDevice, stream));
+  fn<<<(unsigned)grid, kQGWideThreads, smem, stream>>>(dev_, dqg_, d_rows, (uint32_t)nq, d_params, d_seeds,
+                                                             d_out, d_counts, d_stats, scratch.bitmaps, scratch.work,
+                                                             cfg);
+  NGT_CUDA(cudaGetLastError());
+  launches_++;
+  NGT_CUDA(cudaFreeAsync(d_params, stream));
+  NGT_CUDA(cudaFreeAsync(d_seeds, stream));
+  // the pageable host parameter copies above are complete once they return
+}
+
 void GraphEngine::qg_search(const void* queries, QueryType qt, size_t nq, size_t qdim, const QGArgs* args,
-                            size_t nargs, SearchOutput& out) {
+                            size_t nargs, SearchOutput& out, bool relaxed) {
   if (!qg_loaded_) open_qg();
   NGT_CUDA(cudaSetDevice(device_));
   std::vector<uint8_t> rows;
@@ -1357,7 +1433,8 @@ void GraphEngine::qg_search(const void* queries, QueryType qt, size_t nq, size_t
   NGT_CUDA(cudaMallocAsync(&d_counts, nq * 4, s));
   NGT_CUDA(cudaMallocAsync(&d_stats, nq * sizeof(QueryStats), s));
   NGT_CUDA(cudaMemcpyAsync(d_rows, rows.data(), rows.size(), cudaMemcpyHostToDevice, s));
-  qg_search_device(d_rows, nq, args, nargs, d_out, d_counts, d_stats, kmax, s);
+  if (relaxed) qg_search_device_relaxed(d_rows, nq, args, nargs, d_out, d_counts, d_stats, kmax, s);
+  else qg_search_device(d_rows, nq, args, nargs, d_out, d_counts, d_stats, kmax, s);
   NGT_CUDA(cudaMemcpyAsync(out.results.data(), d_out, nq * kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, s));
   NGT_CUDA(cudaMemcpyAsync(out.counts.data(), d_counts, nq * 4, cudaMemcpyDeviceToHost, s));
   NGT_CUDA(cudaMemcpyAsync(out.stats.data(), d_stats, nq * sizeof(QueryStats), cudaMemcpyDeviceToHost, s));

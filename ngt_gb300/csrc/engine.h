@@ -153,13 +153,18 @@ class GraphEngine {
   const HostQG& qg_host() const { return qg_; }
   // ngtqg_search_index over host queries (row-major nq x qdim).
   void qg_search(const void* queries, QueryType qt, size_t nq, size_t qdim, const QGArgs* args, size_t nargs,
-                 SearchOutput& out);
+                 SearchOutput& out, bool relaxed = false);
   // The same over converted query rows resident on the device.
   // bitmaps / overflow: a caller's own visited bitmaps and overflow lists for at most
   // grid_cap CTAs (launches on several streams at once); null: the engine's own.
   void qg_search_device(const uint4* d_rows, size_t nq, const QGArgs* args, size_t nargs, ObjDist* d_out,
                         uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream,
                         uint32_t* bitmaps = nullptr, unsigned long long* overflow = nullptr, size_t grid_cap = 0);
+  // The relaxed-order quantized-graph search (qg_wide.cuh): several parents per step,
+  // the batched tuning's parents (default 8) and list capacity (default 4 x the
+  // result-set size, at least 256).
+  void qg_search_device_relaxed(const uint4* d_rows, size_t nq, const QGArgs* args, size_t nargs, ObjDist* d_out,
+                                uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream);
   // bytes of the visited bitmap and of the overflow lists of one CTA of the exact-order
   // kernels (the quantized graph's included)
   size_t cta_bitmap_bytes() const { return (host_.nrows + 31) / 32 * 4; }

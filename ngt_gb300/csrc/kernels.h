@@ -22,6 +22,13 @@ typedef void (*QGKernelFn)(DevGraph, DevQG, const uint4*, uint32_t, const QGPara
 QGKernelFn qg_kernel(uint32_t m);
 size_t qg_kernel_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, const ExactConfig& c);
 
+struct QGWideConfig;
+typedef void (*QGWideKernelFn)(DevGraph, DevQG, const uint4*, uint32_t, const QGParams*, const uint32_t*, ObjDist*,
+                               uint32_t*, QueryStats*, uint32_t*, uint32_t*, QGWideConfig);
+// Relaxed-order quantized-graph kernel for m subspaces (nullptr above 512) and its shared memory.
+QGWideKernelFn qg_wide_kernel_for(uint32_t m);
+size_t qg_wide_kernel_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, const QGWideConfig& c);
+
 struct QBGConfig;
 typedef void (*QBGKernelFn)(DevGraph, DevQG, const uint32_t*, const uint4*, uint32_t, const QBGParams*,
                             const uint32_t*, ObjDist*, uint32_t*, QueryStats*, uint32_t*, unsigned long long*, float*,

@@ -155,3 +155,45 @@ def test_qg_size_zero_returns_nothing(workdir):
     L.ngtqg_close_index(ix)
     L.ngt_destroy_error_object(err)
     assert ok and (n == 0).all()
+
+
+def _recall(ids, counts, qf, base, kth, k):
+    """Tie-aware recall@k: an id counts when its exact distance is within the k-th true one."""
+    hit = 0
+    for j in range(len(qf)):
+        r = ids[j, :min(k, counts[j])].astype(np.int64) - 1
+        if len(r):
+            d = np.sqrt(((base[r].astype(np.float64) - qf[j]) ** 2).sum(1))
+            hit += int((d <= kth[j] * (1 + 1e-6)).sum())
+    return hit / (k * len(qf))
+
+
+@pytest.mark.parametrize("name", QG_FIXTURES)
+@pytest.mark.parametrize("k,eps,expansion", [(10, 0.0, 3.0), (10, 0.05, 2.0), (10, 0.1, 3.0), (20, 0.02, 1.5)])
+def test_relaxed_qg_kernel_recall_at_least_the_exact_order(name, k, eps, expansion, workdir):
+    """The relaxed-order QG kernel (several parents per step): at the same epsilon and
+    expansion its recall is at least the exact-order kernel's (the reference's) up to a
+    small slack, and every returned distance is the exact L2 of the returned object."""
+    from ngt_gb300 import QuantizedIndex
+    from ngt_gb300.base import KERNEL_EXACT, KERNEL_WIDE
+    path, meta, queries, _ = materialize(name, workdir)
+    files = oracle.IndexFiles(path)
+    base = files.objects[1:, :files.dimension].astype(np.float64)
+    q = np.ascontiguousarray(queries[:200], np.float32)
+    d = np.sqrt(((q.astype(np.float64)[:, None, :] - base[None]) ** 2).sum(2))
+    kth = np.sort(d, axis=1)[:, k - 1]
+    with QuantizedIndex(path, zero_based_numbering=False) as ix:
+        ei, ed, en = ix.batch_search(q, size=k, epsilon=eps, result_expansion=expansion, kernel=KERNEL_EXACT)
+        for parents in (0, 1, 4):
+            ix.set_batched_tuning(parents=parents)
+            wi, wd, wn = ix.batch_search(q, size=k, epsilon=eps, result_expansion=expansion, kernel=KERNEL_WIDE)
+            assert (wn == np.minimum(k, wn)).all() and (wn > 0).all(), (name, parents)
+            r_exact = _recall(ei, en, q.astype(np.float64), base, kth, k)
+            r_wide = _recall(wi, wn, q.astype(np.float64), base, kth, k)
+            assert r_wide >= r_exact - 0.01, (name, parents, r_wide, r_exact)
+            for j in range(len(q)):
+                ids = wi[j, :wn[j]].astype(np.int64) - 1
+                want = np.sqrt(((base[ids] - q[j].astype(np.float64)) ** 2).sum(1))
+                assert np.allclose(wd[j, :wn[j]], want, rtol=1e-5, atol=1e-5), (name, parents, j)
+                assert (np.diff(wd[j, :wn[j]]) >= 0).all()
+                assert len(set(ids.tolist())) == len(ids)
