@@ -77,21 +77,28 @@ __device__ __forceinline__ void qg_lookup8(uint32_t w, const uint32_t (&L)[4], u
   a[3] += __byte_perm(v, 0u, 0x4341u);
 }
 
-// Quantized distances of the 16 neighbours of one code block, by one warp.
-// Returns, in lanes whose bits 1..0 select it, one neighbour's distance:
-// *obj receives the neighbour (0..15) the lane holds, or -1.
+// The code words of one 16-neighbour block this lane reads (subspaces lane + 32j).
 template <int SPL>
-__device__ __forceinline__ float qg_block_distance(const uint8_t* __restrict__ blk, const uint32_t (&L)[SPL][4],
-                                                   uint32_t m, uint32_t ma, float scale, float offset, int lane,
-                                                   int* obj) {
-  uint32_t acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+__device__ __forceinline__ void qg_block_words(const uint8_t* __restrict__ blk, uint32_t ma, int lane,
+                                               uint2 (&w)[SPL]) {
 #pragma unroll
   for (int j = 0; j < SPL; j++) {
     const uint32_t s = (uint32_t)lane + 32u * (uint32_t)j;
-    uint2 w = make_uint2(0u, 0u);
-    if (s < ma) w = *reinterpret_cast<const uint2*>(blk + 8u * s);
-    qg_lookup8(w.x, L[j], acc);
-    qg_lookup8(w.y, L[j], acc + 4);
+    w[j] = s < ma ? *reinterpret_cast<const uint2*>(blk + 8u * s) : make_uint2(0u, 0u);
+  }
+}
+
+// Quantized distances of the 16 neighbours of one code block, by one warp, from the
+// words qg_block_words loaded.  Returns, in lanes whose bits 1..0 select it, one
+// neighbour's distance: *obj receives the neighbour (0..15) the lane holds, or -1.
+template <int SPL>
+__device__ __forceinline__ float qg_block_distance_words(const uint2 (&w)[SPL], const uint32_t (&L)[SPL][4],
+                                                         uint32_t m, float scale, float offset, int lane, int* obj) {
+  uint32_t acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+  for (int j = 0; j < SPL; j++) {
+    qg_lookup8(w[j].x, L[j], acc);
+    qg_lookup8(w[j].y, L[j], acc + 4);
   }
   uint32_t sum;
   int o;
@@ -168,6 +175,16 @@ __device__ __forceinline__ float qg_block_distance(const uint8_t* __restrict__ b
   }
   *obj = o;
   return __fsqrt_rn(__fmaf_rn(__uint2float_rn(sum), scale, offset));
+}
+
+// Quantized distances of the 16 neighbours of one code block, by one warp.
+template <int SPL>
+__device__ __forceinline__ float qg_block_distance(const uint8_t* __restrict__ blk, const uint32_t (&L)[SPL][4],
+                                                   uint32_t m, uint32_t ma, float scale, float offset, int lane,
+                                                   int* obj) {
+  uint2 w[SPL];
+  qg_block_words<SPL>(blk, ma, lane, w);
+  return qg_block_distance_words<SPL>(w, L, m, scale, offset, lane, obj);
 }
 
 inline size_t qg_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, const ExactConfig& c) {

@@ -8,8 +8,10 @@
 //   * per step, up to P unexpanded entries within (1 + epsilon) x r_k (r_k: the
 //     size-th entry's distance, or the radius) are expanded together: the 16-
 //     neighbour code blocks of all of them are scanned by the four warps at once
-//     (one block per warp, the reference's 4-bit lookups and saturating sums);
-//   * neighbours within the limit that are not yet visited (per-CTA bitmap) are
+//     (two blocks per warp iteration, both loaded before either is scored; the
+//     reference's 4-bit lookups and saturating sums);
+//   * the neighbours within the limit are checked against the per-CTA visited
+//     bitmap afterwards, eight atomics in flight per thread, and the fresh ones
 //     sorted and merged into the list (each key's place is its rank in the other
 //     list), which keeps the L best;
 //   * the search stops when no unexpanded entry is within the limit; the first
@@ -38,7 +40,7 @@ struct QGWideConfig {
 };
 
 struct QGWideShared {
-  uint32_t q, n, cur, np, nblk, cnt, status, dc, expansions, edges, visited, seed_leaf;
+  uint32_t q, n, cur, np, nblk, cnt, pend, status, dc, expansions, edges, visited, seed_leaf;
   float lut_min, lut_scale, limit;
   float wmin[kQGWideWarps], wmax[kQGWideWarps];
   uint32_t parents[32], pdeg[32], poff[32], pblk[33];
@@ -293,6 +295,7 @@ qg_wide_kernel(DevGraph g, DevQG qg, const uint4* __restrict__ queries, uint32_t
           s.limit = limit;
           s.expansions += np;
           s.cnt = 0;
+          s.pend = 0;
           uint32_t e = 0;
           for (uint32_t j = 0; j < np; j++) e += s.pdeg[j];
           s.edges += e;
@@ -302,37 +305,84 @@ qg_wide_kernel(DevGraph g, DevQG qg, const uint4* __restrict__ queries, uint32_t
       __syncthreads();
       const uint32_t np = s.np;
       if (np == 0) break;
-      // scan: one 16-neighbour block per warp at a time
+      // scan: two 16-neighbour blocks per warp iteration (both blocks' code words and
+      // ids loaded before either is scored); the neighbours within the limit are kept
+      // as pending (distance bits << 32 | id) in the key buffer
       {
         const uint32_t nblk = s.nblk;
         const float limit = s.limit;
-        for (uint32_t bi = (uint32_t)warp; bi < nblk; bi += kQGWideWarps) {
-          uint32_t j = 0;
-          while (j + 1 < np && s.pblk[j + 1] <= bi) j++;
-          const uint32_t p = s.parents[j], lb = bi - s.pblk[j];
-          const uint8_t* blk = qg.codes + (size_t)qg.code_off16[p] * 16 + (size_t)lb * 8 * qg.ma;
-          int o;
-          const float d = qg_block_distance<SPL>(blk, Lr, M, qg.ma, lscale, loffset, lane, &o);
-          bool fresh = false;
-          uint32_t id = 0;
-          if (o >= 0) {
-            const uint32_t e = lb * 16 + (uint32_t)o;
-            if (e < s.pdeg[j]) {
-              id = qg.ids[s.poff[j] + e];
-              if (d <= limit && id < g.nrows) {
-                const uint32_t bit = 1u << (id & 31u);
-                fresh = (atomicOr(&bitmap[id >> 5], bit) & bit) == 0u;
-              }
+        unsigned long long* pend = nkey;
+        for (uint32_t b0 = (uint32_t)warp * 2u; b0 < nblk; b0 += 2u * kQGWideWarps) {
+          uint2 w[2][SPL];
+          uint32_t idv[2], pj[2], lbk[2];
+          bool on[2];
+#pragma unroll
+          for (int u = 0; u < 2; u++) {
+            const uint32_t bi = b0 + (uint32_t)u;
+            on[u] = bi < nblk;
+            uint32_t j = 0;
+            if (on[u])
+              while (j + 1 < np && s.pblk[j + 1] <= bi) j++;
+            pj[u] = j;
+            lbk[u] = on[u] ? bi - s.pblk[j] : 0u;
+            if (on[u]) {
+              const uint32_t p = s.parents[j];
+              qg_block_words<SPL>(qg.codes + (size_t)qg.code_off16[p] * 16 + (size_t)lbk[u] * 8 * qg.ma, qg.ma,
+                                  lane, w[u]);
+              const uint32_t e = lbk[u] * 16u + (uint32_t)lane;
+              idv[u] = (lane < 16 && e < s.pdeg[j]) ? qg.ids[s.poff[j] + e] : 0u;
+            } else {
+#pragma unroll
+              for (int x = 0; x < SPL; x++) w[u][x] = make_uint2(0u, 0u);
+              idv[u] = 0u;
             }
           }
-          const unsigned bal = __ballot_sync(0xffffffffu, fresh);
-          uint32_t base = 0;
-          if (lane == 0 && bal) base = atomicAdd(&s.cnt, (uint32_t)__popc(bal));
-          base = __shfl_sync(0xffffffffu, base, 0);
-          if (fresh) {
-            const uint32_t pos = base + (uint32_t)__popc(bal & ((1u << lane) - 1u));
-            nid[pos] = id;
-            nd[pos] = d;
+#pragma unroll
+          for (int u = 0; u < 2; u++) {
+            if (!on[u]) continue;                          // uniform over the warp
+            int o;
+            const float d = qg_block_distance_words<SPL>(w[u], Lr, M, lscale, loffset, lane, &o);
+            const uint32_t id = __shfl_sync(0xffffffffu, idv[u], o >= 0 ? o : 0);
+            const bool keep = o >= 0 && lbk[u] * 16u + (uint32_t)o < s.pdeg[pj[u]] && d <= limit && id < g.nrows;
+            const unsigned bal = __ballot_sync(0xffffffffu, keep);
+            uint32_t base = 0;
+            if (lane == 0 && bal) base = atomicAdd(&s.pend, (uint32_t)__popc(bal));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (keep)
+              pend[base + (uint32_t)__popc(bal & ((1u << lane) - 1u))] =
+                  ((unsigned long long)__float_as_uint(d) << 32) | id;
+          }
+        }
+      }
+      __syncthreads();
+      // visited bits of the pending neighbours, eight atomics in flight per thread; the
+      // fresh ones (ids and distances) are compacted into nid / nd
+      {
+        const uint32_t npend = s.pend;
+        const unsigned long long* pend = nkey;
+        for (uint32_t b = 0; b < npend; b += 8u * kQGWideThreads) {
+          uint32_t old[8], bit[8];
+          unsigned long long kv[8];
+#pragma unroll
+          for (int r = 0; r < 8; r++) {
+            const uint32_t i = b + (uint32_t)r * kQGWideThreads + (uint32_t)tid;
+            kv[r] = i < npend ? pend[i] : 0ull;
+            const uint32_t id = (uint32_t)kv[r];
+            bit[r] = 1u << (id & 31u);
+            old[r] = i < npend ? atomicOr(&bitmap[id >> 5], bit[r]) : bit[r];
+          }
+#pragma unroll
+          for (int r = 0; r < 8; r++) {
+            const bool fresh = (old[r] & bit[r]) == 0u;
+            const unsigned bal = __ballot_sync(0xffffffffu, fresh);
+            uint32_t base = 0;
+            if (lane == 0 && bal) base = atomicAdd(&s.cnt, (uint32_t)__popc(bal));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (fresh) {
+              const uint32_t pos = base + (uint32_t)__popc(bal & ((1u << lane) - 1u));
+              nid[pos] = (uint32_t)kv[r];
+              nd[pos] = __uint_as_float((uint32_t)(kv[r] >> 32));
+            }
           }
         }
       }
