@@ -388,7 +388,8 @@ def served_qbg(ix, q, k, probes_min, args, kth=None, x=None, ngt_q=0):
 
 QG_EPS_SWEEP = [0.0, 0.02, 0.04, 0.06, 0.08, 0.1]
 QG_EXPANSIONS = [3.0, 5.0, 10.0]
-QG_WIDE_PARENTS = [4, 8, 16]          # parents per step tried for the relaxed-order QG kernel
+# (parents per step, code blocks each warp loads at a time) tried for the relaxed-order QG kernel
+QG_WIDE_SETTINGS = [(8, 2), (16, 2), (8, 4), (16, 4)]
 
 
 def k100_measurement(ix, rows, queries, base, cfg, steps, warmup, log_fn, k=100):
@@ -514,24 +515,25 @@ def qg_measurement(path, base, queries, kth, k, steps, warmup, log_fn):
     # the relaxed-order QG kernel (several parents per step): the fastest (parents,
     # expansion, epsilon) of a sweep reaching the same recall target
     best_w, curve_w = None, []
-    for parents in QG_WIDE_PARENTS:
-        ix.set_batched_tuning(parents=parents)
+    for parents, bpi in QG_WIDE_SETTINGS:
+        ix.set_batched_tuning(parents=parents, blocks_in_flight=bpi)
         for exp in QG_EXPANSIONS:
             for eps in QG_EPS_SWEEP:
                 qps_w, r, _, _ = run(eps, exp, 1, cal, 1, KERNEL_WIDE)
-                curve_w.append((parents, exp, eps, round(r, 4), round(qps_w, 1)))
-                log_fn("qg relaxed parents %d expansion %.0f epsilon %.2f recall@%d %.4f %.1f q/s"
-                       % (parents, exp, eps, k, r, qps_w))
+                curve_w.append((parents, bpi, exp, eps, round(r, 4), round(qps_w, 1)))
+                log_fn("qg relaxed parents %d blocks %d expansion %.0f epsilon %.2f recall@%d %.4f %.1f q/s"
+                       % (parents, bpi, exp, eps, k, r, qps_w))
                 if r >= RECALL_TARGET:
                     if best_w is None or qps_w > best_w[0]:
-                        best_w = (qps_w, eps, exp, parents)
+                        best_w = (qps_w, eps, exp, parents, bpi)
                     break
     if best_w is not None:
-        _, eps_w, exp_w, par_w = best_w
-        ix.set_batched_tuning(parents=par_w)
+        _, eps_w, exp_w, par_w, bpi_w = best_w
+        ix.set_batched_tuning(parents=par_w, blocks_in_flight=bpi_w)
         qps_w, rec_w, stats_w, ms_w = run(eps_w, exp_w, steps, nq, warmup, KERNEL_WIDE)
         bytes_w = 68.0 * stats_w["edges_read"].astype(np.float64) + 512 + 512 * exp_w * k
         out["relaxed"] = {"qps": round(qps_w, 1), "epsilon": eps_w, "result_expansion": exp_w, "parents": par_w,
+                          "blocks_in_flight": bpi_w,
                           "recall_at_k": round(rec_w, 4), "calibration": curve_w,
                           "kernel": "relaxed-order QG kernel, one query per 128-thread CTA, several parents per step",
                           "mean_expansions": round(float(stats_w["expansions"].mean()), 1),

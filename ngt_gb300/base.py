@@ -575,9 +575,10 @@ class QuantizedIndex:
                                                         kmax, d_counts, d_stats, stream or None, kernel, self._err)
         self._check(ok)
 
-    def set_batched_tuning(self, list_capacity: int = 0, parents: int = 0):
-        """Parents per step and list capacity of the relaxed-order kernel (0: automatic)."""
-        t = BatchedTuning(list_capacity, parents, 0.0, 0, 0, 0, 0, 0, 0, 0)
+    def set_batched_tuning(self, list_capacity: int = 0, parents: int = 0, blocks_in_flight: int = 0):
+        """Parents per step, list capacity and code blocks each warp loads at a time (2 or
+        4) of the relaxed-order kernel (0: automatic)."""
+        t = BatchedTuning(list_capacity, parents, 0.0, blocks_in_flight, 0, 0, 0, 0, 0, 0)
         self._check(self._lib.ngtgpu_set_batched_tuning_ex(self._index, ctypes.byref(t), self._err))
 
     def convert_queries(self, queries) -> np.ndarray:

@@ -1381,7 +1381,9 @@ void GraphEngine::qg_search_device_relaxed(const uint4* d_rows, size_t nq, const
   cfg.group = std::min<uint32_t>(32, next_pow2((uint32_t)dev_.row_chunks));
   cfg.bitmap_words = ((host_.nrows + 31) / 32 + 3) / 4 * 4;
   cfg.max_iters = 1u << 22;
-  QGWideKernelFn fn = qg_wide_kernel_for(qg_.m);
+  // rows_in_flight of the batched tuning: code blocks each warp loads at a time (2 or 4)
+  QGWideKernelFn fn = qg_wide_kernel_for(qg_.m, tuning_.rows_in_flight == 4 ? 4u : 2u);
+  if (!fn) fn = qg_wide_kernel_for(qg_.m, 2u);
   if (!fn) throw std::runtime_error("too many subspaces in the quantized graph");
   const size_t smem = qg_wide_kernel_smem_bytes(dev_.row_chunks, qg_.dim, qg_.m, cfg);
   int max_smem = 0, per_sm = 0, sms = 0;

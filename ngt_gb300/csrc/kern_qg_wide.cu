@@ -5,12 +5,19 @@
 
 namespace ngtg {
 
-QGWideKernelFn qg_wide_kernel_for(uint32_t m) {
-  if (m <= 32) return &qg_wide_kernel<1>;
-  if (m <= 64) return &qg_wide_kernel<2>;
-  if (m <= 128) return &qg_wide_kernel<4>;
-  if (m <= 256) return &qg_wide_kernel<8>;
-  if (m <= 512) return &qg_wide_kernel<16>;
+QGWideKernelFn qg_wide_kernel_for(uint32_t m, uint32_t blocks) {
+  if (blocks == 4) {
+    if (m <= 32) return &qg_wide_kernel<1, 4>;
+    if (m <= 64) return &qg_wide_kernel<2, 4>;
+    if (m <= 128) return &qg_wide_kernel<4, 4>;
+    if (m <= 256) return &qg_wide_kernel<8, 4>;
+    return nullptr;                                 // 16 subspaces per lane: two blocks at a time only
+  }
+  if (m <= 32) return &qg_wide_kernel<1, 2>;
+  if (m <= 64) return &qg_wide_kernel<2, 2>;
+  if (m <= 128) return &qg_wide_kernel<4, 2>;
+  if (m <= 256) return &qg_wide_kernel<8, 2>;
+  if (m <= 512) return &qg_wide_kernel<16, 2>;
   return nullptr;
 }
 

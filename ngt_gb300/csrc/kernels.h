@@ -25,8 +25,10 @@ size_t qg_kernel_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, const
 struct QGWideConfig;
 typedef void (*QGWideKernelFn)(DevGraph, DevQG, const uint4*, uint32_t, const QGParams*, const uint32_t*, ObjDist*,
                                uint32_t*, QueryStats*, uint32_t*, uint32_t*, QGWideConfig);
-// Relaxed-order quantized-graph kernel for m subspaces (nullptr above 512) and its shared memory.
-QGWideKernelFn qg_wide_kernel_for(uint32_t m);
+// Relaxed-order quantized-graph kernel for m subspaces loading `blocks` (2 or 4) code
+// blocks per warp at a time (nullptr above 512 subspaces, or 256 with 4) and its
+// shared memory.
+QGWideKernelFn qg_wide_kernel_for(uint32_t m, uint32_t blocks);
 size_t qg_wide_kernel_smem_bytes(uint32_t row_chunks, uint32_t dim, uint32_t m, const QGWideConfig& c);
 
 struct QBGConfig;

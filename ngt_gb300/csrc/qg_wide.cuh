@@ -75,7 +75,8 @@ __device__ __forceinline__ uint32_t qgw_lower_bound(const unsigned long long* a,
   return lo;
 }
 
-template <int SPL>
+// BPI: code blocks each warp loads before scoring them (2 or 4)
+template <int SPL, int BPI>
 __global__ void __launch_bounds__(kQGWideThreads, 4)
 qg_wide_kernel(DevGraph g, DevQG qg, const uint4* __restrict__ queries, uint32_t nq,
                const QGParams* __restrict__ params, const uint32_t* __restrict__ seed_list,
@@ -305,19 +306,19 @@ qg_wide_kernel(DevGraph g, DevQG qg, const uint4* __restrict__ queries, uint32_t
       __syncthreads();
       const uint32_t np = s.np;
       if (np == 0) break;
-      // scan: two 16-neighbour blocks per warp iteration (both blocks' code words and
-      // ids loaded before either is scored); the neighbours within the limit are kept
+      // scan: BPI 16-neighbour blocks per warp iteration (all their code words and ids
+      // loaded before any is scored); the neighbours within the limit are kept
       // as pending (distance bits << 32 | id) in the key buffer
       {
         const uint32_t nblk = s.nblk;
         const float limit = s.limit;
         unsigned long long* pend = nkey;
-        for (uint32_t b0 = (uint32_t)warp * 2u; b0 < nblk; b0 += 2u * kQGWideWarps) {
-          uint2 w[2][SPL];
-          uint32_t idv[2], pj[2], lbk[2];
-          bool on[2];
+        for (uint32_t b0 = (uint32_t)warp * BPI; b0 < nblk; b0 += (uint32_t)BPI * kQGWideWarps) {
+          uint2 w[BPI][SPL];
+          uint32_t idv[BPI], pj[BPI], lbk[BPI];
+          bool on[BPI];
 #pragma unroll
-          for (int u = 0; u < 2; u++) {
+          for (int u = 0; u < BPI; u++) {
             const uint32_t bi = b0 + (uint32_t)u;
             on[u] = bi < nblk;
             uint32_t j = 0;
@@ -338,7 +339,7 @@ qg_wide_kernel(DevGraph g, DevQG qg, const uint4* __restrict__ queries, uint32_t
             }
           }
 #pragma unroll
-          for (int u = 0; u < 2; u++) {
+          for (int u = 0; u < BPI; u++) {
             if (!on[u]) continue;                          // uniform over the warp
             int o;
             const float d = qg_block_distance_words<SPL>(w[u], Lr, M, lscale, loffset, lane, &o);

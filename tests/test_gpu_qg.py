@@ -171,7 +171,8 @@ def _recall(ids, counts, qf, base, kth, k):
 @pytest.mark.parametrize("name", QG_FIXTURES)
 @pytest.mark.parametrize("k,eps,expansion", [(10, 0.0, 3.0), (10, 0.05, 2.0), (10, 0.1, 3.0), (20, 0.02, 1.5)])
 def test_relaxed_qg_kernel_recall_at_least_the_exact_order(name, k, eps, expansion, workdir):
-    """The relaxed-order QG kernel (several parents per step): at the same epsilon and
+    """The relaxed-order QG kernel (several parents per step, two or four code blocks
+    loaded per warp at a time): at the same epsilon and
     expansion its recall is at least the exact-order kernel's (the reference's) up to a
     small slack, and every returned distance is the exact L2 of the returned object."""
     from ngt_gb300 import QuantizedIndex
@@ -184,8 +185,8 @@ def test_relaxed_qg_kernel_recall_at_least_the_exact_order(name, k, eps, expansi
     kth = np.sort(d, axis=1)[:, k - 1]
     with QuantizedIndex(path, zero_based_numbering=False) as ix:
         ei, ed, en = ix.batch_search(q, size=k, epsilon=eps, result_expansion=expansion, kernel=KERNEL_EXACT)
-        for parents in (0, 1, 4):
-            ix.set_batched_tuning(parents=parents)
+        for parents, blocks in ((0, 0), (1, 2), (4, 4), (16, 4)):
+            ix.set_batched_tuning(parents=parents, blocks_in_flight=blocks)
             wi, wd, wn = ix.batch_search(q, size=k, epsilon=eps, result_expansion=expansion, kernel=KERNEL_WIDE)
             assert (wn == np.minimum(k, wn)).all() and (wn > 0).all(), (name, parents)
             r_exact = _recall(ei, en, q.astype(np.float64), base, kth, k)
