@@ -389,7 +389,7 @@ def served_qbg(ix, q, k, probes_min, args, kth=None, x=None, ngt_q=0):
 QG_EPS_SWEEP = [0.0, 0.02, 0.04, 0.06, 0.08, 0.1]
 QG_EXPANSIONS = [3.0, 5.0, 10.0]
 # (parents per step, code blocks each warp loads at a time) tried for the relaxed-order QG kernel
-QG_WIDE_SETTINGS = [(8, 2), (16, 2), (8, 4), (16, 4)]
+QG_WIDE_SETTINGS = [(8, 2), (16, 2), (16, 4)]
 
 
 def k100_measurement(ix, rows, queries, base, cfg, steps, warmup, log_fn, k=100):
