@@ -29,6 +29,21 @@ def gaussian_mixture(n: int, dim: int, nclusters: int, seed_means: int, seed: in
     return x
 
 
+def clustered_bytes(n: int, dim: int, nclusters: int, seed_means: int, seed: int, sigma: float = 12.0,
+                    chunk: int = 1 << 20) -> np.ndarray:
+    """uint8 points around `nclusters` means uniform on [32, 224]^dim, per-coordinate
+    Gaussian spread sigma, rounded and clipped to [0, 255]; generated in chunks."""
+    means = np.random.default_rng(seed_means).uniform(32.0, 224.0, (nclusters, dim)).astype(np.float32)
+    rng = np.random.default_rng(seed)
+    out = np.empty((n, dim), np.uint8)
+    for s0 in range(0, n, chunk):
+        m = min(chunk, n - s0)
+        lab = rng.integers(0, nclusters, size=m)
+        x = means[lab] + sigma * rng.standard_normal((m, dim), dtype=np.float32)
+        out[s0:s0 + m] = np.clip(np.rint(x), 0, 255).astype(np.uint8)
+    return out
+
+
 def random_bytes(n: int, dim: int, seed: int, p_one: float = 0.5) -> np.ndarray:
     """uint8 vectors whose bits are 1 with probability p_one (for Hamming / Jaccard)."""
     rng = np.random.default_rng(seed)
