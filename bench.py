@@ -109,9 +109,9 @@ def parse():
     ap.add_argument("--qbg-only", action="store_true", help="measure the quantized-blob-graph search alone")
     ap.add_argument("--qbg-n", type=int, default=10_000_000, help="objects of the quantized-blob-graph workload")
     ap.add_argument("--qbg-blobs", type=int, default=65536, help="blobs of the quantized-blob-graph workload")
-    ap.add_argument("--qbg-data", default="iid", choices=["iid", "clusters"],
+    ap.add_argument("--qbg-data", default="iid", choices=["iid", "lowrank"],
                     help="QBG objects: the configuration's i.i.d. clipped-exponential coordinates, or uint8 "
-                         "points around 4,096 cluster means (a contrast with neighbourhood structure)")
+                         "points of intrinsic dimension 16 (a contrast with neighbourhood structure)")
     ap.add_argument("--fixed", default=None,
                     help="EPS_PLAIN:EPS_BATCHED -- skip the epsilon / tuning sweeps (profiling runs)")
     ap.add_argument("--fixed-config", default='{"kernel": 3, "L": 256, "P": 10, "T": 128, "stage": 16}',
@@ -903,15 +903,15 @@ def qbg_workload(args, steps=None, warmup=None):
     from ngt_gb300.synthetic import clipped_exponential
     n, d, nq, k = args.qbg_n, 128, args.nq, args.k
     t0 = time.time()
-    if args.qbg_data == "clusters":
-        from ngt_gb300.synthetic import clustered_bytes
-        x = clustered_bytes(n, d, 4096, 43, 41)
-        q = clustered_bytes(nq, d, 4096, 43, 42).astype(np.float32)
+    if args.qbg_data == "lowrank":
+        from ngt_gb300.synthetic import lowrank_bytes
+        x = lowrank_bytes(n, d, 16, 43, 41)
+        q = lowrank_bytes(nq, d, 16, 43, 42).astype(np.float32)
     else:
         x = clipped_exponential(n, d, seed=41).astype(np.uint8)
         q = clipped_exponential(nq, d, seed=42)
     path = os.path.join(args.workdir, "qbg_%d_%d_%d%s" % (n, d, args.qbg_blobs,
-                                                           "_clusters" if args.qbg_data == "clusters" else ""))
+                                                           "_" + args.qbg_data if args.qbg_data != "iid" else ""))
     if not os.path.exists(os.path.join(path, "obj")):
         build_qbg(path, x, nblobs=args.qbg_blobs, log=log)
     log("qbg setup %.1f s" % (time.time() - t0))
@@ -944,7 +944,7 @@ def qbg_workload(args, steps=None, warmup=None):
     stream = torch.cuda.Stream()
     out = {"workload": "QBG %d x %d uint8 L2, %d blobs, rotation + 4-bit PQ (64 two-dim subspaces), %d queries, k=%d"
                        % (n, d, args.qbg_blobs, nq, k),
-           "data": ("uint8 points around 4,096 cluster means (seed 43), sigma 12" if args.qbg_data == "clusters"
+           "data": ("uint8 points 128 + A z of intrinsic dimension 16 (A seed 43)" if args.qbg_data == "lowrank"
                     else "i.i.d. clipped-exponential coordinates")}
 
     def run(flags, probes, expansion, timed_steps, warm):

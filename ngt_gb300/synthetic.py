@@ -29,18 +29,18 @@ def gaussian_mixture(n: int, dim: int, nclusters: int, seed_means: int, seed: in
     return x
 
 
-def clustered_bytes(n: int, dim: int, nclusters: int, seed_means: int, seed: int, sigma: float = 12.0,
-                    chunk: int = 1 << 20) -> np.ndarray:
-    """uint8 points around `nclusters` means uniform on [32, 224]^dim, per-coordinate
-    Gaussian spread sigma, rounded and clipped to [0, 255]; generated in chunks."""
-    means = np.random.default_rng(seed_means).uniform(32.0, 224.0, (nclusters, dim)).astype(np.float32)
+def lowrank_bytes(n: int, dim: int, rank: int, seed_basis: int, seed: int, spread: float = 10.0,
+                  chunk: int = 1 << 20) -> np.ndarray:
+    """uint8 points of low intrinsic dimension: 128 + A z, z ~ N(0, I_rank), A a fixed
+    dim x rank matrix of N(0, spread^2) entries, rounded and clipped to [0, 255];
+    generated in chunks."""
+    a = np.random.default_rng(seed_basis).standard_normal((rank, dim)).astype(np.float32) * spread
     rng = np.random.default_rng(seed)
     out = np.empty((n, dim), np.uint8)
     for s0 in range(0, n, chunk):
         m = min(chunk, n - s0)
-        lab = rng.integers(0, nclusters, size=m)
-        x = means[lab] + sigma * rng.standard_normal((m, dim), dtype=np.float32)
-        out[s0:s0 + m] = np.clip(np.rint(x), 0, 255).astype(np.uint8)
+        z = rng.standard_normal((m, rank), dtype=np.float32)
+        out[s0:s0 + m] = np.clip(np.rint(128.0 + z @ a), 0, 255).astype(np.uint8)
     return out
 
 
