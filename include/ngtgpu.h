@@ -113,7 +113,7 @@ typedef struct {
   uint32_t rows_in_flight;
   uint32_t ctas_per_sm;
   uint32_t neighbour_capacity;
-  uint32_t cta_threads;        /* NGTGPU_KERNEL_WIDE: 128 or 256 threads per query (float L2: both) */
+  uint32_t cta_threads;        /* NGTGPU_KERNEL_WIDE: 64, 128 or 256 threads per query (64: float L2 only) */
   uint32_t stage_kilobytes;    /* NGTGPU_KERNEL_WIDE: shared memory for staged rows (default 64) */
   uint32_t l2_policy;          /* NGTGPU_KERNEL_WIDE: 1 plain caching, 2 visited bitmaps kept in L2,
                                   3 (default) as 2 and staged rows streamed through L2 (evict-first) */

@@ -667,8 +667,8 @@ bool ngtgpu_set_batched_tuning_ex(NGTIndex index, const NGTGPUBatchedTuning* tun
       tuning->rerank_factor < 0.f || tuning->neighbour_capacity > 4096 ||
       !(tuning->rows_in_flight <= 2 || tuning->rows_in_flight == 4 ||
         tuning->rows_in_flight == 6 || tuning->rows_in_flight == 8) ||
-      tuning->ctas_per_sm > 8 || !(tuning->cta_threads == 0 || tuning->cta_threads == 128 ||
-                                   tuning->cta_threads == 256) || tuning->stage_kilobytes > 200 || tuning->l2_policy > 3 ||
+      tuning->ctas_per_sm > 8 || !(tuning->cta_threads == 0 || tuning->cta_threads == 64 ||
+                                   tuning->cta_threads == 128 || tuning->cta_threads == 256) || tuning->stage_kilobytes > 200 || tuning->l2_policy > 3 ||
       tuning->search_rows > 2) {
     CAPI_PARAM_ERROR(error, "index = " << index << " tuning = " << tuning);
     return false;

@@ -178,9 +178,9 @@ struct WideDot {
   }
 };
 
-// T: threads per CTA (128 or 256), one query per CTA.
+// T: threads per CTA (64, 128 or 256), one query per CTA.
 template <ObjType ST, ObjType OT, Metric M, int T>
-__global__ void __launch_bounds__(T, T == 128 ? 6 : 2)
+__global__ void __launch_bounds__(T, T == 64 ? 10 : T == 128 ? 6 : 2)
 graph_search_wide_kernel(DevGraph g, const uint4* __restrict__ srows, const uint4* __restrict__ queries,
                          uint32_t nq, const QueryParams* __restrict__ params, const uint32_t* __restrict__ seed_list,
                          ObjDist* __restrict__ out, uint32_t* __restrict__ out_count, QueryStats* __restrict__ stats,

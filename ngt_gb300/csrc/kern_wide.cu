@@ -7,13 +7,17 @@ namespace ngtg {
 
 WideKernelFn wide_kernel(ObjType ot, Metric m, SearchRows rows, uint32_t threads) {
   if (ot != ObjType::Qsint8) m = kernel_metric(m);   // qsint8 inner product: its own comparator
-  if (threads != 128 && threads != 256) return nullptr;
+  if (threads != 64 && threads != 128 && threads != 256) return nullptr;
+  // 64 threads (more queries in flight per SM): the float L2 search rows only
   if (ot == ObjType::Float && rows == SearchRows::Bf16 && m == Metric::L2)
-    return threads == 128 ? &graph_search_wide_kernel<ObjType::Bfloat16, ObjType::Float, Metric::L2, 128>
-                          : &graph_search_wide_kernel<ObjType::Bfloat16, ObjType::Float, Metric::L2, 256>;
+    return threads == 64    ? &graph_search_wide_kernel<ObjType::Bfloat16, ObjType::Float, Metric::L2, 64>
+           : threads == 128 ? &graph_search_wide_kernel<ObjType::Bfloat16, ObjType::Float, Metric::L2, 128>
+                            : &graph_search_wide_kernel<ObjType::Bfloat16, ObjType::Float, Metric::L2, 256>;
   if (ot == ObjType::Float && rows == SearchRows::Sq8 && m == Metric::L2)
-    return threads == 128 ? &graph_search_wide_kernel<ObjType::Uint8, ObjType::Float, Metric::L2, 128>
-                          : &graph_search_wide_kernel<ObjType::Uint8, ObjType::Float, Metric::L2, 256>;
+    return threads == 64    ? &graph_search_wide_kernel<ObjType::Uint8, ObjType::Float, Metric::L2, 64>
+           : threads == 128 ? &graph_search_wide_kernel<ObjType::Uint8, ObjType::Float, Metric::L2, 128>
+                            : &graph_search_wide_kernel<ObjType::Uint8, ObjType::Float, Metric::L2, 256>;
+  if (threads == 64) return nullptr;
   if (ot == ObjType::Qsint8 && rows == SearchRows::Native && m == Metric::L2)
     return threads == 128 ? &graph_search_wide_kernel<ObjType::Qsint8, ObjType::Qsint8, Metric::L2, 128>
                           : &graph_search_wide_kernel<ObjType::Qsint8, ObjType::Qsint8, Metric::L2, 256>;

@@ -206,7 +206,8 @@ def test_wide_tuning_knobs_do_not_change_results(tmp_path):
     with Index(path, read_only=True) as ix:
         ix.set_batched_tuning(list_capacity=256, parents=8, search_rows=1)
         ref = ix.batch_search(queries[:300], k=10, epsilon=0.1, kernel=KERNEL_WIDE, with_stats=True)
-        for T, stage, rows, l2 in ((128, 8, 1, 1), (128, 32, 2, 2), (256, 64, 4, 3), (256, 16, 2, 1), (128, 200, 4, 3)):
+        for T, stage, rows, l2 in ((128, 8, 1, 1), (128, 32, 2, 2), (256, 64, 4, 3), (256, 16, 2, 1), (128, 200, 4, 3),
+                                   (64, 8, 4, 3), (64, 4, 2, 1)):
             ix.set_batched_tuning(list_capacity=256, parents=8, search_rows=1, cta_threads=T, stage_kilobytes=stage,
                                   rows_in_flight=rows, l2_policy=l2)
             got = ix.batch_search(queries[:300], k=10, epsilon=0.1, kernel=KERNEL_WIDE, with_stats=True)
