@@ -61,9 +61,7 @@ BATCHED_CANDIDATES = [
     dict(kernel=3, L=256, P=8, T=128, stage=16), dict(kernel=3, L=256, P=8, T=128, stage=8),
     dict(kernel=3, L=256, P=10, T=128, stage=16), dict(kernel=3, L=256, P=12, T=128, stage=16),
     dict(kernel=3, L=256, P=8, T=128, stage=32), dict(kernel=3, L=256, P=16, T=128, stage=16),
-    dict(kernel=3, L=256, P=16, T=256, stage=32), dict(kernel=3, L=256, P=8, T=256, stage=32),
-    dict(kernel=3, L=256, P=10, T=64, stage=8), dict(kernel=3, L=256, P=8, T=64, stage=8),
-    dict(kernel=3, L=256, P=6, T=64, stage=8)]
+    dict(kernel=3, L=256, P=16, T=256, stage=32), dict(kernel=3, L=256, P=8, T=256, stage=32)]
 WIDE_PARENTS = 32                 # parents per step of the CTA-per-query kernel the serving loop uses
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of 2,000 queries on
 # this workload (1M x 128, k=10, epsilon 0.08; ncu captures summarised under
