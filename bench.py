@@ -93,6 +93,7 @@ def parse():
                     help="offered query rates of the serving measurement")
     ap.add_argument("--served-seconds", type=float, default=2.0, help="length of each served-rate run")
     ap.add_argument("--qg", type=int, default=1, help="also measure the quantized-graph search (1) or not (0)")
+    ap.add_argument("--qg-dsv", type=int, default=1, help="dimensions per subspace of the quantized graph")
     ap.add_argument("--k100", type=int, default=1, help="also measure the k=100 point of the graph search (1) or not")
     ap.add_argument("--qs8", type=int, default=1,
                     help="also measure scalar-quantized (QSUInteger-8B) objects on the same graph (1) or not (0)")
@@ -449,7 +450,7 @@ def k100_measurement(ix, rows, queries, base, cfg, steps, warmup, log_fn, k=100)
     return out
 
 
-def qg_measurement(path, base, queries, kth, k, steps, warmup, log_fn):
+def qg_measurement(path, base, queries, kth, k, steps, warmup, log_fn, dsv=1):
     """Quantized-graph search (ngtqg_* C API, the exact-order QG kernel) on the same index:
     a 4-bit PQ with one dimension per subspace (128 subspaces, the reference's default for
     this dimension), each node's first 128 edges; the fastest (result expansion, epsilon)
@@ -457,8 +458,16 @@ def qg_measurement(path, base, queries, kth, k, steps, warmup, log_fn):
     import torch
     from ngt_gb300 import QuantizedIndex, qg_build
     from ngt_gb300.base import KERNEL_EXACT, KERNEL_WIDE, QGQueryParameters, QUERY_STATS_DTYPE
+    if dsv != 1:
+        # another quantizer over the same graph index: a directory of links to its files
+        qpath = path + "_qgd%d" % dsv
+        os.makedirs(qpath, exist_ok=True)
+        for fn in ("prf", "obj", "grp", "tre"):
+            if os.path.exists(os.path.join(path, fn)) and not os.path.exists(os.path.join(qpath, fn)):
+                os.symlink(os.path.join(path, fn), os.path.join(qpath, fn))
+        path = qpath
     if not os.path.exists(os.path.join(path, "qg", "grp")):
-        qg_build.build_qg(path, base, dsv=1, max_edges=128, log=log_fn)
+        qg_build.build_qg(path, base, dsv=dsv, max_edges=128, log=log_fn)
     t0 = time.time()
     ix = QuantizedIndex(path, zero_based_numbering=False)
     log_fn("qg: opened in %.1f s" % (time.time() - t0))
@@ -511,7 +520,8 @@ def qg_measurement(path, base, queries, kth, k, steps, warmup, log_fn):
     out = {"qps": round(qps, 1), "epsilon": eps_sel, "result_expansion": exp_sel,
            "recall_at_k": round(rec, 4), "calibration": curve,
            "kernel": "exact-order QG kernel, one query per CTA (results equal the reference's)",
-           "quantizer": "128 subspaces x 16 centroids (1-dim subvectors), no rotation, 128 edges per node",
+           "quantizer": "%d subspaces x 16 centroids (%d-dim subvectors), no rotation, 128 edges per node"
+                        % (base.shape[1] // dsv, dsv),
            "mean_expansions": round(float(stats["expansions"].mean()), 1),
            "mean_quantized_distances": round(float(stats["distance_computations"].mean()), 1),
            "achieved_gbs": round(float(bytes_q.sum() / (statistics.median(ms) / 1e3) / 1e9), 1)}
@@ -1258,7 +1268,8 @@ def main():
     qg = None
     if args.qg and rank == 0 and world == 1:
         try:
-            qg = qg_measurement(path, base, queries, kth, k, max(3, args.steps // 3), args.warmup, log)
+            qg = qg_measurement(path, base, queries, kth, k, max(3, args.steps // 3), args.warmup, log,
+                                dsv=args.qg_dsv)
             log("qg: %s" % qg)
         except Exception as ex:                 # reported, never fatal to the headline measurement
             qg = {"error": str(ex)}

@@ -77,7 +77,7 @@ __device__ __forceinline__ uint32_t qgw_lower_bound(const unsigned long long* a,
 
 // BPI: code blocks each warp loads before scoring them (2 or 4)
 template <int SPL, int BPI>
-__global__ void __launch_bounds__(kQGWideThreads, 4)
+__global__ void __launch_bounds__(kQGWideThreads, SPL <= 4 && BPI == 2 ? 6 : 4)
 qg_wide_kernel(DevGraph g, DevQG qg, const uint4* __restrict__ queries, uint32_t nq,
                const QGParams* __restrict__ params, const uint32_t* __restrict__ seed_list,
                ObjDist* __restrict__ out, uint32_t* __restrict__ out_count, QueryStats* __restrict__ stats,
