@@ -541,7 +541,8 @@ bool GraphEngine::fast_supported(Kernel k) const {
   if (k == Kernel::Exact) return true;
   if (k == Kernel::Wide)
     return wide_kernel(host_.prop.otype, host_.prop.metric,
-                       host_.prop.otype == ObjType::Float ? SearchRows::Bf16 : SearchRows::Native, 256) != nullptr;
+                       host_.prop.otype == ObjType::Float && kernel_metric(host_.prop.metric) == Metric::L2
+                           ? SearchRows::Bf16 : SearchRows::Native, 256) != nullptr;
   const bool hyperbolic = host_.prop.metric == Metric::Poincare || host_.prop.metric == Metric::Lorentz;
   return fast_kernel(host_.prop.otype, host_.prop.metric, k == Kernel::Fast && !hyperbolic) != nullptr;
 }

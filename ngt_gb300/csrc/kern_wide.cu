@@ -26,7 +26,7 @@ WideKernelFn wide_kernel(ObjType ot, Metric m, SearchRows rows, uint32_t threads
     return &graph_search_wide_kernel<ObjType::Float, ObjType::Float, Metric::L2, 256>;
   if (ot == ObjType::Uint8 && m == Metric::L2)
     return &graph_search_wide_kernel<ObjType::Uint8, ObjType::Uint8, Metric::L2, 256>;
-  return nullptr;
+  return wide_kernel_native(ot, m);           // the other distances (kern_wide_metrics.cu)
 }
 
 size_t wide_kernel_smem_bytes(uint32_t row_chunks, const WideConfig& c) { return wide_smem_bytes(row_chunks, c); }

@@ -58,6 +58,10 @@ typedef void (*WideKernelFn)(DevGraph, const uint4*, const uint4*, uint32_t, con
 // 8-bit or fp32 search rows), uint8 L2 and int8-code L2; 128 also for float L2 on
 // bf16 or 8-bit rows and for int8-code L2; nullptr otherwise.
 WideKernelFn wide_kernel(ObjType ot, Metric m, SearchRows rows, uint32_t threads = 256);
+// The CTA-per-query kernel on the objects themselves for the distances other than L2
+// (float: L1, cosine, angle, normalized, Poincare, Lorentz; uint8: L1, Hamming,
+// Jaccard; float16: L2, L1), 256 threads; nullptr for the rest.
+WideKernelFn wide_kernel_native(ObjType ot, Metric m);
 // float rows (dpad per row, `dim` valid) -> 8-bit codes rint((x - offset) / scale), 0 past dim
 void launch_float_rows_to_sq8(const float* in, uint8_t* out, size_t nrows, uint32_t dpad, uint32_t dim, float offset,
                               float scale, cudaStream_t s);

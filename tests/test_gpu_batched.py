@@ -17,7 +17,6 @@ pytestmark = pytest.mark.gpu
 
 KERNEL_BATCHED = 1
 KERNEL_WIDE = 3
-WIDE_CASES = {"c1_f32_l2", "c1_f32_l2_onng", "u8_l2", "qs8_l2"}      # float, uint8 and int8-code L2 indexes
 
 
 @pytest.fixture(scope="module")
@@ -46,8 +45,6 @@ CASES = [("c1_f32_l2", 0, 10), ("c1_f32_l2", 2, 10), ("c1_f32_l2_onng", 0, 11), 
 @pytest.mark.parametrize("name,graph_setting,linear_setting", CASES)
 def test_batched_recall_not_below_reference(name, graph_setting, linear_setting, kernel, workdir):
     from ngt_gb300 import Index
-    if kernel == KERNEL_WIDE and name not in WIDE_CASES:
-        pytest.skip("the wide kernel is built for L2 indexes of float, uint8 and int8-code objects")
     path, meta, queries, golden = materialize(name, workdir)
     s = meta["settings"][graph_setting]
     k, eps, nq = s["k"], s["epsilon"], s["nq"]
