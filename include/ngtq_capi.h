@@ -227,6 +227,11 @@ int64_t ngtgpu_qbg_server_submit(void *server, const float *queries, size_t nq, 
  * ngtqg_search_index_float's.  Returns an NGTGPUServer (ngtgpu.h). */
 void *ngtgpu_qg_server_create(NGTQGIndex index, uint32_t max_batch_queries, uint32_t inflight, uint32_t max_k,
                               NGTQGError error);
+/* The same with the kernel each launch runs: NGTGPU_KERNEL_EXACT (above) or
+ * NGTGPU_KERNEL_WIDE (the relaxed-order QG kernel of ngtqg_gpu_search_batch_ex_float;
+ * a request's results equal that call's on the same queries). */
+void *ngtgpu_qg_server_create_ex(NGTQGIndex index, uint32_t max_batch_queries, uint32_t inflight, uint32_t max_k,
+                                 uint32_t kernel, NGTQGError error);
 int64_t ngtgpu_qg_server_submit(void *server, const float *queries, size_t nq, int32_t dim,
                                 const NGTQGQueryParameters *params, size_t nparams, NGTQGError error);
 

@@ -176,6 +176,7 @@ def load_library() -> ctypes.CDLL:
         "ngtgpu_server_set_deadline": ([c_void_p, ctypes.c_double, c_void_p], c_bool),
         "ngtgpu_server_cancel": ([c_void_p, ctypes.c_int64, c_void_p], c_bool),
         "ngtgpu_qg_server_create": ([c_void_p, c_uint32, c_uint32, c_uint32, c_void_p], c_void_p),
+        "ngtgpu_qg_server_create_ex": ([c_void_p, c_uint32, c_uint32, c_uint32, c_uint32, c_void_p], c_void_p),
         "ngtgpu_qg_server_submit": ([c_void_p, c_void_p, c_size_t, c_int32, POINTER(QGQueryParameters), c_size_t,
                                      c_void_p], ctypes.c_int64),
         "ngtgpu_qbg_server_create": ([c_void_p, c_uint32, c_uint32, c_uint32, c_uint32, c_void_p], c_void_p),
@@ -766,11 +767,12 @@ class QGServer:
     """The continuous-batching serving loop over an open QuantizedIndex
     (ngtgpu_qg_server_*): every request runs ngtqg_search_index_float's search."""
 
-    def __init__(self, index: "QuantizedIndex", max_batch: int = 1024, inflight: int = 3, max_k: int = 128):
+    def __init__(self, index: "QuantizedIndex", max_batch: int = 1024, inflight: int = 3, max_k: int = 128,
+                 kernel: int = KERNEL_EXACT):
         self._ix = index
         self._lib = index._lib
         self._err = self._lib.ngt_create_error_object()
-        self._srv = self._lib.ngtgpu_qg_server_create(index._index, max_batch, inflight, max_k, self._err)
+        self._srv = self._lib.ngtgpu_qg_server_create_ex(index._index, max_batch, inflight, max_k, kernel, self._err)
         if not self._srv:
             raise NativeError(self._lib.ngt_get_error_string(self._err).decode())
         self.max_k = max_k

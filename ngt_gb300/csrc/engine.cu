@@ -1338,11 +1338,12 @@ void GraphEngine::qg_search_device(const uint4* d_rows, size_t nq, const QGArgs*
 
 void GraphEngine::qg_search_device_relaxed(const uint4* d_rows, size_t nq, const QGArgs* args, size_t nargs,
                                            ObjDist* d_out, uint32_t* d_counts, QueryStats* d_stats, size_t kmax,
-                                           cudaStream_t stream) {
+                                           cudaStream_t stream, size_t slot) {
   if (!qg_loaded_) open_qg();
   std::lock_guard<std::mutex> lock(mu_);
   NGT_CUDA(cudaSetDevice(device_));
   if (nq == 0) return;
+  if (slot >= fast_scratch_.size()) throw std::runtime_error("invalid scratch set");
   std::vector<QGParams> params(nq);
   std::vector<uint32_t> seeds;
   uint32_t max_size = 1;
@@ -1394,7 +1395,7 @@ void GraphEngine::qg_search_device_relaxed(const uint4* d_rows, size_t nq, const
   NGT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, (const void*)fn, (int)kQGWideThreads, smem));
   NGT_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
   const size_t grid = std::min<size_t>(nq, (size_t)std::max(1, per_sm) * sms);
-  FastScratch& scratch = fast_scratch_[0];
+  FastScratch& scratch = fast_scratch_[slot];
   ensure_fast_scratch(scratch, grid, stream);
   NGT_CUDA(cudaMemsetAsync(scratch.work, 0, 4, stream));
   QGParams* d_params = nullptr;

@@ -163,8 +163,10 @@ class GraphEngine {
   // The relaxed-order quantized-graph search (qg_wide.cuh): several parents per step,
   // the batched tuning's parents (default 8) and list capacity (default 4 x the
   // result-set size, at least 256).
+  // slot: scratch set (0: the engine's own; >= 1: one reserved by reserve_scratch_slots).
   void qg_search_device_relaxed(const uint4* d_rows, size_t nq, const QGArgs* args, size_t nargs, ObjDist* d_out,
-                                uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream);
+                                uint32_t* d_counts, QueryStats* d_stats, size_t kmax, cudaStream_t stream,
+                                size_t slot = 0);
   // bytes of the visited bitmap and of the overflow lists of one CTA of the exact-order
   // kernels (the quantized graph's included)
   size_t cta_bitmap_bytes() const { return (host_.nrows + 31) / 32 * 4; }

@@ -150,6 +150,8 @@ class Server {
       // last CTA's warps): no reallocation while serving
       if (qbg_) {
         e->reserve_qbg_slot(l.slot, max_batch, l.stream);
+      } else if (qg_ && kernel == Kernel::Wide) {
+        e->reserve_scratch_slots(l.slot, max_batch + 8);   // the relaxed-order QG kernel's bitmaps
       } else if (qg_) {
         const size_t ctas = std::min(max_batch, kQgLaneCtas);
         SRV_CUDA(cudaMalloc(&l.bitmaps, ctas * e->cta_bitmap_bytes()));
@@ -400,6 +402,9 @@ class Server {
       if (qbg_)
         e_->qbg_search_device(l.d_rows, nq, qargs.data(), qargs.size(), l.d_out, l.d_counts, l.d_stats, l.kmax,
                               l.stream, l.slot);
+      else if (qg_ && kernel_ == Kernel::Wide)
+        e_->qg_search_device_relaxed(l.d_rows, nq, gargs.data(), gargs.size(), l.d_out, l.d_counts, l.d_stats,
+                                     l.kmax, l.stream, l.slot);
       else if (qg_)
         e_->qg_search_device(l.d_rows, nq, gargs.data(), gargs.size(), l.d_out, l.d_counts, l.d_stats, l.kmax,
                              l.stream, l.bitmaps, l.overflow, std::min(max_batch_, kQgLaneCtas));
@@ -578,13 +583,19 @@ bool ngtgpu_server_set_deadline(NGTGPUServer server, double deadline_ms, NGTErro
 
 void* ngtgpu_qg_server_create(NGTQGIndex index, uint32_t max_batch_queries, uint32_t inflight, uint32_t max_k,
                               NGTQGError error) {
-  if (index == nullptr) {
-    server_error(__FUNCTION__, "parametor error: index is NULL", error);
+  return ngtgpu_qg_server_create_ex(index, max_batch_queries, inflight, max_k, NGTGPU_KERNEL_EXACT, error);
+}
+
+void* ngtgpu_qg_server_create_ex(NGTQGIndex index, uint32_t max_batch_queries, uint32_t inflight, uint32_t max_k,
+                                 uint32_t kernel, NGTQGError error) {
+  if (index == nullptr || (kernel != NGTGPU_KERNEL_EXACT && kernel != NGTGPU_KERNEL_WIDE)) {
+    server_error(__FUNCTION__, "parametor error: index is NULL or unknown kernel", error);
     return nullptr;
   }
   try {
     return new ngtg::Server(static_cast<ngtg::GraphEngine*>(index), max_batch_queries, inflight, max_k,
-                            ngtg::Kernel::Exact, ngtg::ServedIndex::Qg);
+                            kernel == NGTGPU_KERNEL_WIDE ? ngtg::Kernel::Wide : ngtg::Kernel::Exact,
+                            ngtg::ServedIndex::Qg);
   } catch (std::exception& ex) {
     server_error(__FUNCTION__, ex.what(), error);
     return nullptr;

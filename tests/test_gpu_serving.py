@@ -113,7 +113,8 @@ def test_qbg_results_in_the_mix_equal_results_alone(tmp_path, two_step, refine):
                 assert lat > 0.0
 
 
-def test_qg_results_in_the_mix_equal_results_alone(tmp_path):
+@pytest.mark.parametrize("kernel", [0, 3])
+def test_qg_results_in_the_mix_equal_results_alone(tmp_path, kernel):
     """The serving loop over a quantized graph: requests with different size,
     epsilon and result expansion, submitted from several threads, each equal to the
     same queries searched alone (and so to ngtqg_search_index_float)."""
@@ -127,8 +128,8 @@ def test_qg_results_in_the_mix_equal_results_alone(tmp_path):
         reqs.append((queries[s0:s0 + n], int(rng.choice([5, 10, 20])), float(rng.choice([0.0, 0.05, 0.1])),
                      float(rng.choice([1.0, 2.0, 3.0]))))
     with QuantizedIndex(path, zero_based_numbering=False) as ix:
-        alone = [ix.batch_search(q, size=k, epsilon=e, result_expansion=x) for q, k, e, x in reqs]
-        with QGServer(ix, max_batch=128, inflight=3, max_k=64) as srv:
+        alone = [ix.batch_search(q, size=k, epsilon=e, result_expansion=x, kernel=kernel) for q, k, e, x in reqs]
+        with QGServer(ix, max_batch=128, inflight=3, max_k=64, kernel=kernel) as srv:
             tickets = [None] * len(reqs)
 
             def submitter(part):
