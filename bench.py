@@ -105,6 +105,8 @@ def parse():
     ap.add_argument("--pp-n", type=int, default=1_000_000, help="rows of the brute-force workload")
     ap.add_argument("--pp-nq", type=int, default=10_000, help="queries of the brute-force workload")
     ap.add_argument("--pp-first-rows", type=int, default=0, help="dense rows before the threshold filter (0 auto)")
+    ap.add_argument("--pp-pair", type=int, default=0,
+                    help="score with the two-CTA cluster kernel (query tiles multicast to both CTAs) (1) or not (0)")
     ap.add_argument("--qbg", type=int, default=1,
                     help="also measure the quantized-blob-graph search on 10M x 128 uint8 objects (1) or not (0)")
     ap.add_argument("--qbg-only", action="store_true", help="measure the quantized-blob-graph search alone")
@@ -747,7 +749,7 @@ def precision_path(args, steps=None, warmup=None):
     The rows (3 GB) exceed L2, so no flush."""
     import torch
     from ngt_gb300 import Index
-    from ngt_gb300.base import TC_BF16, TC_FP8, TC_FP64_TIES
+    from ngt_gb300.base import TC_BF16, TC_FP8, TC_FP64_TIES, TC_PAIR
     from ngt_gb300.graph_build import write_index
     n, dim, nq, k = args.pp_n, 768, args.pp_nq, 100
     means = np.random.default_rng(21).standard_normal((64, dim)).astype(np.float32)
@@ -800,7 +802,8 @@ def precision_path(args, steps=None, warmup=None):
         for prec_name, prec in (("bf16", TC_BF16), ("fp8", TC_FP8)):
 
             def step(C, nqq=nq):
-                ok = ix._lib.ngtgpu_linear_search_tc_ex(ix._index, rows.data_ptr(), nqq, k, C, prec, TC_FP64_TIES,
+                ok = ix._lib.ngtgpu_linear_search_tc_ex(ix._index, rows.data_ptr(), nqq, k, C, prec,
+                                                        TC_FP64_TIES | (TC_PAIR if args.pp_pair else 0),
                                                         res.data_ptr(), k, cnt.data_ptr(), status.data_ptr(),
                                                         stream.cuda_stream, ix._err)
                 ix._check(ok)
@@ -840,7 +843,7 @@ def precision_path(args, steps=None, warmup=None):
                 torch.cuda.synchronize()
                 t = time.perf_counter()
                 ix.linear_search_tc(q, k=k, candidates=C_sel, first_rows=args.pp_first_rows, precision=prec_name,
-                                    fp64_ties=True)
+                                    fp64_ties=True, pair=bool(args.pp_pair))
                 e2e.append(time.perf_counter() - t)
             e2e_s = statistics.median(e2e)
             kp = (dim + 63) // 64 * 64 if prec_name == "bf16" else (dim + 127) // 128 * 128
@@ -851,6 +854,7 @@ def precision_path(args, steps=None, warmup=None):
             achieved = flops_filter / (ph[1] * 1e-3) / 1e12 if ph[1] > 0 else None
             out["%s_%s" % (metric, prec_name)] = {
                 "value": nq / (ms * 1e-3), "unit": "queries/s", "ms_per_step": ms, "candidates": C_sel,
+                "score_kernel": "two-CTA clusters" if args.pp_pair else "one CTA per tile",
                 "dtype": "%s+f32-rerank+fp64-ties" % prec_name,
                 "phases_ms": {"dense_and_select": ph[0], "filtered_scores": ph[1], "rerank": ph[2]},
                 "roofline": {"bound": "tensor", "kernel": "tc_score_kernel (filtered part)",

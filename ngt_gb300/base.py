@@ -30,6 +30,7 @@ KERNEL_WIDE = 3
 TC_BF16 = 0
 TC_FP8 = 1
 TC_FP64_TIES = 1
+TC_PAIR = 2                # flag: two-CTA clusters share each query tile (TMA multicast)
 # QBG search flags (include/ngtq_capi.h)
 QBG_TWO_STEP = 1
 QBG_REFINE = 2
@@ -395,7 +396,7 @@ class Index:
         self._check(self._lib.ngtgpu_set_batched_tuning_ex(self._index, ctypes.byref(t), self._err))
 
     def linear_search_tc(self, queries, k: int = 10, candidates: int = 0, first_rows: int = 0,
-                         precision: str = "bf16", fp64_ties: bool = False):
+                         precision: str = "bf16", fp64_ties: bool = False, pair: bool = False):
         """Exhaustive k-NN of every row of `queries` with the tensor-core
         pre-selection (bf16 or per-row scaled fp8 scores, `candidates` re-ranked
         exactly; fp64_ties: the ties at the cut ordered by FP64 distance).
@@ -412,7 +413,8 @@ class Index:
         status = np.zeros(nq, np.uint32)
         prec = {"bf16": TC_BF16, "fp8": TC_FP8}[precision]
         ok = self._lib.ngtgpu_linear_search_tc_float_ex(self._index, q.ctypes.data, nq, q.shape[1], k, candidates,
-                                                        prec, TC_FP64_TIES if fp64_ties else 0, res.ctypes.data, k,
+                                                        prec, (TC_FP64_TIES if fp64_ties else 0) |
+                                                        (TC_PAIR if pair else 0), res.ctypes.data, k,
                                                         counts.ctypes.data, status.ctypes.data, self._err)
         self._check(ok)
         return res["id"].copy(), res["distance"].copy(), counts, status

@@ -507,7 +507,7 @@ bool ngtgpu_linear_search_tc_float_ex(NGTIndex index, const float* queries, size
 bool ngtgpu_linear_search_tc_ex(NGTIndex index, const void* d_rows, size_t nq, size_t size, size_t candidates,
                                 uint32_t precision, uint32_t flags, NGTObjectDistance* d_results, size_t kmax,
                                 uint32_t* d_counts, uint32_t* d_status, void* stream, NGTError error) {
-  if (index == nullptr || precision > NGTGPU_TC_FP8 || (flags & ~NGTGPU_TC_FP64_TIES) != 0 ||
+  if (index == nullptr || precision > NGTGPU_TC_FP8 || (flags & ~(NGTGPU_TC_FP64_TIES | NGTGPU_TC_PAIR)) != 0 ||
       (nq && (d_rows == nullptr || d_results == nullptr || d_counts == nullptr || d_status == nullptr))) {
     CAPI_PARAM_ERROR(error, "index = " << index << " rows = " << d_rows << " nq = " << nq << " precision = "
                                        << precision << " flags = " << flags);
@@ -518,7 +518,8 @@ bool ngtgpu_linear_search_tc_ex(NGTIndex index, const void* d_rows, size_t nq, s
     cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : e->stream();
     e->linear_search_tc_device(static_cast<const uint4*>(d_rows), nq, size, candidates,
                                reinterpret_cast<ngtg::ObjDist*>(d_results), kmax, d_counts, d_status, s,
-                               precision == NGTGPU_TC_FP8, (flags & NGTGPU_TC_FP64_TIES) != 0);
+                               precision == NGTGPU_TC_FP8, (flags & NGTGPU_TC_FP64_TIES) != 0,
+                               (flags & NGTGPU_TC_PAIR) != 0);
     return true;
   }
   CAPI_CATCH(error, false)
@@ -528,7 +529,8 @@ namespace {
 bool tc_float_impl(NGTIndex index, const float* queries, size_t nq, int32_t dim, size_t size, size_t candidates,
                    uint32_t precision, uint32_t flags, NGTObjectDistance* results, size_t kmax, uint32_t* counts,
                    uint32_t* status, NGTError error) {
-  if (index == nullptr || dim <= 0 || precision > NGTGPU_TC_FP8 || (flags & ~NGTGPU_TC_FP64_TIES) != 0 ||
+  if (index == nullptr || dim <= 0 || precision > NGTGPU_TC_FP8 ||
+      (flags & ~(NGTGPU_TC_FP64_TIES | NGTGPU_TC_PAIR)) != 0 ||
       (nq && (queries == nullptr || results == nullptr || counts == nullptr || status == nullptr))) {
     CAPI_PARAM_ERROR(error, "index = " << index << " queries = " << queries << " nq = " << nq << " dim = " << dim);
     return false;
@@ -558,7 +560,7 @@ bool tc_float_impl(NGTIndex index, const float* queries, size_t nq, int32_t dim,
     e->linear_search_tc_device(static_cast<const uint4*>(b.p[0]), nq, size, candidates,
                                static_cast<ngtg::ObjDist*>(b.p[1]), kmax, static_cast<uint32_t*>(b.p[2]),
                                static_cast<uint32_t*>(b.p[3]), s, precision == NGTGPU_TC_FP8,
-                               (flags & NGTGPU_TC_FP64_TIES) != 0);
+                               (flags & NGTGPU_TC_FP64_TIES) != 0, (flags & NGTGPU_TC_PAIR) != 0);
     ck(cudaMemcpyAsync(results, b.p[1], nq * kmax * sizeof(NGTObjectDistance), cudaMemcpyDeviceToHost, s));
     ck(cudaMemcpyAsync(counts, b.p[2], nq * 4, cudaMemcpyDeviceToHost, s));
     ck(cudaMemcpyAsync(status, b.p[3], nq * 4, cudaMemcpyDeviceToHost, s));

@@ -208,7 +208,7 @@ class GraphEngine {
   // window too wide, fp32 order kept).
   void linear_search_tc_device(const uint4* d_rows, size_t nq, size_t size, size_t candidates, ObjDist* d_out,
                                size_t kmax, uint32_t* d_counts, uint32_t* d_status, cudaStream_t stream,
-                               bool fp8 = false, bool fp64_ties = false);
+                               bool fp8 = false, bool fp64_ties = false, bool pair = false);
   // The approximate scores alone: d_scores[q * ld + row] (-inf for the unused
   // row 0 and removed objects).
   void tc_scores_device(const uint4* d_rows, size_t nq, float* d_scores, size_t ld, cudaStream_t stream);

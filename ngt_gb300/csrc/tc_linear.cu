@@ -147,6 +147,27 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
+// The same load, multicast: the box lands at the same shared-memory offset in every
+// CTA of the cluster named in `mask`, and signals the mbarrier at the same offset in
+// each of them.
+__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y,
+                                               uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster"
+      " [%0], [%1, {%3, %4}], [%2], %5;"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y), "h"(mask)
+      : "memory");
+}
+__device__ __forceinline__ uint32_t cluster_ctarank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+// Every thread of every CTA of the cluster (all of them execute it, converged).
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
 
@@ -173,6 +194,12 @@ __device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t
 }
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+// The commit's arrive on the mbarrier at the same offset in every CTA of `mask`.
+__device__ __forceinline__ void mma_commit_mc(uint32_t bar, uint16_t mask) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+               ::"r"(bar), "h"(mask)
+               : "memory");
 }
 
 // 32 consecutive fp32 columns of this warp's 32 TMEM lanes, one lane per thread.
@@ -216,7 +243,12 @@ __device__ __forceinline__ float key_score(uint32_t key) {
 // kFp8: A (rows) and B (queries) hold per-row / per-query scaled E4M3 values; the
 // accumulator is multiplied by the query's scale in the epilogue (the row's scale
 // is folded into row_scale).
-template <bool kDense, bool kFp8>
+// kPair: the CTAs run in clusters of two that take row tiles 2i and 2i+1 of the same
+// query tile: each loads its own row tile and one half of the query tile, multicast
+// to both (mapB then has 128-row boxes), so the query tiles cross L2 half as often;
+// a stage is free again when the MMAs of both CTAs consumed it (their commits
+// arrive on the stage's empty barrier in both CTAs).
+template <bool kDense, bool kFp8, bool kPair>
 __global__ void __launch_bounds__(THREADS, 1)
 tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, ScoreArgs a) {
   extern __shared__ __align__(1024) unsigned char dsmem[];
@@ -227,12 +259,18 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t mtiles = (a.row_end - a.row_begin + BM - 1) / BM;
   const uint32_t ntiles = (a.nq + BN - 1) / BN;
-  const uint32_t tiles = mtiles * ntiles;
+  // work units: tiles, or (kPair) pairs of row tiles of one query tile per cluster
+  const uint32_t rank = kPair ? cluster_ctarank() : 0u;
+  const uint32_t unit0 = kPair ? blockIdx.x >> 1 : blockIdx.x;
+  const uint32_t ustep = kPair ? gridDim.x >> 1 : gridDim.x;
+  const uint32_t units = kPair ? (mtiles + 1) / 2 * ntiles : mtiles * ntiles;
+  // row tile and query tile of work unit u
+  auto row_tile = [&](uint32_t u) { return kPair ? 2 * (u / ntiles) + rank : u / ntiles; };
 
   if (threadIdx.x == 0) {
     for (uint32_t s = 0; s < STAGES; s++) {
       mbar_init(smem_u32(&bar_full[s]), 1);
-      mbar_init(smem_u32(&bar_empty[s]), 1);
+      mbar_init(smem_u32(&bar_empty[s]), kPair ? 2 : 1);
     }
     for (uint32_t b = 0; b < 2; b++) {
       mbar_init(smem_u32(&bar_tfull[b]), 1);
@@ -251,6 +289,7 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
+  if constexpr (kPair) cluster_sync();        // both CTAs' barriers exist before any multicast
   const uint32_t tmem = tmem_base_sh;
 
   if (warp == 0) {
@@ -258,8 +297,8 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
       // TMA producer
       uint32_t stage = 0, phase = 0;
       uint32_t pending = 0, last_parity = 0;     // per stage: a load in flight, parity of its phase
-      for (uint32_t t = blockIdx.x; t < tiles && !abort_sh; t += gridDim.x) {
-        const int row0 = (int)(a.row_begin + (t / ntiles) * BM);
+      for (uint32_t t = unit0; t < units && !abort_sh; t += ustep) {
+        const int row0 = (int)(a.row_begin + row_tile(t) * BM);
         const int q0 = (int)((t % ntiles) * BN);
         for (uint32_t kb = 0; kb < a.kblocks; kb++) {
           if (!mbar_wait(smem_u32(&bar_empty[stage]), phase ^ 1u, &abort_sh)) {
@@ -271,7 +310,10 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
           const uint32_t fb = smem_u32(&bar_full[stage]);
           mbar_expect_tx(fb, STAGE_BYTES);
           tma_load_2d(sA, &mapA, fb, (int)(kb * BK), row0);
-          tma_load_2d(sB, &mapB, fb, (int)(kb * BK), q0);
+          if constexpr (kPair)
+            tma_load_2d_mc(sB + rank * (B_BYTES / 2), &mapB, fb, (int)(kb * BK), q0 + (int)(rank * (BN / 2)), 3);
+          else
+            tma_load_2d(sB, &mapB, fb, (int)(kb * BK), q0);
           pending |= 1u << stage;
           last_parity = (last_parity & ~(1u << stage)) | (phase << stage);
           if (++stage == STAGES) {
@@ -288,7 +330,7 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
     if (lane == 0) {
       // MMA issuer
       uint32_t stage = 0, phase = 0, local = 0;
-      for (uint32_t t = blockIdx.x; t < tiles && !abort_sh; t += gridDim.x, local++) {
+      for (uint32_t t = unit0; t < units && !abort_sh; t += ustep, local++) {
         const uint32_t buf = local & 1u, tphase = (local >> 1) & 1u;
         if (!mbar_wait(smem_u32(&bar_tempty[buf]), tphase ^ 1u, &abort_sh)) {
           atomicOr(a.error, 2u);
@@ -314,7 +356,8 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
             else
               mma_bf16(d, sw128_desc(sA + k * 32), sw128_desc(sB + k * 32), (kb | k) != 0 ? 1u : 0u);
           }
-          mma_commit(smem_u32(&bar_empty[stage]));
+          if constexpr (kPair) mma_commit_mc(smem_u32(&bar_empty[stage]), 3);
+          else mma_commit(smem_u32(&bar_empty[stage]));
           if (++stage == STAGES) {
             stage = 0;
             phase ^= 1u;
@@ -333,10 +376,10 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
     const uint32_t quad = warp & 3u;
     const uint32_t half = (warp - 2u) >> 2;
     uint32_t local = 0;
-    for (uint32_t t = blockIdx.x; t < tiles; t += gridDim.x, local++) {
+    for (uint32_t t = unit0; t < units; t += ustep, local++) {
       const uint32_t buf = local & 1u, tphase = (local >> 1) & 1u;
       // what does not depend on the accumulator is loaded before the wait
-      const uint32_t row0 = a.row_begin + (t / ntiles) * BM;
+      const uint32_t row0 = a.row_begin + row_tile(t) * BM;
       const uint32_t q0 = (t % ntiles) * BN;
       const uint32_t row = row0 + quad * 32 + lane;
       const bool in_range = row < a.row_end;
@@ -394,6 +437,9 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
   }
   tc_fence_before();
   __syncthreads();
+  // the peer's multicast copies into this CTA and its MMA commits on this CTA's
+  // barriers are over before either CTA leaves
+  if constexpr (kPair) cluster_sync();
   if (warp == 1) {
     tc_fence_after();
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
@@ -918,26 +964,50 @@ void GraphEngine::ensure_tc_rows8() {
 
 namespace {
 
-template <bool kFp8>
+template <bool kFp8, bool kPair>
 void launch_scores_t(const CUtensorMap& mapA, const CUtensorMap& mapB, const tc::ScoreArgs& a, bool dense,
                      cudaStream_t s, unsigned grid) {
-  auto fn = dense ? tc::tc_score_kernel<true, kFp8> : tc::tc_score_kernel<false, kFp8>;
+  auto fn = dense ? tc::tc_score_kernel<true, kFp8, kPair> : tc::tc_score_kernel<false, kFp8, kPair>;
   TC_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_BYTES));
-  fn<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(mapA, mapB, a);
+  if constexpr (kPair) {
+    // clusters of two CTAs (grid even)
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(tc::THREADS);
+    cfg.dynamicSmemBytes = tc::SMEM_BYTES;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = 2;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    TC_CUDA(cudaLaunchKernelEx(&cfg, fn, mapA, mapB, a));
+  } else {
+    fn<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(mapA, mapB, a);
+  }
 }
 
-void launch_scores(const TcState& st, const CUtensorMap& mapB, tc::ScoreArgs a, bool dense, cudaStream_t s,
-                   int sms, bool fp8 = false) {
+// mapB: the query tiles (256-row boxes); mapBh: the same with 128-row boxes, for
+// the two-CTA (pair) kernel, which runs when `pair` is set.
+void launch_scores(const TcState& st, const CUtensorMap& mapB, const CUtensorMap* mapBh, tc::ScoreArgs a, bool dense,
+                   cudaStream_t s, int sms, bool fp8 = false) {
   const uint32_t mtiles = (a.row_end - a.row_begin + tc::BM - 1) / tc::BM;
-  const uint32_t tiles = mtiles * ((a.nq + tc::BN - 1) / tc::BN);
+  const uint32_t ntiles = (a.nq + tc::BN - 1) / tc::BN;
+  const uint32_t tiles = mtiles * ntiles;
   if (tiles == 0) return;
-  const unsigned grid = (unsigned)std::min<uint32_t>(tiles, (uint32_t)sms);
+  const bool pair = mapBh != nullptr;
+  const unsigned grid = pair ? 2u * (unsigned)std::min<uint32_t>((mtiles + 1) / 2 * ntiles, (uint32_t)sms / 2)
+                             : (unsigned)std::min<uint32_t>(tiles, (uint32_t)sms);
   if (fp8) {
     a.row_scale = st.scale8;
     a.kblocks = st.kpad8 / 128;
-    launch_scores_t<true>(st.mapA8, mapB, a, dense, s, grid);
+    if (pair) launch_scores_t<true, true>(st.mapA8, *mapBh, a, dense, s, grid);
+    else launch_scores_t<true, false>(st.mapA8, mapB, a, dense, s, grid);
   } else {
-    launch_scores_t<false>(st.mapA, mapB, a, dense, s, grid);
+    if (pair) launch_scores_t<false, true>(st.mapA, *mapBh, a, dense, s, grid);
+    else launch_scores_t<false, false>(st.mapA, mapB, a, dense, s, grid);
   }
   TC_CUDA(cudaGetLastError());
 }
@@ -982,7 +1052,7 @@ void GraphEngine::tc_scores_device(const uint4* d_rows, size_t nq, float* d_scor
   a.dense = d_scores;
   a.dense_ld = (uint32_t)ld;
   a.error = st.error;
-  launch_scores(st, mapB, a, true, stream, sms);
+  launch_scores(st, mapB, nullptr, a, true, stream, sms);
   launches_ += 2;
   TC_CUDA(cudaFreeAsync(qb, stream));
   check_error(st, stream);
@@ -990,7 +1060,7 @@ void GraphEngine::tc_scores_device(const uint4* d_rows, size_t nq, float* d_scor
 
 void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t size, size_t candidates,
                                           ObjDist* d_out, size_t kmax, uint32_t* d_counts, uint32_t* d_status,
-                                          cudaStream_t stream, bool fp8, bool fp64_ties) {
+                                          cudaStream_t stream, bool fp8, bool fp64_ties, bool pair) {
   std::lock_guard<std::mutex> lock(mu_);
   TC_CUDA(cudaSetDevice(device_));
   ensure_tc_rows();
@@ -1063,14 +1133,17 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
     const uint32_t nbpad = (nb + tc::BN - 1) / tc::BN * tc::BN;
     TC_CUDA(cudaEventRecord(st.ev[0], stream));
     const float* qrows = reinterpret_cast<const float*>(d_rows) + q0 * host_.dpad;
-    CUtensorMap mapB;
+    CUtensorMap mapB, mapBh;
     if (fp8) {
       tc::tc_queries8_kernel<<<1024, 256, 0, stream>>>(qrows, host_.dpad, nb, nbpad, st.kpad8, qbuf8, qscale);
       mapB = tc::make_map8(qbuf8, nbpad, st.kpad8, tc::BN);
+      if (pair) mapBh = tc::make_map8(qbuf8, nbpad, st.kpad8, tc::BN / 2);
     } else {
       tc::tc_queries_kernel<<<1024, 256, 0, stream>>>(qrows, host_.dpad, nb, nbpad, st.kpad, qbuf);
       mapB = tc::make_map(qbuf, nbpad, st.kpad, tc::BN);
+      if (pair) mapBh = tc::make_map(qbuf, nbpad, st.kpad, tc::BN / 2);
     }
+    const CUtensorMap* half = pair ? &mapBh : nullptr;
     TC_CUDA(cudaGetLastError());
     tc::ScoreArgs a{};
     a.nq = nb;
@@ -1085,7 +1158,7 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
     a.row_end = r0;
     a.dense = dense;
     a.dense_ld = (uint32_t)first;
-    launch_scores(st, mapB, a, true, stream, sms, fp8);
+    launch_scores(st, mapB, half, a, true, stream, sms, fp8);
     tc::tc_first_select_kernel<<<nb, 512, first * 8, stream>>>(dense, (uint32_t)first, r0 - rb, (uint32_t)C, thr,
                                                                cand, ccount, cap, rb);
     TC_CUDA(cudaGetLastError());
@@ -1122,7 +1195,7 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
       }
       a.row_begin = row;
       a.row_end = end;
-      launch_scores(st, mapB, a, false, stream, sms, fp8);
+      launch_scores(st, mapB, half, a, false, stream, sms, fp8);
       launches_++;
       if (end < nrows) {
         tc::tc_compact_kernel<<<nb, 512, cap * 8, stream>>>(cand, ccount, cap, (uint32_t)C, thr, d_status + q0);

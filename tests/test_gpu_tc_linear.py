@@ -260,3 +260,28 @@ def test_row_range_shards_merge_to_the_whole_search(workdir, nshards):
     assert np.array_equal(mn, wn)
     assert np.array_equal(mi, wi)
     assert np.array_equal(md.view(np.uint32), wd.view(np.uint32))
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp8"])
+def test_pair_clusters_equal_single_ctas(precision, workdir):
+    """The two-CTA cluster form of the score kernel (row tiles 2i and 2i+1 of one
+    query tile, the query tile multicast to both) returns the single-CTA results bit
+    for bit: 20,001 slots (157 row tiles, the last pair's second tile past the end),
+    600 queries (three query tiles, the last ragged), a 2,048-row dense part and the
+    filtered parts; and on a 1,000-row fixture with one row tile."""
+    from ngt_gb300 import Index
+    path, x, _ = _cluster_index(workdir)
+    rng = np.random.default_rng(5)
+    q = x[rng.integers(0, len(x), 600)] + 0.05 * rng.standard_normal((600, x.shape[1])).astype(np.float32)
+    with Index(path, read_only=True) as ix:
+        ref = ix.linear_search_tc(q, k=100, candidates=400, first_rows=2048, precision=precision)
+        got = ix.linear_search_tc(q, k=100, candidates=400, first_rows=2048, precision=precision, pair=True)
+    assert (ref[3] == 0).all()
+    for a, b in zip(ref, got):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    path, meta, queries, golden = materialize("c1_f32_l2", workdir)
+    with Index(path, read_only=True) as ix:
+        ref = ix.linear_search_tc(queries, k=10, candidates=64, first_rows=0, precision=precision)
+        got = ix.linear_search_tc(queries, k=10, candidates=64, first_rows=0, precision=precision, pair=True)
+    for a, b in zip(ref, got):
+        assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
