@@ -386,6 +386,17 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
       const bool rvalid = in_range && row != 0 && a.present[row];
       const float sc = rvalid ? a.row_scale[row] : 0.f;
       const float bi = rvalid ? a.row_bias[row] : 0.f;
+      // per chunk of 32 queries of this warp's half: lane j holds the threshold
+      // (+inf past the last query) and the scale of query qb + j
+      constexpr uint32_t CH = BN / 64;
+      static_assert(CH == 4, "four chunks of 32 queries per epilogue warp");
+      float thr_c[CH], qs_c[CH];
+#pragma unroll
+      for (uint32_t i = 0; i < CH; i++) {
+        const uint32_t qj = q0 + (half * CH + i) * 32 + lane;
+        thr_c[i] = (!kDense && qj < a.nq) ? __ldg(a.thr + qj) : INFINITY;
+        qs_c[i] = (kFp8 && qj < a.nq) ? __ldg(a.qscale + qj) : 1.f;
+      }
       uint32_t ok = 1;
       if (lane == 0) ok = mbar_wait(smem_u32(&bar_tfull[buf]), tphase, &abort_sh) ? 1u : 0u;
       ok = __shfl_sync(0xffffffffu, ok, 0);     // the warp stays converged for tcgen05.ld
@@ -395,38 +406,66 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
         break;
       }
       tc_fence_after();
-      for (uint32_t c = half * (BN / 64); c < (half + 1) * (BN / 64); c++) {
-        const uint32_t qb = q0 + c * 32;
+      // a rolled loop over the chunks keeps the epilogue's code small (the
+      // thresholds of the next chunks shift down into thr_c[0] / qs_c[0])
+#pragma unroll 1
+      for (uint32_t i = 0; i < CH; i++) {
+        const uint32_t qb = q0 + (half * CH + i) * 32;
         if (qb >= a.nq) break;                   // warp-uniform
-        // lane j holds the threshold of query qb + j (+inf past the last query)
-        float my_thr = INFINITY, my_qs = 1.f;
-        if (!kDense && qb + lane < a.nq) my_thr = __ldg(a.thr + qb + lane);
-        if (kFp8 && qb + lane < a.nq) my_qs = __ldg(a.qscale + qb + lane);
+        const float thr = thr_c[0], qs = qs_c[0];
+#pragma unroll
+        for (uint32_t c = 0; c + 1 < CH; c++) {
+          thr_c[c] = thr_c[c + 1];
+          qs_c[c] = qs_c[c + 1];
+        }
         uint32_t v[32];
-        tmem_ld32(tmem + ((quad * 32u) << 16) + buf * BN + c * 32, v);
+        tmem_ld32(tmem + ((quad * 32u) << 16) + buf * BN + (half * CH + i) * 32, v);
         tmem_ld_wait(v);
         if (kDense) {
 #pragma unroll
           for (uint32_t j = 0; j < 32; j++) {
             const uint32_t q = qb + j;
             // the shuffle runs on every lane of the warp, whatever its row
-            const float scj = kFp8 ? sc * __shfl_sync(0xffffffffu, my_qs, j) : sc;
+            const float scj = kFp8 ? sc * __shfl_sync(0xffffffffu, qs, j) : sc;
             const float s = fmaf(__uint_as_float(v[j]), scj, bi) + 0.0f;
             if (in_range && q < a.nq) a.dense[(size_t)q * a.dense_ld + (row - a.row_begin)] = rvalid ? s : -INFINITY;
           }
         } else {
+          // passed: the queries of the chunk whose threshold this lane's row passes
+          uint32_t passed = 0;
 #pragma unroll
           for (uint32_t j = 0; j < 32; j++) {
-            const float t = __shfl_sync(0xffffffffu, my_thr, j);
-            const float scj = kFp8 ? sc * __shfl_sync(0xffffffffu, my_qs, j) : sc;
+            const float t = __shfl_sync(0xffffffffu, thr, j);
+            const float scj = kFp8 ? sc * __shfl_sync(0xffffffffu, qs, j) : sc;
             const float s = fmaf(__uint_as_float(v[j]), scj, bi);
-            if (rvalid && s > t) {
-              const uint32_t q = qb + j;
-              const uint32_t slot = atomicAdd(a.cand_count + q, 1u);
-              if (slot < a.cap)
-                a.cand[(size_t)q * a.cap + slot] = ((unsigned long long)score_key(s) << 32) | row;
-              else
-                atomicOr(a.status + q, 1u);
+            passed |= (rvalid && s > t) ? 1u << j : 0u;
+          }
+          if (__any_sync(0xffffffffu, passed != 0u)) {
+            // mine (lane j): the rows of this warp that pass query qb + j; one
+            // atomic per query reserves the slots of all of them
+            uint32_t mine = 0;
+#pragma unroll
+            for (uint32_t j = 0; j < 32; j++) {
+              const uint32_t m = __ballot_sync(0xffffffffu, (passed >> j) & 1u);
+              mine = lane == j ? m : mine;
+            }
+            uint32_t base = 0;
+            if (mine != 0u) base = atomicAdd(a.cand_count + qb + lane, (uint32_t)__popc(mine));
+            const uint32_t below = (1u << lane) - 1u;
+#pragma unroll
+            for (uint32_t j = 0; j < 32; j++) {
+              const uint32_t mj = __shfl_sync(0xffffffffu, mine, j);
+              const uint32_t bj = __shfl_sync(0xffffffffu, base, j);
+              const float scj = kFp8 ? sc * __shfl_sync(0xffffffffu, qs, j) : sc;
+              if ((passed >> j) & 1u) {
+                const uint32_t q = qb + j;
+                const uint32_t slot = bj + (uint32_t)__popc(mj & below);
+                const float s = fmaf(__uint_as_float(v[j]), scj, bi);
+                if (slot < a.cap)
+                  a.cand[(size_t)q * a.cap + slot] = ((unsigned long long)score_key(s) << 32) | row;
+                else
+                  atomicOr(a.status + q, 1u);
+              }
             }
           }
         }
