@@ -69,11 +69,18 @@ constexpr uint32_t A_BYTES = BM * BK * 2;
 constexpr uint32_t B_BYTES = BN * BK * 2;
 constexpr uint32_t STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr uint32_t SMEM_BYTES = STAGES * STAGE_BYTES + 1024;   // + slack for 1024-byte alignment
+// The two-SM form (cta_group::2): each CTA of a pair stages its own 128 rows and
+// one half (128 queries) of the query tile, 32 KB per k-block, in 6 stages.
+constexpr uint32_t STAGES2 = 6;
+constexpr uint32_t STAGE2_BYTES = A_BYTES + B_BYTES / 2;
+constexpr uint32_t MAX_STAGES = STAGES2 > STAGES ? STAGES2 : STAGES;
+static_assert(STAGES2 * STAGE2_BYTES + 1024 <= SMEM_BYTES, "two-SM stages fit the same shared memory");
 constexpr uint32_t EPI_WARPS = 8;       // two per TMEM lane quadrant, each half of the columns
 constexpr uint32_t THREADS = 64 + 32 * EPI_WARPS;   // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
 constexpr uint32_t TMEM_COLS = 2 * BN;
 constexpr uint32_t kInvalidKey = 0xff800000u;   // score key of -inf; valid keys are smaller
 constexpr uint64_t kWaitNs = 2000000000ull;     // bound of every wait (2 s)
+constexpr int kDeferQueries = 8;                // filter epilogue: see tc_score_kernel
 
 // Instruction descriptor of tcgen05.mma kind::f16: D fp32 (bits 4-5 = 1), A and
 // B bf16 (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
@@ -83,6 +90,10 @@ constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((BN >> 3) << 1
 // consumes K = 32 one-byte elements, the same 32 bytes of each 128-byte swizzle
 // row as a bf16 MMA's K = 16, so staging, descriptors and k-steps are shared.
 constexpr uint32_t kIdescF8 = (1u << 4) | ((BN >> 3) << 17) | ((BM >> 4) << 24);
+// The same with M = 256 for a pair of CTAs (cta_group::2): rows 0-127 from the
+// first CTA's A tile, 128-255 from the second's; each accumulates its own 128 rows.
+constexpr uint32_t kIdesc2 = (kIdesc & ~(0x1Fu << 24)) | (((2 * BM) >> 4) << 24);
+constexpr uint32_t kIdescF8_2 = (kIdescF8 & ~(0x1Fu << 24)) | (((2 * BM) >> 4) << 24);
 constexpr float kE4M3Max = 448.f;       // largest finite E4M3 value
 
 struct ScoreArgs {
@@ -128,6 +139,16 @@ __device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+__device__ __forceinline__ bool mbar_try_cluster(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
 // Waits until the phase of parity `parity` completed; false when the wait ran
 // out (kWaitNs) or another role aborted (abort may be null: no abort check).
 __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, const volatile uint32_t* abort) {
@@ -135,6 +156,16 @@ __device__ __noinline__ bool mbar_wait(uint32_t bar, uint32_t parity, const vola
   const uint64_t t0 = global_ns();
   while (true) {
     if (mbar_try(bar, parity)) return true;
+    if (abort && *abort) return false;
+    if (global_ns() - t0 > kWaitNs) return false;
+  }
+}
+// The same with acquire at cluster scope (arrivals from the other CTA of a pair).
+__device__ __noinline__ bool mbar_wait_cluster(uint32_t bar, uint32_t parity, const volatile uint32_t* abort) {
+  if (mbar_try_cluster(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  while (true) {
+    if (mbar_try_cluster(bar, parity)) return true;
     if (abort && *abort) return false;
     if (global_ns() - t0 > kWaitNs) return false;
   }
@@ -147,16 +178,25 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
-// The same load, multicast: the box lands at the same shared-memory offset in every
-// CTA of the cluster named in `mask`, and signals the mbarrier at the same offset in
-// each of them.
-__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y,
-                                               uint16_t mask) {
+// The same load for a CTA pair (cta_group::2): the box lands in this CTA's shared
+// memory and completes on `bar`, a shared::cluster address that may name the
+// mbarrier of the other CTA of the pair.
+__device__ __forceinline__ void tma_load_2d_pair(uint32_t dst, const CUtensorMap* map, uint32_t bar, int x, int y) {
   asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster"
-      " [%0], [%1, {%3, %4}], [%2], %5;"
-      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y), "h"(mask)
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.cta_group::2"
+      " [%0], [%1, {%3, %4}], [%2];"
+      ::"r"(dst), "l"(reinterpret_cast<uint64_t>(map)), "r"(bar), "r"(x), "r"(y)
       : "memory");
+}
+// shared::cluster address of this CTA's shared-memory address `addr` in CTA `rank`.
+__device__ __forceinline__ uint32_t map_to_rank(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+// Arrive on an mbarrier of any CTA of the cluster (release at cluster scope).
+__device__ __forceinline__ void mbar_arrive_cluster(uint32_t bar_cluster) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];" ::"r"(bar_cluster) : "memory");
 }
 __device__ __forceinline__ uint32_t cluster_ctarank() {
   uint32_t r;
@@ -195,11 +235,32 @@ __device__ __forceinline__ void mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t
 __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
-// The commit's arrive on the mbarrier at the same offset in every CTA of `mask`.
-__device__ __forceinline__ void mma_commit_mc(uint32_t bar, uint16_t mask) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
-               ::"r"(bar), "h"(mask)
-               : "memory");
+
+// The CTA-pair forms (every tcgen05 instruction of a kernel has the same
+// cta_group): one thread of the pair's first CTA issues the M = 256 MMA, whose
+// A and B descriptors name the same shared-memory offsets in both CTAs.
+__device__ __forceinline__ void mma_bf16_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}"
+      ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(kIdesc2), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void mma_f8_pair(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::2.kind::f8f6f4 [%0], %1, %2, %3, p;\n}"
+      ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(kIdescF8_2), "r"(accumulate)
+      : "memory");
+}
+// Arrive on the mbarrier at offset `bar` of both CTAs of the pair when the
+// pair's MMAs issued so far have completed.
+__device__ __forceinline__ void mma_commit_pair_both(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;"
+      ::"r"(bar), "h"((uint16_t)3)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit_pair_local(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
 // 32 consecutive fp32 columns of this warp's 32 TMEM lanes, one lane per thread.
@@ -226,6 +287,16 @@ __device__ __forceinline__ void tmem_ld_wait(uint32_t (&v)[32]) {
                : "memory");
 }
 
+// One fp32 column of this warp's 32 TMEM lanes, one lane per thread, loaded and waited for.
+__device__ __forceinline__ uint32_t tmem_ld1(uint32_t taddr) {
+  uint32_t r;
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x1.b32 {%0}, [%1];\n\ttcgen05.wait::ld.sync.aligned;"
+               : "=r"(r)
+               : "r"(taddr)
+               : "memory");
+  return r;
+}
+
 // Larger score -> smaller key (unsigned order); NaN and -inf -> kInvalidKey or
 // above.  -0 is folded to +0, so that "key < key(t)" and "s > t" agree.
 __device__ __forceinline__ uint32_t score_key(float s) {
@@ -243,53 +314,67 @@ __device__ __forceinline__ float key_score(uint32_t key) {
 // kFp8: A (rows) and B (queries) hold per-row / per-query scaled E4M3 values; the
 // accumulator is multiplied by the query's scale in the epilogue (the row's scale
 // is folded into row_scale).
-// kPair: the CTAs run in clusters of two that take row tiles 2i and 2i+1 of the same
-// query tile: each loads its own row tile and one half of the query tile, multicast
-// to both (mapB then has 128-row boxes), so the query tiles cross L2 half as often;
-// a stage is free again when the MMAs of both CTAs consumed it (their commits
-// arrive on the stage's empty barrier in both CTAs).
+// kPair: the CTAs run in pairs (clusters of two) on the two-SM MMA: a work unit is
+// row tiles 2i and 2i+1 of one query tile.  Each CTA stages its own row tile and
+// one half of the query tile (128 queries); the first CTA's MMA thread issues
+// M = 256 x N = 256 MMAs over both CTAs' shared memory, each CTA's TMEM holding
+// its own rows' accumulator.  Both CTAs' copies complete on the first CTA's
+// stage barrier; the MMA commits arrive on both CTAs' stage-empty and
+// accumulator-full barriers; both CTAs' epilogue warps arrive on the first
+// CTA's accumulator-empty barrier.
 template <bool kDense, bool kFp8, bool kPair>
 __global__ void __launch_bounds__(THREADS, 1)
 tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, ScoreArgs a) {
+  constexpr uint32_t NST = kPair ? STAGES2 : STAGES;
+  constexpr uint32_t SBYTES = kPair ? STAGE2_BYTES : STAGE_BYTES;
   extern __shared__ __align__(1024) unsigned char dsmem[];
-  __shared__ __align__(8) uint64_t bar_full[STAGES], bar_empty[STAGES], bar_tfull[2], bar_tempty[2], bar_drain;
+  __shared__ __align__(8) uint64_t bar_full[MAX_STAGES], bar_empty[MAX_STAGES], bar_tfull[2], bar_tempty[2], bar_drain;
   __shared__ uint32_t tmem_base_sh;
   __shared__ volatile uint32_t abort_sh;
   const uint32_t base = (smem_u32(dsmem) + 1023u) & ~1023u;
   const uint32_t warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t mtiles = (a.row_end - a.row_begin + BM - 1) / BM;
   const uint32_t ntiles = (a.nq + BN - 1) / BN;
-  // work units: tiles, or (kPair) pairs of row tiles of one query tile per cluster
+  // work units: tiles, or (kPair) pairs of row tiles of one query tile per CTA pair
   const uint32_t rank = kPair ? cluster_ctarank() : 0u;
   const uint32_t unit0 = kPair ? blockIdx.x >> 1 : blockIdx.x;
   const uint32_t ustep = kPair ? gridDim.x >> 1 : gridDim.x;
   const uint32_t units = kPair ? (mtiles + 1) / 2 * ntiles : mtiles * ntiles;
-  // row tile and query tile of work unit u
+  // row tile of work unit u (the query tile is u % ntiles)
   auto row_tile = [&](uint32_t u) { return kPair ? 2 * (u / ntiles) + rank : u / ntiles; };
 
   if (threadIdx.x == 0) {
-    for (uint32_t s = 0; s < STAGES; s++) {
+    for (uint32_t s = 0; s < NST; s++) {
       mbar_init(smem_u32(&bar_full[s]), 1);
-      mbar_init(smem_u32(&bar_empty[s]), kPair ? 2 : 1);
+      mbar_init(smem_u32(&bar_empty[s]), 1);
     }
     for (uint32_t b = 0; b < 2; b++) {
       mbar_init(smem_u32(&bar_tfull[b]), 1);
-      mbar_init(smem_u32(&bar_tempty[b]), 32 * EPI_WARPS);
+      // one arrival per epilogue thread, or (kPair) per epilogue warp of both CTAs
+      mbar_init(smem_u32(&bar_tempty[b]), kPair ? 2 * EPI_WARPS : 32 * EPI_WARPS);
     }
     mbar_init(smem_u32(&bar_drain), 1);
     abort_sh = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tmem_base_sh)),
-                 "r"(TMEM_COLS)
-                 : "memory");
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    if constexpr (kPair) {
+      // one warp of each CTA of the pair allocates collectively: the same columns in both
+      asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], %1;"
+                   ::"r"(smem_u32(&tmem_base_sh)), "r"(TMEM_COLS)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;" ::: "memory");
+    } else {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                   ::"r"(smem_u32(&tmem_base_sh)), "r"(TMEM_COLS)
+                   : "memory");
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
   }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  if constexpr (kPair) cluster_sync();        // both CTAs' barriers exist before any multicast
+  if constexpr (kPair) cluster_sync();        // both CTAs' barriers exist before any remote arrive
   const uint32_t tmem = tmem_base_sh;
 
   if (warp == 0) {
@@ -306,33 +391,46 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
             abort_sh = 1;
             break;
           }
-          const uint32_t sA = base + stage * STAGE_BYTES, sB = sA + A_BYTES;
+          const uint32_t sA = base + stage * SBYTES, sB = sA + A_BYTES;
           const uint32_t fb = smem_u32(&bar_full[stage]);
-          mbar_expect_tx(fb, STAGE_BYTES);
-          tma_load_2d(sA, &mapA, fb, (int)(kb * BK), row0);
-          if constexpr (kPair)
-            tma_load_2d_mc(sB + rank * (B_BYTES / 2), &mapB, fb, (int)(kb * BK), q0 + (int)(rank * (BN / 2)), 3);
-          else
+          if constexpr (kPair) {
+            // both CTAs' copies complete on the first CTA's stage barrier
+            if (rank == 0) mbar_expect_tx(fb, 2 * STAGE2_BYTES);
+            const uint32_t fb0 = map_to_rank(fb, 0);
+            tma_load_2d_pair(sA, &mapA, fb0, (int)(kb * BK), row0);
+            tma_load_2d_pair(sB, &mapB, fb0, (int)(kb * BK), q0 + (int)(rank * (BN / 2)));
+          } else {
+            mbar_expect_tx(fb, STAGE_BYTES);
+            tma_load_2d(sA, &mapA, fb, (int)(kb * BK), row0);
             tma_load_2d(sB, &mapB, fb, (int)(kb * BK), q0);
+          }
           pending |= 1u << stage;
           last_parity = (last_parity & ~(1u << stage)) | (phase << stage);
-          if (++stage == STAGES) {
+          if (++stage == NST) {
             stage = 0;
             phase ^= 1u;
           }
         }
       }
-      // no copy may land in shared memory after the CTA exits
-      for (uint32_t s = 0; s < STAGES; s++)
-        if (pending & (1u << s)) mbar_wait(smem_u32(&bar_full[s]), (last_parity >> s) & 1u, nullptr);
+      // no copy may land in shared memory after the CTA exits: wait for the last
+      // phase of each stage used (kPair: its consumption, which follows the copies)
+      for (uint32_t s = 0; s < NST; s++) {
+        if (!(pending & (1u << s))) continue;
+        if constexpr (kPair)
+          mbar_wait(smem_u32(&bar_empty[s]), (last_parity >> s) & 1u, nullptr);
+        else
+          mbar_wait(smem_u32(&bar_full[s]), (last_parity >> s) & 1u, nullptr);
+      }
     }
   } else if (warp == 1) {
-    if (lane == 0) {
-      // MMA issuer
+    if (lane == 0 && rank == 0) {
+      // MMA issuer (kPair: the first CTA's, for both)
       uint32_t stage = 0, phase = 0, local = 0;
       for (uint32_t t = unit0; t < units && !abort_sh; t += ustep, local++) {
         const uint32_t buf = local & 1u, tphase = (local >> 1) & 1u;
-        if (!mbar_wait(smem_u32(&bar_tempty[buf]), tphase ^ 1u, &abort_sh)) {
+        const bool ready = kPair ? mbar_wait_cluster(smem_u32(&bar_tempty[buf]), tphase ^ 1u, &abort_sh)
+                                 : mbar_wait(smem_u32(&bar_tempty[buf]), tphase ^ 1u, &abort_sh);
+        if (!ready) {
           atomicOr(a.error, 2u);
           abort_sh = 1;
           break;
@@ -348,26 +446,30 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
             break;
           }
           tc_fence_after();
-          const uint32_t sA = base + stage * STAGE_BYTES, sB = sA + A_BYTES;
+          const uint32_t sA = base + stage * SBYTES, sB = sA + A_BYTES;
 #pragma unroll
           for (uint32_t k = 0; k < BK / 16; k++) {
-            if constexpr (kFp8)
-              mma_f8(d, sw128_desc(sA + k * 32), sw128_desc(sB + k * 32), (kb | k) != 0 ? 1u : 0u);
-            else
-              mma_bf16(d, sw128_desc(sA + k * 32), sw128_desc(sB + k * 32), (kb | k) != 0 ? 1u : 0u);
+            const uint64_t da = sw128_desc(sA + k * 32), db = sw128_desc(sB + k * 32);
+            const uint32_t acc = (kb | k) != 0 ? 1u : 0u;
+            if constexpr (kPair && kFp8) mma_f8_pair(d, da, db, acc);
+            else if constexpr (kPair) mma_bf16_pair(d, da, db, acc);
+            else if constexpr (kFp8) mma_f8(d, da, db, acc);
+            else mma_bf16(d, da, db, acc);
           }
-          if constexpr (kPair) mma_commit_mc(smem_u32(&bar_empty[stage]), 3);
+          if constexpr (kPair) mma_commit_pair_both(smem_u32(&bar_empty[stage]));
           else mma_commit(smem_u32(&bar_empty[stage]));
-          if (++stage == STAGES) {
+          if (++stage == NST) {
             stage = 0;
             phase ^= 1u;
           }
         }
         if (!ok) break;
-        mma_commit(smem_u32(&bar_tfull[buf]));
+        if constexpr (kPair) mma_commit_pair_both(smem_u32(&bar_tfull[buf]));
+        else mma_commit(smem_u32(&bar_tfull[buf]));
       }
       // every MMA issued has completed before TMEM is released
-      mma_commit(smem_u32(&bar_drain));
+      if constexpr (kPair) mma_commit_pair_local(smem_u32(&bar_drain));
+      else mma_commit(smem_u32(&bar_drain));
       mbar_wait(smem_u32(&bar_drain), 0, nullptr);
     }
   } else {
@@ -406,22 +508,21 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
         break;
       }
       tc_fence_after();
-      // a rolled loop over the chunks keeps the epilogue's code small (the
-      // thresholds of the next chunks shift down into thr_c[0] / qs_c[0])
+      // this warp's first TMEM column: lanes 32 * quad.., columns of its half
+      const uint32_t tcol = tmem + ((quad * 32u) << 16) + buf * BN + half * CH * 32;
+      // rolled loops over the chunks keep the epilogue's code small (per-chunk
+      // values shift down into index 0 of their arrays)
+      if constexpr (kDense) {
 #pragma unroll 1
-      for (uint32_t i = 0; i < CH; i++) {
-        const uint32_t qb = q0 + (half * CH + i) * 32;
-        if (qb >= a.nq) break;                   // warp-uniform
-        const float thr = thr_c[0], qs = qs_c[0];
+        for (uint32_t i = 0; i < CH; i++) {
+          const uint32_t qb = q0 + (half * CH + i) * 32;
+          if (qb >= a.nq) break;                 // warp-uniform
+          const float qs = qs_c[0];
 #pragma unroll
-        for (uint32_t c = 0; c + 1 < CH; c++) {
-          thr_c[c] = thr_c[c + 1];
-          qs_c[c] = qs_c[c + 1];
-        }
-        uint32_t v[32];
-        tmem_ld32(tmem + ((quad * 32u) << 16) + buf * BN + (half * CH + i) * 32, v);
-        tmem_ld_wait(v);
-        if (kDense) {
+          for (uint32_t c = 0; c + 1 < CH; c++) qs_c[c] = qs_c[c + 1];
+          uint32_t v[32];
+          tmem_ld32(tcol + i * 32, v);
+          tmem_ld_wait(v);
 #pragma unroll
           for (uint32_t j = 0; j < 32; j++) {
             const uint32_t q = qb + j;
@@ -430,8 +531,33 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
             const float s = fmaf(__uint_as_float(v[j]), scj, bi) + 0.0f;
             if (in_range && q < a.nq) a.dense[(size_t)q * a.dense_ld + (row - a.row_begin)] = rvalid ? s : -INFINITY;
           }
-        } else {
-          // passed: the queries of the chunk whose threshold this lane's row passes
+        }
+      } else {
+        // Pass 1 over the chunks: the filter.  A chunk where more than
+        // kDeferQueries queries have passing rows stores its entries at once (one
+        // atomic per query, all 32 queries in one warp-wide step).  Otherwise each
+        // such query gets one atomic that reserves its rows' slots, issued without
+        // waiting for its result, and pass 2 reads that query's score column again
+        // from TMEM and stores the (key, row) entries: the tile's atomics are in
+        // flight together instead of one round trip per chunk.
+        float qs_k[CH];
+        uint32_t pass_c[CH] = {}, base_c[CH] = {}, any_c[CH] = {};
+#pragma unroll
+        for (uint32_t c = 0; c < CH; c++) qs_k[c] = qs_c[c];
+#pragma unroll 1
+        for (uint32_t i = 0; i < CH; i++) {
+          const uint32_t qb = q0 + (half * CH + i) * 32;
+          const float thr = thr_c[0], qs = qs_c[0];
+#pragma unroll
+          for (uint32_t c = 0; c + 1 < CH; c++) {
+            thr_c[c] = thr_c[c + 1];
+            qs_c[c] = qs_c[c + 1];
+          }
+          uint32_t v[32];
+          tmem_ld32(tcol + i * 32, v);
+          tmem_ld_wait(v);
+          // passed: the queries of the chunk whose threshold this lane's row
+          // passes (none past the last query: its threshold is +inf)
           uint32_t passed = 0;
 #pragma unroll
           for (uint32_t j = 0; j < 32; j++) {
@@ -440,16 +566,17 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
             const float s = fmaf(__uint_as_float(v[j]), scj, bi);
             passed |= (rvalid && s > t) ? 1u << j : 0u;
           }
-          if (__any_sync(0xffffffffu, passed != 0u)) {
-            // mine (lane j): the rows of this warp that pass query qb + j; one
-            // atomic per query reserves the slots of all of them
+          uint32_t qany = __reduce_or_sync(0xffffffffu, passed);
+          uint32_t base = 0;                     // lane j: first reserved slot of query qb + j
+          if (__popc(qany) > kDeferQueries) {
+            // many queries pass (the first parts): all 32 served at once, now.
+            // mine (lane j): the rows that pass query qb + j; one atomic per lane
             uint32_t mine = 0;
 #pragma unroll
             for (uint32_t j = 0; j < 32; j++) {
               const uint32_t m = __ballot_sync(0xffffffffu, (passed >> j) & 1u);
               mine = lane == j ? m : mine;
             }
-            uint32_t base = 0;
             if (mine != 0u) base = atomicAdd(a.cand_count + qb + lane, (uint32_t)__popc(mine));
             const uint32_t below = (1u << lane) - 1u;
 #pragma unroll
@@ -467,21 +594,76 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
                   atomicOr(a.status + q, 1u);
               }
             }
+            qany = 0;                            // nothing left for pass 2
+          } else {
+            for (uint32_t bits = qany; bits != 0u; bits &= bits - 1u) {
+              const uint32_t j = (uint32_t)__ffs(bits) - 1u;
+              const uint32_t m = __ballot_sync(0xffffffffu, (passed >> j) & 1u);
+              if (lane == j) base = atomicAdd(a.cand_count + qb + j, (uint32_t)__popc(m));
+            }
+          }
+#pragma unroll
+          for (uint32_t c = 0; c + 1 < CH; c++) {
+            pass_c[c] = pass_c[c + 1];
+            base_c[c] = base_c[c + 1];
+            any_c[c] = any_c[c + 1];
+          }
+          pass_c[CH - 1] = passed;
+          base_c[CH - 1] = base;
+          any_c[CH - 1] = qany;
+        }
+        const uint32_t below = (1u << lane) - 1u;
+#pragma unroll 1
+        for (uint32_t i = 0; i < CH; i++) {
+          const uint32_t passed = pass_c[0], base = base_c[0], qany = any_c[0];
+          const float qs = qs_k[0];
+#pragma unroll
+          for (uint32_t c = 0; c + 1 < CH; c++) {
+            pass_c[c] = pass_c[c + 1];
+            base_c[c] = base_c[c + 1];
+            any_c[c] = any_c[c + 1];
+            qs_k[c] = qs_k[c + 1];
+          }
+          const uint32_t qb = q0 + (half * CH + i) * 32;
+          for (uint32_t bits = qany; bits != 0u; bits &= bits - 1u) {
+            const uint32_t j = (uint32_t)__ffs(bits) - 1u;
+            const uint32_t m = __ballot_sync(0xffffffffu, (passed >> j) & 1u);
+            const uint32_t bj = __shfl_sync(0xffffffffu, base, j);
+            const float scj = kFp8 ? sc * __shfl_sync(0xffffffffu, qs, j) : sc;
+            const uint32_t raw = tmem_ld1(tcol + i * 32 + j);
+            if ((passed >> j) & 1u) {
+              const uint32_t q = qb + j;
+              const uint32_t slot = bj + (uint32_t)__popc(m & below);
+              const float s = fmaf(__uint_as_float(raw), scj, bi);
+              if (slot < a.cap)
+                a.cand[(size_t)q * a.cap + slot] = ((unsigned long long)score_key(s) << 32) | row;
+              else
+                atomicOr(a.status + q, 1u);
+            }
           }
         }
       }
       tc_fence_before();
-      mbar_arrive(smem_u32(&bar_tempty[buf]));
+      if constexpr (kPair) {
+        // the warp's TMEM loads are complete (tcgen05.wait::ld); lane 0 tells the MMA CTA
+        __syncwarp();
+        if (lane == 0) mbar_arrive_cluster(map_to_rank(smem_u32(&bar_tempty[buf]), 0));
+      } else {
+        mbar_arrive(smem_u32(&bar_tempty[buf]));
+      }
     }
   }
   tc_fence_before();
   __syncthreads();
-  // the peer's multicast copies into this CTA and its MMA commits on this CTA's
-  // barriers are over before either CTA leaves
+  // kPair: the first CTA's MMAs into this CTA's TMEM, its commits on this CTA's
+  // barriers and this CTA's arrivals on its barriers are over before either leaves
   if constexpr (kPair) cluster_sync();
   if (warp == 1) {
     tc_fence_after();
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    if constexpr (kPair)
+      asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
+    else
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS) : "memory");
   }
 }
 
