@@ -852,12 +852,28 @@ tc_final_kernel(DevGraph g, const uint4* __restrict__ queries, uint32_t q0, cons
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int gl = lane & (G - 1);
   const uint32_t gpw = 32 / G, ngroups = blockDim.x / G;
-  for (uint32_t b = warp * gpw; b < m; b += ngroups) {
-    const uint32_t i = b + (uint32_t)(lane / G);
-    const bool valid = i < m;
-    const uint32_t row = valid ? (uint32_t)sel[i] : 0u;
-    const float d = group_distance<ObjType::Float, M>(qv, g.objects + (size_t)row * rc, (int)rc, gl, G);
-    if (valid && gl == 0) sel[i] = pack_key(d, row);
+  // each group computes kRows rows at once (their loads in flight together);
+  // every row's lanes and summation order are those of group_distance
+  constexpr uint32_t kRows = 4;
+  for (uint32_t b = warp * gpw * kRows; b < m; b += ngroups * kRows) {
+    uint32_t idx[kRows], row[kRows];
+    Acc<ObjType::Float, M> acc[kRows];
+#pragma unroll
+    for (uint32_t r = 0; r < kRows; r++) {
+      idx[r] = b + r * gpw + (uint32_t)(lane / G);
+      row[r] = idx[r] < m ? (uint32_t)sel[idx[r]] : 0u;
+    }
+    for (int c = gl; c < (int)rc; c += G) {
+      const uint4 qc = qv[c];
+#pragma unroll
+      for (uint32_t r = 0; r < kRows; r++) acc[r].add(qc, __ldg(g.objects + (size_t)row[r] * rc + c), c);
+    }
+#pragma unroll
+    for (uint32_t r = 0; r < kRows; r++) {
+      acc[r].reduce(G);
+      const float d = acc[r].finish();
+      if (idx[r] < m && gl == 0) sel[idx[r]] = pack_key(d, row[r]);
+    }
   }
   __syncthreads();
   // bitonic sort of P keys (P a power of two)
