@@ -75,8 +75,9 @@ constexpr uint32_t STAGES2 = 6;
 constexpr uint32_t STAGE2_BYTES = A_BYTES + B_BYTES / 2;
 constexpr uint32_t MAX_STAGES = STAGES2 > STAGES ? STAGES2 : STAGES;
 static_assert(STAGES2 * STAGE2_BYTES + 1024 <= SMEM_BYTES, "two-SM stages fit the same shared memory");
-constexpr uint32_t EPI_WARPS = 8;       // two per TMEM lane quadrant, each half of the columns
-constexpr uint32_t THREADS = 64 + 32 * EPI_WARPS;   // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
+constexpr uint32_t EPI_WARPS = 16;      // four per TMEM lane quadrant, each a quarter of the columns
+constexpr uint32_t EPI_PARTS = EPI_WARPS / 4;
+constexpr uint32_t THREADS = 64 + 32 * EPI_WARPS;   // warp 0 TMA, warp 1 MMA, warps 2.. epilogue
 constexpr uint32_t TMEM_COLS = 2 * BN;
 constexpr uint32_t kInvalidKey = 0xff800000u;   // score key of -inf; valid keys are smaller
 constexpr uint64_t kWaitNs = 2000000000ull;     // bound of every wait (2 s)
@@ -474,9 +475,9 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
     }
   } else {
     // epilogue: warp w reads TMEM lanes 32 * (w % 4) .. + 31 (one row per
-    // thread) and one half of the 256 columns
+    // thread) and one of EPI_PARTS column ranges of the 256 columns
     const uint32_t quad = warp & 3u;
-    const uint32_t half = (warp - 2u) >> 2;
+    const uint32_t part = (warp - 2u) >> 2;
     uint32_t local = 0;
     for (uint32_t t = unit0; t < units; t += ustep, local++) {
       const uint32_t buf = local & 1u, tphase = (local >> 1) & 1u;
@@ -488,14 +489,14 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
       const bool rvalid = in_range && row != 0 && a.present[row];
       const float sc = rvalid ? a.row_scale[row] : 0.f;
       const float bi = rvalid ? a.row_bias[row] : 0.f;
-      // per chunk of 32 queries of this warp's half: lane j holds the threshold
-      // (+inf past the last query) and the scale of query qb + j
-      constexpr uint32_t CH = BN / 64;
-      static_assert(CH == 4, "four chunks of 32 queries per epilogue warp");
+      // per chunk of 32 queries of this warp's columns: lane j holds the
+      // threshold (+inf past the last query) and the scale of query qb + j
+      constexpr uint32_t CH = BN / (32 * EPI_PARTS);
+      static_assert(CH * 32 * EPI_PARTS == BN, "whole chunks of 32 queries per epilogue warp");
       float thr_c[CH], qs_c[CH];
 #pragma unroll
       for (uint32_t i = 0; i < CH; i++) {
-        const uint32_t qj = q0 + (half * CH + i) * 32 + lane;
+        const uint32_t qj = q0 + (part * CH + i) * 32 + lane;
         thr_c[i] = (!kDense && qj < a.nq) ? __ldg(a.thr + qj) : INFINITY;
         qs_c[i] = (kFp8 && qj < a.nq) ? __ldg(a.qscale + qj) : 1.f;
       }
@@ -508,14 +509,14 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
         break;
       }
       tc_fence_after();
-      // this warp's first TMEM column: lanes 32 * quad.., columns of its half
-      const uint32_t tcol = tmem + ((quad * 32u) << 16) + buf * BN + half * CH * 32;
+      // this warp's first TMEM column: lanes 32 * quad.., its column range
+      const uint32_t tcol = tmem + ((quad * 32u) << 16) + buf * BN + part * CH * 32;
       // rolled loops over the chunks keep the epilogue's code small (per-chunk
       // values shift down into index 0 of their arrays)
       if constexpr (kDense) {
 #pragma unroll 1
         for (uint32_t i = 0; i < CH; i++) {
-          const uint32_t qb = q0 + (half * CH + i) * 32;
+          const uint32_t qb = q0 + (part * CH + i) * 32;
           if (qb >= a.nq) break;                 // warp-uniform
           const float qs = qs_c[0];
 #pragma unroll
@@ -546,7 +547,7 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
         for (uint32_t c = 0; c < CH; c++) qs_k[c] = qs_c[c];
 #pragma unroll 1
         for (uint32_t i = 0; i < CH; i++) {
-          const uint32_t qb = q0 + (half * CH + i) * 32;
+          const uint32_t qb = q0 + (part * CH + i) * 32;
           const float thr = thr_c[0], qs = qs_c[0];
 #pragma unroll
           for (uint32_t c = 0; c + 1 < CH; c++) {
@@ -624,7 +625,7 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
             any_c[c] = any_c[c + 1];
             qs_k[c] = qs_k[c + 1];
           }
-          const uint32_t qb = q0 + (half * CH + i) * 32;
+          const uint32_t qb = q0 + (part * CH + i) * 32;
           for (uint32_t bits = qany; bits != 0u; bits &= bits - 1u) {
             const uint32_t j = (uint32_t)__ffs(bits) - 1u;
             const uint32_t m = __ballot_sync(0xffffffffu, (passed >> j) & 1u);
