@@ -11,9 +11,11 @@
 #include <climits>
 #include <cmath>
 #include <cstring>
+#include <exception>
 #include <stdexcept>
 #include <sstream>
 #include <string>
+#include <thread>
 
 #include "graph_exact.cuh"
 #include "graph_fast.cuh"
@@ -320,7 +322,6 @@ void GraphEngine::build_params(const SearchArgs* args, size_t nargs, size_t nq, 
   params.resize(nq);
   seed_list.clear();
   max_size = 0;
-  const Property& p = host_.prop;
   uint32_t shared_seeds = UINT32_MAX;
   for (size_t i = 0; i < nq; i++) {
     if (nargs == 1 && i > 0) {
@@ -445,81 +446,104 @@ void GraphEngine::convert_queries(const void* queries, QueryType qt, size_t nq, 
     throw std::runtime_error("the query dimension " + std::to_string(qdim) + " differs from the index dimension " +
                              std::to_string(user_dim));
   const size_t rb = host_.row_bytes();
-  std::memset(rows, 0, nq * rb);
   const bool norm = is_normalized(host_.prop.metric);
-  if (host_.prop.otype == ObjType::Float && qt == QueryType::Float32 && !norm) {
-    // float rows are the queries themselves, zero padded
-    const float* src = static_cast<const float*>(queries);
-    for (size_t q = 0; q < nq; q++) std::memcpy(rows + q * rb, src + q * qdim, qdim * sizeof(float));
+  // queries [q_begin, q_end): each query's arithmetic is independent of the others
+  auto convert_range = [&](size_t q_begin, size_t q_end) {
+    std::memset(rows + q_begin * rb, 0, (q_end - q_begin) * rb);
+    if (host_.prop.otype == ObjType::Float && qt == QueryType::Float32 && !norm) {
+      // float rows are the queries themselves, zero padded
+      const float* src = static_cast<const float*>(queries);
+      for (size_t q = q_begin; q < q_end; q++) std::memcpy(rows + q * rb, src + q * qdim, qdim * sizeof(float));
+      return;
+    }
+    std::vector<float> tmp(qdim);
+    for (size_t q = q_begin; q < q_end; q++) {
+      uint8_t* dst = rows + q * rb;
+      for (size_t i = 0; i < qdim; i++) tmp[i] = (float)query_elem(queries, qt, q * qdim + i);
+      switch (host_.prop.otype) {
+        case ObjType::Float: {
+          float* o = reinterpret_cast<float*>(dst);
+          for (size_t i = 0; i < qdim; i++) o[i] = qt == QueryType::Float64
+                                                     ? (float)static_cast<const double*>(queries)[q * qdim + i]
+                                                     : tmp[i];
+          if (norm) {
+            // ObjectSpace::normalize (lib/NGT/ObjectSpace.h:356-384): float sum, sqrt, divide.
+            float sum = 0.0f;
+            for (size_t i = 0; i < qdim; i++) sum += o[i] * o[i];
+            if (sum == 0.0f) throw std::runtime_error("the query is a zero vector; it cannot be normalized");
+            sum = (float)std::sqrt(sum);
+            for (size_t i = 0; i < qdim; i++) o[i] = o[i] / sum;
+          }
+          break;
+        }
+        case ObjType::Float16: {
+          __half* o = reinterpret_cast<__half*>(dst);
+          for (size_t i = 0; i < qdim; i++) o[i] = __float2half_rn(tmp[i]);
+          if (norm) {
+            float sum = 0.0f;
+            for (size_t i = 0; i < qdim; i++) {
+              float v = __half2float(o[i]);
+              sum += v * v;
+            }
+            if (sum == 0.0f) throw std::runtime_error("the query is a zero vector; it cannot be normalized");
+            sum = (float)std::sqrt(sum);
+            for (size_t i = 0; i < qdim; i++) o[i] = __float2half_rn(__half2float(o[i]) / sum);
+          }
+          break;
+        }
+        case ObjType::Uint8: {
+          for (size_t i = 0; i < qdim; i++) {
+            double v = query_elem(queries, qt, q * qdim + i);
+            dst[i] = (uint8_t)(int)v;       // static_cast<uint8_t> truncates toward zero
+          }
+          break;
+        }
+        case ObjType::Qsint8: {
+          // ObjectSpace::quantizeSymmetrically (lib/NGT/ObjectSpace.h:432-441): the
+          // division in float, the product with 127.5 and the rounding in double; under a
+          // normalized distance the float query is normalized first
+          // (ObjectSpaceRepository::allocateNormalizedObject, ObjectSpaceRepository.h:1120-1160)
+          const float scale = host_.prop.quantization_scale;
+          if (norm) {
+            float sum = 0.0f;
+            for (size_t i = 0; i < qdim; i++) sum += tmp[i] * tmp[i];
+            if (sum == 0.0f) throw std::runtime_error("the query is a zero vector; it cannot be normalized");
+            sum = (float)std::sqrt(sum);
+            for (size_t i = 0; i < qdim; i++) tmp[i] = tmp[i] / sum;
+          }
+          for (size_t i = 0; i < qdim; i++) {
+            float fv = tmp[i];
+            fv = (float)std::round((double)(fv / scale) * 127.5);
+            fv = fv < -127.0f ? -127.0f : fv;
+            fv = fv > 127.0f ? 127.0f : fv;
+            dst[i] = (uint8_t)(int8_t)fv;
+          }
+          break;
+        }
+        default: throw std::runtime_error("unsupported object type");
+      }
+    }
+  };
+  // large batches are converted by several host threads
+  const size_t hw = std::max<size_t>(1, std::thread::hardware_concurrency());
+  const size_t nt = nq * qdim < ((size_t)1 << 20) ? 1 : std::min<size_t>({hw, (size_t)16, nq});
+  if (nt <= 1) {
+    convert_range(0, nq);
     return;
   }
-  std::vector<float> tmp(qdim);
-  for (size_t q = 0; q < nq; q++) {
-    uint8_t* dst = rows + q * rb;
-    for (size_t i = 0; i < qdim; i++) tmp[i] = (float)query_elem(queries, qt, q * qdim + i);
-    switch (host_.prop.otype) {
-      case ObjType::Float: {
-        float* o = reinterpret_cast<float*>(dst);
-        for (size_t i = 0; i < qdim; i++) o[i] = qt == QueryType::Float64
-                                                   ? (float)static_cast<const double*>(queries)[q * qdim + i]
-                                                   : tmp[i];
-        if (norm) {
-          // ObjectSpace::normalize (lib/NGT/ObjectSpace.h:356-384): float sum, sqrt, divide.
-          float sum = 0.0f;
-          for (size_t i = 0; i < qdim; i++) sum += o[i] * o[i];
-          if (sum == 0.0f) throw std::runtime_error("the query is a zero vector; it cannot be normalized");
-          sum = (float)std::sqrt(sum);
-          for (size_t i = 0; i < qdim; i++) o[i] = o[i] / sum;
-        }
-        break;
+  std::vector<std::thread> threads;
+  std::vector<std::exception_ptr> errors(nt);
+  for (size_t t = 0; t < nt; t++)
+    threads.emplace_back([&, t] {
+      try {
+        convert_range(nq * t / nt, nq * (t + 1) / nt);
+      } catch (...) {
+        errors[t] = std::current_exception();
       }
-      case ObjType::Float16: {
-        __half* o = reinterpret_cast<__half*>(dst);
-        for (size_t i = 0; i < qdim; i++) o[i] = __float2half_rn(tmp[i]);
-        if (norm) {
-          float sum = 0.0f;
-          for (size_t i = 0; i < qdim; i++) {
-            float v = __half2float(o[i]);
-            sum += v * v;
-          }
-          if (sum == 0.0f) throw std::runtime_error("the query is a zero vector; it cannot be normalized");
-          sum = (float)std::sqrt(sum);
-          for (size_t i = 0; i < qdim; i++) o[i] = __float2half_rn(__half2float(o[i]) / sum);
-        }
-        break;
-      }
-      case ObjType::Uint8: {
-        for (size_t i = 0; i < qdim; i++) {
-          double v = query_elem(queries, qt, q * qdim + i);
-          dst[i] = (uint8_t)(int)v;       // static_cast<uint8_t> truncates toward zero
-        }
-        break;
-      }
-      case ObjType::Qsint8: {
-        // ObjectSpace::quantizeSymmetrically (lib/NGT/ObjectSpace.h:432-441): the
-        // division in float, the product with 127.5 and the rounding in double; under a
-        // normalized distance the float query is normalized first
-        // (ObjectSpaceRepository::allocateNormalizedObject, ObjectSpaceRepository.h:1120-1160)
-        const float scale = host_.prop.quantization_scale;
-        if (norm) {
-          float sum = 0.0f;
-          for (size_t i = 0; i < qdim; i++) sum += tmp[i] * tmp[i];
-          if (sum == 0.0f) throw std::runtime_error("the query is a zero vector; it cannot be normalized");
-          sum = (float)std::sqrt(sum);
-          for (size_t i = 0; i < qdim; i++) tmp[i] = tmp[i] / sum;
-        }
-        for (size_t i = 0; i < qdim; i++) {
-          float fv = tmp[i];
-          fv = (float)std::round((double)(fv / scale) * 127.5);
-          fv = fv < -127.0f ? -127.0f : fv;
-          fv = fv > 127.0f ? 127.0f : fv;
-          dst[i] = (uint8_t)(int8_t)fv;
-        }
-        break;
-      }
-      default: throw std::runtime_error("unsupported object type");
-    }
-  }
+    });
+  for (auto& th : threads) th.join();
+  for (auto& e : errors)
+    if (e) std::rethrow_exception(e);
 }
 
 void GraphEngine::ensure_scratch(size_t grid) {

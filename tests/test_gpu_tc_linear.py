@@ -285,3 +285,17 @@ def test_pair_clusters_equal_single_ctas(precision, workdir):
         got = ix.linear_search_tc(queries, k=10, candidates=64, first_rows=0, precision=precision, pair=True)
     for a, b in zip(ref, got):
         assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_large_query_batches_convert_like_single_queries(workdir):
+    """A batch large enough to be converted by several host threads (2,000 x 768
+    NormalizedCosine queries: normalised in float, as ObjectSpace::normalize,
+    lib/NGT/ObjectSpace.h:356-384) gives every query the row that converting it
+    alone gives, bit for bit."""
+    from ngt_gb300 import Index
+    path, x, q = _cluster_index(workdir)
+    big = np.repeat(q, 10, axis=0) * np.linspace(0.5, 2.0, 2000, dtype=np.float32)[:, None]
+    with Index(path, read_only=True) as ix:
+        rows = ix.convert_queries(big)
+        for j in range(0, len(big), 97):
+            assert np.array_equal(ix.convert_queries(big[j:j + 1])[0], rows[j]), j
