@@ -264,6 +264,9 @@ uint32_t GraphEngine::seed_table(size_t seed_size) {
     h_seed_ids_.insert(h_seed_ids_.end(), ids.begin(), ids.end());
   }
   h_seed_off_.push_back((uint32_t)h_seed_ids_.size());
+  // launches on any stream (serving and coalescing lanes) may still read the
+  // previous tables: they finish before the tables are replaced
+  if (d_seed_off_ || d_seed_ids_) NGT_CUDA(cudaDeviceSynchronize());
   cudaFree(d_seed_off_);
   cudaFree(d_seed_ids_);
   d_seed_off_ = dmalloc_copy<uint32_t>(h_seed_off_.data(), h_seed_off_.size() * 4);
@@ -1077,7 +1080,11 @@ void GraphEngine::run_coalesced(std::vector<std::shared_ptr<CoalescedCall>>& bat
   std::vector<QueryParams> params;
   std::vector<uint32_t> seeds;
   uint32_t max_size = 0;
-  build_params(args.data(), nq, nq, kmax, params, seeds, max_size);
+  {
+    // the parameters may create a seed table (engine state shared with every lane)
+    std::lock_guard<std::mutex> lock(mu_);
+    build_params(args.data(), nq, nq, kmax, params, seeds, max_size);
+  }
   auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
   const size_t o_par = al(nq * rb), o_seed = o_par + al(nq * sizeof(QueryParams));
   const size_t o_out = o_seed + al(seeds.size() * 4), o_cnt = o_out + al(nq * kmax * sizeof(ObjDist));

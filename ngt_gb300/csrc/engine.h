@@ -290,6 +290,8 @@ class GraphEngine {
     size_t slots = 0;
   };
   void upload();
+  // seed_table, build_params and seed_params may add a seed table (shared state):
+  // callers hold mu_
   uint32_t seed_table(size_t seed_size);        // index of the thinned-seed table
   void build_params(const SearchArgs* args, size_t nargs, size_t nq, size_t kmax, std::vector<QueryParams>& params,
                     std::vector<uint32_t>& seed_list, uint32_t& max_size);
