@@ -450,10 +450,11 @@ void GraphEngine::convert_queries(const void* queries, QueryType qt, size_t nq, 
                              std::to_string(user_dim));
   const size_t rb = host_.row_bytes();
   const bool norm = is_normalized(host_.prop.metric);
+  const bool plain_copy = host_.prop.otype == ObjType::Float && qt == QueryType::Float32 && !norm;
   // queries [q_begin, q_end): each query's arithmetic is independent of the others
   auto convert_range = [&](size_t q_begin, size_t q_end) {
     std::memset(rows + q_begin * rb, 0, (q_end - q_begin) * rb);
-    if (host_.prop.otype == ObjType::Float && qt == QueryType::Float32 && !norm) {
+    if (plain_copy) {
       // float rows are the queries themselves, zero padded
       const float* src = static_cast<const float*>(queries);
       for (size_t q = q_begin; q < q_end; q++) std::memcpy(rows + q * rb, src + q * qdim, qdim * sizeof(float));
@@ -527,9 +528,9 @@ void GraphEngine::convert_queries(const void* queries, QueryType qt, size_t nq, 
       }
     }
   };
-  // large batches are converted by several host threads
+  // large batches that are more than a copy are converted by several host threads
   const size_t hw = std::max<size_t>(1, std::thread::hardware_concurrency());
-  const size_t nt = nq * qdim < ((size_t)1 << 20) ? 1 : std::min<size_t>({hw, (size_t)16, nq});
+  const size_t nt = plain_copy || nq * qdim < ((size_t)1 << 20) ? 1 : std::min<size_t>({hw, (size_t)16, nq});
   if (nt <= 1) {
     convert_range(0, nq);
     return;
