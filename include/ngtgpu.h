@@ -190,9 +190,9 @@ bool ngtgpu_linear_search_tc_float(NGTIndex, const float *queries, size_t nq, in
                                     the fp32 evaluation error (1e-4 x max(d, 1)) are ordered by their FP64
                                     distance at the cut, so the returned ids are the FP64 top `size` among
                                     the candidates (status bit 4: more than 64 such ties, fp32 order kept) */
-#define NGTGPU_TC_PAIR 2u         /* flag: the score kernel runs in clusters of two CTAs that share each
-                                    query tile (TMA multicast), so query tiles cross L2 half as often;
-                                    the scores and results are the same */
+#define NGTGPU_TC_PAIR 2u         /* flag: the score kernel runs on the two-SM MMA (cta_group::2): pairs
+                                    of CTAs compute 256-row x 256-query tiles, each staging its own rows
+                                    and half of the query tile; the scores and results are the same */
 /* ngtgpu_linear_search_tc_device / _float with a score precision and flags. */
 bool ngtgpu_linear_search_tc_ex(NGTIndex, const void *d_rows, size_t nq, size_t size, size_t candidates,
                                 uint32_t precision, uint32_t flags, NGTObjectDistance *d_results, size_t kmax,

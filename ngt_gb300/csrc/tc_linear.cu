@@ -669,11 +669,12 @@ tc_score_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant_
 }
 
 // The k-th smallest (1-based, 1 <= k <= n) of n distinct 64-bit keys in shared
-// memory: eight 8-bit radix passes; warp 0 scans the 256-bin histogram.
+// memory: up to eight 8-bit radix passes (warp 0 scans the 256-bin histogram),
+// ended early once the k-th key is the only key with the prefix found so far.
 __device__ unsigned long long block_select_u64(const unsigned long long* keys, uint32_t n, uint32_t k,
                                                uint32_t* hist) {
   __shared__ unsigned long long sh_prefix;
-  __shared__ uint32_t sh_need;
+  __shared__ uint32_t sh_need, sh_single;
   const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned long long prefix = 0, mask = 0;
   uint32_t need = k;
@@ -708,13 +709,24 @@ __device__ unsigned long long block_select_u64(const unsigned long long* keys, u
         }
         sh_prefix = prefix | ((unsigned long long)(lane * 8 + j) << shift);
         sh_need = need - acc;
+        sh_single = c[j] == 1u ? 1u : 0u;
       }
     }
     __syncthreads();
     prefix = sh_prefix;
     need = sh_need;
     mask |= 255ull << shift;
+    const bool single = sh_single != 0u && shift > 0;
     __syncthreads();
+    if (single) {
+      // one key has this prefix: it is the k-th
+      for (uint32_t i = threadIdx.x; i < n; i += blockDim.x)
+        if ((keys[i] & mask) == prefix) sh_prefix = keys[i];
+      __syncthreads();
+      const unsigned long long r = sh_prefix;
+      __syncthreads();
+      return r;
+    }
   }
   return prefix;
 }
