@@ -535,44 +535,11 @@ bool tc_float_impl(NGTIndex index, const float* queries, size_t nq, int32_t dim,
     CAPI_PARAM_ERROR(error, "index = " << index << " queries = " << queries << " nq = " << nq << " dim = " << dim);
     return false;
   }
-  // the device buffers of this call: one stream-ordered allocation, freed on every exit
-  // after the work queued on the stream
-  struct Buffers {
-    void* base = nullptr;
-    cudaStream_t stream = nullptr;
-    void* p[4] = {nullptr, nullptr, nullptr, nullptr};
-    ~Buffers() {
-      if (base) cudaFreeAsync(base, stream);
-    }
-  } b;
   try {
     GraphEngine* e = engine(index);
-    if (nq == 0) return true;
-    std::vector<uint8_t> rows;
-    e->convert_queries(queries, QueryType::Float32, nq, (size_t)dim, rows);
-    cudaStream_t s = e->stream();
-    auto ck = [](cudaError_t c) {
-      if (c != cudaSuccess) throw std::runtime_error(std::string("CUDA error ") + cudaGetErrorString(c));
-    };
-    ck(cudaSetDevice(e->device()));
-    const size_t r_bytes = (rows.size() + 255) / 256 * 256;
-    const size_t o_bytes = (nq * kmax * sizeof(NGTObjectDistance) + 255) / 256 * 256;
-    const size_t c_bytes = (nq * 4 + 255) / 256 * 256;
-    ck(cudaMallocAsync(&b.base, r_bytes + o_bytes + 2 * c_bytes, s));
-    b.stream = s;
-    b.p[0] = b.base;
-    b.p[1] = static_cast<uint8_t*>(b.base) + r_bytes;
-    b.p[2] = static_cast<uint8_t*>(b.p[1]) + o_bytes;
-    b.p[3] = static_cast<uint8_t*>(b.p[2]) + c_bytes;
-    ck(cudaMemcpyAsync(b.p[0], rows.data(), rows.size(), cudaMemcpyHostToDevice, s));
-    e->linear_search_tc_device(static_cast<const uint4*>(b.p[0]), nq, size, candidates,
-                               static_cast<ngtg::ObjDist*>(b.p[1]), kmax, static_cast<uint32_t*>(b.p[2]),
-                               static_cast<uint32_t*>(b.p[3]), s, precision == NGTGPU_TC_FP8,
-                               (flags & NGTGPU_TC_FP64_TIES) != 0, (flags & NGTGPU_TC_PAIR) != 0);
-    ck(cudaMemcpyAsync(results, b.p[1], nq * kmax * sizeof(NGTObjectDistance), cudaMemcpyDeviceToHost, s));
-    ck(cudaMemcpyAsync(counts, b.p[2], nq * 4, cudaMemcpyDeviceToHost, s));
-    ck(cudaMemcpyAsync(status, b.p[3], nq * 4, cudaMemcpyDeviceToHost, s));
-    ck(cudaStreamSynchronize(s));
+    e->linear_search_tc_host(queries, nq, (size_t)dim, size, candidates, reinterpret_cast<ngtg::ObjDist*>(results),
+                             kmax, counts, status, precision == NGTGPU_TC_FP8, (flags & NGTGPU_TC_FP64_TIES) != 0,
+                             (flags & NGTGPU_TC_PAIR) != 0);
     return true;
   }
   CAPI_CATCH(error, false)

@@ -943,6 +943,44 @@ void GraphEngine::search(const void* queries, QueryType qt, size_t nq, size_t qd
   NGT_CUDA(cudaStreamSynchronize(s));
 }
 
+void GraphEngine::linear_search_tc_host(const float* queries, size_t nq, size_t qdim, size_t size,
+                                        size_t candidates, ObjDist* results, size_t kmax, uint32_t* counts,
+                                        uint32_t* status, bool fp8, bool fp64_ties, bool pair) {
+  NGT_CUDA(cudaSetDevice(device_));
+  if (nq == 0) return;
+  std::lock_guard<std::mutex> staging(staging_mu_);
+  const size_t row_total = nq * host_.row_bytes();
+  if (staging_bytes_ < row_total) {
+    if (staging_) NGT_CUDA(cudaFreeHost(staging_));
+    staging_ = nullptr;
+    staging_bytes_ = 0;
+    NGT_CUDA(cudaMallocHost(&staging_, row_total));
+    staging_bytes_ = row_total;
+  }
+  convert_queries(queries, QueryType::Float32, nq, qdim, static_cast<uint8_t*>(staging_));
+  auto al = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t o_out = al(row_total), o_cnt = o_out + al(nq * kmax * sizeof(ObjDist));
+  const size_t o_st = o_cnt + al(nq * 4), total = o_st + al(nq * 4);
+  cudaStream_t s = stream_;
+  uint8_t* d = nullptr;
+  NGT_CUDA(cudaMallocAsync(&d, total, s));
+  try {
+    NGT_CUDA(cudaMemcpyAsync(d, staging_, row_total, cudaMemcpyHostToDevice, s));
+    linear_search_tc_device(reinterpret_cast<const uint4*>(d), nq, size, candidates,
+                            reinterpret_cast<ObjDist*>(d + o_out), kmax, reinterpret_cast<uint32_t*>(d + o_cnt),
+                            reinterpret_cast<uint32_t*>(d + o_st), s, fp8, fp64_ties, pair);
+    NGT_CUDA(cudaMemcpyAsync(results, d + o_out, nq * kmax * sizeof(ObjDist), cudaMemcpyDeviceToHost, s));
+    NGT_CUDA(cudaMemcpyAsync(counts, d + o_cnt, nq * 4, cudaMemcpyDeviceToHost, s));
+    NGT_CUDA(cudaMemcpyAsync(status, d + o_st, nq * 4, cudaMemcpyDeviceToHost, s));
+  } catch (...) {
+    cudaFreeAsync(d, s);
+    cudaStreamSynchronize(s);
+    throw;
+  }
+  NGT_CUDA(cudaFreeAsync(d, s));
+  NGT_CUDA(cudaStreamSynchronize(s));
+}
+
 void GraphEngine::search_refined(const void* queries, QueryType qt, size_t nq, size_t qdim, const SearchArgs* args,
                                  size_t nargs, SearchOutput& out, Kernel kernel) {
   // GraphIndex::search(SearchQuery&) with a refinement expansion (lib/NGT/Index.h:1146-1236):

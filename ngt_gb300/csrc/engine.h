@@ -209,6 +209,11 @@ class GraphEngine {
   void linear_search_tc_device(const uint4* d_rows, size_t nq, size_t size, size_t candidates, ObjDist* d_out,
                                size_t kmax, uint32_t* d_counts, uint32_t* d_status, cudaStream_t stream,
                                bool fp8 = false, bool fp64_ties = false, bool pair = false);
+  // The same from host float queries into host buffers: the query rows are converted
+  // into the pinned staging buffer and copied from there.
+  void linear_search_tc_host(const float* queries, size_t nq, size_t qdim, size_t size, size_t candidates,
+                             ObjDist* results, size_t kmax, uint32_t* counts, uint32_t* status, bool fp8,
+                             bool fp64_ties, bool pair);
   // The approximate scores alone: d_scores[q * ld + row] (-inf for the unused
   // row 0 and removed objects).
   void tc_scores_device(const uint4* d_rows, size_t nq, float* d_scores, size_t ld, cudaStream_t stream);
