@@ -17,11 +17,13 @@
 //      N = 256 queries, K = 16 per instruction), operands staged by TMA
 //      (cp.async.bulk.tensor, 128-byte swizzle) through a 4-stage mbarrier
 //      pipeline, accumulators double-buffered in TMEM (2 x 256 columns) and
-//      read back with tcgen05.ld by eight epilogue warps (two per TMEM lane
+//      read back with tcgen05.ld by sixteen epilogue warps (four per TMEM lane
 //      quadrant).  The first `first_rows` rows are written out densely; on the
 //      remaining rows, taken in parts that double in size, the epilogue keeps
 //      only scores that beat the query's threshold, and tc_compact_kernel cuts
 //      each list back to the C best and raises the threshold between two parts.
+//      A two-SM form (cta_group::2, M = 256 over a pair of CTAs, each staging
+//      its own rows and half of the query tile) gives the same scores.
 //   3. tc_first_select_kernel: per query, the C best scores of the dense part
 //      (exact radix select on 64-bit (score key, row) keys); the C-th becomes
 //      the threshold, and the C keys the first candidates.  Every row past the
@@ -31,7 +33,8 @@
 //      candidates (the global top C by approximate score, ties by id), their
 //      exact distances with the index's comparator on the fp32 rows (the same
 //      lane grouping as the plain linear search, hence the same rounding), a
-//      bitonic sort by (distance, id), and the first `size` of them.
+//      bitonic sort by (distance, id), optionally the FP64 order of the
+//      candidates tied at the cut, and the first `size` of them.
 //
 // The result equals the plain linear search whenever the true `size` nearest
 // rows are among the C best approximate scores; the candidate oversampling C
