@@ -451,9 +451,12 @@ void GraphEngine::convert_queries(const void* queries, QueryType qt, size_t nq, 
   const size_t rb = host_.row_bytes();
   const bool norm = is_normalized(host_.prop.metric);
   const bool plain_copy = host_.prop.otype == ObjType::Float && qt == QueryType::Float32 && !norm;
+  // bytes of a row the query's elements fill; the rest of the row is zero padding
+  const size_t esize = host_.prop.otype == ObjType::Float ? 4 : host_.prop.otype == ObjType::Float16 ? 2 : 1;
+  const size_t filled = std::min(rb, qdim * esize);
   // queries [q_begin, q_end): each query's arithmetic is independent of the others
   auto convert_range = [&](size_t q_begin, size_t q_end) {
-    std::memset(rows + q_begin * rb, 0, (q_end - q_begin) * rb);
+    for (size_t q = q_begin; q < q_end; q++) std::memset(rows + q * rb + filled, 0, rb - filled);
     if (plain_copy) {
       // float rows are the queries themselves, zero padded
       const float* src = static_cast<const float*>(queries);
