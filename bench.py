@@ -879,6 +879,31 @@ def precision_path(args, steps=None, warmup=None):
                 ix.linear_search(q[j], k=k)
                 plain.append(time.perf_counter() - t)
             out["plain_fp32_linear_qps"] = 1.0 / statistics.median(plain)
+            # a small batch (256 queries, bf16): its ~17 launches issued directly, or
+            # captured once into a CUDA graph and replayed (ngtgpu_set_tc_graphs)
+            small = {}
+            for on in (0, 1):
+                ix._check(ix._lib.ngtgpu_set_tc_graphs(ix._index, on, ix._err))
+
+                def small_step():
+                    ix._check(ix._lib.ngtgpu_linear_search_tc_ex(
+                        ix._index, rows.data_ptr(), 256, k, 400, TC_BF16, TC_FP64_TIES, res.data_ptr(), k,
+                        cnt.data_ptr(), status.data_ptr(), stream.cuda_stream, ix._err))
+
+                for _ in range(3):
+                    small_step()
+                torch.cuda.synchronize()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(20):
+                    small_step()
+                e1.record(stream)
+                e1.synchronize()
+                small["graph_replay_ms" if on else "direct_ms"] = e0.elapsed_time(e1) / 20
+            ix._check(ix._lib.ngtgpu_set_tc_graphs(ix._index, 0, ix._err))
+            out["small_batch_256_queries"] = small
+            log("precision path: 256-query batch %.3f ms direct, %.3f ms replayed" % (
+                small["direct_ms"], small["graph_replay_ms"]))
         del xd
         ix.close()
         torch.cuda.empty_cache()

@@ -217,6 +217,14 @@ bool ngtgpu_tc_phase_times(NGTIndex, float *ms3, NGTError);
  * tensor-core search (rounded up to a multiple of 128, at least `candidates`,
  * at most 16384; 0 = automatic, 8192).  Results do not depend on it. */
 bool ngtgpu_set_tc_first_rows(NGTIndex, size_t rows, NGTError);
+/* enable != 0: ngtgpu_linear_search_tc_* on this handle capture their launch
+ * sequence (about 2 launches per part of the objects, 17 for 1M objects) into a
+ * CUDA graph on the first call of a given shape, buffers and options (up to 8
+ * kept) and replay it on later calls that match; ngtgpu_tc_phase_times then
+ * reports a replay's whole time as [1].  A call on a stream that the caller is
+ * capturing is recorded into the caller's capture.  enable = 0 (default):
+ * launched directly; the kept graphs are released.  Results are the same. */
+bool ngtgpu_set_tc_graphs(NGTIndex, int enable, NGTError);
 /* Row-range shard of the tensor-core exhaustive search: later ngtgpu_linear_search_tc_*
  * calls on this handle search objects [begin, end) only (begin a multiple of 128,
  * end 0 = through the last object; 0, 0 restores the whole index).  Each GPU of a

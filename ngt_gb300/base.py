@@ -153,6 +153,7 @@ def load_library() -> ctypes.CDLL:
         "ngtgpu_tc_scores_device": ([c_void_p, c_void_p, c_size_t, c_void_p, c_size_t, c_void_p, c_void_p],
                                     c_bool),
         "ngtgpu_set_tc_first_rows": ([c_void_p, c_size_t, c_void_p], c_bool),
+        "ngtgpu_set_tc_graphs": ([c_void_p, c_int32, c_void_p], c_bool),
         "ngtgpu_tc_phase_times": ([c_void_p, c_void_p, c_void_p], c_bool),
         "ngtgpu_kernel_launches": ([c_void_p, c_void_p], c_uint64),
         "ngtgpu_coalescing_stats": ([c_void_p, c_void_p, c_void_p, c_void_p], c_bool),
@@ -418,6 +419,11 @@ class Index:
                                                         counts.ctypes.data, status.ctypes.data, self._err)
         self._check(ok)
         return res["id"].copy(), res["distance"].copy(), counts, status
+
+    def set_tc_graphs(self, enable: bool = True) -> None:
+        """Replay captured CUDA graphs of the tensor-core search's launch sequence
+        (one per shape, buffers and options) instead of launching it each call."""
+        self._check(self._lib.ngtgpu_set_tc_graphs(self._index, 1 if enable else 0, self._err))
 
     def tc_phase_times(self):
         """CUDA-event milliseconds of the last tensor-core search batch: (dense

@@ -613,6 +613,18 @@ bool ngtgpu_set_tc_first_rows(NGTIndex index, size_t rows, NGTError error) {
   return true;
 }
 
+bool ngtgpu_set_tc_graphs(NGTIndex index, int enable, NGTError error) {
+  if (index == nullptr) {
+    CAPI_PARAM_ERROR(error, "index = " << index);
+    return false;
+  }
+  try {
+    engine(index)->set_tc_graphs(enable != 0);
+    return true;
+  }
+  CAPI_CATCH(error, false)
+}
+
 bool ngtgpu_set_batched_tuning(NGTIndex index, uint32_t list_capacity, uint32_t parents, float rerank_factor,
                                NGTError error) {
   if (index == nullptr || list_capacity > 1024 || parents > 16 || rerank_factor < 0.f) {

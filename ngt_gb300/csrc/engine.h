@@ -223,6 +223,9 @@ class GraphEngine {
   void tc_phase_ms(float* out) const;
   // rows scored densely before the threshold filter (0: automatic, 8192)
   void set_tc_first_rows(size_t rows) { tc_first_rows_ = rows; }
+  // Tensor-core searches replay captured CUDA graphs of their launch sequence (one
+  // per shape, buffers and options; off: launched directly).
+  void set_tc_graphs(bool on);
   // the tensor-core search covers rows [begin, end) only (a shard of a row-range
   // split; begin a multiple of 128; end 0 = the last row)
   void set_tc_row_range(size_t begin, size_t end) {
@@ -440,6 +443,7 @@ class GraphEngine {
   void ensure_tc_rows8();
   TcState* tc_ = nullptr;
   size_t tc_first_rows_ = 0;
+  bool tc_graphs_ = false;
   uint32_t tc_row_begin_ = 0, tc_row_end_ = 0;
 };
 

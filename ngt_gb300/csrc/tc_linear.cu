@@ -45,10 +45,12 @@
 #include <cuda_bf16.h>
 #include <cuda_fp8.h>
 #include <algorithm>
+#include <array>
 #include <cfloat>
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <vector>
 #include "engine.h"
 #include "distance.cuh"
 #include "kernels.h"
@@ -1150,7 +1152,19 @@ struct TcState {
   // part (the score kernel over the remaining rows), final re-rank
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   float phase_ms[3] = {0.f, 0.f, 0.f};
+  // captured launch sequences (opt-in): one per shape, buffers and scratch
+  struct Graph {
+    std::array<uint64_t, 16> key;
+    cudaGraphExec_t exec;
+    uint64_t launches;
+  };
+  std::vector<Graph> graphs;
 };
+
+void tc_drop_graphs(TcState* s) {
+  for (auto& g : s->graphs) cudaGraphExecDestroy(g.exec);
+  s->graphs.clear();
+}
 
 void tc_release(TcState* s) {
   if (!s) return;
@@ -1163,6 +1177,7 @@ void tc_release(TcState* s) {
   cudaFree(s->error);
   for (cudaEvent_t e : s->ev)
     if (e) cudaEventDestroy(e);
+  tc_drop_graphs(s);
   delete s;
 }
 
@@ -1221,7 +1236,6 @@ template <bool kFp8, bool kPair>
 void launch_scores_t(const CUtensorMap& mapA, const CUtensorMap& mapB, const tc::ScoreArgs& a, bool dense,
                      cudaStream_t s, unsigned grid) {
   auto fn = dense ? tc::tc_score_kernel<true, kFp8, kPair> : tc::tc_score_kernel<false, kFp8, kPair>;
-  TC_CUDA(cudaFuncSetAttribute((const void*)fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_BYTES));
   if constexpr (kPair) {
     // clusters of two CTAs (grid even)
     cudaLaunchConfig_t cfg{};
@@ -1239,6 +1253,23 @@ void launch_scores_t(const CUtensorMap& mapA, const CUtensorMap& mapB, const tc:
     TC_CUDA(cudaLaunchKernelEx(&cfg, fn, mapA, mapB, a));
   } else {
     fn<<<grid, tc::THREADS, tc::SMEM_BYTES, s>>>(mapA, mapB, a);
+  }
+}
+
+// The shared-memory size of every form of the score kernel on the current device
+// (set before the launches, so that a launch sequence can be captured into a graph).
+void prepare_score_kernels() {
+  {
+    const void* fns[] = {(const void*)tc::tc_score_kernel<true, false, false>,
+                         (const void*)tc::tc_score_kernel<false, false, false>,
+                         (const void*)tc::tc_score_kernel<true, true, false>,
+                         (const void*)tc::tc_score_kernel<false, true, false>,
+                         (const void*)tc::tc_score_kernel<true, false, true>,
+                         (const void*)tc::tc_score_kernel<false, false, true>,
+                         (const void*)tc::tc_score_kernel<true, true, true>,
+                         (const void*)tc::tc_score_kernel<false, true, true>};
+    for (const void* f : fns)
+      TC_CUDA(cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::SMEM_BYTES));
   }
 }
 
@@ -1305,6 +1336,7 @@ void GraphEngine::tc_scores_device(const uint4* d_rows, size_t nq, float* d_scor
   a.dense = d_scores;
   a.dense_ld = (uint32_t)ld;
   a.error = st.error;
+  prepare_score_kernels();
   launch_scores(st, mapB, nullptr, a, true, stream, sms);
   launches_ += 2;
   TC_CUDA(cudaFreeAsync(qb, stream));
@@ -1357,6 +1389,7 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
   const size_t need = b_q + b_d + b_c + 2 * qbmax * 4 + qbpad * 4 + 512;
   if (tc_->scratch_bytes < need) {
     TC_CUDA(cudaStreamSynchronize(stream));
+    tc_drop_graphs(tc_);                       // they name the old scratch
     TC_CUDA(cudaFree(tc_->scratch));
     tc_->scratch = nullptr;
     tc_->scratch_bytes = 0;
@@ -1380,11 +1413,14 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
                                (int)(first * 8)));
   TC_CUDA(cudaFuncSetAttribute((const void*)tc::tc_compact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)(cap * 8)));
+  prepare_score_kernels();
+  // the launch sequence (timing: phase events between its parts)
+  auto enqueue = [&](bool timing) {
   TC_CUDA(cudaMemsetAsync(d_status, 0, nq * 4, stream));
   for (size_t q0 = 0; q0 < nq; q0 += qbmax) {
     const uint32_t nb = (uint32_t)std::min(qbmax, nq - q0);
     const uint32_t nbpad = (nb + tc::BN - 1) / tc::BN * tc::BN;
-    TC_CUDA(cudaEventRecord(st.ev[0], stream));
+    if (timing) TC_CUDA(cudaEventRecord(st.ev[0], stream));
     const float* qrows = reinterpret_cast<const float*>(d_rows) + q0 * host_.dpad;
     CUtensorMap mapB, mapBh;
     if (fp8) {
@@ -1416,7 +1452,7 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
                                                                cand, ccount, cap, rb);
     TC_CUDA(cudaGetLastError());
     launches_ += 3;
-    TC_CUDA(cudaEventRecord(st.ev[1], stream));
+    if (timing) TC_CUDA(cudaEventRecord(st.ev[1], stream));
     // filtered rest, in parts that double in size; between two parts the
     // candidate lists are cut back to C and the thresholds move up
     a.dense = nullptr;
@@ -1457,15 +1493,80 @@ void GraphEngine::linear_search_tc_device(const uint4* d_rows, size_t nq, size_t
       }
       row = end;
     }
-    TC_CUDA(cudaEventRecord(st.ev[2], stream));
+    if (timing) TC_CUDA(cudaEventRecord(st.ev[2], stream));
     fin<<<nb, 256, fin_smem, stream>>>(dev_, d_rows, (uint32_t)q0, cand, ccount, cap, (uint32_t)C, P,
                                        (uint32_t)size, group, d_out, (uint32_t)kmax, d_counts, d_status);
     TC_CUDA(cudaGetLastError());
-    TC_CUDA(cudaEventRecord(st.ev[3], stream));
+    if (timing) TC_CUDA(cudaEventRecord(st.ev[3], stream));
     launches_++;
   }
+  };
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  TC_CUDA(cudaStreamIsCapturing(stream, &capture));
+  if (!tc_graphs_ || capture != cudaStreamCaptureStatusNone) {
+    // launched directly (also into a capture the caller runs on this stream)
+    enqueue(capture == cudaStreamCaptureStatusNone);
+    if (capture != cudaStreamCaptureStatusNone) return;
+    check_error(st, stream);
+    for (int i = 0; i < 3; i++) TC_CUDA(cudaEventElapsedTime(&tc_->phase_ms[i], st.ev[i], st.ev[i + 1]));
+    return;
+  }
+  // graph replay: the sequence is captured once per shape, buffers, scratch, row range
+  // and options, and replayed on later calls that match
+  const std::array<uint64_t, 16> key = {(uint64_t)(uintptr_t)d_rows, nq, size, C,
+                                        (uint64_t)(uintptr_t)d_out, kmax, (uint64_t)(uintptr_t)d_counts,
+                                        (uint64_t)(uintptr_t)d_status,
+                                        (uint64_t)fp8 | (uint64_t)fp64_ties << 1 | (uint64_t)pair << 2, rb, nrows,
+                                        first, (uint64_t)(uintptr_t)tc_->scratch, tc_->scratch_bytes, 0, 0};
+  TcState::Graph* g = nullptr;
+  for (auto& x : tc_->graphs)
+    if (x.key == key) g = &x;
+  if (!g) {
+    if (tc_->graphs.size() >= 8) {
+      TC_CUDA(cudaStreamSynchronize(stream));
+      cudaGraphExecDestroy(tc_->graphs.front().exec);
+      tc_->graphs.erase(tc_->graphs.begin());
+    }
+    const uint64_t l0 = launches_;
+    TC_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    cudaGraph_t graph = nullptr;
+    try {
+      enqueue(false);
+    } catch (...) {
+      cudaStreamEndCapture(stream, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    TC_CUDA(cudaStreamEndCapture(stream, &graph));
+    cudaGraphExec_t exec = nullptr;
+    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    TC_CUDA(ie);
+    tc_->graphs.push_back(TcState::Graph{key, exec, launches_ - l0});
+    g = &tc_->graphs.back();
+    launches_ = l0;
+  }
+  TC_CUDA(cudaEventRecord(st.ev[0], stream));
+  TC_CUDA(cudaGraphLaunch(g->exec, stream));
+  TC_CUDA(cudaEventRecord(st.ev[3], stream));
+  launches_ += g->launches;
   check_error(st, stream);
-  for (int i = 0; i < 3; i++) TC_CUDA(cudaEventElapsedTime(&tc_->phase_ms[i], st.ev[i], st.ev[i + 1]));
+  // one replay: its whole time is reported as the middle phase
+  float total = 0.f;
+  TC_CUDA(cudaEventElapsedTime(&total, st.ev[0], st.ev[3]));
+  tc_->phase_ms[0] = 0.f;
+  tc_->phase_ms[1] = total;
+  tc_->phase_ms[2] = 0.f;
+}
+
+void GraphEngine::set_tc_graphs(bool on) {
+  std::lock_guard<std::mutex> lock(mu_);
+  tc_graphs_ = on;
+  if (!on && tc_) {
+    TC_CUDA(cudaSetDevice(device_));
+    TC_CUDA(cudaDeviceSynchronize());
+    tc_drop_graphs(tc_);
+  }
 }
 
 void GraphEngine::tc_phase_ms(float* out) const {

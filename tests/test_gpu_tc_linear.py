@@ -299,3 +299,26 @@ def test_large_query_batches_convert_like_single_queries(workdir):
         rows = ix.convert_queries(big)
         for j in range(0, len(big), 97):
             assert np.array_equal(ix.convert_queries(big[j:j + 1])[0], rows[j]), j
+
+
+def test_graph_replay_returns_the_direct_results(workdir):
+    """With captured launch sequences on, repeated calls (the first captures, the
+    rest replay) and calls of other shapes and options return the results of the
+    directly launched search, bit for bit."""
+    from ngt_gb300 import Index
+    path, x, q = _cluster_index(workdir)
+    with Index(path, read_only=True) as ix:
+        ref = {}
+        for nq, prec, pair in ((200, "bf16", False), (64, "bf16", False), (200, "fp8", False), (200, "bf16", True)):
+            ref[nq, prec, pair] = ix.linear_search_tc(q[:nq], k=100, candidates=400, first_rows=2048,
+                                                      precision=prec, pair=pair)
+        ix.set_tc_graphs(True)
+        for _ in range(3):
+            for (nq, prec, pair), want in ref.items():
+                got = ix.linear_search_tc(q[:nq], k=100, candidates=400, first_rows=2048, precision=prec, pair=pair)
+                for a, b in zip(want, got):
+                    assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), (nq, prec, pair)
+        ix.set_tc_graphs(False)
+        got = ix.linear_search_tc(q[:200], k=100, candidates=400, first_rows=2048)
+        for a, b in zip(ref[200, "bf16", False], got):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
