@@ -144,6 +144,9 @@ def test_tensor_core_search_rejects_null_arguments(lib):
         "ngtgpu_tc_scores_device": ([vp, vp, sz, vp, sz, vp, vp], (None, None, 4, None, 100, None)),
         "ngtgpu_set_tc_first_rows": ([vp, sz, vp], (None, 0)),
         "ngtgpu_tc_phase_times": ([vp, vp, vp], (None, None)),
+        "ngtgpu_set_tc_graphs": ([vp, ctypes.c_int32, vp], (None, 1)),
+        "ngtgpu_linear_search_tc_ex": ([vp, vp, sz, sz, sz, ctypes.c_uint32, ctypes.c_uint32, vp, sz, vp, vp, vp, vp],
+                                       (None, None, 4, 10, 0, 0, 2, None, 10, None, None, None)),
     }
     for name, (argtypes, args) in calls.items():
         fn = getattr(lib, name)
