@@ -322,3 +322,18 @@ def test_graph_replay_returns_the_direct_results(workdir):
         got = ix.linear_search_tc(q[:200], k=100, candidates=400, first_rows=2048)
         for a, b in zip(ref[200, "bf16", False], got):
             assert np.array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_empty_batches_and_the_candidate_limit(workdir):
+    """An empty query batch returns empty results; more than 4,096 candidates per
+    query is refused with an error before any launch, and the handle still serves
+    the next call."""
+    from ngt_gb300 import Index
+    path, meta, queries, golden = materialize("c1_f32_l2", workdir)
+    with Index(path, read_only=True) as ix:
+        ids, ds, n, status = ix.linear_search_tc(np.zeros((0, queries.shape[1]), np.float32), k=10)
+        assert ids.shape == (0, 10) and n.shape == (0,)
+        with pytest.raises(Exception):
+            ix.linear_search_tc(queries[:4], k=10, candidates=5000)
+        ids, ds, n, status = ix.linear_search_tc(queries[:4], k=10, candidates=64)
+        assert (status == 0).all() and (n == 10).all()
